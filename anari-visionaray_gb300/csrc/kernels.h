@@ -1,0 +1,40 @@
+// Host-side launch entry points of the CUDA kernels (called by runtime.cpp).
+#pragma once
+
+#include "vsr_device.h"
+#include <cuda_runtime.h>
+#include <stddef.h>
+
+namespace vsr {
+
+cudaError_t launchRaycast(const DScene &S, const DCamera &C, const DRenderer &R, const DFrame &F,
+                          int stageTFSize, bool count, cudaStream_t stream);
+cudaError_t launchPathtrace(const DScene &S, const DCamera &C, const DRenderer &R, const DFrame &F,
+                            bool count, cudaStream_t stream);
+
+// Accumulation reset: accum = 0, depth = 1e31 (frame/Frame.cpp:287-312).
+cudaError_t launchFrameReset(float4 *accum, float *depth, size_t numPixels, cudaStream_t stream);
+
+// Brick majorant grid of a structured volume: one cell per brick of
+// `brick` voxels per edge; majorant = max TF alpha over the TF bins that the
+// brick's texel value range can reach under trilinear + linear TF filtering.
+cudaError_t launchBrickMajorants(const float *field, const int dims[3], int brick,
+                                 const float4 *tf, int tfSize, float vrMin, float vrMax,
+                                 float *outMajorant, const int gdims[3], cudaStream_t stream);
+
+// On-device LBVH build (63-bit Morton codes, Karras-style hierarchy,
+// bottom-up refit) for one group's triangles.
+//   v1/e1/e2 : device float3-packed arrays, n triangles (local order)
+//   nodesOut : 4*max(n-1,1) float4 (BVH2 node layout of vsr_device.h)
+//   trisOut  : 3*n float4 in leaf order
+// Temporary device memory is allocated internally. Returns cudaSuccess or
+// the first CUDA error.
+struct BvhBuildStats {
+  int numNodes;
+  float buildMs;
+};
+cudaError_t buildGroupBVH(const float *v1, const float *e1, const float *e2, int n,
+                          float4 *nodesOut, float4 *trisOut, BvhBuildStats *stats,
+                          cudaStream_t stream);
+
+} // namespace vsr

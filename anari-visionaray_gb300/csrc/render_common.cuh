@@ -1,0 +1,775 @@
+// Device functions of the per-pixel hot path: RNG, cameras, clip planes,
+// BVH2 traversal, triangle test, materials, directional light, structured
+// field sampling, transfer-function lookup, DDA, delta tracking and frame
+// writes. Each function names the reference code whose behaviour it
+// reproduces (file:line in anari-visionaray).
+#pragma once
+
+#include "vsr_device.h"
+#include <float.h>
+#include <stdint.h>
+
+namespace vsr {
+
+// ----------------------------------------------------------------- float3 ops
+__device__ __forceinline__ float3 f3(float a) { return make_float3(a, a, a); }
+__device__ __forceinline__ float3 f3(float a, float b, float c) { return make_float3(a, b, c); }
+__device__ __forceinline__ float3 ld3(const float *p) { return make_float3(p[0], p[1], p[2]); }
+__device__ __forceinline__ float3 operator+(float3 a, float3 b) { return f3(a.x + b.x, a.y + b.y, a.z + b.z); }
+__device__ __forceinline__ float3 operator-(float3 a, float3 b) { return f3(a.x - b.x, a.y - b.y, a.z - b.z); }
+__device__ __forceinline__ float3 operator*(float3 a, float3 b) { return f3(a.x * b.x, a.y * b.y, a.z * b.z); }
+__device__ __forceinline__ float3 operator/(float3 a, float3 b) { return f3(a.x / b.x, a.y / b.y, a.z / b.z); }
+__device__ __forceinline__ float3 operator*(float3 a, float s) { return f3(a.x * s, a.y * s, a.z * s); }
+__device__ __forceinline__ float3 operator*(float s, float3 a) { return f3(a.x * s, a.y * s, a.z * s); }
+__device__ __forceinline__ float3 operator/(float3 a, float s) { return f3(a.x / s, a.y / s, a.z / s); }
+__device__ __forceinline__ float3 operator-(float3 a) { return f3(-a.x, -a.y, -a.z); }
+__device__ __forceinline__ void operator+=(float3 &a, float3 b) { a = a + b; }
+__device__ __forceinline__ void operator*=(float3 &a, float3 b) { a = a * b; }
+__device__ __forceinline__ void operator/=(float3 &a, float s) { a = a / s; }
+__device__ __forceinline__ float dot(float3 a, float3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+__device__ __forceinline__ float3 cross(float3 a, float3 b) {
+  return f3(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x);
+}
+__device__ __forceinline__ float length(float3 a) { return sqrtf(dot(a, a)); }
+__device__ __forceinline__ float3 normalize(float3 a) { return a / length(a); }
+__device__ __forceinline__ float3 fabs3(float3 a) { return f3(fabsf(a.x), fabsf(a.y), fabsf(a.z)); }
+__device__ __forceinline__ float3 min3(float3 a, float3 b) { return f3(fminf(a.x, b.x), fminf(a.y, b.y), fminf(a.z, b.z)); }
+__device__ __forceinline__ float3 max3(float3 a, float3 b) { return f3(fmaxf(a.x, b.x), fmaxf(a.y, b.y), fmaxf(a.z, b.z)); }
+__device__ __forceinline__ float maxe(float3 a) { return fmaxf(a.x, fmaxf(a.y, a.z)); }
+__device__ __forceinline__ float mine(float3 a) { return fminf(a.x, fminf(a.y, a.z)); }
+__device__ __forceinline__ float lerpf(float a, float b, float t) { return a + t * (b - a); }
+__device__ __forceinline__ float3 lerpR(float3 a, float3 b, float t) { return a * (1.f - t) + b * t; }
+__device__ __forceinline__ float3 mat3mul(const float *m, float3 v) {
+  return f3(m[0] * v.x + m[3] * v.y + m[6] * v.z, m[1] * v.x + m[4] * v.y + m[7] * v.z,
+            m[2] * v.x + m[5] * v.y + m[8] * v.z);
+}
+
+constexpr float kPi = 3.14159265358979323846f;
+constexpr float kTwoPi = 6.28318530717958647692f;
+constexpr float kInvPi = 0.31830988618379067154f;
+
+// faceforward: n flipped into the hemisphere (around nref) that i lies in.
+__device__ __forceinline__ float3 faceforward(float3 n, float3 i, float3 nref) {
+  return dot(i, nref) < 0.f ? -n : n;
+}
+// reflect: mirror of i (pointing away from the surface) about n.
+__device__ __forceinline__ float3 reflect(float3 i, float3 n) { return 2.f * dot(n, i) * n - i; }
+// refract: i points away from the surface, eta = eta_t/eta_i; 0 on TIR.
+__device__ __forceinline__ float3 refract(float3 i, float3 n, float eta) {
+  float r = 1.f / eta;
+  float cosi = dot(i, n);
+  float k = 1.f - r * r * (1.f - cosi * cosi);
+  if (k < 0.f) return f3(0.f);
+  return -r * i + (r * cosi - sqrtf(k)) * n;
+}
+__device__ __forceinline__ float3 cosineSampleHemisphere(float u1, float u2) {
+  float r = sqrtf(u1);
+  float phi = kTwoPi * u2;
+  float s, c;
+  sincosf(phi, &s, &c);
+  return f3(r * c, r * s, sqrtf(fmaxf(0.f, 1.f - u1)));
+}
+__device__ __forceinline__ float3 uniformSampleSphere(float u1, float u2) {
+  float z = 1.f - 2.f * u1;
+  float r = sqrtf(fmaxf(0.f, 1.f - z * z));
+  float phi = kTwoPi * u2;
+  float s, c;
+  sincosf(phi, &s, &c);
+  return f3(r * c, r * s, z);
+}
+__device__ __forceinline__ void orthonormalBasis(float3 &u, float3 &v, float3 w) {
+  v = fabsf(w.x) > fabsf(w.y) ? normalize(f3(-w.z, 0.f, w.x)) : normalize(f3(0.f, w.z, -w.y));
+  u = cross(v, w);
+}
+__device__ __forceinline__ float luminance(float3 c) { return 0.3f * c.x + 0.59f * c.y + 0.11f * c.z; }
+__device__ __forceinline__ float safeRcp(float f) { return f > 0.f ? 1.f / f : 0.f; }
+
+// epsilonFrom, renderer/common.h:14-18.
+__device__ __forceinline__ float epsilonFrom(float3 P, float3 dir, float t) {
+  float3 aP = fabs3(P);
+  float m = fmaxf(fmaxf(aP.x, aP.y), fmaxf(aP.z, maxe(fabs3(dir)) * t));
+  return m * 0x1.fp-18f;
+}
+
+// LCG<4>, common.h:55-102.
+struct Rng {
+  uint32_t state;
+  __device__ __forceinline__ void init(uint32_t v0, uint32_t v1) {
+    uint32_t s0 = 0;
+#pragma unroll
+    for (int n = 0; n < 4; n++) {
+      s0 += 0x9e3779b9u;
+      v0 += ((v1 << 4) + 0xa341316cu) ^ (v1 + s0) ^ ((v1 >> 5) + 0xc8013ea4u);
+      v1 += ((v0 << 4) + 0xad90777du) ^ (v0 + s0) ^ ((v0 >> 5) + 0x7e95761eu);
+    }
+    state = v0;
+  }
+  __device__ __forceinline__ float operator()() {
+    state = 1664525u * state + 1013904223u;
+    return (state & 0x00FFFFFFu) / (float)0x01000000;
+  }
+};
+
+struct Ray {
+  float3 o, d;
+  float tmin, tmax;
+};
+
+// ------------------------------------------------------------------ camera
+// dco::Camera::primary_ray (DeviceCopyableObjects.h:2583-2600) for the
+// thin-lens, matrix, orthographic and omnidirectional cameras. The thin
+// lens draws two numbers (used only with a positive aperture) and every
+// stochastic primary ray draws one more for ray.time.
+template <bool Stochastic>
+__device__ __forceinline__ Ray primaryRay(const DCamera &c, Rng &rng, float x, float y, float w,
+                                          float h) {
+  Ray r;
+  r.tmin = 0.f;
+  r.tmax = FLT_MAX;
+  if (c.type == CAM_PERSPECTIVE) {
+    float sx = (x + 0.5f) / w, sy = (y + 0.5f) / h;
+    sx = (1.f - sx) * c.region[0] + sx * c.region[2];
+    sy = (1.f - sy) * c.region[1] + sy * c.region[3];
+    float u = 2.f * sx - 1.f, v = 2.f * sy - 1.f;
+    float3 U = ld3(c.U), V = ld3(c.V), W = ld3(c.W);
+    r.o = ld3(c.eye);
+    r.d = normalize(U * u + V * v + W);
+    if (Stochastic) {
+      float l1 = rng(), l2 = rng();
+      if (c.lensRadius > 0.f) {
+        float3 focal = r.o + r.d * (c.focusDistance / dot(r.d, W));
+        float a = 2.f * l1 - 1.f, b = 2.f * l2 - 1.f, rr, phi;
+        if (a == 0.f && b == 0.f) { rr = 0.f; phi = 0.f; }
+        else if (fabsf(a) > fabsf(b)) { rr = a; phi = (kPi / 4.f) * (b / a); }
+        else { rr = b; phi = (kPi / 2.f) - (kPi / 4.f) * (a / b); }
+        float dx = rr * cosf(phi) * c.lensRadius, dy = rr * sinf(phi) * c.lensRadius;
+        r.o = ld3(c.eye) + normalize(U) * dx + normalize(V) * dy;
+        r.d = normalize(focal - r.o);
+      }
+    }
+  } else if (c.type == CAM_MATRIX) {
+    float u = 2.f * (x + 0.5f) / w - 1.f, v = 2.f * (y + 0.5f) / h - 1.f;
+    const float *m = c.inv;
+    float4 p0, p1;
+    p0.x = m[0] * u + m[4] * v + m[8] * -1.f + m[12];
+    p0.y = m[1] * u + m[5] * v + m[9] * -1.f + m[13];
+    p0.z = m[2] * u + m[6] * v + m[10] * -1.f + m[14];
+    p0.w = m[3] * u + m[7] * v + m[11] * -1.f + m[15];
+    p1.x = m[0] * u + m[4] * v + m[8] + m[12];
+    p1.y = m[1] * u + m[5] * v + m[9] + m[13];
+    p1.z = m[2] * u + m[6] * v + m[10] + m[14];
+    p1.w = m[3] * u + m[7] * v + m[11] + m[15];
+    float3 a = f3(p0.x / p0.w, p0.y / p0.w, p0.z / p0.w);
+    float3 b = f3(p1.x / p1.w, p1.y / p1.w, p1.z / p1.w);
+    r.o = a;
+    r.d = normalize(b - a);
+  } else if (c.type == CAM_ORTHO) {
+    float sx = (x + 0.5f) / w, sy = (y + 0.5f) / h;
+    sx = (1.f - sx) * c.region[0] + sx * c.region[2];
+    sy = (1.f - sy) * c.region[1] + sy * c.region[3];
+    r.o = ld3(c.U) * sx + ld3(c.V) * sy + ld3(c.W);
+    r.d = normalize(ld3(c.dir));
+  } else {  // omnidirectional
+    float sx = (x + 0.5f) / w, sy = (y + 0.5f) / h;
+    float theta = kPi * sy, phi = kTwoPi * sx;
+    float3 ld = f3(sinf(theta) * cosf(phi), cosf(theta), sinf(theta) * sinf(phi));
+    r.o = ld3(c.U) * sx + ld3(c.V) * sy + ld3(c.W);
+    r.d = ld * f3(1.f, -1.f, 1.f);
+  }
+  if (Stochastic) (void)rng();  // ray.time = lerp(shutter, rng())
+  return r;
+}
+
+// clipRay, renderer/common.h:1469-1482.
+__device__ __forceinline__ void clipRay(Ray &r, const DRenderer &R) {
+  for (int i = 0; i < R.numClipPlanes; ++i) {
+    float3 N = f3(R.clip[i][0], R.clip[i][1], R.clip[i][2]);
+    float D = R.clip[i][3];
+    float s = dot(N, r.d);
+    if (s != 0.f) {
+      float t = (D - dot(N, r.o)) / s;
+      if (s < 0.f) r.tmin = fmaxf(r.tmin, t);
+      else r.tmax = fminf(r.tmax, t);
+    }
+  }
+}
+
+// ------------------------------------------------------------ traversal
+struct Hit {
+  float t, u, v;
+  int inst;   // instance index, -1 = none
+  int tri;    // local triangle id within the instance's group
+  int leaf;   // position of the triangle in the group's leaf-ordered array
+};
+
+__device__ __forceinline__ void localRay(const DInstance &I, float3 o, float3 d, float3 &lo,
+                                         float3 &ld) {
+  lo = mat3mul(I.affineInv, o + ld3(I.transInv));
+  ld = mat3mul(I.affineInv, d);
+}
+
+// Stack-based BVH2 traversal, near child first. Closest hit ordered by
+// (t, instance, triangle), the order the CPU restatement uses, so any valid
+// BVH gives the same hit. AnyHit stops at the first accepted hit.
+template <bool AnyHit, bool Count>
+__device__ __forceinline__ bool traverseGroup(const DGroup &G, float3 o, float3 d, float tmin,
+                                              int inst, Hit &best, uint32_t &err,
+                                              unsigned long long *cnt) {
+  const float3 inv = f3(1.f / d.x, 1.f / d.y, 1.f / d.z);
+  const float3 oi = f3(-o.x * inv.x, -o.y * inv.y, -o.z * inv.z);
+  int stack[kTraversalStack];
+  int sp = 0;
+  int node = 0;
+  bool found = false;
+  unsigned nodeVisits = 0, triTests = 0;
+  for (;;) {
+    if (node >= 0) {
+      const float4 *N = G.nodes + 4 * (size_t)node;
+      const float4 n0 = __ldg(N), n1 = __ldg(N + 1), n2 = __ldg(N + 2);
+      const int4 n3 = __ldg(reinterpret_cast<const int4 *>(N + 3));
+      if (Count) ++nodeVisits;
+      const float tb = best.t;
+      float a0 = fmaf(n0.x, inv.x, oi.x), b0 = fmaf(n0.y, inv.x, oi.x);
+      float a1 = fmaf(n0.z, inv.y, oi.y), b1 = fmaf(n0.w, inv.y, oi.y);
+      float a2 = fmaf(n2.x, inv.z, oi.z), b2 = fmaf(n2.y, inv.z, oi.z);
+      float c0min = fmaxf(fmaxf(fminf(a0, b0), fminf(a1, b1)), fmaxf(fminf(a2, b2), tmin));
+      float c0max = fminf(fminf(fmaxf(a0, b0), fmaxf(a1, b1)), fminf(fmaxf(a2, b2), tb));
+      a0 = fmaf(n1.x, inv.x, oi.x); b0 = fmaf(n1.y, inv.x, oi.x);
+      a1 = fmaf(n1.z, inv.y, oi.y); b1 = fmaf(n1.w, inv.y, oi.y);
+      a2 = fmaf(n2.z, inv.z, oi.z); b2 = fmaf(n2.w, inv.z, oi.z);
+      float c1min = fmaxf(fmaxf(fminf(a0, b0), fminf(a1, b1)), fmaxf(fminf(a2, b2), tmin));
+      float c1max = fminf(fminf(fmaxf(a0, b0), fmaxf(a1, b1)), fminf(fmaxf(a2, b2), tb));
+      const bool h0 = c0min <= c0max, h1 = c1min <= c1max;
+      if (!h0 && !h1) {
+        if (sp == 0) break;
+        node = stack[--sp];
+      } else {
+        int near = h0 ? n3.x : n3.y;
+        if (h0 && h1) {
+          int far = n3.y;
+          if (c1min < c0min) { near = n3.y; far = n3.x; }
+          if (sp < kTraversalStack) stack[sp++] = far;
+          else err |= ERR_STACK_OVERFLOW;
+        }
+        node = near;
+      }
+      continue;
+    }
+    // leaf
+    const uint32_t code = ~(uint32_t)node;
+    const int first = (int)(code & kLeafFirstMask);
+    const int count = (int)(code >> kLeafCountShift) + 1;
+    for (int k = 0; k < count; ++k) {
+      const float4 *T = G.tris + 3 * (size_t)(first + k);
+      const float4 ta = __ldg(T), tbv = __ldg(T + 1), tc = __ldg(T + 2);
+      if (Count) ++triTests;
+      const float3 v1 = f3(ta.x, ta.y, ta.z), e1 = f3(tbv.x, tbv.y, tbv.z), e2 = f3(tc.x, tc.y, tc.z);
+      const float3 s1 = cross(d, e2);
+      const float div = dot(s1, e1);
+      if (div == 0.f) continue;
+      const float idiv = 1.f / div;
+      const float3 dd = o - v1;
+      const float bb1 = dot(dd, s1) * idiv;
+      if (bb1 < 0.f || bb1 > 1.f) continue;
+      const float3 s2 = cross(dd, e1);
+      const float bb2 = dot(d, s2) * idiv;
+      if (bb2 < 0.f || bb1 + bb2 > 1.f) continue;
+      const float t = dot(e2, s2) * idiv;
+      if (!(t >= tmin)) continue;
+      const int local = __float_as_int(ta.w);
+      const bool closer =
+          t < best.t || (t == best.t && best.inst >= 0 &&
+                         (inst < best.inst || (inst == best.inst && local < best.tri)));
+      if (!closer) continue;
+      best.t = t; best.u = bb1; best.v = bb2; best.inst = inst; best.tri = local;
+      best.leaf = first + k;
+      found = true;
+      if (AnyHit) {
+        sp = 0;
+        break;
+      }
+    }
+    if (AnyHit && found) break;
+    if (sp == 0) break;
+    node = stack[--sp];
+  }
+  if (Count) {
+    atomicAdd(&cnt[1], (unsigned long long)nodeVisits);
+    atomicAdd(&cnt[2], (unsigned long long)triTests);
+  }
+  return found;
+}
+
+// intersectSurfaces(Ray, TLS, shadow), DeviceCopyableObjects.h:1826-1839,
+// with intersect(Ray, Instance) :1772-1814 for the instance transform.
+template <bool AnyHit, bool Count>
+__device__ __forceinline__ bool traceSurfaces(const DScene &S, const Ray &r, Hit &h, uint32_t &err,
+                                              unsigned long long *cnt) {
+  h.t = r.tmax;
+  h.inst = -1;
+  h.tri = -1;
+  h.leaf = -1;
+  h.u = h.v = 0.f;
+  if (Count) atomicAdd(&cnt[0], 1ull);
+  bool any = false;
+  for (int i = 0; i < S.numInstances; ++i) {
+    const DInstance &I = S.instances[i];
+    const DGroup &G = S.groups[I.group];
+    if (G.numNodes == 0) continue;
+    float3 lo, ld;
+    localRay(I, r.o, r.d, lo, ld);
+    if (traverseGroup<AnyHit, Count>(G, lo, ld, r.tmin, i, h, err, cnt)) {
+      any = true;
+      if (AnyHit) break;
+    }
+  }
+  if (!any) h.t = FLT_MAX;
+  return any;
+}
+
+// --------------------------------------------------------------- materials
+// renderer/common.h:793-1415 with constant parameters and no tangent frame.
+__device__ __forceinline__ float pow5(float f) { return f * f * f * f * f; }
+__device__ __forceinline__ float mapRoughness(float r) { return fmaxf(0.045f, r); }
+__device__ __forceinline__ float D_GGX(float NdotH, float alpha, float EPS) {
+  float alpha2 = alpha * alpha;
+  float d = (NdotH * alpha2 - NdotH) * NdotH + 1.f;
+  float denom = kPi * d * d;
+  return alpha2 / fmaxf(EPS, denom);
+}
+
+__device__ __forceinline__ float3 materialColor(const DMaterial &m) {
+  float3 base = ld3(m.baseColor);
+  return m.type == MAT_PBR ? lerpR(base, f3(0.f), m.metallic) : base;
+}
+
+__device__ __forceinline__ float materialOpacity(const DMaterial &m) {
+  if (m.alphaMode == ALPHA_OPAQUE) return 1.f;
+  if (m.alphaMode == ALPHA_BLEND) return m.opacity;
+  return m.opacity >= m.alphaCutoff ? 1.f : 0.f;
+}
+
+__device__ float3 evalPBR(const DMaterial &m, float3 Ns, float3 viewDir, float3 lightDir) {
+  const float metallic = m.metallic;
+  const float pr = mapRoughness(m.roughness);
+  const float pcr = mapRoughness(m.clearcoatRoughness);
+  const float psr = mapRoughness(m.sheenRoughness);
+  const float alpha = pr * pr;
+  const float clearcoatAlpha = pcr * pcr;
+  const float EPS = 1e-14f;
+  const float3 H = normalize(lightDir + viewDir);
+  const float NdotV = fabsf(dot(Ns, viewDir)) + EPS;
+  const float NdotH = fmaxf(EPS, dot(Ns, H));
+  const float NdotL = fmaxf(EPS, dot(Ns, lightDir));
+  const float LdotH = fmaxf(EPS, dot(lightDir, H));
+  const float VdotH = fmaxf(EPS, dot(viewDir, H));
+  const float3 baseColor = ld3(m.baseColor);
+  const float3 diffuseColor = lerpR(baseColor, f3(0.f), metallic);
+  float f0s = (1.f - m.ior) / (1.f + m.ior);
+  f0s = f0s * f0s;
+  const float3 f0 = lerpR(f3(f0s), baseColor, metallic);
+  const float3 F = f0 + (f3(1.f) - f0) * pow5(1.f - VdotH);
+  const float f90 = 0.5f + 2.f * alpha * LdotH * LdotH;
+  const float lightScatter = 1.f + (f90 - 1.f) * pow5(1.f - NdotL);
+  const float viewScatter = 1.f + (f90 - 1.f) * pow5(1.f - NdotV);
+  const float3 diffuseBRDF = diffuseColor * (lightScatter * viewScatter * kInvPi);
+  const float D = D_GGX(NdotH, alpha, EPS);
+  const float a2 = alpha * alpha;
+  const float GGXV = NdotL / (NdotV + sqrtf(a2 + (1.f - a2) * NdotV * NdotV));
+  const float GGXL = NdotV / (NdotL + sqrtf(a2 + (1.f - a2) * NdotL * NdotL));
+  const float V = 0.5f / (GGXV + GGXL);
+  const float3 specularBRDF = F * (D * V);
+  const float Dc = D_GGX(NdotH, clearcoatAlpha, EPS);
+  const float Vc = 0.25f / fmaxf(EPS, LdotH * LdotH);
+  const float Fc = (0.04f + (1.f - 0.04f) * pow5(1.f - LdotH)) * m.clearcoat;
+  const float Frc = (Dc * Vc) * Fc;
+  const float sheenAlphaInv = 1.f / psr;
+  const float cos2h = NdotH * NdotH;
+  const float sin2h = fmaxf(1.f - cos2h, 0.0078125f);
+  const float3 Ds =
+      ld3(m.sheenColor) * ((2.f + sheenAlphaInv) * powf(sin2h, sheenAlphaInv * 0.5f) / kTwoPi);
+  return ((diffuseBRDF + specularBRDF) * (1.f - Fc) + f3(Frc)) + Ds;
+}
+
+__device__ __forceinline__ float3 evalMaterial(const DMaterial &m, float3 Ns, float3 viewDir,
+                                               float3 lightDir) {
+  if (m.type == MAT_MATTE) return ld3(m.baseColor) * kInvPi;
+  return evalPBR(m, Ns, viewDir, lightDir);
+}
+
+struct BSDFSample {
+  float3 dir, f;
+  float pdf, cosT;
+};
+
+__device__ __forceinline__ float3 sampleGGXVNDF(float3 V, float ax, float ay, float U1, float U2) {
+  float3 Vh = normalize(V * f3(ax, ay, 1.f));
+  float lensq = Vh.x * Vh.x + Vh.y * Vh.y;
+  float3 T1 = lensq > 0.f ? f3(-Vh.y, Vh.x, 0.f) / sqrtf(lensq) : f3(1.f, 0.f, 0.f);
+  float3 T2 = cross(Vh, T1);
+  float r = sqrtf(U1);
+  float phi = kTwoPi * U2;
+  float sp, cp;
+  sincosf(phi, &sp, &cp);
+  float t1 = r * cp;
+  float t2 = r * sp;
+  float s = 0.5f * (1.f + Vh.z);
+  t2 = (1.f - s) * sqrtf(fmaxf(0.f, 1.f - t1 * t1)) + s * t2;
+  float3 Nh = t1 * T1 + t2 * T2 + sqrtf(1.f - t1 * t1 - t2 * t2) * Vh;
+  return normalize(f3(Nh.x * ax, Nh.y * ay, fmaxf(0.f, Nh.z)));
+}
+
+__device__ __forceinline__ void pdfGGXVNDF(float3 L, float3 V, float ax, float eta_i, float eta_t,
+                                           float3 Ns, float &pdfSpec, float &pdfTrans) {
+  const float EPS = 1e-14f;
+  pdfSpec = 0.f;
+  pdfTrans = 0.f;
+  const float NdotL = dot(Ns, L);
+  const float NdotV = fmaxf(EPS, dot(Ns, V));
+  const float ax2 = ax * ax;
+  if (NdotL > 0.f) {
+    float3 H = V + L;
+    float lenH = length(H);
+    if (lenH > 1e-4f) {
+      H /= lenH;
+      float NdotH = fmaxf(EPS, dot(Ns, H));
+      float D = D_GGX(NdotH, ax, EPS);
+      float G1 = 2.f * NdotV / (NdotV + sqrtf(ax2 + (1.f - ax2) * NdotV * NdotV));
+      pdfSpec = (D * G1) / (4.f * NdotV);
+    }
+  } else if (NdotL < 0.f) {
+    float3 H = -(V * eta_i + L * eta_t);
+    float lenH = length(H);
+    if (lenH > 1e-4f) {
+      H /= lenH;
+      if (dot(Ns, H) < 0.f) H = -H;
+      float NdotH = fmaxf(EPS, dot(Ns, H));
+      float LdotH = fabsf(dot(L, H));
+      float VdotH = fabsf(dot(V, H));
+      if (VdotH > 0.f && LdotH > 0.f) {
+        float D = D_GGX(NdotH, ax, EPS);
+        float G1 = 2.f * NdotV / (NdotV + sqrtf(ax2 + (1.f - ax2) * NdotV * NdotV));
+        float pdfNe = (D * G1 * VdotH) / NdotV;
+        float denom = (eta_i * VdotH + eta_t * LdotH);
+        float jacobian = (eta_t * eta_t * LdotH) / (denom * denom);
+        pdfTrans = pdfNe * jacobian;
+      }
+    }
+  }
+}
+
+// sampleMaterial, renderer/common.h:1371-1415 and :1209-1368.
+__device__ BSDFSample sampleMaterial(const DMaterial &m, float3 Ng, float3 Ns, float3 viewDir,
+                                     Rng &rnd) {
+  BSDFSample res;
+  float3 w = faceforward(Ns, viewDir, Ng);
+  float3 v = fabsf(w.x) > fabsf(w.y) ? normalize(f3(-w.z, 0.f, w.x)) : normalize(f3(0.f, w.z, -w.y));
+  float3 u = cross(v, w);
+  if (m.type == MAT_MATTE) {
+    float u1 = rnd(), u2 = rnd();
+    float3 sp = cosineSampleHemisphere(u1, u2);
+    res.dir = normalize(sp.x * u + sp.y * v + sp.z * w);
+    res.pdf = fmaxf(0.f, dot(Ns, res.dir)) * kInvPi;
+  } else {
+    const float EPS = 1e-14f;
+    const float metallic = m.metallic;
+    const float pr = mapRoughness(m.roughness);
+    const float alpha = pr * pr;
+    const float pcr = mapRoughness(m.clearcoatRoughness);
+    const float clearcoatAlpha = pcr * pcr;
+    const float NdotV = fmaxf(EPS, dot(Ns, viewDir));
+    const float3 baseColor = ld3(m.baseColor);
+    const float3 diffuseColor = lerpR(baseColor, f3(0.f), metallic);
+    float f0s = (1.f - m.ior) / (1.f + m.ior);
+    f0s = f0s * f0s;
+    const float3 f0 = lerpR(f3(f0s), baseColor, metallic);
+    const float3 F = f0 + (f3(1.f) - f0) * pow5(1.f - NdotV);
+    const float fClear = m.clearcoat * 0.04f;
+    const float baseEnergy = 1.f - fClear;
+    const float fSpec = luminance(F);
+    const float remainingEnergy = baseEnergy * (1.f - fSpec);
+    const float wDiff = luminance(diffuseColor) * remainingEnergy * (1.f - m.transmission);
+    const float wSpec = baseEnergy * fSpec;
+    const float wTrans = remainingEnergy * m.transmission;
+    const float wSum = wDiff + wSpec + wTrans + fClear;
+    const float pDiff = wSum > 0.f ? wDiff / wSum : 0.0f;
+    const float pSpec = wSum > 0.f ? wSpec / wSum : 0.333f;
+    const float pTrans = wSum > 0.f ? wTrans / wSum : 0.667f;
+    const float pClear = 1.f - pDiff - pSpec - pTrans;
+    const float lobe = rnd();
+    const float3 V = f3(dot(u, viewDir), dot(v, viewDir), dot(w, viewDir));
+    const bool entering = dot(Ns, viewDir) > 0.f;
+    const float eta_i = entering ? 1.0f : m.ior;
+    const float eta_t = entering ? m.ior : 1.0f;
+    const float u1 = rnd(), u2 = rnd();
+    if (lobe < pDiff) {
+      float3 sp = cosineSampleHemisphere(u1, u2);
+      res.dir = normalize(sp.x * u + sp.y * v + sp.z * w);
+    } else if (lobe < pDiff + pSpec) {
+      float3 Ne = sampleGGXVNDF(V, alpha, alpha, u1, u2);
+      res.dir = reflect(viewDir, u * Ne.x + v * Ne.y + w * Ne.z);
+    } else if (lobe < pDiff + pSpec + pTrans) {
+      float3 Ne = sampleGGXVNDF(V, alpha, alpha, u1, u2);
+      if (dot(V, Ne) < 0.f) Ne = -Ne;
+      float3 Nw = u * Ne.x + v * Ne.y + w * Ne.z;
+      res.dir = refract(viewDir, Nw, eta_t / eta_i);
+      if (length(res.dir) < 1e-4f) res.dir = reflect(viewDir, Nw);
+    } else {
+      float3 Ne = sampleGGXVNDF(V, clearcoatAlpha, clearcoatAlpha, u1, u2);
+      res.dir = reflect(viewDir, u * Ne.x + v * Ne.y + w * Ne.z);
+    }
+    const float pdfDiff = fmaxf(0.f, dot(Ns, res.dir)) * kInvPi;
+    float pdfSpec = 0.f, pdfTrans = 0.f;
+    pdfGGXVNDF(res.dir, viewDir, alpha, eta_i, eta_t, Ns, pdfSpec, pdfTrans);
+    float pdfClear = 0.f, dummy = 0.f;
+    pdfGGXVNDF(res.dir, viewDir, clearcoatAlpha, entering ? 1.0f : 1.5f, entering ? 1.5f : 1.0f, Ns,
+               pdfClear, dummy);
+    res.pdf = pDiff * pdfDiff + pSpec * pdfSpec + pTrans * pdfTrans + pClear * pdfClear;
+  }
+  res.cosT = fmaxf(0.f, dot(Ns, res.dir));
+  res.f = evalMaterial(m, Ns, viewDir, res.dir);
+  return res;
+}
+
+// ------------------------------------------------------------------ light
+// Directional light: scene/light/Directional.cpp:30-40 and sampleLight,
+// renderer/common.h:1432-1466 (dist2 = 1, pdf = 1, dist = FLT_MAX).
+struct LightSample {
+  float3 intensity, dir;
+  float pdf, dist, dist2;
+};
+
+__device__ __forceinline__ LightSample sampleLight(const DLight &L, Rng &rnd) {
+  LightSample s;
+  float3 d = ld3(L.dir);
+  if (L.cosHalfAngle < 1.f) {
+    float u1 = rnd(), u2 = rnd();
+    float cz = 1.f - u1 * (1.f - L.cosHalfAngle);
+    float sz = sqrtf(fmaxf(0.f, 1.f - cz * cz));
+    float phi = kTwoPi * u2;
+    float3 a, b;
+    orthonormalBasis(a, b, d);
+    d = normalize(a * (sz * cosf(phi)) + b * (sz * sinf(phi)) + d * cz);
+  }
+  s.dir = d;
+  s.dist = FLT_MAX;
+  s.pdf = 1.f;
+  s.dist2 = 1.f;
+  s.intensity = ld3(L.intensity);
+  return s;
+}
+
+// ----------------------------------------------------------------- volumes
+// tex3D(normalized coords, linear, clamp) on the structured field,
+// sampleField DeviceCopyableObjects.h:478-481; texel i is centred at
+// (i+0.5)/N.
+__device__ __forceinline__ float sampleField(const DVolume &V, float3 P) {
+  const int nx = V.dims[0], ny = V.dims[1], nz = V.dims[2];
+  const float x = P.x * nx - 0.5f, y = P.y * ny - 0.5f, z = P.z * nz - 0.5f;
+  const float fx0 = floorf(x), fy0 = floorf(y), fz0 = floorf(z);
+  const float fx = x - fx0, fy = y - fy0, fz = z - fz0;
+  const int ix = (int)fminf(fmaxf(fx0, -1.f), (float)nx);
+  const int iy = (int)fminf(fmaxf(fy0, -1.f), (float)ny);
+  const int iz = (int)fminf(fmaxf(fz0, -1.f), (float)nz);
+  const int x0 = min(max(ix, 0), nx - 1), x1 = min(max(ix + 1, 0), nx - 1);
+  const int y0 = min(max(iy, 0), ny - 1), y1 = min(max(iy + 1, 0), ny - 1);
+  const int z0 = min(max(iz, 0), nz - 1), z1 = min(max(iz + 1, 0), nz - 1);
+  const float *d = V.data;
+  const size_t sy = (size_t)nx, sz = (size_t)nx * ny;
+  const size_t r00 = z0 * sz + y0 * sy, r10 = z0 * sz + y1 * sy;
+  const size_t r01 = z1 * sz + y0 * sy, r11 = z1 * sz + y1 * sy;
+  const float c00 = lerpf(__ldg(d + r00 + x0), __ldg(d + r00 + x1), fx);
+  const float c10 = lerpf(__ldg(d + r10 + x0), __ldg(d + r10 + x1), fx);
+  const float c01 = lerpf(__ldg(d + r01 + x0), __ldg(d + r01 + x1), fx);
+  const float c11 = lerpf(__ldg(d + r11 + x0), __ldg(d + r11 + x1), fx);
+  const float c0 = lerpf(c00, c10, fy);
+  const float c1 = lerpf(c01, c11, fy);
+  return lerpf(c0, c1, fz);
+}
+
+// tex1D over the TF table (normalized, linear, clamp) after postClassify's
+// value-range normalisation, DeviceCopyableObjects.h:614-619.
+__device__ __forceinline__ float4 tfLookup(const float4 *tf, int n, float vrMin, float vrMax,
+                                           float val) {
+  val = (val - vrMin) / (vrMax - vrMin);
+  const float x = val * n - 0.5f;
+  const float f0 = floorf(x);
+  const float f = x - f0;
+  const int i = (int)fminf(fmaxf(f0, -1.f), (float)n);
+  const int i0 = min(max(i, 0), n - 1), i1 = min(max(i + 1, 0), n - 1);
+  const float4 a = tf[i0], b = tf[i1];
+  return make_float4(lerpf(a.x, b.x, f), lerpf(a.y, b.y, f), lerpf(a.z, b.z, f), lerpf(a.w, b.w, f));
+}
+
+struct BoxHit {
+  bool hit;
+  float tnear, tfar;
+};
+__device__ __forceinline__ BoxHit intersectBox(float3 o, float3 d, const float *lo, const float *hi) {
+  float3 inv = f3(1.f) / d;
+  float3 t1 = (ld3(lo) - o) * inv, t2 = (ld3(hi) - o) * inv;
+  BoxHit b;
+  b.tnear = maxe(min3(t1, t2));
+  b.tfar = mine(max3(t1, t2));
+  b.hit = b.tnear <= b.tfar;
+  return b;
+}
+
+__device__ __forceinline__ int projectOnGrid1(float v, float lo, float hi, int n) {
+  float v01 = (v - lo) / (hi - lo);
+  int c = (int)fminf(fmaxf(v01 * (float)n, -1.f), (float)n);
+  return min(max(c, 0), n - 1);
+}
+
+// Delta tracking through one volume: intersect(Ray, Volume),
+// DeviceCopyableObjects.h:680-796, with the DDA of renderer/DDA.h:12-113
+// over the majorant grid (voxel-space bounds [0,1]^3). Returns true on a
+// scattering event at object-space parameter tHit.
+template <bool Count>
+__device__ bool deltaTrack(const DVolume &V, float3 o, float3 d, float tmin, float tmax, Rng &rnd,
+                           float &tHit, float3 &albedo, uint32_t &err, unsigned long long *cnt) {
+  BoxHit bh = intersectBox(o, d, V.boundsLo, V.boundsHi);
+  if (!bh.hit || bh.tfar < tmin || bh.tnear > tmax) return false;
+  tmin = fmaxf(tmin, bh.tnear);
+  tmax = fminf(tmax, bh.tfar);
+  const float3 S = ld3(V.S);
+  o = S * (o + ld3(V.T));
+  d = S * d;
+  const float dt_scale = length(d);
+  d = normalize(d);
+  tmin *= dt_scale;
+  tmax *= dt_scale;
+  const float unitDistance = V.unitDistance * dt_scale;
+  const float invUnitDistance = 1.f / unitDistance;
+  bool hit = false;
+  float ht = tmax;
+  unsigned samples = 0, cells = 0;
+  int budget = 1 << 22;
+
+  auto woodcock = [&](int leafID, float t0, float t1) -> bool {
+    if (Count) ++cells;
+    const float majorant = V.majorant ? __ldg(V.majorant + leafID) : 1.f;
+    float t = t0;
+    while (true) {
+      if (majorant <= 0.f) break;
+      t -= (logf(1.f - rnd()) / (majorant * invUnitDistance));
+      if (t >= t1) break;
+      if (Count) ++samples;
+      if (--budget <= 0) { err |= ERR_TRACK_LIMIT; return false; }
+      float3 P = o + d * t;
+      float4 s = tfLookup(V.tf, V.tfSize, V.vrMin, V.vrMax, sampleField(V, P));
+      float u = rnd();
+      if (s.w >= u * majorant) {
+        albedo = f3(s.x, s.y, s.z);
+        hit = true;
+        ht = t;
+        return false;
+      }
+    }
+    return true;
+  };
+
+  if (V.majorant) {
+    // dda3 with modelBounds = [0,1]^3 in voxel space
+    const float ray_tmin = tmin;
+    const float3 ro = o + tmin * d;
+    const float rtmax = tmax - ray_tmin;
+    const float3 rcp = f3(1.f) / d;
+    const float3 lo = (f3(0.f) - ro) * rcp;
+    const float3 hi = (f3(1.f) - ro) * rcp;
+    float3 tnear = min3(lo, hi);
+    const float3 tfar = max3(lo, hi);
+    if (d.x == 0.f) tnear.x = FLT_MAX;
+    if (d.y == 0.f) tnear.y = FLT_MAX;
+    if (d.z == 0.f) tnear.z = FLT_MAX;
+    const int gx = V.gdims[0], gy = V.gdims[1], gz = V.gdims[2];
+    int cx = projectOnGrid1(ro.x, 0.f, 1.f, gx);
+    int cy = projectOnGrid1(ro.y, 0.f, 1.f, gy);
+    int cz = projectOnGrid1(ro.z, 0.f, 1.f, gz);
+    const float3 dist = max3(f3(0.f), (tfar - tnear) / f3((float)gx, (float)gy, (float)gz));
+    const int stx = d.x > 0.f ? 1 : -1, sty = d.y > 0.f ? 1 : -1, stz = d.z > 0.f ? 1 : -1;
+    const int spx = d.x > 0.f ? gx : -1, spy = d.y > 0.f ? gy : -1, spz = d.z > 0.f ? gz : -1;
+    float3 tnext;
+    tnext.x = d.x > 0.f ? tnear.x + float(cx + 1) * dist.x : tnear.x + float(gx - cx) * dist.x;
+    tnext.y = d.y > 0.f ? tnear.y + float(cy + 1) * dist.y : tnear.y + float(gy - cy) * dist.y;
+    tnext.z = d.z > 0.f ? tnear.z + float(cz + 1) * dist.z : tnear.z + float(gz - cz) * dist.z;
+    float t0 = 0.f;
+    int steps = 4 * (gx + gy + gz) + 16;
+    while (true) {
+      if (--steps < 0) { err |= ERR_DDA_LIMIT; break; }
+      const float t1 = fminf(mine(tnext), rtmax);
+      const int id = (cz * gy + cy) * gx + cx;
+      if (!woodcock(id, ray_tmin + t0, ray_tmin + t1)) break;
+      const float tc = mine(tnext);
+      if (tnext.x == tc) {
+        tnext.x += dist.x;
+        cx += stx;
+        if (cx == spx) break;
+      }
+      if (tnext.y == tc) {
+        tnext.y += dist.y;
+        cy += sty;
+        if (cy == spy) break;
+      }
+      if (tnext.z == tc) {
+        tnext.z += dist.z;
+        cz += stz;
+        if (cz == spz) break;
+      }
+      t0 = t1;
+    }
+  } else {
+    woodcock(-1, tmin, tmax);
+  }
+  if (Count) {
+    atomicAdd(&cnt[4], (unsigned long long)samples);
+    atomicAdd(&cnt[5], (unsigned long long)cells);
+  }
+  if (hit) tHit = ht / dt_scale;
+  return hit;
+}
+
+// ------------------------------------------------------------------- frame
+// dco::Frame::writeSample = fillGBuffer + accumSample + toneMap,
+// DeviceCopyableObjects.h:2692-2781; cvt_uint32(_srgb), frame/common.h:31-48.
+__device__ __forceinline__ float linearToSrgb(float x) {
+  return x <= 0.0031308f ? 12.92f * x : 1.055f * powf(x, 1.f / 2.4f) - 0.055f;
+}
+__device__ __forceinline__ uint32_t cvtU8(float f) {
+  return (uint32_t)(255.f * fminf(fmaxf(f, 0.f), 1.f));
+}
+
+__device__ __forceinline__ void writeSample(const DFrame &F, int x, int y, bool stochastic,
+                                            float4 color, float depth, float3 Ng, float3 albedo) {
+  const size_t idx = (size_t)y * F.width + x;
+  if (F.depth && !(depth > F.depth[idx])) {
+    F.depth[idx] = depth;
+    if (F.normal) {
+      F.normal[3 * idx] = Ng.x;
+      F.normal[3 * idx + 1] = Ng.y;
+      F.normal[3 * idx + 2] = Ng.z;
+    }
+    if (F.albedo) {
+      F.albedo[3 * idx] = albedo.x;
+      F.albedo[3 * idx + 1] = albedo.y;
+      F.albedo[3 * idx + 2] = albedo.z;
+    }
+  }
+  if (stochastic) {
+    const float a = 1.f / (F.accumID + 1);
+    const float4 acc = F.accum[idx];
+    color = make_float4((1 - a) * acc.x + a * color.x, (1 - a) * acc.y + a * color.y,
+                        (1 - a) * acc.z + a * color.z, (1 - a) * acc.w + a * color.w);
+    F.accum[idx] = color;
+  }
+  if (F.colorType == COLOR_FLOAT4) {
+    reinterpret_cast<float4 *>(F.color)[idx] = color;
+  } else if (F.colorType == COLOR_UFIXED8 || F.colorType == COLOR_SRGB8) {
+    float r = color.x, g = color.y, b = color.z;
+    if (F.colorType == COLOR_SRGB8) { r = linearToSrgb(r); g = linearToSrgb(g); b = linearToSrgb(b); }
+    reinterpret_cast<uint32_t *>(F.color)[idx] =
+        cvtU8(r) | (cvtU8(g) << 8) | (cvtU8(b) << 16) | (cvtU8(color.w) << 24);
+  }
+}
+
+} // namespace vsr

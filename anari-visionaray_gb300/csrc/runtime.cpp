@@ -1,0 +1,1516 @@
+// Host runtime of the renderer core: the C ABI of include/vsr.h.
+//
+// Object model and parameter handling follow the reference ANARI device
+// (VisionarayDevice.cpp, the per-object commitParameters()/finalize() of
+// camera/, scene/, renderer/, frame/). Differences by design:
+//  * all scene data lives in device memory owned by the objects (the
+//    reference keeps frame buffers in pinned host memory, DeviceArray.h:50);
+//  * one BVH per group over all its triangle surfaces, built on the device at
+//    render time when any object reachable from the world changed;
+//  * kernels take the scene/camera/renderer/frame records by value, with no
+//    per-frame allocations (renderer/Renderer.cpp:19-22 allocates four).
+#include "vsr.h"
+
+#include "kernels.h"
+#include "vsr_device.h"
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <atomic>
+#include <chrono>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <set>
+#include <string>
+#include <vector>
+
+namespace vsr {
+
+struct Object;
+
+// ------------------------------------------------------------------ device
+struct Device {
+  VSRStatusCallback cb = nullptr;
+  const void *cbUser = nullptr;
+  int cudaDevice = 0;
+  cudaStream_t stream = nullptr;
+  uint64_t stamp = 0;
+  std::recursive_mutex mtx;
+  std::set<Object *> live;
+
+  uint64_t nextStamp() { return ++stamp; }
+  void report(Object *src, VSRDataType srcType, VSRSeverity sev, VSRStatus code, const char *fmt,
+              ...) {
+    if (!cb) return;
+    char buf[1024];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    cb(cbUser, (VSRDevice)this, (VSRObject)src, srcType, sev, code, buf);
+  }
+};
+
+struct DevBuf {
+  void *p = nullptr;
+  size_t bytes = 0;
+  DevBuf() = default;
+  DevBuf(const DevBuf &) = delete;
+  DevBuf &operator=(const DevBuf &) = delete;
+  ~DevBuf() { release(); }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    bytes = 0;
+  }
+  cudaError_t alloc(size_t b) {
+    release();
+    bytes = b;
+    if (!b) return cudaSuccess;
+    return cudaMalloc(&p, b);
+  }
+  cudaError_t upload(const void *src, size_t b, cudaStream_t s) {
+    cudaError_t e = alloc(b);
+    if (e != cudaSuccess || !b) return e;
+    return cudaMemcpyAsync(p, src, b, cudaMemcpyHostToDevice, s);
+  }
+  template <class T> T *as() const { return (T *)p; }
+};
+
+static size_t typeSize(VSRDataType t) {
+  switch (t) {
+  case VSR_BOOL: case VSR_INT32: case VSR_UINT32: case VSR_FLOAT32: case VSR_DATA_TYPE: return 4;
+  case VSR_UFIXED8: return 1;
+  case VSR_UFIXED16: return 2;
+  case VSR_INT32_VEC2: case VSR_UINT32_VEC2: case VSR_FLOAT32_VEC2: case VSR_FLOAT32_BOX1: return 8;
+  case VSR_UINT32_VEC3: case VSR_FLOAT32_VEC3: return 12;
+  case VSR_FLOAT32_VEC4: return 16;
+  case VSR_UFIXED8_VEC4: case VSR_UFIXED8_RGBA_SRGB: return 4;
+  case VSR_FLOAT32_MAT4: return 64;
+  case VSR_FLOAT32_MAT3x4: return 48;
+  case VSR_FLOAT64_BOX1: return 16;
+  case VSR_UINT64: case VSR_FLOAT64: return 8;
+  default: return 0;
+  }
+}
+
+static bool isObjectType(VSRDataType t) { return t >= VSR_OBJECT && t <= VSR_WORLD; }
+
+// ------------------------------------------------------------------ objects
+struct Param {
+  VSRDataType type = VSR_UNKNOWN;
+  std::vector<uint8_t> data;
+  Object *obj = nullptr;
+  std::string str;
+};
+
+void retainObj(Object *o);
+void releaseObj(Object *o);
+
+struct Object {
+  Device *dev;
+  VSRDataType kind;
+  std::string subtype;
+  int refs = 1;
+  std::map<std::string, Param> params;
+  uint64_t stamp = 0;  // last commit
+  bool valid = false;
+
+  Object(Device *d, VSRDataType k, std::string st) : dev(d), kind(k), subtype(std::move(st)) {
+    dev->live.insert(this);
+  }
+  virtual ~Object() {
+    for (auto &kv : params)
+      if (kv.second.obj) releaseObj(kv.second.obj);
+    dev->live.erase(this);
+  }
+  // commitParameters + finalize: read committed params into typed state.
+  virtual void commit() { valid = true; }
+  // largest commit stamp of this object and everything it references
+  virtual uint64_t deepStamp() {
+    uint64_t s = stamp;
+    for (auto &kv : params)
+      if (kv.second.obj) s = std::max(s, kv.second.obj->deepStamp());
+    return s;
+  }
+
+  void warn(const char *fmt, const char *a = "", const char *b = "") {
+    dev->report(this, kind, VSR_SEVERITY_WARNING, VSR_ERROR_INVALID_ARGUMENT, fmt, a, b);
+  }
+
+  const Param *find(const char *name) const {
+    auto it = params.find(name);
+    return it == params.end() ? nullptr : &it->second;
+  }
+  bool getf(const char *name, float &out) const {
+    const Param *p = find(name);
+    if (!p) return false;
+    if (p->type == VSR_FLOAT32) { memcpy(&out, p->data.data(), 4); return true; }
+    if (p->type == VSR_FLOAT64) { double d; memcpy(&d, p->data.data(), 8); out = (float)d; return true; }
+    return false;
+  }
+  bool geti(const char *name, int &out) const {
+    const Param *p = find(name);
+    if (!p) return false;
+    if (p->type == VSR_INT32 || p->type == VSR_UINT32) { memcpy(&out, p->data.data(), 4); return true; }
+    if (p->type == VSR_BOOL) { uint32_t b; memcpy(&b, p->data.data(), 4); out = b ? 1 : 0; return true; }
+    return false;
+  }
+  bool getv(const char *name, VSRDataType t, float *out) const {
+    const Param *p = find(name);
+    if (!p || p->type != t) return false;
+    memcpy(out, p->data.data(), typeSize(t));
+    return true;
+  }
+  bool getType(const char *name, VSRDataType &out) const {
+    const Param *p = find(name);
+    if (!p || p->type != VSR_DATA_TYPE) return false;
+    int32_t v;
+    memcpy(&v, p->data.data(), 4);
+    out = (VSRDataType)v;
+    return true;
+  }
+  std::string gets(const char *name, const char *def) const {
+    const Param *p = find(name);
+    return (p && p->type == VSR_STRING) ? p->str : std::string(def);
+  }
+  template <class T> T *geto(const char *name, VSRDataType k) const {
+    const Param *p = find(name);
+    if (!p || !p->obj || p->obj->kind != k) return nullptr;
+    return static_cast<T *>(p->obj);
+  }
+};
+
+void retainObj(Object *o) { o->refs++; }
+void releaseObj(Object *o) {
+  if (--o->refs == 0) delete o;
+}
+
+struct Array : Object {
+  VSRDataType elemType;
+  uint64_t n[3];
+  std::vector<uint8_t> data;
+  std::vector<Object *> objs;
+  Array(Device *d, VSRDataType kind, VSRDataType et, uint64_t n1, uint64_t n2, uint64_t n3)
+      : Object(d, kind, ""), elemType(et) {
+    n[0] = n1; n[1] = n2; n[2] = n3;
+    stamp = d->nextStamp();
+    valid = true;
+  }
+  ~Array() override {
+    for (Object *o : objs)
+      if (o) releaseObj(o);
+  }
+  uint64_t size() const { return n[0] * n[1] * n[2]; }
+  template <class T> const T *as() const { return (const T *)data.data(); }
+  uint64_t deepStamp() override {
+    uint64_t s = stamp;
+    for (Object *o : objs)
+      if (o) s = std::max(s, o->deepStamp());
+    return s;
+  }
+};
+
+// structuredRegular field, scene/volume/spatial_field/StructuredRegularField.cpp:16-93
+struct SpatialField : Object {
+  int dims[3] = {0, 0, 0};
+  float origin[3] = {0, 0, 0}, spacing[3] = {1, 1, 1};
+  DevBuf data;
+  using Object::Object;
+  void commit() override {
+    valid = false;
+    Array *a = geto<Array>("data", VSR_ARRAY3D);
+    getv("origin", VSR_FLOAT32_VEC3, origin);
+    getv("spacing", VSR_FLOAT32_VEC3, spacing);
+    if (!a) {
+      warn("missing required parameter 'data' on 'structuredRegular' field");
+      return;
+    }
+    for (int i = 0; i < 3; ++i) dims[i] = (int)a->n[i];
+    size_t nv = a->size();
+    std::vector<float> host;
+    const float *src = nullptr;
+    if (a->elemType == VSR_FLOAT32) {
+      src = a->as<float>();
+    } else if (a->elemType == VSR_UFIXED8) {
+      host.resize(nv);
+      for (size_t i = 0; i < nv; ++i) host[i] = a->as<uint8_t>()[i] / 255.f;
+      src = host.data();
+    } else if (a->elemType == VSR_UFIXED16) {
+      host.resize(nv);
+      for (size_t i = 0; i < nv; ++i) host[i] = a->as<uint16_t>()[i] / 65535.f;
+      src = host.data();
+    } else {
+      warn("unsupported element type of 'data' on 'structuredRegular' field");
+      return;
+    }
+    if (data.upload(src, nv * sizeof(float), dev->stream) != cudaSuccess) {
+      dev->report(this, kind, VSR_SEVERITY_ERROR, VSR_ERROR_OUT_OF_MEMORY, "field upload failed");
+      return;
+    }
+    cudaStreamSynchronize(dev->stream);
+    valid = dims[0] >= 2 && dims[1] >= 2 && dims[2] >= 2;
+  }
+  void bounds(float lo[3], float hi[3]) const {
+    for (int i = 0; i < 3; ++i) {
+      lo[i] = origin[i];
+      hi[i] = origin[i] + ((float)dims[i] - 1.f) * spacing[i];
+    }
+  }
+};
+
+// transferFunction1D volume, scene/volume/TransferFunction1D.cpp:22-165
+struct Volume : Object {
+  DevBuf tf, majorant;
+  std::vector<float> tfHost;
+  int tfSize = 0;
+  float vr[2] = {0.f, 1.f};
+  float unitDistance = 1.f;
+  int gdims[3] = {0, 0, 0};
+  int brick = 16;
+  SpatialField *field = nullptr;
+  using Object::Object;
+  void commit() override {
+    valid = false;
+    field = geto<SpatialField>("value", VSR_SPATIAL_FIELD);
+    if (!field) field = geto<SpatialField>("field", VSR_SPATIAL_FIELD);
+    vr[0] = 0.f; vr[1] = 1.f;
+    getv("valueRange", VSR_FLOAT32_BOX1, vr);
+    if (const Param *p = find("valueRange"))
+      if (p->type == VSR_FLOAT64_BOX1) {
+        double d[2];
+        memcpy(d, p->data.data(), 16);
+        vr[0] = (float)d[0]; vr[1] = (float)d[1];
+      }
+    float uniformColor[4] = {1, 1, 1, 1};
+    Array *colorArr = geto<Array>("color", VSR_ARRAY1D);
+    if (!getv("color", VSR_FLOAT32_VEC3, uniformColor)) getv("color", VSR_FLOAT32_VEC4, uniformColor);
+    Array *opacityArr = geto<Array>("opacity", VSR_ARRAY1D);
+    float opacity = 1.f;
+    getf("opacity", opacity);
+    float uniformOpacity = opacity * uniformColor[3];
+    unitDistance = 1.f;
+    getf("unitDistance", unitDistance);
+    int b = 16;
+    if (geti("majorantBrickSize", b) && b > 0) brick = b;
+    if (!field) {
+      warn("no spatial field provided to transferFunction1D volume");
+      return;
+    }
+    if (!field->valid) {
+      warn("invalid spatial field provided to transferFunction1D volume");
+      return;
+    }
+    int nch = 4;
+    if (colorArr && colorArr->elemType == VSR_FLOAT32_VEC3) nch = 3;
+    const float *colorData = colorArr ? colorArr->as<float>() : nullptr;
+    const float *opacityData = opacityArr ? opacityArr->as<float>() : nullptr;
+    size_t numColors = colorArr ? colorArr->size() : 1;
+    size_t numOpac = opacityArr ? opacityArr->size() : 1;
+    size_t n = std::max(numColors, numOpac);
+    tfHost.assign(4 * n, 0.f);
+    auto lerp = [](float a, float b2, float t) { return a * (1.f - t) + b2 * t; };
+    for (size_t i = 0; i < n; ++i) {
+      float colorPos = n > 1 ? (float(i) / (n - 1)) * (numColors - 1) : 0.f;
+      float colorFrac = colorPos - floorf(colorPos);
+      float c0[4] = {uniformColor[0], uniformColor[1], uniformColor[2], uniformOpacity};
+      float c1[4] = {uniformColor[0], uniformColor[1], uniformColor[2], uniformOpacity};
+      if (colorData) {
+        int i0 = (int)floorf(colorPos), i1 = (int)ceilf(colorPos);
+        for (int k = 0; k < nch; ++k) {
+          c0[k] = colorData[nch * i0 + k];
+          c1[k] = colorData[nch * i1 + k];
+        }
+      }
+      float c[4];
+      for (int k = 0; k < 4; ++k) c[k] = lerp(c0[k], c1[k], colorFrac);
+      if (opacityData) {
+        float ap = n > 1 ? (float(i) / (n - 1)) * (numOpac - 1) : 0.f;
+        float af = ap - floorf(ap);
+        float a0 = opacityData[(int)floorf(ap)], a1 = opacityData[(int)ceilf(ap)];
+        c[3] *= lerp(a0, a1, af);
+      }
+      for (int k = 0; k < 4; ++k) tfHost[4 * i + k] = c[k];
+    }
+    tfSize = (int)n;
+    if (unitDistance == 0.f) unitDistance = 1.f;
+    if (tf.upload(tfHost.data(), tfHost.size() * sizeof(float), dev->stream) != cudaSuccess) return;
+    for (int a = 0; a < 3; ++a) gdims[a] = (field->dims[a] + brick - 1) / brick;
+    size_t nc = (size_t)gdims[0] * gdims[1] * gdims[2];
+    if (majorant.alloc(nc * sizeof(float)) != cudaSuccess) return;
+    if (launchBrickMajorants(field->data.as<float>(), field->dims, brick, tf.as<float4>(), tfSize,
+                             vr[0], vr[1], majorant.as<float>(), gdims, dev->stream) != cudaSuccess)
+      return;
+    cudaStreamSynchronize(dev->stream);
+    valid = true;
+  }
+  DVolume record() const {
+    DVolume v{};
+    v.data = field->data.as<float>();
+    v.tf = tf.as<float4>();
+    v.majorant = majorant.as<float>();
+    for (int a = 0; a < 3; ++a) {
+      v.dims[a] = field->dims[a];
+      v.gdims[a] = gdims[a];
+    }
+    v.tfSize = tfSize;
+    v.unitDistance = unitDistance;
+    field->bounds(v.boundsLo, v.boundsHi);
+    float minSp = field->spacing[0];
+    for (int a = 0; a < 3; ++a) {
+      v.S[a] = 1.f / (v.boundsHi[a] - v.boundsLo[a]);
+      v.T[a] = -v.boundsLo[a];
+      minSp = std::min(minSp, field->spacing[a]);
+    }
+    v.cellSize = minSp;
+    v.vrMin = vr[0];
+    v.vrMax = vr[1];
+    return v;
+  }
+};
+
+// triangle geometry, scene/surface/geometry/Triangle.cpp:46-133
+struct Geometry : Object {
+  std::vector<float> v1, e1, e2;  // per triangle, float3 packed
+  using Object::Object;
+  void commit() override {
+    valid = false;
+    v1.clear(); e1.clear(); e2.clear();
+    Array *pos = geto<Array>("vertex.position", VSR_ARRAY1D);
+    Array *idx = geto<Array>("primitive.index", VSR_ARRAY1D);
+    if (!pos || pos->elemType != VSR_FLOAT32_VEC3) {
+      warn("missing required parameter 'vertex.position' on triangle geometry");
+      return;
+    }
+    const float *P = pos->as<float>();
+    size_t nv = pos->size();
+    auto add = [&](size_t a, size_t b, size_t c) {
+      for (int k = 0; k < 3; ++k) {
+        float p1 = P[3 * a + k], p2 = P[3 * b + k], p3 = P[3 * c + k];
+        v1.push_back(p1);
+        e1.push_back(p2 - p1);
+        e2.push_back(p3 - p1);
+      }
+    };
+    if (idx) {
+      if (idx->elemType != VSR_UINT32_VEC3) {
+        warn("unsupported type for 'primitive.index' on triangle geometry");
+        return;
+      }
+      const uint32_t *I = idx->as<uint32_t>();
+      for (size_t i = 0; i < idx->size(); ++i) {
+        if (I[3 * i] >= nv || I[3 * i + 1] >= nv || I[3 * i + 2] >= nv) {
+          warn("'primitive.index' out of range on triangle geometry");
+          return;
+        }
+        add(I[3 * i], I[3 * i + 1], I[3 * i + 2]);
+      }
+    } else {
+      for (size_t i = 0; i + 2 < nv; i += 3) add(i, i + 1, i + 2);
+    }
+    if (find("vertex.normal"))
+      dev->report(this, kind, VSR_SEVERITY_WARNING, VSR_OK,
+                  "'vertex.normal' is not used: shading uses the geometric normal");
+    valid = true;
+  }
+  size_t numTris() const { return v1.size() / 3; }
+};
+
+// matte / physicallyBased, scene/surface/material/{Matte,PBM}.cpp
+struct Material : Object {
+  DMaterial m{};
+  using Object::Object;
+  void commit() override {
+    m = DMaterial{};
+    float c4[4] = {1, 1, 1, 1};
+    m.opacity = 1.f;
+    getf("opacity", m.opacity);
+    std::string am = gets("alphaMode", "opaque");
+    m.alphaMode = am == "blend" ? ALPHA_BLEND : (am == "mask" ? ALPHA_MASK : ALPHA_OPAQUE);
+    m.alphaCutoff = 0.5f;
+    getf("alphaCutoff", m.alphaCutoff);
+    if (subtype == "matte") {
+      m.type = MAT_MATTE;
+      if (!getv("color", VSR_FLOAT32_VEC3, c4)) getv("color", VSR_FLOAT32_VEC4, c4);
+    } else {
+      m.type = MAT_PBR;
+      if (!getv("baseColor", VSR_FLOAT32_VEC3, c4)) getv("baseColor", VSR_FLOAT32_VEC4, c4);
+      m.metallic = 1.f; getf("metallic", m.metallic);
+      m.roughness = 1.f; getf("roughness", m.roughness);
+      m.ior = 1.5f; getf("ior", m.ior);
+      m.clearcoat = 0.f; getf("clearcoat", m.clearcoat);
+      m.clearcoatRoughness = 0.f; getf("clearcoatRoughness", m.clearcoatRoughness);
+      m.transmission = 0.f; getf("transmission", m.transmission);
+      float sc[3] = {0, 0, 0};
+      getv("sheenColor", VSR_FLOAT32_VEC3, sc);
+      for (int k = 0; k < 3; ++k) m.sheenColor[k] = sc[k];
+      m.sheenRoughness = 0.f; getf("sheenRoughness", m.sheenRoughness);
+    }
+    for (int k = 0; k < 3; ++k) m.baseColor[k] = c4[k];
+    valid = true;
+  }
+};
+
+// directional light, scene/light/Directional.cpp:17-40 and Light.cpp:27-28
+struct Light : Object {
+  float direction[3] = {0, 0, -1}, color[3] = {1, 1, 1};
+  float irradiance = 1.f, angularDiameter = 0.f;
+  int visible = 1;
+  using Object::Object;
+  void commit() override {
+    direction[0] = 0; direction[1] = 0; direction[2] = -1;
+    getv("direction", VSR_FLOAT32_VEC3, direction);
+    float l = std::sqrt(direction[0] * direction[0] + direction[1] * direction[1] + direction[2] * direction[2]);
+    for (float &d : direction) d /= l;
+    color[0] = color[1] = color[2] = 1.f;
+    getv("color", VSR_FLOAT32_VEC3, color);
+    irradiance = 1.f; getf("irradiance", irradiance);
+    irradiance = std::max(irradiance, 0.f);
+    angularDiameter = 0.f; getf("angularDiameter", angularDiameter);
+    angularDiameter = std::max(angularDiameter, 0.f);
+    visible = 1; geti("visible", visible);
+    valid = true;
+  }
+};
+
+struct Surface : Object {
+  Geometry *geom = nullptr;
+  Material *mat = nullptr;
+  using Object::Object;
+  void commit() override {
+    geom = geto<Geometry>("geometry", VSR_GEOMETRY);
+    mat = geto<Material>("material", VSR_MATERIAL);
+    valid = geom && mat;
+    if (!valid) warn("surface requires 'geometry' and 'material'");
+  }
+};
+
+template <class T> static std::vector<T *> objectList(Array *a, VSRDataType k) {
+  std::vector<T *> out;
+  if (!a) return out;
+  for (Object *o : a->objs)
+    if (o && o->kind == k) out.push_back(static_cast<T *>(o));
+  return out;
+}
+
+struct Group : Object {
+  std::vector<Surface *> surfaces;
+  std::vector<Volume *> volumes;
+  std::vector<Light *> lights;
+  using Object::Object;
+  void commit() override {
+    surfaces = objectList<Surface>(geto<Array>("surface", VSR_ARRAY1D), VSR_SURFACE);
+    volumes = objectList<Volume>(geto<Array>("volume", VSR_ARRAY1D), VSR_VOLUME);
+    lights = objectList<Light>(geto<Array>("light", VSR_ARRAY1D), VSR_LIGHT);
+    valid = true;
+  }
+};
+
+struct Instance : Object {
+  Group *group = nullptr;
+  float xfm[12] = {1, 0, 0, 0, 1, 0, 0, 0, 1, 0, 0, 0};
+  uint32_t userID = ~0u;
+  using Object::Object;
+  void commit() override {
+    group = geto<Group>("group", VSR_GROUP);
+    float m4[16];
+    float i12[12] = {1, 0, 0, 0, 1, 0, 0, 0, 1, 0, 0, 0};
+    memcpy(xfm, i12, sizeof(xfm));
+    if (getv("transform", VSR_FLOAT32_MAT4, m4)) {
+      for (int c = 0; c < 4; ++c)
+        for (int r = 0; r < 3; ++r) xfm[3 * c + r] = m4[4 * c + r];
+    } else {
+      getv("transform", VSR_FLOAT32_MAT3x4, xfm);
+    }
+    int id;
+    if (geti("id", id)) userID = (uint32_t)id;
+    valid = group != nullptr;
+    if (!valid) warn("instance requires 'group'");
+  }
+};
+
+struct Camera : Object {
+  DCamera c{};
+  using Object::Object;
+  static void normalize3(float *v) {
+    float l = std::sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
+    for (int i = 0; i < 3; ++i) v[i] /= l;
+  }
+  static void cross3(const float *a, const float *b, float *o) {
+    o[0] = a[1] * b[2] - a[2] * b[1];
+    o[1] = a[2] * b[0] - a[0] * b[2];
+    o[2] = a[0] * b[1] - a[1] * b[0];
+  }
+  static bool inv44(const float *m, float *out) {
+    double a[4][8];
+    for (int r = 0; r < 4; ++r)
+      for (int k = 0; k < 4; ++k) {
+        a[r][k] = m[k * 4 + r];
+        a[r][k + 4] = r == k ? 1.0 : 0.0;
+      }
+    for (int k = 0; k < 4; ++k) {
+      int p = k;
+      for (int r = k + 1; r < 4; ++r)
+        if (std::fabs(a[r][k]) > std::fabs(a[p][k])) p = r;
+      if (a[p][k] == 0.0) return false;
+      if (p != k)
+        for (int j = 0; j < 8; ++j) std::swap(a[p][j], a[k][j]);
+      double d = a[k][k];
+      for (int j = 0; j < 8; ++j) a[k][j] /= d;
+      for (int r = 0; r < 4; ++r)
+        if (r != k) {
+          double f = a[r][k];
+          for (int j = 0; j < 8; ++j) a[r][j] -= f * a[k][j];
+        }
+    }
+    for (int r = 0; r < 4; ++r)
+      for (int k = 0; k < 4; ++k) out[k * 4 + r] = (float)a[r][k + 4];
+    return true;
+  }
+  // Camera::commitParameters camera/Camera.cpp:30-36; Perspective.cpp:13-44;
+  // Matrix.cpp:13-27; DCO ortho/omni init DeviceCopyableObjects.h:2506-2575.
+  void commit() override {
+    c = DCamera{};
+    float pos[3] = {0, 0, 0}, dir[3] = {0, 0, 1}, up[3] = {0, 1, 0};
+    getv("position", VSR_FLOAT32_VEC3, pos);
+    getv("direction", VSR_FLOAT32_VEC3, dir);
+    getv("up", VSR_FLOAT32_VEC3, up);
+    normalize3(dir);
+    normalize3(up);
+    float region[4] = {0, 0, 1, 1};
+    float r4[4];
+    if (getv("imageRegion", VSR_FLOAT32_VEC4, r4)) memcpy(region, r4, sizeof(region));
+    float shutter[2] = {0.5f, 0.5f};
+    getv("shutter", VSR_FLOAT32_BOX1, shutter);
+    memcpy(c.eye, pos, sizeof(pos));
+    memcpy(c.dir, dir, sizeof(dir));
+    memcpy(c.region, region, sizeof(region));
+    memcpy(c.shutter, shutter, sizeof(shutter));
+    float aspect = 1.f;
+    getf("aspect", aspect);
+    valid = true;
+    if (subtype == "perspective") {
+      c.type = CAM_PERSPECTIVE;
+      float fovy = 60.f * 3.14159265358979f / 180.f;
+      getf("fovy", fovy);
+      c.lensRadius = 0.f; getf("apertureRadius", c.lensRadius);
+      c.focusDistance = 1.f; getf("focusDistance", c.focusDistance);
+      float th = std::tan(0.5f * fovy);
+      float U[3], V[3];
+      cross3(dir, up, U);
+      normalize3(U);
+      for (float &u : U) u *= th * aspect;
+      cross3(U, dir, V);
+      normalize3(V);
+      for (float &v : V) v *= th;
+      memcpy(c.U, U, sizeof(U));
+      memcpy(c.V, V, sizeof(V));
+      memcpy(c.W, dir, sizeof(dir));
+    } else if (subtype == "orthographic" || subtype == "omnidirectional") {
+      bool ortho = subtype == "orthographic";
+      c.type = ortho ? CAM_ORTHO : CAM_OMNI;
+      float height = 1.f;
+      getf("height", height);
+      float U[3], V[3], W[3];
+      cross3(dir, up, U);
+      normalize3(U);
+      if (ortho) for (float &u : U) u *= height * aspect;
+      cross3(U, dir, V);
+      normalize3(V);
+      if (ortho) for (float &v : V) v *= height;
+      for (int i = 0; i < 3; ++i) W[i] = pos[i] - 0.5f * U[i] - 0.5f * V[i];
+      memcpy(c.U, U, sizeof(U));
+      memcpy(c.V, V, sizeof(V));
+      memcpy(c.W, W, sizeof(W));
+    } else if (subtype == "matrix") {
+      c.type = CAM_MATRIX;
+      float proj[16] = {1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1};
+      float view[16] = {1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1};
+      getv("proj", VSR_FLOAT32_MAT4, proj);
+      getv("view", VSR_FLOAT32_MAT4, view);
+      float pv[16];
+      for (int col = 0; col < 4; ++col)
+        for (int row = 0; row < 4; ++row) {
+          float s = 0.f;
+          for (int k = 0; k < 4; ++k) s += proj[k * 4 + row] * view[col * 4 + k];
+          pv[col * 4 + row] = s;
+        }
+      if (!inv44(pv, c.inv)) {
+        warn("singular proj*view on matrix camera");
+        valid = false;
+      }
+    }
+  }
+};
+
+struct Renderer : Object {
+  DRenderer r{};
+  int sampleLimit = 1024;
+  using Object::Object;
+  // Renderer.cpp:34-45, Raycast.cpp:16-20, Pathtrace.cpp:16-28
+  void commit() override {
+    r = DRenderer{};
+    r.type = subtype == "raycast" ? REND_RAYCAST : REND_PATHTRACE;
+    float bg[4] = {0, 0, 0, 1};
+    getv("background", VSR_FLOAT32_VEC4, bg);
+    memcpy(r.bg, bg, sizeof(bg));
+    float ac[3] = {1, 1, 1};
+    getv("ambientColor", VSR_FLOAT32_VEC3, ac);
+    float ar = 0.2f;
+    getf("ambientRadiance", ar);
+    for (int k = 0; k < 3; ++k) r.ambient[k] = ac[k] * ar;
+    std::string mode = gets("mode", "default");
+    if (mode != "default")
+      dev->report(this, kind, VSR_SEVERITY_WARNING, VSR_ERROR_INVALID_ARGUMENT,
+                  "render mode '%s' is not supported; using 'default'", mode.c_str());
+    int b = 0;
+    if (geti("gradientShading", b) && b)
+      dev->report(this, kind, VSR_SEVERITY_WARNING, VSR_ERROR_INVALID_ARGUMENT,
+                  "'gradientShading' is not supported");
+    if (geti("taa", b) && b)
+      dev->report(this, kind, VSR_SEVERITY_WARNING, VSR_ERROR_INVALID_ARGUMENT, "'taa' is not supported");
+    int v;
+    r.maxBounce = 7;
+    if (geti("maxBounce", v)) r.maxBounce = std::min(std::max(v, 0), 256);
+    r.occlusionDistance = 1e20f;
+    getf("ambientOcclusionDistance", r.occlusionDistance);
+    r.ambientSamples = 1;
+    if (geti("ambientSamples", v)) r.ambientSamples = std::min(std::max(v, 0), 256);
+    r.pixelSamples = 1;
+    if (r.type == REND_PATHTRACE && geti("pixelSamples", v)) r.pixelSamples = std::min(std::max(v, 1), 256);
+    sampleLimit = 1024;
+    if (geti("sampleLimit", v)) sampleLimit = std::max(v, 1);
+    float vsr = 0.5f;
+    getf("volumeSamplingRate", vsr);
+    r.samplingRateInv = vsr > 0.f ? 1.f / vsr : 0.f;
+    r.numClipPlanes = 0;
+    if (Array *cp = geto<Array>("clipPlane", VSR_ARRAY1D)) {
+      if (cp->elemType != VSR_FLOAT32_VEC4) {
+        warn("'clipPlane' must be an array of FLOAT32_VEC4");
+      } else {
+        size_t n = std::min<size_t>(cp->size(), kMaxClipPlanes);
+        if (cp->size() > kMaxClipPlanes) warn("more than 8 clip planes; extra planes ignored");
+        for (size_t i = 0; i < n; ++i)
+          for (int k = 0; k < 4; ++k) r.clip[i][k] = cp->as<float>()[4 * i + k];
+        r.numClipPlanes = (int)n;
+      }
+    }
+    valid = true;
+  }
+};
+
+// ----------------------------------------------------------------- world
+struct GroupGPU {
+  DevBuf v1, e1, e2, nodes, tris, triSurface, triPrim;
+  int numTris = 0, numNodes = 0;
+  float buildMs = 0.f;
+};
+
+struct World : Object {
+  Group implicitGroup;
+  bool implicitUsed = false;
+  std::vector<Instance *> instances;
+  // device scene
+  uint64_t builtStamp = 0;
+  std::vector<std::unique_ptr<GroupGPU>> groupsGPU;
+  DevBuf dInstances, dGroups, dMaterials, dLights, dVolumes, dGroupVolumes;
+  DScene scene{};
+  std::vector<DVolume> volsHost;
+  float commitMs = 0.f;
+  uint64_t bvhNodes = 0, bvhTris = 0;
+
+  World(Device *d, VSRDataType k, std::string st)
+      : Object(d, k, st), implicitGroup(d, VSR_GROUP, "") {
+    d->live.erase(&implicitGroup);
+  }
+  void commit() override {
+    instances = objectList<Instance>(geto<Array>("instance", VSR_ARRAY1D), VSR_INSTANCE);
+    // world-level surfaces/volumes/lights go into a group with an identity
+    // instance, as the reference's World does (scene/World.cpp).
+    for (auto &kv : implicitGroup.params)
+      if (kv.second.obj) releaseObj(kv.second.obj);
+    implicitGroup.params.clear();
+    const char *names[3] = {"surface", "volume", "light"};
+    for (const char *n : names) {
+      const Param *p = find(n);
+      if (p && p->obj) {
+        Param q = *p;
+        retainObj(q.obj);
+        implicitGroup.params[n] = q;
+      }
+    }
+    implicitGroup.commit();
+    implicitUsed = !implicitGroup.surfaces.empty() || !implicitGroup.volumes.empty() ||
+                   !implicitGroup.lights.empty();
+    valid = true;
+  }
+
+  bool buildScene(uint64_t deep) {
+    auto t0 = std::chrono::steady_clock::now();
+    cudaStream_t s = dev->stream;
+    struct InstRec { Group *g; float xfm[12]; uint32_t userID; };
+    std::vector<InstRec> insts;
+    if (implicitUsed) insts.push_back({&implicitGroup, {1, 0, 0, 0, 1, 0, 0, 0, 1, 0, 0, 0}, ~0u});
+    for (Instance *I : instances) {
+      if (!I->valid || !I->group) continue;
+      InstRec r;
+      r.g = I->group;
+      memcpy(r.xfm, I->xfm, sizeof(r.xfm));
+      r.userID = I->userID;
+      insts.push_back(r);
+    }
+    std::vector<Group *> groups;
+    std::map<Group *, int> gidx;
+    for (auto &r : insts)
+      if (!gidx.count(r.g)) { gidx[r.g] = (int)groups.size(); groups.push_back(r.g); }
+
+    std::vector<DMaterial> mats;
+    std::vector<DGroup> dgroups(groups.size());
+    std::vector<DVolume> vols;
+    std::vector<int> groupVols;
+    std::map<Volume *, int> vidx;
+    groupsGPU.clear();
+    bvhNodes = bvhTris = 0;
+    bool allOpaque = true, anySurf = false;
+    for (size_t gi = 0; gi < groups.size(); ++gi) {
+      Group *g = groups[gi];
+      auto gg = std::make_unique<GroupGPU>();
+      std::vector<float> v1, e1, e2;
+      std::vector<uint32_t> triSurf, triPrim;
+      float lo[3] = {1e30f, 1e30f, 1e30f}, hi[3] = {-1e30f, -1e30f, -1e30f};
+      for (Surface *sf : g->surfaces) {
+        if (!sf->valid || !sf->geom->valid || !sf->mat->valid) continue;
+        uint32_t sid = (uint32_t)mats.size();
+        mats.push_back(sf->mat->m);
+        if (sf->mat->m.alphaMode != ALPHA_OPAQUE) allOpaque = false;
+        Geometry *G = sf->geom;
+        size_t nt = G->numTris();
+        v1.insert(v1.end(), G->v1.begin(), G->v1.end());
+        e1.insert(e1.end(), G->e1.begin(), G->e1.end());
+        e2.insert(e2.end(), G->e2.begin(), G->e2.end());
+        for (size_t t = 0; t < nt; ++t) {
+          triSurf.push_back(sid);
+          triPrim.push_back((uint32_t)t);
+        }
+        for (size_t i = 0; i < G->v1.size(); ++i) {
+          int a = (int)(i % 3);
+          float p = G->v1[i];
+          lo[a] = std::min(lo[a], std::min(p, std::min(p + G->e1[i], p + G->e2[i])));
+          hi[a] = std::max(hi[a], std::max(p, std::max(p + G->e1[i], p + G->e2[i])));
+        }
+      }
+      int nt = (int)triSurf.size();
+      if (nt >= (1 << 27)) {
+        dev->report(this, kind, VSR_SEVERITY_ERROR, VSR_ERROR_INVALID_ARGUMENT,
+                    "group has more than 2^27 triangles");
+        return false;
+      }
+      DGroup dg{};
+      dg.volBegin = (int)groupVols.size();
+      for (Volume *v : g->volumes) {
+        if (!v->valid) continue;
+        if (!vidx.count(v)) { vidx[v] = (int)vols.size(); vols.push_back(v->record()); }
+        groupVols.push_back(vidx[v]);
+      }
+      dg.volEnd = (int)groupVols.size();
+      if (nt > 0) {
+        anySurf = true;
+        size_t fb = (size_t)nt * 3 * sizeof(float);
+        if (gg->v1.upload(v1.data(), fb, s) || gg->e1.upload(e1.data(), fb, s) ||
+            gg->e2.upload(e2.data(), fb, s) ||
+            gg->triSurface.upload(triSurf.data(), nt * sizeof(uint32_t), s) ||
+            gg->triPrim.upload(triPrim.data(), nt * sizeof(uint32_t), s) ||
+            gg->nodes.alloc((size_t)std::max(nt - 1, 1) * 4 * sizeof(float4)) ||
+            gg->tris.alloc((size_t)nt * 3 * sizeof(float4))) {
+          dev->report(this, kind, VSR_SEVERITY_ERROR, VSR_ERROR_OUT_OF_MEMORY, "scene upload failed");
+          return false;
+        }
+        BvhBuildStats st{};
+        cudaError_t e = buildGroupBVH(gg->v1.as<float>(), gg->e1.as<float>(), gg->e2.as<float>(), nt,
+                                      gg->nodes.as<float4>(), gg->tris.as<float4>(), &st, s);
+        if (e != cudaSuccess) {
+          dev->report(this, kind, VSR_SEVERITY_ERROR, VSR_ERROR_CUDA, "BVH build failed: %s",
+                      cudaGetErrorString(e));
+          return false;
+        }
+        gg->numTris = nt;
+        gg->numNodes = st.numNodes;
+        gg->buildMs = st.buildMs;
+        // the build inputs are not needed once the leaf-ordered copy exists
+        gg->v1.release();
+        gg->e1.release();
+        gg->e2.release();
+        bvhNodes += (uint64_t)st.numNodes;
+        bvhTris += (uint64_t)nt;
+      }
+      dg.nodes = gg->nodes.as<float4>();
+      dg.tris = gg->tris.as<float4>();
+      dg.triSurface = gg->triSurface.as<uint32_t>();
+      dg.triPrim = gg->triPrim.as<uint32_t>();
+      dg.numTris = nt;
+      dg.numNodes = gg->numNodes;
+      for (int a = 0; a < 3; ++a) { dg.boundsLo[a] = lo[a]; dg.boundsHi[a] = hi[a]; }
+      dgroups[gi] = dg;
+      groupsGPU.push_back(std::move(gg));
+    }
+    std::vector<DInstance> dinst;
+    std::vector<DLight> lights;
+    for (auto &r : insts) {
+      DInstance di{};
+      // affineInv = inverse(top_left), transInv = -translation,
+      // normalXfm = transpose(affineInv)  (scene/Instance.cpp:92-98)
+      const float *m = r.xfm;
+      double a[9];
+      for (int i = 0; i < 9; ++i) a[i] = m[i];
+      double c00 = a[4] * a[8] - a[7] * a[5], c01 = a[7] * a[2] - a[1] * a[8], c02 = a[1] * a[5] - a[4] * a[2];
+      double det = a[0] * c00 + a[3] * c01 + a[6] * c02;
+      if (det == 0.0) {
+        dev->report(this, kind, VSR_SEVERITY_WARNING, VSR_ERROR_INVALID_ARGUMENT,
+                    "singular instance transform; instance skipped");
+        continue;
+      }
+      // inverse of column-major 3x3 via cofactors (column-major output)
+      float inv[9];
+      inv[0] = (float)(c00 / det);
+      inv[1] = (float)(c01 / det);
+      inv[2] = (float)(c02 / det);
+      inv[3] = (float)((a[6] * a[5] - a[3] * a[8]) / det);
+      inv[4] = (float)((a[0] * a[8] - a[6] * a[2]) / det);
+      inv[5] = (float)((a[3] * a[2] - a[0] * a[5]) / det);
+      inv[6] = (float)((a[3] * a[7] - a[6] * a[4]) / det);
+      inv[7] = (float)((a[6] * a[1] - a[0] * a[7]) / det);
+      inv[8] = (float)((a[0] * a[4] - a[3] * a[1]) / det);
+      memcpy(di.affineInv, inv, sizeof(inv));
+      for (int k = 0; k < 3; ++k) di.transInv[k] = -m[9 + k];
+      for (int c = 0; c < 3; ++c)
+        for (int rr = 0; rr < 3; ++rr) di.normalXfm[3 * c + rr] = inv[3 * rr + c];
+      di.group = gidx[r.g];
+      di.userID = r.userID;
+      dinst.push_back(di);
+      for (Light *L : r.g->lights) {
+        if (!L->valid) continue;
+        DLight dl{};
+        // direction transformed by the instance's linear part
+        float d[3];
+        for (int k = 0; k < 3; ++k)
+          d[k] = m[k] * L->direction[0] + m[3 + k] * L->direction[1] + m[6 + k] * L->direction[2];
+        float l = std::sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
+        for (int k = 0; k < 3; ++k) {
+          dl.dir[k] = -d[k] / l;
+          dl.intensity[k] = L->color[k] * L->irradiance;
+        }
+        dl.cosHalfAngle = L->angularDiameter > 0.f ? std::cos(0.5f * L->angularDiameter) : 1.f;
+        dl.type = 0;
+        dl.visible = L->visible;
+        lights.push_back(dl);
+      }
+    }
+    if (dInstances.upload(dinst.data(), dinst.size() * sizeof(DInstance), s) ||
+        dGroups.upload(dgroups.data(), dgroups.size() * sizeof(DGroup), s) ||
+        dMaterials.upload(mats.data(), mats.size() * sizeof(DMaterial), s) ||
+        dLights.upload(lights.data(), lights.size() * sizeof(DLight), s) ||
+        dVolumes.upload(vols.data(), vols.size() * sizeof(DVolume), s) ||
+        dGroupVolumes.upload(groupVols.data(), groupVols.size() * sizeof(int), s)) {
+      dev->report(this, kind, VSR_SEVERITY_ERROR, VSR_ERROR_OUT_OF_MEMORY, "scene upload failed");
+      return false;
+    }
+    cudaStreamSynchronize(s);
+    volsHost = vols;
+    scene = DScene{};
+    scene.instances = dInstances.as<DInstance>();
+    scene.groups = dGroups.as<DGroup>();
+    scene.materials = dMaterials.as<DMaterial>();
+    scene.lights = dLights.as<DLight>();
+    scene.volumes = dVolumes.as<DVolume>();
+    scene.groupVolumes = dGroupVolumes.as<int>();
+    scene.numInstances = (int)dinst.size();
+    scene.numGroups = (int)dgroups.size();
+    scene.numLights = (int)lights.size();
+    scene.numVolumes = (int)vols.size();
+    scene.allOpaque = allOpaque ? 1 : 0;
+    scene.hasSurfaces = anySurf ? 1 : 0;
+    builtStamp = deep;
+    commitMs = std::chrono::duration<float, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    return true;
+  }
+
+  uint64_t deepStamp() override {
+    uint64_t s = Object::deepStamp();
+    return s;
+  }
+};
+
+struct FrameObj : Object {
+  Renderer *renderer = nullptr;
+  Camera *camera = nullptr;
+  World *world = nullptr;
+  int width = 10, height = 10;
+  VSRDataType colorType = VSR_UNKNOWN, depthType = VSR_UNKNOWN, normalType = VSR_UNKNOWN,
+              albedoType = VSR_UNKNOWN;
+  DevBuf color, depth, normal, albedo, accum, errFlags;
+  std::map<std::string, void *> pinned;
+  uint32_t *errHost = nullptr;
+  cudaEvent_t evStart = nullptr, evRender = nullptr, evStop = nullptr;
+  int accumID = 0;
+  uint64_t lastStamp = 0;
+  bool rendered = false;
+  bool nextReset = true;
+  bool countStats = false;
+  DevBuf counters;
+  unsigned long long countersHost[8] = {0};
+
+  FrameObj(Device *d, VSRDataType k, std::string st) : Object(d, k, st) {
+    cudaEventCreate(&evStart);
+    cudaEventCreate(&evRender);
+    cudaEventCreate(&evStop);
+    cudaMallocHost((void **)&errHost, sizeof(uint32_t));
+    *errHost = 0;
+  }
+  ~FrameObj() override {
+    if (evStart) cudaEventSynchronize(evStop);
+    for (auto &kv : pinned) cudaFreeHost(kv.second);
+    if (errHost) cudaFreeHost(errHost);
+    cudaEventDestroy(evStart);
+    cudaEventDestroy(evRender);
+    cudaEventDestroy(evStop);
+  }
+  // frame/Frame.cpp:75-160
+  void commit() override {
+    renderer = geto<Renderer>("renderer", VSR_RENDERER);
+    camera = geto<Camera>("camera", VSR_CAMERA);
+    world = geto<World>("world", VSR_WORLD);
+    uint32_t sz[2] = {10, 10};
+    if (const Param *p = find("size"))
+      if (p->type == VSR_UINT32_VEC2 || p->type == VSR_INT32_VEC2) memcpy(sz, p->data.data(), 8);
+    colorType = depthType = normalType = albedoType = VSR_UNKNOWN;
+    getType("channel.color", colorType);
+    getType("channel.depth", depthType);
+    getType("channel.normal", normalType);
+    getType("channel.albedo", albedoType);
+    int cs = 0;
+    countStats = geti("collectStatistics", cs) && cs;
+    if (!renderer) warn("missing required parameter 'renderer' on frame");
+    if (!camera) warn("missing required parameter 'camera' on frame");
+    if (!world) warn("missing required parameter 'world' on frame");
+    if (colorType != VSR_UNKNOWN && colorType != VSR_FLOAT32_VEC4 && colorType != VSR_UFIXED8_VEC4 &&
+        colorType != VSR_UFIXED8_RGBA_SRGB) {
+      warn("unsupported 'channel.color' type");
+      colorType = VSR_UNKNOWN;
+    }
+    cudaEventSynchronize(evStop);
+    width = (int)sz[0];
+    height = (int)sz[1];
+    size_t np = (size_t)width * height;
+    {
+      bool ok = accum.alloc(np * sizeof(float4)) == cudaSuccess &&
+                depth.alloc(np * sizeof(float)) == cudaSuccess &&
+                normal.alloc(np * 3 * sizeof(float)) == cudaSuccess &&
+                albedo.alloc(np * 3 * sizeof(float)) == cudaSuccess &&
+                color.alloc(np * (colorType == VSR_FLOAT32_VEC4 ? 16 : 4)) == cudaSuccess &&
+                errFlags.alloc(sizeof(uint32_t)) == cudaSuccess &&
+                counters.alloc(8 * sizeof(unsigned long long)) == cudaSuccess;
+      for (auto &kv : pinned) cudaFreeHost(kv.second);
+      pinned.clear();
+      if (!ok) {
+        dev->report(this, kind, VSR_SEVERITY_ERROR, VSR_ERROR_OUT_OF_MEMORY,
+                    "frame buffer allocation failed");
+        valid = false;
+        return;
+      }
+      cudaMemset(errFlags.p, 0, sizeof(uint32_t));
+    }
+    nextReset = true;
+    valid = renderer && renderer->valid && camera && camera->valid && world && world->valid;
+  }
+  DFrame record() {
+    DFrame f{};
+    f.width = width;
+    f.height = height;
+    f.accumID = accumID;
+    f.colorType = colorType == VSR_FLOAT32_VEC4 ? COLOR_FLOAT4
+                  : colorType == VSR_UFIXED8_VEC4 ? COLOR_UFIXED8
+                  : colorType == VSR_UFIXED8_RGBA_SRGB ? COLOR_SRGB8 : COLOR_NONE;
+    f.color = color.p;
+    f.depth = depth.as<float>();
+    f.normal = normal.as<float>();
+    f.albedo = albedo.as<float>();
+    f.accum = accum.as<float4>();
+    f.errorFlags = errFlags.as<uint32_t>();
+    f.counters = countStats ? counters.as<unsigned long long>() : nullptr;
+    return f;
+  }
+};
+
+Object *asObj(VSRObject o) { return reinterpret_cast<Object *>(o); }
+Device *asDev(VSRDevice d) { return reinterpret_cast<Device *>(d); }
+
+VSRStatus renderFrame(Device *dev, FrameObj *F) {
+  cudaStream_t s = dev->stream;
+  cudaEventSynchronize(F->evStop);
+  if (!F->valid) {
+    dev->report(F, VSR_FRAME, VSR_SEVERITY_ERROR, VSR_ERROR_INCOMPLETE,
+                "skipping render of incomplete frame object");
+    return VSR_ERROR_INCOMPLETE;
+  }
+  World *W = F->world;
+  uint64_t deep = W->deepStamp();
+  if (deep > W->builtStamp) {
+    if (!W->buildScene(deep)) return VSR_ERROR_CUDA;
+  }
+  // checkAccumulationReset, frame/Frame.cpp:499-513
+  uint64_t stampAll = std::max({deep, F->stamp, F->renderer->deepStamp(), F->camera->stamp});
+  if (stampAll > F->lastStamp) {
+    F->lastStamp = stampAll;
+    F->nextReset = true;
+  }
+  cudaEventRecord(F->evStart, s);
+  if (F->nextReset) {
+    launchFrameReset(F->accum.as<float4>(), F->depth.as<float>(), (size_t)F->width * F->height, s);
+    F->accumID = 0;
+    F->nextReset = false;
+  }
+  cudaMemsetAsync(F->errFlags.p, 0, sizeof(uint32_t), s);
+  if (F->countStats) cudaMemsetAsync(F->counters.p, 0, 8 * sizeof(unsigned long long), s);
+  cudaEventRecord(F->evRender, s);
+  cudaError_t e = cudaSuccess;
+  if (F->accumID < F->renderer->sampleLimit) {
+    DFrame fr = F->record();
+    const DRenderer &R = F->renderer->r;
+    if (R.type == REND_RAYCAST) {
+      // stage the first volume's TF in shared memory when it fits (64 KB)
+      int stage = 0;
+      if (!W->volsHost.empty() && W->volsHost[0].tfSize <= 4096) stage = W->volsHost[0].tfSize;
+      e = launchRaycast(W->scene, F->camera->c, R, fr, stage, F->countStats, s);
+    } else {
+      e = launchPathtrace(W->scene, F->camera->c, R, fr, F->countStats, s);
+    }
+    F->accumID++;
+  }
+  cudaEventRecord(F->evStop, s);
+  cudaMemcpyAsync(F->errHost, F->errFlags.p, sizeof(uint32_t), cudaMemcpyDeviceToHost, s);
+  if (F->countStats)
+    cudaMemcpyAsync(F->countersHost, F->counters.p, 8 * sizeof(unsigned long long),
+                    cudaMemcpyDeviceToHost, s);
+  F->rendered = true;
+  if (e != cudaSuccess) {
+    dev->report(F, VSR_FRAME, VSR_SEVERITY_ERROR, VSR_ERROR_CUDA, "render launch failed: %s",
+                cudaGetErrorString(e));
+    return VSR_ERROR_CUDA;
+  }
+  return VSR_OK;
+}
+
+} // namespace vsr
+
+using namespace vsr;
+
+static VSRArray newArray(VSRDevice dv, VSRDataType kind, const void *mem, VSRDataType type,
+                         uint64_t n1, uint64_t n2, uint64_t n3) {
+  Device *d = asDev(dv);
+  if (!d) return nullptr;
+  std::lock_guard<std::recursive_mutex> lk(d->mtx);
+  size_t es = isObjectType(type) ? sizeof(void *) : typeSize(type);
+  if (es == 0) {
+    d->report(nullptr, kind, VSR_SEVERITY_ERROR, VSR_ERROR_INVALID_ARGUMENT, "unsupported array element type");
+    return nullptr;
+  }
+  auto *a = new Array(d, kind, type, n1, n2, n3);
+  size_t bytes = es * n1 * n2 * n3;
+  a->data.resize(bytes);
+  if (mem) memcpy(a->data.data(), mem, bytes);
+  if (isObjectType(type)) {
+    const VSRObject *h = (const VSRObject *)mem;
+    for (uint64_t i = 0; i < n1 * n2 * n3; ++i) {
+      Object *o = h ? asObj(h[i]) : nullptr;
+      if (o) retainObj(o);
+      a->objs.push_back(o);
+    }
+  }
+  return (VSRArray)a;
+}
+
+template <class T>
+static VSRObject newObj(VSRDevice dv, VSRDataType kind, const char *subtype,
+                        std::initializer_list<const char *> allowed) {
+  Device *d = asDev(dv);
+  if (!d) return nullptr;
+  std::lock_guard<std::recursive_mutex> lk(d->mtx);
+  std::string st = subtype ? subtype : "";
+  if (allowed.size()) {
+    bool ok = false;
+    for (const char *a : allowed) ok |= st == a;
+    if (!ok) {
+      d->report(nullptr, kind, VSR_SEVERITY_ERROR, VSR_ERROR_UNKNOWN_SUBTYPE,
+                "unknown object subtype '%s'", st.c_str());
+      return nullptr;
+    }
+  }
+  if (kind == VSR_RENDERER && st == "default") st = "pathtrace";
+  return (VSRObject) new T(d, kind, st);
+}
+
+static bool checkObj(Device *d, Object *o) {
+  if (!d || !o || !d->live.count(o)) {
+    if (d)
+      d->report(nullptr, VSR_UNKNOWN, VSR_SEVERITY_ERROR, VSR_ERROR_INVALID_OBJECT,
+                "invalid object handle");
+    return false;
+  }
+  return true;
+}
+
+static bool channelBuf(FrameObj *F, const std::string &ch, void *&p, size_t &bytes,
+                       VSRDataType &t) {
+  size_t np = (size_t)F->width * F->height;
+  if (ch == "channel.color" && F->colorType != VSR_UNKNOWN) {
+    p = F->color.p;
+    t = F->colorType;
+    bytes = np * (t == VSR_FLOAT32_VEC4 ? 16 : 4);
+  } else if (ch == "channel.depth" && F->depthType == VSR_FLOAT32) {
+    p = F->depth.p;
+    t = VSR_FLOAT32;
+    bytes = np * 4;
+  } else if (ch == "channel.normal" && F->normalType == VSR_FLOAT32_VEC3) {
+    p = F->normal.p;
+    t = VSR_FLOAT32_VEC3;
+    bytes = np * 12;
+  } else if (ch == "channel.albedo" && F->albedoType == VSR_FLOAT32_VEC3) {
+    p = F->albedo.p;
+    t = VSR_FLOAT32_VEC3;
+    bytes = np * 12;
+  } else {
+    return false;
+  }
+  return true;
+}
+
+// ---------------------------------------------------------------- C ABI
+extern "C" {
+
+VSRDevice vsrNewDevice(const char *subtype, VSRStatusCallback cb, const void *cbUserPtr) {
+  if (subtype && strcmp(subtype, "default") != 0) {
+    if (cb) cb(cbUserPtr, nullptr, nullptr, VSR_UNKNOWN, VSR_SEVERITY_ERROR, VSR_ERROR_UNKNOWN_SUBTYPE,
+               "unknown device subtype");
+    return nullptr;
+  }
+  int count = 0;
+  if (cudaGetDeviceCount(&count) != cudaSuccess || count == 0) {
+    if (cb) cb(cbUserPtr, nullptr, nullptr, VSR_UNKNOWN, VSR_SEVERITY_FATAL_ERROR, VSR_ERROR_CUDA,
+               "no CUDA device available: this renderer core has no CPU fallback");
+    return nullptr;
+  }
+  auto *d = new Device;
+  d->cb = cb;
+  d->cbUser = cbUserPtr;
+  // GPU selection as the reference's VISIONARAY_CUDA_DEVICE
+  // (VisionarayDevice.cpp:373-380); default: the current CUDA device.
+  cudaGetDevice(&d->cudaDevice);
+  if (const char *env = getenv("VISIONARAY_CUDA_DEVICE")) d->cudaDevice = atoi(env);
+  if (cudaSetDevice(d->cudaDevice) != cudaSuccess ||
+      cudaStreamCreateWithFlags(&d->stream, cudaStreamNonBlocking) != cudaSuccess) {
+    if (cb) cb(cbUserPtr, nullptr, nullptr, VSR_UNKNOWN, VSR_SEVERITY_FATAL_ERROR, VSR_ERROR_CUDA,
+               "CUDA device initialisation failed");
+    delete d;
+    return nullptr;
+  }
+  return (VSRDevice)d;
+}
+
+VSRStatus vsrReleaseDevice(VSRDevice dv) {
+  Device *d = asDev(dv);
+  if (!d) return VSR_ERROR_INVALID_ARGUMENT;
+  cudaStreamSynchronize(d->stream);
+  std::vector<Object *> left(d->live.begin(), d->live.end());
+  if (!left.empty())
+    d->report(nullptr, VSR_UNKNOWN, VSR_SEVERITY_WARNING, VSR_OK,
+              "%zu objects still alive at device release", left.size());
+  cudaStreamDestroy(d->stream);
+  delete d;
+  return VSR_OK;
+}
+
+VSRArray vsrNewArray1D(VSRDevice d, const void *m, VSRDataType t, uint64_t n1) {
+  return newArray(d, VSR_ARRAY1D, m, t, n1, 1, 1);
+}
+VSRArray vsrNewArray2D(VSRDevice d, const void *m, VSRDataType t, uint64_t n1, uint64_t n2) {
+  return newArray(d, VSR_ARRAY2D, m, t, n1, n2, 1);
+}
+VSRArray vsrNewArray3D(VSRDevice d, const void *m, VSRDataType t, uint64_t n1, uint64_t n2,
+                       uint64_t n3) {
+  return newArray(d, VSR_ARRAY3D, m, t, n1, n2, n3);
+}
+
+VSRObject vsrNewSpatialField(VSRDevice d, const char *s) {
+  return newObj<SpatialField>(d, VSR_SPATIAL_FIELD, s, {"structuredRegular"});
+}
+VSRObject vsrNewVolume(VSRDevice d, const char *s) {
+  return newObj<Volume>(d, VSR_VOLUME, s, {"transferFunction1D"});
+}
+VSRObject vsrNewGeometry(VSRDevice d, const char *s) {
+  return newObj<Geometry>(d, VSR_GEOMETRY, s, {"triangle"});
+}
+VSRObject vsrNewMaterial(VSRDevice d, const char *s) {
+  return newObj<Material>(d, VSR_MATERIAL, s, {"matte", "physicallyBased"});
+}
+VSRObject vsrNewLight(VSRDevice d, const char *s) {
+  return newObj<Light>(d, VSR_LIGHT, s, {"directional"});
+}
+VSRObject vsrNewSurface(VSRDevice d) { return newObj<Surface>(d, VSR_SURFACE, "", {}); }
+VSRObject vsrNewGroup(VSRDevice d) { return newObj<Group>(d, VSR_GROUP, "", {}); }
+VSRObject vsrNewInstance(VSRDevice d, const char *s) {
+  return newObj<Instance>(d, VSR_INSTANCE, s, {"transform"});
+}
+VSRObject vsrNewWorld(VSRDevice d) { return newObj<World>(d, VSR_WORLD, "", {}); }
+VSRObject vsrNewCamera(VSRDevice d, const char *s) {
+  return newObj<Camera>(d, VSR_CAMERA, s, {"perspective", "matrix", "orthographic", "omnidirectional"});
+}
+VSRObject vsrNewRenderer(VSRDevice d, const char *s) {
+  return newObj<Renderer>(d, VSR_RENDERER, s, {"raycast", "pathtrace", "default"});
+}
+VSRFrame vsrNewFrame(VSRDevice d) { return newObj<FrameObj>(d, VSR_FRAME, "", {}); }
+
+VSRStatus vsrSetParameter(VSRDevice dv, VSRObject ov, const char *name, VSRDataType type,
+                          const void *mem) {
+  Device *d = asDev(dv);
+  if (!d) return VSR_ERROR_INVALID_ARGUMENT;
+  std::lock_guard<std::recursive_mutex> lk(d->mtx);
+  Object *o = asObj(ov);
+  if (!checkObj(d, o)) return VSR_ERROR_INVALID_OBJECT;
+  if (!name || !mem) return VSR_ERROR_INVALID_ARGUMENT;
+  Param p;
+  p.type = type;
+  if (type == VSR_STRING) {
+    p.str = (const char *)mem;
+  } else if (isObjectType(type)) {
+    Object *ref = asObj(*(const VSRObject *)mem);
+    if (ref && !d->live.count(ref)) {
+      d->report(o, o->kind, VSR_SEVERITY_ERROR, VSR_ERROR_INVALID_OBJECT,
+                "parameter '%s' refers to an invalid object", name);
+      return VSR_ERROR_INVALID_OBJECT;
+    }
+    p.obj = ref;
+    if (ref) retainObj(ref);
+  } else {
+    size_t sz = typeSize(type);
+    if (!sz) {
+      d->report(o, o->kind, VSR_SEVERITY_ERROR, VSR_ERROR_INVALID_ARGUMENT,
+                "parameter '%s' has an unsupported type", name);
+      return VSR_ERROR_INVALID_ARGUMENT;
+    }
+    p.data.resize(sz);
+    memcpy(p.data.data(), mem, sz);
+  }
+  auto it = o->params.find(name);
+  if (it != o->params.end() && it->second.obj) releaseObj(it->second.obj);
+  o->params[name] = std::move(p);
+  return VSR_OK;
+}
+
+VSRStatus vsrUnsetParameter(VSRDevice dv, VSRObject ov, const char *name) {
+  Device *d = asDev(dv);
+  if (!d) return VSR_ERROR_INVALID_ARGUMENT;
+  std::lock_guard<std::recursive_mutex> lk(d->mtx);
+  Object *o = asObj(ov);
+  if (!checkObj(d, o)) return VSR_ERROR_INVALID_OBJECT;
+  auto it = o->params.find(name);
+  if (it != o->params.end()) {
+    if (it->second.obj) releaseObj(it->second.obj);
+    o->params.erase(it);
+  }
+  return VSR_OK;
+}
+
+VSRStatus vsrCommitParameters(VSRDevice dv, VSRObject ov) {
+  Device *d = asDev(dv);
+  if (!d) return VSR_ERROR_INVALID_ARGUMENT;
+  std::lock_guard<std::recursive_mutex> lk(d->mtx);
+  Object *o = asObj(ov);
+  if (!checkObj(d, o)) return VSR_ERROR_INVALID_OBJECT;
+  o->commit();
+  o->stamp = d->nextStamp();
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) {
+    d->report(o, o->kind, VSR_SEVERITY_ERROR, VSR_ERROR_CUDA, "CUDA error during commit: %s",
+              cudaGetErrorString(e));
+    return VSR_ERROR_CUDA;
+  }
+  return o->valid ? VSR_OK : VSR_ERROR_INVALID_ARGUMENT;
+}
+
+VSRStatus vsrRelease(VSRDevice dv, VSRObject ov) {
+  Device *d = asDev(dv);
+  if (!d) return VSR_ERROR_INVALID_ARGUMENT;
+  std::lock_guard<std::recursive_mutex> lk(d->mtx);
+  Object *o = asObj(ov);
+  if (!checkObj(d, o)) return VSR_ERROR_INVALID_OBJECT;
+  releaseObj(o);
+  return VSR_OK;
+}
+
+VSRStatus vsrRetain(VSRDevice dv, VSRObject ov) {
+  Device *d = asDev(dv);
+  if (!d) return VSR_ERROR_INVALID_ARGUMENT;
+  std::lock_guard<std::recursive_mutex> lk(d->mtx);
+  Object *o = asObj(ov);
+  if (!checkObj(d, o)) return VSR_ERROR_INVALID_OBJECT;
+  retainObj(o);
+  return VSR_OK;
+}
+
+int vsrGetProperty(VSRDevice dv, VSRObject ov, const char *name, VSRDataType type, void *mem,
+                   uint64_t size, VSRWaitMask mask) {
+  Device *d = asDev(dv);
+  if (!d || !name || !mem) return 0;
+  std::lock_guard<std::recursive_mutex> lk(d->mtx);
+  Object *o = asObj(ov);
+  if (!checkObj(d, o)) return 0;
+  std::string n = name;
+  if (o->kind == VSR_FRAME) {
+    FrameObj *F = static_cast<FrameObj *>(o);
+    if (mask == VSR_WAIT) cudaEventSynchronize(F->evStop);
+    else if (cudaEventQuery(F->evStop) != cudaSuccess) return 0;
+    if ((n == "duration" || n == "duration.render") && type == VSR_FLOAT32 && size >= 4) {
+      if (!F->rendered) return 0;
+      float ms = 0.f;
+      cudaEventElapsedTime(&ms, n == "duration" ? F->evStart : F->evRender, F->evStop);
+      *(float *)mem = ms * 1e-3f;
+      return 1;
+    }
+    if (n == "numSamples" && type == VSR_INT32 && size >= 4) {
+      *(int32_t *)mem = F->accumID;
+      return 1;
+    }
+    if (n == "errorFlags" && type == VSR_UINT32 && size >= 4) {
+      *(uint32_t *)mem = *F->errHost;
+      return 1;
+    }
+    if (n == "commitDuration" && type == VSR_FLOAT32 && size >= 4 && F->world) {
+      *(float *)mem = F->world->commitMs * 1e-3f;
+      return 1;
+    }
+    if (n == "statistics" && type == VSR_UINT64 && size >= 8 * sizeof(uint64_t)) {
+      memcpy(mem, F->countersHost, 8 * sizeof(uint64_t));
+      return 1;
+    }
+  }
+  if (o->kind == VSR_WORLD) {
+    World *W = static_cast<World *>(o);
+    if (n == "bvh.nodes" && type == VSR_UINT64 && size >= 8) { *(uint64_t *)mem = W->bvhNodes; return 1; }
+    if (n == "bvh.triangles" && type == VSR_UINT64 && size >= 8) { *(uint64_t *)mem = W->bvhTris; return 1; }
+    if (n == "bvh.buildDuration" && type == VSR_FLOAT32 && size >= 4) {
+      float ms = 0.f;
+      for (auto &g : W->groupsGPU) ms += g->buildMs;
+      *(float *)mem = ms * 1e-3f;
+      return 1;
+    }
+  }
+  return 0;
+}
+
+VSRStatus vsrRenderFrame(VSRDevice dv, VSRFrame fv) {
+  Device *d = asDev(dv);
+  if (!d) return VSR_ERROR_INVALID_ARGUMENT;
+  std::lock_guard<std::recursive_mutex> lk(d->mtx);
+  Object *o = asObj(fv);
+  if (!checkObj(d, o) || o->kind != VSR_FRAME) return VSR_ERROR_INVALID_OBJECT;
+  return renderFrame(d, static_cast<FrameObj *>(o));
+}
+
+int vsrFrameReady(VSRDevice dv, VSRFrame fv, VSRWaitMask mask) {
+  Device *d = asDev(dv);
+  if (!d) return 0;
+  std::lock_guard<std::recursive_mutex> lk(d->mtx);
+  Object *o = asObj(fv);
+  if (!checkObj(d, o) || o->kind != VSR_FRAME) return 0;
+  FrameObj *F = static_cast<FrameObj *>(o);
+  if (mask == VSR_WAIT) {
+    cudaError_t e = cudaStreamSynchronize(d->stream);
+    if (e != cudaSuccess) {
+      d->report(F, VSR_FRAME, VSR_SEVERITY_ERROR, VSR_ERROR_CUDA, "render failed: %s",
+                cudaGetErrorString(e));
+      return 0;
+    }
+  } else if (cudaEventQuery(F->evStop) != cudaSuccess) {
+    return 0;
+  }
+  if (*F->errHost)
+    d->report(F, VSR_FRAME, VSR_SEVERITY_WARNING, VSR_OK, "device error flags 0x%x in last render",
+              *F->errHost);
+  return 1;
+}
+
+VSRStatus vsrDiscardFrame(VSRDevice dv, VSRFrame fv) {
+  (void)dv;
+  (void)fv;
+  return VSR_OK;
+}
+
+const void *vsrMapFrame(VSRDevice dv, VSRFrame fv, const char *channel, uint32_t *width,
+                        uint32_t *height, VSRDataType *pixelType) {
+  Device *d = asDev(dv);
+  if (!d || !channel) return nullptr;
+  std::lock_guard<std::recursive_mutex> lk(d->mtx);
+  Object *o = asObj(fv);
+  if (!checkObj(d, o) || o->kind != VSR_FRAME) return nullptr;
+  FrameObj *F = static_cast<FrameObj *>(o);
+  void *p;
+  size_t bytes;
+  VSRDataType t;
+  if (!channelBuf(F, channel, p, bytes, t)) {
+    d->report(F, VSR_FRAME, VSR_SEVERITY_WARNING, VSR_ERROR_INVALID_ARGUMENT,
+              "channel '%s' is not enabled on this frame", channel);
+    if (width) *width = 0;
+    if (height) *height = 0;
+    if (pixelType) *pixelType = VSR_UNKNOWN;
+    return nullptr;
+  }
+  void *&host = F->pinned[channel];
+  if (!host && cudaMallocHost(&host, bytes) != cudaSuccess) {
+    host = nullptr;
+    return nullptr;
+  }
+  cudaMemcpyAsync(host, p, bytes, cudaMemcpyDeviceToHost, d->stream);
+  cudaStreamSynchronize(d->stream);
+  if (width) *width = (uint32_t)F->width;
+  if (height) *height = (uint32_t)F->height;
+  if (pixelType) *pixelType = t;
+  return host;
+}
+
+VSRStatus vsrUnmapFrame(VSRDevice dv, VSRFrame fv, const char *channel) {
+  (void)dv;
+  (void)fv;
+  (void)channel;
+  return VSR_OK;
+}
+
+const void *vsrMapFrameDevice(VSRDevice dv, VSRFrame fv, const char *channel, uint32_t *width,
+                              uint32_t *height, VSRDataType *pixelType) {
+  Device *d = asDev(dv);
+  if (!d || !channel) return nullptr;
+  std::lock_guard<std::recursive_mutex> lk(d->mtx);
+  Object *o = asObj(fv);
+  if (!checkObj(d, o) || o->kind != VSR_FRAME) return nullptr;
+  FrameObj *F = static_cast<FrameObj *>(o);
+  void *p;
+  size_t bytes;
+  VSRDataType t;
+  if (!channelBuf(F, channel, p, bytes, t)) return nullptr;
+  if (width) *width = (uint32_t)F->width;
+  if (height) *height = (uint32_t)F->height;
+  if (pixelType) *pixelType = t;
+  return p;
+}
+
+void *vsrDeviceStream(VSRDevice dv) {
+  Device *d = asDev(dv);
+  return d ? (void *)d->stream : nullptr;
+}
+
+} // extern "C"

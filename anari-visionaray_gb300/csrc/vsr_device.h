@@ -1,0 +1,150 @@
+// Device-side scene, camera, renderer and frame records.
+//
+// These are the flat POD records the render kernels read. They are passed
+// to each launch by value (kernel parameters), replacing the reference's
+// per-frame DevicePointer copies of the object registry, renderer state,
+// frame and camera (renderer/Renderer.cpp:19-22, DeviceArray.h:377-394).
+//
+// HBM layout per group (one BVH per group over all its triangle surfaces):
+//   nodes : 4 x float4 per BVH2 node (64 B): child boxes interleaved
+//           (lo0.x,hi0.x,lo0.y,hi0.y) (lo1.x,hi1.x,lo1.y,hi1.y)
+//           (lo0.z,hi0.z,lo1.z,hi1.z) (child0,child1,-,-) as int bits.
+//           child >= 0: inner node index; child < 0: leaf code ~(first |
+//           (count-1) << 27) over the leaf-ordered triangle array.
+//   tris  : 3 x float4 per triangle in leaf order (48 B):
+//           (v1.xyz, local id), (e1.xyz, 0), (e2.xyz, 0)
+//           with e1 = v2 - v1, e2 = v3 - v1 (scene/surface/geometry/Triangle.cpp:76-83).
+//   triSurface : local triangle id -> global surface index (material).
+//   triPrim    : local triangle id -> primitive id inside its geometry.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace vsr {
+
+enum { MAT_MATTE = 0, MAT_PBR = 1 };
+enum { ALPHA_OPAQUE = 0, ALPHA_BLEND = 1, ALPHA_MASK = 2 };
+enum { CAM_PERSPECTIVE = 0, CAM_MATRIX = 1, CAM_ORTHO = 2, CAM_OMNI = 3 };
+enum { REND_RAYCAST = 0, REND_PATHTRACE = 1 };
+enum { COLOR_FLOAT4 = 0, COLOR_UFIXED8 = 1, COLOR_SRGB8 = 2, COLOR_NONE = 3 };
+
+// Device-side error bits, read back as frame property "errorFlags".
+enum : uint32_t {
+  ERR_STACK_OVERFLOW = 1u,   // BVH traversal stack full: traversal stopped
+  ERR_DDA_LIMIT = 2u,        // DDA step limit reached
+  ERR_TRACK_LIMIT = 4u,      // delta-tracking step limit reached
+  ERR_PATH_LIMIT = 8u,       // path pass limit reached
+};
+
+constexpr int kTraversalStack = 64;
+constexpr int kMaxClipPlanes = 8;
+constexpr uint32_t kLeafCountShift = 27;
+constexpr uint32_t kLeafFirstMask = (1u << kLeafCountShift) - 1u;
+
+struct DMaterial {
+  float baseColor[3];
+  int type;
+  float metallic, roughness, ior, opacity;
+  float clearcoat, clearcoatRoughness, transmission, sheenRoughness;
+  float sheenColor[3];
+  int alphaMode;
+  float alphaCutoff;
+  float pad[3];
+};
+
+struct DLight {
+  float dir[3];        // unit vector towards the light (-direction)
+  float intensity[3];  // color * irradiance
+  float cosHalfAngle;  // cos(angularDiameter/2); 1 = delta light
+  int type;
+  int visible;
+  int pad;
+};
+
+struct DVolume {
+  const float *data;   // dims.x*dims.y*dims.z, x fastest
+  const float4 *tf;    // transfer function table
+  const float *majorant;  // gdims cells or null
+  int dims[3];
+  int tfSize;
+  int gdims[3];
+  float unitDistance;
+  float boundsLo[3], boundsHi[3];
+  float S[3], T[3];    // voxel space = S * (p + T)
+  float cellSize;
+  float vrMin, vrMax;
+};
+
+struct DGroup {
+  const float4 *nodes;
+  const float4 *tris;
+  const uint32_t *triSurface;
+  const uint32_t *triPrim;
+  int numTris;
+  int numNodes;
+  int volBegin, volEnd;   // range in DScene::groupVolumes
+  float boundsLo[3], boundsHi[3];
+};
+
+struct DInstance {
+  float affineInv[9];  // column-major 3x3
+  float transInv[3];
+  float normalXfm[9];  // transpose(affineInv)
+  int group;
+  uint32_t userID;
+};
+
+struct DScene {
+  const DInstance *instances;
+  const DGroup *groups;
+  const DMaterial *materials;
+  const DLight *lights;
+  const DVolume *volumes;
+  const int *groupVolumes;
+  int numInstances;
+  int numGroups;
+  int numLights;
+  int numVolumes;
+  int allOpaque;
+  int hasSurfaces;
+};
+
+struct DCamera {
+  int type;
+  float eye[3];
+  float U[3], V[3], W[3];
+  float dir[3];
+  float lensRadius, focusDistance;
+  float region[4];
+  float shutter[2];
+  float inv[16];       // matrix camera: inverse(proj * view), column-major
+};
+
+struct DRenderer {
+  int type;
+  float bg[4];
+  float ambient[3];    // ambientColor * ambientRadiance
+  float occlusionDistance;
+  int ambientSamples;
+  int maxBounce;
+  int pixelSamples;
+  float samplingRateInv;
+  int numClipPlanes;
+  float clip[kMaxClipPlanes][4];
+};
+
+struct DFrame {
+  int width, height;
+  int accumID;
+  int colorType;
+  void *color;
+  float *depth;
+  float *normal;   // float3 packed
+  float *albedo;   // float3 packed
+  float4 *accum;
+  uint32_t *errorFlags;
+  unsigned long long *counters;  // optional statistics (null = off)
+};
+
+} // namespace vsr

@@ -1,0 +1,313 @@
+"""Seeded synthetic scenes of the benchmark configurations, and their
+construction through the renderer core's object API.
+
+No public dataset is involved: each configuration is generated from a
+numpy PCG64 stream seeded with 0x5EED0000 + config index; the draw order
+is fixed in each generator. A scene is a plain dict:
+
+  surfaces : [{"vertices": (V,3) f32, "indices": (T,3) u32, "material": {...}}]
+  volumes  : [{"data": (nz,ny,nx) f32, "origin", "spacing", "color": (N,3),
+               "opacity": (N,), "valueRange", "unitDistance"}]
+  lights   : [{"direction", "color", "irradiance"}]
+  instances: [{"transform": 12 floats (column-major 3x4), "surfaces": [...],
+               "volumes": [...], "lights": [...]}]   (optional)
+  camera   : {"type": "perspective", "position", "direction", "up", "fovy", "aspect"}
+  renderer : {"type": "raycast"|"pathtrace", parameters...}
+  frame    : {"size": (W, H)}
+
+World-level surfaces/volumes/lights go into one group with an identity
+instance, which comes before the explicit instances.
+"""
+import math
+
+import numpy as np
+
+from . import vsr
+
+SEED_BASE = 0x5EED0000
+
+
+def _look_at_camera(target, eye, fovy_deg, aspect):
+    d = np.asarray(target, np.float64) - np.asarray(eye, np.float64)
+    d /= np.linalg.norm(d)
+    return {"type": "perspective", "position": [float(x) for x in eye],
+            "direction": [float(x) for x in d], "up": [0.0, 1.0, 0.0],
+            "fovy": math.radians(fovy_deg), "aspect": float(aspect)}
+
+
+def blob_field(n, rng, num_blobs=16):
+    """Sum of isotropic Gaussian blobs at voxel centres (i+0.5)/n, normalised to [0,1]."""
+    centres = rng.uniform(0.0, 1.0, size=(num_blobs, 3))
+    sigma = rng.uniform(0.05, 0.15, size=num_blobs)
+    amp = rng.uniform(0.2, 1.0, size=num_blobs)
+    p = (np.arange(n, dtype=np.float64) + 0.5) / n
+    field = np.zeros((n, n, n), np.float64)
+    for c, s, a in zip(centres, sigma, amp):
+        gx = np.exp(-((p - c[0]) ** 2) / (2 * s * s))
+        gy = np.exp(-((p - c[1]) ** 2) / (2 * s * s))
+        gz = np.exp(-((p - c[2]) ** 2) / (2 * s * s))
+        field += a * gz[:, None, None] * gy[None, :, None] * gx[None, None, :]
+    lo, hi = field.min(), field.max()
+    return ((field - lo) / (hi - lo)).astype(np.float32)
+
+
+def linear_tf(n=256, alpha_max=0.05):
+    """Colour blue->red, opacity 0->alpha_max, n entries."""
+    t = np.linspace(0.0, 1.0, n, dtype=np.float32)
+    color = np.stack([t, np.zeros_like(t), 1.0 - t], axis=1).astype(np.float32)
+    opacity = (t * alpha_max).astype(np.float32)
+    return color, opacity
+
+
+def config0(res=512, n=128, seed=SEED_BASE + 0):
+    """Raycast renderer over a structured-regular Gaussian-blob volume."""
+    rng = np.random.default_rng(seed)
+    data = blob_field(n, rng)
+    color, opacity = linear_tf(256, 0.05)
+    extent = float(n - 1)
+    centre = [extent / 2] * 3
+    diag = math.sqrt(3.0) * extent
+    view = np.array([0.6, 0.45, 0.66])
+    view /= np.linalg.norm(view)
+    eye = np.array(centre) + 2.5 * diag * view
+    return {
+        "surfaces": [], "lights": [],
+        "volumes": [{"data": data, "origin": [0.0, 0.0, 0.0], "spacing": [1.0, 1.0, 1.0],
+                     "color": color, "opacity": opacity, "valueRange": [0.0, 1.0],
+                     "unitDistance": 1.0}],
+        "camera": _look_at_camera(centre, eye, 40.0, 1.0),
+        "renderer": {"type": "raycast", "volumeSamplingRate": 2.0, "background": [0, 0, 0, 1]},
+        "frame": {"size": (res, res)},
+    }
+
+
+def uv_sphere(centre, radius, nu=64, nv=32):
+    """UV sphere without degenerate pole triangles: nu*(2*nv-2) triangles,
+    counter-clockwise seen from outside."""
+    th = np.pi * np.arange(nv + 1) / nv
+    ph = 2 * np.pi * np.arange(nu + 1) / nu
+    st, ct = np.sin(th)[:, None], np.cos(th)[:, None]
+    sp, cp = np.sin(ph)[None, :], np.cos(ph)[None, :]
+    v = np.stack([st * cp, np.broadcast_to(ct, (nv + 1, nu + 1)), st * sp], axis=-1)
+    v = (v * radius + np.asarray(centre)).reshape(-1, 3).astype(np.float32)
+    j, i = np.meshgrid(np.arange(nv), np.arange(nu), indexing="ij")
+    a = j * (nu + 1) + i
+    b = (j + 1) * (nu + 1) + i
+    c = (j + 1) * (nu + 1) + i + 1
+    d = j * (nu + 1) + i + 1
+    # row r contributes (a,d,b) unless it touches the top pole (r == 0) and
+    # (b,d,c) unless it touches the bottom pole (r == nv-1)
+    rows = []
+    for r in range(nv):
+        q = []
+        if r > 0:
+            q.append(np.stack([a[r], d[r], b[r]], -1))
+        if r < nv - 1:
+            q.append(np.stack([b[r], d[r], c[r]], -1))
+        rows.append(np.concatenate(q))
+    return v, np.concatenate(rows).astype(np.uint32)
+
+
+def sphere_set(rng, num_spheres=256, nu=64, nv=32):
+    """The config-1 sphere set: surfaces list (ground quad last)."""
+    centres = rng.uniform(-10.0, 10.0, size=(num_spheres, 3))
+    radii = rng.uniform(0.3, 1.5, size=num_spheres)
+    coin = rng.uniform(0.0, 1.0, size=num_spheres)
+    colors = rng.uniform(0.1, 0.9, size=(num_spheres, 3))
+    metallic = rng.uniform(0.0, 1.0, size=num_spheres)
+    roughness = rng.uniform(0.0, 1.0, size=num_spheres)
+    surfaces = []
+    for k in range(num_spheres):
+        v, t = uv_sphere(centres[k], radii[k], nu, nv)
+        if coin[k] < 0.5:
+            mat = {"type": "matte", "color": [float(x) for x in colors[k]]}
+        else:
+            mat = {"type": "physicallyBased", "baseColor": [float(x) for x in colors[k]],
+                   "metallic": float(metallic[k]), "roughness": float(roughness[k])}
+        surfaces.append({"vertices": v, "indices": t, "material": mat})
+    g = 20.0
+    quad = np.array([[-g, -11.5, -g], [g, -11.5, -g], [g, -11.5, g], [-g, -11.5, g]], np.float32)
+    surfaces.append({"vertices": quad, "indices": np.array([[0, 2, 1], [0, 3, 2]], np.uint32),
+                     "material": {"type": "matte", "color": [0.8, 0.8, 0.8]}})
+    return surfaces
+
+
+def config1(res=1024, spp=64, num_spheres=256, nu=64, nv=32, max_bounce=5,
+            seed=SEED_BASE + 1):
+    """Path tracer over ~1M triangles: 256 UV spheres + a 40x40 ground quad."""
+    rng = np.random.default_rng(seed)
+    surfaces = sphere_set(rng, num_spheres, nu, nv)
+    light_dir = np.array([-0.35, -1.0, -0.45])
+    light_dir /= np.linalg.norm(light_dir)
+    return {
+        "surfaces": surfaces, "volumes": [],
+        "lights": [{"direction": [float(x) for x in light_dir], "color": [1.0, 1.0, 1.0],
+                    "irradiance": 3.0}],
+        "camera": _look_at_camera([0.0, -1.0, 0.0], [6.0, 9.0, 34.0], 45.0, 1.0),
+        "renderer": {"type": "pathtrace", "pixelSamples": spp, "maxBounce": max_bounce,
+                     "ambientRadiance": 0.2, "background": [0, 0, 0, 1]},
+        "frame": {"size": (res, res)},
+    }
+
+
+def triangle_count(scene):
+    return sum(len(s["indices"]) for s in scene["surfaces"])
+
+
+# --------------------------------------------------------------- build via ABI
+def _material(dev, m):
+    mat = dev.material(m["type"])
+    for k, v in m.items():
+        if k == "type":
+            continue
+        if isinstance(v, str):
+            dev.set(mat, k, v)
+        elif isinstance(v, (list, tuple)):
+            dev.set(mat, k, v, vsr.FLOAT32_VEC3 if len(v) == 3 else vsr.FLOAT32_VEC4)
+        else:
+            dev.set(mat, k, float(v))
+    dev.commit(mat)
+    return mat
+
+
+def _surfaces(dev, surfs, keep):
+    out = []
+    for s in surfs:
+        g = dev.geometry("triangle")
+        va = dev.array1d(np.asarray(s["vertices"], np.float32))
+        ia = dev.array1d(np.asarray(s["indices"], np.uint32))
+        dev.set(g, "vertex.position", va)
+        dev.set(g, "primitive.index", ia)
+        dev.commit(g)
+        mat = _material(dev, s["material"])
+        sf = dev.surface()
+        dev.set(sf, "geometry", g)
+        dev.set(sf, "material", mat)
+        dev.commit(sf)
+        keep += [g, va, ia, mat]
+        out.append(sf)
+    return out
+
+
+def _volumes(dev, vols, keep):
+    out = []
+    for v in vols:
+        f = dev.spatial_field("structuredRegular")
+        da = dev.array3d(np.asarray(v["data"], np.float32))
+        dev.set(f, "data", da)
+        dev.set(f, "origin", v["origin"], vsr.FLOAT32_VEC3)
+        dev.set(f, "spacing", v["spacing"], vsr.FLOAT32_VEC3)
+        dev.commit(f)
+        vol = dev.volume("transferFunction1D")
+        dev.set(vol, "value", f)
+        ca = dev.array1d(np.asarray(v["color"], np.float32))
+        oa = dev.array1d(np.asarray(v["opacity"], np.float32))
+        dev.set(vol, "color", ca)
+        dev.set(vol, "opacity", oa)
+        dev.set(vol, "valueRange", v["valueRange"], vsr.FLOAT32_BOX1)
+        dev.set(vol, "unitDistance", float(v["unitDistance"]))
+        if "majorantBrickSize" in v:
+            dev.set(vol, "majorantBrickSize", int(v["majorantBrickSize"]))
+        dev.commit(vol)
+        keep += [f, da, ca, oa]
+        out.append(vol)
+    return out
+
+
+def _lights(dev, lights, keep):
+    out = []
+    for L in lights:
+        lt = dev.light("directional")
+        dev.set(lt, "direction", L["direction"], vsr.FLOAT32_VEC3)
+        dev.set(lt, "color", L.get("color", [1, 1, 1]), vsr.FLOAT32_VEC3)
+        dev.set(lt, "irradiance", float(L.get("irradiance", 1.0)))
+        dev.commit(lt)
+        out.append(lt)
+    return out
+
+
+def _set_lists(dev, obj, surfs, vols, lights, keep):
+    for name, lst in (("surface", surfs), ("volume", vols), ("light", lights)):
+        if lst:
+            arr = dev.array1d(lst)
+            dev.set(obj, name, arr)
+            keep.append(arr)
+        keep += lst
+
+
+def apply_renderer(dev, rend, params):
+    for k, v in params.items():
+        if k == "type":
+            continue
+        if k == "clipPlanes":
+            arr = dev.array1d(np.asarray(v, np.float32).reshape(-1, 4))
+            dev.set(rend, "clipPlane", arr)
+            dev.release(arr)
+        elif k == "background":
+            dev.set(rend, k, v, vsr.FLOAT32_VEC4)
+        elif k == "ambientColor":
+            dev.set(rend, k, v, vsr.FLOAT32_VEC3)
+        elif isinstance(v, (int, np.integer)) and not isinstance(v, bool):
+            dev.set(rend, k, int(v))
+        else:
+            dev.set(rend, k, float(v))
+    dev.commit(rend)
+
+
+def apply_camera(dev, cam, c):
+    for k in ("position", "direction", "up"):
+        dev.set(cam, k, c[k], vsr.FLOAT32_VEC3)
+    for k in ("fovy", "aspect", "apertureRadius", "focusDistance", "height"):
+        if k in c:
+            dev.set(cam, k, float(c[k]))
+    if "view" in c:
+        dev.set(cam, "view", c["view"], vsr.FLOAT32_MAT4)
+        dev.set(cam, "proj", c["proj"], vsr.FLOAT32_MAT4)
+    dev.commit(cam)
+
+
+def build(dev, scene, channels=("color", "depth", "normal", "albedo"), collect_stats=False):
+    """Create the scene's objects through the C ABI; returns a dict of handles."""
+    keep = []
+    world = dev.world()
+    surfs = _surfaces(dev, scene.get("surfaces", []), keep)
+    vols = _volumes(dev, scene.get("volumes", []), keep)
+    lights = _lights(dev, scene.get("lights", []), keep)
+    _set_lists(dev, world, surfs, vols, lights, keep)
+    insts = []
+    for I in scene.get("instances", []):
+        grp = dev.group()
+        _set_lists(dev, grp,
+                   _surfaces(dev, I.get("surfaces", []), keep),
+                   _volumes(dev, I.get("volumes", []), keep),
+                   _lights(dev, I.get("lights", []), keep), keep)
+        dev.commit(grp)
+        inst = dev.instance("transform")
+        dev.set(inst, "group", grp)
+        dev.set(inst, "transform", I["transform"], vsr.FLOAT32_MAT3x4)
+        dev.commit(inst)
+        keep.append(grp)
+        insts.append(inst)
+    if insts:
+        arr = dev.array1d(insts)
+        dev.set(world, "instance", arr)
+        keep += [arr] + insts
+    dev.commit(world)
+    cam = dev.camera(scene["camera"]["type"])
+    apply_camera(dev, cam, scene["camera"])
+    rend = dev.renderer(scene["renderer"]["type"])
+    apply_renderer(dev, rend, scene["renderer"])
+    frame = dev.frame()
+    W, H = scene["frame"]["size"]
+    dev.set(frame, "size", (W, H), vsr.UINT32_VEC2)
+    types = {"color": vsr.FLOAT32_VEC4, "depth": vsr.FLOAT32, "normal": vsr.FLOAT32_VEC3,
+             "albedo": vsr.FLOAT32_VEC3}
+    for ch in channels:
+        dev.set(frame, "channel." + ch, types[ch], vsr.DATA_TYPE)
+    if collect_stats:
+        dev.set(frame, "collectStatistics", True)
+    dev.set(frame, "world", world)
+    dev.set(frame, "camera", cam)
+    dev.set(frame, "renderer", rend)
+    dev.commit(frame)
+    return {"world": world, "camera": cam, "renderer": rend, "frame": frame, "keep": keep}

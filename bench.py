@@ -1,0 +1,324 @@
+#!/usr/bin/env python3
+"""Benchmark of the renderer core: path-traced Mpx*spp/s on the config-1 scene.
+
+Workload (default): 256 UV spheres (64x32 segments, 1,015,808 triangles) +
+a 40x40 ground quad, 50/50 matte / physically-based materials, one
+directional light (irradiance 3), ambient 0.2, 1024x1024, 64 samples per
+pixel per frame, maximum depth 5; BVH built on the device at commit. One
+step = one frame (64 spp over every pixel) rendered through the C ABI.
+
+  value : W*H*spp / render-kernel time (CUDA events on the render stream),
+          scene resident in HBM, L2 flushed (256 MiB write) between steps.
+  e2e   : the same metric through the public call sequence with host
+          buffers: camera update + commit, render, wait, map the colour,
+          depth, normal and albedo channels into host memory (wall clock).
+
+--impl reference times the CPU restatement of the reference CPU device
+(the oracle, 64x64 tiles on all host threads) on a bounded band of rows of
+the same workload; there is no runnable reference binary in this
+environment (Visionaray and the ANARI SDK are not available).
+"""
+import argparse
+import importlib
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+MPX = 1e6
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=5)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    p.add_argument("--res", type=int, default=1024)
+    p.add_argument("--spp", type=int, default=64)
+    p.add_argument("--e2e-steps", type=int, default=3)
+    p.add_argument("--cpu-rows", type=int, default=48,
+                   help="rows of the frame the CPU baseline renders (bounded sample)")
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    return p.parse_args()
+
+
+def dist_info():
+    return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), \
+        int(os.environ.get("LOCAL_RANK", 0))
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled during the timed region."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.QUERY}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            d = json.load(f)
+        return d.get("hbm_gbs", 6800.0), "measured"
+    return 6800.0, "fallback"
+
+
+def profiled_traffic():
+    """DRAM bytes per launch of the path-trace kernel from the committed ncu summary."""
+    path = os.path.join(ROOT, "profiles", "pathtrace_config1.md")
+    if not os.path.exists(path):
+        return None
+    with open(path) as f:
+        for ln in f:
+            if ln.strip().startswith("traffic_bytes_per_launch"):
+                try:
+                    return float(ln.split("=")[1].split()[0])
+                except (IndexError, ValueError):
+                    return None
+    return None
+
+
+def cpu_baseline(scene, rows, threads=0):
+    """Time the oracle on a band of rows spread over the frame; Mpx*spp/s."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import pyoracle as po
+
+    S = po.Scene(scene)
+    W, H = scene["frame"]["size"]
+    spp = scene["renderer"]["pixelSamples"]
+    F = po.Frame(W, H)
+    bands = 8
+    per = max(1, rows // bands)
+    starts = [int((b + 0.5) * H / bands) - per // 2 for b in range(bands)]
+    t0 = time.perf_counter()
+    for s in starts:
+        po.render(S, F, num_threads=threads, rows=(s, s + per))
+    dt = time.perf_counter() - t0
+    px = W * per * bands
+    cores = threads if threads > 0 else os.cpu_count()
+    return px * spp / dt / MPX, dt, px, cores
+
+
+def run_reference(args):
+    rank, world, _ = dist_info()
+    if rank != 0:
+        return
+    pkg = importlib.import_module("anari-visionaray_gb300")
+    scene = pkg.scenes.config1(res=args.res, spp=args.spp)
+    rows = max(8, args.cpu_rows // 2)
+    vals = []
+    for i in range(args.warmup + args.steps):
+        v, dt, px, cores = cpu_baseline(scene, rows)
+        if i >= args.warmup:
+            vals.append((v, dt))
+    value = sum(px * args.spp for _ in vals) / sum(dt for _, dt in vals) / MPX
+    unit = "Mpx*spp/s"
+    line = {
+        "impl": "reference", "metric": "pathtracer Mpx*spp/s (config 1)", "value": value,
+        "unit": unit, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * statistics.mean(dt for _, dt in vals),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic",
+        "config": {"workload": f"config1 pathtracer {args.res}x{args.res} {args.spp}spp depth5 "
+                               "1015810 tris", "sample": f"{px} pixels per step"},
+        "cpu_baseline": {"value": value, "unit": unit, "cores": cores, "kind": "port",
+                         "sample": f"{px} of {args.res * args.res} pixels ({rows} rows in 8 bands) "
+                                   f"x {args.spp} spp per step"},
+        "e2e": {"value": value, "unit": unit, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args):
+    import torch
+
+    rank, world, local = dist_info()
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    torch.cuda.set_device(local)
+    os.environ.setdefault("VISIONARAY_CUDA_DEVICE", str(local))
+    pkg = importlib.import_module("anari-visionaray_gb300")
+    vsr = pkg.vsr
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+
+    scene = pkg.scenes.config1(res=args.res, spp=args.spp)
+    ntris = pkg.scenes.triangle_count(scene)
+    dev = vsr.Device()
+    h = pkg.scenes.build(dev, scene)
+    frame = h["frame"]
+    dev.set(h["renderer"], "sampleLimit", 1 << 30)
+    dev.commit(h["renderer"])
+    W, H = args.res, args.res
+    px_samples = W * H * args.spp
+
+    # first frame builds the BVH on the device (commit work, reported apart)
+    dev.render(frame)
+    dev.wait(frame)
+    commit_s = dev.get_float(frame, "commitDuration")
+    bvh_s = dev.get_float(h["world"], "bvh.buildDuration")
+
+    # counting pass (untimed): rays, BVH node visits, triangle tests of one frame
+    dev.set(frame, "collectStatistics", True)
+    dev.commit(frame)
+    dev.render(frame)
+    dev.wait(frame)
+    counts = dev.get_u64(frame, "statistics", 8) or [0] * 8
+    dev.set(frame, "collectStatistics", False)
+    dev.commit(frame)
+
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    for _ in range(args.warmup):
+        dev.render(frame)
+        dev.wait(frame)
+    clocks = ClockSampler(local)
+    clocks.start()
+    durations = []
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        flush.fill_(1.0)
+        torch.cuda.synchronize()
+        assert dev.render(frame) == 0
+        dev.wait(frame)
+        durations.append(dev.get_float(frame, "duration.render"))
+    barrier()
+    wall = time.perf_counter() - t0
+    clk = clocks.stop()
+    err = dev.get_uint(frame, "errorFlags")
+
+    # end to end through the public API with host buffers
+    cam = h["camera"]
+    c = scene["camera"]
+    e2e_times = []
+    d2h = W * H * (16 + 4 + 12 + 12)
+    for i in range(args.e2e_steps + 1):
+        pos = list(c["position"])
+        pos[0] += 1e-3 * (i % 2)
+        flush.fill_(1.0)
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        dev.set(cam, "position", pos, vsr.FLOAT32_VEC3)
+        dev.commit(cam)
+        dev.render(frame)
+        dev.wait(frame)
+        for ch in ("channel.color", "channel.depth", "channel.normal", "channel.albedo"):
+            dev.map_raw(frame, ch)
+        if i > 0:
+            e2e_times.append(time.perf_counter() - t)
+    h2d = 3 * 4 + 4 * 4 * 0  # the camera position crosses to the device as kernel parameters
+
+    kernel_s = sum(durations) / len(durations)
+    t_max = kernel_s
+    if world > 1:
+        tt = torch.tensor([kernel_s], device="cuda")
+        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        t_max = float(tt.item())
+    value = world * px_samples / t_max / MPX
+    e2e_value = world * px_samples / statistics.mean(e2e_times) / MPX
+
+    if rank != 0:
+        dev.close()
+        return
+    rays, nodes, tris = counts[0], counts[1], counts[2]
+    alg_bytes = nodes * 64 + tris * 48 + W * H * (16 + 16 + 4 + 12 + 12)
+    peak, peak_kind = measured_peaks()
+    achieved = alg_bytes / kernel_s / 1e9
+    traffic = profiled_traffic()
+    line = {
+        "metric": "pathtracer Mpx*spp/s (config 1)",
+        "value": value, "unit": "Mpx*spp/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 * kernel_s, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": f"config1 pathtracer {W}x{H} {args.spp}spp depth5 {ntris} tris",
+                   "l2": "flushed (256 MiB write) between steps", "parallelism": f"replicas{world}"},
+        "e2e": {"value": e2e_value, "unit": "Mpx*spp/s", "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h},
+        "gpu_launches": args.steps,
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "traffic": traffic,
+                     "note": f"algorithmic bytes = BVH node fetches x64 B + triangle fetches x48 B "
+                             f"+ frame bytes; peak {peak_kind}; most fetches hit L1/L2"},
+        "traversal": {"rays": rays, "node_visits": nodes, "tri_tests": tris,
+                      "grays_per_s": rays / kernel_s / 1e9},
+        "commit_s": commit_s, "bvh_build_s": bvh_s,
+        "wall_s_timed": wall, "clocks": clk, "error_flags": err,
+    }
+    if world == 1 and not args.no_cpu_baseline:
+        v, dt, px, cores = cpu_baseline(scene, args.cpu_rows)
+        line["cpu_baseline"] = {"value": v, "unit": "Mpx*spp/s", "cores": cores, "kind": "port",
+                                "sample": f"{px} of {W * H} pixels ({args.cpu_rows} rows in 8 bands) "
+                                          f"x {args.spp} spp, {dt:.1f} s"}
+    print(json.dumps(line), flush=True)
+    dev.close()
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

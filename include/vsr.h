@@ -1,0 +1,196 @@
+/* vsr.h — C ABI of the GB300 renderer core behind the anari-visionaray
+ * "raycast" and "pathtracer" per-pixel hot path.
+ *
+ * Each entry point is the counterpart of one call of the ANARI API that the
+ * reference device implements; the reference site it replaces is cited
+ * beside it. Object model, parameter names and channel names follow the
+ * reference device (VisionarayDevice.cpp:59-214, frame/Frame.cpp:75-94).
+ * The ANARI SDK headers are not part of this build, so data-type values are
+ * this library's own (VSR_*); INTEGRATION.md maps them to ANARI_*.
+ *
+ * Errors: every call returns a VSRStatus (0 = success) and reports problems
+ * through the device's status callback with a severity, as the reference
+ * reports them through reportMessage (e.g. frame/Frame.cpp:98-110).
+ * Rendering is asynchronous on one CUDA stream; vsrFrameReady waits on the
+ * frame's completion event (frame/Frame.cpp:474-497).
+ */
+#ifndef VSR_H
+#define VSR_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#if defined(_WIN32)
+#define VSR_API __declspec(dllexport)
+#else
+#define VSR_API __attribute__((visibility("default")))
+#endif
+
+typedef struct VSRDevice_ *VSRDevice;
+typedef struct VSRObject_ *VSRObject;
+typedef VSRObject VSRArray;
+typedef VSRObject VSRFrame;
+
+typedef enum VSRStatus {
+  VSR_OK = 0,
+  VSR_ERROR_INVALID_ARGUMENT = 1,
+  VSR_ERROR_INVALID_OBJECT = 2,
+  VSR_ERROR_UNKNOWN_SUBTYPE = 3,
+  VSR_ERROR_OUT_OF_MEMORY = 4,
+  VSR_ERROR_CUDA = 5,
+  VSR_ERROR_INCOMPLETE = 6,
+  VSR_ERROR_TIMEOUT = 7
+} VSRStatus;
+
+typedef enum VSRSeverity {
+  VSR_SEVERITY_FATAL_ERROR = 1,
+  VSR_SEVERITY_ERROR = 2,
+  VSR_SEVERITY_WARNING = 3,
+  VSR_SEVERITY_PERFORMANCE_WARNING = 4,
+  VSR_SEVERITY_INFO = 5,
+  VSR_SEVERITY_DEBUG = 6
+} VSRSeverity;
+
+typedef enum VSRDataType {
+  VSR_UNKNOWN = 0,
+  VSR_STRING = 1,
+  VSR_OBJECT = 2,
+  VSR_ARRAY1D = 3,
+  VSR_ARRAY2D = 4,
+  VSR_ARRAY3D = 5,
+  VSR_CAMERA = 6,
+  VSR_FRAME = 7,
+  VSR_GEOMETRY = 8,
+  VSR_GROUP = 9,
+  VSR_INSTANCE = 10,
+  VSR_LIGHT = 11,
+  VSR_MATERIAL = 12,
+  VSR_RENDERER = 13,
+  VSR_SURFACE = 14,
+  VSR_SPATIAL_FIELD = 15,
+  VSR_VOLUME = 16,
+  VSR_WORLD = 17,
+  VSR_DATA_TYPE = 18,      /* a VSRDataType value, e.g. for "channel.color" */
+  VSR_BOOL = 19,
+  VSR_INT32 = 20,
+  VSR_UINT32 = 21,
+  VSR_INT32_VEC2 = 22,
+  VSR_UINT32_VEC2 = 23,
+  VSR_UINT32_VEC3 = 24,
+  VSR_FLOAT32 = 25,
+  VSR_FLOAT32_VEC2 = 26,
+  VSR_FLOAT32_VEC3 = 27,
+  VSR_FLOAT32_VEC4 = 28,
+  VSR_FLOAT32_BOX1 = 29,
+  VSR_FLOAT32_MAT4 = 30,   /* column-major 4x4 */
+  VSR_FLOAT32_MAT3x4 = 31, /* column-major 3x4 affine */
+  VSR_UFIXED8 = 32,
+  VSR_UFIXED8_VEC4 = 33,
+  VSR_UFIXED8_RGBA_SRGB = 34,
+  VSR_UFIXED16 = 35,
+  VSR_FLOAT64_BOX1 = 36,
+  VSR_UINT64 = 37,
+  VSR_FLOAT64 = 38
+} VSRDataType;
+
+typedef enum VSRWaitMask { VSR_NO_WAIT = 0, VSR_WAIT = 1 } VSRWaitMask;
+
+typedef void (*VSRStatusCallback)(const void *userPtr, VSRDevice device, VSRObject source,
+                                  VSRDataType sourceType, VSRSeverity severity,
+                                  VSRStatus code, const char *message);
+
+/* Device creation; replaces anariNewVisionarayDevice (VisionarayLibrary.cpp:69-73)
+   and the device-level parameters of deviceCommitParameters
+   (VisionarayDevice.cpp:354-391). subtype "default" selects the current
+   CUDA device, or the one named by the VISIONARAY_CUDA_DEVICE environment
+   variable as in the reference (VisionarayDevice.cpp:373-380). Returns NULL
+   (and reports VSR_ERROR_CUDA) when no CUDA device is present: there is no
+   CPU fallback. */
+VSR_API VSRDevice vsrNewDevice(const char *subtype, VSRStatusCallback cb, const void *cbUserPtr);
+VSR_API VSRStatus vsrReleaseDevice(VSRDevice device);
+
+/* Arrays; replace newArray1D/2D/3D (VisionarayDevice.cpp:59-122). The data is
+   copied at creation (the reference copies into HostDeviceArrays on commit). */
+VSR_API VSRArray vsrNewArray1D(VSRDevice d, const void *appMemory, VSRDataType type, uint64_t n1);
+VSR_API VSRArray vsrNewArray2D(VSRDevice d, const void *appMemory, VSRDataType type, uint64_t n1,
+                               uint64_t n2);
+VSR_API VSRArray vsrNewArray3D(VSRDevice d, const void *appMemory, VSRDataType type, uint64_t n1,
+                               uint64_t n2, uint64_t n3);
+
+/* Object factories; replace newSpatialField/newVolume/newGeometry/newMaterial/
+   newLight/newSurface/newGroup/newInstance/newWorld/newCamera/newRenderer/
+   newFrame (VisionarayDevice.cpp:125-214). Supported subtypes:
+   spatial field "structuredRegular"; volume "transferFunction1D";
+   geometry "triangle"; material "matte", "physicallyBased"; light
+   "directional"; instance "transform"; camera "perspective", "matrix",
+   "orthographic", "omnidirectional"; renderer "raycast", "pathtrace",
+   "default" (= pathtrace, renderer/Renderer.cpp:144-152).
+   Unknown subtypes return NULL and report VSR_ERROR_UNKNOWN_SUBTYPE. */
+VSR_API VSRObject vsrNewSpatialField(VSRDevice d, const char *subtype);
+VSR_API VSRObject vsrNewVolume(VSRDevice d, const char *subtype);
+VSR_API VSRObject vsrNewGeometry(VSRDevice d, const char *subtype);
+VSR_API VSRObject vsrNewMaterial(VSRDevice d, const char *subtype);
+VSR_API VSRObject vsrNewLight(VSRDevice d, const char *subtype);
+VSR_API VSRObject vsrNewSurface(VSRDevice d);
+VSR_API VSRObject vsrNewGroup(VSRDevice d);
+VSR_API VSRObject vsrNewInstance(VSRDevice d, const char *subtype);
+VSR_API VSRObject vsrNewWorld(VSRDevice d);
+VSR_API VSRObject vsrNewCamera(VSRDevice d, const char *subtype);
+VSR_API VSRObject vsrNewRenderer(VSRDevice d, const char *subtype);
+VSR_API VSRFrame vsrNewFrame(VSRDevice d);
+
+/* Parameters; replace anariSetParameter/anariUnsetParameter/
+   anariCommitParameters (helium BaseObject, used by every commitParameters()
+   in the reference). Object-valued parameters pass a pointer to the handle;
+   VSR_STRING passes the C string itself. Parameter names and defaults are
+   the reference's (e.g. renderer/Pathtrace.cpp:16-28, renderer/Raycast.cpp:16-20,
+   renderer/Renderer.cpp:34-45, camera/Camera.cpp:30-36). */
+VSR_API VSRStatus vsrSetParameter(VSRDevice d, VSRObject o, const char *name, VSRDataType type,
+                                  const void *mem);
+VSR_API VSRStatus vsrUnsetParameter(VSRDevice d, VSRObject o, const char *name);
+VSR_API VSRStatus vsrCommitParameters(VSRDevice d, VSRObject o);
+VSR_API VSRStatus vsrRelease(VSRDevice d, VSRObject o);
+VSR_API VSRStatus vsrRetain(VSRDevice d, VSRObject o);
+
+/* Properties; replace anariGetProperty (frame/Frame.cpp:171-213): frame
+   "duration" (FLOAT32, seconds of GPU time of the last render),
+   "duration.render" (FLOAT32, render kernel only), "numSamples" (INT32),
+   "commitDuration" (FLOAT32, seconds of the last scene update incl. BVH
+   build), "errorFlags" (UINT32, device-side error bits of the last render);
+   world "bvh.nodes" / "bvh.triangles" (UINT64). Returns 1 if found. */
+VSR_API int vsrGetProperty(VSRDevice d, VSRObject o, const char *name, VSRDataType type,
+                           void *mem, uint64_t size, VSRWaitMask mask);
+
+/* Rendering; replaces anariRenderFrame / anariFrameReady / anariDiscardFrame
+   (Frame::renderFrame frame/Frame.cpp:215-397, Frame::wait :474-497). */
+VSR_API VSRStatus vsrRenderFrame(VSRDevice d, VSRFrame f);
+VSR_API int vsrFrameReady(VSRDevice d, VSRFrame f, VSRWaitMask mask);
+VSR_API VSRStatus vsrDiscardFrame(VSRDevice d, VSRFrame f);
+
+/* Mapping; replaces anariMapFrame / anariUnmapFrame (frame/Frame.cpp:399-447).
+   Channels: "channel.color", "channel.depth", "channel.normal",
+   "channel.albedo". Returns a host pointer valid until the next render or
+   unmap; the copy from device memory happens inside this call. */
+VSR_API const void *vsrMapFrame(VSRDevice d, VSRFrame f, const char *channel, uint32_t *width,
+                                uint32_t *height, VSRDataType *pixelType);
+VSR_API VSRStatus vsrUnmapFrame(VSRDevice d, VSRFrame f, const char *channel);
+
+/* Device-resident view of a channel (no copy): the CUDA device pointer of
+   the frame buffer, for consumers that stay on the GPU. Same channels as
+   vsrMapFrame. Not in the reference (its frame buffers are pinned host
+   memory, DeviceArray.h:50). */
+VSR_API const void *vsrMapFrameDevice(VSRDevice d, VSRFrame f, const char *channel,
+                                      uint32_t *width, uint32_t *height, VSRDataType *pixelType);
+
+/* The CUDA stream the device renders on (cudaStream_t), so that callers can
+   order their own GPU work against frames. */
+VSR_API void *vsrDeviceStream(VSRDevice d);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

@@ -1,0 +1,1616 @@
+// CPU oracle: restatement of the anari-visionaray CPU device's per-pixel hot
+// path (raycast + pathtrace renderers, volume marching, delta tracking, frame
+// accumulation).
+//
+// TEST INFRASTRUCTURE ONLY: the checker for the CUDA product path, and the
+// timed CPU baseline. The product never links this file.
+//
+// Citations are file:line in the reference project. Arithmetic follows the
+// reference's order; helpers that live in the (un-vendored) Visionaray
+// library are restated in oracle_math.h with their conventions named.
+#include "vsr_oracle.h"
+#include "oracle_math.h"
+
+#include <atomic>
+#include <cstring>
+#include <memory>
+#include <thread>
+#include <vector>
+
+using namespace orc;
+
+namespace {
+
+struct Ray {
+  f3 ori, dir;
+  float tmin, tmax, time;
+};
+
+// ---------------------------------------------------------------------------
+// Affine transforms (scene/Instance.cpp:92-98: affineInv = inverse(top_left),
+// transInv = -translation, normalXfm = transpose(affineInv)).
+// ---------------------------------------------------------------------------
+struct M3 {
+  f3 c0, c1, c2; // columns
+  f3 operator*(f3 v) const { return c0 * v.x + c1 * v.y + c2 * v.z; }
+};
+
+M3 inverse3(const M3 &m) {
+  f3 a = m.c0, b = m.c1, c = m.c2;
+  f3 r0 = cross(b, c), r1 = cross(c, a), r2 = cross(a, b);
+  float det = dot(a, r0);
+  float id = 1.f / det;
+  // rows of the inverse are r0/det, r1/det, r2/det
+  M3 inv;
+  inv.c0 = f3(r0.x, r1.x, r2.x) * id;
+  inv.c1 = f3(r0.y, r1.y, r2.y) * id;
+  inv.c2 = f3(r0.z, r1.z, r2.z) * id;
+  return inv;
+}
+
+M3 transpose3(const M3 &m) {
+  M3 t;
+  t.c0 = f3(m.c0.x, m.c1.x, m.c2.x);
+  t.c1 = f3(m.c0.y, m.c1.y, m.c2.y);
+  t.c2 = f3(m.c0.z, m.c1.z, m.c2.z);
+  return t;
+}
+
+struct Inst {
+  M3 affineInv, normalXfm;
+  f3 transInv;
+  int group;
+  uint32_t userID;
+  Ray toLocal(const Ray &r) const {
+    Ray l = r;
+    l.ori = affineInv * (r.ori + transInv);
+    l.dir = affineInv * r.dir;
+    return l;
+  }
+};
+
+// ---------------------------------------------------------------------------
+// Triangles (basic_triangle v1/e1/e2, scene/surface/geometry/Triangle.cpp:76-83)
+// and a binned-SAH BVH2 per group. The BVH shape only affects speed: closest
+// hits are resolved by (t, instance, triangle) so any valid BVH gives the same
+// answer.
+// ---------------------------------------------------------------------------
+struct Tri { f3 v1, e1, e2; };
+
+struct Box {
+  f3 lo{FLT_MAX}, hi{-FLT_MAX};
+  void grow(f3 p) { lo = min3(lo, p); hi = max3(hi, p); }
+  void grow(const Box &b) { lo = min3(lo, b.lo); hi = max3(hi, b.hi); }
+  float area() const {
+    f3 d = hi - lo;
+    if (d.x < 0) return 0.f;
+    return 2.f * (d.x * d.y + d.y * d.z + d.z * d.x);
+  }
+};
+
+struct BNode {
+  Box box;
+  int32_t first; // leaf: first index into prim; inner: left child (right = first+1)
+  int32_t count; // >0 leaf
+};
+
+struct GroupBVH {
+  std::vector<BNode> nodes;
+  std::vector<int32_t> prim; // global triangle ids
+};
+
+void buildBVH(GroupBVH &bvh, const std::vector<Tri> &tris, int begin, int end) {
+  int n = end - begin;
+  bvh.nodes.clear();
+  bvh.prim.resize(n);
+  if (n <= 0) return;
+  std::vector<Box> pb(n);
+  std::vector<f3> pc(n);
+  for (int i = 0; i < n; ++i) {
+    const Tri &t = tris[begin + i];
+    Box b;
+    b.grow(t.v1);
+    b.grow(t.v1 + t.e1);
+    b.grow(t.v1 + t.e2);
+    pb[i] = b;
+    pc[i] = (b.lo + b.hi) * 0.5f;
+    bvh.prim[i] = begin + i;
+  }
+  std::vector<int32_t> idx(n);
+  for (int i = 0; i < n; ++i) idx[i] = i;
+  bvh.nodes.reserve(2 * n);
+  bvh.nodes.push_back(BNode{});
+  struct Task { int node, lo, hi; };
+  std::vector<Task> stack{{0, 0, n}};
+  const int kBins = 16;
+  while (!stack.empty()) {
+    Task tk = stack.back();
+    stack.pop_back();
+    Box nb, cb;
+    for (int i = tk.lo; i < tk.hi; ++i) { nb.grow(pb[idx[i]]); cb.grow(pc[idx[i]]); }
+    int cnt = tk.hi - tk.lo;
+    bvh.nodes[tk.node].box = nb;
+    if (cnt <= 4) {
+      bvh.nodes[tk.node].first = tk.lo;
+      bvh.nodes[tk.node].count = cnt;
+      continue;
+    }
+    int bestAxis = -1, bestSplit = -1;
+    float bestCost = FLT_MAX;
+    for (int axis = 0; axis < 3; ++axis) {
+      float clo = cb.lo[axis], chi = cb.hi[axis];
+      if (!(chi > clo)) continue;
+      Box bins[kBins];
+      int bc[kBins] = {0};
+      float scale = kBins / (chi - clo);
+      for (int i = tk.lo; i < tk.hi; ++i) {
+        int b = std::min(kBins - 1, (int)((pc[idx[i]][axis] - clo) * scale));
+        bins[b].grow(pb[idx[i]]);
+        bc[b]++;
+      }
+      Box rb[kBins];
+      int rc[kBins];
+      Box acc;
+      int ac = 0;
+      for (int b = kBins - 1; b > 0; --b) {
+        acc.grow(bins[b]);
+        ac += bc[b];
+        rb[b] = acc;
+        rc[b] = ac;
+      }
+      Box lb;
+      int lc = 0;
+      for (int b = 0; b < kBins - 1; ++b) {
+        lb.grow(bins[b]);
+        lc += bc[b];
+        if (lc == 0 || rc[b + 1] == 0) continue;
+        float cost = lb.area() * lc + rb[b + 1].area() * rc[b + 1];
+        if (cost < bestCost) { bestCost = cost; bestAxis = axis; bestSplit = b; }
+      }
+    }
+    int mid;
+    if (bestAxis < 0) {
+      mid = tk.lo + cnt / 2;
+    } else {
+      float clo = cb.lo[bestAxis], chi = cb.hi[bestAxis];
+      float scale = kBins / (chi - clo);
+      int *l = &idx[tk.lo], *r = &idx[tk.hi - 1];
+      while (l <= r) {
+        int b = std::min(kBins - 1, (int)((pc[*l][bestAxis] - clo) * scale));
+        if (b <= bestSplit) ++l;
+        else { std::swap(*l, *r); --r; }
+      }
+      mid = (int)(l - &idx[0]);
+      if (mid == tk.lo || mid == tk.hi) mid = tk.lo + cnt / 2;
+    }
+    int left = (int)bvh.nodes.size();
+    bvh.nodes.push_back(BNode{});
+    bvh.nodes.push_back(BNode{});
+    bvh.nodes[tk.node].first = left;
+    bvh.nodes[tk.node].count = 0;
+    stack.push_back({left, tk.lo, mid});
+    stack.push_back({left + 1, mid, tk.hi});
+  }
+  std::vector<int32_t> p2(n);
+  for (int i = 0; i < n; ++i) p2[i] = begin + idx[i];
+  bvh.prim.swap(p2);
+}
+
+// ---------------------------------------------------------------------------
+// Volumes: structuredRegular field + transferFunction1D.
+// ---------------------------------------------------------------------------
+struct Vol {
+  const OrVolume *v;
+  Box bounds;           // StructuredRegularField.cpp:90-93
+  f3 S, T;              // voxel space: S * (P + T), StructuredRegularField.cpp:37-39
+  float cellSize;       // min(spacing), :40
+  int gdims[3] = {0, 0, 0};
+  std::vector<float> maxOpacity;
+  f3 pointToVoxelSpace(f3 p) const { return S * (p + T); }
+  f3 vectorToVoxelSpace(f3 d) const { return S * d; }
+};
+
+// tex3D with normalized coordinates, linear filter, clamp addressing; texel
+// i is centred at (i+0.5)/N (sampleField, DeviceCopyableObjects.h:478-481).
+float sampleField(const OrVolume *v, f3 P) {
+  const int nx = v->dims[0], ny = v->dims[1], nz = v->dims[2];
+  float x = P.x * nx - 0.5f, y = P.y * ny - 0.5f, z = P.z * nz - 0.5f;
+  float fx0 = std::floor(x), fy0 = std::floor(y), fz0 = std::floor(z);
+  float fx = x - fx0, fy = y - fy0, fz = z - fz0;
+  auto cl = [](float f, int n) {
+    return f < 0.f ? 0 : (f > (float)(n - 1) ? n - 1 : (int)f);
+  };
+  int x0 = cl(fx0, nx), x1 = cl(fx0 + 1.f, nx);
+  int y0 = cl(fy0, ny), y1 = cl(fy0 + 1.f, ny);
+  int z0 = cl(fz0, nz), z1 = cl(fz0 + 1.f, nz);
+  const float *d = v->data;
+  auto at = [&](int i, int j, int k) { return d[(size_t(k) * ny + j) * nx + i]; };
+  float c00 = lerpf(at(x0, y0, z0), at(x1, y0, z0), fx);
+  float c10 = lerpf(at(x0, y1, z0), at(x1, y1, z0), fx);
+  float c01 = lerpf(at(x0, y0, z1), at(x1, y0, z1), fx);
+  float c11 = lerpf(at(x0, y1, z1), at(x1, y1, z1), fx);
+  float c0 = lerpf(c00, c10, fy);
+  float c1 = lerpf(c01, c11, fy);
+  return lerpf(c0, c1, fz);
+}
+
+// tex1D over the TF table, normalized coordinates, linear, clamp.
+f4 tfTex(const OrVolume *v, float u) {
+  const int n = v->tfSize;
+  float x = u * n - 0.5f;
+  float f0 = std::floor(x);
+  float f = x - f0;
+  int i0 = f0 < 0.f ? 0 : (f0 > (float)(n - 1) ? n - 1 : (int)f0);
+  int i1 = (f0 + 1.f) < 0.f ? 0 : ((f0 + 1.f) > (float)(n - 1) ? n - 1 : (int)(f0 + 1.f));
+  const float *a = v->tf + 4 * i0, *b = v->tf + 4 * i1;
+  return f4(lerpf(a[0], b[0], f), lerpf(a[1], b[1], f), lerpf(a[2], b[2], f), lerpf(a[3], b[3], f));
+}
+
+// postClassify, DeviceCopyableObjects.h:614-619.
+f4 postClassify(const OrVolume *v, float val) {
+  val = (val - v->valueRange[0]) / (v->valueRange[1] - v->valueRange[0]);
+  return tfTex(v, val);
+}
+
+// projectOnGrid / linearIndex, GridAccel-common.h:9-25.
+void projectOnGrid(f3 V, const int *dims, const Box &wb, int *out) {
+  f3 V01 = (V - wb.lo) / (wb.hi - wb.lo);
+  for (int a = 0; a < 3; ++a) {
+    int c = (int)(V01[a] * (float)dims[a]);
+    out[a] = std::min(std::max(c, 0), dims[a] - 1);
+  }
+}
+
+void buildMajorants(Vol &vol) {
+  const OrVolume *v = vol.v;
+  if (v->gridMethod == OR_GRID_REFERENCE) {
+    // StructuredRegularField::buildGrid (:95-127) + rasterizeBox
+    // (GridAccel.h:51-68) + computeMaxOpacities (GridAccel.cpp:69-108).
+    for (int a = 0; a < 3; ++a) vol.gdims[a] = v->gridDims[a];
+    size_t nc = size_t(vol.gdims[0]) * vol.gdims[1] * vol.gdims[2];
+    std::vector<float> vmin(nc, FLT_MAX), vmax(nc, -FLT_MAX);
+    f3 org(v->origin[0], v->origin[1], v->origin[2]);
+    f3 sp(v->spacing[0], v->spacing[1], v->spacing[2]);
+    for (int z = 0; z < v->dims[2]; ++z)
+      for (int y = 0; y < v->dims[1]; ++y)
+        for (int x = 0; x < v->dims[0]; ++x) {
+          f3 xyz((float)x, (float)y, (float)z);
+          f3 P = org + xyz * sp;
+          float value = sampleField(v, vol.pointToVoxelSpace(P));
+          Box cell;
+          cell.lo = org + xyz * sp;
+          cell.hi = org + (xyz + f3(1.f)) * sp;
+          int lo[3], hi[3];
+          projectOnGrid(cell.lo, vol.gdims, vol.bounds, lo);
+          projectOnGrid(cell.hi, vol.gdims, vol.bounds, hi);
+          for (int mz = lo[2]; mz <= hi[2]; ++mz)
+            for (int my = lo[1]; my <= hi[1]; ++my)
+              for (int mx = lo[0]; mx <= hi[0]; ++mx) {
+                size_t id = (size_t(mz) * vol.gdims[1] + my) * vol.gdims[0] + mx;
+                vmin[id] = std::min(vmin[id], value);
+                vmax[id] = std::max(vmax[id], value);
+              }
+        }
+    vol.maxOpacity.assign(nc, 0.f);
+    const int N = v->tfSize;
+    for (size_t c = 0; c < nc; ++c) {
+      if (vmax[c] < vmin[c]) { vol.maxOpacity[c] = 0.f; continue; }
+      float lo = (vmin[c] - v->valueRange[0]) / (v->valueRange[1] - v->valueRange[0]);
+      float hi = (vmax[c] - v->valueRange[0]) / (v->valueRange[1] - v->valueRange[0]);
+      int ilo = std::min(std::max((int)(lo * (N - 1)), 0), N - 1);
+      int ihi = std::min(std::max((int)(hi * (N - 1)) + 1, 0), N - 1);
+      float m = 0.f;
+      for (int i = ilo; i <= ihi; ++i) m = std::fmax(m, tfTex(v, (i + .5f) / N).w);
+      vol.maxOpacity[c] = m;
+    }
+  } else if (v->gridMethod == OR_GRID_BRICK) {
+    // Brick majorants: cell k along an axis covers normalized coordinates
+    // [k/G, (k+1)/G]; every trilinear sample there reads texels
+    // floor(k*N/G-0.5) .. floor((k+1)*N/G-0.5)+1 (clamped), whose min/max
+    // bound the sample; the TF bins touched by [min,max] bound its alpha.
+    const int B = v->brickSize;
+    for (int a = 0; a < 3; ++a) vol.gdims[a] = (v->dims[a] + B - 1) / B;
+    size_t nc = size_t(vol.gdims[0]) * vol.gdims[1] * vol.gdims[2];
+    vol.maxOpacity.assign(nc, 0.f);
+    const int N = v->tfSize;
+    for (int kz = 0; kz < vol.gdims[2]; ++kz)
+      for (int ky = 0; ky < vol.gdims[1]; ++ky)
+        for (int kx = 0; kx < vol.gdims[0]; ++kx) {
+          int k[3] = {kx, ky, kz}, t0[3], t1[3];
+          for (int a = 0; a < 3; ++a) {
+            int n = v->dims[a], G = vol.gdims[a];
+            double lo = std::floor(double(k[a]) * n / G - 0.5);
+            double hi = std::floor(double(k[a] + 1) * n / G - 0.5) + 1.0;
+            t0[a] = (int)std::min(std::max(lo, 0.0), double(n - 1));
+            t1[a] = (int)std::min(std::max(hi, 0.0), double(n - 1));
+          }
+          float mn = FLT_MAX, mx = -FLT_MAX;
+          for (int z = t0[2]; z <= t1[2]; ++z)
+            for (int y = t0[1]; y <= t1[1]; ++y)
+              for (int x = t0[0]; x <= t1[0]; ++x) {
+                float val = v->data[(size_t(z) * v->dims[1] + y) * v->dims[0] + x];
+                mn = std::min(mn, val);
+                mx = std::max(mx, val);
+              }
+          float lo = (mn - v->valueRange[0]) / (v->valueRange[1] - v->valueRange[0]);
+          float hi = (mx - v->valueRange[0]) / (v->valueRange[1] - v->valueRange[0]);
+          int ilo = (int)std::floor(lo * N - 0.5f);
+          int ihi = (int)std::floor(hi * N - 0.5f) + 1;
+          ilo = std::min(std::max(ilo, 0), N - 1);
+          ihi = std::min(std::max(ihi, 0), N - 1);
+          float m = 0.f;
+          for (int i = ilo; i <= ihi; ++i) m = std::fmax(m, v->tf[4 * i + 3]);
+          vol.maxOpacity[(size_t(kz) * vol.gdims[1] + ky) * vol.gdims[0] + kx] = m;
+        }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Committed scene.
+// ---------------------------------------------------------------------------
+struct Scene {
+  const OrScene *src;
+  std::vector<Tri> tris;
+  std::vector<GroupBVH> bvh;
+  std::vector<Vol> vols;
+  std::vector<Inst> insts;
+};
+
+struct Counters {
+  uint64_t rays = 0, nodes = 0, tris = 0, march = 0, track = 0, cells = 0;
+};
+
+// Slab test (Visionaray intersect(ray, aabb)): tnear = max of per-axis
+// minima, tfar = min of per-axis maxima, hit = tnear <= tfar.
+struct BoxHit { bool hit; float tnear, tfar; };
+BoxHit intersectBox(const Ray &r, const Box &b) {
+  f3 inv = f3(1.f) / r.dir;
+  f3 t1 = (b.lo - r.ori) * inv, t2 = (b.hi - r.ori) * inv;
+  float tn = max_element(min3(t1, t2)), tf = min_element(max3(t1, t2));
+  return BoxHit{tn <= tf, tn, tf};
+}
+
+struct SurfHit {
+  bool hit = false;
+  float t = FLT_MAX, u = 0, v = 0;
+  int inst = -1, tri = -1;
+  f3 isect_pos;
+};
+
+// Ray/triangle test in the basic_triangle (Moller-Trumbore) form; u,v are
+// the barycentrics of v2 and v3.
+inline bool hitTri(const Ray &r, const Tri &T, float tmin, float &t, float &u, float &v) {
+  f3 s1 = cross(r.dir, T.e2);
+  float div = dot(s1, T.e1);
+  if (div == 0.f) return false;
+  float inv = 1.f / div;
+  f3 d = r.ori - T.v1;
+  float b1 = dot(d, s1) * inv;
+  if (b1 < 0.f || b1 > 1.f) return false;
+  f3 s2 = cross(d, T.e1);
+  float b2 = dot(r.dir, s2) * inv;
+  if (b2 < 0.f || b1 + b2 > 1.f) return false;
+  float tt = dot(T.e2, s2) * inv;
+  if (!(tt >= tmin)) return false;
+  t = tt; u = b1; v = b2;
+  return true;
+}
+
+// Closest hit over all instances: intersectSurfaces(Ray,TLS) with the
+// instance transform of intersect(Ray, Instance), DeviceCopyableObjects.h:
+// 1772-1839. Hits are ordered by (t, instance, triangle).
+SurfHit traceSurfaces(const Scene &sc, const Ray &ray, Counters &c) {
+  SurfHit best;
+  best.t = ray.tmax;
+  c.rays++;
+  for (size_t ii = 0; ii < sc.insts.size(); ++ii) {
+    const Inst &inst = sc.insts[ii];
+    const GroupBVH &bvh = sc.bvh[inst.group];
+    if (bvh.nodes.empty()) continue;
+    Ray l = inst.toLocal(ray);
+    f3 inv = f3(1.f) / l.dir;
+    int stack[128];
+    int sp = 0;
+    stack[sp++] = 0;
+    while (sp) {
+      const BNode &n = bvh.nodes[stack[--sp]];
+      c.nodes++;
+      f3 t1 = (n.box.lo - l.ori) * inv, t2 = (n.box.hi - l.ori) * inv;
+      float tn = std::fmax(max_element(min3(t1, t2)), l.tmin);
+      float tf = std::fmin(min_element(max3(t1, t2)), best.t);
+      if (tn > tf) continue;
+      if (n.count > 0) {
+        for (int k = 0; k < n.count; ++k) {
+          int tri = bvh.prim[n.first + k];
+          c.tris++;
+          float t, u, v;
+          if (!hitTri(l, sc.tris[tri], l.tmin, t, u, v)) continue;
+          bool closer = t < best.t ||
+                        (t == best.t && best.hit &&
+                         ((int)ii < best.inst || ((int)ii == best.inst && tri < best.tri)));
+          if (!closer) continue;
+          best.hit = true; best.t = t; best.u = u; best.v = v;
+          best.inst = (int)ii; best.tri = tri;
+          best.isect_pos = l.ori + t * l.dir;
+        }
+      } else {
+        stack[sp++] = n.first;
+        stack[sp++] = n.first + 1;
+      }
+    }
+  }
+  if (!best.hit) best.t = FLT_MAX;
+  return best;
+}
+
+// ---------------------------------------------------------------------------
+// DDA (renderer/DDA.h:12-113) with the callback func(cellID, t0, t1).
+// ---------------------------------------------------------------------------
+template <typename Func>
+void dda3(Ray ray, const int *gridDims, const Box &modelBounds, Func &&func) {
+  const float ray_tmin = ray.tmin;
+  ray.ori = ray.ori + ray.tmin * ray.dir;
+  ray.tmin = 0.f;
+  ray.tmax -= ray_tmin;
+  const f3 rcp_dir = f3(1.f) / ray.dir;
+  const f3 lo = (modelBounds.lo - ray.ori) * rcp_dir;
+  const f3 hi = (modelBounds.hi - ray.ori) * rcp_dir;
+  f3 tnear = min3(lo, hi);
+  const f3 tfar = max3(lo, hi);
+  if (ray.dir.x == 0.f) tnear.x = FLT_MAX;
+  if (ray.dir.y == 0.f) tnear.y = FLT_MAX;
+  if (ray.dir.z == 0.f) tnear.z = FLT_MAX;
+  int cell[3];
+  projectOnGrid(ray.ori, gridDims, modelBounds, cell);
+  f3 gd((float)gridDims[0], (float)gridDims[1], (float)gridDims[2]);
+  const f3 dist = max3(f3(0.f), (tfar - tnear) / gd);
+  const int step[3] = {ray.dir.x > 0.f ? 1 : -1, ray.dir.y > 0.f ? 1 : -1,
+                       ray.dir.z > 0.f ? 1 : -1};
+  const int stop[3] = {ray.dir.x > 0.f ? gridDims[0] : -1,
+                       ray.dir.y > 0.f ? gridDims[1] : -1,
+                       ray.dir.z > 0.f ? gridDims[2] : -1};
+  f3 tnext;
+  for (int a = 0; a < 3; ++a)
+    tnext[a] = ray.dir[a] > 0.f ? tnear[a] + float(cell[a] + 1) * dist[a]
+                                : tnear[a] + float(gridDims[a] - cell[a]) * dist[a];
+  float t0 = 0.f;
+  while (1) {
+    const float t1 = std::fmin(min_element(tnext), ray.tmax);
+    int id = (cell[2] * gridDims[1] + cell[1]) * gridDims[0] + cell[0];
+    if (!func(id, ray_tmin + t0, ray_tmin + t1)) return;
+    const float tc = min_element(tnext);
+    bool done = false;
+    for (int a = 0; a < 3 && !done; ++a) {
+      if (tnext[a] == tc) {
+        tnext[a] += dist[a];
+        cell[a] += step[a];
+        if (cell[a] == stop[a]) done = true;
+      }
+    }
+    if (done) break;
+    t0 = t1;
+  }
+}
+
+struct VolHit {
+  bool hit = false;
+  float t = FLT_MAX;
+  f3 albedo;
+  float Tr = 1.f;
+  int inst = -1, vol = -1;
+};
+
+// Delta tracking, intersect(Ray, Volume), DeviceCopyableObjects.h:680-796.
+// Returns true with t (object-space ray parameter) on a scattering event.
+bool deltaTrack(const Vol &vol, Ray ray, LCG &rnd, float &tHit, f3 &albedo, Counters &c) {
+  const OrVolume *v = vol.v;
+  BoxHit bh = intersectBox(ray, vol.bounds);
+  // The BVH over volumes culls boxes whose [tnear,tfar] misses [tmin,tmax].
+  if (!bh.hit || bh.tfar < ray.tmin || bh.tnear > ray.tmax) return false;
+  ray.tmin = std::fmax(ray.tmin, bh.tnear);
+  ray.tmax = std::fmin(ray.tmax, bh.tfar);
+  ray.ori = vol.pointToVoxelSpace(ray.ori);
+  ray.dir = vol.vectorToVoxelSpace(ray.dir);
+  const float dt_scale = length(ray.dir);
+  ray.dir = normalize(ray.dir);
+  ray.tmin = ray.tmin * dt_scale;
+  ray.tmax = ray.tmax * dt_scale;
+  float unitDistance = v->unitDistance * dt_scale;
+  float invUnitDistance = 1.f / unitDistance;
+  bool hit = false;
+  float ht = ray.tmax;
+  const bool gridValid = !vol.maxOpacity.empty();
+  auto woodcock = [&](int leafID, float t0, float t1) -> bool {
+    c.cells++;
+    const float majorant = gridValid ? vol.maxOpacity[leafID] : 1.f;
+    float t = t0;
+    while (1) {
+      if (majorant <= 0.f) break;
+      t -= (std::log(1.f - rnd()) / (majorant * invUnitDistance));
+      if (t >= t1) break;
+      c.track++;
+      f3 P = ray.ori + ray.dir * t;
+      f4 s = postClassify(v, sampleField(v, P));
+      float u = rnd();
+      if (s.w >= u * majorant) {
+        albedo = s.xyz();
+        hit = true;
+        ht = t;
+        return false;
+      }
+    }
+    return true;
+  };
+  if (gridValid) {
+    Box gb;
+    gb.lo = f3(0.f);
+    gb.hi = f3(1.f);
+    dda3(ray, vol.gdims, gb, woodcock);
+  } else {
+    woodcock(-1, ray.tmin, ray.tmax);
+  }
+  if (hit) tHit = ht / dt_scale;
+  return hit;
+}
+
+// intersectVolumes over the world (DeviceCopyableObjects.h:1861-1879).
+VolHit traceVolumes(const Scene &sc, const Ray &ray, LCG &rnd, Counters &c) {
+  VolHit best;
+  for (size_t ii = 0; ii < sc.insts.size(); ++ii) {
+    const Inst &inst = sc.insts[ii];
+    const OrGroup &g = sc.src->groups[inst.group];
+    for (int vi = g.volBegin; vi < g.volEnd; ++vi) {
+      Ray l = inst.toLocal(ray);
+      float t;
+      f3 alb;
+      if (deltaTrack(sc.vols[vi], l, rnd, t, alb, c) && t < best.t) {
+        best.hit = true;
+        best.t = t;
+        best.albedo = alb;
+        best.Tr = 0.f;
+        best.inst = (int)ii;
+        best.vol = vi;
+      }
+    }
+  }
+  return best;
+}
+
+// ---------------------------------------------------------------------------
+// Camera (DeviceCopyableObjects.h:2497-2600; camera/Perspective.cpp:33-44).
+// Thin-lens convention: u = 2 s.x - 1, v = 2 s.y - 1 with s the image-region
+// mapped ((x+.5)/w, (y+.5)/h); dir = normalize(u U + v V + W), |U| =
+// tan(fovy/2) aspect, |V| = tan(fovy/2), W = view direction. The lens draws
+// two random numbers per ray (used only when apertureRadius > 0); every
+// primary ray then draws one for ray.time.
+// ---------------------------------------------------------------------------
+struct Cam {
+  OrCamera c;
+  f3 U, V, W, eye;
+  float inv[16];
+};
+
+void mul44(const float *a, const float *b, float *o) {
+  for (int col = 0; col < 4; ++col)
+    for (int row = 0; row < 4; ++row) {
+      float s = 0.f;
+      for (int k = 0; k < 4; ++k) s += a[k * 4 + row] * b[col * 4 + k];
+      o[col * 4 + row] = s;
+    }
+}
+
+bool inv44(const float *m, float *out) {
+  double a[4][8];
+  for (int r = 0; r < 4; ++r)
+    for (int cidx = 0; cidx < 4; ++cidx) {
+      a[r][cidx] = m[cidx * 4 + r];
+      a[r][cidx + 4] = (r == cidx) ? 1.0 : 0.0;
+    }
+  for (int cidx = 0; cidx < 4; ++cidx) {
+    int p = cidx;
+    for (int r = cidx + 1; r < 4; ++r)
+      if (std::fabs(a[r][cidx]) > std::fabs(a[p][cidx])) p = r;
+    if (a[p][cidx] == 0.0) return false;
+    if (p != cidx)
+      for (int k = 0; k < 8; ++k) std::swap(a[p][k], a[cidx][k]);
+    double d = a[cidx][cidx];
+    for (int k = 0; k < 8; ++k) a[cidx][k] /= d;
+    for (int r = 0; r < 4; ++r)
+      if (r != cidx) {
+        double f = a[r][cidx];
+        for (int k = 0; k < 8; ++k) a[r][k] -= f * a[cidx][k];
+      }
+  }
+  for (int r = 0; r < 4; ++r)
+    for (int cidx = 0; cidx < 4; ++cidx) out[cidx * 4 + r] = (float)a[r][cidx + 4];
+  return true;
+}
+
+Cam makeCam(const OrCamera &c) {
+  Cam k;
+  k.c = c;
+  f3 dir = normalize(f3(c.direction[0], c.direction[1], c.direction[2]));
+  f3 up = normalize(f3(c.up[0], c.up[1], c.up[2]));
+  k.eye = f3(c.position[0], c.position[1], c.position[2]);
+  if (c.type == OR_CAM_PERSPECTIVE) {
+    float th = std::tan(0.5f * c.fovy);
+    k.W = dir;
+    k.U = normalize(cross(dir, up)) * (th * c.aspect);
+    k.V = normalize(cross(k.U, dir)) * th;
+  } else if (c.type == OR_CAM_ORTHO) {
+    k.U = normalize(cross(dir, up)) * (c.height * c.aspect);
+    k.V = normalize(cross(k.U, dir)) * c.height;
+    k.W = k.eye - 0.5f * k.U - 0.5f * k.V;
+  } else if (c.type == OR_CAM_OMNI) {
+    k.U = normalize(cross(dir, up));
+    k.V = normalize(cross(k.U, dir));
+    k.W = k.eye - 0.5f * k.U - 0.5f * k.V;
+  } else if (c.type == OR_CAM_MATRIX) {
+    float pv[16];
+    mul44(c.proj, c.view, pv);
+    inv44(pv, k.inv);
+  }
+  return k;
+}
+
+Ray primaryRay(const Cam &k, LCG *rng, float x, float y, float w, float h) {
+  Ray r;
+  r.tmin = 0.f;
+  r.tmax = FLT_MAX;
+  r.time = 0.5f;
+  const OrCamera &c = k.c;
+  if (c.type == OR_CAM_PERSPECTIVE) {
+    float sx = (x + 0.5f) / w, sy = (y + 0.5f) / h;
+    sx = (1.f - sx) * c.imageRegion[0] + sx * c.imageRegion[2];
+    sy = (1.f - sy) * c.imageRegion[1] + sy * c.imageRegion[3];
+    float u = 2.f * sx - 1.f, v = 2.f * sy - 1.f;
+    r.ori = k.eye;
+    r.dir = normalize(k.U * u + k.V * v + k.W);
+    float l1 = 0.f, l2 = 0.f;
+    if (rng) { l1 = (*rng)(); l2 = (*rng)(); }
+    if (c.apertureRadius > 0.f) {
+      f3 focal = r.ori + r.dir * (c.focusDistance / dot(r.dir, k.W));
+      // concentric disk (Shirley-Chiu)
+      float a = 2.f * l1 - 1.f, b = 2.f * l2 - 1.f, rr, phi;
+      if (a == 0.f && b == 0.f) { rr = 0.f; phi = 0.f; }
+      else if (std::fabs(a) > std::fabs(b)) { rr = a; phi = (kPi / 4.f) * (b / a); }
+      else { rr = b; phi = (kPi / 2.f) - (kPi / 4.f) * (a / b); }
+      float dx = rr * std::cos(phi) * c.apertureRadius, dy = rr * std::sin(phi) * c.apertureRadius;
+      r.ori = k.eye + normalize(k.U) * dx + normalize(k.V) * dy;
+      r.dir = normalize(focal - r.ori);
+    }
+  } else if (c.type == OR_CAM_MATRIX) {
+    float u = 2.f * (x + 0.5f) / w - 1.f, v = 2.f * (y + 0.5f) / h - 1.f;
+    auto xf = [&](float z) {
+      float p[4] = {u, v, z, 1.f}, o[4];
+      for (int row = 0; row < 4; ++row) {
+        o[row] = 0.f;
+        for (int col = 0; col < 4; ++col) o[row] += k.inv[col * 4 + row] * p[col];
+      }
+      return f3(o[0] / o[3], o[1] / o[3], o[2] / o[3]);
+    };
+    f3 p0 = xf(-1.f), p1 = xf(1.f);
+    r.ori = p0;
+    r.dir = normalize(p1 - p0);
+  } else if (c.type == OR_CAM_ORTHO) {
+    float sx = (x + 0.5f) / w, sy = (y + 0.5f) / h;
+    sx = (1.f - sx) * c.imageRegion[0] + sx * c.imageRegion[2];
+    sy = (1.f - sy) * c.imageRegion[1] + sy * c.imageRegion[3];
+    r.ori = k.U * sx + k.V * sy + k.W;
+    r.dir = normalize(f3(c.direction[0], c.direction[1], c.direction[2]));
+  } else if (c.type == OR_CAM_OMNI) {
+    float sx = (x + 0.5f) / w, sy = (y + 0.5f) / h;
+    float theta = kPi * sy, phi = kTwoPi * sx;
+    f3 ld(std::sin(theta) * std::cos(phi), std::cos(theta), std::sin(theta) * std::sin(phi));
+    r.ori = k.U * sx + k.V * sy + k.W;
+    r.dir = ld * f3(1.f, -1.f, 1.f);
+  }
+  if (rng) {
+    float tr = (*rng)();
+    r.time = (1.f - tr) * c.shutter[0] + tr * c.shutter[1];
+  }
+  return r;
+}
+
+// clipRay, renderer/common.h:1469-1482.
+Ray clipRay(Ray ray, const OrRenderer &R) {
+  for (int i = 0; i < R.numClipPlanes; ++i) {
+    const float *p = R.clipPlanes + 4 * i;
+    f3 N(p[0], p[1], p[2]);
+    float D = p[3];
+    float s = dot(N, ray.dir);
+    if (s != 0.f) {
+      float t = (D - dot(N, ray.ori)) / s;
+      if (s < 0.f) ray.tmin = std::fmax(ray.tmin, t);
+      else ray.tmax = std::fmin(ray.tmax, t);
+    }
+  }
+  return ray;
+}
+
+// ---------------------------------------------------------------------------
+// Materials (renderer/common.h:793-1415). Constant parameters only; tangent
+// frames are absent, so the anisotropic branches never activate (their
+// guard compares a NaN length) and are not restated.
+// ---------------------------------------------------------------------------
+inline float pow5(float f) { return f * f * f * f * f; }
+inline f3 lerpR(f3 a, f3 b, float t) { return a * (1.f - t) + b * t; }
+inline float mapRoughness(float r) { return std::fmax(0.045f, r); }
+
+inline float D_GGX(float NdotH, float roughness, float EPS) {
+  float alpha = roughness;
+  float alpha2 = alpha * alpha;
+  float d = (NdotH * alpha2 - NdotH) * NdotH + 1.f;
+  float denom = kPi * d * d;
+  return alpha2 / std::fmax(EPS, denom);
+}
+
+f3 materialColor(const OrMaterial &m) {
+  f3 base(m.baseColor[0], m.baseColor[1], m.baseColor[2]);
+  if (m.type == OR_PBR) return lerpR(base, f3(0.f), m.metallic); // getColorPBM :708-718
+  return base;
+}
+
+float materialOpacity(const OrMaterial &m) { // getOpacity :735-760
+  float op = m.opacity;
+  if (m.alphaMode == OR_ALPHA_OPAQUE) return 1.f;
+  if (m.alphaMode == OR_ALPHA_BLEND) return op;
+  return op >= m.alphaCutoff ? 1.f : 0.f;
+}
+
+f3 evalPBR(const OrMaterial &m, f3 Ns, f3 viewDir, f3 lightDir) {
+  const float metallic = m.metallic, roughness = m.roughness;
+  const float clearcoat = m.clearcoat, clearcoatRoughness = m.clearcoatRoughness;
+  const float ior = m.ior;
+  f3 sheenColor(m.sheenColor[0], m.sheenColor[1], m.sheenColor[2]);
+  const float perceptualRoughness = mapRoughness(roughness);
+  const float perceptualClearcoatRoughness = mapRoughness(clearcoatRoughness);
+  const float perceptualSheenRoughness = mapRoughness(m.sheenRoughness);
+  const float alpha = perceptualRoughness * perceptualRoughness;
+  const float clearcoatAlpha = perceptualClearcoatRoughness * perceptualClearcoatRoughness;
+  const float EPS = 1e-14f;
+  const f3 H = normalize(lightDir + viewDir);
+  const float NdotV = std::fabs(dot(Ns, viewDir)) + EPS;
+  const float NdotH = std::fmax(EPS, dot(Ns, H));
+  const float NdotL = std::fmax(EPS, dot(Ns, lightDir));
+  const float LdotH = std::fmax(EPS, dot(lightDir, H));
+  const float VdotH = std::fmax(EPS, dot(viewDir, H));
+  f3 baseColor(m.baseColor[0], m.baseColor[1], m.baseColor[2]);
+  f3 diffuseColor = lerpR(baseColor, f3(0.f), metallic);
+  float f0s = ((1.f - ior) / (1.f + ior));
+  f0s = f0s * f0s;
+  f3 f0 = lerpR(f3(f0s), baseColor, metallic);
+  f3 F = f0 + (f3(1.f) - f0) * pow5(1.f - VdotH);
+  // Fd_Burley
+  float f90 = 0.5f + 2.f * alpha * LdotH * LdotH;
+  float lightScatter = 1.f + (f90 - 1.f) * pow5(1.f - NdotL);
+  float viewScatter = 1.f + (f90 - 1.f) * pow5(1.f - NdotV);
+  f3 diffuseBRDF = diffuseColor * (lightScatter * viewScatter * kInvPi);
+  float D = D_GGX(NdotH, alpha, EPS);
+  // V_SmithGGXCorrelated as written at renderer/common.h:891-899
+  float a2 = alpha * alpha;
+  float GGXV = NdotL / (NdotV + std::sqrt(a2 + (1.f - a2) * NdotV * NdotV));
+  float GGXL = NdotV / (NdotL + std::sqrt(a2 + (1.f - a2) * NdotL * NdotL));
+  float V = 0.5f / (GGXV + GGXL);
+  f3 specularBRDF = F * (D * V);
+  float Dc = D_GGX(NdotH, clearcoatAlpha, EPS);
+  float Vc = 0.25f / std::fmax(EPS, LdotH * LdotH);
+  float Fc = (0.04f + (1.f - 0.04f) * pow5(1.f - LdotH)) * clearcoat;
+  float Frc = (Dc * Vc) * Fc;
+  float sheenAlphaInv = 1.f / perceptualSheenRoughness;
+  float cos2h = NdotH * NdotH;
+  float sin2h = std::fmax(1.f - cos2h, 0.0078125f);
+  f3 Ds = sheenColor * ((2.f + sheenAlphaInv) * std::pow(sin2h, sheenAlphaInv * 0.5f) / kTwoPi);
+  return ((diffuseBRDF + specularBRDF) * (1.f - Fc) + f3(Frc)) + Ds;
+}
+
+f3 evalMaterial(const OrMaterial &m, f3 Ns, f3 viewDir, f3 lightDir) {
+  if (m.type == OR_MATTE) return materialColor(m) * kInvPi;
+  return evalPBR(m, Ns, viewDir, lightDir);
+}
+
+struct BSDFSample { f3 dir, f; float pdf, cosT; };
+
+f3 sampleGGXVNDF(f3 V, float ax, float ay, float U1, float U2) {
+  f3 Vh = normalize(V * f3(ax, ay, 1.f));
+  float lensq = Vh.x * Vh.x + Vh.y * Vh.y;
+  f3 T1 = lensq > 0.f ? f3(-Vh.y, Vh.x, 0.f) / std::sqrt(lensq) : f3(1.f, 0.f, 0.f);
+  f3 T2 = cross(Vh, T1);
+  float r = std::sqrt(U1);
+  float phi = kTwoPi * U2;
+  float t1 = r * std::cos(phi);
+  float t2 = r * std::sin(phi);
+  float s = 0.5f * (1.f + Vh.z);
+  t2 = (1.f - s) * std::sqrt(std::fmax(0.f, 1.f - t1 * t1)) + s * t2;
+  f3 Nh = t1 * T1 + t2 * T2 + std::sqrt(1.f - t1 * t1 - t2 * t2) * Vh;
+  return normalize(f3(Nh.x * ax, Nh.y * ay, std::fmax(0.f, Nh.z)));
+}
+
+void pdfGGXVNDF(f3 L, f3 V, float ax, float eta_i, float eta_t, f3 Ns, float &pdfSpec,
+                float &pdfTrans) {
+  const float EPS = 1e-14f;
+  pdfSpec = 0.f;
+  pdfTrans = 0.f;
+  const float NdotL = dot(Ns, L);
+  const float NdotV = std::fmax(EPS, dot(Ns, V));
+  if (NdotL > 0.f) {
+    f3 H = V + L;
+    float lenH = length(H);
+    if (lenH > 1e-4f) {
+      H /= lenH;
+      float NdotH = std::fmax(EPS, dot(Ns, H));
+      const float ax2 = ax * ax;
+      float D = D_GGX(NdotH, ax, EPS);
+      float G1 = 2.f * NdotV / (NdotV + std::sqrt(ax2 + (1.f - ax2) * NdotV * NdotV));
+      pdfSpec = (D * G1) / (4.f * NdotV);
+    }
+  } else if (NdotL < 0.f) {
+    f3 H = -(V * eta_i + L * eta_t);
+    float lenH = length(H);
+    if (lenH > 1e-4f) {
+      H /= lenH;
+      if (dot(Ns, H) < 0.f) H = -H;
+      const float alpha2 = ax * ax;
+      float NdotH = std::fmax(EPS, dot(Ns, H));
+      float LdotH = std::fabs(dot(L, H));
+      float VdotH = std::fabs(dot(V, H));
+      if (VdotH > 0.f && LdotH > 0.f) {
+        float D = D_GGX(NdotH, ax, EPS);
+        float G1 = 2.f * NdotV / (NdotV + std::sqrt(alpha2 + (1.f - alpha2) * NdotV * NdotV));
+        float pdfNe = (D * G1 * VdotH) / NdotV;
+        float denom = (eta_i * VdotH + eta_t * LdotH);
+        float jacobian = (eta_t * eta_t * LdotH) / (denom * denom);
+        pdfTrans = pdfNe * jacobian;
+      }
+    }
+  }
+}
+
+// sampleMaterial, renderer/common.h:1371-1415 (and :1209-1368 for PBR).
+// Two-argument calls such as cosine_sample_hemisphere(rnd(), rnd()) draw
+// their arguments left to right.
+BSDFSample sampleMaterial(const OrMaterial &m, f3 Ng, f3 Ns, f3 viewDir, LCG &rnd) {
+  BSDFSample res;
+  f3 w = faceforward(Ns, viewDir, Ng);
+  f3 v = std::fabs(w.x) > std::fabs(w.y) ? normalize(f3(-w.z, 0.f, w.x))
+                                         : normalize(f3(0.f, w.z, -w.y));
+  f3 u = cross(v, w);
+  if (m.type == OR_MATTE) {
+    float u1 = rnd(), u2 = rnd();
+    f3 sp = cosine_sample_hemisphere(u1, u2);
+    res.dir = normalize(sp.x * u + sp.y * v + sp.z * w);
+    res.pdf = std::fmax(0.f, dot(Ns, res.dir)) * kInvPi;
+  } else {
+    const float EPS = 1e-14f;
+    const float metallic = m.metallic;
+    const float alpha = mapRoughness(m.roughness) * mapRoughness(m.roughness);
+    const float ccR = mapRoughness(m.clearcoatRoughness);
+    const float clearcoatAlpha = ccR * ccR;
+    const float transmission = m.transmission, ior = m.ior, clearcoat = m.clearcoat;
+    const float NdotV = std::fmax(EPS, dot(Ns, viewDir));
+    f3 baseColor(m.baseColor[0], m.baseColor[1], m.baseColor[2]);
+    f3 diffuseColor = lerpR(baseColor, f3(0.f), metallic);
+    float f0s = ((1.f - ior) / (1.f + ior));
+    f0s = f0s * f0s;
+    f3 f0 = lerpR(f3(f0s), baseColor, metallic);
+    f3 F = f0 + (f3(1.f) - f0) * pow5(1.f - NdotV);
+    const float fClear = clearcoat * 0.04f;
+    const float baseEnergy = 1.f - fClear;
+    const float fSpec = rgb_to_luminance(F);
+    const float remainingEnergy = baseEnergy * (1.f - fSpec);
+    float wDiff = rgb_to_luminance(diffuseColor) * remainingEnergy * (1.f - transmission);
+    float wSpec = baseEnergy * fSpec;
+    float wTrans = remainingEnergy * transmission;
+    float wClear = fClear;
+    float wSum = wDiff + wSpec + wTrans + wClear;
+    float pDiff = wSum > 0.f ? wDiff / wSum : 0.0f;
+    float pSpec = wSum > 0.f ? wSpec / wSum : 0.333f;
+    float pTrans = wSum > 0.f ? wTrans / wSum : 0.667f;
+    float pClear = 1.f - pDiff - pSpec - pTrans;
+    float lobe = rnd();
+    f3 V(dot(u, viewDir), dot(v, viewDir), dot(w, viewDir));
+    bool entering = dot(Ns, viewDir) > 0.f;
+    float eta_i = entering ? 1.0f : ior;
+    float eta_t = entering ? ior : 1.0f;
+    auto toWorld = [&](f3 n) { return u * n.x + v * n.y + w * n.z; };
+    if (lobe < pDiff) {
+      float u1 = rnd(), u2 = rnd();
+      f3 sp = cosine_sample_hemisphere(u1, u2);
+      res.dir = normalize(sp.x * u + sp.y * v + sp.z * w);
+    } else if (lobe < pDiff + pSpec) {
+      float u1 = rnd(), u2 = rnd();
+      f3 Ne = sampleGGXVNDF(V, alpha, alpha, u1, u2);
+      res.dir = reflect(viewDir, toWorld(Ne));
+    } else if (lobe < pDiff + pSpec + pTrans) {
+      float u1 = rnd(), u2 = rnd();
+      f3 Ne = sampleGGXVNDF(V, alpha, alpha, u1, u2);
+      if (dot(V, Ne) < 0.f) Ne = -Ne;
+      res.dir = refract(viewDir, toWorld(Ne), eta_t / eta_i);
+      if (length(res.dir) < 1e-4f) res.dir = reflect(viewDir, toWorld(Ne));
+    } else {
+      float u1 = rnd(), u2 = rnd();
+      f3 Ne = sampleGGXVNDF(V, clearcoatAlpha, clearcoatAlpha, u1, u2);
+      res.dir = reflect(viewDir, toWorld(Ne));
+    }
+    float pdfDiff = std::fmax(0.f, dot(Ns, res.dir)) * kInvPi;
+    float pdfSpec = 0.f, pdfTrans = 0.f;
+    pdfGGXVNDF(res.dir, viewDir, alpha, eta_i, eta_t, Ns, pdfSpec, pdfTrans);
+    float pdfClear = 0.f, dummy = 0.f;
+    float ceta_i = entering ? 1.0f : 1.5f;
+    float ceta_t = entering ? 1.5f : 1.0f;
+    pdfGGXVNDF(res.dir, viewDir, clearcoatAlpha, ceta_i, ceta_t, Ns, pdfClear, dummy);
+    res.pdf = pDiff * pdfDiff + pSpec * pdfSpec + pTrans * pdfTrans + pClear * pdfClear;
+  }
+  res.cosT = std::fmax(0.f, dot(Ns, res.dir));
+  res.f = evalMaterial(m, Ns, viewDir, res.dir);
+  return res;
+}
+
+// ---------------------------------------------------------------------------
+// Lights: directional (scene/light/Directional.cpp:30-40; sampleLight,
+// renderer/common.h:1432-1466). The stored direction is -direction; with
+// angularDiameter == 0 no random number is drawn, dist = FLT_MAX, pdf = 1,
+// dist2 = 1. A positive angular diameter samples a uniform cone (2 draws).
+// ---------------------------------------------------------------------------
+struct LightSample { f3 intensity, dir; float pdf = 0.f, dist = 0.f, dist2 = 0.f; };
+
+LightSample sampleLight(const OrLight &L, LCG &rnd) {
+  LightSample s;
+  f3 d = -normalize(f3(L.direction[0], L.direction[1], L.direction[2]));
+  if (L.angularDiameter > 0.f) {
+    float cosMax = std::cos(0.5f * L.angularDiameter);
+    float u1 = rnd(), u2 = rnd();
+    float cz = 1.f - u1 * (1.f - cosMax);
+    float sz = std::sqrt(std::fmax(0.f, 1.f - cz * cz));
+    float phi = kTwoPi * u2;
+    f3 a, b;
+    make_orthonormal_basis(a, b, d);
+    d = normalize(a * (sz * std::cos(phi)) + b * (sz * std::sin(phi)) + d * cz);
+  }
+  s.dir = d;
+  s.dist = FLT_MAX;
+  s.pdf = 1.f;
+  s.dist2 = 1.f;
+  s.intensity = f3(L.color[0], L.color[1], L.color[2]) * L.irradiance;
+  return s;
+}
+
+inline float safe_rcp(float f) { return f > 0.f ? 1.f / f : 0.f; }
+
+struct PixelSample {
+  f4 color;
+  float depth = 1e31f;
+  f3 Ng, albedo;
+};
+
+// Raycast renderSample, renderer/Raycast_impl.cpp:10-243.
+PixelSample raycastSample(const Scene &sc, const OrRenderer &R, Ray ray, Counters &c) {
+  PixelSample result;
+  f4 bgColor(R.background[0], R.background[1], R.background[2], R.background[3]);
+  result.color = bgColor;
+  result.depth = 1e31f;
+  if (sc.insts.empty()) return result;
+  const OrScene &S = *sc.src;
+  SurfHit hr = traceSurfaces(sc, ray, c);
+  bool hit = false;
+  f3 surfaceColor(0.f);
+  float surfaceAlpha = 0.f;
+  while (true) {
+    if (!hr.hit) break;
+    const Inst &inst = sc.insts[hr.inst];
+    uint32_t surf = S.triSurface[hr.tri];
+    const OrMaterial &mat = S.surfMaterial[surf];
+    f3 hitPos = ray.ori + hr.t * ray.dir;
+    const Tri &T = sc.tris[hr.tri];
+    f3 gn = normalize(cross(T.e1, T.e2));
+    f3 sn = gn;
+    gn = normalize(inst.normalXfm * gn);
+    sn = normalize(inst.normalXfm * sn);
+    f3 color = materialColor(mat);
+    f3 shadedColor(0.f);
+    f3 viewDir = -ray.dir;
+    for (int li = 0; li < S.numLights; ++li) {
+      LCG dummy(0, 0);
+      LightSample ls = sampleLight(S.lights[li], dummy);
+      f3 lightDir = normalize(ls.dir);
+      f3 lightIntensity = ls.intensity * safe_rcp(ls.dist2);
+      const float NdotL = std::fmax(0.f, dot(sn, lightDir));
+      f3 bsdf = evalMaterial(mat, sn, normalize(viewDir), lightDir);
+      shadedColor += bsdf * lightIntensity * NdotL * safe_rcp(ls.pdf);
+    }
+    shadedColor += color * f3(R.ambientColor[0], R.ambientColor[1], R.ambientColor[2]) *
+                   R.ambientRadiance;
+    float a = materialOpacity(mat);
+    surfaceColor += (1.f - surfaceAlpha) * a * shadedColor;
+    surfaceAlpha += (1.f - surfaceAlpha) * a;
+    if (!hit) {
+      result.depth = hr.t;
+      result.Ng = gn;
+      result.albedo = color;
+    }
+    hit = true;
+    if (surfaceAlpha < 0.999f) {
+      const float eps = epsilonFrom(hitPos, ray.dir, hr.t);
+      ray.tmin = hr.t + eps;
+      hr = traceSurfaces(sc, ray, c);
+    } else {
+      ray.tmax = hr.t;
+      break;
+    }
+  }
+  result.color = over(f4(surfaceColor, surfaceAlpha), bgColor);
+
+  // intersectVolumeBounds: closest volume box entry.
+  int vInst = -1, vIdx = -1;
+  float vT = FLT_MAX;
+  for (size_t ii = 0; ii < sc.insts.size(); ++ii) {
+    const Inst &inst = sc.insts[ii];
+    const OrGroup &g = S.groups[inst.group];
+    for (int vi = g.volBegin; vi < g.volEnd; ++vi) {
+      Ray l = inst.toLocal(ray);
+      BoxHit bh = intersectBox(l, sc.vols[vi].bounds);
+      bool h = bh.hit && (bh.tfar >= l.tmin) && (bh.tnear <= l.tmax);
+      float t = std::fmax(l.tmin, bh.tnear);
+      if (h && t < vT) { vT = t; vInst = (int)ii; vIdx = vi; }
+    }
+  }
+  if (vIdx >= 0) {
+    const Vol &vol = sc.vols[vIdx];
+    Ray l = sc.insts[vInst].toLocal(ray);
+    // rayMarchVolume<0>, renderer/VolumeIntegration.h:374-468.
+    BoxHit bh = intersectBox(l, vol.bounds);
+    l.tmin = std::fmax(l.tmin, bh.tnear);
+    l.tmax = std::fmin(l.tmax, bh.tfar);
+    l.ori = vol.pointToVoxelSpace(l.ori);
+    l.dir = vol.vectorToVoxelSpace(l.dir);
+    float dt = vol.cellSize * (R.volumeSamplingRate > 0.f ? 1.f / R.volumeSamplingRate : 0.f);
+    f3 color(0.f);
+    float alpha = 0.f;
+    float t = l.tmin;
+    float transmittance = 1.f;
+    const float expo = dt / vol.v->unitDistance;
+    for (; t <= l.tmax && alpha < 0.99f; t += dt) {
+      f3 P = l.ori + l.dir * t;
+      c.march++;
+      float v = sampleField(vol.v, P);
+      f4 s = postClassify(vol.v, v);
+      float stepTransmittance = std::pow(1.f - s.w, expo);
+      color += transmittance * (1.f - stepTransmittance) * s.xyz();
+      alpha += transmittance * (1.f - stepTransmittance);
+      transmittance *= stepTransmittance;
+    }
+    result.color = over(alpha * f4(color, 1.f), result.color);
+    result.Ng = f3(0.f);
+    result.albedo = f3(0.f);
+  }
+  return result;
+}
+
+enum RayType { Radiance, Shadow, AO, Miss };
+
+struct HitRec {
+  SurfHit surface;
+  VolHit volume;
+  bool hit = false, volumeHit = false;
+};
+
+// intersectAll (renderer/common.h:1605-1620) with intersectSurfaces<1>
+// (:1502-1543): one random number is drawn per surface hit for stochastic
+// opacity, then the volumes are tracked with the same generator.
+HitRec intersectAll(const Scene &sc, const Ray &ray, LCG &rnd, Counters &c) {
+  HitRec h;
+  const OrScene &S = *sc.src;
+  Ray r = ray;
+  SurfHit hr = traceSurfaces(sc, r, c);
+  while (hr.hit) {
+    const OrMaterial &mat = S.surfMaterial[S.triSurface[hr.tri]];
+    float opacity = materialOpacity(mat);
+    float u = rnd();
+    if (u > opacity) {
+      f3 hitPos = r.ori + hr.t * r.dir;
+      const float eps = epsilonFrom(hitPos, r.dir, hr.t);
+      r.tmin = hr.t + eps;
+      hr = traceSurfaces(sc, r, c);
+    } else {
+      break;
+    }
+  }
+  h.surface = hr;
+  h.volume = traceVolumes(sc, ray, rnd, c);
+  h.hit = h.surface.hit || h.volume.hit;
+  h.volumeHit = h.volume.hit && (!h.surface.hit || h.volume.t < h.surface.t);
+  return h;
+}
+
+struct ShadeState {
+  f3 baseColor, shadedColor, hitPosOff, sn;
+  int aoSamples = 0;
+  float aoWeights = 0.f, aoCount = 0.f;
+  BSDFSample bsdf{};
+  LightSample light{};
+  float misWeightNEE = 0.f;
+  RayType nextType = Miss;
+  Ray nextRay{};
+  float visLight = 1.f, visAO = 1.f;
+};
+
+// shade(), renderer/Pathtrace_impl.cpp:93-487 (default render mode).
+void shade(const Scene &sc, const OrRenderer &R, LCG &rnd, const Ray &ray, RayType rayType,
+           const HitRec &hitRec, ShadeState &ss, PixelSample &result, unsigned bounceID) {
+  const OrScene &S = *sc.src;
+  ss.nextType = Miss;
+  if (rayType == Radiance) {
+    ss.baseColor = f3(0.f);
+    ss.visLight = 1.f;
+    ss.visAO = 1.f;
+    ss.aoSamples = 0;
+    ss.aoWeights = 0.f;
+    ss.aoCount = 0.f;
+    if (!hitRec.hit) {
+      ss.shadedColor = f3(0.f);
+      ss.nextType = Miss;
+      return;
+    }
+    f3 hitPos, gn, sn, color;
+    float eps;
+    f3 viewDir = -normalize(ray.dir);
+    const OrMaterial *mat = nullptr;
+    if (hitRec.volumeHit) {
+      const VolHit &hv = hitRec.volume;
+      const Inst &inst = sc.insts[hv.inst];
+      hitPos = ray.ori + hv.t * ray.dir;
+      eps = epsilonFrom(hitPos, ray.dir, hv.t);
+      gn = f3(0.f);
+      if (R.ambientSamples > 0 && length(gn) < 1e-3f) {
+        float u1 = rnd(), u2 = rnd();
+        gn = uniform_sample_sphere(u1, u2);
+      }
+      sn = gn;
+      gn = inst.normalXfm * gn;
+      sn = inst.normalXfm * sn;
+      sn = faceforward(sn, viewDir, gn);
+      gn = faceforward(gn, viewDir, gn);
+      color = hv.albedo;
+      if (bounceID == 0) result.depth = hv.t;
+    } else {
+      const SurfHit &hr = hitRec.surface;
+      const Inst &inst = sc.insts[hr.inst];
+      hitPos = ray.ori + hr.t * ray.dir;
+      eps = epsilonFrom(hitPos, ray.dir, hr.t);
+      mat = &S.surfMaterial[S.triSurface[hr.tri]];
+      const Tri &T = sc.tris[hr.tri];
+      gn = normalize(cross(T.e1, T.e2));
+      sn = gn;
+      gn = normalize(inst.normalXfm * gn);
+      sn = normalize(inst.normalXfm * sn);
+      sn = faceforward(sn, viewDir, gn);
+      gn = faceforward(gn, viewDir, gn);
+      color = materialColor(*mat);
+      if (bounceID == 0) result.depth = hr.t;
+    }
+    if (bounceID == 0) {
+      result.Ng = gn;
+      result.albedo = color;
+    }
+    ss.sn = sn;
+    ss.hitPosOff = hitPos + sn * eps;
+    int lightID = -1;
+    if (S.numLights > 0) {
+      float r = rnd();
+      lightID = int(r * S.numLights);
+      if (lightID == S.numLights) lightID = 0;
+      ss.light = sampleLight(S.lights[lightID], rnd);
+    }
+    f3 lightDir = normalize(ss.light.dir);
+    f3 lightIntensity = ss.light.intensity * safe_rcp(ss.light.dist2);
+    const float NdotL = std::fmax(0.f, dot(sn, lightDir));
+    if (hitRec.volumeHit) {
+      const f3 &alb = hitRec.volume.albedo;
+      ss.shadedColor = alb * lightIntensity * safe_rcp(ss.light.pdf) * safe_rcp(ss.light.dist2);
+      float u1 = rnd(), u2 = rnd();
+      ss.bsdf.dir = uniform_sample_sphere(u1, u2);
+      ss.bsdf.f = alb;
+      ss.bsdf.pdf = 1.f;
+      ss.bsdf.cosT = 1.f;
+    } else {
+      f3 f = evalMaterial(*mat, sn, viewDir, lightDir);
+      ss.shadedColor = f * lightIntensity * NdotL * safe_rcp(ss.light.pdf) * float(S.numLights);
+      ss.bsdf = sampleMaterial(*mat, gn, sn, viewDir, rnd);
+    }
+    ss.misWeightNEE = 0.f;
+    if (S.numLights > 0) ss.misWeightNEE = 1.f; // delta light (directional)
+    ss.baseColor = color;
+  }
+
+  auto prepShadow = [&]() {
+    ss.nextType = Shadow;
+    ss.nextRay.ori = ss.hitPosOff;
+    ss.nextRay.dir = normalize(ss.light.dir);
+    ss.nextRay.tmin = 0.f;
+    ss.nextRay.tmax = ss.light.dist;
+    ss.nextRay.time = ray.time;
+  };
+  auto prepAO = [&]() {
+    f3 u, v, w = ss.sn;
+    make_orthonormal_basis(u, v, w);
+    float u1 = rnd(), u2 = rnd();
+    f3 sp = cosine_sample_hemisphere(u1, u2);
+    ss.nextType = AO;
+    ss.nextRay.ori = ss.hitPosOff;
+    ss.nextRay.dir = normalize(sp.x * u + sp.y * v + sp.z * w);
+    ss.nextRay.tmin = 0.f;
+    ss.nextRay.tmax = R.occlusionDistance;
+    ss.nextRay.time = ray.time;
+  };
+  auto prepBounce = [&]() {
+    ss.nextType = Radiance;
+    ss.nextRay.ori = ss.hitPosOff;
+    ss.nextRay.dir = normalize(ss.bsdf.dir);
+    ss.nextRay.tmin = 0.f;
+    ss.nextRay.tmax = 1e31f;
+    ss.nextRay.time = ray.time;
+  };
+
+  if (rayType == Radiance) {
+    if (ss.light.pdf >= 0.f) { prepShadow(); return; }
+    if (ss.aoSamples < R.ambientSamples) { prepAO(); return; }
+    if (ss.bsdf.pdf >= 0.f) { prepBounce(); return; }
+    return;
+  } else if (rayType == Shadow) {
+    int surfV = hitRec.surface.hit ? 0 : 1;
+    int volV = hitRec.volumeHit ? 0 : 1;
+    ss.visLight = surfV * volV * hitRec.volume.Tr;
+    if (ss.aoSamples < R.ambientSamples) { prepAO(); return; }
+    if (ss.bsdf.pdf >= 0.f) { prepBounce(); return; }
+    return;
+  } else if (rayType == AO) {
+    ss.aoSamples++;
+    float weight = std::fmax(0.f, dot(ray.dir, ss.sn));
+    ss.aoWeights += weight;
+    if (weight > 0.f && hitRec.hit) ss.aoCount += weight;
+    if (ss.aoSamples < R.ambientSamples) { prepAO(); return; }
+    float aoV = 0.f;
+    if (ss.aoWeights > 0.f) aoV = 1.f - (ss.aoCount / ss.aoWeights);
+    ss.visAO *= aoV;
+    if (ss.bsdf.pdf >= 0.f) { prepBounce(); return; }
+    return;
+  }
+}
+
+struct Ctx {
+  const Scene *sc;
+  Cam cam;
+  const OrRenderer *R;
+  OrFrame *F;
+};
+
+// Per-pixel body of VisionarayRendererPathtrace::renderFrame,
+// renderer/Pathtrace_impl.cpp:498-640, followed by dco::Frame::writeSample.
+void pathtracePixel(const Ctx &cx, int x, int y, Counters &c) {
+  const Scene &sc = *cx.sc;
+  const OrRenderer &R = *cx.R;
+  OrFrame &F = *cx.F;
+  const int W = F.width, H = F.height;
+  int pixelID = x + W * y;
+  LCG rng((uint32_t)pixelID, (uint32_t)F.accumID);
+  LCG rnd = rng; // ScreenSample keeps its own copy (:512-513)
+  f4 accumColor(0.f);
+  PixelSample closest;
+  closest.depth = 1e31f;
+  const int spp = R.pixelSamples;
+  const f3 ambient = f3(R.ambientColor[0], R.ambientColor[1], R.ambientColor[2]) * R.ambientRadiance;
+  for (int sampleID = 0; sampleID < spp; ++sampleID) {
+    float xf = (float)x, yf = (float)y;
+    float jx = rnd() - .5f;
+    float jy = rnd() - .5f;
+    xf += jx;
+    yf += jy;
+    Ray ray = primaryRay(cx.cam, &rnd, xf, yf, (float)W, (float)H);
+    PixelSample ps;
+    ps.color = f4(R.background[0], R.background[1], R.background[2], R.background[3]);
+    ps.depth = 1e31f;
+    if (!sc.insts.empty()) {
+      bool firstHit = false;
+      ShadeState ss;
+      RayType rayType = Radiance;
+      f3 throughput(1.f), intensity(0.f);
+      for (unsigned passID = 0, bounceID = 0; true; ++passID) {
+        ray = clipRay(ray, R);
+        HitRec hitRec = intersectAll(sc, ray, rnd, c);
+        shade(sc, R, rnd, ray, rayType, hitRec, ss, ps, bounceID);
+        if (passID == 0 && bounceID == 0) firstHit = hitRec.hit;
+        ray = ss.nextRay;
+        rayType = ss.nextType;
+        if (rayType == Miss || rayType == Radiance) {
+          f3 direct = ss.shadedColor * ss.visLight;
+          f3 amb = ss.baseColor * ambient * ss.visAO;
+          intensity += throughput * ss.misWeightNEE * direct;
+          intensity += throughput * amb;
+          throughput *= ss.bsdf.f * ss.bsdf.cosT * safe_rcp(ss.bsdf.pdf);
+          bounceID++;
+        }
+        if (rayType == Miss || bounceID > (unsigned)R.maxBounce) break;
+        if (bounceID > 1) {
+          float prob = max_element(throughput);
+          if (rng.next() > prob) break;
+          throughput /= prob;
+        }
+      }
+      if (firstHit) ps.color = f4(intensity, 1.f);
+    }
+    accumColor += ps.color;
+    if (F.sampleSum) {
+      double *s = F.sampleSum + 3 * size_t(pixelID);
+      double *q = F.sampleSumSq + 3 * size_t(pixelID);
+      s[0] += ps.color.x; s[1] += ps.color.y; s[2] += ps.color.z;
+      q[0] += double(ps.color.x) * ps.color.x;
+      q[1] += double(ps.color.y) * ps.color.y;
+      q[2] += double(ps.color.z) * ps.color.z;
+    }
+    if (ps.depth < closest.depth) closest = ps;
+  }
+  PixelSample fin = closest;
+  fin.color = accumColor * (1.f / spp);
+  // writeSample = fillGBuffer + accumSample + toneMap (DeviceCopyableObjects.h:2692-2781)
+  size_t idx = size_t(y) * W + x;
+  if (F.depth && !(fin.depth > F.depth[idx])) {
+    F.depth[idx] = fin.depth;
+    if (F.normal) { F.normal[3 * idx] = fin.Ng.x; F.normal[3 * idx + 1] = fin.Ng.y; F.normal[3 * idx + 2] = fin.Ng.z; }
+    if (F.albedo) { F.albedo[3 * idx] = fin.albedo.x; F.albedo[3 * idx + 1] = fin.albedo.y; F.albedo[3 * idx + 2] = fin.albedo.z; }
+  }
+  float a = 1.f / (F.accumID + 1);
+  float *acc = F.accum + 4 * idx;
+  acc[0] = (1 - a) * acc[0] + a * fin.color.x;
+  acc[1] = (1 - a) * acc[1] + a * fin.color.y;
+  acc[2] = (1 - a) * acc[2] + a * fin.color.z;
+  acc[3] = (1 - a) * acc[3] + a * fin.color.w;
+  fin.color = f4(acc[0], acc[1], acc[2], acc[3]);
+  if (F.color) {
+    if (F.colorType == OR_COLOR_FLOAT4) {
+      float *o = (float *)F.color + 4 * idx;
+      o[0] = fin.color.x; o[1] = fin.color.y; o[2] = fin.color.z; o[3] = fin.color.w;
+    } else {
+      auto cv = [](float f) { return (uint32_t)(255.f * std::min(std::max(f, 0.f), 1.f)); };
+      f4 cc = fin.color;
+      if (F.colorType == OR_COLOR_SRGB8)
+        cc = f4(linear_to_srgb1(cc.x), linear_to_srgb1(cc.y), linear_to_srgb1(cc.z), cc.w);
+      ((uint32_t *)F.color)[idx] = cv(cc.x) | (cv(cc.y) << 8) | (cv(cc.z) << 16) | (cv(cc.w) << 24);
+    }
+  }
+}
+
+// Per-pixel body of VisionarayRendererRaycast::renderFrame,
+// renderer/Raycast_impl.cpp:254-321 (non-stochastic: color written as is).
+void raycastPixel(const Ctx &cx, int x, int y, Counters &c) {
+  const Scene &sc = *cx.sc;
+  const OrRenderer &R = *cx.R;
+  OrFrame &F = *cx.F;
+  const int W = F.width, H = F.height;
+  f4 accumColor(0.f);
+  PixelSample first;
+  const int spp = R.pixelSamples;
+  for (int sampleID = 0; sampleID < spp; ++sampleID) {
+    Ray ray = primaryRay(cx.cam, nullptr, (float)x, (float)y, (float)W, (float)H);
+    ray = clipRay(ray, R);
+    PixelSample ps = raycastSample(sc, R, ray, c);
+    accumColor += ps.color;
+    if (sampleID == 0) first = ps;
+  }
+  PixelSample fin = first;
+  fin.color = accumColor * (1.f / spp);
+  size_t idx = size_t(y) * W + x;
+  if (F.sampleSum) {
+    double *s = F.sampleSum + 3 * idx;
+    double *q = F.sampleSumSq + 3 * idx;
+    s[0] += fin.color.x; s[1] += fin.color.y; s[2] += fin.color.z;
+    q[0] += double(fin.color.x) * fin.color.x;
+    q[1] += double(fin.color.y) * fin.color.y;
+    q[2] += double(fin.color.z) * fin.color.z;
+  }
+  if (F.depth && !(fin.depth > F.depth[idx])) {
+    F.depth[idx] = fin.depth;
+    if (F.normal) { F.normal[3 * idx] = fin.Ng.x; F.normal[3 * idx + 1] = fin.Ng.y; F.normal[3 * idx + 2] = fin.Ng.z; }
+    if (F.albedo) { F.albedo[3 * idx] = fin.albedo.x; F.albedo[3 * idx + 1] = fin.albedo.y; F.albedo[3 * idx + 2] = fin.albedo.z; }
+  }
+  if (F.color) {
+    if (F.colorType == OR_COLOR_FLOAT4) {
+      float *o = (float *)F.color + 4 * idx;
+      o[0] = fin.color.x; o[1] = fin.color.y; o[2] = fin.color.z; o[3] = fin.color.w;
+    } else {
+      auto cv = [](float f) { return (uint32_t)(255.f * std::min(std::max(f, 0.f), 1.f)); };
+      f4 cc = fin.color;
+      if (F.colorType == OR_COLOR_SRGB8)
+        cc = f4(linear_to_srgb1(cc.x), linear_to_srgb1(cc.y), linear_to_srgb1(cc.z), cc.w);
+      ((uint32_t *)F.color)[idx] = cv(cc.x) | (cv(cc.y) << 8) | (cv(cc.z) << 16) | (cv(cc.w) << 24);
+    }
+  }
+}
+
+Scene *commit(const OrScene *s) {
+  auto *sc = new Scene;
+  sc->src = s;
+  sc->tris.resize(s->numTriangles);
+  for (int i = 0; i < s->numTriangles; ++i) {
+    const float *p = s->triVerts + 9 * i;
+    f3 v1(p[0], p[1], p[2]), v2(p[3], p[4], p[5]), v3(p[6], p[7], p[8]);
+    sc->tris[i] = Tri{v1, v2 - v1, v3 - v1};
+  }
+  sc->bvh.resize(s->numGroups);
+  for (int g = 0; g < s->numGroups; ++g)
+    buildBVH(sc->bvh[g], sc->tris, s->groups[g].triBegin, s->groups[g].triEnd);
+  sc->vols.resize(s->numVolumes);
+  for (int i = 0; i < s->numVolumes; ++i) {
+    Vol &v = sc->vols[i];
+    v.v = &s->volumes[i];
+    f3 org(v.v->origin[0], v.v->origin[1], v.v->origin[2]);
+    f3 sp(v.v->spacing[0], v.v->spacing[1], v.v->spacing[2]);
+    f3 dims((float)v.v->dims[0], (float)v.v->dims[1], (float)v.v->dims[2]);
+    v.bounds.lo = org;
+    v.bounds.hi = org + (dims - f3(1.f)) * sp;
+    v.S = f3(1.f) / (v.bounds.hi - v.bounds.lo);
+    v.T = -v.bounds.lo;
+    v.cellSize = min_element(sp);
+    buildMajorants(v);
+  }
+  sc->insts.resize(s->numInstances);
+  for (int i = 0; i < s->numInstances; ++i) {
+    const OrInstance &oi = s->instances[i];
+    M3 a;
+    a.c0 = f3(oi.xfm[0], oi.xfm[1], oi.xfm[2]);
+    a.c1 = f3(oi.xfm[3], oi.xfm[4], oi.xfm[5]);
+    a.c2 = f3(oi.xfm[6], oi.xfm[7], oi.xfm[8]);
+    Inst &in = sc->insts[i];
+    in.affineInv = inverse3(a);
+    in.transInv = -f3(oi.xfm[9], oi.xfm[10], oi.xfm[11]);
+    in.normalXfm = transpose3(in.affineInv);
+    in.group = oi.group;
+    in.userID = oi.userID;
+  }
+  return sc;
+}
+
+} // namespace
+
+extern "C" {
+
+void *or_scene_commit(const OrScene *scene) { return commit(scene); }
+void or_scene_release(void *h) { delete (Scene *)h; }
+
+void or_frame_reset(OrFrame *F) {
+  size_t n = size_t(F->width) * F->height;
+  if (F->accum) std::fill(F->accum, F->accum + 4 * n, 0.f);
+  if (F->depth) std::fill(F->depth, F->depth + n, 1e31f);
+  F->accumID = 0;
+}
+
+int or_render_frame(void *scene, const OrCamera *cam, const OrRenderer *rend, OrFrame *frame,
+                    int numThreads, OrStats *stats) {
+  Ctx cx{(const Scene *)scene, makeCam(*cam), rend, frame};
+  const int W = frame->width, H = frame->height;
+  int r0 = frame->rowBegin, r1 = frame->rowEnd;
+  if (r0 == 0 && r1 == 0) r1 = H;
+  // 64x64 tiles on a pool of hardware_concurrency() threads (for_each.h:71-85,
+  // SyncContext.cpp:21).
+  const int T = 64;
+  const int tx = (W + T - 1) / T, ty = (r1 - r0 + T - 1) / T;
+  const int ntiles = tx * ty;
+  if (numThreads <= 0) numThreads = (int)std::max(1u, std::thread::hardware_concurrency());
+  std::atomic<int> next{0};
+  std::vector<Counters> cnt(numThreads);
+  auto worker = [&](int tid) {
+    Counters &c = cnt[tid];
+    for (;;) {
+      int t = next.fetch_add(1);
+      if (t >= ntiles) break;
+      int bx = (t % tx) * T, by = r0 + (t / tx) * T;
+      for (int y = by; y < std::min(by + T, r1); ++y)
+        for (int x = bx; x < std::min(bx + T, W); ++x) {
+          if (rend->type == OR_PATHTRACE) pathtracePixel(cx, x, y, c);
+          else raycastPixel(cx, x, y, c);
+        }
+    }
+  };
+  std::vector<std::thread> th;
+  for (int i = 1; i < numThreads; ++i) th.emplace_back(worker, i);
+  worker(0);
+  for (auto &t : th) t.join();
+  if (stats) {
+    for (auto &c : cnt) {
+      stats->rays += c.rays; stats->nodeVisits += c.nodes; stats->triTests += c.tris;
+      stats->marchSamples += c.march; stats->trackingSamples += c.track; stats->cellsVisited += c.cells;
+    }
+  }
+  frame->accumID++;
+  return 0;
+}
+
+void or_lcg_sequence(uint32_t v0, uint32_t v1, int n, float *out) {
+  LCG r(v0, v1);
+  for (int i = 0; i < n; ++i) out[i] = r();
+}
+
+float or_sample_field(const OrVolume *vol, float px, float py, float pz) {
+  return sampleField(vol, f3(px, py, pz));
+}
+
+void or_tf_lookup(const OrVolume *vol, float v, float *rgba) {
+  f4 c = postClassify(vol, v);
+  rgba[0] = c.x; rgba[1] = c.y; rgba[2] = c.z; rgba[3] = c.w;
+}
+
+void or_primary_ray(const OrCamera *cam, float x, float y, float w, float h, uint32_t s0,
+                    uint32_t s1, float *ori, float *dir) {
+  Cam k = makeCam(*cam);
+  LCG r(s0, s1);
+  Ray ray = primaryRay(k, &r, x, y, w, h);
+  ori[0] = ray.ori.x; ori[1] = ray.ori.y; ori[2] = ray.ori.z;
+  dir[0] = ray.dir.x; dir[1] = ray.dir.y; dir[2] = ray.dir.z;
+}
+
+void or_eval_material(const OrMaterial *mat, const float *Ng, const float *Ns, const float *vd,
+                      const float *ld, float *out) {
+  (void)Ng;
+  f3 r = evalMaterial(*mat, f3(Ns[0], Ns[1], Ns[2]), f3(vd[0], vd[1], vd[2]), f3(ld[0], ld[1], ld[2]));
+  out[0] = r.x; out[1] = r.y; out[2] = r.z;
+}
+
+void or_sample_material(const OrMaterial *mat, const float *Ng, const float *Ns, const float *vd,
+                        uint32_t s0, uint32_t s1, float *dir, float *f, float *pdf, float *cosT) {
+  LCG r(s0, s1);
+  BSDFSample b = sampleMaterial(*mat, f3(Ng[0], Ng[1], Ng[2]), f3(Ns[0], Ns[1], Ns[2]),
+                                f3(vd[0], vd[1], vd[2]), r);
+  dir[0] = b.dir.x; dir[1] = b.dir.y; dir[2] = b.dir.z;
+  f[0] = b.f.x; f[1] = b.f.y; f[2] = b.f.z;
+  *pdf = b.pdf;
+  *cosT = b.cosT;
+}
+
+int or_majorants(void *scene, int vol, int32_t *dims, float *out, int maxCells) {
+  const Scene *sc = (const Scene *)scene;
+  const Vol &v = sc->vols[vol];
+  for (int a = 0; a < 3; ++a) dims[a] = v.gdims[a];
+  int n = (int)v.maxOpacity.size();
+  for (int i = 0; i < n && i < maxCells; ++i) out[i] = v.maxOpacity[i];
+  return n;
+}
+
+int or_dda(const float *ori, const float *dir, float tmin, float tmax, const int32_t *dims,
+           const float *lo, const float *hi, int32_t *cells, float *t01, int maxCells) {
+  Ray r;
+  r.ori = f3(ori[0], ori[1], ori[2]);
+  r.dir = f3(dir[0], dir[1], dir[2]);
+  r.tmin = tmin;
+  r.tmax = tmax;
+  Box b;
+  b.lo = f3(lo[0], lo[1], lo[2]);
+  b.hi = f3(hi[0], hi[1], hi[2]);
+  int d[3] = {dims[0], dims[1], dims[2]};
+  int n = 0;
+  dda3(r, d, b, [&](int id, float t0, float t1) {
+    if (n < maxCells) { cells[n] = id; t01[2 * n] = t0; t01[2 * n + 1] = t1; }
+    ++n;
+    return n < 1000000;
+  });
+  return n;
+}
+
+int or_trace(void *scene, const float *ori, const float *dir, float tmin, float tmax, float *t,
+             uint32_t *inst, uint32_t *tri, float *uv) {
+  const Scene *sc = (const Scene *)scene;
+  Ray r;
+  r.ori = f3(ori[0], ori[1], ori[2]);
+  r.dir = f3(dir[0], dir[1], dir[2]);
+  r.tmin = tmin;
+  r.tmax = tmax;
+  r.time = 0.5f;
+  Counters c;
+  SurfHit h = traceSurfaces(*sc, r, c);
+  *t = h.t;
+  *inst = (uint32_t)h.inst;
+  *tri = (uint32_t)h.tri;
+  uv[0] = h.u;
+  uv[1] = h.v;
+  return h.hit ? 1 : 0;
+}
+
+} // extern "C"

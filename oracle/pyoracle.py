@@ -1,0 +1,374 @@
+"""ctypes binding of the CPU oracle (liboracle.so, built by oracle/Makefile).
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, the smoke check and the
+CPU-baseline leg of bench.py. It converts a scene dict (the format of the
+package's scenes.py) into the oracle's flat C structures with the same
+group / surface / triangle order the renderer core uses, so triangle and
+surface indices agree between the two.
+"""
+import ctypes
+import math
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "build", "liboracle.so")
+
+c_int32, c_uint32, c_float, c_void_p = ctypes.c_int32, ctypes.c_uint32, ctypes.c_float, ctypes.c_void_p
+FP = ctypes.POINTER(ctypes.c_float)
+DP = ctypes.POINTER(ctypes.c_double)
+UP = ctypes.POINTER(ctypes.c_uint32)
+
+MATTE, PBR = 0, 1
+CAM_PERSPECTIVE, CAM_MATRIX, CAM_ORTHO, CAM_OMNI = 0, 1, 2, 3
+RAYCAST, PATHTRACE = 0, 1
+GRID_NONE, GRID_REFERENCE, GRID_BRICK = 0, 1, 2
+COLOR_FLOAT4 = 0
+
+
+class OrMaterial(ctypes.Structure):
+    _fields_ = [("type", c_int32), ("baseColor", c_float * 3), ("opacity", c_float),
+                ("metallic", c_float), ("roughness", c_float), ("ior", c_float),
+                ("clearcoat", c_float), ("clearcoatRoughness", c_float), ("transmission", c_float),
+                ("sheenColor", c_float * 3), ("sheenRoughness", c_float), ("alphaMode", c_int32),
+                ("alphaCutoff", c_float)]
+
+
+class OrVolume(ctypes.Structure):
+    _fields_ = [("data", FP), ("dims", c_int32 * 3), ("origin", c_float * 3),
+                ("spacing", c_float * 3), ("tf", FP), ("tfSize", c_int32),
+                ("valueRange", c_float * 2), ("unitDistance", c_float), ("gridMethod", c_int32),
+                ("gridDims", c_int32 * 3), ("brickSize", c_int32)]
+
+
+class OrGroup(ctypes.Structure):
+    _fields_ = [("triBegin", c_int32), ("triEnd", c_int32), ("volBegin", c_int32), ("volEnd", c_int32)]
+
+
+class OrInstance(ctypes.Structure):
+    _fields_ = [("xfm", c_float * 12), ("group", c_int32), ("userID", c_uint32)]
+
+
+class OrLight(ctypes.Structure):
+    _fields_ = [("type", c_int32), ("direction", c_float * 3), ("color", c_float * 3),
+                ("irradiance", c_float), ("angularDiameter", c_float), ("visible", c_int32)]
+
+
+class OrScene(ctypes.Structure):
+    _fields_ = [("numTriangles", c_int32), ("triVerts", FP), ("triSurface", UP), ("triPrimID", UP),
+                ("numSurfaces", c_int32), ("surfMaterial", ctypes.POINTER(OrMaterial)),
+                ("surfObjID", UP), ("numVolumes", c_int32), ("volumes", ctypes.POINTER(OrVolume)),
+                ("numGroups", c_int32), ("groups", ctypes.POINTER(OrGroup)),
+                ("numInstances", c_int32), ("instances", ctypes.POINTER(OrInstance)),
+                ("numLights", c_int32), ("lights", ctypes.POINTER(OrLight))]
+
+
+class OrCamera(ctypes.Structure):
+    _fields_ = [("type", c_int32), ("position", c_float * 3), ("direction", c_float * 3),
+                ("up", c_float * 3), ("fovy", c_float), ("aspect", c_float),
+                ("apertureRadius", c_float), ("focusDistance", c_float),
+                ("imageRegion", c_float * 4), ("shutter", c_float * 2), ("height", c_float),
+                ("view", c_float * 16), ("proj", c_float * 16)]
+
+
+class OrRenderer(ctypes.Structure):
+    _fields_ = [("type", c_int32), ("background", c_float * 4), ("ambientColor", c_float * 3),
+                ("ambientRadiance", c_float), ("occlusionDistance", c_float),
+                ("ambientSamples", c_int32), ("maxBounce", c_int32), ("pixelSamples", c_int32),
+                ("volumeSamplingRate", c_float), ("numClipPlanes", c_int32), ("clipPlanes", FP)]
+
+
+class OrFrame(ctypes.Structure):
+    _fields_ = [("width", c_int32), ("height", c_int32), ("accumID", c_int32),
+                ("colorType", c_int32), ("color", c_void_p), ("depth", FP), ("normal", FP),
+                ("albedo", FP), ("accum", FP), ("sampleSum", DP), ("sampleSumSq", DP),
+                ("rowBegin", c_int32), ("rowEnd", c_int32)]
+
+
+class OrStats(ctypes.Structure):
+    _fields_ = [("rays", ctypes.c_uint64), ("nodeVisits", ctypes.c_uint64),
+                ("triTests", ctypes.c_uint64), ("marchSamples", ctypes.c_uint64),
+                ("trackingSamples", ctypes.c_uint64), ("cellsVisited", ctypes.c_uint64)]
+
+
+_lib = None
+
+
+def build():
+    """Compile liboracle.so with the committed Makefile (idempotent)."""
+    subprocess.run(["make", "-s", "-C", HERE], check=True)
+    return LIB_PATH
+
+
+def load():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            build()
+        lib = ctypes.CDLL(LIB_PATH)
+        lib.or_scene_commit.restype = c_void_p
+        lib.or_scene_commit.argtypes = [ctypes.POINTER(OrScene)]
+        lib.or_scene_release.argtypes = [c_void_p]
+        lib.or_frame_reset.argtypes = [ctypes.POINTER(OrFrame)]
+        lib.or_render_frame.restype = ctypes.c_int
+        lib.or_render_frame.argtypes = [c_void_p, ctypes.POINTER(OrCamera), ctypes.POINTER(OrRenderer),
+                                        ctypes.POINTER(OrFrame), ctypes.c_int, ctypes.POINTER(OrStats)]
+        lib.or_lcg_sequence.argtypes = [c_uint32, c_uint32, ctypes.c_int, FP]
+        lib.or_sample_field.restype = c_float
+        lib.or_sample_field.argtypes = [ctypes.POINTER(OrVolume), c_float, c_float, c_float]
+        lib.or_tf_lookup.argtypes = [ctypes.POINTER(OrVolume), c_float, FP]
+        lib.or_primary_ray.argtypes = [ctypes.POINTER(OrCamera), c_float, c_float, c_float, c_float,
+                                       c_uint32, c_uint32, FP, FP]
+        lib.or_eval_material.argtypes = [ctypes.POINTER(OrMaterial), FP, FP, FP, FP, FP]
+        lib.or_sample_material.argtypes = [ctypes.POINTER(OrMaterial), FP, FP, FP, c_uint32, c_uint32,
+                                           FP, FP, FP, FP]
+        lib.or_majorants.restype = ctypes.c_int
+        lib.or_majorants.argtypes = [c_void_p, ctypes.c_int, ctypes.POINTER(c_int32), FP, ctypes.c_int]
+        lib.or_dda.restype = ctypes.c_int
+        lib.or_dda.argtypes = [FP, FP, c_float, c_float, ctypes.POINTER(c_int32), FP, FP,
+                               ctypes.POINTER(c_int32), FP, ctypes.c_int]
+        lib.or_trace.restype = ctypes.c_int
+        lib.or_trace.argtypes = [c_void_p, FP, FP, c_float, c_float, FP, UP, UP, FP]
+        _lib = lib
+    return _lib
+
+
+def fptr(a):
+    return a.ctypes.data_as(FP)
+
+
+def farr(n, vals):
+    return (c_float * n)(*[float(v) for v in vals])
+
+
+def material(m):
+    om = OrMaterial()
+    om.opacity = float(m.get("opacity", 1.0))
+    mode = m.get("alphaMode", "opaque")
+    om.alphaMode = {"opaque": 0, "blend": 1, "mask": 2}[mode]
+    om.alphaCutoff = float(m.get("alphaCutoff", 0.5))
+    if m["type"] == "matte":
+        om.type = MATTE
+        c = m.get("color", [1, 1, 1])
+        om.baseColor = farr(3, c[:3])
+    else:
+        om.type = PBR
+        c = m.get("baseColor", [1, 1, 1])
+        om.baseColor = farr(3, c[:3])
+        om.metallic = float(m.get("metallic", 1.0))
+        om.roughness = float(m.get("roughness", 1.0))
+        om.ior = float(m.get("ior", 1.5))
+        om.clearcoat = float(m.get("clearcoat", 0.0))
+        om.clearcoatRoughness = float(m.get("clearcoatRoughness", 0.0))
+        om.transmission = float(m.get("transmission", 0.0))
+        om.sheenColor = farr(3, m.get("sheenColor", [0, 0, 0]))
+        om.sheenRoughness = float(m.get("sheenRoughness", 0.0))
+    return om
+
+
+def build_tf(color, opacity):
+    """TF table restated from TransferFunction1D::finalize
+    (scene/volume/TransferFunction1D.cpp:50-112), colour float3 + opacity array."""
+    color = np.asarray(color, np.float32)
+    opacity = np.asarray(opacity, np.float32)
+    nc, no = len(color), len(opacity)
+    n = max(nc, no)
+    out = np.zeros((n, 4), np.float32)
+    f32 = np.float32
+    for i in range(n):
+        cp = f32((f32(i) / f32(n - 1)) * f32(nc - 1)) if n > 1 else f32(0)
+        cf = f32(cp - f32(math.floor(cp)))
+        c0 = np.append(color[int(math.floor(cp))], f32(1))
+        c1 = np.append(color[int(math.ceil(cp))], f32(1))
+        c = (c0 * (f32(1) - cf) + c1 * cf).astype(np.float32)
+        ap = f32((f32(i) / f32(n - 1)) * f32(no - 1)) if n > 1 else f32(0)
+        af = f32(ap - f32(math.floor(ap)))
+        a0, a1 = opacity[int(math.floor(ap))], opacity[int(math.ceil(ap))]
+        c[3] = f32(c[3] * f32(a0 * (f32(1) - af) + a1 * af))
+        out[i] = c
+    return out
+
+
+class Scene:
+    """A scene dict committed to the oracle (owns all buffers it points to)."""
+
+    def __init__(self, scene, grid_method=GRID_BRICK, grid_dims=(16, 16, 16)):
+        lib = load()
+        self._keep = []
+        groups = []   # (surfaces, volumes, lights, xfm)
+        if scene.get("surfaces") or scene.get("volumes") or scene.get("lights"):
+            groups.append((scene.get("surfaces", []), scene.get("volumes", []),
+                           scene.get("lights", []), [1, 0, 0, 0, 1, 0, 0, 0, 1, 0, 0, 0]))
+        for inst in scene.get("instances", []):
+            groups.append((inst.get("surfaces", []), inst.get("volumes", []),
+                           inst.get("lights", []), inst["transform"]))
+        verts, tsurf, tprim, mats, vols, ogroups, oinsts, lights = [], [], [], [], [], [], [], []
+        ntri = 0
+        for gi, (surfs, vls, lts, xfm) in enumerate(groups):
+            g = OrGroup()
+            g.triBegin = ntri
+            for s in surfs:
+                v = np.asarray(s["vertices"], np.float32)
+                t = np.asarray(s["indices"], np.uint32)
+                verts.append(v[t].reshape(-1, 9))
+                sid = len(mats)
+                mats.append(material(s["material"]))
+                tsurf.append(np.full(len(t), sid, np.uint32))
+                tprim.append(np.arange(len(t), dtype=np.uint32))
+                ntri += len(t)
+            g.triEnd = ntri
+            g.volBegin = len(vols)
+            for v in vls:
+                ov = OrVolume()
+                data = np.ascontiguousarray(v["data"], np.float32)
+                tf = build_tf(v["color"], v["opacity"])
+                self._keep += [data, tf]
+                ov.data = fptr(data)
+                nz, ny, nx = data.shape
+                ov.dims = (c_int32 * 3)(nx, ny, nz)
+                ov.origin = farr(3, v["origin"])
+                ov.spacing = farr(3, v["spacing"])
+                ov.tf = fptr(tf)
+                ov.tfSize = len(tf)
+                ov.valueRange = farr(2, v["valueRange"])
+                ov.unitDistance = float(v["unitDistance"]) or 1.0
+                ov.gridMethod = grid_method
+                ov.gridDims = (c_int32 * 3)(*grid_dims)
+                ov.brickSize = int(v.get("majorantBrickSize", 16))
+                vols.append(ov)
+            g.volEnd = len(vols)
+            ogroups.append(g)
+            oi = OrInstance()
+            oi.xfm = farr(12, xfm)
+            oi.group = gi
+            oi.userID = 0xffffffff
+            oinsts.append(oi)
+            lin = np.asarray(xfm, np.float64)[:9].reshape(3, 3).T  # column-major -> matrix
+            for L in lts:
+                ol = OrLight()
+                d = lin @ np.asarray(L["direction"], np.float64)
+                ol.direction = farr(3, d / np.linalg.norm(d))
+                ol.color = farr(3, L.get("color", [1, 1, 1]))
+                ol.irradiance = float(L.get("irradiance", 1.0))
+                ol.angularDiameter = float(L.get("angularDiameter", 0.0))
+                ol.visible = 1
+                lights.append(ol)
+        tri = np.ascontiguousarray(np.concatenate(verts) if verts else np.zeros((0, 9), np.float32))
+        ts = np.ascontiguousarray(np.concatenate(tsurf) if tsurf else np.zeros(0, np.uint32))
+        tp = np.ascontiguousarray(np.concatenate(tprim) if tprim else np.zeros(0, np.uint32))
+        self._keep += [tri, ts, tp]
+        self.mats = (OrMaterial * max(1, len(mats)))(*mats)
+        self.vols = (OrVolume * max(1, len(vols)))(*vols)
+        self.groups = (OrGroup * max(1, len(ogroups)))(*ogroups)
+        self.insts = (OrInstance * max(1, len(oinsts)))(*oinsts)
+        self.lights = (OrLight * max(1, len(lights)))(*lights)
+        objid = np.zeros(max(1, len(mats)), np.uint32)
+        self._keep.append(objid)
+        sc = OrScene()
+        sc.numTriangles = len(tri)
+        sc.triVerts = fptr(tri)
+        sc.triSurface = ts.ctypes.data_as(UP)
+        sc.triPrimID = tp.ctypes.data_as(UP)
+        sc.numSurfaces = len(mats)
+        sc.surfMaterial = self.mats
+        sc.surfObjID = objid.ctypes.data_as(UP)
+        sc.numVolumes = len(vols)
+        sc.volumes = self.vols
+        sc.numGroups = len(ogroups)
+        sc.groups = self.groups
+        sc.numInstances = len(oinsts)
+        sc.instances = self.insts
+        sc.numLights = len(lights)
+        sc.lights = self.lights
+        self.scene = sc
+        self.handle = lib.or_scene_commit(ctypes.byref(sc))
+        self.camera = camera(scene["camera"])
+        self.renderer = renderer(scene["renderer"])
+        self.size = tuple(scene["frame"]["size"])
+
+    def close(self):
+        if self.handle:
+            load().or_scene_release(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def camera(c):
+    oc = OrCamera()
+    oc.type = {"perspective": CAM_PERSPECTIVE, "matrix": CAM_MATRIX, "orthographic": CAM_ORTHO,
+               "omnidirectional": CAM_OMNI}[c["type"]]
+    oc.position = farr(3, c.get("position", [0, 0, 0]))
+    oc.direction = farr(3, c.get("direction", [0, 0, 1]))
+    oc.up = farr(3, c.get("up", [0, 1, 0]))
+    oc.fovy = float(c.get("fovy", math.radians(60.0)))
+    oc.aspect = float(c.get("aspect", 1.0))
+    oc.apertureRadius = float(c.get("apertureRadius", 0.0))
+    oc.focusDistance = float(c.get("focusDistance", 1.0))
+    oc.imageRegion = farr(4, c.get("imageRegion", [0, 0, 1, 1]))
+    oc.shutter = farr(2, c.get("shutter", [0.5, 0.5]))
+    oc.height = float(c.get("height", 1.0))
+    oc.view = farr(16, c.get("view", np.eye(4).reshape(-1)))
+    oc.proj = farr(16, c.get("proj", np.eye(4).reshape(-1)))
+    return oc
+
+
+def renderer(r):
+    orr = OrRenderer()
+    orr.type = RAYCAST if r["type"] == "raycast" else PATHTRACE
+    orr.background = farr(4, r.get("background", [0, 0, 0, 1]))
+    orr.ambientColor = farr(3, r.get("ambientColor", [1, 1, 1]))
+    orr.ambientRadiance = float(r.get("ambientRadiance", 0.2))
+    orr.occlusionDistance = float(r.get("ambientOcclusionDistance", 1e20))
+    orr.ambientSamples = int(r.get("ambientSamples", 1))
+    orr.maxBounce = int(r.get("maxBounce", 7))
+    orr.pixelSamples = int(r.get("pixelSamples", 1)) if orr.type == PATHTRACE else 1
+    orr.volumeSamplingRate = float(r.get("volumeSamplingRate", 0.5))
+    planes = np.asarray(r.get("clipPlanes", np.zeros((0, 4))), np.float32).reshape(-1, 4)
+    orr.numClipPlanes = len(planes)
+    orr._planes = np.ascontiguousarray(planes)
+    orr.clipPlanes = fptr(orr._planes)
+    return orr
+
+
+class Frame:
+    """Frame buffers of the oracle (float4 colour, depth, normal, albedo)."""
+
+    def __init__(self, w, h, stats=False):
+        self.w, self.h = w, h
+        self.color = np.zeros((h, w, 4), np.float32)
+        self.depth = np.zeros((h, w), np.float32)
+        self.normal = np.zeros((h, w, 3), np.float32)
+        self.albedo = np.zeros((h, w, 3), np.float32)
+        self.accum = np.zeros((h, w, 4), np.float32)
+        self.sum = np.zeros((h, w, 3), np.float64) if stats else None
+        self.sumsq = np.zeros((h, w, 3), np.float64) if stats else None
+        f = OrFrame()
+        f.width, f.height = w, h
+        f.colorType = COLOR_FLOAT4
+        f.color = self.color.ctypes.data
+        f.depth = fptr(self.depth)
+        f.normal = fptr(self.normal)
+        f.albedo = fptr(self.albedo)
+        f.accum = fptr(self.accum)
+        if stats:
+            f.sampleSum = self.sum.ctypes.data_as(DP)
+            f.sampleSumSq = self.sumsq.ctypes.data_as(DP)
+        self.f = f
+        load().or_frame_reset(ctypes.byref(f))
+
+
+def render(sc, frame, num_threads=0, rows=None, stats=None):
+    """Render one frame of committed scene `sc` into `frame` (accumulating)."""
+    if rows is not None:
+        frame.f.rowBegin, frame.f.rowEnd = rows
+    st = stats if stats is not None else OrStats()
+    load().or_render_frame(sc.handle, ctypes.byref(sc.camera), ctypes.byref(sc.renderer),
+                           ctypes.byref(frame.f), num_threads, ctypes.byref(st))
+    return st

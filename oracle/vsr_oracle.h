@@ -1,0 +1,182 @@
+/* CPU oracle for the raycast / pathtrace hot path: C API.
+ *
+ * TEST INFRASTRUCTURE ONLY. This is a CPU restatement of the reference
+ * anari-visionaray CPU device for the per-pixel hot path; it is the checker
+ * used by tests/, the smoke check and the CPU-baseline leg of bench.py. The
+ * product library never includes, links or calls it.
+ *
+ * The reference (Visionaray + ANARI-SDK based) cannot be compiled in this
+ * environment, so parity is unpinned against the reference binary; each
+ * function cites the reference source it restates.
+ */
+#ifndef VSR_ORACLE_H
+#define VSR_ORACLE_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum { OR_MATTE = 0, OR_PBR = 1 };
+enum { OR_ALPHA_OPAQUE = 0, OR_ALPHA_BLEND = 1, OR_ALPHA_MASK = 2 };
+enum { OR_CAM_PERSPECTIVE = 0, OR_CAM_MATRIX = 1, OR_CAM_ORTHO = 2, OR_CAM_OMNI = 3 };
+enum { OR_RAYCAST = 0, OR_PATHTRACE = 1 };
+enum { OR_GRID_NONE = 0, OR_GRID_REFERENCE = 1, OR_GRID_BRICK = 2 };
+enum { OR_COLOR_FLOAT4 = 0, OR_COLOR_UFIXED8 = 1, OR_COLOR_SRGB8 = 2 };
+
+/* dco::Material (DeviceCopyableObjects.h) with constant parameters. */
+typedef struct OrMaterial {
+  int32_t type;
+  float baseColor[3];
+  float opacity;
+  float metallic, roughness, ior;
+  float clearcoat, clearcoatRoughness, transmission;
+  float sheenColor[3];
+  float sheenRoughness;
+  int32_t alphaMode;
+  float alphaCutoff;
+} OrMaterial;
+
+/* structuredRegular field + transferFunction1D volume. */
+typedef struct OrVolume {
+  const float *data;      /* dims.x*dims.y*dims.z floats, x fastest */
+  int32_t dims[3];
+  float origin[3];
+  float spacing[3];
+  const float *tf;        /* tfSize RGBA float4 entries */
+  int32_t tfSize;
+  float valueRange[2];
+  float unitDistance;
+  int32_t gridMethod;     /* OR_GRID_* : majorant grid for delta tracking */
+  int32_t gridDims[3];    /* OR_GRID_REFERENCE: cell grid; OR_GRID_BRICK: ignored */
+  int32_t brickSize;      /* OR_GRID_BRICK: voxels per brick edge */
+} OrVolume;
+
+typedef struct OrGroup {
+  int32_t triBegin, triEnd; /* range in the scene's triangle array */
+  int32_t volBegin, volEnd; /* range in the scene's volume array */
+} OrGroup;
+
+typedef struct OrInstance {
+  float xfm[12];            /* column-major 3x4 affine: 3 columns + translation */
+  int32_t group;
+  uint32_t userID;
+} OrInstance;
+
+typedef struct OrLight {
+  int32_t type;             /* 0 = directional */
+  float direction[3];       /* direction the light travels (ANARI "direction") */
+  float color[3];
+  float irradiance;
+  float angularDiameter;
+  int32_t visible;
+} OrLight;
+
+typedef struct OrScene {
+  int32_t numTriangles;
+  const float *triVerts;     /* 9 floats per triangle (object space) */
+  const uint32_t *triSurface;/* surface index per triangle */
+  const uint32_t *triPrimID; /* primitive index inside its geometry */
+  int32_t numSurfaces;
+  const OrMaterial *surfMaterial;
+  const uint32_t *surfObjID;
+  int32_t numVolumes;
+  const OrVolume *volumes;
+  int32_t numGroups;
+  const OrGroup *groups;
+  int32_t numInstances;
+  const OrInstance *instances;
+  int32_t numLights;
+  const OrLight *lights;
+} OrScene;
+
+typedef struct OrCamera {
+  int32_t type;
+  float position[3], direction[3], up[3];
+  float fovy, aspect;
+  float apertureRadius, focusDistance;
+  float imageRegion[4];      /* min.x, min.y, max.x, max.y */
+  float shutter[2];
+  float height;              /* orthographic */
+  float view[16], proj[16];  /* matrix camera, column-major */
+} OrCamera;
+
+typedef struct OrRenderer {
+  int32_t type;
+  float background[4];
+  float ambientColor[3];
+  float ambientRadiance;
+  float occlusionDistance;
+  int32_t ambientSamples;
+  int32_t maxBounce;
+  int32_t pixelSamples;
+  float volumeSamplingRate;
+  int32_t numClipPlanes;
+  const float *clipPlanes;   /* float4 (n.xyz, d) each */
+} OrRenderer;
+
+typedef struct OrFrame {
+  int32_t width, height;
+  int32_t accumID;           /* in/out: incremented by or_render_frame */
+  int32_t colorType;         /* OR_COLOR_* */
+  void *color;               /* float4 or uint32 per pixel */
+  float *depth;
+  float *normal;             /* float3 */
+  float *albedo;             /* float3 */
+  float *accum;              /* float4 accumulation buffer */
+  double *sampleSum;         /* optional: per-pixel sum of sample rgb (3 doubles) */
+  double *sampleSumSq;       /* optional: per-pixel sum of squares (3 doubles) */
+  int32_t rowBegin, rowEnd;  /* render rows [rowBegin,rowEnd) only (0,0 = all) */
+} OrFrame;
+
+typedef struct OrStats {
+  uint64_t rays;             /* traversals started */
+  uint64_t nodeVisits;       /* BVH inner-node visits */
+  uint64_t triTests;         /* ray/triangle tests */
+  uint64_t marchSamples;     /* rayMarchVolume samples taken */
+  uint64_t trackingSamples;  /* delta-tracking tentative collisions */
+  uint64_t cellsVisited;     /* DDA cells visited */
+} OrStats;
+
+/* Build the per-group BVHs and majorant grids; arrays must outlive the handle. */
+void *or_scene_commit(const OrScene *scene);
+void or_scene_release(void *handle);
+
+/* Clear the accumulation buffer and set depth to 1e31, accumID = 0
+   (frame/Frame.cpp:287-312). */
+void or_frame_reset(OrFrame *frame);
+
+/* Render one frame (frame/Frame.cpp:215-397 minus the device plumbing).
+   numThreads <= 0 uses std::thread::hardware_concurrency(). */
+int or_render_frame(void *scene, const OrCamera *cam, const OrRenderer *rend,
+                    OrFrame *frame, int numThreads, OrStats *stats);
+
+/* ---- unit-level entry points used by the oracle's own tests ---- */
+void or_lcg_sequence(uint32_t v0, uint32_t v1, int n, float *out);
+float or_sample_field(const OrVolume *vol, float px, float py, float pz);
+void or_tf_lookup(const OrVolume *vol, float v, float *rgba);
+void or_primary_ray(const OrCamera *cam, float x, float y, float w, float h,
+                    uint32_t seed0, uint32_t seed1, float *ori, float *dir);
+void or_eval_material(const OrMaterial *mat, const float *Ng, const float *Ns,
+                      const float *viewDir, const float *lightDir, float *out);
+/* Draws from an LCG seeded (seed0,seed1); writes dir[3], f[3], pdf, cosT. */
+void or_sample_material(const OrMaterial *mat, const float *Ng, const float *Ns,
+                        const float *viewDir, uint32_t seed0, uint32_t seed1,
+                        float *dir, float *f, float *pdf, float *cosT);
+/* Majorant grid of volume `vol` of a committed scene: writes dims and up to
+   maxCells floats; returns the cell count. */
+int or_majorants(void *scene, int vol, int32_t *dims, float *out, int maxCells);
+/* DDA over a grid: writes visited cell ids and [t0,t1] pairs; returns count. */
+int or_dda(const float *ori, const float *dir, float tmin, float tmax,
+           const int32_t *dims, const float *boundsLo, const float *boundsHi,
+           int32_t *cells, float *t01, int maxCells);
+/* Closest hit through the committed scene: returns 1 on hit. */
+int or_trace(void *scene, const float *ori, const float *dir, float tmin, float tmax,
+             float *t, uint32_t *inst, uint32_t *tri, float *uv);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

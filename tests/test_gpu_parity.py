@@ -1,0 +1,216 @@
+"""GPU parity: the CUDA renderer core (through the C ABI) against the CPU
+oracle on the same seeded scenes.
+
+Tolerances (from the project's parity bar):
+  raycast    : per-channel |delta| <= 2e-3 on >= 99.9 % of pixels; depth within
+               1e-4 relative on surface-hit pixels (volume-only frames write 1e31).
+  pathtracer : the GPU mean image lies inside the oracle's per-pixel 3 sigma band
+               (sigma from per-sample variance of both estimates) on >= 98.5 % of
+               pixels for independent random streams; with the same stream the
+               GPU reproduces the oracle sample for sample (>= 97 % of pixels
+               within 1e-3), since both follow the reference's per-pixel LCG.
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+RAYCAST_TOL = 2e-3
+
+
+def render_gpu(pkg, dev, scene, frames=1, accum_offset=0):
+    h = pkg.scenes.build(dev, scene)
+    for _ in range(frames):
+        assert dev.render(h["frame"]) == 0
+        assert dev.wait(h["frame"])
+    out = {c: dev.map(h["frame"], "channel." + c) for c in ("color", "depth", "normal", "albedo")}
+    out["errorFlags"] = dev.get_uint(h["frame"], "errorFlags")
+    for o in (h["frame"], h["renderer"], h["camera"], h["world"]):
+        dev.release(o)
+    for o in h["keep"]:
+        dev.release(o)
+    return out
+
+
+def render_oracle(oracle, scene, frames=1, accum_start=0, stats=False, grid=None):
+    kw = {} if grid is None else {"grid_method": grid}
+    S = oracle.Scene(scene, **kw)
+    W, H = scene["frame"]["size"]
+    F = oracle.Frame(W, H, stats=stats)
+    F.f.accumID = accum_start
+    for _ in range(frames):
+        oracle.render(S, F)
+    return S, F
+
+
+def raycast_ok(gpu, F, tol=RAYCAST_TOL, frac=0.999):
+    d = np.abs(gpu["color"] - F.color).max(axis=-1)
+    ok = float((d <= tol).mean())
+    return ok >= frac, ok
+
+
+def test_raycast_volume_full_config0(pkg, device, oracle):
+    """Config 0 at its full size: 128^3 blob volume, 512x512."""
+    sc = pkg.scenes.config0()
+    gpu = render_gpu(pkg, device, sc)
+    _, F = render_oracle(oracle, sc)
+    good, frac = raycast_ok(gpu, F)
+    assert good, f"only {frac:.5f} of pixels within {RAYCAST_TOL}"
+    assert np.all(gpu["depth"] == np.float32(1e31)) and np.all(F.depth == np.float32(1e31))
+    assert np.all(gpu["normal"] == 0) and np.all(gpu["albedo"] == 0)
+    assert gpu["errorFlags"] == 0
+    assert gpu["color"][..., :3].max() > 0.05  # the volume is visible
+
+
+def test_raycast_volume_sampling_rates(pkg, device, oracle):
+    for rate in (0.5, 1.0, 3.0):
+        sc = pkg.scenes.config0(res=96, n=40)
+        sc["renderer"]["volumeSamplingRate"] = rate
+        gpu = render_gpu(pkg, device, sc)
+        _, F = render_oracle(oracle, sc)
+        good, frac = raycast_ok(gpu, F)
+        assert good, (rate, frac)
+
+
+def small_spheres(pkg, res=128, spp=4, n=24, renderer="pathtrace", bounce=5, seed=None):
+    kw = {} if seed is None else {"seed": seed}
+    sc = pkg.scenes.config1(res=res, spp=spp, num_spheres=n, nu=24, nv=12, max_bounce=bounce, **kw)
+    sc["renderer"]["type"] = renderer
+    return sc
+
+
+def test_raycast_triangles(pkg, device, oracle):
+    sc = small_spheres(pkg, res=192, renderer="raycast")
+    gpu = render_gpu(pkg, device, sc)
+    _, F = render_oracle(oracle, sc)
+    good, frac = raycast_ok(gpu, F)
+    assert good, frac
+    hit = (F.depth < 1e30) & (gpu["depth"] < 1e30)
+    assert hit.mean() > 0.2
+    assert np.array_equal(F.depth < 1e30, gpu["depth"] < 1e30) or \
+        (np.mean((F.depth < 1e30) != (gpu["depth"] < 1e30)) < 1e-3)
+    rel = np.abs(gpu["depth"][hit] - F.depth[hit]) / F.depth[hit]
+    assert float((rel <= 1e-4).mean()) >= 0.999
+    nd = np.abs(gpu["normal"] - F.normal).max(axis=-1)
+    assert float((nd <= 1e-3).mean()) >= 0.999
+    ad = np.abs(gpu["albedo"] - F.albedo).max(axis=-1)
+    assert float((ad <= 1e-5).mean()) >= 0.999
+
+
+def test_pathtrace_same_stream(pkg, device, oracle):
+    """Same seeds: the GPU path tracer follows the oracle sample for sample."""
+    sc = small_spheres(pkg, res=128, spp=8)
+    gpu = render_gpu(pkg, device, sc)
+    _, F = render_oracle(oracle, sc)
+    assert not np.isnan(gpu["color"]).any()
+    d = np.abs(gpu["color"][..., :3] - F.color[..., :3]).max(axis=-1)
+    assert float((d <= 1e-3).mean()) >= 0.97, float((d <= 1e-3).mean())
+    hit = (F.depth < 1e30) & (gpu["depth"] < 1e30)
+    rel = np.abs(gpu["depth"][hit] - F.depth[hit]) / F.depth[hit]
+    assert float((rel <= 1e-4).mean()) >= 0.99
+    assert gpu["errorFlags"] == 0
+
+
+def test_pathtrace_statistical_band(pkg, device, oracle):
+    """Independent streams: GPU mean within the combined 3-sigma band."""
+    frames, spp = 16, 16
+    sc = small_spheres(pkg, res=64, spp=spp, n=16)
+    gpu = render_gpu(pkg, device, sc, frames=frames)
+    # oracle with accumulation IDs 1000.. (independent LCG seeds) and
+    # per-sample statistics
+    S, F = render_oracle(oracle, sc, frames=frames, accum_start=1000, stats=True)
+    n = frames * spp
+    mean = F.sum / n
+    var = np.maximum(F.sumsq / n - mean * mean, 0.0) * n / (n - 1)
+    # the GPU estimate has the same per-sample variance
+    sigma = np.sqrt(2.0 * var / n)
+    diff = np.abs(gpu["color"][..., :3] - mean)
+    inside = diff <= 3.0 * sigma + 1e-6
+    frac = float(inside.all(axis=-1).mean())
+    rmse = float(np.sqrt(np.mean((gpu["color"][..., :3] - mean) ** 2)))
+    print(f"3-sigma band: {frac:.4f} of pixels, RMSE {rmse:.5f}")
+    assert frac >= 0.985, frac
+
+
+def test_pathtrace_accumulation(pkg, device, oracle):
+    """Progressive accumulation over frames (frame/Frame.cpp running mean)."""
+    sc = small_spheres(pkg, res=64, spp=2, n=12)
+    gpu = render_gpu(pkg, device, sc, frames=4)
+    _, F = render_oracle(oracle, sc, frames=4)
+    d = np.abs(gpu["color"][..., :3] - F.color[..., :3]).max(axis=-1)
+    assert float((d <= 1e-3).mean()) >= 0.97
+
+
+def test_clip_plane(pkg, device, oracle):
+    sc = small_spheres(pkg, res=128, renderer="raycast")
+    sc["renderer"]["clipPlanes"] = [[0.0, 0.0, 1.0, 0.0]]
+    gpu = render_gpu(pkg, device, sc)
+    _, F = render_oracle(oracle, sc)
+    good, frac = raycast_ok(gpu, F)
+    assert good, frac
+    sc["renderer"]["type"] = "pathtrace"
+    gpu = render_gpu(pkg, device, sc)
+    _, F = render_oracle(oracle, sc)
+    d = np.abs(gpu["color"][..., :3] - F.color[..., :3]).max(axis=-1)
+    assert float((d <= 1e-3).mean()) >= 0.97
+
+
+def test_instance_transform(pkg, device, oracle):
+    """A group placed by an instance transform (rotation + scale + translation)."""
+    base = small_spheres(pkg, res=128, renderer="raycast", n=10)
+    c, s = np.cos(0.4), np.sin(0.4)
+    xfm = [c * 1.2, 0.0, -s * 1.2, 0.0, 1.2, 0.0, s * 1.2, 0.0, c * 1.2, 1.0, -0.5, 2.0]
+    sc = dict(base)
+    sc["instances"] = [{"transform": xfm, "surfaces": base["surfaces"][:5]}]
+    sc["surfaces"] = base["surfaces"][5:]
+    gpu = render_gpu(pkg, device, sc)
+    _, F = render_oracle(oracle, sc)
+    good, frac = raycast_ok(gpu, F)
+    assert good, frac
+
+
+def test_color_formats(pkg, device, oracle):
+    sc = pkg.scenes.config0(res=64, n=32)
+    h = pkg.scenes.build(device, sc, channels=("depth",))
+    vsr = pkg.vsr
+    for t in (vsr.UFIXED8_VEC4, vsr.UFIXED8_RGBA_SRGB):
+        device.set(h["frame"], "channel.color", t, vsr.DATA_TYPE)
+        device.commit(h["frame"])
+        device.render(h["frame"])
+        device.wait(h["frame"])
+        px = device.map(h["frame"], "channel.color")
+        _, F = render_oracle(oracle, sc)
+        c = np.clip(F.color, 0, 1)
+        if t == vsr.UFIXED8_RGBA_SRGB:
+            lin = c[..., :3]
+            c[..., :3] = np.where(lin <= 0.0031308, 12.92 * lin, 1.055 * lin ** (1 / 2.4) - 0.055)
+        ref = (255.0 * c).astype(np.uint32)
+        got = np.stack([(px >> (8 * k)) & 255 for k in range(4)], -1)
+        assert np.abs(got.astype(np.int64) - ref).max() <= 1
+
+
+def test_incomplete_frame_reports_error(pkg, device):
+    vsr = pkg.vsr
+    f = device.frame()
+    device.set(f, "size", (8, 8), vsr.UINT32_VEC2)
+    device.commit(f)
+    n0 = len(device.messages)
+    assert device.render(f) == 6  # VSR_ERROR_INCOMPLETE
+    assert any("incomplete" in m[2] for m in device.messages[n0:])
+    device.release(f)
+
+
+def test_full_config1_rows_against_oracle(pkg, device, oracle):
+    """Config 1 at full size on the GPU; a band of rows checked against the oracle."""
+    sc = pkg.scenes.config1()
+    h = pkg.scenes.build(device, sc)
+    device.render(h["frame"])
+    device.wait(h["frame"])
+    color = device.map(h["frame"], "channel.color")
+    assert device.get_uint(h["frame"], "errorFlags") == 0
+    assert not np.isnan(color).any()
+    S = oracle.Scene(sc)
+    F = oracle.Frame(1024, 1024)
+    oracle.render(S, F, rows=(500, 504))
+    d = np.abs(color[500:504, :, :3] - F.color[500:504, :, :3]).max(axis=-1)
+    assert float((d <= 1e-3).mean()) >= 0.95

@@ -1,0 +1,275 @@
+"""The CPU oracle pinned against known answers (no GPU).
+
+The reference ships no tests, golden images or fixtures, so the oracle is
+pinned by (a) golden vectors of the in-reference LCG computed by an
+independent restatement (tests/golden/lcg.json), (b) closed-form cases:
+texel-centred trilinear sampling, a Lambertian plane under a directional
+light, an emission-absorption slab, (c) brute-force cross-checks of the BVH
+and of the majorant grid, and (d) invariants of the DDA and the BSDF
+sampler.
+"""
+import ctypes
+import json
+import math
+import os
+
+import numpy as np
+import pytest
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+def test_lcg_matches_golden(oracle):
+    lib = oracle.load()
+    with open(os.path.join(GOLDEN, "lcg.json")) as f:
+        cases = json.load(f)
+    for c in cases:
+        out = np.zeros(len(c["values"]), np.float32)
+        lib.or_lcg_sequence(c["seed"][0], c["seed"][1], len(out), oracle.fptr(out))
+        assert np.array_equal(out, np.asarray(c["values"], np.float32)), c["seed"]
+
+
+def _volume(oracle, data, tf):
+    v = oracle.OrVolume()
+    v._data = np.ascontiguousarray(data, np.float32)
+    v._tf = np.ascontiguousarray(tf, np.float32)
+    v.data = oracle.fptr(v._data)
+    nz, ny, nx = v._data.shape
+    v.dims = (ctypes.c_int32 * 3)(nx, ny, nz)
+    v.origin = oracle.farr(3, [0, 0, 0])
+    v.spacing = oracle.farr(3, [1, 1, 1])
+    v.tf = oracle.fptr(v._tf)
+    v.tfSize = len(v._tf)
+    v.valueRange = oracle.farr(2, [0, 1])
+    v.unitDistance = 1.0
+    return v
+
+
+def test_trilinear_texel_centres_and_clamp(oracle):
+    lib = oracle.load()
+    rng = np.random.default_rng(1)
+    data = rng.uniform(0, 1, (5, 6, 7)).astype(np.float32)
+    v = _volume(oracle, data, np.ones((4, 4)))
+    nz, ny, nx = data.shape
+    for (i, j, k) in [(0, 0, 0), (6, 5, 4), (3, 2, 1)]:
+        p = ((i + 0.5) / nx, (j + 0.5) / ny, (k + 0.5) / nz)
+        assert lib.or_sample_field(ctypes.byref(v), *p) == pytest.approx(data[k, j, i], abs=1e-6)
+    # clamp addressing outside [0,1]
+    assert lib.or_sample_field(ctypes.byref(v), -3.0, -3.0, -3.0) == pytest.approx(data[0, 0, 0])
+    assert lib.or_sample_field(ctypes.byref(v), 4.0, 4.0, 4.0) == pytest.approx(data[-1, -1, -1])
+    # linear along x between centres
+    p = ((1 + 0.5 + 0.25) / nx, (2 + 0.5) / ny, (3 + 0.5) / nz)
+    ref = 0.75 * data[3, 2, 1] + 0.25 * data[3, 2, 2]
+    assert lib.or_sample_field(ctypes.byref(v), *p) == pytest.approx(ref, abs=1e-6)
+
+
+def test_tf_lookup_bins(oracle):
+    lib = oracle.load()
+    tf = np.stack([np.linspace(0, 1, 8)] * 4, -1).astype(np.float32)
+    v = _volume(oracle, np.zeros((2, 2, 2)), tf)
+    out = np.zeros(4, np.float32)
+    for i in range(8):
+        lib.or_tf_lookup(ctypes.byref(v), (i + 0.5) / 8, oracle.fptr(out))
+        assert np.allclose(out, tf[i])
+    lib.or_tf_lookup(ctypes.byref(v), 2.0, oracle.fptr(out))
+    assert np.allclose(out, tf[-1])
+
+
+def test_tf_build_restatement(oracle):
+    """TransferFunction1D::finalize resampling: 3 colours, 5 opacities -> 5 entries."""
+    color = np.array([[1, 0, 0], [0, 1, 0], [0, 0, 1]], np.float32)
+    opacity = np.array([0, 0.25, 0.5, 0.75, 1.0], np.float32)
+    tf = oracle.build_tf(color, opacity)
+    assert tf.shape == (5, 4)
+    assert np.allclose(tf[0], [1, 0, 0, 0])
+    assert np.allclose(tf[2], [0, 1, 0, 0.5])
+    assert np.allclose(tf[1], [0.5, 0.5, 0, 0.25])
+    assert np.allclose(tf[4], [0, 0, 1, 1])
+
+
+def plane_scene(color=(0.6, 0.5, 0.4), light_dir=(0.0, -0.6, -0.8), irradiance=2.0,
+                renderer="raycast"):
+    g = 50.0
+    quad = np.array([[-g, -g, 0], [g, -g, 0], [g, g, 0], [-g, g, 0]], np.float32)
+    return {
+        "surfaces": [{"vertices": quad, "indices": np.array([[0, 1, 2], [0, 2, 3]], np.uint32),
+                      "material": {"type": "matte", "color": list(color)}}],
+        "volumes": [],
+        "lights": [{"direction": list(light_dir), "irradiance": irradiance}],
+        "camera": {"type": "perspective", "position": [0.0, 0.0, 10.0],
+                   "direction": [0.0, 0.0, -1.0], "up": [0.0, 1.0, 0.0],
+                   "fovy": math.radians(30.0), "aspect": 1.0},
+        "renderer": {"type": renderer, "ambientRadiance": 0.2, "background": [0, 0, 0, 1]},
+        "frame": {"size": (16, 16)},
+    }
+
+
+def test_lambertian_plane_closed_form(oracle):
+    """Raycast of a matte plane: c/pi * E * cos(theta) + c * ambient."""
+    sc = plane_scene()
+    S = oracle.Scene(sc)
+    F = oracle.Frame(16, 16)
+    oracle.render(S, F)
+    c = np.array([0.6, 0.5, 0.4])
+    L = -np.array([0.0, -0.6, -0.8])
+    cos = max(0.0, float(np.dot([0, 0, 1], L / np.linalg.norm(L))))
+    expect = c / math.pi * 2.0 * cos + c * 0.2
+    assert np.allclose(F.color[..., :3], expect, atol=1e-5)
+    assert np.allclose(F.color[..., 3], 1.0)
+    assert np.allclose(F.depth[8, 8], 10.0, rtol=1e-3)
+    assert np.allclose(F.normal, [0, 0, 1], atol=1e-6)
+    assert np.allclose(F.albedo, c, atol=1e-6)
+
+
+def test_emission_absorption_slab(oracle):
+    """Constant field, TF alpha a: alpha after k steps is 1 - (1-a)^(k dt/ud)."""
+    n = 16
+    data = np.full((n, n, n), 0.5, np.float32)
+    a = 0.02
+    tf = np.array([[1, 1, 1, a]] * 4, np.float32)
+    sc = {
+        "surfaces": [], "lights": [],
+        "volumes": [{"data": data, "origin": [0, 0, 0], "spacing": [1, 1, 1],
+                     "color": tf[:, :3], "opacity": tf[:, 3], "valueRange": [0, 1],
+                     "unitDistance": 1.0}],
+        "camera": {"type": "orthographic", "position": [7.5, 7.5, 40.0],
+                   "direction": [0, 0, -1], "up": [0, 1, 0], "height": 4.0, "aspect": 1.0},
+        "renderer": {"type": "raycast", "volumeSamplingRate": 1.0, "background": [0, 0, 0, 1]},
+        "frame": {"size": (4, 4)},
+    }
+    S = oracle.Scene(sc)
+    F = oracle.Frame(4, 4)
+    oracle.render(S, F)
+    # path length through the box is 15 (z from 15 to 0): 16 samples at dt = 1
+    k = 16
+    alpha = 1.0 - (1.0 - a) ** k
+    # colour = alpha * sum(T_i (1-Tr)) -> alpha*alpha; composited over black bg (alpha 1)
+    assert np.allclose(F.color[..., 0], alpha * alpha, rtol=1e-4)
+    assert np.allclose(F.color[..., 3], alpha + (1 - alpha), rtol=1e-6)
+
+
+def test_bvh_closest_hit_matches_brute_force(oracle, pkg):
+    lib = oracle.load()
+    rng = np.random.default_rng(3)
+    sc = pkg.scenes.config1(res=8, spp=1, num_spheres=12, nu=12, nv=6)
+    S = oracle.Scene(sc)
+    tris = []
+    for s in sc["surfaces"]:
+        tris.append(np.asarray(s["vertices"])[np.asarray(s["indices"])])
+    T = np.concatenate(tris).astype(np.float64)
+    v1, e1, e2 = T[:, 0], T[:, 1] - T[:, 0], T[:, 2] - T[:, 0]
+    for _ in range(200):
+        o = rng.uniform(-14, 14, 3)
+        d = rng.normal(size=3)
+        d /= np.linalg.norm(d)
+        s1 = np.cross(d, e2)
+        div = np.einsum("ij,ij->i", s1, e1)
+        with np.errstate(divide="ignore", invalid="ignore"):
+            inv = 1.0 / div
+            dd = o - v1
+            b1 = np.einsum("ij,ij->i", dd, s1) * inv
+            s2 = np.cross(dd, e1)
+            b2 = (s2 @ d) * inv
+            t = np.einsum("ij,ij->i", e2, s2) * inv
+        ok = (div != 0) & (b1 >= 0) & (b1 <= 1) & (b2 >= 0) & (b1 + b2 <= 1) & (t >= 0)
+        of = (ctypes.c_float * 3)(*o)
+        df = (ctypes.c_float * 3)(*d)
+        tt = ctypes.c_float(0)
+        ins, tri = ctypes.c_uint32(0), ctypes.c_uint32(0)
+        uv = (ctypes.c_float * 2)()
+        hit = lib.or_trace(S.handle, of, df, 0.0, 3.0e38, ctypes.byref(tt), ctypes.byref(ins),
+                           ctypes.byref(tri), uv)
+        assert bool(hit) == bool(ok.any())
+        if hit:
+            assert tt.value == pytest.approx(t[ok].min(), rel=1e-4)
+
+
+def test_dda_visits_a_connected_cell_path(oracle):
+    lib = oracle.load()
+    rng = np.random.default_rng(5)
+    dims = (ctypes.c_int32 * 3)(8, 5, 7)
+    lo, hi = oracle.farr(3, [0, 0, 0]), oracle.farr(3, [1, 1, 1])
+    for _ in range(50):
+        o = rng.uniform(0.05, 0.95, 3)
+        d = rng.normal(size=3)
+        d /= np.linalg.norm(d)
+        cells = (ctypes.c_int32 * 64)()
+        t01 = (ctypes.c_float * 128)()
+        n = lib.or_dda(oracle.farr(3, o), oracle.farr(3, d), 0.0, 10.0, dims, lo, hi, cells, t01, 64)
+        assert 1 <= n <= 8 + 5 + 7
+        ids = [cells[i] for i in range(n)]
+        xyz = [(c % 8, (c // 8) % 5, c // 40) for c in ids]
+        for a, b in zip(xyz, xyz[1:]):
+            assert sum(abs(p - q) for p, q in zip(a, b)) >= 1
+            assert max(abs(p - q) for p, q in zip(a, b)) == 1
+        ts = [t01[i] for i in range(2 * n)]
+        assert all(ts[2 * i] <= ts[2 * i + 1] + 1e-6 for i in range(n))
+        start = (min(int(o[0] * 8), 7), min(int(o[1] * 5), 4), min(int(o[2] * 7), 6))
+        assert xyz[0] == start
+
+
+def test_brick_majorants_bound_samples(oracle):
+    """Every trilinear sample inside a brick has TF alpha <= the brick's majorant."""
+    lib = oracle.load()
+    rng = np.random.default_rng(7)
+    n = 20
+    data = rng.uniform(0, 1, (n, n, n)).astype(np.float32)
+    tfa = rng.uniform(0, 1, 32).astype(np.float32)
+    color = np.ones((32, 3), np.float32)
+    vol = {"data": data, "origin": [0, 0, 0], "spacing": [1, 1, 1], "color": color,
+           "opacity": tfa, "valueRange": [0, 1], "unitDistance": 1.0, "majorantBrickSize": 8}
+    sc = {"surfaces": [], "lights": [], "volumes": [vol],
+          "camera": {"type": "perspective", "position": [0, 0, 0], "direction": [0, 0, 1],
+                     "up": [0, 1, 0]}, "renderer": {"type": "pathtrace"}, "frame": {"size": (1, 1)}}
+    S = oracle.Scene(sc, grid_method=oracle.GRID_BRICK)
+    dims = (ctypes.c_int32 * 3)()
+    out = np.zeros(64, np.float32)
+    nc = lib.or_majorants(S.handle, 0, dims, oracle.fptr(out), 64)
+    G = dims[0]
+    assert nc == G ** 3 == 27
+    V = S.vols[0]
+    res = np.zeros(4, np.float32)
+    for _ in range(3000):
+        p = rng.uniform(0, 1, 3)
+        k = np.minimum((p * G).astype(int), G - 1)
+        v = lib.or_sample_field(ctypes.byref(V), *p)
+        lib.or_tf_lookup(ctypes.byref(V), v, oracle.fptr(res))
+        cell = (k[2] * G + k[1]) * G + k[0]
+        assert res[3] <= out[cell] + 1e-6
+
+
+def test_sample_material_invariants(oracle):
+    lib = oracle.load()
+    rng = np.random.default_rng(9)
+    for mtype in ("matte", "physicallyBased"):
+        for _ in range(200):
+            m = {"type": mtype, "color": [0.5, 0.6, 0.7], "baseColor": [0.5, 0.6, 0.7],
+                 "metallic": float(rng.uniform()), "roughness": float(rng.uniform())}
+            om = oracle.material(m)
+            n = np.array([0.0, 0.0, 1.0])
+            v = rng.normal(size=3)
+            v[2] = abs(v[2]) + 0.05
+            v /= np.linalg.norm(v)
+            d = np.zeros(3, np.float32)
+            f = np.zeros(3, np.float32)
+            pdf, cosT = ctypes.c_float(), ctypes.c_float()
+            lib.or_sample_material(ctypes.byref(om), oracle.farr(3, n), oracle.farr(3, n),
+                                   oracle.farr(3, v), int(rng.integers(1 << 30)), 7,
+                                   oracle.fptr(d), oracle.fptr(f), ctypes.byref(pdf), ctypes.byref(cosT))
+            if np.isnan(d).any():
+                continue
+            assert abs(np.linalg.norm(d) - 1.0) < 1e-4
+            assert cosT.value == pytest.approx(max(0.0, d[2]), abs=1e-5)
+            if d[2] > 1e-3:
+                assert pdf.value > 0
+            assert np.all(f >= 0)
+
+
+def test_render_is_thread_count_independent(oracle, pkg):
+    sc = pkg.scenes.config1(res=24, spp=2, num_spheres=6, nu=12, nv=6)
+    S = oracle.Scene(sc)
+    a, b = oracle.Frame(24, 24), oracle.Frame(24, 24)
+    oracle.render(S, a, num_threads=1)
+    oracle.render(S, b, num_threads=4)
+    assert np.array_equal(a.color, b.color)
+    assert np.array_equal(a.depth, b.depth)

@@ -150,6 +150,70 @@ def config1(res=1024, spp=64, num_spheres=256, nu=64, nv=32, max_bounce=5,
     }
 
 
+def value_noise(n, rng, octaves=6, base_freq=4, persistence=0.5):
+    """Multi-octave value noise at voxel centres, clamped to [0,1].
+
+    Octave o has a (f+1)^3 lattice (f = base_freq * 2^o) of uniform values,
+    smoothstep-weighted trilinear interpolation, amplitude persistence^o:
+    field = clamp(0.5 + sum_o persistence^o * (noise_o - 0.5), 0, 1).
+    Interpolation is separable, so each octave is three small matrix products.
+    """
+    p = (np.arange(n, dtype=np.float64) + 0.5) / n
+    field = np.full((n, n, n), 0.5, np.float64)
+    for o in range(octaves):
+        f = base_freq * (2 ** o)
+        lat = rng.uniform(0.0, 1.0, size=(f + 1, f + 1, f + 1))
+        x = p * f
+        i0 = np.minimum(np.floor(x).astype(int), f - 1)
+        t = x - i0
+        t = t * t * (3 - 2 * t)
+        M = np.zeros((n, f + 1))
+        M[np.arange(n), i0] = 1 - t
+        M[np.arange(n), i0 + 1] += t
+        # lat indexed [z, y, x]
+        a = np.einsum("zyx,ix->zyi", lat, M)
+        a = np.einsum("zyi,jy->zji", a, M)
+        a = np.einsum("zji,kz->kji", a, M)
+        field += (persistence ** o) * (a - 0.5)
+    return np.clip(field, 0.0, 1.0).astype(np.float32)
+
+
+def smoke_tf(n=256, start=0.5, alpha_max=0.5):
+    """Smoke-like TF: zero opacity below `start`, then linear to alpha_max."""
+    t = np.linspace(0.0, 1.0, n, dtype=np.float32)
+    color = np.stack([0.9 + 0.1 * t, 0.85 - 0.25 * t, 0.8 - 0.5 * t], axis=1).astype(np.float32)
+    opacity = (np.clip((t - start) / (1.0 - start), 0.0, 1.0) * alpha_max).astype(np.float32)
+    return color, opacity
+
+
+def config2(res=(1920, 1080), spp=256, n=512, num_spheres=256, nu=64, nv=32, max_bounce=8,
+            seed=SEED_BASE + 2):
+    """Volumetric path tracing: value-noise volume over [-12,12]^3 (density
+    scale 50: unitDistance = 1/50 world units), delta tracking against 16^3
+    voxel brick majorants, the config-1 sphere set, clip plane (0,0,1,0)."""
+    rng = np.random.default_rng(seed)
+    data = value_noise(n, rng)
+    color, opacity = smoke_tf()
+    surfaces = sphere_set(np.random.default_rng(SEED_BASE + 1), num_spheres, nu, nv)
+    spacing = 24.0 / (n - 1)
+    light_dir = np.array([-0.35, -1.0, -0.45])
+    light_dir /= np.linalg.norm(light_dir)
+    W, H = res
+    return {
+        "surfaces": surfaces,
+        "volumes": [{"data": data, "origin": [-12.0, -12.0, -12.0], "spacing": [spacing] * 3,
+                     "color": color, "opacity": opacity, "valueRange": [0.0, 1.0],
+                     "unitDistance": 1.0 / 50.0, "majorantBrickSize": 16}],
+        "lights": [{"direction": [float(x) for x in light_dir], "color": [1.0, 1.0, 1.0],
+                    "irradiance": 3.0}],
+        "camera": _look_at_camera([0.0, -1.0, 0.0], [6.0, 9.0, 34.0], 45.0, W / H),
+        "renderer": {"type": "pathtrace", "pixelSamples": spp, "maxBounce": max_bounce,
+                     "ambientRadiance": 0.2, "background": [0, 0, 0, 1],
+                     "clipPlanes": [[0.0, 0.0, 1.0, 0.0]]},
+        "frame": {"size": (W, H)},
+    }
+
+
 def triangle_count(scene):
     return sum(len(s["indices"]) for s in scene["surfaces"])
 

@@ -22,7 +22,7 @@ CXX_FLAGS = ["-std=c++17", "-O2", "-fPIC", "-fvisibility=hidden", "-ffp-contract
 
 CU_SOURCES = ["k_render.cu", "k_bvh.cu", "k_volume.cu"]
 CPP_SOURCES = ["runtime.cpp"]
-HEADERS = ["vsr_device.h", "render_common.cuh", "kernels.h"]
+HEADERS = ["vsr_device.h", "render_common.cuh", "kernels.h", "bvh_kernels.cuh"]
 
 
 def _cuda_home():

@@ -1513,4 +1513,14 @@ void *vsrDeviceStream(VSRDevice dv) {
   return d ? (void *)d->stream : nullptr;
 }
 
+VSRStatus vsrBuildTriangleBVH(const float *v1, const float *e1, const float *e2, uint32_t n,
+                              void *nodesOut, void *trisOut, void *stream) {
+  if (n == 0) return VSR_OK;
+  if (!v1 || !e1 || !e2 || !nodesOut || !trisOut || n >= (1u << 27))
+    return VSR_ERROR_INVALID_ARGUMENT;
+  cudaError_t e = buildGroupBVH(v1, e1, e2, (int)n, (float4 *)nodesOut, (float4 *)trisOut, nullptr,
+                                (cudaStream_t)stream);
+  return e == cudaSuccess ? VSR_OK : VSR_ERROR_CUDA;
+}
+
 } // extern "C"

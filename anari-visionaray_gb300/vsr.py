@@ -65,6 +65,7 @@ _SIGNATURES = [
     ("vsrMapFrameDevice", _P, [_P, _P, ctypes.c_char_p, ctypes.POINTER(ctypes.c_uint32),
                                ctypes.POINTER(ctypes.c_uint32), ctypes.POINTER(ctypes.c_int)]),
     ("vsrDeviceStream", _P, [_P]),
+    ("vsrBuildTriangleBVH", ctypes.c_int, [_P, _P, _P, ctypes.c_uint32, _P, _P, _P]),
 ]
 
 EXPORTED_SYMBOLS = [s[0] for s in _SIGNATURES]

@@ -189,6 +189,22 @@ VSR_API const void *vsrMapFrameDevice(VSRDevice d, VSRFrame f, const char *chann
    order their own GPU work against frames. */
 VSR_API void *vsrDeviceStream(VSRDevice d);
 
+/* Device-side BVH build for a triangle set whose data already lives in GPU
+   memory; replaces DeviceBVH<basic_triangle>::update + deviceIndexBVH2
+   (DeviceBVH.h:51-55, :266-335), which the reference's Triangle::finalize
+   calls (scene/surface/geometry/Triangle.cpp:200-206).
+     v1, e1, e2 : device pointers, n packed float3 each (e1 = v2-v1,
+                  e2 = v3-v1, Triangle.cpp:76-83)
+     nodesOut   : device pointer, 4*max(n-1,1) float4 (64-byte BVH2 nodes)
+     trisOut    : device pointer, 3*n float4 (leaf-ordered triangles)
+     stream     : cudaStream_t to run on (NULL = legacy default stream)
+   Temporary device memory is taken from the stream-ordered allocator and
+   returned before the call completes on the stream. The call returns once
+   the work is enqueued. Returns VSR_OK, VSR_ERROR_INVALID_ARGUMENT or
+   VSR_ERROR_CUDA. Requires n < 2^27. */
+VSR_API VSRStatus vsrBuildTriangleBVH(const float *v1, const float *e1, const float *e2,
+                                      uint32_t n, void *nodesOut, void *trisOut, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

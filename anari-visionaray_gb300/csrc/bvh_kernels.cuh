@@ -80,21 +80,34 @@ __device__ __forceinline__ uint64_t expandBits21(uint32_t v) {
   return x;
 }
 
+// Sort key: a 3-bit size class above 60 bits of Morton code (20 bits per
+// axis). Triangles whose extent is a large fraction of the scene get the
+// smallest classes, so the hierarchy separates them near the root instead of
+// inflating the boxes of a deep chain of ancestors in the Morton order.
 __global__ void kMorton(const float *v1, const float *e1, const float *e2, int n,
                         const uint32_t *bounds, uint64_t *keys, uint32_t *vals) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   uint32_t q[3];
+  float triExt = 0.f, sceneExt = 0.f;
 #pragma unroll
   for (int a = 0; a < 3; ++a) {
     float lo = orderedToFloat(bounds[a]), hi = orderedToFloat(bounds[3 + a]);
-    float c = v1[3 * i + a] + (e1[3 * i + a] + e2[3 * i + a]) * (1.f / 3.f);
+    float p0 = v1[3 * i + a], p1 = p0 + e1[3 * i + a], p2 = p0 + e2[3 * i + a];
+    float c = p0 + (e1[3 * i + a] + e2[3 * i + a]) * (1.f / 3.f);
     float ext = hi - lo;
     float u = ext > 0.f ? (c - lo) / ext : 0.5f;
     u = fminf(fmaxf(u, 0.f), 1.f);
-    q[a] = (uint32_t)fminf(u * 2097152.f, 2097151.f);
+    q[a] = (uint32_t)fminf(u * 1048576.f, 1048575.f);
+    triExt = fmaxf(triExt, fmaxf(p0, fmaxf(p1, p2)) - fminf(p0, fminf(p1, p2)));
+    sceneExt = fmaxf(sceneExt, ext);
   }
-  keys[i] = (expandBits21(q[0]) << 2) | (expandBits21(q[1]) << 1) | expandBits21(q[2]);
+  // class 0: triangle spans >= 1/4 of the centroid extent ... class 7: < 1/512
+  const float rel = sceneExt > 0.f ? triExt / sceneExt : 0.f;
+  int cls = rel > 0.f ? (int)floorf(-log2f(rel)) - 1 : 7;
+  cls = min(max(cls, 0), 7);
+  keys[i] = ((uint64_t)cls << 60) |
+            (((expandBits21(q[0]) << 2) | (expandBits21(q[1]) << 1) | expandBits21(q[2])));
   vals[i] = (uint32_t)i;
 }
 

@@ -12,6 +12,14 @@ cudaError_t launchRaycast(const DScene &S, const DCamera &C, const DRenderer &R,
 cudaError_t launchPathtrace(const DScene &S, const DCamera &C, const DRenderer &R, const DFrame &F,
                             bool count, cudaStream_t stream);
 
+// Wavefront path tracer (same per-pixel random stream as launchPathtrace):
+// init + iterations of trace/shade over compacted pixel queues until every
+// pixel has finished its pixelSamples samples. pinnedCount is a host-pinned
+// uint32 used to poll the queue size between batches of iterations.
+cudaError_t launchPathtraceWavefront(const DScene &S, const DCamera &C, const DRenderer &R,
+                                     const DFrame &F, const DWave &Wv, uint32_t *pinnedCount,
+                                     bool count, cudaStream_t stream, int *iterations);
+
 // Accumulation reset: accum = 0, depth = 1e31 (frame/Frame.cpp:287-312).
 cudaError_t launchFrameReset(float4 *accum, float *depth, size_t numPixels, cudaStream_t stream);
 

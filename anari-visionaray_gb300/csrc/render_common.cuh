@@ -296,6 +296,9 @@ __device__ __forceinline__ bool traverseGroup(const DGroup &G, float3 o, float3 
   if (Count) {
     atomicAdd(&cnt[1], (unsigned long long)nodeVisits);
     atomicAdd(&cnt[2], (unsigned long long)triTests);
+    // histogram of inner-node visits per traversal, bins [2^k, 2^(k+1))
+    const int bin = nodeVisits ? min(31 - __clz(nodeVisits), 15) : 0;
+    atomicAdd(&cnt[8 + bin], 1ull);
   }
   return found;
 }
@@ -349,7 +352,7 @@ __device__ __forceinline__ float materialOpacity(const DMaterial &m) {
   return m.opacity >= m.alphaCutoff ? 1.f : 0.f;
 }
 
-__device__ float3 evalPBR(const DMaterial &m, float3 Ns, float3 viewDir, float3 lightDir) {
+__device__ inline float3 evalPBR(const DMaterial &m, float3 Ns, float3 viewDir, float3 lightDir) {
   const float metallic = m.metallic;
   const float pr = mapRoughness(m.roughness);
   const float pcr = mapRoughness(m.clearcoatRoughness);
@@ -459,7 +462,7 @@ __device__ __forceinline__ void pdfGGXVNDF(float3 L, float3 V, float ax, float e
 }
 
 // sampleMaterial, renderer/common.h:1371-1415 and :1209-1368.
-__device__ BSDFSample sampleMaterial(const DMaterial &m, float3 Ng, float3 Ns, float3 viewDir,
+__device__ inline BSDFSample sampleMaterial(const DMaterial &m, float3 Ng, float3 Ns, float3 viewDir,
                                      Rng &rnd) {
   BSDFSample res;
   float3 w = faceforward(Ns, viewDir, Ng);

@@ -652,6 +652,7 @@ struct Camera : Object {
 struct Renderer : Object {
   DRenderer r{};
   int sampleLimit = 1024;
+  bool wavefront = true;
   using Object::Object;
   // Renderer.cpp:34-45, Raycast.cpp:16-20, Pathtrace.cpp:16-28
   void commit() override {
@@ -686,6 +687,10 @@ struct Renderer : Object {
     if (r.type == REND_PATHTRACE && geti("pixelSamples", v)) r.pixelSamples = std::min(std::max(v, 1), 256);
     sampleLimit = 1024;
     if (geti("sampleLimit", v)) sampleLimit = std::max(v, 1);
+    // path tracer execution: wavefront queues (default) or one thread per
+    // pixel for the whole frame; both follow the same per-pixel random stream
+    wavefront = true;
+    if (geti("wavefront", v)) wavefront = v != 0;
     float vsr = 0.5f;
     getf("volumeSamplingRate", vsr);
     r.samplingRateInv = vsr > 0.f ? 1.f / vsr : 0.f;
@@ -963,7 +968,40 @@ struct FrameObj : Object {
   bool nextReset = true;
   bool countStats = false;
   DevBuf counters;
-  unsigned long long countersHost[8] = {0};
+  unsigned long long countersHost[24] = {0};
+  // wavefront path-tracer state (allocated on first wavefront render)
+  static constexpr int kWaveF4 = 15;
+  DevBuf waveF4[kWaveF4], waveMeta, waveHit, waveQueue[2], waveCount;
+  size_t wavePixels = 0;
+  uint32_t *pinnedCount = nullptr;
+  int lastIterations = 0;
+
+  bool ensureWave() {
+    size_t np = (size_t)width * height;
+    if (wavePixels == np) return true;
+    bool ok = true;
+    for (auto &b : waveF4) ok = ok && b.alloc(np * sizeof(float4)) == cudaSuccess;
+    ok = ok && waveMeta.alloc(np * sizeof(uint4)) == cudaSuccess &&
+         waveHit.alloc(np * sizeof(int4)) == cudaSuccess &&
+         waveQueue[0].alloc(np * sizeof(uint32_t)) == cudaSuccess &&
+         waveQueue[1].alloc(np * sizeof(uint32_t)) == cudaSuccess &&
+         waveCount.alloc(2 * sizeof(uint32_t)) == cudaSuccess;
+    if (!pinnedCount) ok = ok && cudaMallocHost((void **)&pinnedCount, sizeof(uint32_t)) == cudaSuccess;
+    wavePixels = ok ? np : 0;
+    return ok;
+  }
+  DWave wave() {
+    DWave w{};
+    float4 **f[kWaveF4] = {&w.rayO, &w.rayD, &w.thr, &w.inten, &w.base, &w.shaded, &w.hpo, &w.sn,
+                           &w.bdir, &w.bf, &w.acc, &w.pNg, &w.pAlb, &w.cNg, &w.cAlb};
+    for (int i = 0; i < kWaveF4; ++i) *f[i] = waveF4[i].as<float4>();
+    w.meta = waveMeta.as<uint4>();
+    w.hit = waveHit.as<int4>();
+    w.queue[0] = waveQueue[0].as<uint32_t>();
+    w.queue[1] = waveQueue[1].as<uint32_t>();
+    w.count = waveCount.as<uint32_t>();
+    return w;
+  }
 
   FrameObj(Device *d, VSRDataType k, std::string st) : Object(d, k, st) {
     cudaEventCreate(&evStart);
@@ -976,6 +1014,7 @@ struct FrameObj : Object {
     if (evStart) cudaEventSynchronize(evStop);
     for (auto &kv : pinned) cudaFreeHost(kv.second);
     if (errHost) cudaFreeHost(errHost);
+    if (pinnedCount) cudaFreeHost(pinnedCount);
     cudaEventDestroy(evStart);
     cudaEventDestroy(evRender);
     cudaEventDestroy(evStop);
@@ -1014,7 +1053,7 @@ struct FrameObj : Object {
                 albedo.alloc(np * 3 * sizeof(float)) == cudaSuccess &&
                 color.alloc(np * (colorType == VSR_FLOAT32_VEC4 ? 16 : 4)) == cudaSuccess &&
                 errFlags.alloc(sizeof(uint32_t)) == cudaSuccess &&
-                counters.alloc(8 * sizeof(unsigned long long)) == cudaSuccess;
+                counters.alloc(24 * sizeof(unsigned long long)) == cudaSuccess;
       for (auto &kv : pinned) cudaFreeHost(kv.second);
       pinned.clear();
       if (!ok) {
@@ -1076,7 +1115,7 @@ VSRStatus renderFrame(Device *dev, FrameObj *F) {
     F->nextReset = false;
   }
   cudaMemsetAsync(F->errFlags.p, 0, sizeof(uint32_t), s);
-  if (F->countStats) cudaMemsetAsync(F->counters.p, 0, 8 * sizeof(unsigned long long), s);
+  if (F->countStats) cudaMemsetAsync(F->counters.p, 0, 24 * sizeof(unsigned long long), s);
   cudaEventRecord(F->evRender, s);
   cudaError_t e = cudaSuccess;
   if (F->accumID < F->renderer->sampleLimit) {
@@ -1087,6 +1126,14 @@ VSRStatus renderFrame(Device *dev, FrameObj *F) {
       int stage = 0;
       if (!W->volsHost.empty() && W->volsHost[0].tfSize <= 4096) stage = W->volsHost[0].tfSize;
       e = launchRaycast(W->scene, F->camera->c, R, fr, stage, F->countStats, s);
+    } else if (F->renderer->wavefront) {
+      if (!F->ensureWave()) {
+        dev->report(F, VSR_FRAME, VSR_SEVERITY_ERROR, VSR_ERROR_OUT_OF_MEMORY,
+                    "wavefront state allocation failed");
+        return VSR_ERROR_OUT_OF_MEMORY;
+      }
+      e = launchPathtraceWavefront(W->scene, F->camera->c, R, fr, F->wave(), F->pinnedCount,
+                                   F->countStats, s, &F->lastIterations);
     } else {
       e = launchPathtrace(W->scene, F->camera->c, R, fr, F->countStats, s);
     }
@@ -1095,7 +1142,7 @@ VSRStatus renderFrame(Device *dev, FrameObj *F) {
   cudaEventRecord(F->evStop, s);
   cudaMemcpyAsync(F->errHost, F->errFlags.p, sizeof(uint32_t), cudaMemcpyDeviceToHost, s);
   if (F->countStats)
-    cudaMemcpyAsync(F->countersHost, F->counters.p, 8 * sizeof(unsigned long long),
+    cudaMemcpyAsync(F->countersHost, F->counters.p, 24 * sizeof(unsigned long long),
                     cudaMemcpyDeviceToHost, s);
   F->rendered = true;
   if (e != cudaSuccess) {
@@ -1382,6 +1429,10 @@ int vsrGetProperty(VSRDevice dv, VSRObject ov, const char *name, VSRDataType typ
       *(float *)mem = ms * 1e-3f;
       return 1;
     }
+    if (n == "wavefrontIterations" && type == VSR_INT32 && size >= 4) {
+      *(int32_t *)mem = F->lastIterations;
+      return 1;
+    }
     if (n == "numSamples" && type == VSR_INT32 && size >= 4) {
       *(int32_t *)mem = F->accumID;
       return 1;
@@ -1395,7 +1446,7 @@ int vsrGetProperty(VSRDevice dv, VSRObject ov, const char *name, VSRDataType typ
       return 1;
     }
     if (n == "statistics" && type == VSR_UINT64 && size >= 8 * sizeof(uint64_t)) {
-      memcpy(mem, F->countersHost, 8 * sizeof(uint64_t));
+      memcpy(mem, F->countersHost, std::min<size_t>(size, 24 * sizeof(uint64_t)));
       return 1;
     }
   }

@@ -147,4 +147,29 @@ struct DFrame {
   unsigned long long *counters;  // optional statistics (null = off)
 };
 
+// Wavefront path-tracer state: one slot per pixel, structure of arrays
+// (float4 / uint4 / int4 per pixel, so a warp working on consecutive queue
+// entries reads consecutive 16-byte records), two pixel queues and their
+// counts. Field packing (x,y,z | w):
+//   rayO  : origin         | tmin        rayD  : direction     | tmax
+//   thr   : throughput     | visLight    inten : intensity     | visAO
+//   base  : baseColor      | aoWeights   shaded: shadedColor   | aoCount
+//   hpo   : hitPosOff      | bsdf.pdf    sn    : shading normal| bsdf.cosT
+//   bdir  : bsdf.dir       | tmin of the pass before opacity retraces
+//   bf    : bsdf.f         | retrace count
+//   acc   : sum of sample colours (rgba)
+//   pNg   : sample Ng      | sample depth      pAlb : sample albedo | closest depth
+//   cNg   : closest Ng     | -                 cAlb : closest albedo | -
+//   meta  : rnd state, rng state, flags, passID
+//           flags: rayType(2) firstHit(1) bounceID(9) aoSamples(9) sampleID(9) retrace(1)
+//   hit   : t bits, instance (-1 = miss), local triangle, leaf index
+struct DWave {
+  float4 *rayO, *rayD, *thr, *inten, *base, *shaded, *hpo, *sn, *bdir, *bf, *acc, *pNg, *pAlb,
+      *cNg, *cAlb;
+  uint4 *meta;
+  int4 *hit;
+  uint32_t *queue[2];
+  uint32_t *count;  // [0], [1]
+};
+
 } // namespace vsr

@@ -311,7 +311,9 @@ def apply_renderer(dev, rend, params):
             dev.set(rend, k, v, vsr.FLOAT32_VEC4)
         elif k == "ambientColor":
             dev.set(rend, k, v, vsr.FLOAT32_VEC3)
-        elif isinstance(v, (int, np.integer)) and not isinstance(v, bool):
+        elif isinstance(v, bool):
+            dev.set(rend, k, v)
+        elif isinstance(v, (int, np.integer)):
             dev.set(rend, k, int(v))
         else:
             dev.set(rend, k, float(v))

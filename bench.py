@@ -264,7 +264,7 @@ def run_ours(args):
     dev.commit(frame)
     dev.render(frame)
     dev.wait(frame)
-    counts = dev.get_u64(frame, "statistics", 8) or [0] * 8
+    counts = dev.get_u64(frame, "statistics", 24) or [0] * 24
     dev.set(frame, "collectStatistics", False)
     dev.commit(frame)
 
@@ -287,6 +287,7 @@ def run_ours(args):
     wall = time.perf_counter() - t0
     clk = clocks.stop()
     err = dev.get_uint(frame, "errorFlags")
+    iterations = dev.get_int(frame, "wavefrontIterations")
 
     # end to end through the public API with host buffers
     cam = h["camera"]
@@ -343,9 +344,11 @@ def run_ours(args):
                      "note": f"algorithmic bytes = BVH node fetches x64 B + triangle fetches x48 B "
                              f"+ frame bytes; peak {peak_kind}; most fetches hit L1/L2"},
         "traversal": {"rays": rays, "node_visits": nodes, "tri_tests": tris,
+                      "node_visit_histogram_log2": counts[8:24],
                       "grays_per_s": rays / kernel_s / 1e9},
         "commit_s": commit_s, "bvh_build_s": bvh_s, "raycast_config0": raycast,
         "wall_s_timed": wall, "clocks": clk, "error_flags": err,
+        "wavefront_iterations": iterations,
     }
     if world == 1 and not args.no_cpu_baseline:
         v, dt, px, cores = cpu_baseline(scene, args.cpu_rows)

@@ -97,9 +97,12 @@ def test_raycast_triangles(pkg, device, oracle):
     assert float((ad <= 1e-5).mean()) >= 0.999
 
 
-def test_pathtrace_same_stream(pkg, device, oracle):
-    """Same seeds: the GPU path tracer follows the oracle sample for sample."""
+@pytest.mark.parametrize("wavefront", [True, False])
+def test_pathtrace_same_stream(pkg, device, oracle, wavefront):
+    """Same seeds: the GPU path tracer follows the oracle sample for sample,
+    in both execution modes (wavefront queues / one thread per pixel)."""
     sc = small_spheres(pkg, res=128, spp=8)
+    sc["renderer"]["wavefront"] = wavefront
     gpu = render_gpu(pkg, device, sc)
     _, F = render_oracle(oracle, sc)
     assert not np.isnan(gpu["color"]).any()
@@ -236,9 +239,11 @@ def small_volume_scene(pkg, res=64, spp=4, n=40, spheres=8):
     return sc
 
 
-def test_volume_pathtrace_same_stream(pkg, device, oracle):
+@pytest.mark.parametrize("wavefront", [True, False])
+def test_volume_pathtrace_same_stream(pkg, device, oracle, wavefront):
     """Delta tracking through the brick-majorant DDA: same stream as the oracle."""
     sc = small_volume_scene(pkg)
+    sc["renderer"]["wavefront"] = wavefront
     gpu = render_gpu(pkg, device, sc)
     _, F = render_oracle(oracle, sc, grid=oracle.GRID_BRICK)
     assert gpu["errorFlags"] == 0
@@ -271,3 +276,15 @@ def test_volume_pathtrace_unbiased_vs_unit_majorant(pkg, device, oracle):
     frac = float(inside.all(axis=-1).mean())
     print(f"volume 3-sigma band: {frac:.4f}")
     assert frac >= 0.98, frac
+
+
+def test_wavefront_equals_megakernel(pkg, device):
+    """The two execution modes produce the same frame (same stream, same math)."""
+    sc = small_spheres(pkg, res=96, spp=4, n=16)
+    sc["renderer"]["wavefront"] = True
+    a = render_gpu(pkg, device, sc, frames=2)
+    sc["renderer"]["wavefront"] = False
+    b = render_gpu(pkg, device, sc, frames=2)
+    d = np.abs(a["color"] - b["color"]).max(axis=-1)
+    assert float((d <= 1e-5).mean()) >= 0.99
+    assert np.array_equal(a["depth"], b["depth"])

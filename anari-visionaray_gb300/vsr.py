@@ -79,7 +79,7 @@ def load_library(path=LIB_PATH):
     if _lib is not None:
         return _lib
     if not os.path.exists(path):
-        raise RuntimeError(f"renderer core library not built: {path} (run __graft_entry__.build())")
+        raise RuntimeError(f"renderer core library not built: {path} (run anari-visionaray_gb300/build.py)")
     lib = ctypes.CDLL(path)
     for name, res, args in _SIGNATURES:
         fn = getattr(lib, name)

@@ -121,7 +121,7 @@ def measured_peaks():
 
 def profiled_traffic():
     """DRAM bytes per launch of the path-trace kernel from the committed ncu summary."""
-    path = os.path.join(ROOT, "profiles", "pathtrace_config1.md")
+    path = os.path.join(ROOT, "profiles", "pathtrace_config1.txt")
     if not os.path.exists(path):
         return None
     with open(path) as f:

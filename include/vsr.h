@@ -6,7 +6,7 @@
  * beside it. Object model, parameter names and channel names follow the
  * reference device (VisionarayDevice.cpp:59-214, frame/Frame.cpp:75-94).
  * The ANARI SDK headers are not part of this build, so data-type values are
- * this library's own (VSR_*); INTEGRATION.md maps them to ANARI_*.
+ * this library's own (VSR_*), named after the ANARI_* type they stand for.
  *
  * Errors: every call returns a VSRStatus (0 = success) and reports problems
  * through the device's status callback with a severity, as the reference

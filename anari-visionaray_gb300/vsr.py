@@ -66,6 +66,7 @@ _SIGNATURES = [
                                ctypes.POINTER(ctypes.c_uint32), ctypes.POINTER(ctypes.c_int)]),
     ("vsrDeviceStream", _P, [_P]),
     ("vsrBuildTriangleBVH", ctypes.c_int, [_P, _P, _P, ctypes.c_uint32, _P, _P, _P]),
+    ("vsrBuildTriangleBVHNoAlloc", ctypes.c_int, [_P, _P, _P, ctypes.c_uint32, _P, _P, _P]),
 ]
 
 EXPORTED_SYMBOLS = [s[0] for s in _SIGNATURES]

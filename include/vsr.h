@@ -42,7 +42,8 @@ typedef enum VSRStatus {
   VSR_ERROR_OUT_OF_MEMORY = 4,
   VSR_ERROR_CUDA = 5,
   VSR_ERROR_INCOMPLETE = 6,
-  VSR_ERROR_TIMEOUT = 7
+  VSR_ERROR_TIMEOUT = 7,
+  VSR_ERROR_LIMIT_EXCEEDED = 8
 } VSRStatus;
 
 typedef enum VSRSeverity {
@@ -204,6 +205,27 @@ VSR_API void *vsrDeviceStream(VSRDevice d);
    VSR_ERROR_CUDA. Requires n < 2^27. */
 VSR_API VSRStatus vsrBuildTriangleBVH(const float *v1, const float *e1, const float *e2,
                                       uint32_t n, void *nodesOut, void *trisOut, void *stream);
+
+/* vsrBuildTriangleBVHNoAlloc has no counterpart in the reference. It is the
+   same device BVH build as vsrBuildTriangleBVH (same arguments, bit-identical
+   output) for callers that cannot let a library allocate GPU memory: a host
+   application that owns a fixed GPU memory budget and only passes in buffers
+   it allocated itself, or a per-frame loop that must not risk an allocation
+   or a free (a free can synchronize the whole device) mid-frame. It calls no
+   cudaMalloc, cudaFree or other allocating routine.
+   Limit: n <= VSR_BVH_NOALLOC_MAX_TRIANGLES; a larger n returns
+   VSR_ERROR_LIMIT_EXCEEDED and does nothing.
+   Temporaries live in one 8 MiB buffer in the library's device data, held by
+   every GPU that loads the library until the process exits. All calls on a
+   device share it and it keeps the last call's contents (each call clears
+   what must start at zero). Calls that overlap on the GPU race on the buffer
+   and corrupt each other's result: order them (one stream, or events).
+   The first call on each device, made with that device current, looks up the
+   buffer's device address; make that first call before any stream capture. */
+#define VSR_BVH_NOALLOC_MAX_TRIANGLES 65536u
+VSR_API VSRStatus vsrBuildTriangleBVHNoAlloc(const float *v1, const float *e1, const float *e2,
+                                             uint32_t n, void *nodesOut, void *trisOut,
+                                             void *stream);
 
 #ifdef __cplusplus
 }

@@ -27,7 +27,7 @@ __device__ void raycastSample(const DScene &S, const DRenderer &R, Ray ray, cons
   float surfaceAlpha = 0.f;
   if (S.hasSurfaces) {
     Hit hr;
-    bool hit = traceSurfaces<false, Count>(S, ray, hr, err, cnt);
+    bool hit = traceSurfaces<Count>(S, ray, false, hr, err, cnt);
     bool first = true;
     while (hit) {
       const DInstance &I = S.instances[hr.inst];
@@ -67,7 +67,7 @@ __device__ void raycastSample(const DScene &S, const DRenderer &R, Ray ray, cons
       if (surfaceAlpha < 0.999f) {
         const float eps = epsilonFrom(hitPos, ray.d, hr.t);
         ray.tmin = hr.t + eps;
-        hit = traceSurfaces<false, Count>(S, ray, hr, err, cnt);
+        hit = traceSurfaces<Count>(S, ray, false, hr, err, cnt);
       } else {
         ray.tmax = hr.t;
         break;
@@ -190,9 +190,8 @@ __device__ __forceinline__ void intersectAll(const DScene &S, const Ray &ray, bo
   h.surfHit = false;
   if (S.hasSurfaces) {
     Ray r = ray;
-    bool anyHit = shadow && S.allOpaque;
-    bool hit = anyHit ? traceSurfaces<true, Count>(S, r, h.surf, err, cnt)
-                      : traceSurfaces<false, Count>(S, r, h.surf, err, cnt);
+    const bool anyHit = shadow && S.allOpaque;
+    bool hit = traceSurfaces<Count>(S, r, anyHit, h.surf, err, cnt);
     int guard = 1 << 16;
     while (hit) {
       const DGroup &G = S.groups[S.instances[h.surf.inst].group];
@@ -201,7 +200,7 @@ __device__ __forceinline__ void intersectAll(const DScene &S, const Ray &ray, bo
       if (u > opacity && --guard > 0) {
         const float3 hp = r.o + h.surf.t * r.d;
         r.tmin = h.surf.t + epsilonFrom(hp, r.d, h.surf.t);
-        hit = traceSurfaces<false, Count>(S, r, h.surf, err, cnt);
+        hit = traceSurfaces<Count>(S, r, false, h.surf, err, cnt);
       } else {
         break;
       }

@@ -185,8 +185,7 @@ __global__ void __launch_bounds__(256) kWaveTrace(DScene S, DWave Wv, int cur, u
       h.inst = -1;
     } else if (S.hasSurfaces) {
       const bool anyHit = (rt == RT_SHADOW || rt == RT_AO) && S.allOpaque && !fRetrace(flags);
-      hit = anyHit ? traceSurfaces<true, Count>(S, r, h, err, cnt)
-                   : traceSurfaces<false, Count>(S, r, h, err, cnt);
+      hit = traceSurfaces<Count>(S, r, anyHit, h, err, cnt);
     }
     Wv.hit[p] = hit ? make_int4(__float_as_int(h.t), h.inst, h.tri, h.leaf)
                     : make_int4(__float_as_int(FLT_MAX), -1, -1, -1);

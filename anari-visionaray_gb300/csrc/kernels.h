@@ -45,4 +45,11 @@ cudaError_t buildGroupBVH(const float *v1, const float *e1, const float *e2, int
                           float4 *nodesOut, float4 *trisOut, BvhBuildStats *stats,
                           cudaStream_t stream);
 
+// Same inputs/outputs, PLOC clustering instead of the Karras hierarchy:
+// tighter boxes (close to a greedy SAH build), a few ms more per 1M
+// triangles. Used for world commits unless the world asks for "fast".
+cudaError_t buildGroupBVHQuality(const float *v1, const float *e1, const float *e2, int n,
+                                 float4 *nodesOut, float4 *trisOut, BvhBuildStats *stats,
+                                 cudaStream_t stream);
+
 } // namespace vsr

@@ -208,22 +208,26 @@ __device__ __forceinline__ void localRay(const DInstance &I, float3 o, float3 d,
   ld = mat3mul(I.affineInv, d);
 }
 
-// Stack-based BVH2 traversal, near child first. Closest hit ordered by
-// (t, instance, triangle), the order the CPU restatement uses, so any valid
-// BVH gives the same hit. AnyHit stops at the first accepted hit.
-template <bool AnyHit, bool Count>
+// Stack-based BVH2 traversal, near child first, in the while-while form
+// (an inner-node loop, then a leaf loop) so the lanes of a warp stay in
+// step. One loop serves closest-hit and any-hit rays (anyHit stops at the
+// first accepted hit), so shadow/AO rays and radiance rays in one warp share
+// the same instructions. Closest hits are ordered by (t, instance, triangle),
+// the order the CPU restatement uses, so any valid BVH gives the same hit.
+template <bool Count>
 __device__ __forceinline__ bool traverseGroup(const DGroup &G, float3 o, float3 d, float tmin,
-                                              int inst, Hit &best, uint32_t &err,
+                                              int inst, bool anyHit, Hit &best, uint32_t &err,
                                               unsigned long long *cnt) {
   const float3 inv = f3(1.f / d.x, 1.f / d.y, 1.f / d.z);
   const float3 oi = f3(-o.x * inv.x, -o.y * inv.y, -o.z * inv.z);
   int stack[kTraversalStack];
   int sp = 0;
   int node = 0;
-  bool found = false;
+  bool found = false, done = false;
   unsigned nodeVisits = 0, triTests = 0;
-  for (;;) {
-    if (node >= 0) {
+  while (!done) {
+    // inner nodes until a leaf comes up or nothing is left
+    while (node >= 0) {
       const float4 *N = G.nodes + 4 * (size_t)node;
       const float4 n0 = __ldg(N), n1 = __ldg(N + 1), n2 = __ldg(N + 2);
       const int4 n3 = __ldg(reinterpret_cast<const int4 *>(N + 3));
@@ -232,16 +236,19 @@ __device__ __forceinline__ bool traverseGroup(const DGroup &G, float3 o, float3 
       float a0 = fmaf(n0.x, inv.x, oi.x), b0 = fmaf(n0.y, inv.x, oi.x);
       float a1 = fmaf(n0.z, inv.y, oi.y), b1 = fmaf(n0.w, inv.y, oi.y);
       float a2 = fmaf(n2.x, inv.z, oi.z), b2 = fmaf(n2.y, inv.z, oi.z);
-      float c0min = fmaxf(fmaxf(fminf(a0, b0), fminf(a1, b1)), fmaxf(fminf(a2, b2), tmin));
-      float c0max = fminf(fminf(fmaxf(a0, b0), fmaxf(a1, b1)), fminf(fmaxf(a2, b2), tb));
+      const float c0min = fmaxf(fmaxf(fminf(a0, b0), fminf(a1, b1)), fmaxf(fminf(a2, b2), tmin));
+      const float c0max = fminf(fminf(fmaxf(a0, b0), fmaxf(a1, b1)), fminf(fmaxf(a2, b2), tb));
       a0 = fmaf(n1.x, inv.x, oi.x); b0 = fmaf(n1.y, inv.x, oi.x);
       a1 = fmaf(n1.z, inv.y, oi.y); b1 = fmaf(n1.w, inv.y, oi.y);
       a2 = fmaf(n2.z, inv.z, oi.z); b2 = fmaf(n2.w, inv.z, oi.z);
-      float c1min = fmaxf(fmaxf(fminf(a0, b0), fminf(a1, b1)), fmaxf(fminf(a2, b2), tmin));
-      float c1max = fminf(fminf(fmaxf(a0, b0), fmaxf(a1, b1)), fminf(fmaxf(a2, b2), tb));
+      const float c1min = fmaxf(fmaxf(fminf(a0, b0), fminf(a1, b1)), fmaxf(fminf(a2, b2), tmin));
+      const float c1max = fminf(fminf(fmaxf(a0, b0), fmaxf(a1, b1)), fminf(fmaxf(a2, b2), tb));
       const bool h0 = c0min <= c0max, h1 = c1min <= c1max;
       if (!h0 && !h1) {
-        if (sp == 0) break;
+        if (sp == 0) {
+          done = true;
+          break;
+        }
         node = stack[--sp];
       } else {
         int near = h0 ? n3.x : n3.y;
@@ -253,45 +260,45 @@ __device__ __forceinline__ bool traverseGroup(const DGroup &G, float3 o, float3 
         }
         node = near;
       }
-      continue;
     }
-    // leaf
-    const uint32_t code = ~(uint32_t)node;
-    const int first = (int)(code & kLeafFirstMask);
-    const int count = (int)(code >> kLeafCountShift) + 1;
-    for (int k = 0; k < count; ++k) {
-      const float4 *T = G.tris + 3 * (size_t)(first + k);
-      const float4 ta = __ldg(T), tbv = __ldg(T + 1), tc = __ldg(T + 2);
-      if (Count) ++triTests;
-      const float3 v1 = f3(ta.x, ta.y, ta.z), e1 = f3(tbv.x, tbv.y, tbv.z), e2 = f3(tc.x, tc.y, tc.z);
-      const float3 s1 = cross(d, e2);
-      const float div = dot(s1, e1);
-      if (div == 0.f) continue;
-      const float idiv = 1.f / div;
-      const float3 dd = o - v1;
-      const float bb1 = dot(dd, s1) * idiv;
-      if (bb1 < 0.f || bb1 > 1.f) continue;
-      const float3 s2 = cross(dd, e1);
-      const float bb2 = dot(d, s2) * idiv;
-      if (bb2 < 0.f || bb1 + bb2 > 1.f) continue;
-      const float t = dot(e2, s2) * idiv;
-      if (!(t >= tmin)) continue;
-      const int local = __float_as_int(ta.w);
-      const bool closer =
-          t < best.t || (t == best.t && best.inst >= 0 &&
-                         (inst < best.inst || (inst == best.inst && local < best.tri)));
-      if (!closer) continue;
-      best.t = t; best.u = bb1; best.v = bb2; best.inst = inst; best.tri = local;
-      best.leaf = first + k;
-      found = true;
-      if (AnyHit) {
-        sp = 0;
+    // leaves until an inner node comes up or nothing is left
+    while (!done && node < 0) {
+      const uint32_t code = ~(uint32_t)node;
+      const int first = (int)(code & kLeafFirstMask);
+      const int count = (int)(code >> kLeafCountShift) + 1;
+      for (int k = 0; k < count; ++k) {
+        const float4 *T = G.tris + 3 * (size_t)(first + k);
+        const float4 ta = __ldg(T), tbv = __ldg(T + 1), tc = __ldg(T + 2);
+        if (Count) ++triTests;
+        const float3 v1 = f3(ta.x, ta.y, ta.z), e1 = f3(tbv.x, tbv.y, tbv.z),
+                     e2 = f3(tc.x, tc.y, tc.z);
+        const float3 s1 = cross(d, e2);
+        const float div = dot(s1, e1);
+        if (div == 0.f) continue;
+        const float idiv = 1.f / div;
+        const float3 dd = o - v1;
+        const float bb1 = dot(dd, s1) * idiv;
+        if (bb1 < 0.f || bb1 > 1.f) continue;
+        const float3 s2 = cross(dd, e1);
+        const float bb2 = dot(d, s2) * idiv;
+        if (bb2 < 0.f || bb1 + bb2 > 1.f) continue;
+        const float t = dot(e2, s2) * idiv;
+        if (!(t >= tmin)) continue;
+        const int local = __float_as_int(ta.w);
+        const bool closer =
+            t < best.t || (t == best.t && best.inst >= 0 &&
+                           (inst < best.inst || (inst == best.inst && local < best.tri)));
+        if (!closer) continue;
+        best.t = t; best.u = bb1; best.v = bb2; best.inst = inst; best.tri = local;
+        best.leaf = first + k;
+        found = true;
+      }
+      if ((anyHit && found) || sp == 0) {
+        done = true;
         break;
       }
+      node = stack[--sp];
     }
-    if (AnyHit && found) break;
-    if (sp == 0) break;
-    node = stack[--sp];
   }
   if (Count) {
     atomicAdd(&cnt[1], (unsigned long long)nodeVisits);
@@ -305,9 +312,9 @@ __device__ __forceinline__ bool traverseGroup(const DGroup &G, float3 o, float3 
 
 // intersectSurfaces(Ray, TLS, shadow), DeviceCopyableObjects.h:1826-1839,
 // with intersect(Ray, Instance) :1772-1814 for the instance transform.
-template <bool AnyHit, bool Count>
-__device__ __forceinline__ bool traceSurfaces(const DScene &S, const Ray &r, Hit &h, uint32_t &err,
-                                              unsigned long long *cnt) {
+template <bool Count>
+__device__ __forceinline__ bool traceSurfaces(const DScene &S, const Ray &r, bool anyHit, Hit &h,
+                                              uint32_t &err, unsigned long long *cnt) {
   h.t = r.tmax;
   h.inst = -1;
   h.tri = -1;
@@ -321,9 +328,9 @@ __device__ __forceinline__ bool traceSurfaces(const DScene &S, const Ray &r, Hit
     if (G.numNodes == 0) continue;
     float3 lo, ld;
     localRay(I, r.o, r.d, lo, ld);
-    if (traverseGroup<AnyHit, Count>(G, lo, ld, r.tmin, i, h, err, cnt)) {
+    if (traverseGroup<Count>(G, lo, ld, r.tmin, i, anyHit, h, err, cnt)) {
       any = true;
-      if (AnyHit) break;
+      if (anyHit) break;
     }
   }
   if (!any) h.t = FLT_MAX;

@@ -729,6 +729,7 @@ struct World : Object {
   std::vector<DVolume> volsHost;
   float commitMs = 0.f;
   uint64_t bvhNodes = 0, bvhTris = 0;
+  bool fastBuild = false;
 
   World(Device *d, VSRDataType k, std::string st)
       : Object(d, k, st), implicitGroup(d, VSR_GROUP, "") {
@@ -751,6 +752,9 @@ struct World : Object {
       }
     }
     implicitGroup.commit();
+    // BVH build policy, as the reference's DeviceBVH build flags
+    // (PREFER_FAST_BUILD vs a quality build): "quality" (default) or "fast"
+    fastBuild = gets("bvhBuild", "quality") == "fast";
     implicitUsed = !implicitGroup.surfaces.empty() || !implicitGroup.volumes.empty() ||
                    !implicitGroup.lights.empty();
     valid = true;
@@ -837,8 +841,9 @@ struct World : Object {
           return false;
         }
         BvhBuildStats st{};
-        cudaError_t e = buildGroupBVH(gg->v1.as<float>(), gg->e1.as<float>(), gg->e2.as<float>(), nt,
-                                      gg->nodes.as<float4>(), gg->tris.as<float4>(), &st, s);
+        auto build = fastBuild ? buildGroupBVH : buildGroupBVHQuality;
+        cudaError_t e = build(gg->v1.as<float>(), gg->e1.as<float>(), gg->e2.as<float>(), nt,
+                              gg->nodes.as<float4>(), gg->tris.as<float4>(), &st, s);
         if (e != cudaSuccess) {
           dev->report(this, kind, VSR_SEVERITY_ERROR, VSR_ERROR_CUDA, "BVH build failed: %s",
                       cudaGetErrorString(e));

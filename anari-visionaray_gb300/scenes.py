@@ -358,6 +358,8 @@ def build(dev, scene, channels=("color", "depth", "normal", "albedo"), collect_s
         arr = dev.array1d(insts)
         dev.set(world, "instance", arr)
         keep += [arr] + insts
+    if "bvhBuild" in scene:
+        dev.set(world, "bvhBuild", scene["bvhBuild"])
     dev.commit(world)
     cam = dev.camera(scene["camera"]["type"])
     apply_camera(dev, cam, scene["camera"])

@@ -288,3 +288,17 @@ def test_wavefront_equals_megakernel(pkg, device):
     d = np.abs(a["color"] - b["color"]).max(axis=-1)
     assert float((d <= 1e-5).mean()) >= 0.99
     assert np.array_equal(a["depth"], b["depth"])
+
+
+def test_bvh_build_policies_give_the_same_image(pkg, device):
+    """The fast (LBVH) and quality (PLOC) builds are different trees over the
+    same triangles; closest hits are ordered by (t, instance, triangle), so
+    the frames are identical."""
+    sc = small_spheres(pkg, res=96, spp=2, n=20)
+    sc["bvhBuild"] = "fast"
+    a = render_gpu(pkg, device, sc)
+    sc["bvhBuild"] = "quality"
+    b = render_gpu(pkg, device, sc)
+    assert np.array_equal(a["depth"], b["depth"])
+    d = np.abs(a["color"] - b["color"]).max(axis=-1)
+    assert float((d <= 1e-6).mean()) >= 0.995

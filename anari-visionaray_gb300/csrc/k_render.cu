@@ -238,7 +238,8 @@ __device__ __forceinline__ void intersectAll(const DScene &S, const Ray &ray, bo
 // Per-pixel body of VisionarayRendererPathtrace::renderFrame
 // (renderer/Pathtrace_impl.cpp:498-640) with shade() (:93-487) inlined.
 template <bool Count>
-__global__ void __launch_bounds__(128) kPathtrace(DScene S, DCamera C, DRenderer R, DFrame F) {
+__global__ void __launch_bounds__(16 * VSR_MEGA_BLOCK_Y, VSR_MEGA_MIN_BLOCKS)
+    kPathtrace(DScene S, DCamera C, DRenderer R, DFrame F) {
   const int x = blockIdx.x * blockDim.x + threadIdx.x;
   const int y = blockIdx.y * blockDim.y + threadIdx.y;
   if (x >= F.width || y >= F.height) return;
@@ -467,7 +468,7 @@ cudaError_t launchRaycast(const DScene &S, const DCamera &C, const DRenderer &R,
 
 cudaError_t launchPathtrace(const DScene &S, const DCamera &C, const DRenderer &R, const DFrame &F,
                             bool count, cudaStream_t stream) {
-  dim3 block(16, 8);
+  dim3 block(16, VSR_MEGA_BLOCK_Y);
   if (count)
     kPathtrace<true><<<tileGrid(F, block), block, 0, stream>>>(S, C, R, F);
   else

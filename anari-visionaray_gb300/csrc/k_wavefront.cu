@@ -165,8 +165,8 @@ __global__ void __launch_bounds__(256) kWaveInit(DScene S, DCamera C, DRenderer 
 }
 
 template <bool Count>
-__global__ void __launch_bounds__(256) kWaveTrace(DScene S, DWave Wv, int cur, uint32_t *errFlags,
-                                                  unsigned long long *cnt) {
+__global__ void __launch_bounds__(256, VSR_WAVE_TRACE_MIN_BLOCKS) kWaveTrace(
+    DScene S, DWave Wv, int cur, uint32_t *errFlags, unsigned long long *cnt) {
   const uint32_t n = Wv.count[cur];
   if (blockIdx.x == 0 && threadIdx.x == 0) Wv.count[cur ^ 1] = 0;
   const uint32_t *q = Wv.queue[cur];
@@ -194,8 +194,8 @@ __global__ void __launch_bounds__(256) kWaveTrace(DScene S, DWave Wv, int cur, u
 }
 
 template <bool Count>
-__global__ void __launch_bounds__(256, 1) kWaveShade(DScene S, DCamera C, DRenderer R, DFrame F,
-                                                  DWave Wv, int cur) {
+__global__ void __launch_bounds__(256, VSR_WAVE_SHADE_MIN_BLOCKS) kWaveShade(
+    DScene S, DCamera C, DRenderer R, DFrame F, DWave Wv, int cur) {
   const uint32_t n = Wv.count[cur];
   const uint32_t *qin = Wv.queue[cur];
   uint32_t *qout = Wv.queue[cur ^ 1];

@@ -37,6 +37,21 @@ enum : uint32_t {
   ERR_PATH_LIMIT = 8u,       // path pass limit reached
 };
 
+// Launch-bound tunables (minimum resident blocks per SM) of the path-tracer
+// kernels; they trade registers for occupancy.
+#ifndef VSR_MEGA_MIN_BLOCKS
+#define VSR_MEGA_MIN_BLOCKS 12  // ~40 registers: latency hiding beats spill cost
+#endif
+#ifndef VSR_MEGA_BLOCK_Y
+#define VSR_MEGA_BLOCK_Y 8  // path-tracer megakernel tile: 16 x VSR_MEGA_BLOCK_Y pixels
+#endif
+#ifndef VSR_WAVE_TRACE_MIN_BLOCKS
+#define VSR_WAVE_TRACE_MIN_BLOCKS 1
+#endif
+#ifndef VSR_WAVE_SHADE_MIN_BLOCKS
+#define VSR_WAVE_SHADE_MIN_BLOCKS 1
+#endif
+
 constexpr int kTraversalStack = 64;
 constexpr int kMaxClipPlanes = 8;
 constexpr uint32_t kLeafCountShift = 27;

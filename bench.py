@@ -46,8 +46,8 @@ def parse():
     p.add_argument("--cpu-rows", type=int, default=48,
                    help="rows of the frame the CPU baseline renders (bounded sample)")
     p.add_argument("--no-cpu-baseline", action="store_true")
-    p.add_argument("--megakernel", action="store_true",
-                   help="path tracer with one thread per pixel instead of wavefront queues")
+    p.add_argument("--wavefront", action="store_true",
+                   help="path tracer with wavefront queues instead of one thread per pixel")
     p.add_argument("--no-raycast", dest="raycast", action="store_false",
                    help="skip the config-0 raycast (volume marcher) measurement")
     return p.parse_args()
@@ -246,7 +246,7 @@ def run_ours(args):
         torch.cuda.synchronize()
 
     scene = pkg.scenes.config1(res=args.res, spp=args.spp)
-    scene["renderer"]["wavefront"] = not args.megakernel
+    scene["renderer"]["wavefront"] = args.wavefront
     ntris = pkg.scenes.triangle_count(scene)
     dev = vsr.Device()
     h = pkg.scenes.build(dev, scene)

@@ -269,7 +269,7 @@ __global__ void __launch_bounds__(256, VSR_WAVE_SHADE_MIN_BLOCKS) kWaveShade(
               float t;
               float3 alb;
               if (deltaTrack<Count>(S.volumes[S.groupVolumes[k]], lo, ld, ray.tmin, ray.tmax, rnd,
-                                    t, alb, err, cnt) &&
+                                    t, alb, err, cnt, R.hwFilter != 0) &&
                   t < volT) {
                 volHit = true;
                 volT = t;

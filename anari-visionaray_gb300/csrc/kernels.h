@@ -7,8 +7,11 @@
 
 namespace vsr {
 
+// marchItems (48 B per pixel) and marchCounters (2 uint): device scratch of
+// the warp-per-ray marcher for volume-only worlds; both may be null.
 cudaError_t launchRaycast(const DScene &S, const DCamera &C, const DRenderer &R, const DFrame &F,
-                          int stageTFSize, bool count, cudaStream_t stream);
+                          int stageTFSize, bool count, void *marchItems,
+                          unsigned *marchCounters, cudaStream_t stream);
 cudaError_t launchPathtrace(const DScene &S, const DCamera &C, const DRenderer &R, const DFrame &F,
                             bool count, cudaStream_t stream);
 
@@ -44,6 +47,14 @@ struct BvhBuildStats {
 cudaError_t buildGroupBVH(const float *v1, const float *e1, const float *e2, int n,
                           float4 *nodesOut, float4 *trisOut, BvhBuildStats *stats,
                           cudaStream_t stream);
+
+// Collapse a BVH2 (traversal layout, root 0) into a BVH4 (layout above):
+// each BVH4 node opens the largest-area inner child until it holds four
+// children. nodes4Out needs room for numNodes2 BVH4 nodes. Leaf codes and
+// the leaf-ordered triangles are unchanged. Returns the BVH4 node count in
+// *numNodes4 (synchronizes the stream).
+cudaError_t collapseBVH4(const float4 *nodes2, int numNodes2, float4 *nodes4Out, int *numNodes4,
+                         cudaStream_t stream);
 
 // Same inputs/outputs, PLOC clustering instead of the Karras hierarchy:
 // tighter boxes (close to a greedy SAH build), a few ms more per 1M

@@ -310,6 +310,124 @@ __device__ __forceinline__ bool traverseGroup(const DGroup &G, float3 o, float3 
   return found;
 }
 
+__device__ __forceinline__ void cswap(float &ka, int &ca, float &kb, int &cb) {
+  if (kb < ka) {
+    const float tk = ka; ka = kb; kb = tk;
+    const int tc = ca; ca = cb; cb = tc;
+  }
+}
+
+// Same contract as traverseGroup, over 4-wide nodes (vsr_device.h): one
+// 128-byte fetch tests four child boxes; hit children are ordered by entry
+// distance (a five-exchange sorting network), the nearest is visited next
+// and the others are pushed farthest first.
+template <bool Count>
+__device__ __forceinline__ bool traverseGroup4(const DGroup &G, float3 o, float3 d, float tmin,
+                                               int inst, bool anyHit, Hit &best, uint32_t &err,
+                                               unsigned long long *cnt) {
+  const float3 inv = f3(1.f / d.x, 1.f / d.y, 1.f / d.z);
+  const float3 oi = f3(-o.x * inv.x, -o.y * inv.y, -o.z * inv.z);
+  int stack[kTraversalStack];
+  int sp = 0;
+  int node = 0;
+  bool found = false, done = false;
+  unsigned nodeVisits = 0, triTests = 0;
+  while (!done) {
+    while (node >= 0) {
+      const float4 *N = G.nodes + 8 * (size_t)node;
+      const float4 lx = __ldg(N), hx = __ldg(N + 1), ly = __ldg(N + 2), hy = __ldg(N + 3),
+                   lz = __ldg(N + 4), hz = __ldg(N + 5);
+      const int4 cc = __ldg(reinterpret_cast<const int4 *>(N + 6));
+      if (Count) ++nodeVisits;
+      const float tb = best.t;
+      float k[4];
+      int c[4] = {cc.x, cc.y, cc.z, cc.w};
+      const float lxs[4] = {lx.x, lx.y, lx.z, lx.w}, hxs[4] = {hx.x, hx.y, hx.z, hx.w};
+      const float lys[4] = {ly.x, ly.y, ly.z, ly.w}, hys[4] = {hy.x, hy.y, hy.z, hy.w};
+      const float lzs[4] = {lz.x, lz.y, lz.z, lz.w}, hzs[4] = {hz.x, hz.y, hz.z, hz.w};
+      int hits = 0;
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        const float a0 = fmaf(lxs[j], inv.x, oi.x), b0 = fmaf(hxs[j], inv.x, oi.x);
+        const float a1 = fmaf(lys[j], inv.y, oi.y), b1 = fmaf(hys[j], inv.y, oi.y);
+        const float a2 = fmaf(lzs[j], inv.z, oi.z), b2 = fmaf(hzs[j], inv.z, oi.z);
+        const float cmin = fmaxf(fmaxf(fminf(a0, b0), fminf(a1, b1)), fmaxf(fminf(a2, b2), tmin));
+        const float cmax = fminf(fminf(fmaxf(a0, b0), fmaxf(a1, b1)), fminf(fmaxf(a2, b2), tb));
+        // empty slots are excluded by their code: no box encoding is safe
+        // against a slab test that orders the two planes itself
+        const bool h = cmin <= cmax && c[j] != kEmptyChild;
+        k[j] = h ? cmin : FLT_MAX;
+        hits += h;
+      }
+      if (hits == 0) {
+        if (sp == 0) {
+          done = true;
+          break;
+        }
+        node = stack[--sp];
+        continue;
+      }
+      cswap(k[0], c[0], k[1], c[1]);
+      cswap(k[2], c[2], k[3], c[3]);
+      cswap(k[0], c[0], k[2], c[2]);
+      cswap(k[1], c[1], k[3], c[3]);
+      cswap(k[1], c[1], k[2], c[2]);
+      if (sp + hits - 1 > kTraversalStack) {
+        err |= ERR_STACK_OVERFLOW;
+        hits = 1 + (kTraversalStack - sp);
+      }
+      if (hits > 3) stack[sp++] = c[3];
+      if (hits > 2) stack[sp++] = c[2];
+      if (hits > 1) stack[sp++] = c[1];
+      node = c[0];
+    }
+    while (!done && node < 0) {
+      const uint32_t code = ~(uint32_t)node;
+      const int first = (int)(code & kLeafFirstMask);
+      const int count = (int)(code >> kLeafCountShift) + 1;
+      for (int kk = 0; kk < count; ++kk) {
+        const float4 *T = G.tris + 3 * (size_t)(first + kk);
+        const float4 ta = __ldg(T), tbv = __ldg(T + 1), tc = __ldg(T + 2);
+        if (Count) ++triTests;
+        const float3 v1 = f3(ta.x, ta.y, ta.z), e1 = f3(tbv.x, tbv.y, tbv.z),
+                     e2 = f3(tc.x, tc.y, tc.z);
+        const float3 s1 = cross(d, e2);
+        const float div = dot(s1, e1);
+        if (div == 0.f) continue;
+        const float idiv = 1.f / div;
+        const float3 dd = o - v1;
+        const float bb1 = dot(dd, s1) * idiv;
+        if (bb1 < 0.f || bb1 > 1.f) continue;
+        const float3 s2 = cross(dd, e1);
+        const float bb2 = dot(d, s2) * idiv;
+        if (bb2 < 0.f || bb1 + bb2 > 1.f) continue;
+        const float t = dot(e2, s2) * idiv;
+        if (!(t >= tmin)) continue;
+        const int local = __float_as_int(ta.w);
+        const bool closer =
+            t < best.t || (t == best.t && best.inst >= 0 &&
+                           (inst < best.inst || (inst == best.inst && local < best.tri)));
+        if (!closer) continue;
+        best.t = t; best.u = bb1; best.v = bb2; best.inst = inst; best.tri = local;
+        best.leaf = first + kk;
+        found = true;
+      }
+      if ((anyHit && found) || sp == 0) {
+        done = true;
+        break;
+      }
+      node = stack[--sp];
+    }
+  }
+  if (Count) {
+    atomicAdd(&cnt[1], (unsigned long long)nodeVisits);
+    atomicAdd(&cnt[2], (unsigned long long)triTests);
+    const int bin = nodeVisits ? min(31 - __clz(nodeVisits), 15) : 0;
+    atomicAdd(&cnt[8 + bin], 1ull);
+  }
+  return found;
+}
+
 // intersectSurfaces(Ray, TLS, shadow), DeviceCopyableObjects.h:1826-1839,
 // with intersect(Ray, Instance) :1772-1814 for the instance transform.
 template <bool Count>
@@ -328,7 +446,9 @@ __device__ __forceinline__ bool traceSurfaces(const DScene &S, const Ray &r, boo
     if (G.numNodes == 0) continue;
     float3 lo, ld;
     localRay(I, r.o, r.d, lo, ld);
-    if (traverseGroup<Count>(G, lo, ld, r.tmin, i, anyHit, h, err, cnt)) {
+    const bool f = G.width == 4 ? traverseGroup4<Count>(G, lo, ld, r.tmin, i, anyHit, h, err, cnt)
+                                : traverseGroup<Count>(G, lo, ld, r.tmin, i, anyHit, h, err, cnt);
+    if (f) {
       any = true;
       if (anyHit) break;
     }
@@ -597,12 +717,33 @@ __device__ __forceinline__ float sampleField(const DVolume &V, float3 P) {
   return lerpf(c0, c1, fz);
 }
 
+// Field sample in voxel space: the texture unit's trilinear filter (as
+// tex3D in the reference's CUDA device) or the exact fp32 filter above.
+__device__ __forceinline__ float fieldAt(const DVolume &V, float3 P, bool hw) {
+  return hw ? tex3D<float>(V.tex, P.x, P.y, P.z) : sampleField(V, P);
+}
+
 // tex1D over the TF table (normalized, linear, clamp) after postClassify's
 // value-range normalisation, DeviceCopyableObjects.h:614-619.
 __device__ __forceinline__ float4 tfLookup(const float4 *tf, int n, float vrMin, float vrMax,
                                            float val) {
   val = (val - vrMin) / (vrMax - vrMin);
   const float x = val * n - 0.5f;
+  const float f0 = floorf(x);
+  const float f = x - f0;
+  const int i = (int)fminf(fmaxf(f0, -1.f), (float)n);
+  const int i0 = min(max(i, 0), n - 1), i1 = min(max(i + 1, 0), n - 1);
+  const float4 a = tf[i0], b = tf[i1];
+  return make_float4(lerpf(a.x, b.x, f), lerpf(a.y, b.y, f), lerpf(a.z, b.z, f), lerpf(a.w, b.w, f));
+}
+
+// Classification of a field value. The exact path divides by the value
+// range as postClassify does; the hardware-filter path, already approximate,
+// multiplies by the precomputed reciprocal.
+__device__ __forceinline__ float4 classify(const DVolume &V, const float4 *tf, float val, bool hw) {
+  if (!hw) return tfLookup(tf, V.tfSize, V.vrMin, V.vrMax, val);
+  const int n = V.tfSize;
+  const float x = (val - V.vrMin) * V.vrScale * n - 0.5f;
   const float f0 = floorf(x);
   const float f = x - f0;
   const int i = (int)fminf(fmaxf(f0, -1.f), (float)n);
@@ -637,7 +778,8 @@ __device__ __forceinline__ int projectOnGrid1(float v, float lo, float hi, int n
 // scattering event at object-space parameter tHit.
 template <bool Count>
 __device__ bool deltaTrack(const DVolume &V, float3 o, float3 d, float tmin, float tmax, Rng &rnd,
-                           float &tHit, float3 &albedo, uint32_t &err, unsigned long long *cnt) {
+                           float &tHit, float3 &albedo, uint32_t &err, unsigned long long *cnt,
+                           bool hw) {
   BoxHit bh = intersectBox(o, d, V.boundsLo, V.boundsHi);
   if (!bh.hit || bh.tfar < tmin || bh.tnear > tmax) return false;
   tmin = fmaxf(tmin, bh.tnear);
@@ -667,7 +809,7 @@ __device__ bool deltaTrack(const DVolume &V, float3 o, float3 d, float tmin, flo
       if (Count) ++samples;
       if (--budget <= 0) { err |= ERR_TRACK_LIMIT; return false; }
       float3 P = o + d * t;
-      float4 s = tfLookup(V.tf, V.tfSize, V.vrMin, V.vrMax, sampleField(V, P));
+      float4 s = classify(V, V.tf, fieldAt(V, P, hw), hw);
       float u = rnd();
       if (s.w >= u * majorant) {
         albedo = f3(s.x, s.y, s.z);

@@ -222,7 +222,40 @@ struct SpatialField : Object {
   int dims[3] = {0, 0, 0};
   float origin[3] = {0, 0, 0}, spacing[3] = {1, 1, 1};
   DevBuf data;
+  // texture copy for hardware trilinear filtering (the reference's CUDA
+  // device samples structured fields with tex3D, StructuredRegularField.cpp:42-76)
+  cudaArray_t array = nullptr;
+  cudaTextureObject_t tex = 0;
   using Object::Object;
+  ~SpatialField() override { releaseTexture(); }
+  void releaseTexture() {
+    if (tex) cudaDestroyTextureObject(tex);
+    if (array) cudaFreeArray(array);
+    tex = 0;
+    array = nullptr;
+  }
+  bool makeTexture() {
+    releaseTexture();
+    cudaChannelFormatDesc ch = cudaCreateChannelDesc<float>();
+    cudaExtent ext = make_cudaExtent((size_t)dims[0], (size_t)dims[1], (size_t)dims[2]);
+    if (cudaMalloc3DArray(&array, &ch, ext) != cudaSuccess) return false;
+    cudaMemcpy3DParms cp = {};
+    cp.srcPtr = make_cudaPitchedPtr(data.p, (size_t)dims[0] * sizeof(float), (size_t)dims[0],
+                                    (size_t)dims[1]);
+    cp.dstArray = array;
+    cp.extent = ext;
+    cp.kind = cudaMemcpyDeviceToDevice;
+    if (cudaMemcpy3DAsync(&cp, dev->stream) != cudaSuccess) return false;
+    cudaResourceDesc rd = {};
+    rd.resType = cudaResourceTypeArray;
+    rd.res.array.array = array;
+    cudaTextureDesc td = {};
+    td.addressMode[0] = td.addressMode[1] = td.addressMode[2] = cudaAddressModeClamp;
+    td.filterMode = cudaFilterModeLinear;
+    td.readMode = cudaReadModeElementType;
+    td.normalizedCoords = 1;
+    return cudaCreateTextureObject(&tex, &rd, &td, nullptr) == cudaSuccess;
+  }
   void commit() override {
     valid = false;
     Array *a = geto<Array>("data", VSR_ARRAY3D);
@@ -254,8 +287,12 @@ struct SpatialField : Object {
       dev->report(this, kind, VSR_SEVERITY_ERROR, VSR_ERROR_OUT_OF_MEMORY, "field upload failed");
       return;
     }
-    cudaStreamSynchronize(dev->stream);
     valid = dims[0] >= 2 && dims[1] >= 2 && dims[2] >= 2;
+    if (valid && !makeTexture()) {
+      dev->report(this, kind, VSR_SEVERITY_ERROR, VSR_ERROR_OUT_OF_MEMORY, "field texture creation failed");
+      valid = false;
+    }
+    cudaStreamSynchronize(dev->stream);
   }
   void bounds(float lo[3], float hi[3]) const {
     for (int i = 0; i < 3; ++i) {
@@ -352,6 +389,7 @@ struct Volume : Object {
   }
   DVolume record() const {
     DVolume v{};
+    v.tex = field->tex;
     v.data = field->data.as<float>();
     v.tf = tf.as<float4>();
     v.majorant = majorant.as<float>();
@@ -371,6 +409,7 @@ struct Volume : Object {
     v.cellSize = minSp;
     v.vrMin = vr[0];
     v.vrMax = vr[1];
+    v.vrScale = 1.f / (vr[1] - vr[0]);
     return v;
   }
 };
@@ -695,6 +734,12 @@ struct Renderer : Object {
     float vsr = 0.5f;
     getf("volumeSamplingRate", vsr);
     r.samplingRateInv = vsr > 0.f ? 1.f / vsr : 0.f;
+    // field filtering: "hardware" (texture unit, as the reference's CUDA
+    // device) or "exact" (fp32 trilinear, bit-compatible with the CPU
+    // device). Default: hardware for raycast, exact for the path tracer,
+    // whose delta tracking then follows the CPU device's random stream.
+    std::string vf = gets("volumeFilter", r.type == REND_RAYCAST ? "hardware" : "exact");
+    r.hwFilter = vf == "hardware" ? 1 : 0;
     r.numClipPlanes = 0;
     if (Array *cp = geto<Array>("clipPlane", VSR_ARRAY1D)) {
       if (cp->elemType != VSR_FLOAT32_VEC4) {
@@ -713,8 +758,8 @@ struct Renderer : Object {
 
 // ----------------------------------------------------------------- world
 struct GroupGPU {
-  DevBuf v1, e1, e2, nodes, tris, triSurface, triPrim;
-  int numTris = 0, numNodes = 0;
+  DevBuf v1, e1, e2, nodes, nodes4, tris, triSurface, triPrim;
+  int numTris = 0, numNodes = 0, width = 2;
   float buildMs = 0.f;
 };
 
@@ -731,6 +776,7 @@ struct World : Object {
   float commitMs = 0.f;
   uint64_t bvhNodes = 0, bvhTris = 0;
   bool fastBuild = false;
+  int bvhWidth = 2;
 
   World(Device *d, VSRDataType k, std::string st)
       : Object(d, k, st), implicitGroup(d, VSR_GROUP, "") {
@@ -756,6 +802,11 @@ struct World : Object {
     // BVH build policy, as the reference's DeviceBVH build flags
     // (PREFER_FAST_BUILD vs a quality build): "quality" (default) or "fast"
     fastBuild = gets("bvhBuild", "quality") == "fast";
+    // node width of the traversal BVH: 2 (default, measured faster on the
+    // benchmark scene) or 4
+    int w = 2;
+    geti("bvhWidth", w);
+    bvhWidth = w == 4 ? 4 : 2;
     implicitUsed = !implicitGroup.surfaces.empty() || !implicitGroup.volumes.empty() ||
                    !implicitGroup.lights.empty();
     valid = true;
@@ -853,6 +904,25 @@ struct World : Object {
         gg->numTris = nt;
         gg->numNodes = st.numNodes;
         gg->buildMs = st.buildMs;
+        gg->width = 2;
+        if (bvhWidth == 4 && st.numNodes > 0) {
+          int n4 = 0;
+          auto t4 = std::chrono::steady_clock::now();
+          if (gg->nodes4.alloc((size_t)st.numNodes * 8 * sizeof(float4)) != cudaSuccess ||
+              (e = collapseBVH4(gg->nodes.as<float4>(), st.numNodes, gg->nodes4.as<float4>(), &n4,
+                                s)) != cudaSuccess) {
+            dev->report(this, kind, VSR_SEVERITY_ERROR, VSR_ERROR_CUDA, "BVH4 collapse failed: %s",
+                        cudaGetErrorString(e));
+            return false;
+          }
+          gg->buildMs += std::chrono::duration<float, std::milli>(std::chrono::steady_clock::now() - t4).count();
+          gg->nodes.release();
+          std::swap(gg->nodes.p, gg->nodes4.p);
+          std::swap(gg->nodes.bytes, gg->nodes4.bytes);
+          gg->numNodes = n4;
+          gg->width = 4;
+          st.numNodes = n4;
+        }
         // the build inputs are not needed once the leaf-ordered copy exists
         gg->v1.release();
         gg->e1.release();
@@ -866,6 +936,7 @@ struct World : Object {
       dg.triPrim = gg->triPrim.as<uint32_t>();
       dg.numTris = nt;
       dg.numNodes = gg->numNodes;
+      dg.width = gg->width;
       for (int a = 0; a < 3; ++a) { dg.boundsLo[a] = lo[a]; dg.boundsHi[a] = hi[a]; }
       dgroups[gi] = dg;
       groupsGPU.push_back(std::move(gg));
@@ -964,7 +1035,7 @@ struct FrameObj : Object {
   int width = 10, height = 10;
   VSRDataType colorType = VSR_UNKNOWN, depthType = VSR_UNKNOWN, normalType = VSR_UNKNOWN,
               albedoType = VSR_UNKNOWN;
-  DevBuf color, depth, normal, albedo, accum, errFlags;
+  DevBuf color, depth, normal, albedo, accum, errFlags, marchItems, marchCounters;
   std::map<std::string, void *> pinned;
   uint32_t *errHost = nullptr;
   cudaEvent_t evStart = nullptr, evRender = nullptr, evStop = nullptr;
@@ -1059,6 +1130,8 @@ struct FrameObj : Object {
                 albedo.alloc(np * 3 * sizeof(float)) == cudaSuccess &&
                 color.alloc(np * (colorType == VSR_FLOAT32_VEC4 ? 16 : 4)) == cudaSuccess &&
                 errFlags.alloc(sizeof(uint32_t)) == cudaSuccess &&
+                marchItems.alloc(np * 48) == cudaSuccess &&
+                marchCounters.alloc(2 * sizeof(unsigned)) == cudaSuccess &&
                 counters.alloc(24 * sizeof(unsigned long long)) == cudaSuccess;
       for (auto &kv : pinned) cudaFreeHost(kv.second);
       pinned.clear();
@@ -1131,7 +1204,8 @@ VSRStatus renderFrame(Device *dev, FrameObj *F) {
       // stage the first volume's TF in shared memory when it fits (64 KB)
       int stage = 0;
       if (!W->volsHost.empty() && W->volsHost[0].tfSize <= 4096) stage = W->volsHost[0].tfSize;
-      e = launchRaycast(W->scene, F->camera->c, R, fr, stage, F->countStats, s);
+      e = launchRaycast(W->scene, F->camera->c, R, fr, stage, F->countStats,
+                        F->marchItems.p, F->marchCounters.as<unsigned>(), s);
     } else if (F->renderer->wavefront) {
       if (!F->ensureWave()) {
         dev->report(F, VSR_FRAME, VSR_SEVERITY_ERROR, VSR_ERROR_OUT_OF_MEMORY,

@@ -35,7 +35,12 @@ enum : uint32_t {
   ERR_DDA_LIMIT = 2u,        // DDA step limit reached
   ERR_TRACK_LIMIT = 4u,      // delta-tracking step limit reached
   ERR_PATH_LIMIT = 8u,       // path pass limit reached
+  ERR_MARCH_LIMIT = 16u,     // ray-march step limit reached (dt too small for t)
+  ERR_LAYER_LIMIT = 32u,     // transparent-surface loop limit reached
 };
+
+constexpr int kMaxMarchSteps = 1 << 20;
+constexpr int kMaxSurfaceLayers = 1 << 12;
 
 // Launch-bound tunables (minimum resident blocks per SM) of the path-tracer
 // kernels; they trade registers for occupancy.
@@ -44,6 +49,18 @@ enum : uint32_t {
 #endif
 #ifndef VSR_MEGA_BLOCK_Y
 #define VSR_MEGA_BLOCK_Y 8  // path-tracer megakernel tile: 16 x VSR_MEGA_BLOCK_Y pixels
+#endif
+#ifndef VSR_MARCH_BATCH
+#define VSR_MARCH_BATCH 4  // field fetches issued per thread before compositing
+#endif
+#ifndef VSR_RAYCAST_MIN_BLOCKS
+#define VSR_RAYCAST_MIN_BLOCKS 1
+#endif
+#ifndef VSR_RAYCAST_BLOCK_X
+#define VSR_RAYCAST_BLOCK_X 16  // raycast tile: VSR_RAYCAST_BLOCK_X x VSR_RAYCAST_BLOCK_Y pixels
+#endif
+#ifndef VSR_RAYCAST_BLOCK_Y
+#define VSR_RAYCAST_BLOCK_Y 8
 #endif
 #ifndef VSR_WAVE_TRACE_MIN_BLOCKS
 #define VSR_WAVE_TRACE_MIN_BLOCKS 1
@@ -78,6 +95,8 @@ struct DLight {
 };
 
 struct DVolume {
+  cudaTextureObject_t tex;    // the same field as a 3D texture (linear, clamp, normalized)
+  float vrScale;              // 1 / (vrMax - vrMin)
   const float *data;   // dims.x*dims.y*dims.z, x fastest
   const float4 *tf;    // transfer function table
   const float *majorant;  // gdims cells or null
@@ -91,6 +110,13 @@ struct DVolume {
   float vrMin, vrMax;
 };
 
+// BVH4 node (128 B, 8 x float4): child boxes as structure of arrays
+//   [0] lo.x of children 0..3   [1] hi.x   [2] lo.y   [3] hi.y   [4] lo.z   [5] hi.z
+//   [6] child codes (int bits): >= 0 inner node index, kEmptyChild = no child
+//       (must be tested by code: its box bytes are meaningless), otherwise a
+//       leaf code as for BVH2   [7] unused
+constexpr int kEmptyChild = 0x7fffffff;
+
 struct DGroup {
   const float4 *nodes;
   const float4 *tris;
@@ -98,6 +124,7 @@ struct DGroup {
   const uint32_t *triPrim;
   int numTris;
   int numNodes;
+  int width;              // 2: BVH2 nodes (64 B), 4: BVH4 nodes (128 B)
   int volBegin, volEnd;   // range in DScene::groupVolumes
   float boundsLo[3], boundsHi[3];
 };
@@ -145,6 +172,7 @@ struct DRenderer {
   int maxBounce;
   int pixelSamples;
   float samplingRateInv;
+  int hwFilter;        // 1: field samples through the texture unit's trilinear filter
   int numClipPlanes;
   float clip[kMaxClipPlanes][4];
 };

@@ -311,7 +311,7 @@ def apply_renderer(dev, rend, params):
             dev.set(rend, k, v, vsr.FLOAT32_VEC4)
         elif k == "ambientColor":
             dev.set(rend, k, v, vsr.FLOAT32_VEC3)
-        elif isinstance(v, bool):
+        elif isinstance(v, (str, bool)):
             dev.set(rend, k, v)
         elif isinstance(v, (int, np.integer)):
             dev.set(rend, k, int(v))
@@ -360,6 +360,8 @@ def build(dev, scene, channels=("color", "depth", "normal", "albedo"), collect_s
         keep += [arr] + insts
     if "bvhBuild" in scene:
         dev.set(world, "bvhBuild", scene["bvhBuild"])
+    if "bvhWidth" in scene:
+        dev.set(world, "bvhWidth", int(scene["bvhWidth"]))
     dev.commit(world)
     cam = dev.camera(scene["camera"]["type"])
     apply_camera(dev, cam, scene["camera"])

@@ -995,8 +995,10 @@ PixelSample raycastSample(const Scene &sc, const OrRenderer &R, Ray ray, Counter
   bool hit = false;
   f3 surfaceColor(0.f);
   float surfaceAlpha = 0.f;
+  int layers = 0;
   while (true) {
     if (!hr.hit) break;
+    if (++layers > (1 << 12)) break;  // same bound as the GPU path (zero epsilon would loop)
     const Inst &inst = sc.insts[hr.inst];
     uint32_t surf = S.triSurface[hr.tri];
     const OrMaterial &mat = S.surfMaterial[surf];
@@ -1069,7 +1071,10 @@ PixelSample raycastSample(const Scene &sc, const OrRenderer &R, Ray ray, Counter
     float t = l.tmin;
     float transmittance = 1.f;
     const float expo = dt / vol.v->unitDistance;
-    for (; t <= l.tmax && alpha < 0.99f; t += dt) {
+    int steps = 0;
+    // bounded like the GPU path: dt <= 0 or dt below the float spacing of t
+    // would never end
+    for (; t <= l.tmax && alpha < 0.99f && dt > 0.f && steps < (1 << 20); t += dt, ++steps) {
       f3 P = l.ori + l.dir * t;
       c.march++;
       float v = sampleField(vol.v, P);

@@ -49,9 +49,13 @@ def raycast_ok(gpu, F, tol=RAYCAST_TOL, frac=0.999):
     return ok >= frac, ok
 
 
-def test_raycast_volume_full_config0(pkg, device, oracle):
-    """Config 0 at its full size: 128^3 blob volume, 512x512."""
+@pytest.mark.parametrize("filt", ["hardware", "exact"])
+def test_raycast_volume_full_config0(pkg, device, oracle, filt):
+    """Config 0 at its full size: 128^3 blob volume, 512x512, with the
+    texture unit's trilinear filter (default, as the reference's CUDA device)
+    and with the exact fp32 filter of the CPU device."""
     sc = pkg.scenes.config0()
+    sc["renderer"]["volumeFilter"] = filt
     gpu = render_gpu(pkg, device, sc)
     _, F = render_oracle(oracle, sc)
     good, frac = raycast_ok(gpu, F)
@@ -60,6 +64,8 @@ def test_raycast_volume_full_config0(pkg, device, oracle):
     assert np.all(gpu["normal"] == 0) and np.all(gpu["albedo"] == 0)
     assert gpu["errorFlags"] == 0
     assert gpu["color"][..., :3].max() > 0.05  # the volume is visible
+    if filt == "exact":
+        assert float(np.abs(gpu["color"] - F.color).max()) < 1e-4
 
 
 def test_raycast_volume_sampling_rates(pkg, device, oracle):
@@ -290,14 +296,14 @@ def test_wavefront_equals_megakernel(pkg, device):
     assert np.array_equal(a["depth"], b["depth"])
 
 
-def test_bvh_build_policies_give_the_same_image(pkg, device):
-    """The fast (LBVH) and quality (PLOC) builds are different trees over the
+@pytest.mark.parametrize("build,width", [("fast", 2), ("quality", 4), ("fast", 4)])
+def test_bvh_build_policies_give_the_same_image(pkg, device, build, width):
+    """LBVH / PLOC builds and 2- / 4-wide nodes are different trees over the
     same triangles; closest hits are ordered by (t, instance, triangle), so
-    the frames are identical."""
+    every combination renders the frame of the default (PLOC, 2-wide)."""
     sc = small_spheres(pkg, res=96, spp=2, n=20)
-    sc["bvhBuild"] = "fast"
     a = render_gpu(pkg, device, sc)
-    sc["bvhBuild"] = "quality"
+    sc["bvhBuild"], sc["bvhWidth"] = build, width
     b = render_gpu(pkg, device, sc)
     assert np.array_equal(a["depth"], b["depth"])
     d = np.abs(a["color"] - b["color"]).max(axis=-1)

@@ -203,188 +203,6 @@ __global__ void __launch_bounds__(VSR_RAYCAST_BLOCK_X * VSR_RAYCAST_BLOCK_Y, VSR
   if (err) atomicOr(F.errorFlags, err);
 }
 
-// ------------------------------------------------- warp-cooperative marcher
-// Volume-only raycast worlds: rayMarchVolume<0> (renderer/VolumeIntegration.h:
-// 374-468) with one warp per ray. A warp takes a tile of 32 pixels; each
-// lane sets up its own pixel's ray (camera, clip planes, closest volume box
-// entry); then the warp marches the tile's rays one after the other, lane i
-// taking the i-th of each 32 consecutive samples. Per-sample values are the
-// reference's, and lane i reaches its t by the same sequential t += dt
-// additions as the reference loop; the samples of a chunk are combined with
-// a warp scan of the associative front-to-back operator
-//   (C, A, T)front o (C, A, T)back = (Cf + Tf Cb, Af + Tf Ab, Tf Tb)
-// and a sample is kept only while the alpha accumulated before it is below
-// 0.99, as in the reference. Only the order of the sums differs.
-__device__ __forceinline__ void overScan(float &c0, float &c1, float &c2, float &a, float &tr) {
-  const int lane = threadIdx.x & 31;
-#pragma unroll
-  for (int off = 1; off < 32; off <<= 1) {
-    const float pc0 = __shfl_up_sync(0xffffffffu, c0, off);
-    const float pc1 = __shfl_up_sync(0xffffffffu, c1, off);
-    const float pc2 = __shfl_up_sync(0xffffffffu, c2, off);
-    const float pa = __shfl_up_sync(0xffffffffu, a, off);
-    const float ptr = __shfl_up_sync(0xffffffffu, tr, off);
-    if (lane >= off) {  // (prev) o (mine)
-      c0 = pc0 + ptr * c0;
-      c1 = pc1 + ptr * c1;
-      c2 = pc2 + ptr * c2;
-      a = pa + ptr * a;
-      tr = ptr * tr;
-    }
-  }
-}
-
-// Pass 1, one thread per pixel: camera ray, clip planes, closest volume box
-// entry. Pixels with nothing to march are written at once; the others are
-// appended to a compact list (one atomic per warp).
-struct MarchItem {
-  float4 o;   // voxel-space origin, tmin
-  float4 d;   // voxel-space direction, tmax
-  int4 info;  // pixel, volume index, -, -
-};
-
-__global__ void __launch_bounds__(256) kVolumeSetup(DScene S, DCamera C, DRenderer R, DFrame F,
-                                                    MarchItem *items, unsigned *counters) {
-  const int numPix = F.width * F.height;
-  const int lane = threadIdx.x & 31;
-  const float4 bg = make_float4(R.bg[0], R.bg[1], R.bg[2], R.bg[3]);
-  Rng none;
-  none.state = 0;
-  for (int base = (blockIdx.x * blockDim.x + threadIdx.x) & ~31; base < numPix;
-       base += gridDim.x * blockDim.x) {
-    const int p = base + lane;
-    bool march = false;
-    MarchItem it;
-    if (p < numPix) {
-      const int x = p % F.width, y = p / F.width;
-      Ray ray = primaryRay<false>(C, none, (float)x, (float)y, (float)F.width, (float)F.height);
-      clipRay(ray, R);
-      int vInst = -1, vIdx = -1;
-      float vT = FLT_MAX;
-      for (int i = 0; i < S.numInstances; ++i) {
-        const DInstance &I = S.instances[i];
-        const DGroup &G = S.groups[I.group];
-        for (int k = G.volBegin; k < G.volEnd; ++k) {
-          const int vi = S.groupVolumes[k];
-          float3 lo, ld;
-          localRay(I, ray.o, ray.d, lo, ld);
-          BoxHit bh = intersectBox(lo, ld, S.volumes[vi].boundsLo, S.volumes[vi].boundsHi);
-          const bool h = bh.hit && bh.tfar >= ray.tmin && bh.tnear <= ray.tmax;
-          const float t = fmaxf(ray.tmin, bh.tnear);
-          if (h && t < vT) { vT = t; vInst = i; vIdx = vi; }
-        }
-      }
-      if (vIdx >= 0) {
-        const DVolume &V = S.volumes[vIdx];
-        float3 lo, ld;
-        localRay(S.instances[vInst], ray.o, ray.d, lo, ld);
-        BoxHit bh = intersectBox(lo, ld, V.boundsLo, V.boundsHi);
-        const float tmin = fmaxf(ray.tmin, bh.tnear);
-        const float tmax = fminf(ray.tmax, bh.tfar);
-        const float3 Sv = ld3(V.S);
-        const float3 o = Sv * (lo + ld3(V.T));
-        const float3 d = Sv * ld;
-        it.o = make_float4(o.x, o.y, o.z, tmin);
-        it.d = make_float4(d.x, d.y, d.z, tmax);
-        it.info = make_int4(p, vIdx, 0, 0);
-        march = tmin <= tmax;
-      }
-      if (!march) writeSample(F, x, y, false, bg, 1e31f, f3(0.f), f3(0.f));
-    }
-    const unsigned mask = __ballot_sync(0xffffffffu, march);
-    if (mask) {
-      const int leader = __ffs(mask) - 1;
-      unsigned off = 0;
-      if (lane == leader) off = atomicAdd(&counters[0], (unsigned)__popc(mask));
-      off = __shfl_sync(0xffffffffu, off, leader);
-      if (march) items[off + __popc(mask & ((1u << lane) - 1u))] = it;
-    }
-  }
-}
-
-// Pass 2: warps take rays from the list one at a time.
-template <bool Count>
-__global__ void __launch_bounds__(256) kVolumeMarch(DScene S, DRenderer R, DFrame F,
-                                                    const MarchItem *items, unsigned *counters,
-                                                    int stageTF) {
-  extern __shared__ float4 sTF[];
-  if (stageTF) {
-    const DVolume &V0 = S.volumes[0];
-    for (int i = threadIdx.x; i < V0.tfSize; i += blockDim.x) sTF[i] = V0.tf[i];
-    __syncthreads();
-  }
-  const int lane = threadIdx.x & 31;
-  const unsigned count = counters[0];
-  const float4 bg = make_float4(R.bg[0], R.bg[1], R.bg[2], R.bg[3]);
-  const bool hw = R.hwFilter != 0;
-  uint32_t err = 0;
-  unsigned long long samples = 0;
-  for (;;) {
-    unsigned idx = 0;
-    if (lane == 0) idx = atomicAdd(&counters[1], 1u);
-    idx = __shfl_sync(0xffffffffu, idx, 0);
-    if (idx >= count) break;
-    const MarchItem it = items[idx];
-    const DVolume &V = S.volumes[it.info.y];
-    const float4 *tf = (stageTF && it.info.y == 0) ? sTF : V.tf;
-    const float3 oj = f3(it.o.x, it.o.y, it.o.z), dj = f3(it.d.x, it.d.y, it.d.z);
-    const float t1 = it.d.w;
-    const float dt = V.cellSize * R.samplingRateInv;
-    const float expo = dt / V.unitDistance;
-    float Cr = 0.f, Cg = 0.f, Cb = 0.f, A = 0.f, T = 1.f;
-    float tChunk = it.o.w;
-    int steps = 0;
-    while (tChunk <= t1 && A < 0.99f) {
-      if (!(dt > 0.f) || (steps += 32) > kMaxMarchSteps) {
-        err |= ERR_MARCH_LIMIT;
-        break;
-      }
-      // this lane's t: the reference's sequential additions from tChunk
-      float t = tChunk;
-#pragma unroll
-      for (int k = 0; k < 31; ++k)
-        if (k < lane) t += dt;
-      const float tLast = __shfl_sync(0xffffffffu, t, 31);
-      const bool in = t <= t1;
-      float c0 = 0.f, c1 = 0.f, c2 = 0.f, a = 0.f, tr = 1.f;
-      if (in) {
-        const float4 sm = classify(V, tf, fieldAt(V, oj + dj * t, hw), hw);
-        const float stepTr = hw ? __powf(1.f - sm.w, expo) : powf(1.f - sm.w, expo);
-        a = 1.f - stepTr;
-        tr = stepTr;
-        c0 = a * sm.x; c1 = a * sm.y; c2 = a * sm.z;
-      }
-      overScan(c0, c1, c2, a, tr);
-      float aEx = __shfl_up_sync(0xffffffffu, a, 1);
-      if (lane == 0) aEx = 0.f;
-      const bool keep = in && (A + T * aEx) < 0.99f;
-      const int cut = __popc(__ballot_sync(0xffffffffu, keep));
-      if (cut > 0) {
-        const int last = cut - 1;
-        const float lc0 = __shfl_sync(0xffffffffu, c0, last);
-        const float lc1 = __shfl_sync(0xffffffffu, c1, last);
-        const float lc2 = __shfl_sync(0xffffffffu, c2, last);
-        const float la = __shfl_sync(0xffffffffu, a, last);
-        const float ltr = __shfl_sync(0xffffffffu, tr, last);
-        Cr += T * lc0; Cg += T * lc1; Cb += T * lc2;
-        A += T * la;
-        T *= ltr;
-        if (Count && lane == 0) samples += cut;
-      }
-      if (cut < 32) break;  // ran past tmax or reached alpha 0.99
-      tChunk = tLast + dt;
-    }
-    if (lane == 0) {
-      const int p = it.info.x;
-      const float4 res = make_float4(A * Cr + (1.f - A) * bg.x, A * Cg + (1.f - A) * bg.y,
-                                     A * Cb + (1.f - A) * bg.z, A + (1.f - A) * bg.w);
-      writeSample(F, p % F.width, p / F.width, false, res, 1e31f, f3(0.f), f3(0.f));
-    }
-  }
-  if (Count && samples) atomicAdd(&F.counters[3], samples);
-  if (err) atomicOr(F.errorFlags, err);
-}
-
 // --------------------------------------------------------------- pathtrace
 enum RayType { RT_RADIANCE = 0, RT_SHADOW = 1, RT_AO = 2, RT_MISS = 3 };
 
@@ -669,8 +487,8 @@ static dim3 tileGrid(const DFrame &F, dim3 block) {
 }
 
 cudaError_t launchRaycast(const DScene &S, const DCamera &C, const DRenderer &R, const DFrame &F,
-                          int stageTFSize, bool count, void *marchItems,
-                          unsigned *marchCounters, cudaStream_t stream) {
+                          int stageTFSize, bool count, const MarchScratch *scratch,
+                          cudaStream_t stream) {
   dim3 block(VSR_RAYCAST_BLOCK_X, VSR_RAYCAST_BLOCK_Y);
   size_t smem = stageTFSize > 0 ? sizeof(float4) * (size_t)stageTFSize : 0;
   const int stage = stageTFSize > 0;
@@ -683,26 +501,9 @@ cudaError_t launchRaycast(const DScene &S, const DCamera &C, const DRenderer &R,
   if (S.hasSurfaces) {
     if (count) launch(kRaycast<true, true>);
     else launch(kRaycast<false, true>);
-  } else if (R.pixelSamples == 1 && marchItems && marchCounters) {
-    // volume-only world: per-pixel set-up, then one warp per ray
-    static int sms = 0;
-    if (!sms) {
-      int dev = 0;
-      cudaGetDevice(&dev);
-      cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    }
-    cudaError_t e = cudaMemsetAsync(marchCounters, 0, 2 * sizeof(unsigned), stream);
-    if (e != cudaSuccess) return e;
-    const int numPix = F.width * F.height;
-    kVolumeSetup<<<min((numPix + 255) / 256, sms * 8), 256, 0, stream>>>(
-        S, C, R, F, reinterpret_cast<MarchItem *>(marchItems), marchCounters);
-    auto kernel = count ? kVolumeMarch<true> : kVolumeMarch<false>;
-    if (smem > 48 * 1024)
-      cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    int perSM = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, kernel, 256, smem);
-    kernel<<<sms * (perSM > 0 ? perSM : 1), 256, smem, stream>>>(
-        S, R, F, reinterpret_cast<const MarchItem *>(marchItems), marchCounters, stage);
+  } else if (R.pixelSamples == 1 && scratch) {
+    // volume-only world: set-up, segments, combination (k_volume_march.cu)
+    return launchVolumeMarch(S, C, R, F, stageTFSize, count, *scratch, stream);
   } else {
     if (count) launch(kRaycast<true, false>);
     else launch(kRaycast<false, false>);

@@ -7,11 +7,25 @@
 
 namespace vsr {
 
-// marchItems (48 B per pixel) and marchCounters (2 uint): device scratch of
-// the warp-per-ray marcher for volume-only worlds; both may be null.
+// Device scratch of the segmented marcher for volume-only raycast worlds at
+// one sample per pixel (k_volume_march.cu): items 48 B per pixel, groups
+// 16 B per 32 pixels, counters 4 uint, and unitCap work units of 32
+// segments (unitGroup 4 B and segOut 1 KiB per unit).
+struct MarchScratch {
+  void *items;
+  void *groups;
+  unsigned *counters;
+  int *unitGroup;
+  void *segOut;
+  unsigned unitCap;
+};
+// scratch null selects the per-pixel kernel for volume-only worlds too
 cudaError_t launchRaycast(const DScene &S, const DCamera &C, const DRenderer &R, const DFrame &F,
-                          int stageTFSize, bool count, void *marchItems,
-                          unsigned *marchCounters, cudaStream_t stream);
+                          int stageTFSize, bool count, const MarchScratch *scratch,
+                          cudaStream_t stream);
+cudaError_t launchVolumeMarch(const DScene &S, const DCamera &C, const DRenderer &R,
+                              const DFrame &F, int stageTFSize, bool count,
+                              const MarchScratch &M, cudaStream_t stream);
 cudaError_t launchPathtrace(const DScene &S, const DCamera &C, const DRenderer &R, const DFrame &F,
                             bool count, cudaStream_t stream);
 

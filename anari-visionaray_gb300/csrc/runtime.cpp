@@ -1035,7 +1035,10 @@ struct FrameObj : Object {
   int width = 10, height = 10;
   VSRDataType colorType = VSR_UNKNOWN, depthType = VSR_UNKNOWN, normalType = VSR_UNKNOWN,
               albedoType = VSR_UNKNOWN;
-  DevBuf color, depth, normal, albedo, accum, errFlags, marchItems, marchCounters;
+  DevBuf color, depth, normal, albedo, accum, errFlags, marchItems, marchGroups, marchCounters,
+      unitGroup, segOut;
+  size_t marchPixels = 0;
+  unsigned unitCap = 0;
   std::map<std::string, void *> pinned;
   uint32_t *errHost = nullptr;
   cudaEvent_t evStart = nullptr, evRender = nullptr, evStop = nullptr;
@@ -1053,6 +1056,28 @@ struct FrameObj : Object {
   uint32_t *pinnedCount = nullptr;
   int lastIterations = 0;
 
+  // scratch of the segmented volume marcher, made on first use: the ray list
+  // (48 B per pixel), groups (16 B per 32 pixels) and work units for 4
+  // segments of 16 samples per pixel (1 KiB per unit of 32 segments); rays
+  // beyond that are marched whole by the combining warps
+  bool ensureMarch() {
+    size_t np = (size_t)width * height;
+    if (marchPixels == np) return true;
+    const size_t cap = std::max<size_t>(np / 8, 4096);
+    const size_t numGroups = (np + 31) / 32;
+    bool ok = marchItems.alloc(np * 48) == cudaSuccess &&
+              marchGroups.alloc(numGroups * 16) == cudaSuccess &&
+              marchCounters.alloc(4 * sizeof(unsigned)) == cudaSuccess &&
+              unitGroup.alloc(cap * sizeof(int)) == cudaSuccess &&
+              segOut.alloc(cap * 1024) == cudaSuccess;
+    unitCap = ok ? (unsigned)cap : 0;
+    marchPixels = ok ? np : 0;
+    return ok;
+  }
+  MarchScratch march() {
+    return MarchScratch{marchItems.p, marchGroups.p, marchCounters.as<unsigned>(),
+                        unitGroup.as<int>(), segOut.p, unitCap};
+  }
   bool ensureWave() {
     size_t np = (size_t)width * height;
     if (wavePixels == np) return true;
@@ -1130,8 +1155,6 @@ struct FrameObj : Object {
                 albedo.alloc(np * 3 * sizeof(float)) == cudaSuccess &&
                 color.alloc(np * (colorType == VSR_FLOAT32_VEC4 ? 16 : 4)) == cudaSuccess &&
                 errFlags.alloc(sizeof(uint32_t)) == cudaSuccess &&
-                marchItems.alloc(np * 48) == cudaSuccess &&
-                marchCounters.alloc(2 * sizeof(unsigned)) == cudaSuccess &&
                 counters.alloc(24 * sizeof(unsigned long long)) == cudaSuccess;
       for (auto &kv : pinned) cudaFreeHost(kv.second);
       pinned.clear();
@@ -1204,8 +1227,16 @@ VSRStatus renderFrame(Device *dev, FrameObj *F) {
       // stage the first volume's TF in shared memory when it fits (64 KB)
       int stage = 0;
       if (!W->volsHost.empty() && W->volsHost[0].tfSize <= 4096) stage = W->volsHost[0].tfSize;
+      MarchScratch ms{};
+      const bool segmented = !W->scene.hasSurfaces && R.pixelSamples == 1;
+      if (segmented && !F->ensureMarch()) {
+        dev->report(F, VSR_FRAME, VSR_SEVERITY_ERROR, VSR_ERROR_OUT_OF_MEMORY,
+                    "volume marcher scratch allocation failed");
+        return VSR_ERROR_OUT_OF_MEMORY;
+      }
+      if (segmented) ms = F->march();
       e = launchRaycast(W->scene, F->camera->c, R, fr, stage, F->countStats,
-                        F->marchItems.p, F->marchCounters.as<unsigned>(), s);
+                        segmented ? &ms : nullptr, s);
     } else if (F->renderer->wavefront) {
       if (!F->ensureWave()) {
         dev->report(F, VSR_FRAME, VSR_SEVERITY_ERROR, VSR_ERROR_OUT_OF_MEMORY,

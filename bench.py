@@ -52,6 +52,9 @@ def parse():
                    help="skip the config-0 raycast (volume marcher) measurement")
     p.add_argument("--no-volume", dest="volume", action="store_false",
                    help="skip the config-2 volumetric path-tracing measurement")
+    p.add_argument("--volume-res", type=int, nargs=2, default=[1920, 1080],
+                   help="config-2 frame size (full size by default; smaller for profiling)")
+    p.add_argument("--volume-spp", type=int, default=256)
     return p.parse_args()
 
 
@@ -123,9 +126,9 @@ def measured_peaks():
     return 6800.0, "fallback"
 
 
-def profiled_traffic():
-    """DRAM bytes per launch of the path-trace kernel from the committed ncu summary."""
-    path = os.path.join(ROOT, "profiles", "pathtrace_config1.txt")
+def profiled_traffic(name="pathtrace_config1.txt"):
+    """DRAM bytes per launch (per frame) from a committed ncu summary."""
+    path = os.path.join(ROOT, "profiles", name)
     if not os.path.exists(path):
         return None
     with open(path) as f:
@@ -195,19 +198,23 @@ def measure_raycast_config0(pkg, dev, flush, steps=20):
             "march_samples": samples,
             "roofline": {"bound": "hbm", "achieved": alg / t / 1e9, "peak": peak, "unit": "GB/s",
                          "frac": alg / t / 1e9 / peak,
+                         "traffic": profiled_traffic("raycast_config0.txt"),
                          "note": f"32 B per trilinear sample + 20 B per pixel; peak {kind}; "
-                                 "the 8 MiB field is L2-resident"}}
+                                 "segmented marcher (set-up, 16-sample segments, combine); "
+                                 "the 8 MiB field is L2-resident, so DRAM traffic is far "
+                                 "below the algorithmic bytes"}}
 
 
-def measure_volume_config2(pkg, dev, flush, count_spp=8):
+def measure_volume_config2(pkg, dev, flush, count_spp=8, res=(1920, 1080), spp=256):
     """Config 2 (volumetric path tracing, 512^3 value noise with 16^3-voxel
     brick majorants + the config-1 spheres, 1920x1080, 256 spp, depth 8,
     clip plane): Mpx*spp/s of one full frame, and the delta-tracking
     roofline from a counting frame at count_spp samples scaled to 256."""
     import torch
 
-    scene = pkg.scenes.config2()
+    scene = pkg.scenes.config2(res=tuple(res), spp=spp)
     W, H = scene["frame"]["size"]
+    count_spp = min(count_spp, spp)
     spp = scene["renderer"]["pixelSamples"]
     h = pkg.scenes.build(dev, scene, channels=("color", "depth"))
     frame, rend = h["frame"], h["renderer"]
@@ -233,7 +240,7 @@ def measure_volume_config2(pkg, dev, flush, count_spp=8):
     for o in (frame, rend, h["camera"], h["world"], *h["keep"]):
         dev.release(o)
     return {"value": W * H * spp / t / MPX, "unit": "Mpx*spp/s", "ms_per_frame": 1e3 * t,
-            "workload": "config2 volumetric pathtracer 1920x1080 256spp depth8, 512^3 value noise "
+            "workload": f"config2 volumetric pathtracer {W}x{H} {spp}spp depth8, 512^3 value noise "
                         "(16^3 bricks) + 1015810 tris, clip plane",
             "error_flags": err,
             "tracking_samples_est": track, "majorant_cells_est": cells,
@@ -361,7 +368,8 @@ def run_ours(args):
     h2d = 3 * 4 + 4 * 4 * 0  # the camera position crosses to the device as kernel parameters
 
     raycast = measure_raycast_config0(pkg, dev, flush) if args.raycast else None
-    volume = measure_volume_config2(pkg, dev, flush) if args.volume else None
+    volume = (measure_volume_config2(pkg, dev, flush, res=args.volume_res, spp=args.volume_spp)
+              if args.volume else None)
 
     kernel_s = sum(durations) / len(durations)
     t_max = kernel_s

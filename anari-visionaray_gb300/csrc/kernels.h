@@ -37,6 +37,31 @@ cudaError_t launchPathtraceWavefront(const DScene &S, const DCamera &C, const DR
                                      const DFrame &F, const DWave &Wv, uint32_t *pinnedCount,
                                      bool count, cudaStream_t stream, int *iterations);
 
+// Batched rendering (k_batch.cu). A job is one frame's records; kinds are
+// rendered by separate persistent kernels, each over its own work list of
+// (job, tile) items with tiles of tileW x (32 / tileW) pixels.
+enum JobKind { JOB_PATHTRACE = 0, JOB_RAYCAST_SURFACES = 1, JOB_RAYCAST_VOLUME = 2, kJobKinds = 3 };
+struct DJob {
+  DScene S;
+  DCamera C;
+  DRenderer R;
+  DFrame F;
+  int kind;
+  int tilesX;
+  int reset;  // restart accumulation before rendering
+  int pad;
+};
+struct BatchLaunch {
+  const DJob *jobs;
+  int numJobs;
+  const uint2 *items[kJobKinds];
+  unsigned numItems[kJobKinds];
+  unsigned *counters;  // kJobKinds work counters
+  int tileW;           // 1..32, a divisor of 32
+  int fetch;           // items per atomic
+};
+cudaError_t launchBatch(const BatchLaunch &L, cudaStream_t stream);
+
 // Accumulation reset: accum = 0, depth = 1e31 (frame/Frame.cpp:287-312).
 cudaError_t launchFrameReset(float4 *accum, float *depth, size_t numPixels, cudaStream_t stream);
 

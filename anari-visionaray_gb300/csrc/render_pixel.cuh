@@ -1,0 +1,473 @@
+// Per-pixel bodies of the raycast and pathtrace renderers, shared by the
+// per-frame kernels (k_render.cu) and the batched kernel (k_batch.cu).
+//
+// Both keep one thread per pixel and the reference's per-pixel random
+// stream (renderer/Pathtrace_impl.cpp:512-513), so the GPU image tracks the
+// CPU restatement sample for sample; the frame write (G-buffer,
+// accumulation, colour conversion) is fused into the end of each body.
+#pragma once
+
+#include "render_common.cuh"
+
+namespace vsr {
+
+// ------------------------------------------------------------------ raycast
+// renderSample, renderer/Raycast_impl.cpp:10-243 (default render mode).
+template <bool Count, bool Surfaces>
+__device__ void raycastSample(const DScene &S, const DRenderer &R, Ray ray, const float4 *sTF,
+                              float4 &outColor, float &outDepth, float3 &outNg, float3 &outAlbedo,
+                              uint32_t &err, unsigned long long *cnt) {
+  const float4 bg = make_float4(R.bg[0], R.bg[1], R.bg[2], R.bg[3]);
+  outColor = bg;
+  outDepth = 1e31f;
+  outNg = f3(0.f);
+  outAlbedo = f3(0.f);
+  if (S.numInstances == 0) return;
+  float3 surfaceColor = f3(0.f);
+  float surfaceAlpha = 0.f;
+  if (Surfaces && S.hasSurfaces) {
+    Hit hr;
+    bool hit = traceSurfaces<Count>(S, ray, false, hr, err, cnt);
+    bool first = true;
+    int layers = 0;
+    while (hit) {
+      if (++layers > kMaxSurfaceLayers) {
+        err |= ERR_LAYER_LIMIT;
+        break;
+      }
+      const DInstance &I = S.instances[hr.inst];
+      const DGroup &G = S.groups[I.group];
+      const DMaterial &mat = S.materials[__ldg(G.triSurface + hr.tri)];
+      const float3 hitPos = ray.o + hr.t * ray.d;
+      // getNormals (renderer/common.h:241-264): Ng = normalize(e1 x e2)
+      const float4 *E = G.tris + 3 * (size_t)hr.leaf;
+      const float4 e1 = __ldg(E + 1), e2 = __ldg(E + 2);
+      float3 gn = normalize(cross(f3(e1.x, e1.y, e1.z), f3(e2.x, e2.y, e2.z)));
+      float3 sn = gn;
+      gn = normalize(mat3mul(I.normalXfm, gn));
+      sn = normalize(mat3mul(I.normalXfm, sn));
+      const float3 color = materialColor(mat);
+      float3 shaded = f3(0.f);
+      const float3 viewDir = -ray.d;
+      for (int li = 0; li < S.numLights; ++li) {
+        Rng dummy;
+        dummy.state = 0;
+        LightSample ls = sampleLight(S.lights[li], dummy);
+        const float3 lightDir = normalize(ls.dir);
+        const float3 li3 = ls.intensity * safeRcp(ls.dist2);
+        const float NdotL = fmaxf(0.f, dot(sn, lightDir));
+        const float3 bsdf = evalMaterial(mat, sn, normalize(viewDir), lightDir);
+        shaded += bsdf * li3 * NdotL * safeRcp(ls.pdf);
+      }
+      shaded += color * ld3(R.ambient);
+      const float a = materialOpacity(mat);
+      surfaceColor += (1.f - surfaceAlpha) * a * shaded;
+      surfaceAlpha += (1.f - surfaceAlpha) * a;
+      if (first) {
+        outDepth = hr.t;
+        outNg = gn;
+        outAlbedo = color;
+        first = false;
+      }
+      if (surfaceAlpha < 0.999f) {
+        const float eps = epsilonFrom(hitPos, ray.d, hr.t);
+        ray.tmin = hr.t + eps;
+        hit = traceSurfaces<Count>(S, ray, false, hr, err, cnt);
+      } else {
+        ray.tmax = hr.t;
+        break;
+      }
+    }
+  }
+  float4 result = make_float4(surfaceColor.x + (1.f - surfaceAlpha) * bg.x,
+                              surfaceColor.y + (1.f - surfaceAlpha) * bg.y,
+                              surfaceColor.z + (1.f - surfaceAlpha) * bg.z,
+                              surfaceAlpha + (1.f - surfaceAlpha) * bg.w);
+  // intersectVolumeBounds: closest volume box entry.
+  int vInst = -1, vIdx = -1;
+  float vT = FLT_MAX;
+  for (int i = 0; i < S.numInstances; ++i) {
+    const DInstance &I = S.instances[i];
+    const DGroup &G = S.groups[I.group];
+    for (int k = G.volBegin; k < G.volEnd; ++k) {
+      const int vi = S.groupVolumes[k];
+      float3 lo, ld;
+      localRay(I, ray.o, ray.d, lo, ld);
+      BoxHit bh = intersectBox(lo, ld, S.volumes[vi].boundsLo, S.volumes[vi].boundsHi);
+      const bool h = bh.hit && bh.tfar >= ray.tmin && bh.tnear <= ray.tmax;
+      const float t = fmaxf(ray.tmin, bh.tnear);
+      if (h && t < vT) { vT = t; vInst = i; vIdx = vi; }
+    }
+  }
+  if (vIdx >= 0) {
+    const DVolume &V = S.volumes[vIdx];
+    float3 lo, ld;
+    localRay(S.instances[vInst], ray.o, ray.d, lo, ld);
+    // rayMarchVolume<0>, renderer/VolumeIntegration.h:374-468
+    BoxHit bh = intersectBox(lo, ld, V.boundsLo, V.boundsHi);
+    const float tmin = fmaxf(ray.tmin, bh.tnear);
+    const float tmax = fminf(ray.tmax, bh.tfar);
+    const float3 Sv = ld3(V.S);
+    const float3 o = Sv * (lo + ld3(V.T));
+    const float3 d = Sv * ld;
+    const float dt = V.cellSize * R.samplingRateInv;
+    const float expo = dt / V.unitDistance;
+    const float4 *tf = (sTF && vIdx == 0) ? sTF : V.tf;
+    float3 color = f3(0.f);
+    float alpha = 0.f, transmittance = 1.f;
+    unsigned samples = 0;
+    const bool hw = R.hwFilter != 0;
+    // for (t = tmin; t <= tmax && alpha < 0.99; t += dt) { composite sample(t) },
+    // with the field fetches of four consecutive steps issued before they are
+    // composited: the positions do not depend on the values, so four
+    // fetches are in flight per thread. Same t sequence, same early exit.
+    float t = tmin;
+    constexpr int kBatch = VSR_MARCH_BATCH;
+    int steps = 0;
+    while (t <= tmax && alpha < 0.99f) {
+      // dt <= 0, or dt below the float spacing of t, would never end
+      if (!(dt > 0.f) || (steps += kBatch) > kMaxMarchSteps) {
+        err |= ERR_MARCH_LIMIT;
+        break;
+      }
+      float tk[kBatch], vk[kBatch];
+#pragma unroll
+      for (int k = 0; k < kBatch; ++k) {
+        tk[k] = t;
+        vk[k] = t <= tmax ? fieldAt(V, o + d * t, hw) : 0.f;
+        t += dt;
+      }
+#pragma unroll
+      for (int k = 0; k < kBatch; ++k) {
+        if (tk[k] <= tmax && alpha < 0.99f) {
+          const float4 s = classify(V, tf, vk[k], hw);
+          // the texture path is already approximate (fixed-point filter
+          // weights): use the fast pow there, the exact one otherwise
+          const float stepTr = hw ? __powf(1.f - s.w, expo) : powf(1.f - s.w, expo);
+          const float w = transmittance * (1.f - stepTr);
+          color += w * f3(s.x, s.y, s.z);
+          alpha += w;
+          transmittance *= stepTr;
+          if (Count) ++samples;
+        }
+      }
+    }
+    if (Count) atomicAdd(&cnt[3], (unsigned long long)samples);
+    result = make_float4(alpha * color.x + (1.f - alpha) * result.x,
+                         alpha * color.y + (1.f - alpha) * result.y,
+                         alpha * color.z + (1.f - alpha) * result.z,
+                         alpha + (1.f - alpha) * result.w);
+    outNg = f3(0.f);
+    outAlbedo = f3(0.f);
+  }
+  outColor = result;
+}
+
+// One pixel of the raycast renderer: pixelSamples camera rays through the
+// pixel centre, averaged (renderer/Raycast_impl.cpp:282-322). sTF is the
+// first volume's TF staged in shared memory, or null.
+template <bool Count, bool Surfaces>
+__device__ __forceinline__ void raycastPixel(const DScene &S, const DCamera &C, const DRenderer &R,
+                                             const DFrame &F, int x, int y, const float4 *sTF) {
+  uint32_t err = 0;
+  unsigned long long *cnt = F.counters;
+  float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
+  float4 c0;
+  float d0 = 1e31f;
+  float3 n0 = f3(0.f), a0 = f3(0.f);
+  Rng none;
+  none.state = 0;
+  for (int s = 0; s < R.pixelSamples; ++s) {
+    Ray ray = primaryRay<false>(C, none, (float)x, (float)y, (float)F.width, (float)F.height);
+    clipRay(ray, R);
+    float4 c;
+    float dd;
+    float3 nn, aa;
+    raycastSample<Count, Surfaces>(S, R, ray, sTF, c, dd, nn, aa, err, cnt);
+    acc.x += c.x; acc.y += c.y; acc.z += c.z; acc.w += c.w;
+    if (s == 0) { c0 = c; d0 = dd; n0 = nn; a0 = aa; }
+  }
+  (void)c0;
+  const float inv = 1.f / R.pixelSamples;
+  writeSample(F, x, y, false, make_float4(acc.x * inv, acc.y * inv, acc.z * inv, acc.w * inv), d0,
+              n0, a0);
+  if (err) atomicOr(F.errorFlags, err);
+}
+
+// --------------------------------------------------------------- pathtrace
+enum RayType { RT_RADIANCE = 0, RT_SHADOW = 1, RT_AO = 2, RT_MISS = 3 };
+
+struct HitRec {
+  bool surfHit, volHit, hit, volumeHit;
+  Hit surf;
+  float volT;
+  float3 volAlbedo;
+  int volInst;
+};
+
+// intersectAll, renderer/common.h:1605-1620, with intersectSurfaces<1>
+// (:1502-1543: one draw per surface hit) and the volume free-flight
+// sampling of every volume in the world.
+template <bool Count>
+__device__ __forceinline__ void intersectAll(const DScene &S, const Ray &ray, bool shadow, Rng &rnd,
+                                             HitRec &h, uint32_t &err, unsigned long long *cnt,
+                                             bool hwFilter) {
+  h.surfHit = false;
+  if (S.hasSurfaces) {
+    Ray r = ray;
+    const bool anyHit = shadow && S.allOpaque;
+    bool hit = traceSurfaces<Count>(S, r, anyHit, h.surf, err, cnt);
+    int guard = 1 << 16;
+    while (hit) {
+      const DGroup &G = S.groups[S.instances[h.surf.inst].group];
+      const float opacity = materialOpacity(S.materials[__ldg(G.triSurface + h.surf.tri)]);
+      const float u = rnd();
+      if (u > opacity && --guard > 0) {
+        const float3 hp = r.o + h.surf.t * r.d;
+        r.tmin = h.surf.t + epsilonFrom(hp, r.d, h.surf.t);
+        hit = traceSurfaces<Count>(S, r, false, h.surf, err, cnt);
+      } else {
+        break;
+      }
+    }
+    h.surfHit = hit;
+  } else {
+    h.surf.t = FLT_MAX;
+  }
+  h.volHit = false;
+  h.volT = FLT_MAX;
+  if (S.numVolumes > 0) {
+    for (int i = 0; i < S.numInstances; ++i) {
+      const DInstance &I = S.instances[i];
+      const DGroup &G = S.groups[I.group];
+      for (int k = G.volBegin; k < G.volEnd; ++k) {
+        float3 lo, ld;
+        localRay(I, ray.o, ray.d, lo, ld);
+        float t;
+        float3 alb;
+        if (deltaTrack<Count>(S.volumes[S.groupVolumes[k]], lo, ld, ray.tmin, ray.tmax, rnd, t, alb,
+                              err, cnt, hwFilter) &&
+            t < h.volT) {
+          h.volHit = true;
+          h.volT = t;
+          h.volAlbedo = alb;
+          h.volInst = i;
+        }
+      }
+    }
+  }
+  h.hit = h.surfHit || h.volHit;
+  h.volumeHit = h.volHit && (!h.surfHit || h.volT < h.surf.t);
+}
+
+// Per-pixel body of VisionarayRendererPathtrace::renderFrame
+// (renderer/Pathtrace_impl.cpp:498-640) with shade() (:93-487) inlined.
+template <bool Count>
+__device__ __forceinline__ void pathtracePixel(const DScene &S, const DCamera &C,
+                                               const DRenderer &R, const DFrame &F, int x, int y) {
+  uint32_t err = 0;
+  unsigned long long *cnt = F.counters;
+  const int W = F.width, H = F.height;
+  Rng rng;
+  rng.init((uint32_t)(x + W * y), (uint32_t)F.accumID);
+  Rng rnd = rng;
+  const float3 ambient = ld3(R.ambient);
+  float4 accum = make_float4(0.f, 0.f, 0.f, 0.f);
+  float cDepth = 1e31f;
+  float3 cNg = f3(0.f), cAlb = f3(0.f);
+  const int maxPasses = (R.maxBounce + 2) * (2 + R.ambientSamples) + 8;
+  for (int sampleID = 0; sampleID < R.pixelSamples; ++sampleID) {
+    float xf = (float)x, yf = (float)y;
+    const float jx = rnd() - .5f;
+    const float jy = rnd() - .5f;
+    xf += jx;
+    yf += jy;
+    Ray ray = primaryRay<true>(C, rnd, xf, yf, (float)W, (float)H);
+    float4 pc = make_float4(R.bg[0], R.bg[1], R.bg[2], R.bg[3]);
+    float pDepth = 1e31f;
+    float3 pNg = f3(0.f), pAlb = f3(0.f);
+    if (S.numInstances > 0) {
+      bool firstHit = false;
+      int rayType = RT_RADIANCE;
+      float3 throughput = f3(1.f), intensity = f3(0.f);
+      // ShadeState
+      float3 baseColor = f3(0.f), shadedColor = f3(0.f), hitPosOff = f3(0.f), sn = f3(0.f);
+      int aoSamples = 0;
+      float aoWeights = 0.f, aoCount = 0.f;
+      BSDFSample bsdf;
+      bsdf.dir = f3(0.f); bsdf.f = f3(0.f); bsdf.pdf = 0.f; bsdf.cosT = 0.f;
+      LightSample ls;
+      ls.intensity = f3(0.f); ls.dir = f3(0.f); ls.pdf = 0.f; ls.dist = 0.f; ls.dist2 = 0.f;
+      float misWeightNEE = 0.f, visLight = 1.f, visAO = 1.f;
+      unsigned bounceID = 0;
+      for (int passID = 0; true; ++passID) {
+        if (passID >= maxPasses) { err |= ERR_PATH_LIMIT; break; }
+        clipRay(ray, R);
+        HitRec hr;
+        if (rayType == RT_SHADOW && S.numLights == 0) {
+          // the shadow ray of a light-less scene has a NaN direction and
+          // cannot hit anything: skip the traversal
+          hr.surfHit = hr.volHit = hr.hit = hr.volumeHit = false;
+        } else {
+          intersectAll<Count>(S, ray, rayType == RT_SHADOW || rayType == RT_AO, rnd, hr, err, cnt,
+                              R.hwFilter != 0);
+        }
+        int nextType = RT_MISS;
+        if (rayType == RT_RADIANCE) {
+          baseColor = f3(0.f);
+          visLight = 1.f;
+          visAO = 1.f;
+          aoSamples = 0;
+          aoWeights = 0.f;
+          aoCount = 0.f;
+          if (!hr.hit) {
+            shadedColor = f3(0.f);
+          } else {
+            const float3 viewDir = -normalize(ray.d);
+            float3 hitPos, gn, color;
+            float eps;
+            const DMaterial *mat = nullptr;
+            if (hr.volumeHit) {
+              const DInstance &I = S.instances[hr.volInst];
+              hitPos = ray.o + hr.volT * ray.d;
+              eps = epsilonFrom(hitPos, ray.d, hr.volT);
+              gn = f3(0.f);
+              if (R.ambientSamples > 0) {
+                const float u1 = rnd(), u2 = rnd();
+                gn = uniformSampleSphere(u1, u2);
+              }
+              sn = mat3mul(I.normalXfm, gn);
+              gn = mat3mul(I.normalXfm, gn);
+              sn = faceforward(sn, viewDir, gn);
+              gn = faceforward(gn, viewDir, gn);
+              color = hr.volAlbedo;
+              if (bounceID == 0) pDepth = hr.volT;
+            } else {
+              const DInstance &I = S.instances[hr.surf.inst];
+              const DGroup &G = S.groups[I.group];
+              hitPos = ray.o + hr.surf.t * ray.d;
+              eps = epsilonFrom(hitPos, ray.d, hr.surf.t);
+              mat = &S.materials[__ldg(G.triSurface + hr.surf.tri)];
+              const float4 *E = G.tris + 3 * (size_t)hr.surf.leaf;
+              const float4 e1 = __ldg(E + 1), e2 = __ldg(E + 2);
+              gn = normalize(cross(f3(e1.x, e1.y, e1.z), f3(e2.x, e2.y, e2.z)));
+              sn = normalize(mat3mul(I.normalXfm, gn));
+              gn = sn;
+              sn = faceforward(sn, viewDir, gn);
+              gn = faceforward(gn, viewDir, gn);
+              color = materialColor(*mat);
+              if (bounceID == 0) pDepth = hr.surf.t;
+            }
+            if (bounceID == 0) {
+              pNg = gn;
+              pAlb = color;
+            }
+            hitPosOff = hitPos + sn * eps;
+            if (S.numLights > 0) {
+              int lightID = int(rnd() * S.numLights);
+              if (lightID == S.numLights) lightID = 0;
+              ls = sampleLight(S.lights[lightID], rnd);
+            }
+            const float3 lightDir = normalize(ls.dir);
+            const float3 lightIntensity = ls.intensity * safeRcp(ls.dist2);
+            const float NdotL = fmaxf(0.f, dot(sn, lightDir));
+            if (hr.volumeHit) {
+              shadedColor = hr.volAlbedo * lightIntensity * safeRcp(ls.pdf) * safeRcp(ls.dist2);
+              const float u1 = rnd(), u2 = rnd();
+              bsdf.dir = uniformSampleSphere(u1, u2);
+              bsdf.f = hr.volAlbedo;
+              bsdf.pdf = 1.f;
+              bsdf.cosT = 1.f;
+            } else {
+              const float3 f = evalMaterial(*mat, sn, viewDir, lightDir);
+              shadedColor = f * lightIntensity * NdotL * safeRcp(ls.pdf) * float(S.numLights);
+              bsdf = sampleMaterial(*mat, gn, sn, viewDir, rnd);
+            }
+            misWeightNEE = S.numLights > 0 ? 1.f : 0.f;
+            baseColor = color;
+          }
+        } else if (rayType == RT_SHADOW) {
+          const int surfV = hr.surfHit ? 0 : 1;
+          const int volV = hr.volumeHit ? 0 : 1;
+          visLight = float(surfV * volV) * (hr.volHit ? 0.f : 1.f);
+        } else {  // AO
+          aoSamples++;
+          const float weight = fmaxf(0.f, dot(ray.d, sn));
+          aoWeights += weight;
+          if (weight > 0.f && hr.hit) aoCount += weight;
+        }
+        // advance the state machine (prepareNextRay, :37-90)
+        const bool radianceHit = rayType == RT_RADIANCE && hr.hit;
+        bool wantShadow = radianceHit && ls.pdf >= 0.f;
+        bool wantAO = false, wantBounce = false;
+        if (radianceHit && !wantShadow) {
+          wantAO = aoSamples < R.ambientSamples;
+          wantBounce = !wantAO && bsdf.pdf >= 0.f;
+        } else if (rayType == RT_SHADOW) {
+          wantAO = aoSamples < R.ambientSamples;
+          wantBounce = !wantAO && bsdf.pdf >= 0.f;
+        } else if (rayType == RT_AO) {
+          wantAO = aoSamples < R.ambientSamples;
+          if (!wantAO) {
+            float aoV = 0.f;
+            if (aoWeights > 0.f) aoV = 1.f - (aoCount / aoWeights);
+            visAO *= aoV;
+            wantBounce = bsdf.pdf >= 0.f;
+          }
+        }
+        if (wantShadow) {
+          nextType = RT_SHADOW;
+          ray.o = hitPosOff;
+          ray.d = normalize(ls.dir);
+          ray.tmin = 0.f;
+          ray.tmax = ls.dist;
+        } else if (wantAO) {
+          float3 u, v, w = sn;
+          orthonormalBasis(u, v, w);
+          const float u1 = rnd(), u2 = rnd();
+          const float3 sp = cosineSampleHemisphere(u1, u2);
+          nextType = RT_AO;
+          ray.o = hitPosOff;
+          ray.d = normalize(sp.x * u + sp.y * v + sp.z * w);
+          ray.tmin = 0.f;
+          ray.tmax = R.occlusionDistance;
+        } else if (wantBounce) {
+          nextType = RT_RADIANCE;
+          ray.o = hitPosOff;
+          ray.d = normalize(bsdf.dir);
+          ray.tmin = 0.f;
+          ray.tmax = 1e31f;
+        }
+        if (passID == 0 && bounceID == 0) firstHit = hr.hit;
+        rayType = nextType;
+        if (rayType == RT_MISS || rayType == RT_RADIANCE) {
+          const float3 direct = shadedColor * visLight;
+          const float3 amb = baseColor * ambient * visAO;
+          intensity += throughput * misWeightNEE * direct;
+          intensity += throughput * amb;
+          throughput *= bsdf.f * bsdf.cosT * safeRcp(bsdf.pdf);
+          bounceID++;
+        }
+        if (rayType == RT_MISS || bounceID > (unsigned)R.maxBounce) break;
+        if (bounceID > 1) {
+          const float prob = maxe(throughput);
+          if (rng() > prob) break;
+          throughput /= prob;
+        }
+      }
+      if (firstHit) pc = make_float4(intensity.x, intensity.y, intensity.z, 1.f);
+    }
+    accum.x += pc.x; accum.y += pc.y; accum.z += pc.z; accum.w += pc.w;
+    if (pDepth < cDepth) {
+      cDepth = pDepth;
+      cNg = pNg;
+      cAlb = pAlb;
+    }
+  }
+  const float inv = 1.f / R.pixelSamples;
+  writeSample(F, x, y, true, make_float4(accum.x * inv, accum.y * inv, accum.z * inv, accum.w * inv),
+              cDepth, cNg, cAlb);
+  if (err) atomicOr(F.errorFlags, err);
+}
+
+} // namespace vsr

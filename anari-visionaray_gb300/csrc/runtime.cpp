@@ -35,8 +35,12 @@ namespace vsr {
 struct Object;
 
 // ------------------------------------------------------------------ device
+struct BatchState;
+void destroyBatch(BatchState *);
+
 struct Device {
   VSRStatusCallback cb = nullptr;
+  BatchState *batch = nullptr;  // batched rendering: plans, tuner, CUDA graph
   const void *cbUser = nullptr;
   int cudaDevice = 0;
   cudaStream_t stream = nullptr;
@@ -1055,6 +1059,7 @@ struct FrameObj : Object {
   size_t wavePixels = 0;
   uint32_t *pinnedCount = nullptr;
   int lastIterations = 0;
+  int batchTileW = 0, batchFetch = 0, batchTuned = 0;  // last batched render
 
   // scratch of the segmented volume marcher, made on first use: the ray list
   // (48 B per pixel), groups (16 B per 32 pixels) and work units for 4
@@ -1264,6 +1269,266 @@ VSRStatus renderFrame(Device *dev, FrameObj *F) {
   return VSR_OK;
 }
 
+// ------------------------------------------------------------ batching
+// Work list of one kind: (job, tile) pairs, jobs ordered by cost per pixel,
+// highest first (stable), all tiles of a job together. Longest-first order
+// keeps the end of the persistent launch short.
+size_t planItems(const uint32_t *w, const uint32_t *h, const float *cost, uint32_t n,
+                 uint32_t tileW, std::vector<uint32_t> &out) {
+  out.clear();
+  if (tileW == 0 || tileW > 32 || 32 % tileW) return 0;
+  const uint32_t tileH = 32 / tileW;
+  std::vector<uint32_t> order(n);
+  for (uint32_t i = 0; i < n; ++i) order[i] = i;
+  std::stable_sort(order.begin(), order.end(),
+                   [&](uint32_t a, uint32_t b) { return cost[a] > cost[b]; });
+  for (uint32_t j : order) {
+    const uint64_t tiles = (uint64_t)((w[j] + tileW - 1) / tileW) * ((h[j] + tileH - 1) / tileH);
+    for (uint64_t t = 0; t < tiles; ++t) {
+      out.push_back(j);
+      out.push_back((uint32_t)t);
+    }
+  }
+  return out.size() / 2;
+}
+
+// Tile shapes and items per fetch the autotuner tries, in this order.
+struct BatchConfig {
+  int tileW, fetch;
+};
+static const BatchConfig kBatchConfigs[] = {{8, 1}, {16, 1}, {32, 1}, {4, 1},
+                                            {8, 4}, {16, 4}, {4, 4},  {8, 16}};
+static const int kNumBatchConfigs = sizeof(kBatchConfigs) / sizeof(kBatchConfigs[0]);
+
+// Online autotuner of one frame set: successive batches of the same set run
+// the candidate configurations in turn (every configuration renders the same
+// image); once each has been timed the fastest is kept.
+struct BatchTuner {
+  float ms[kNumBatchConfigs];
+  int measured = 0;
+  int best = -1;
+  BatchTuner() {
+    for (float &m : ms) m = -1.f;
+  }
+  int pick() const { return best >= 0 ? best : measured; }
+  void record(int cfg, float t) {
+    if (best >= 0 || cfg != measured) return;
+    ms[cfg] = t;
+    if (++measured == kNumBatchConfigs)
+      best = (int)(std::min_element(ms, ms + kNumBatchConfigs) - ms);
+  }
+};
+
+struct BatchState {
+  std::vector<uint64_t> key;  // frame set and its work (sizes, kinds, sample counts)
+  int config = -1;            // configuration of the items and the graph below
+  DevBuf jobs, items[kJobKinds], counters;
+  unsigned numItems[kJobKinds] = {0, 0, 0};
+  DJob *jobsHost = nullptr;  // pinned staging, read by the graph's copy
+  size_t jobsCap = 0;
+  int numJobs = 0;
+  cudaGraphExec_t graph = nullptr;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  bool pending = false;  // a tuning measurement waits in ev0/ev1
+  std::vector<uint64_t> pendingKey;
+  int pendingConfig = -1;
+  std::map<std::vector<uint64_t>, BatchTuner> tuners;
+  ~BatchState() {
+    if (graph) cudaGraphExecDestroy(graph);
+    if (jobsHost) cudaFreeHost(jobsHost);
+    if (ev0) cudaEventDestroy(ev0);
+    if (ev1) cudaEventDestroy(ev1);
+  }
+};
+
+void destroyBatch(BatchState *b) { delete b; }
+
+static float jobCostPerPixel(const DRenderer &R, const DScene &S) {
+  // path tracing: up to (maxBounce + 1) bounces of radiance + shadow + AO
+  // rays per sample; raycast: one ray per sample
+  const float spp = (float)std::max(R.pixelSamples, 1);
+  const float vol = S.numVolumes > 0 ? 2.f : 1.f;
+  if (R.type == REND_RAYCAST) return spp * vol;
+  return spp * (float)(R.maxBounce + 1) * (2.f + (float)R.ambientSamples) * vol;
+}
+
+VSRStatus renderFrames(Device *dev, FrameObj *const *frames, uint32_t count) {
+  cudaStream_t s = dev->stream;
+  if (!dev->batch) dev->batch = new BatchState();
+  BatchState &B = *dev->batch;
+  if (!B.ev0 && (cudaEventCreate(&B.ev0) != cudaSuccess || cudaEventCreate(&B.ev1) != cudaSuccess))
+    return VSR_ERROR_CUDA;
+  // the previous batch: its timing feeds the tuner, and the staging buffer
+  // is free again once it has run
+  cudaEventSynchronize(B.ev1);
+  if (B.pending) {
+    float ms = 0.f;
+    if (cudaEventElapsedTime(&ms, B.ev0, B.ev1) == cudaSuccess)
+      B.tuners[B.pendingKey].record(B.pendingConfig, ms);
+    B.pending = false;
+  }
+  VSRStatus status = VSR_OK;
+  std::vector<FrameObj *> batched, single;
+  std::vector<DJob> jobs;
+  std::vector<uint64_t> key;
+  for (uint32_t i = 0; i < count; ++i) {
+    FrameObj *F = frames[i];
+    cudaEventSynchronize(F->evStop);
+    if (!F->valid) {
+      dev->report(F, VSR_FRAME, VSR_SEVERITY_ERROR, VSR_ERROR_INCOMPLETE,
+                  "skipping render of incomplete frame object");
+      status = VSR_ERROR_INCOMPLETE;
+      continue;
+    }
+    if (F->countStats) {  // statistics are collected by the per-frame kernels
+      single.push_back(F);
+      continue;
+    }
+    World *W = F->world;
+    uint64_t deep = W->deepStamp();
+    if (deep > W->builtStamp && !W->buildScene(deep)) {
+      status = VSR_ERROR_CUDA;
+      continue;
+    }
+    uint64_t stampAll = std::max({deep, F->stamp, F->renderer->deepStamp(), F->camera->stamp});
+    if (stampAll > F->lastStamp) {
+      F->lastStamp = stampAll;
+      F->nextReset = true;
+    }
+    DJob j{};
+    j.S = W->scene;
+    j.C = F->camera->c;
+    j.R = F->renderer->r;
+    j.reset = F->nextReset ? 1 : 0;
+    if (F->nextReset) {
+      F->accumID = 0;
+      F->nextReset = false;
+    }
+    j.F = F->record();
+    j.kind = j.R.type == REND_RAYCAST
+                 ? (j.S.hasSurfaces ? JOB_RAYCAST_SURFACES : JOB_RAYCAST_VOLUME)
+                 : JOB_PATHTRACE;
+    // a frame past its sample limit only clears its error flags
+    if (F->accumID >= F->renderer->sampleLimit) j.F.width = j.F.height = 0;
+    jobs.push_back(j);
+    batched.push_back(F);
+    key.insert(key.end(), {(uint64_t)(uintptr_t)F, (uint64_t)j.F.width, (uint64_t)j.F.height,
+                           (uint64_t)j.kind, (uint64_t)j.R.pixelSamples, (uint64_t)j.R.maxBounce,
+                           (uint64_t)j.S.numVolumes});
+  }
+  if (!batched.empty()) {
+    BatchTuner &tuner = B.tuners[key];
+    const int cfg = tuner.pick();
+    const BatchConfig C = kBatchConfigs[cfg];
+    const int tileH = 32 / C.tileW;
+    for (DJob &j : jobs) j.tilesX = (j.F.width + C.tileW - 1) / C.tileW;
+    bool ok = true;
+    if (key != B.key || cfg != B.config) {
+      if (B.graph) cudaGraphExecDestroy(B.graph);
+      B.graph = nullptr;
+      B.key = key;
+      B.config = cfg;
+      std::vector<uint32_t> w, h, items;
+      std::vector<float> cost;
+      for (int k = 0; k < kJobKinds && ok; ++k) {
+        w.clear(); h.clear(); cost.clear();
+        for (const DJob &j : jobs) {
+          const bool mine = j.kind == k;
+          w.push_back(mine ? (uint32_t)j.F.width : 0u);
+          h.push_back(mine ? (uint32_t)j.F.height : 0u);
+          cost.push_back(jobCostPerPixel(j.R, j.S));
+        }
+        B.numItems[k] = (unsigned)planItems(w.data(), h.data(), cost.data(), (uint32_t)jobs.size(),
+                                            (uint32_t)C.tileW, items);
+        ok = B.items[k].alloc(std::max<size_t>(items.size(), 2) * sizeof(uint32_t)) == cudaSuccess &&
+             (items.empty() || cudaMemcpy(B.items[k].p, items.data(), items.size() * 4,
+                                          cudaMemcpyHostToDevice) == cudaSuccess);
+      }
+      ok = ok && B.counters.alloc(kJobKinds * sizeof(unsigned)) == cudaSuccess;
+      if (jobs.size() > B.jobsCap) {
+        if (B.jobsHost) cudaFreeHost(B.jobsHost);
+        B.jobsHost = nullptr;
+        B.jobsCap = 0;
+        ok = ok && cudaMallocHost((void **)&B.jobsHost, jobs.size() * sizeof(DJob)) == cudaSuccess &&
+             B.jobs.alloc(jobs.size() * sizeof(DJob)) == cudaSuccess;
+        if (ok) B.jobsCap = jobs.size();
+      }
+      B.numJobs = (int)jobs.size();
+      if (!ok) {
+        B.key.clear();
+        dev->report(nullptr, VSR_FRAME, VSR_SEVERITY_ERROR, VSR_ERROR_OUT_OF_MEMORY,
+                    "batch work list allocation failed");
+        return VSR_ERROR_OUT_OF_MEMORY;
+      }
+    }
+    (void)tileH;
+    memcpy(B.jobsHost, jobs.data(), jobs.size() * sizeof(DJob));
+    BatchLaunch L{};
+    L.jobs = B.jobs.as<DJob>();
+    L.numJobs = B.numJobs;
+    for (int k = 0; k < kJobKinds; ++k) {
+      L.items[k] = B.items[k].as<uint2>();
+      L.numItems[k] = B.numItems[k];
+    }
+    L.counters = B.counters.as<unsigned>();
+    L.tileW = C.tileW;
+    L.fetch = C.fetch;
+    // one CUDA graph per frame set and configuration: the job records are
+    // copied from the pinned staging buffer when the graph runs
+    if (!B.graph) {
+      cudaGraph_t g = nullptr;
+      if (cudaStreamBeginCapture(s, cudaStreamCaptureModeRelaxed) == cudaSuccess) {
+        cudaMemcpyAsync(B.jobs.p, B.jobsHost, jobs.size() * sizeof(DJob), cudaMemcpyHostToDevice, s);
+        cudaError_t le = launchBatch(L, s);
+        cudaError_t ce = cudaStreamEndCapture(s, &g);
+        if (le == cudaSuccess && ce == cudaSuccess && g &&
+            cudaGraphInstantiate(&B.graph, g, 0) != cudaSuccess)
+          B.graph = nullptr;
+        if (g) cudaGraphDestroy(g);
+      }
+      cudaGetLastError();  // a failed capture falls back to direct launches
+    }
+    for (FrameObj *F : batched) {
+      cudaEventRecord(F->evStart, s);
+      cudaEventRecord(F->evRender, s);
+    }
+    cudaEventRecord(B.ev0, s);
+    cudaError_t e;
+    if (B.graph) {
+      e = cudaGraphLaunch(B.graph, s);
+    } else {
+      e = cudaMemcpyAsync(B.jobs.p, B.jobsHost, jobs.size() * sizeof(DJob), cudaMemcpyHostToDevice, s);
+      if (e == cudaSuccess) e = launchBatch(L, s);
+    }
+    cudaEventRecord(B.ev1, s);
+    if (tuner.best < 0) {
+      B.pending = true;
+      B.pendingKey = key;
+      B.pendingConfig = cfg;
+    }
+    for (size_t i = 0; i < batched.size(); ++i) {
+      FrameObj *F = batched[i];
+      cudaEventRecord(F->evStop, s);
+      cudaMemcpyAsync(F->errHost, F->errFlags.p, sizeof(uint32_t), cudaMemcpyDeviceToHost, s);
+      if (jobs[i].F.width) F->accumID++;
+      F->rendered = true;
+      F->batchTileW = C.tileW;
+      F->batchFetch = C.fetch;
+      F->batchTuned = tuner.best >= 0 ? 1 : 0;
+    }
+    if (e != cudaSuccess) {
+      dev->report(nullptr, VSR_FRAME, VSR_SEVERITY_ERROR, VSR_ERROR_CUDA,
+                  "batched render launch failed: %s", cudaGetErrorString(e));
+      return VSR_ERROR_CUDA;
+    }
+  }
+  for (FrameObj *F : single) {
+    VSRStatus r = renderFrame(dev, F);
+    if (r != VSR_OK) status = r;
+  }
+  return status;
+}
+
 } // namespace vsr
 
 using namespace vsr;
@@ -1384,6 +1649,8 @@ VSRStatus vsrReleaseDevice(VSRDevice dv) {
   Device *d = asDev(dv);
   if (!d) return VSR_ERROR_INVALID_ARGUMENT;
   cudaStreamSynchronize(d->stream);
+  destroyBatch(d->batch);
+  d->batch = nullptr;
   std::vector<Object *> left(d->live.begin(), d->live.end());
   if (!left.empty())
     d->report(nullptr, VSR_UNKNOWN, VSR_SEVERITY_WARNING, VSR_OK,
@@ -1544,6 +1811,13 @@ int vsrGetProperty(VSRDevice dv, VSRObject ov, const char *name, VSRDataType typ
       *(int32_t *)mem = F->lastIterations;
       return 1;
     }
+    if ((n == "batch.tileWidth" || n == "batch.fetch" || n == "batch.tuned") &&
+        type == VSR_INT32 && size >= 4) {
+      *(int32_t *)mem = n == "batch.tileWidth" ? F->batchTileW
+                        : n == "batch.fetch"   ? F->batchFetch
+                                               : F->batchTuned;
+      return 1;
+    }
     if (n == "numSamples" && type == VSR_INT32 && size >= 4) {
       *(int32_t *)mem = F->accumID;
       return 1;
@@ -1573,6 +1847,31 @@ int vsrGetProperty(VSRDevice dv, VSRObject ov, const char *name, VSRDataType typ
     }
   }
   return 0;
+}
+
+VSRStatus vsrRenderFrames(VSRDevice dv, const VSRFrame *fv, uint32_t count) {
+  Device *d = asDev(dv);
+  if (!d || (!fv && count)) return VSR_ERROR_INVALID_ARGUMENT;
+  std::lock_guard<std::recursive_mutex> lk(d->mtx);
+  std::vector<FrameObj *> fs;
+  for (uint32_t i = 0; i < count; ++i) {
+    Object *o = asObj(fv[i]);
+    if (!checkObj(d, o) || o->kind != VSR_FRAME) return VSR_ERROR_INVALID_OBJECT;
+    FrameObj *F = static_cast<FrameObj *>(o);
+    if (std::find(fs.begin(), fs.end(), F) != fs.end()) return VSR_ERROR_INVALID_ARGUMENT;
+    fs.push_back(F);
+  }
+  if (fs.empty()) return VSR_OK;
+  return renderFrames(d, fs.data(), (uint32_t)fs.size());
+}
+
+uint64_t vsrPlanBatch(const uint32_t *width, const uint32_t *height, const float *costPerPixel,
+                      uint32_t numJobs, uint32_t tileWidth, uint32_t *items, uint64_t capacity) {
+  if ((!width || !height || !costPerPixel) && numJobs) return 0;
+  std::vector<uint32_t> out;
+  const size_t n = planItems(width, height, costPerPixel, numJobs, tileWidth, out);
+  if (items) memcpy(items, out.data(), std::min<uint64_t>(n, capacity) * 2 * sizeof(uint32_t));
+  return n;
 }
 
 VSRStatus vsrRenderFrame(VSRDevice dv, VSRFrame fv) {

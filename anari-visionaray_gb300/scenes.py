@@ -214,6 +214,72 @@ def config2(res=(1920, 1080), spp=256, n=512, num_spheres=256, nu=64, nv=32, max
     }
 
 
+def blob_field_fast(n, rng, num_blobs=16):
+    """blob_field's distribution (centres U[0,1]^3, sigma U[0.05,0.15],
+    amplitude U[0.2,1]) evaluated separably as one matrix product: the
+    Gaussian of blob b factors into gz_b(z) gy_b(y) gx_b(x), so the field is
+    Gz (n x B) times the B x n^2 matrix of a_b gy_b(y) gx_b(x). Normalised to
+    [0,1]."""
+    centres = rng.uniform(0.0, 1.0, size=(num_blobs, 3))
+    sigma = rng.uniform(0.05, 0.15, size=num_blobs)
+    amp = rng.uniform(0.2, 1.0, size=num_blobs)
+    p = (np.arange(n, dtype=np.float64) + 0.5) / n
+    inv = 1.0 / (2.0 * sigma * sigma)
+    gx = np.exp(-((p[None, :] - centres[:, 0:1]) ** 2) * inv[:, None])   # (B, n)
+    gy = np.exp(-((p[None, :] - centres[:, 1:2]) ** 2) * inv[:, None])
+    gz = np.exp(-((p[None, :] - centres[:, 2:3]) ** 2) * inv[:, None])
+    yx = (amp[:, None, None] * gy[:, :, None] * gx[:, None, :]).reshape(num_blobs, n * n)
+    field = (gz.T.astype(np.float32) @ yx.astype(np.float32)).reshape(n, n, n)
+    lo, hi = float(field.min()), float(field.max())
+    return ((field - lo) / (hi - lo)).astype(np.float32)
+
+
+def config3(num_scenes=64, seed=SEED_BASE + 3, sizes=(256, 512, 768, 1024), side=(64, 384),
+            tris=(10_000, 500_000), spp=(1, 64), max_bounce=5):
+    """Batched rendering: independent scenes, each seeded with seed + index.
+
+    Per scene, in draw order: volume side U{side}, raycast or pathtrace
+    (coin), spheres or not (coin), triangle count U[tris] as UV spheres of
+    64x32 segments (4032 triangles each) over [-10,10]^3, image size from
+    `sizes`, spp U{spp} (pixelSamples of the path tracer; the raycast
+    renderer takes one sample per pixel). The volume is a config-0 style blob field over
+    [-12,12]^3 (unitDistance one voxel spacing, dt half a voxel, opacity
+    0..0.05); light, ambient and camera as config 1."""
+    scenes = []
+    light_dir = np.array([-0.35, -1.0, -0.45])
+    light_dir /= np.linalg.norm(light_dir)
+    for i in range(num_scenes):
+        rng = np.random.default_rng(seed + i)
+        n = int(rng.integers(side[0], side[1] + 1))
+        kind = "raycast" if rng.uniform() < 0.5 else "pathtrace"
+        with_spheres = rng.uniform() < 0.5
+        ntri = int(rng.integers(tris[0], tris[1] + 1))
+        res = int(sizes[int(rng.integers(0, len(sizes)))])
+        s = int(rng.integers(spp[0], spp[1] + 1))
+        data = blob_field_fast(n, rng)
+        color, opacity = linear_tf(256, 0.05)
+        spacing = 24.0 / (n - 1)
+        surfaces = []
+        if with_spheres:
+            surfaces = sphere_set(rng, max(1, round(ntri / 4032)))[:-1]  # no ground quad
+        renderer = {"type": kind, "pixelSamples": s, "volumeSamplingRate": 2.0,
+                    "ambientRadiance": 0.2, "background": [0, 0, 0, 1]}
+        if kind == "pathtrace":
+            renderer["maxBounce"] = max_bounce
+        scenes.append({
+            "surfaces": surfaces,
+            "volumes": [{"data": data, "origin": [-12.0] * 3, "spacing": [spacing] * 3,
+                         "color": color, "opacity": opacity, "valueRange": [0.0, 1.0],
+                         "unitDistance": spacing, "majorantBrickSize": 16}],
+            "lights": [{"direction": [float(x) for x in light_dir], "color": [1.0, 1.0, 1.0],
+                        "irradiance": 3.0}],
+            "camera": _look_at_camera([0.0, -1.0, 0.0], [6.0, 9.0, 34.0], 45.0, 1.0),
+            "renderer": renderer,
+            "frame": {"size": (res, res)},
+        })
+    return scenes
+
+
 def triangle_count(scene):
     return sum(len(s["indices"]) for s in scene["surfaces"])
 

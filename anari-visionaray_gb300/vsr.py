@@ -57,6 +57,10 @@ _SIGNATURES = [
     ("vsrGetProperty", ctypes.c_int, [_P, _P, ctypes.c_char_p, ctypes.c_int, _P, ctypes.c_uint64,
                                       ctypes.c_int]),
     ("vsrRenderFrame", ctypes.c_int, [_P, _P]),
+    ("vsrRenderFrames", ctypes.c_int, [_P, ctypes.POINTER(_P), ctypes.c_uint32]),
+    ("vsrPlanBatch", ctypes.c_uint64, [ctypes.POINTER(ctypes.c_uint32), ctypes.POINTER(ctypes.c_uint32),
+                                       ctypes.POINTER(ctypes.c_float), ctypes.c_uint32, ctypes.c_uint32,
+                                       ctypes.POINTER(ctypes.c_uint32), ctypes.c_uint64]),
     ("vsrFrameReady", ctypes.c_int, [_P, _P, ctypes.c_int]),
     ("vsrDiscardFrame", ctypes.c_int, [_P, _P]),
     ("vsrMapFrame", _P, [_P, _P, ctypes.c_char_p, ctypes.POINTER(ctypes.c_uint32),
@@ -72,6 +76,23 @@ _SIGNATURES = [
 EXPORTED_SYMBOLS = [s[0] for s in _SIGNATURES]
 
 _lib = None
+
+
+def plan_batch(widths, heights, costs, tile_width, lib=None):
+    """Work list of a batch (vsrPlanBatch): an (n, 2) uint32 array of (job,
+    tile) pairs. Needs no GPU."""
+    import numpy as np
+    lib = lib or load_library()
+    n = len(widths)
+    w = (ctypes.c_uint32 * n)(*widths)
+    h = (ctypes.c_uint32 * n)(*heights)
+    c = (ctypes.c_float * n)(*costs)
+    count = lib.vsrPlanBatch(w, h, c, n, tile_width, None, 0)
+    out = np.zeros((count, 2), dtype=np.uint32)
+    if count:
+        lib.vsrPlanBatch(w, h, c, n, tile_width,
+                         out.ctypes.data_as(ctypes.POINTER(ctypes.c_uint32)), count)
+    return out
 
 
 def load_library(path=LIB_PATH):
@@ -248,6 +269,11 @@ class Device:
     # -- frames ------------------------------------------------------------
     def render(self, frame):
         return self.lib.vsrRenderFrame(self.handle, frame.ptr)
+
+    def render_batch(self, frames):
+        """Render several frames as one batch (vsrRenderFrames)."""
+        arr = (_P * len(frames))(*[f.ptr for f in frames])
+        return self.lib.vsrRenderFrames(self.handle, arr, len(frames))
 
     def wait(self, frame):
         return self.lib.vsrFrameReady(self.handle, frame.ptr, WAIT)

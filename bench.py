@@ -55,6 +55,8 @@ def parse():
     p.add_argument("--volume-res", type=int, nargs=2, default=[1920, 1080],
                    help="config-2 frame size (full size by default; smaller for profiling)")
     p.add_argument("--volume-spp", type=int, default=256)
+    p.add_argument("--no-batch", dest="batch", action="store_false",
+                   help="skip the config-3 batched-rendering measurement")
     return p.parse_args()
 
 
@@ -203,6 +205,68 @@ def measure_raycast_config0(pkg, dev, flush, steps=20):
                                  "segmented marcher (set-up, 16-sample segments, combine); "
                                  "the 8 MiB field is L2-resident, so DRAM traffic is far "
                                  "below the algorithmic bytes"}}
+
+
+def measure_batch_config3(pkg, dev, steps=3, num_scenes=64):
+    """Config 3 (64 independent scenes: blob volumes of side 64..384, optional
+    10k..500k-triangle sphere sets, images 256^2..1024^2, 1..64 spp, raycast
+    and path tracing): the 64 frames as one batch (vsrRenderFrames, CUDA
+    graph, tuned tiles) against the same frames rendered one after another
+    with vsrRenderFrame. Both are timed on the host from the first call to
+    the end of the last frame; each step renders every frame once more."""
+    t_gen = time.perf_counter()
+    scenes = pkg.scenes.config3(num_scenes=num_scenes)
+    gen_s = time.perf_counter() - t_gen
+    hs = [pkg.scenes.build(dev, sc, channels=("color", "depth")) for sc in scenes]
+    frames = [h["frame"] for h in hs]
+    # the raycast renderer takes one sample per pixel (pixelSamples is a
+    # path-tracer parameter)
+    px_spp = sum(sc["frame"]["size"][0] * sc["frame"]["size"][1] *
+                 (sc["renderer"]["pixelSamples"] if sc["renderer"]["type"] == "pathtrace" else 1)
+                 for sc in scenes)
+
+    def wait_all():
+        for f in frames:
+            dev.wait(f)
+
+    def sequential():
+        t = time.perf_counter()
+        for f in frames:
+            dev.render(f)
+        wait_all()
+        return time.perf_counter() - t
+
+    def batched():
+        t = time.perf_counter()
+        dev.render_batch(frames)
+        wait_all()
+        return time.perf_counter() - t
+
+    sequential()  # commits, BVH builds, first-use allocations
+    tune = 0
+    while not dev.get_int(frames[0], "batch.tuned") and tune < 32:
+        batched()
+        tune += 1
+    batched()
+    seq = [sequential() for _ in range(steps)]
+    bat = [batched() for _ in range(steps)]
+    err = 0
+    for f in frames:
+        err |= dev.get_uint(f, "errorFlags") or 0
+    tile_w, fetch = dev.get_int(frames[0], "batch.tileWidth"), dev.get_int(frames[0], "batch.fetch")
+    for h in hs:
+        for o in (h["frame"], h["renderer"], h["camera"], h["world"], *h["keep"]):
+            dev.release(o)
+    ts, tb = statistics.mean(seq), statistics.mean(bat)
+    kinds = {k: sum(1 for sc in scenes if sc["renderer"]["type"] == k) for k in ("raycast", "pathtrace")}
+    return {"value": px_spp / tb / MPX, "unit": "Mpx*spp/s", "batched_ms": 1e3 * tb,
+            "sequential_ms": 1e3 * ts, "speedup_vs_sequential": ts / tb,
+            "sequential_value": px_spp / ts / MPX,
+            "workload": f"config3 {num_scenes} scenes ({kinds['raycast']} raycast, "
+                        f"{kinds['pathtrace']} pathtrace), {px_spp / 1e6:.0f} Mpx*spp per pass",
+            "tile": f"{tile_w}x{32 // max(tile_w, 1)}", "fetch": fetch, "tuning_batches": tune,
+            "error_flags": err, "generate_s": gen_s,
+            "timing": "host wall clock, first call to last frame done; synthetic seeded scenes"}
 
 
 def measure_volume_config2(pkg, dev, flush, count_spp=8, res=(1920, 1080), spp=256):
@@ -368,6 +432,7 @@ def run_ours(args):
     h2d = 3 * 4 + 4 * 4 * 0  # the camera position crosses to the device as kernel parameters
 
     raycast = measure_raycast_config0(pkg, dev, flush) if args.raycast else None
+    batch = measure_batch_config3(pkg, dev) if args.batch else None
     volume = (measure_volume_config2(pkg, dev, flush, res=args.volume_res, spp=args.volume_spp)
               if args.volume else None)
 
@@ -406,7 +471,7 @@ def run_ours(args):
                       "node_visit_histogram_log2": counts[8:24],
                       "grays_per_s": rays / kernel_s / 1e9},
         "commit_s": commit_s, "bvh_build_s": bvh_s, "raycast_config0": raycast,
-        "volume_pathtracer_config2": volume,
+        "volume_pathtracer_config2": volume, "batch_config3": batch,
         "wall_s_timed": wall, "clocks": clk, "error_flags": err,
         "wavefront_iterations": iterations,
     }

@@ -171,6 +171,29 @@ VSR_API VSRStatus vsrRenderFrame(VSRDevice d, VSRFrame f);
 VSR_API int vsrFrameReady(VSRDevice d, VSRFrame f, VSRWaitMask mask);
 VSR_API VSRStatus vsrDiscardFrame(VSRDevice d, VSRFrame f);
 
+/* vsrRenderFrames has no counterpart in the reference (which renders one
+   frame per anariRenderFrame call). It renders `count` distinct frames, of
+   any scenes, cameras, renderers and sizes, as one batch: each frame gets
+   what vsrRenderFrame would do to it (accumulation reset after commits,
+   sampleLimit, one more accumulated frame) and the same image, but all
+   frames' pixels are drawn from shared work lists by persistent kernels,
+   replayed as one CUDA graph per frame set. Successive batches of the same
+   frame set try the tile shapes and fetch sizes of a built-in autotuner and
+   then keep the fastest (frame properties batch.tileWidth, batch.fetch,
+   batch.tuned). Frames collecting statistics are rendered one by one.
+   Completion: vsrFrameReady on any of the frames. */
+VSR_API VSRStatus vsrRenderFrames(VSRDevice d, const VSRFrame *frames, uint32_t count);
+
+/* Work list of a batch, without a device (vsrPlanBatch has no counterpart in
+   the reference): tiles of tileWidth x (32 / tileWidth) pixels for jobs of
+   the given sizes, as (job, tile) uint32 pairs ordered by cost per pixel,
+   highest first, all tiles of a job together. Writes at most `capacity`
+   pairs to `items` (may be null) and returns the number of pairs; 0 for a
+   tileWidth that does not divide 32. */
+VSR_API uint64_t vsrPlanBatch(const uint32_t *width, const uint32_t *height,
+                              const float *costPerPixel, uint32_t numJobs, uint32_t tileWidth,
+                              uint32_t *items, uint64_t capacity);
+
 /* Mapping; replaces anariMapFrame / anariUnmapFrame (frame/Frame.cpp:399-447).
    Channels: "channel.color", "channel.depth", "channel.normal",
    "channel.albedo". Returns a host pointer valid until the next render or

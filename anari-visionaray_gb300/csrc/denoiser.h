@@ -1,0 +1,76 @@
+// The learned denoiser: a 4-level U-Net of 3x3 convolutions (channels
+// 32 -> 64 -> 128 -> 256, two convolutions per level, 2x2 max pooling,
+// nearest 2x upsampling, skip connections by channel concatenation, ReLU),
+// bf16 weights and activations with fp32 accumulation, trained with L1 on
+// log(1 + colour) and Adam. Inputs: 16 channels per pixel (log(1 + colour),
+// albedo, normal, depth / (1 + depth), six zeros); output: log(1 + colour)
+// in the first 3 of 16 fp32 channels.
+#pragma once
+
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <vector>
+
+namespace vsr {
+
+struct DenoiseLayer {
+  int cin, cout;
+  size_t w, b;  // offsets of weights [cout][9][cin] and bias [cout] in the parameter array
+  size_t wt;    // offset of the flipped, transposed bf16 copy [cin][9][cout]
+};
+
+class Denoiser {
+ public:
+  static constexpr int kInC = 16, kOutC = 16, kColorC = 3;
+  explicit Denoiser(uint64_t seed);
+  ~Denoiser();
+  bool ok() const { return ok_; }
+  size_t numParams() const { return numParams_; }
+  const std::vector<DenoiseLayer> &layers() const { return layers_; }
+
+  // parameters in the canonical order (per layer: weights, then bias), fp32
+  cudaError_t getParams(float *host, cudaStream_t s);
+  cudaError_t setParams(const float *host, cudaStream_t s);
+
+  // x: N x H x W x 16 bf16 (device), out: N x H x W x 16 fp32 (device);
+  // H and W multiples of 8
+  cudaError_t forward(const __nv_bfloat16 *x, int N, int H, int W, float *out, cudaStream_t s);
+  // forward + backward: fp32 gradients into grad() (zeroed first), L1 loss
+  // against the linear target colour (tC floats per pixel, first 3 used)
+  cudaError_t backward(const __nv_bfloat16 *x, const float *target, int tC, int N, int H, int W,
+                       float *lossDevice, cudaStream_t s);
+  // one Adam step (beta 0.9 / 0.999, eps 1e-8) with the current gradients
+  cudaError_t adam(float lr, cudaStream_t s);
+  const float *grad() const { return grad_; }
+  int steps() const { return step_; }
+
+ private:
+  struct Act {
+    __nv_bfloat16 *a0, *e0, *p0, *a1, *e1, *p1, *a2, *e2, *p2, *a3, *e3, *cat2, *b2, *d2, *cat1,
+        *b1, *d1, *cat0, *b0, *d0;
+  };
+  cudaError_t ensure(int N, int H, int W, bool train);
+  cudaError_t run(const __nv_bfloat16 *x, int N, int H, int W, float *out, cudaStream_t s);
+  void conv(int layer, const __nv_bfloat16 *x, int xC, __nv_bfloat16 *y, float *yf, int yC, int N,
+            int H, int W, bool relu, cudaStream_t s);
+  void convBack(int layer, const __nv_bfloat16 *x, int xC, const __nv_bfloat16 *dy,
+                __nv_bfloat16 *dx, const __nv_bfloat16 *mask, int N, int H, int W,
+                cudaStream_t s);
+
+  bool ok_ = false;
+  std::vector<DenoiseLayer> layers_;
+  size_t numParams_ = 0, numWt_ = 0;
+  float *params_ = nullptr, *m_ = nullptr, *v_ = nullptr, *grad_ = nullptr;
+  __nv_bfloat16 *wbf_ = nullptr, *wt_ = nullptr;
+  int step_ = 0;
+  // activations (and, for training, their gradients), sized for (N, H, W)
+  int n_ = 0, h_ = 0, w_ = 0;
+  bool train_ = false;
+  std::vector<void *> bufs_;
+  Act act_{}, grd_{};
+  float *out_ = nullptr;
+  __nv_bfloat16 *gout_ = nullptr;
+};
+
+}  // namespace vsr

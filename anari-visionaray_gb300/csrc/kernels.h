@@ -3,6 +3,7 @@
 
 #include "vsr_device.h"
 #include <cuda_runtime.h>
+#include <cuda_bf16.h>
 #include <stddef.h>
 
 namespace vsr {
@@ -61,6 +62,61 @@ struct BatchLaunch {
   int fetch;           // items per atomic
 };
 cudaError_t launchBatch(const BatchLaunch &L, cudaStream_t stream);
+
+// Denoiser kernels (k_denoise.cu). Activations NHWC bf16; a tensor view is
+// (pointer, channels per pixel, first channel), both multiples of 8.
+// Convolution weights are [Cout][9][Cin] bf16 (tap = 3 (dy + 1) + dx + 1),
+// biases fp32.
+struct ConvArgs {
+  const __nv_bfloat16 *x;
+  int xC, xOff, Cin;  // Cin a multiple of 16
+  const __nv_bfloat16 *w;
+  const float *bias;  // or null
+  int Cout;
+  __nv_bfloat16 *y;   // bf16 output, or
+  float *yf;          // fp32 output
+  int yC, yOff;
+  const __nv_bfloat16 *mask;  // zero outputs where mask <= 0 (a ReLU's backward), or null
+  int maskC, maskOff;
+  int relu;
+  int N, H, W;
+};
+struct WgradArgs {
+  const __nv_bfloat16 *dy;  // output gradient (after the ReLU mask)
+  int dyC, dyOff, Cout;     // Cout a multiple of 8
+  const __nv_bfloat16 *x;   // layer input
+  int xC, xOff, Cin;        // Cin a multiple of 8
+  float *dw;                // [Cout][9][Cin], accumulated
+  int N, H, W;
+  int chunk;                // pixels per CTA
+};
+cudaError_t launchConv3x3(const ConvArgs &a, cudaStream_t s);
+cudaError_t launchConvWgrad(const WgradArgs &a, cudaStream_t s);
+cudaError_t launchBiasGrad(const __nv_bfloat16 *dy, int dyC, int dyOff, int C, int P, float *db,
+                           cudaStream_t s);
+cudaError_t launchMaxPool(const __nv_bfloat16 *x, int C, int N, int H, int W, __nv_bfloat16 *y,
+                          cudaStream_t s);
+cudaError_t launchMaxPoolGrad(const __nv_bfloat16 *x, const __nv_bfloat16 *dy, int C, int N, int H,
+                              int W, const __nv_bfloat16 *mask, __nv_bfloat16 *dx, cudaStream_t s);
+cudaError_t launchUpsample(const __nv_bfloat16 *x, int C, int N, int H, int W, __nv_bfloat16 *y,
+                           int yC, int yOff, cudaStream_t s);
+cudaError_t launchUpsampleGrad(const __nv_bfloat16 *dy, int dyC, int dyOff, int C, int N, int H,
+                               int W, const __nv_bfloat16 *mask, __nv_bfloat16 *dx, cudaStream_t s);
+cudaError_t launchCopyChannels(const __nv_bfloat16 *x, int xC, int xOff, __nv_bfloat16 *y, int yC,
+                               int yOff, int C, size_t P, int add, cudaStream_t s);
+cudaError_t launchReluMask(__nv_bfloat16 *d, int dC, int dOff, const __nv_bfloat16 *post, int pC,
+                           int pOff, int C, size_t P, cudaStream_t s);
+cudaError_t launchL1(const float *out, int oC, const float *target, int tC, int C, size_t P,
+                     __nv_bfloat16 *grad, int gC, float *loss, cudaStream_t s);
+cudaError_t launchAdam(float *w, float *m, float *v, const float *g, size_t n, float lr, float b1,
+                       float b2, float eps, int step, __nv_bfloat16 *wb, __nv_bfloat16 *wt, int Cin,
+                       int CoutT, cudaStream_t s);
+cudaError_t launchDenoiseInput(const float4 *color, const float *albedo, const float *normal,
+                               const float *depth, int W, int H, int Wp, int Hp,
+                               __nv_bfloat16 *x, int xC, cudaStream_t s);
+cudaError_t launchDenoiseOutput(const float *out, int oC, int W, int H, int Wp, const float4 *mean,
+                                const float *var, float k, float floorAbs, float4 *result,
+                                uint8_t *retry, unsigned *numRetry, cudaStream_t s);
 
 // Accumulation reset: accum = 0, depth = 1e31 (frame/Frame.cpp:287-312).
 cudaError_t launchFrameReset(float4 *accum, float *depth, size_t numPixels, cudaStream_t stream);

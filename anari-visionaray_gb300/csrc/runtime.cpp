@@ -13,6 +13,7 @@
 
 #include "kernels.h"
 #include "vsr_device.h"
+#include "denoiser.h"
 
 #include <cuda_runtime.h>
 
@@ -41,6 +42,7 @@ void destroyBatch(BatchState *);
 struct Device {
   VSRStatusCallback cb = nullptr;
   BatchState *batch = nullptr;  // batched rendering: plans, tuner, CUDA graph
+  std::set<Denoiser *> denoisers;
   const void *cbUser = nullptr;
   int cudaDevice = 0;
   cudaStream_t stream = nullptr;
@@ -1041,6 +1043,8 @@ struct FrameObj : Object {
               albedoType = VSR_UNKNOWN;
   DevBuf color, depth, normal, albedo, accum, errFlags, marchItems, marchGroups, marchCounters,
       unitGroup, segOut;
+  DevBuf variance, accumSq;                    // optional: variance of the mean (luminance)
+  DevBuf denoiseIn, denoiseOut, denoiseCount;  // denoiser scratch, made on first use
   size_t marchPixels = 0;
   unsigned unitCap = 0;
   std::map<std::string, void *> pinned;
@@ -1651,6 +1655,8 @@ VSRStatus vsrReleaseDevice(VSRDevice dv) {
   cudaStreamSynchronize(d->stream);
   destroyBatch(d->batch);
   d->batch = nullptr;
+  for (Denoiser *n : d->denoisers) delete n;
+  d->denoisers.clear();
   std::vector<Object *> left(d->live.begin(), d->live.end());
   if (!left.empty())
     d->report(nullptr, VSR_UNKNOWN, VSR_SEVERITY_WARNING, VSR_OK,
@@ -1863,6 +1869,201 @@ VSRStatus vsrRenderFrames(VSRDevice dv, const VSRFrame *fv, uint32_t count) {
   }
   if (fs.empty()) return VSR_OK;
   return renderFrames(d, fs.data(), (uint32_t)fs.size());
+}
+
+static Denoiser *asDenoiser(Device *d, VSRDenoiser n) {
+  Denoiser *p = reinterpret_cast<Denoiser *>(n);
+  return d && d->denoisers.count(p) ? p : nullptr;
+}
+
+static VSRStatus cudaStatus(Device *d, cudaError_t e, const char *what) {
+  if (e == cudaSuccess) return VSR_OK;
+  const VSRStatus st = e == cudaErrorInvalidValue ? VSR_ERROR_INVALID_ARGUMENT
+                       : e == cudaErrorMemoryAllocation ? VSR_ERROR_OUT_OF_MEMORY
+                                                        : VSR_ERROR_CUDA;
+  d->report(nullptr, VSR_UNKNOWN, VSR_SEVERITY_ERROR, st, "%s: %s", what, cudaGetErrorString(e));
+  return st;
+}
+
+VSRDenoiser vsrNewDenoiser(VSRDevice dv, uint64_t seed) {
+  Device *d = asDev(dv);
+  if (!d) return nullptr;
+  std::lock_guard<std::recursive_mutex> lk(d->mtx);
+  Denoiser *n = new Denoiser(seed);
+  if (!n->ok()) {
+    delete n;
+    d->report(nullptr, VSR_UNKNOWN, VSR_SEVERITY_ERROR, VSR_ERROR_OUT_OF_MEMORY,
+              "denoiser allocation failed");
+    return nullptr;
+  }
+  d->denoisers.insert(n);
+  return reinterpret_cast<VSRDenoiser>(n);
+}
+
+VSRStatus vsrReleaseDenoiser(VSRDevice dv, VSRDenoiser nv) {
+  Device *d = asDev(dv);
+  if (!d) return VSR_ERROR_INVALID_ARGUMENT;
+  std::lock_guard<std::recursive_mutex> lk(d->mtx);
+  Denoiser *n = asDenoiser(d, nv);
+  if (!n) return VSR_ERROR_INVALID_OBJECT;
+  cudaStreamSynchronize(d->stream);
+  d->denoisers.erase(n);
+  delete n;
+  return VSR_OK;
+}
+
+uint64_t vsrDenoiserParameterCount(VSRDevice dv, VSRDenoiser nv) {
+  Device *d = asDev(dv);
+  if (!d) return 0;
+  std::lock_guard<std::recursive_mutex> lk(d->mtx);
+  Denoiser *n = asDenoiser(d, nv);
+  return n ? n->numParams() : 0;
+}
+
+VSRStatus vsrDenoiserGetParameters(VSRDevice dv, VSRDenoiser nv, float *params, uint64_t count) {
+  Device *d = asDev(dv);
+  if (!d || !params) return VSR_ERROR_INVALID_ARGUMENT;
+  std::lock_guard<std::recursive_mutex> lk(d->mtx);
+  Denoiser *n = asDenoiser(d, nv);
+  if (!n) return VSR_ERROR_INVALID_OBJECT;
+  if (count != n->numParams()) return VSR_ERROR_INVALID_ARGUMENT;
+  return cudaStatus(d, n->getParams(params, d->stream), "denoiser parameters");
+}
+
+VSRStatus vsrDenoiserSetParameters(VSRDevice dv, VSRDenoiser nv, const float *params,
+                                   uint64_t count) {
+  Device *d = asDev(dv);
+  if (!d || !params) return VSR_ERROR_INVALID_ARGUMENT;
+  std::lock_guard<std::recursive_mutex> lk(d->mtx);
+  Denoiser *n = asDenoiser(d, nv);
+  if (!n) return VSR_ERROR_INVALID_OBJECT;
+  if (count != n->numParams()) return VSR_ERROR_INVALID_ARGUMENT;
+  return cudaStatus(d, n->setParams(params, d->stream), "denoiser parameters");
+}
+
+VSRStatus vsrDenoiserForward(VSRDevice dv, VSRDenoiser nv, const void *input, uint32_t N,
+                             uint32_t H, uint32_t W, float *output) {
+  Device *d = asDev(dv);
+  if (!d || !input || !output) return VSR_ERROR_INVALID_ARGUMENT;
+  std::lock_guard<std::recursive_mutex> lk(d->mtx);
+  Denoiser *n = asDenoiser(d, nv);
+  if (!n) return VSR_ERROR_INVALID_OBJECT;
+  return cudaStatus(
+      d, n->forward((const __nv_bfloat16 *)input, (int)N, (int)H, (int)W, output, d->stream),
+      "denoiser forward");
+}
+
+// forward + backward; the loss (if wanted) is copied to the host
+static VSRStatus denoiserBackward(Device *d, Denoiser *n, const void *input, const float *target,
+                                  uint32_t tC, uint32_t N, uint32_t H, uint32_t W, float *loss) {
+  static float *lossDev = nullptr;  // one float per process, guarded by the device mutex
+  if (!lossDev && cudaMalloc(&lossDev, sizeof(float)) != cudaSuccess) {
+    lossDev = nullptr;
+    return VSR_ERROR_OUT_OF_MEMORY;
+  }
+  VSRStatus st = cudaStatus(d, n->backward((const __nv_bfloat16 *)input, target, (int)tC, (int)N,
+                                           (int)H, (int)W, lossDev, d->stream),
+                            "denoiser backward");
+  if (st == VSR_OK && loss)
+    st = cudaStatus(d, cudaMemcpyAsync(loss, lossDev, sizeof(float), cudaMemcpyDeviceToHost,
+                                       d->stream),
+                    "denoiser loss");
+  return st;
+}
+
+VSRStatus vsrDenoiserGradients(VSRDevice dv, VSRDenoiser nv, const void *input, const float *target,
+                               uint32_t tC, uint32_t N, uint32_t H, uint32_t W, float *grads,
+                               uint64_t count, float *loss) {
+  Device *d = asDev(dv);
+  if (!d || !input || !target || !grads) return VSR_ERROR_INVALID_ARGUMENT;
+  std::lock_guard<std::recursive_mutex> lk(d->mtx);
+  Denoiser *n = asDenoiser(d, nv);
+  if (!n) return VSR_ERROR_INVALID_OBJECT;
+  if (count != n->numParams()) return VSR_ERROR_INVALID_ARGUMENT;
+  VSRStatus st = denoiserBackward(d, n, input, target, tC, N, H, W, loss);
+  if (st == VSR_OK)
+    st = cudaStatus(d, cudaMemcpyAsync(grads, n->grad(), count * sizeof(float),
+                                       cudaMemcpyDeviceToHost, d->stream),
+                    "denoiser gradients");
+  if (st == VSR_OK) st = cudaStatus(d, cudaStreamSynchronize(d->stream), "denoiser gradients");
+  return st;
+}
+
+VSRStatus vsrDenoiserTrainStep(VSRDevice dv, VSRDenoiser nv, const void *input, const float *target,
+                               uint32_t tC, uint32_t N, uint32_t H, uint32_t W, float lr,
+                               float *loss) {
+  Device *d = asDev(dv);
+  if (!d || !input || !target) return VSR_ERROR_INVALID_ARGUMENT;
+  std::lock_guard<std::recursive_mutex> lk(d->mtx);
+  Denoiser *n = asDenoiser(d, nv);
+  if (!n) return VSR_ERROR_INVALID_OBJECT;
+  VSRStatus st = denoiserBackward(d, n, input, target, tC, N, H, W, loss);
+  if (st == VSR_OK) st = cudaStatus(d, n->adam(lr, d->stream), "denoiser update");
+  if (st == VSR_OK && loss) st = cudaStatus(d, cudaStreamSynchronize(d->stream), "denoiser step");
+  return st;
+}
+
+VSRStatus vsrDenoiserFrameInput(VSRDevice dv, VSRFrame fv, void *input) {
+  Device *d = asDev(dv);
+  if (!d || !input) return VSR_ERROR_INVALID_ARGUMENT;
+  std::lock_guard<std::recursive_mutex> lk(d->mtx);
+  Object *o = asObj(fv);
+  if (!checkObj(d, o) || o->kind != VSR_FRAME) return VSR_ERROR_INVALID_OBJECT;
+  FrameObj *F = static_cast<FrameObj *>(o);
+  if (!F->valid || !F->accum.p) return VSR_ERROR_INCOMPLETE;
+  const int Wp = (F->width + 7) / 8 * 8, Hp = (F->height + 7) / 8 * 8;
+  return cudaStatus(d, launchDenoiseInput(F->accum.as<float4>(), F->albedo.as<float>(),
+                                          F->normal.as<float>(), F->depth.as<float>(), F->width,
+                                          F->height, Wp, Hp, (__nv_bfloat16 *)input,
+                                          Denoiser::kInC, d->stream),
+                    "denoiser input");
+}
+
+VSRStatus vsrDenoiseFrame(VSRDevice dv, VSRDenoiser nv, VSRFrame fv, float k, float floorAbs,
+                          float *colorOut, uint8_t *retry, uint32_t *numRetry) {
+  Device *d = asDev(dv);
+  if (!d || !colorOut) return VSR_ERROR_INVALID_ARGUMENT;
+  std::lock_guard<std::recursive_mutex> lk(d->mtx);
+  Denoiser *n = asDenoiser(d, nv);
+  Object *o = asObj(fv);
+  if (!n || !checkObj(d, o) || o->kind != VSR_FRAME) return VSR_ERROR_INVALID_OBJECT;
+  FrameObj *F = static_cast<FrameObj *>(o);
+  if (!F->valid || !F->accum.p) return VSR_ERROR_INCOMPLETE;
+  const int Wp = (F->width + 7) / 8 * 8, Hp = (F->height + 7) / 8 * 8;
+  const size_t np = (size_t)Wp * Hp;
+  if (F->denoiseIn.bytes < np * Denoiser::kInC * 2 ||
+      F->denoiseOut.bytes < np * Denoiser::kOutC * 4 || !F->denoiseCount.p) {
+    if (F->denoiseIn.alloc(np * Denoiser::kInC * 2) != cudaSuccess ||
+        F->denoiseOut.alloc(np * Denoiser::kOutC * 4) != cudaSuccess ||
+        F->denoiseCount.alloc(sizeof(unsigned)) != cudaSuccess)
+      return VSR_ERROR_OUT_OF_MEMORY;
+  }
+  cudaStream_t s = d->stream;
+  const float4 *mean = F->accum.as<float4>();
+  VSRStatus st = cudaStatus(
+      d, launchDenoiseInput(mean, F->albedo.as<float>(), F->normal.as<float>(), F->depth.as<float>(),
+                            F->width, F->height, Wp, Hp, F->denoiseIn.as<__nv_bfloat16>(),
+                            Denoiser::kInC, s),
+      "denoiser input");
+  if (st == VSR_OK)
+    st = cudaStatus(d, n->forward(F->denoiseIn.as<__nv_bfloat16>(), 1, Hp, Wp,
+                                  F->denoiseOut.as<float>(), s),
+                    "denoiser forward");
+  if (st == VSR_OK) cudaMemsetAsync(F->denoiseCount.p, 0, sizeof(unsigned), s);
+  const float *var = F->variance.p ? F->variance.as<float>() : nullptr;
+  if (st == VSR_OK)
+    st = cudaStatus(d, launchDenoiseOutput(F->denoiseOut.as<float>(), Denoiser::kOutC, F->width,
+                                           F->height, Wp, mean, var, k, floorAbs,
+                                           (float4 *)colorOut, retry,
+                                           F->denoiseCount.as<unsigned>(), s),
+                    "denoiser output");
+  if (st == VSR_OK && numRetry) {
+    st = cudaStatus(d, cudaMemcpyAsync(numRetry, F->denoiseCount.p, sizeof(unsigned),
+                                       cudaMemcpyDeviceToHost, s),
+                    "denoiser retry count");
+    if (st == VSR_OK) st = cudaStatus(d, cudaStreamSynchronize(s), "denoiser");
+  }
+  return st;
 }
 
 uint64_t vsrPlanBatch(const uint32_t *width, const uint32_t *height, const float *costPerPixel,

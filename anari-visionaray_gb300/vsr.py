@@ -61,6 +61,20 @@ _SIGNATURES = [
     ("vsrPlanBatch", ctypes.c_uint64, [ctypes.POINTER(ctypes.c_uint32), ctypes.POINTER(ctypes.c_uint32),
                                        ctypes.POINTER(ctypes.c_float), ctypes.c_uint32, ctypes.c_uint32,
                                        ctypes.POINTER(ctypes.c_uint32), ctypes.c_uint64]),
+    ("vsrNewDenoiser", _P, [_P, ctypes.c_uint64]),
+    ("vsrReleaseDenoiser", ctypes.c_int, [_P, _P]),
+    ("vsrDenoiserParameterCount", ctypes.c_uint64, [_P, _P]),
+    ("vsrDenoiserGetParameters", ctypes.c_int, [_P, _P, ctypes.POINTER(ctypes.c_float), ctypes.c_uint64]),
+    ("vsrDenoiserSetParameters", ctypes.c_int, [_P, _P, ctypes.POINTER(ctypes.c_float), ctypes.c_uint64]),
+    ("vsrDenoiserForward", ctypes.c_int, [_P, _P, _P, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32, _P]),
+    ("vsrDenoiserGradients", ctypes.c_int, [_P, _P, _P, _P, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32,
+                                            ctypes.c_uint32, ctypes.POINTER(ctypes.c_float), ctypes.c_uint64,
+                                            ctypes.POINTER(ctypes.c_float)]),
+    ("vsrDenoiserTrainStep", ctypes.c_int, [_P, _P, _P, _P, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32,
+                                            ctypes.c_uint32, ctypes.c_float, ctypes.POINTER(ctypes.c_float)]),
+    ("vsrDenoiserFrameInput", ctypes.c_int, [_P, _P, _P]),
+    ("vsrDenoiseFrame", ctypes.c_int, [_P, _P, _P, ctypes.c_float, ctypes.c_float, _P, _P,
+                                       ctypes.POINTER(ctypes.c_uint32)]),
     ("vsrFrameReady", ctypes.c_int, [_P, _P, ctypes.c_int]),
     ("vsrDiscardFrame", ctypes.c_int, [_P, _P]),
     ("vsrMapFrame", _P, [_P, _P, ctypes.c_char_p, ctypes.POINTER(ctypes.c_uint32),
@@ -132,6 +146,79 @@ _ARRAY_TYPES = {
     (np.dtype(np.uint8), 1): UFIXED8,
     (np.dtype(np.uint16), 1): UFIXED16,
 }
+
+
+class Denoiser:
+    """The learned denoiser (vsrNewDenoiser). Image arguments are device
+    pointers (ints), e.g. torch's data_ptr(); inputs NHWC bf16 with 16
+    channels, outputs NHWC fp32 with 16 channels (log(1 + colour) in 0..2)."""
+
+    IN_C = 16
+    OUT_C = 16
+
+    def __init__(self, dev, seed=0):
+        self.dev = dev
+        self.lib = dev.lib
+        self.handle = self.lib.vsrNewDenoiser(dev.handle, seed)
+        if not self.handle:
+            raise RuntimeError("vsrNewDenoiser failed: " + "; ".join(m[2] for m in dev.messages))
+        self.count = int(self.lib.vsrDenoiserParameterCount(dev.handle, self.handle))
+
+    def close(self):
+        if self.handle:
+            self.lib.vsrReleaseDenoiser(self.dev.handle, self.handle)
+            self.handle = None
+
+    def params(self):
+        out = np.zeros(self.count, np.float32)
+        rc = self.lib.vsrDenoiserGetParameters(self.dev.handle, self.handle,
+                                               out.ctypes.data_as(ctypes.POINTER(ctypes.c_float)), self.count)
+        if rc:
+            raise RuntimeError(f"vsrDenoiserGetParameters failed ({rc})")
+        return out
+
+    def set_params(self, p):
+        p = np.ascontiguousarray(p, np.float32)
+        rc = self.lib.vsrDenoiserSetParameters(self.dev.handle, self.handle,
+                                               p.ctypes.data_as(ctypes.POINTER(ctypes.c_float)), self.count)
+        if rc:
+            raise RuntimeError(f"vsrDenoiserSetParameters failed ({rc})")
+
+    def forward(self, x_ptr, n, h, w, out_ptr):
+        rc = self.lib.vsrDenoiserForward(self.dev.handle, self.handle, x_ptr, n, h, w, out_ptr)
+        if rc:
+            raise RuntimeError(f"vsrDenoiserForward failed ({rc})")
+
+    def gradients(self, x_ptr, t_ptr, t_stride, n, h, w):
+        g = np.zeros(self.count, np.float32)
+        loss = ctypes.c_float(0)
+        rc = self.lib.vsrDenoiserGradients(self.dev.handle, self.handle, x_ptr, t_ptr, t_stride, n, h, w,
+                                           g.ctypes.data_as(ctypes.POINTER(ctypes.c_float)), self.count,
+                                           ctypes.byref(loss))
+        if rc:
+            raise RuntimeError(f"vsrDenoiserGradients failed ({rc})")
+        return g, loss.value
+
+    def train_step(self, x_ptr, t_ptr, t_stride, n, h, w, lr, want_loss=True):
+        loss = ctypes.c_float(0)
+        rc = self.lib.vsrDenoiserTrainStep(self.dev.handle, self.handle, x_ptr, t_ptr, t_stride, n, h, w,
+                                           lr, ctypes.byref(loss) if want_loss else None)
+        if rc:
+            raise RuntimeError(f"vsrDenoiserTrainStep failed ({rc})")
+        return loss.value if want_loss else None
+
+    def frame_input(self, frame, x_ptr):
+        rc = self.lib.vsrDenoiserFrameInput(self.dev.handle, frame.ptr, x_ptr)
+        if rc:
+            raise RuntimeError(f"vsrDenoiserFrameInput failed ({rc})")
+
+    def denoise_frame(self, frame, color_ptr, k=3.0, floor=0.0, retry_ptr=None):
+        n = ctypes.c_uint32(0)
+        rc = self.lib.vsrDenoiseFrame(self.dev.handle, self.handle, frame.ptr, k, floor, color_ptr,
+                                      retry_ptr, ctypes.byref(n))
+        if rc:
+            raise RuntimeError(f"vsrDenoiseFrame failed ({rc})")
+        return n.value
 
 
 class Device:

@@ -184,6 +184,54 @@ VSR_API VSRStatus vsrDiscardFrame(VSRDevice d, VSRFrame f);
    Completion: vsrFrameReady on any of the frames. */
 VSR_API VSRStatus vsrRenderFrames(VSRDevice d, const VSRFrame *frames, uint32_t count);
 
+/* Learned denoiser (no counterpart in the reference): a 4-level U-Net of
+   3x3 convolutions (32/64/128/256 channels, ~1.9M parameters), bf16
+   weights and activations with fp32 accumulation, trained and run by this
+   library's own kernels. Network images are N x H x W pixels, H and W
+   multiples of 8, NHWC: input 16 bf16 channels (log(1 + colour), albedo,
+   normal, depth / (1 + depth), six zeros), output 16 fp32 channels whose
+   first three are log(1 + colour). Pointers to images are device pointers;
+   work runs on the device's stream (vsrDeviceStream). */
+typedef struct VSRDenoiser_ *VSRDenoiser;
+VSR_API VSRDenoiser vsrNewDenoiser(VSRDevice d, uint64_t seed);
+VSR_API VSRStatus vsrReleaseDenoiser(VSRDevice d, VSRDenoiser n);
+VSR_API uint64_t vsrDenoiserParameterCount(VSRDevice d, VSRDenoiser n);
+/* Parameters in layer order (weights [cout][3][3][cin], then bias), as fp32
+   host arrays of vsrDenoiserParameterCount floats; setting them restarts
+   the optimiser. */
+VSR_API VSRStatus vsrDenoiserGetParameters(VSRDevice d, VSRDenoiser n, float *params,
+                                           uint64_t count);
+VSR_API VSRStatus vsrDenoiserSetParameters(VSRDevice d, VSRDenoiser n, const float *params,
+                                           uint64_t count);
+VSR_API VSRStatus vsrDenoiserForward(VSRDevice d, VSRDenoiser n, const void *input, uint32_t N,
+                                     uint32_t H, uint32_t W, float *output);
+/* L1 loss of log(1 + colour) against a linear target colour (targetStride
+   floats per pixel, first three used). vsrDenoiserGradients returns the
+   loss and the fp32 parameter gradients (host, `count` floats) without
+   changing the network; vsrDenoiserTrainStep applies one Adam step (beta
+   0.9 / 0.999, eps 1e-8) at the given learning rate. loss may be null. */
+VSR_API VSRStatus vsrDenoiserGradients(VSRDevice d, VSRDenoiser n, const void *input,
+                                       const float *target, uint32_t targetStride, uint32_t N,
+                                       uint32_t H, uint32_t W, float *grads, uint64_t count,
+                                       float *loss);
+VSR_API VSRStatus vsrDenoiserTrainStep(VSRDevice d, VSRDenoiser n, const void *input,
+                                       const float *target, uint32_t targetStride, uint32_t N,
+                                       uint32_t H, uint32_t W, float learningRate, float *loss);
+/* The network input of a frame (its accumulated colour, albedo, normal and
+   depth channels; absent channels read as zero), W8 x H8 pixels with W8, H8
+   the frame size rounded up to multiples of 8. */
+VSR_API VSRStatus vsrDenoiserFrameInput(VSRDevice d, VSRFrame f, void *input);
+/* Denoise a frame: the network on its accumulated image, then the variance
+   gate: a pixel keeps the denoised colour when |lum(denoised) - lum(mean)|
+   <= k * sqrt(variance of the mean) + floorAbs, else the accumulated mean,
+   and is marked for more samples (retry: one byte per pixel, device, may be
+   null). Without a variance channel on the frame every pixel takes the
+   denoised colour. colorOut: device float4 per pixel; numRetry: host, may be
+   null. */
+VSR_API VSRStatus vsrDenoiseFrame(VSRDevice d, VSRDenoiser n, VSRFrame f, float k,
+                                  float floorAbs, float *colorOut, uint8_t *retry,
+                                  uint32_t *numRetry);
+
 /* Work list of a batch, without a device (vsrPlanBatch has no counterpart in
    the reference): tiles of tileWidth x (32 / tileWidth) pixels for jobs of
    the given sizes, as (job, tile) uint32 pairs ordered by cost per pixel,

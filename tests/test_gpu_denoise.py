@@ -1,0 +1,120 @@
+"""The denoiser's GPU kernels (through the C ABI) against the CPU
+restatement: forward output, loss and every layer's parameter gradients on
+the same bf16 inputs and weights; one Adam step; and that training lowers
+the loss."""
+import numpy as np
+import pytest
+
+import denoise_oracle as D
+
+pytestmark = pytest.mark.gpu
+
+
+def make_case(seed, n=2, h=16, w=16):
+    rng = np.random.default_rng(seed)
+    x = rng.uniform(0, 1, (n, h, w, 16)).astype(np.float32)
+    x[..., 6:9] = rng.uniform(-1, 1, (n, h, w, 3))
+    x[..., 10:] = 0.0
+    x = D.bf16(x)
+    target = rng.uniform(0, 3, (n, h, w, 4)).astype(np.float32)
+    return x, target
+
+
+def to_device(x, target):
+    import torch
+    xd = torch.from_numpy(x).to(torch.bfloat16).cuda().contiguous()
+    td = torch.from_numpy(target).cuda().contiguous()
+    return xd, td
+
+
+def perturbed_params(seed, every):
+    """He-normal weights with a small offset on every `every`-th parameter
+    (biases included), the output layer's unused channels 3..15 kept zero."""
+    params = D.init_params(seed)
+    params[np.arange(len(params)) % every == 0] += 0.02
+    ws, bs = list(layer_slices())[-1]
+    w = params[ws].reshape(16, -1)
+    w[3:] = 0.0
+    params[bs][3:] = 0.0
+    return params
+
+
+def layer_slices():
+    off = 0
+    for cin, cout in D.LAYERS:
+        n = cout * 9 * cin
+        yield slice(off, off + n), slice(off + n, off + n + cout)
+        off += n + cout
+
+
+@pytest.fixture
+def net(pkg, device):
+    dn = pkg.vsr.Denoiser(device, seed=11)
+    yield dn
+    dn.close()
+
+
+def test_forward_matches_oracle(net):
+    import torch
+    params = perturbed_params(5, 11)
+    net.set_params(params)
+    x, target = make_case(6)
+    xd, _ = to_device(x, target)
+    out = torch.zeros((2, 16, 16, 16), dtype=torch.float32, device="cuda")
+    net.forward(xd.data_ptr(), 2, 16, 16, out.data_ptr())
+    torch.cuda.synchronize()
+    ref = D.forward(params, x)["out"]
+    got = out.cpu().numpy()
+    scale = np.abs(ref[..., :3]).max()
+    err = np.abs(got[..., :3] - ref[..., :3]).max()
+    print("forward max err", err, "scale", scale)
+    assert err <= 2e-2 * scale + 1e-3
+    assert np.abs(got[..., 3:]).max() == 0.0  # the unused output channels
+
+
+def test_gradients_match_oracle(net):
+    params = perturbed_params(7, 13)
+    net.set_params(params)
+    x, target = make_case(8)
+    xd, td = to_device(x, target)
+    g, loss = net.gradients(xd.data_ptr(), td.data_ptr(), 4, 2, 16, 16)
+    ref_loss, ref_g, _ = D.loss_and_grads(params, x, target)
+    print("loss", loss, ref_loss)
+    assert abs(loss - ref_loss) <= 1e-3 * ref_loss + 1e-5
+    for i, (ws, bs) in enumerate(layer_slices()):
+        for sl, what in ((ws, "weights"), (bs, "bias")):
+            a, b = g[sl], ref_g[sl]
+            if i == len(D.LAYERS) - 1:  # only the three colour outputs train
+                cout = D.LAYERS[i][1]
+                keep = np.zeros(cout, bool)
+                keep[:3] = True
+                mask = np.repeat(keep, a.size // cout)
+                assert np.abs(a[~mask]).max() == 0.0
+                a, b = a[mask], b[mask]
+            rel = np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-12)
+            print(f"layer {i} {what}: rel err {rel:.2e}")
+            assert rel < 3e-2, f"layer {i} {what}"
+
+
+def test_adam_step(net):
+    params = D.init_params(9)
+    net.set_params(params)
+    x, target = make_case(10)
+    xd, td = to_device(x, target)
+    g, _ = net.gradients(xd.data_ptr(), td.data_ptr(), 4, 2, 16, 16)
+    lr = 1e-3
+    net.train_step(xd.data_ptr(), td.data_ptr(), 4, 2, 16, 16, lr)
+    after = net.params()
+    # first step: m^ = g, v^ = g^2, so the update is lr * g / (|g| + eps)
+    expect = params - lr * g / (np.abs(g) + 1e-8)
+    assert np.abs(after - expect).max() <= 1e-6 + 1e-3 * lr
+
+
+def test_training_lowers_the_loss(net):
+    x, target = make_case(12, n=4, h=32, w=32)
+    xd, td = to_device(x, target)
+    first = net.train_step(xd.data_ptr(), td.data_ptr(), 4, 4, 32, 32, 1e-3)
+    for _ in range(150):
+        last = net.train_step(xd.data_ptr(), td.data_ptr(), 4, 4, 32, 32, 1e-3)
+    print("loss", first, "->", last)
+    assert last < 0.5 * first

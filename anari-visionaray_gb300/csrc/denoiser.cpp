@@ -150,7 +150,7 @@ cudaError_t Denoiser::ensure(int N, int H, int W, bool train) {
 }
 
 void Denoiser::conv(int li, const __nv_bfloat16 *x, int xC, __nv_bfloat16 *y, float *yf, int yC,
-                    int N, int H, int W, bool relu, cudaStream_t s) {
+                    int N, int H, int W, bool relu, cudaStream_t s, const __nv_bfloat16 *resid) {
   const DenoiseLayer &L = layers_[li];
   ConvArgs a{};
   a.x = x;
@@ -166,6 +166,9 @@ void Denoiser::conv(int li, const __nv_bfloat16 *x, int xC, __nv_bfloat16 *y, fl
   a.N = N;
   a.H = H;
   a.W = W;
+  a.resid = resid;
+  a.residC = kInC;
+  a.residN = kColorC;
   launchConv3x3(a, s);
 }
 
@@ -242,7 +245,8 @@ cudaError_t Denoiser::run(const __nv_bfloat16 *x, int N, int H, int W, float *ou
   launchCopyChannels(A.e0, 32, 0, A.cat0, 96, 64, 32, P0, 0, s);
   conv(L_D0A, A.cat0, 96, A.b0, nullptr, 32, N, H, W, true, s);
   conv(L_D0B, A.b0, 32, A.d0, nullptr, 32, N, H, W, true, s);
-  conv(L_OUT, A.d0, 32, nullptr, out, kOutC, N, H, W, false, s);
+  // the output is a correction of the input's log(1 + colour)
+  conv(L_OUT, A.d0, 32, nullptr, out, kOutC, N, H, W, false, s, x);
   return cudaGetLastError();
 }
 

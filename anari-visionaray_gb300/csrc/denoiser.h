@@ -4,7 +4,8 @@
 // bf16 weights and activations with fp32 accumulation, trained with L1 on
 // log(1 + colour) and Adam. Inputs: 16 channels per pixel (log(1 + colour),
 // albedo, normal, depth / (1 + depth), six zeros); output: log(1 + colour)
-// in the first 3 of 16 fp32 channels.
+// in the first 3 of 16 fp32 channels, as the input's log(1 + colour) plus
+// the last convolution (a residual).
 #pragma once
 
 #include <cuda_bf16.h>
@@ -53,7 +54,7 @@ class Denoiser {
   cudaError_t ensure(int N, int H, int W, bool train);
   cudaError_t run(const __nv_bfloat16 *x, int N, int H, int W, float *out, cudaStream_t s);
   void conv(int layer, const __nv_bfloat16 *x, int xC, __nv_bfloat16 *y, float *yf, int yC, int N,
-            int H, int W, bool relu, cudaStream_t s);
+            int H, int W, bool relu, cudaStream_t s, const __nv_bfloat16 *resid = nullptr);
   void convBack(int layer, const __nv_bfloat16 *x, int xC, const __nv_bfloat16 *dy,
                 __nv_bfloat16 *dx, const __nv_bfloat16 *mask, int N, int H, int W,
                 cudaStream_t s);

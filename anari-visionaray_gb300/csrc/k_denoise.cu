@@ -145,6 +145,11 @@ __global__ void __launch_bounds__(128) kConv3x3(ConvArgs a) {
           v0 = fmaxf(v0, 0.f);
           v1 = fmaxf(v1, 0.f);
         }
+        if (a.resid) {
+          const bf16 *r = a.resid + (size_t)pp * a.residC + c;
+          if (c < a.residN) v0 += __bfloat162float(r[0]);
+          if (c + 1 < a.residN) v1 += __bfloat162float(r[1]);
+        }
         if (a.mask) {
           const bf16 *m = a.mask + (size_t)pp * a.maskC + a.maskOff + c;
           if (c < a.Cout && !(__bfloat162float(m[0]) > 0.f)) v0 = 0.f;

@@ -80,6 +80,8 @@ struct ConvArgs {
   int maskC, maskOff;
   int relu;
   int N, H, W;
+  const __nv_bfloat16 *resid;  // added to output channels [0, residN), or null
+  int residC, residN;
 };
 struct WgradArgs {
   const __nv_bfloat16 *dy;  // output gradient (after the ReLU mask)

@@ -891,8 +891,12 @@ __device__ __forceinline__ uint32_t cvtU8(float f) {
   return (uint32_t)(255.f * fminf(fmaxf(f, 0.f), 1.f));
 }
 
+// lumSqMean: the mean over this frame's samples of the squared sample
+// luminance (0.3 r + 0.59 g + 0.11 b), for the optional variance channel;
+// negative when the caller does not track it.
 __device__ __forceinline__ void writeSample(const DFrame &F, int x, int y, bool stochastic,
-                                            float4 color, float depth, float3 Ng, float3 albedo) {
+                                            float4 color, float depth, float3 Ng, float3 albedo,
+                                            float lumSqMean = -1.f) {
   const size_t idx = (size_t)y * F.width + x;
   if (F.depth && !(depth > F.depth[idx])) {
     F.depth[idx] = depth;
@@ -913,6 +917,14 @@ __device__ __forceinline__ void writeSample(const DFrame &F, int x, int y, bool 
     color = make_float4((1 - a) * acc.x + a * color.x, (1 - a) * acc.y + a * color.y,
                         (1 - a) * acc.z + a * color.z, (1 - a) * acc.w + a * color.w);
     F.accum[idx] = color;
+    if (F.accumSq && lumSqMean >= 0.f) {
+      // variance of the mean luminance over all (accumID + 1) * spp samples
+      const float m2 = (1 - a) * F.accumSq[idx] + a * lumSqMean;
+      F.accumSq[idx] = m2;
+      const float lm = 0.3f * color.x + 0.59f * color.y + 0.11f * color.z;
+      const float n = (float)(F.accumID + 1) * (float)F.pixelSamples;
+      F.variance[idx] = n > 1.f ? fmaxf(m2 - lm * lm, 0.f) / (n - 1.f) : FLT_MAX;
+    }
   }
   if (F.colorType == COLOR_FLOAT4) {
     reinterpret_cast<float4 *>(F.color)[idx] = color;

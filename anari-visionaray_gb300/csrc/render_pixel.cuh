@@ -273,6 +273,7 @@ __device__ __forceinline__ void pathtracePixel(const DScene &S, const DCamera &C
   Rng rnd = rng;
   const float3 ambient = ld3(R.ambient);
   float4 accum = make_float4(0.f, 0.f, 0.f, 0.f);
+  float lumSq = 0.f;  // sum of squared sample luminances (variance channel)
   float cDepth = 1e31f;
   float3 cNg = f3(0.f), cAlb = f3(0.f);
   const int maxPasses = (R.maxBounce + 2) * (2 + R.ambientSamples) + 8;
@@ -458,6 +459,8 @@ __device__ __forceinline__ void pathtracePixel(const DScene &S, const DCamera &C
       if (firstHit) pc = make_float4(intensity.x, intensity.y, intensity.z, 1.f);
     }
     accum.x += pc.x; accum.y += pc.y; accum.z += pc.z; accum.w += pc.w;
+    const float lum = 0.3f * pc.x + 0.59f * pc.y + 0.11f * pc.z;
+    lumSq += lum * lum;
     if (pDepth < cDepth) {
       cDepth = pDepth;
       cNg = pNg;
@@ -466,7 +469,7 @@ __device__ __forceinline__ void pathtracePixel(const DScene &S, const DCamera &C
   }
   const float inv = 1.f / R.pixelSamples;
   writeSample(F, x, y, true, make_float4(accum.x * inv, accum.y * inv, accum.z * inv, accum.w * inv),
-              cDepth, cNg, cAlb);
+              cDepth, cNg, cAlb, lumSq * inv);
   if (err) atomicOr(F.errorFlags, err);
 }
 

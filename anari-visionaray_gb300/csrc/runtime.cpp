@@ -1040,7 +1040,7 @@ struct FrameObj : Object {
   World *world = nullptr;
   int width = 10, height = 10;
   VSRDataType colorType = VSR_UNKNOWN, depthType = VSR_UNKNOWN, normalType = VSR_UNKNOWN,
-              albedoType = VSR_UNKNOWN;
+              albedoType = VSR_UNKNOWN, varianceType = VSR_UNKNOWN;
   DevBuf color, depth, normal, albedo, accum, errFlags, marchItems, marchGroups, marchCounters,
       unitGroup, segOut;
   DevBuf variance, accumSq;                    // optional: variance of the mean (luminance)
@@ -1138,11 +1138,17 @@ struct FrameObj : Object {
     uint32_t sz[2] = {10, 10};
     if (const Param *p = find("size"))
       if (p->type == VSR_UINT32_VEC2 || p->type == VSR_INT32_VEC2) memcpy(sz, p->data.data(), 8);
-    colorType = depthType = normalType = albedoType = VSR_UNKNOWN;
+    colorType = depthType = normalType = albedoType = varianceType = VSR_UNKNOWN;
     getType("channel.color", colorType);
     getType("channel.depth", depthType);
     getType("channel.normal", normalType);
     getType("channel.albedo", albedoType);
+    // extension: variance of the accumulated mean's luminance (path tracer)
+    getType("channel.variance", varianceType);
+    if (varianceType != VSR_UNKNOWN && varianceType != VSR_FLOAT32) {
+      warn("unsupported 'channel.variance' type");
+      varianceType = VSR_UNKNOWN;
+    }
     int cs = 0;
     countStats = geti("collectStatistics", cs) && cs;
     if (!renderer) warn("missing required parameter 'renderer' on frame");
@@ -1165,6 +1171,17 @@ struct FrameObj : Object {
                 color.alloc(np * (colorType == VSR_FLOAT32_VEC4 ? 16 : 4)) == cudaSuccess &&
                 errFlags.alloc(sizeof(uint32_t)) == cudaSuccess &&
                 counters.alloc(24 * sizeof(unsigned long long)) == cudaSuccess;
+      if (varianceType == VSR_FLOAT32) {
+        ok = ok && variance.alloc(np * sizeof(float)) == cudaSuccess &&
+             accumSq.alloc(np * sizeof(float)) == cudaSuccess;
+        if (ok) {
+          cudaMemset(variance.p, 0, np * sizeof(float));
+          cudaMemset(accumSq.p, 0, np * sizeof(float));
+        }
+      } else {
+        variance.release();
+        accumSq.release();
+      }
       for (auto &kv : pinned) cudaFreeHost(kv.second);
       pinned.clear();
       if (!ok) {
@@ -1193,6 +1210,9 @@ struct FrameObj : Object {
     f.accum = accum.as<float4>();
     f.errorFlags = errFlags.as<uint32_t>();
     f.counters = countStats ? counters.as<unsigned long long>() : nullptr;
+    f.accumSq = accumSq.as<float>();
+    f.variance = variance.as<float>();
+    f.pixelSamples = renderer ? renderer->r.pixelSamples : 1;
     return f;
   }
 };
@@ -1611,6 +1631,10 @@ static bool channelBuf(FrameObj *F, const std::string &ch, void *&p, size_t &byt
     p = F->albedo.p;
     t = VSR_FLOAT32_VEC3;
     bytes = np * 12;
+  } else if (ch == "channel.variance" && F->varianceType == VSR_FLOAT32) {
+    p = F->variance.p;
+    t = VSR_FLOAT32;
+    bytes = np * 4;
   } else {
     return false;
   }

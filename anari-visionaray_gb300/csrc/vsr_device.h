@@ -188,6 +188,11 @@ struct DFrame {
   float4 *accum;
   uint32_t *errorFlags;
   unsigned long long *counters;  // optional statistics (null = off)
+  // optional (null = off): running mean over frames of the per-sample
+  // squared luminance, and the variance of the accumulated mean's luminance
+  float *accumSq;
+  float *variance;
+  int pixelSamples;  // samples per frame
 };
 
 // Wavefront path-tracer state: one slot per pixel, structure of arrays

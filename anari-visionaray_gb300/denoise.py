@@ -1,0 +1,206 @@
+"""Training data, training and evaluation of the learned denoiser.
+
+Everything that computes runs through the renderer core's C ABI: the path
+tracer renders the low/high-sample pairs, vsrDenoiserFrameInput builds the
+network inputs, vsrDenoiserTrainStep runs forward, backward and Adam, and
+vsrDenoiseFrame denoises and applies the variance gate. torch only holds
+device buffers (and cuts training crops out of them).
+
+Scenes come from the config-1/2 generators with per-scene seeds: a random
+UV-sphere set (32 x 16 segments), a value-noise volume in half of them,
+a random camera orbit and light direction. Inputs are 4 samples per
+pixel; references are accumulated high-sample renders of the same view.
+"""
+import math
+import time
+
+import numpy as np
+
+from . import scenes, vsr
+
+CHANNELS = ("color", "depth", "normal", "albedo")
+
+
+def training_scene(seed, res=256, spp=4, max_bounce=5):
+    """One random scene in the style of configs 1 and 2, seeded by `seed`."""
+    rng = np.random.default_rng(seed)
+    num = int(rng.integers(12, 64))
+    surfaces = scenes.sphere_set(rng, num, nu=32, nv=16)
+    volumes = []
+    if rng.uniform() < 0.5:
+        n = 64
+        data = scenes.value_noise(n, rng, octaves=4)
+        color, opacity = scenes.smoke_tf(alpha_max=float(rng.uniform(0.2, 0.6)))
+        spacing = 24.0 / (n - 1)
+        volumes.append({"data": data, "origin": [-12.0] * 3, "spacing": [spacing] * 3,
+                        "color": color, "opacity": opacity, "valueRange": [0.0, 1.0],
+                        "unitDistance": float(1.0 / rng.uniform(5.0, 40.0)),
+                        "majorantBrickSize": 16})
+    theta = rng.uniform(0, 2 * math.pi)
+    dist = rng.uniform(26.0, 40.0)
+    height = rng.uniform(2.0, 16.0)
+    eye = [dist * math.sin(theta), height, dist * math.cos(theta)]
+    ld = np.array([rng.uniform(-0.6, 0.6), -1.0, rng.uniform(-0.6, 0.6)])
+    ld /= np.linalg.norm(ld)
+    return {
+        "surfaces": surfaces, "volumes": volumes,
+        "lights": [{"direction": [float(x) for x in ld], "color": [1.0, 1.0, 1.0],
+                    "irradiance": float(rng.uniform(2.0, 4.0))}],
+        "camera": scenes._look_at_camera([0.0, -1.0, 0.0], eye, 45.0, 1.0),
+        "renderer": {"type": "pathtrace", "pixelSamples": spp, "maxBounce": max_bounce,
+                     "ambientRadiance": float(rng.uniform(0.1, 0.3)), "background": [0, 0, 0, 1]},
+        "frame": {"size": (res, res)},
+    }
+
+
+def _second_frame(dev, h, spp):
+    """A colour-only frame of the same world and camera with its own renderer."""
+    rend = dev.renderer("pathtrace")
+    scenes.apply_renderer(dev, rend, dict(h["scene"]["renderer"], pixelSamples=spp))
+    frame = dev.frame()
+    W, H = h["scene"]["frame"]["size"]
+    dev.set(frame, "size", (W, H), vsr.UINT32_VEC2)
+    dev.set(frame, "channel.color", vsr.FLOAT32_VEC4, vsr.DATA_TYPE)
+    dev.set(frame, "world", h["world"])
+    dev.set(frame, "camera", h["camera"])
+    dev.set(frame, "renderer", rend)
+    dev.commit(frame)
+    return rend, frame
+
+
+def render_reference(dev, h, spp_total, per_frame=256):
+    """The accumulated mean of spp_total samples per pixel, (H, W, 4) float32."""
+    rend, frame = _second_frame(dev, h, min(per_frame, spp_total))
+    for _ in range(max(1, spp_total // per_frame)):
+        dev.render(frame)
+    dev.wait(frame)
+    ref = dev.map(frame, "channel.color")
+    dev.release(frame)
+    dev.release(rend)
+    return ref
+
+
+def build(dev, scene, variance=True):
+    """The scene's objects with colour, depth, normal and albedo channels
+    (and the variance channel)."""
+    h = scenes.build(dev, scene, channels=CHANNELS)
+    if variance:
+        dev.set(h["frame"], "channel.variance", vsr.FLOAT32, vsr.DATA_TYPE)
+        dev.commit(h["frame"])
+    h["scene"] = scene
+    return h
+
+
+def release(dev, h):
+    for o in (h["frame"], h["renderer"], h["camera"], h["world"], *h["keep"]):
+        dev.release(o)
+
+
+def make_dataset(dev, seeds, res=256, ref_spp=1024, input_spp=4):
+    """Network inputs (N, res, res, 16) bf16 and reference colours (N, res,
+    res, 4) fp32 on the GPU, rendered by the path tracer."""
+    import torch
+
+    n = len(seeds)
+    x = torch.zeros((n, res, res, vsr.Denoiser.IN_C), dtype=torch.bfloat16, device="cuda")
+    t = torch.zeros((n, res, res, 4), dtype=torch.float32, device="cuda")
+    for i, seed in enumerate(seeds):
+        h = build(dev, training_scene(seed, res, input_spp), variance=False)
+        dev.render(h["frame"])
+        dev.wait(h["frame"])
+        torch.cuda.synchronize()
+        dev.denoise_input(h["frame"], x[i].data_ptr())
+        dev.wait(h["frame"])
+        t[i] = torch.from_numpy(render_reference(dev, h, ref_spp)).cuda()
+        release(dev, h)
+    torch.cuda.synchronize()
+    return x, t
+
+
+def train(dn, x, t, steps, batch=16, crop=128, lr=1e-3, seed=0, log_every=0):
+    """Adam with cosine decay of the learning rate on random crops; returns
+    the logged (step, loss) pairs and the wall time."""
+    import torch
+
+    g = torch.Generator(device="cpu")
+    g.manual_seed(seed)
+    n, H, W, _ = x.shape
+    losses = []
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for s in range(steps):
+        idx = torch.randint(0, n, (batch,), generator=g)
+        oy = torch.randint(0, (H - crop) // 8 + 1, (batch,), generator=g) * 8
+        ox = torch.randint(0, (W - crop) // 8 + 1, (batch,), generator=g) * 8
+        xb = torch.stack([x[int(i), int(a):int(a) + crop, int(b):int(b) + crop]
+                          for i, a, b in zip(idx, oy, ox)]).contiguous()
+        tb = torch.stack([t[int(i), int(a):int(a) + crop, int(b):int(b) + crop]
+                          for i, a, b in zip(idx, oy, ox)]).contiguous()
+        # torch made the crops on its own stream; the step runs on the device's
+        torch.cuda.synchronize()
+        rate = lr * 0.5 * (1.0 + math.cos(math.pi * s / steps))
+        want = bool(log_every) and (s % log_every == 0 or s == steps - 1)
+        loss = dn.train_step(xb.data_ptr(), tb.data_ptr(), 4, batch, crop, crop, rate,
+                             want_loss=True)
+        if want:
+            losses.append((s, loss))
+    return losses, time.perf_counter() - t0
+
+
+def rmse(a, b):
+    d = a[..., :3].astype(np.float64) - b[..., :3].astype(np.float64)
+    return float(np.sqrt(np.mean(d * d)))
+
+
+def evaluate(dev, dn, seeds, res=256, ref_spp=4096, spp_levels=(4, 8, 16, 32, 64, 128, 256),
+             denoise_levels=(4, 8, 16), k=3.0, floor=0.01):
+    """Pooled RMSE against ref_spp references of plain path tracing at
+    spp_levels, of the denoised image at denoise_levels, and of the
+    variance-gated image, with the share of pixels the gate sends back for
+    more samples."""
+    import torch
+
+    sq_plain = {s: 0.0 for s in spp_levels}
+    sq_dn = {s: 0.0 for s in denoise_levels}
+    sq_gate = {s: 0.0 for s in denoise_levels}
+    retry = {s: 0 for s in denoise_levels}
+    npx = 0
+    out = torch.zeros((res * res, 4), dtype=torch.float32, device="cuda")
+    for seed in seeds:
+        h = build(dev, training_scene(seed, res, 4), variance=True)
+        ref = render_reference(dev, h, ref_spp)
+        done = 0
+        for s in sorted(set(spp_levels) | set(denoise_levels)):
+            while done < s:
+                dev.render(h["frame"])
+                done += 4
+            dev.wait(h["frame"])
+            img = dev.map(h["frame"], "channel.color")
+            if s in sq_plain:
+                sq_plain[s] += rmse(img, ref) ** 2 * res * res
+            if s in sq_dn:
+                dn.denoise_frame(h["frame"], out.data_ptr(), k=1e30, floor=0.0)
+                sq_dn[s] += rmse(out.cpu().numpy().reshape(res, res, 4), ref) ** 2 * res * res
+                retry[s] += dn.denoise_frame(h["frame"], out.data_ptr(), k=k, floor=floor)
+                sq_gate[s] += rmse(out.cpu().numpy().reshape(res, res, 4), ref) ** 2 * res * res
+        npx += res * res
+        release(dev, h)
+    return ({s: math.sqrt(v / npx) for s, v in sq_plain.items()},
+            {s: math.sqrt(v / npx) for s, v in sq_dn.items()},
+            {s: math.sqrt(v / npx) for s, v in sq_gate.items()},
+            {s: v / npx for s, v in retry.items()})
+
+
+def time_to_rmse(plain, dn, pt_s_per_spp, dn_s, target_spp=256):
+    """Time for plain path tracing to reach its target_spp RMSE, and for
+    denoised path tracing (the fewest input samples whose denoised RMSE is
+    at most that) to reach it, from per-sample render time and denoiser
+    time. Returns (goal RMSE, plain seconds, input spp or None, denoised
+    seconds or None)."""
+    goal = plain[target_spp]
+    t_plain = target_spp * pt_s_per_spp
+    ok = [s for s in sorted(dn) if dn[s] <= goal]
+    if not ok:
+        return goal, t_plain, None, None
+    s = ok[0]
+    return goal, t_plain, s, s * pt_s_per_spp + dn_s

@@ -357,6 +357,13 @@ class Device:
     def render(self, frame):
         return self.lib.vsrRenderFrame(self.handle, frame.ptr)
 
+    def denoise_input(self, frame, x_ptr):
+        """The denoiser's input image of a frame (vsrDenoiserFrameInput) into
+        a device buffer of W8 x H8 x 16 bf16."""
+        rc = self.lib.vsrDenoiserFrameInput(self.handle, frame.ptr, x_ptr)
+        if rc:
+            raise RuntimeError(f"vsrDenoiserFrameInput failed ({rc})")
+
     def render_batch(self, frames):
         """Render several frames as one batch (vsrRenderFrames)."""
         arr = (_P * len(frames))(*[f.ptr for f in frames])

@@ -190,7 +190,7 @@ VSR_API VSRStatus vsrRenderFrames(VSRDevice d, const VSRFrame *frames, uint32_t 
    library's own kernels. Network images are N x H x W pixels, H and W
    multiples of 8, NHWC: input 16 bf16 channels (log(1 + colour), albedo,
    normal, depth / (1 + depth), six zeros), output 16 fp32 channels whose
-   first three are log(1 + colour). Pointers to images are device pointers;
+   first three are log(1 + colour): the input's plus a learned correction. Pointers to images are device pointers;
    work runs on the device's stream (vsrDeviceStream). */
 typedef struct VSRDenoiser_ *VSRDenoiser;
 VSR_API VSRDenoiser vsrNewDenoiser(VSRDevice d, uint64_t seed);

@@ -139,6 +139,7 @@ def forward(params, x):
     a["cat0"] = np.concatenate([upsample(a["d1"]), a["e0"]], -1)
     a["b0"] = c(12, a["cat0"]);  a["d0"] = c(13, a["b0"])
     a["out"] = c(14, a["d0"], act=False)
+    a["out"][..., :COLOR_C] += a["x"][..., :COLOR_C]  # residual on the input's log colour
     return a
 
 
@@ -221,6 +222,7 @@ def exact_loss(params, x, target):
     d1 = c(11, c(10, np.concatenate([up(d2), e1], -1)))
     d0 = c(13, c(12, np.concatenate([up(d1), e0], -1)))
     out = c(14, d0, act=False)
+    out[..., :COLOR_C] += h[..., :COLOR_C]
     t = np.log1p(np.maximum(target[..., :COLOR_C].astype(np.float64), 0.0))
     return float(np.abs(out[..., :COLOR_C] - t).mean())
 

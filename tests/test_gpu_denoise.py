@@ -70,6 +70,11 @@ def test_forward_matches_oracle(net):
     print("forward max err", err, "scale", scale)
     assert err <= 2e-2 * scale + 1e-3
     assert np.abs(got[..., 3:]).max() == 0.0  # the unused output channels
+    # with every weight zero the network returns its input's log colour
+    net.set_params(np.zeros_like(params))
+    net.forward(xd.data_ptr(), 2, 16, 16, out.data_ptr())
+    torch.cuda.synchronize()
+    assert np.array_equal(out.cpu().numpy()[..., :3], x[..., :3])
 
 
 def test_gradients_match_oracle(net):

@@ -453,6 +453,10 @@ __global__ void __launch_bounds__(256, VSR_WAVE_SHADE_MIN_BLOCKS) kWaveShade(
         // end of sample: accumulate, keep the closest G-buffer sample
         float4 pc = firstHitF ? make_float4(s.inten.x, s.inten.y, s.inten.z, 1.f)
                               : make_float4(R.bg[0], R.bg[1], R.bg[2], R.bg[3]);
+        if (!finiteSample(pc)) {
+          pc = make_float4(0.f, 0.f, 0.f, 0.f);
+          err |= ERR_NONFINITE;
+        }
         s.acc = make_float4(s.acc.x + pc.x, s.acc.y + pc.y, s.acc.z + pc.z, s.acc.w + pc.w);
         if (s.pDepth < s.cDepth) {
           s.cDepth = s.pDepth;

@@ -458,6 +458,10 @@ __device__ __forceinline__ void pathtracePixel(const DScene &S, const DCamera &C
       }
       if (firstHit) pc = make_float4(intensity.x, intensity.y, intensity.z, 1.f);
     }
+    if (!finiteSample(pc)) {
+      pc = make_float4(0.f, 0.f, 0.f, 0.f);
+      err |= ERR_NONFINITE;
+    }
     accum.x += pc.x; accum.y += pc.y; accum.z += pc.z; accum.w += pc.w;
     const float lum = 0.3f * pc.x + 0.59f * pc.y + 0.11f * pc.z;
     lumSq += lum * lum;

@@ -37,7 +37,17 @@ enum : uint32_t {
   ERR_PATH_LIMIT = 8u,       // path pass limit reached
   ERR_MARCH_LIMIT = 16u,     // ray-march step limit reached (dt too small for t)
   ERR_LAYER_LIMIT = 32u,     // transparent-surface loop limit reached
+  ERR_NONFINITE = 64u,       // a path sample was NaN or infinite and was dropped
 };
+
+#ifdef __CUDACC__
+// A path sample is dropped (counts as zero) when a component is NaN or
+// infinite, so that one degenerate sample (e.g. a half vector of opposite
+// directions) does not poison a pixel's running mean forever.
+__device__ __forceinline__ bool finiteSample(const float4 &c) {
+  return isfinite(c.x) && isfinite(c.y) && isfinite(c.z) && isfinite(c.w);
+}
+#endif
 
 constexpr int kMaxMarchSteps = 1 << 20;
 constexpr int kMaxSurfaceLayers = 1 << 12;

@@ -8,8 +8,9 @@ device buffers (and cuts training crops out of them).
 
 Scenes come from the config-1/2 generators with per-scene seeds: a random
 UV-sphere set (32 x 16 segments), a value-noise volume in half of them,
-a random camera orbit and light direction. Inputs are 4 samples per
-pixel; references are accumulated high-sample renders of the same view.
+a random camera orbit and light direction. Inputs are the accumulated
+images after a few samples per pixel (4 to 32); references are
+accumulated high-sample renders of the same view.
 """
 import math
 import time
@@ -96,22 +97,33 @@ def release(dev, h):
         dev.release(o)
 
 
-def make_dataset(dev, seeds, res=256, ref_spp=1024, input_spp=4):
-    """Network inputs (N, res, res, 16) bf16 and reference colours (N, res,
-    res, 4) fp32 on the GPU, rendered by the path tracer."""
+def make_dataset(dev, seeds, res=256, ref_spp=1024, input_spp=(4,)):
+    """Network inputs (N * L, res, res, 16) bf16 and their reference colours
+    (N * L, res, res, 4) fp32 on the GPU, rendered by the path tracer: for
+    each scene, the inputs after each of the L sample counts input_spp
+    (ascending, multiples of 4) of one accumulating frame, all with the
+    same reference."""
     import torch
 
-    n = len(seeds)
+    levels = sorted(input_spp)
+    n = len(seeds) * len(levels)
     x = torch.zeros((n, res, res, vsr.Denoiser.IN_C), dtype=torch.bfloat16, device="cuda")
     t = torch.zeros((n, res, res, 4), dtype=torch.float32, device="cuda")
-    for i, seed in enumerate(seeds):
-        h = build(dev, training_scene(seed, res, input_spp), variance=False)
-        dev.render(h["frame"])
-        dev.wait(h["frame"])
-        torch.cuda.synchronize()
-        dev.denoise_input(h["frame"], x[i].data_ptr())
-        dev.wait(h["frame"])
-        t[i] = torch.from_numpy(render_reference(dev, h, ref_spp)).cuda()
+    i = 0
+    for seed in seeds:
+        h = build(dev, training_scene(seed, res, 4), variance=False)
+        ref = torch.from_numpy(render_reference(dev, h, ref_spp)).cuda()
+        done = 0
+        for s in levels:
+            while done < s:
+                dev.render(h["frame"])
+                done += 4
+            dev.wait(h["frame"])
+            torch.cuda.synchronize()
+            dev.denoise_input(h["frame"], x[i].data_ptr())
+            dev.wait(h["frame"])
+            t[i] = ref
+            i += 1
         release(dev, h)
     torch.cuda.synchronize()
     return x, t

@@ -55,6 +55,8 @@ def parse():
     p.add_argument("--volume-res", type=int, nargs=2, default=[1920, 1080],
                    help="config-2 frame size (full size by default; smaller for profiling)")
     p.add_argument("--volume-spp", type=int, default=256)
+    p.add_argument("--no-denoise", dest="denoise", action="store_false",
+                   help="skip the config-4 denoiser training and evaluation")
     p.add_argument("--no-batch", dest="batch", action="store_false",
                    help="skip the config-3 batched-rendering measurement")
     return p.parse_args()
@@ -126,6 +128,16 @@ def measured_peaks():
             d = json.load(f)
         return d.get("hbm_gbs", 6800.0), "measured"
     return 6800.0, "fallback"
+
+
+def measured_peaks_tensor():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            d = json.load(f)
+        if "bf16_tflops" in d:
+            return d["bf16_tflops"], "measured"
+    return 1900.0, "fallback"
 
 
 def profiled_traffic(name="pathtrace_config1.txt"):
@@ -267,6 +279,78 @@ def measure_batch_config3(pkg, dev, steps=3, num_scenes=64):
             "tile": f"{tile_w}x{32 // max(tile_w, 1)}", "fetch": fetch, "tuning_batches": tune,
             "error_flags": err, "generate_s": gen_s,
             "timing": "host wall clock, first call to last frame done; synthetic seeded scenes"}
+
+
+def measure_denoiser_config4(pkg, dev, train_scenes=48, eval_scenes=8, steps=2000,
+                             train_ref_spp=1024, eval_ref_spp=4096, res=256):
+    """Config 4 (learned denoiser): train the U-Net on path-traced pairs
+    (inputs after 4, 8, 16 and 32 spp, 1024-spp references, 256^2 images,
+    128^2 crops, batch 16, L1 on log colour, Adam with cosine decay), then
+    on held-out scenes compare plain path tracing (4..256 spp) and denoised
+    path tracing against 4096-spp references, and turn the RMSEs into the
+    time to reach the plain 256-spp RMSE at 1920x1080 from the measured
+    per-sample render time and denoiser time there."""
+    import torch
+
+    D = importlib.import_module(pkg.__name__ + ".denoise")
+    t0 = time.perf_counter()
+    x, t = D.make_dataset(dev, list(range(1, 1 + train_scenes)), res=res, ref_spp=train_ref_spp,
+                          input_spp=(4, 8, 16, 32))
+    data_s = time.perf_counter() - t0
+    dn = pkg.vsr.Denoiser(dev, seed=1)
+    losses, train_s = D.train(dn, x, t, steps, log_every=max(1, steps // 4))
+    del x, t
+    levels = (4, 8, 16, 32, 64)
+    plain, den, gate, retry = D.evaluate(dev, dn, list(range(10001, 10001 + eval_scenes)), res=res,
+                                         ref_spp=eval_ref_spp, denoise_levels=levels)
+    # 1920x1080: path-tracing time per sample per pixel, and the denoiser
+    sc = D.training_scene(10001, res=1920, spp=16)
+    sc["frame"]["size"] = (1920, 1080)
+    sc["camera"]["aspect"] = 1920 / 1080
+    h = D.build(dev, sc, variance=True)
+    for _ in range(2):
+        dev.render(h["frame"])
+        dev.wait(h["frame"])
+    pt = []
+    for _ in range(3):
+        dev.render(h["frame"])
+        dev.wait(h["frame"])
+        pt.append(dev.get_float(h["frame"], "duration.render"))
+    pt_s_per_spp = statistics.median(pt) / 16
+    out = torch.zeros((1920 * 1080, 4), dtype=torch.float32, device="cuda")
+    for _ in range(3):
+        dn.denoise_frame(h["frame"], out.data_ptr())
+    ds = []
+    for _ in range(10):
+        tt = time.perf_counter()
+        dn.denoise_frame(h["frame"], out.data_ptr())  # synchronous: returns the retry count
+        ds.append(time.perf_counter() - tt)
+    dn_s = statistics.median(ds)
+    D.release(dev, h)
+    dn.close()
+    goal, t_plain, s_dn, t_dn = D.time_to_rmse(plain, den, pt_s_per_spp, dn_s)
+    layers = [(16, 32, 0), (32, 32, 0), (32, 64, 1), (64, 64, 1), (64, 128, 2), (128, 128, 2),
+              (128, 256, 3), (256, 256, 3), (384, 128, 2), (128, 128, 2), (192, 64, 1), (64, 64, 1),
+              (96, 32, 0), (32, 32, 0), (32, 16, 0)]
+    flops = sum(2.0 * ci * co * 9 * 1920 * 1080 / 4 ** lvl for ci, co, lvl in layers)
+    peak = measured_peaks_tensor()
+    return {
+        "workload": f"config4 denoiser: {train_scenes} training scenes x 4 input spp levels "
+                    f"({res}^2, {train_ref_spp}-spp references), {steps} Adam steps of 16 "
+                    f"128^2 crops; {eval_scenes} held-out scenes vs {eval_ref_spp}-spp references",
+        "rmse_plain": plain, "rmse_denoised": den, "rmse_gated": gate, "gate_retry_share": retry,
+        "goal_rmse_plain256": goal, "plain256_s_1080p": t_plain,
+        "denoised_input_spp": s_dn, "denoised_s_1080p": t_dn,
+        "speedup_to_equal_rmse": (t_plain / t_dn) if t_dn else None,
+        "pt_ms_per_spp_1080p": 1e3 * pt_s_per_spp, "denoise_ms_1080p": 1e3 * dn_s,
+        "train_s": train_s, "train_ms_per_step": 1e3 * train_s / steps, "data_s": data_s,
+        "loss": losses,
+        "roofline": {"bound": "tensor", "achieved": flops / dn_s / 1e12, "peak": peak[0],
+                     "unit": "TFLOP/s", "frac": flops / dn_s / 1e12 / peak[0],
+                     "note": f"denoiser forward at 1920x1080 ({flops / 1e12:.3f} TFLOP incl. "
+                             f"input and gate kernels in the time); peak bf16 {peak[1]}; "
+                             "mma.sync m16n8k16 bf16 implicit GEMM"},
+    }
 
 
 def measure_volume_config2(pkg, dev, flush, count_spp=8, res=(1920, 1080), spp=256):
@@ -433,6 +517,7 @@ def run_ours(args):
 
     raycast = measure_raycast_config0(pkg, dev, flush) if args.raycast else None
     batch = measure_batch_config3(pkg, dev) if args.batch else None
+    denoiser = measure_denoiser_config4(pkg, dev) if args.denoise else None
     volume = (measure_volume_config2(pkg, dev, flush, res=args.volume_res, spp=args.volume_spp)
               if args.volume else None)
 
@@ -472,6 +557,7 @@ def run_ours(args):
                       "grays_per_s": rays / kernel_s / 1e9},
         "commit_s": commit_s, "bvh_build_s": bvh_s, "raycast_config0": raycast,
         "volume_pathtracer_config2": volume, "batch_config3": batch,
+        "denoiser_config4": denoiser,
         "wall_s_timed": wall, "clocks": clk, "error_flags": err,
         "wavefront_iterations": iterations,
     }

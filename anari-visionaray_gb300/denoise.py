@@ -159,25 +159,38 @@ def train(dn, x, t, steps, batch=16, crop=128, lr=1e-3, seed=0, log_every=0):
     return losses, time.perf_counter() - t0
 
 
-def rmse(a, b):
-    d = a[..., :3].astype(np.float64) - b[..., :3].astype(np.float64)
-    return float(np.sqrt(np.mean(d * d)))
+def sq_errors(a, b):
+    """Sums of squared errors of the colour channels: linear, and after the
+    Reinhard tone map c / (1 + c), which bounds the rare very bright
+    samples ("fireflies") that otherwise dominate a linear RMSE."""
+    x, y = a[..., :3].astype(np.float64), b[..., :3].astype(np.float64)
+    d = x - y
+    tm = np.clip(x, 0, None) / (1 + np.clip(x, 0, None)) - np.clip(y, 0, None) / (1 + np.clip(y, 0, None))
+    return float(np.sum(d * d)), float(np.sum(tm * tm))
 
 
 def evaluate(dev, dn, seeds, res=256, ref_spp=4096, spp_levels=(4, 8, 16, 32, 64, 128, 256),
              denoise_levels=(4, 8, 16), k=3.0, floor=0.01):
-    """Pooled RMSE against ref_spp references of plain path tracing at
+    """Pooled errors against ref_spp references of plain path tracing at
     spp_levels, of the denoised image at denoise_levels, and of the
     variance-gated image, with the share of pixels the gate sends back for
-    more samples."""
+    more samples. Returns {"plain" | "denoised" | "gated": {"rmse": {spp:
+    linear RMSE}, "rmse_tm": {spp: tone-mapped RMSE}, "psnr_tm": {spp: dB}},
+    "retry": {spp: share}}."""
     import torch
 
-    sq_plain = {s: 0.0 for s in spp_levels}
-    sq_dn = {s: 0.0 for s in denoise_levels}
-    sq_gate = {s: 0.0 for s in denoise_levels}
+    kinds = ("plain", "denoised", "gated")
+    sums = {kd: {} for kd in kinds}
     retry = {s: 0 for s in denoise_levels}
     npx = 0
     out = torch.zeros((res * res, 4), dtype=torch.float32, device="cuda")
+
+    def add(kind, s, img, ref):
+        lin, tm = sq_errors(img, ref)
+        a = sums[kind].setdefault(s, [0.0, 0.0])
+        a[0] += lin
+        a[1] += tm
+
     for seed in seeds:
         h = build(dev, training_scene(seed, res, 4), variance=True)
         ref = render_reference(dev, h, ref_spp)
@@ -187,28 +200,34 @@ def evaluate(dev, dn, seeds, res=256, ref_spp=4096, spp_levels=(4, 8, 16, 32, 64
                 dev.render(h["frame"])
                 done += 4
             dev.wait(h["frame"])
-            img = dev.map(h["frame"], "channel.color")
-            if s in sq_plain:
-                sq_plain[s] += rmse(img, ref) ** 2 * res * res
-            if s in sq_dn:
+            if s in spp_levels:
+                add("plain", s, dev.map(h["frame"], "channel.color"), ref)
+            if s in denoise_levels:
                 dn.denoise_frame(h["frame"], out.data_ptr(), k=1e30, floor=0.0)
-                sq_dn[s] += rmse(out.cpu().numpy().reshape(res, res, 4), ref) ** 2 * res * res
+                add("denoised", s, out.cpu().numpy().reshape(res, res, 4), ref)
                 retry[s] += dn.denoise_frame(h["frame"], out.data_ptr(), k=k, floor=floor)
-                sq_gate[s] += rmse(out.cpu().numpy().reshape(res, res, 4), ref) ** 2 * res * res
+                add("gated", s, out.cpu().numpy().reshape(res, res, 4), ref)
         npx += res * res
         release(dev, h)
-    return ({s: math.sqrt(v / npx) for s, v in sq_plain.items()},
-            {s: math.sqrt(v / npx) for s, v in sq_dn.items()},
-            {s: math.sqrt(v / npx) for s, v in sq_gate.items()},
-            {s: v / npx for s, v in retry.items()})
+    n = 3.0 * npx
+    res_ = {}
+    for kd in kinds:
+        rm = {s: math.sqrt(v[0] / n) for s, v in sorted(sums[kd].items())}
+        rt = {s: math.sqrt(v[1] / n) for s, v in sorted(sums[kd].items())}
+        res_[kd] = {"rmse": rm, "rmse_tm": rt,
+                    "psnr_tm": {s: (20 * math.log10(1.0 / v) if v > 0 else float("inf"))
+                                for s, v in rt.items()}}
+    res_["retry"] = {s: v / npx for s, v in retry.items()}
+    return res_
 
 
 def time_to_rmse(plain, dn, pt_s_per_spp, dn_s, target_spp=256):
-    """Time for plain path tracing to reach its target_spp RMSE, and for
-    denoised path tracing (the fewest input samples whose denoised RMSE is
+    """Time for plain path tracing to reach its target_spp error, and for
+    denoised path tracing (the fewest input samples whose denoised error is
     at most that) to reach it, from per-sample render time and denoiser
-    time. Returns (goal RMSE, plain seconds, input spp or None, denoised
-    seconds or None)."""
+    time; plain and dn map spp to an error (e.g. tone-mapped RMSE). Returns
+    (goal error, plain seconds, input spp or None, denoised seconds or
+    None)."""
     goal = plain[target_spp]
     t_plain = target_spp * pt_s_per_spp
     ok = [s for s in sorted(dn) if dn[s] <= goal]

@@ -57,6 +57,9 @@ def parse():
     p.add_argument("--volume-spp", type=int, default=256)
     p.add_argument("--no-denoise", dest="denoise", action="store_false",
                    help="skip the config-4 denoiser training and evaluation")
+    p.add_argument("--denoise-train-scenes", type=int, default=48)
+    p.add_argument("--denoise-eval-scenes", type=int, default=8)
+    p.add_argument("--denoise-steps", type=int, default=2000)
     p.add_argument("--no-batch", dest="batch", action="store_false",
                    help="skip the config-3 batched-rendering measurement")
     return p.parse_args()
@@ -301,8 +304,8 @@ def measure_denoiser_config4(pkg, dev, train_scenes=48, eval_scenes=8, steps=200
     losses, train_s = D.train(dn, x, t, steps, log_every=max(1, steps // 4))
     del x, t
     levels = (4, 8, 16, 32, 64)
-    plain, den, gate, retry = D.evaluate(dev, dn, list(range(10001, 10001 + eval_scenes)), res=res,
-                                         ref_spp=eval_ref_spp, denoise_levels=levels)
+    ev = D.evaluate(dev, dn, list(range(10001, 10001 + eval_scenes)), res=res,
+                    ref_spp=eval_ref_spp, denoise_levels=levels)
     # 1920x1080: path-tracing time per sample per pixel, and the denoiser
     sc = D.training_scene(10001, res=1920, spp=16)
     sc["frame"]["size"] = (1920, 1080)
@@ -328,7 +331,8 @@ def measure_denoiser_config4(pkg, dev, train_scenes=48, eval_scenes=8, steps=200
     dn_s = statistics.median(ds)
     D.release(dev, h)
     dn.close()
-    goal, t_plain, s_dn, t_dn = D.time_to_rmse(plain, den, pt_s_per_spp, dn_s)
+    goal, t_plain, s_dn, t_dn = D.time_to_rmse(ev["plain"]["rmse_tm"], ev["denoised"]["rmse_tm"],
+                                               pt_s_per_spp, dn_s)
     layers = [(16, 32, 0), (32, 32, 0), (32, 64, 1), (64, 64, 1), (64, 128, 2), (128, 128, 2),
               (128, 256, 3), (256, 256, 3), (384, 128, 2), (128, 128, 2), (192, 64, 1), (64, 64, 1),
               (96, 32, 0), (32, 32, 0), (32, 16, 0)]
@@ -338,8 +342,11 @@ def measure_denoiser_config4(pkg, dev, train_scenes=48, eval_scenes=8, steps=200
         "workload": f"config4 denoiser: {train_scenes} training scenes x 4 input spp levels "
                     f"({res}^2, {train_ref_spp}-spp references), {steps} Adam steps of 16 "
                     f"128^2 crops; {eval_scenes} held-out scenes vs {eval_ref_spp}-spp references",
-        "rmse_plain": plain, "rmse_denoised": den, "rmse_gated": gate, "gate_retry_share": retry,
-        "goal_rmse_plain256": goal, "plain256_s_1080p": t_plain,
+        "plain": ev["plain"], "denoised": ev["denoised"], "gated": ev["gated"],
+        "gate_retry_share": ev["retry"],
+        "error_measure": "RMSE of Reinhard tone-mapped colour c/(1+c) against the reference "
+                         "(linear RMSE reported too; it is dominated by rare very bright samples)",
+        "goal_rmse_tm_plain256": goal, "plain256_s_1080p": t_plain,
         "denoised_input_spp": s_dn, "denoised_s_1080p": t_dn,
         "speedup_to_equal_rmse": (t_plain / t_dn) if t_dn else None,
         "pt_ms_per_spp_1080p": 1e3 * pt_s_per_spp, "denoise_ms_1080p": 1e3 * dn_s,
@@ -517,7 +524,9 @@ def run_ours(args):
 
     raycast = measure_raycast_config0(pkg, dev, flush) if args.raycast else None
     batch = measure_batch_config3(pkg, dev) if args.batch else None
-    denoiser = measure_denoiser_config4(pkg, dev) if args.denoise else None
+    denoiser = (measure_denoiser_config4(pkg, dev, train_scenes=args.denoise_train_scenes,
+                                         eval_scenes=args.denoise_eval_scenes,
+                                         steps=args.denoise_steps) if args.denoise else None)
     volume = (measure_volume_config2(pkg, dev, flush, res=args.volume_res, spp=args.volume_spp)
               if args.volume else None)
 

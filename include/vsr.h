@@ -160,8 +160,13 @@ VSR_API VSRStatus vsrRetain(VSRDevice d, VSRObject o);
    "duration" (FLOAT32, seconds of GPU time of the last render),
    "duration.render" (FLOAT32, render kernel only), "numSamples" (INT32),
    "commitDuration" (FLOAT32, seconds of the last scene update incl. BVH
-   build), "errorFlags" (UINT32, device-side error bits of the last render);
-   world "bvh.nodes" / "bvh.triangles" (UINT64). Returns 1 if found. */
+   build), "errorFlags" (UINT32, device-side error bits of the last render:
+   1 traversal stack full, 2 DDA step limit, 4 delta-tracking step limit,
+   8 path pass limit, 16 ray-march step limit, 32 transparent-layer limit,
+   64 a NaN or infinite path sample was dropped); world "bvh.nodes" /
+   "bvh.triangles" (UINT64). Frame channel "channel.variance" (FLOAT32, an
+   extension) holds the path tracer's variance of each pixel's accumulated
+   mean luminance. Returns 1 if found. */
 VSR_API int vsrGetProperty(VSRDevice d, VSRObject o, const char *name, VSRDataType type,
                            void *mem, uint64_t size, VSRWaitMask mask);
 

@@ -137,11 +137,12 @@ def test_trained_network_beats_the_noisy_input(pkg, device):
     dn = pkg.vsr.Denoiser(device, seed=3)
     try:
         losses, _ = D.train(dn, x, t, 300, batch=8, crop=64, log_every=100)
-        plain, den, gate, retry = D.evaluate(device, dn, [20001, 20002], res=128, ref_spp=1024,
-                                             spp_levels=(4, 16), denoise_levels=(4,))
-        print("loss", losses, "plain", plain, "denoised", den, "gated", gate, "retry", retry)
+        ev = D.evaluate(device, dn, [20001, 20002], res=128, ref_spp=1024,
+                        spp_levels=(4, 16), denoise_levels=(4,))
+        print("loss", losses, ev)
+        plain, den, gate = (ev[k]["rmse_tm"] for k in ("plain", "denoised", "gated"))
         assert losses[-1][1] < losses[0][1]
         assert den[4] < 0.7 * plain[4]
-        assert 0.0 <= retry[4] <= 1.0 and gate[4] <= plain[4]
+        assert 0.0 <= ev["retry"][4] <= 1.0 and gate[4] <= plain[4]
     finally:
         dn.close()

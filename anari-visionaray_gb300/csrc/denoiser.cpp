@@ -66,14 +66,16 @@ Denoiser::Denoiser(uint64_t seed) {
         alloc(v_, off) == cudaSuccess && alloc(grad_, off) == cudaSuccess &&
         alloc(wbf_, off) == cudaSuccess && alloc(wt_, offT) == cudaSuccess;
   if (!ok_) return;
-  // He-normal weights (std sqrt(2 / fan_in)), zero biases; the output
-  // layer's unused channels 3..15 stay zero
+  // He-normal weights (std sqrt(2 / fan_in)), zero biases. The output layer
+  // starts at zero: the network begins as the identity on the input's
+  // colour and grows its correction from there (a random correction at the
+  // start drives the first steps to switch the ReLUs off instead).
   std::vector<float> h(off, 0.f);
   Normal rng{seed};
   for (size_t li = 0; li < layers_.size(); ++li) {
     const DenoiseLayer &L = layers_[li];
     const double sd = std::sqrt(2.0 / (9.0 * L.cin));
-    const int used = li + 1 == layers_.size() ? kColorC : L.cout;
+    const int used = li + 1 == layers_.size() ? 0 : L.cout;
     for (int co = 0; co < used; ++co)
       for (int k = 0; k < 9 * L.cin; ++k) h[L.w + (size_t)co * 9 * L.cin + k] = (float)(sd * rng());
   }

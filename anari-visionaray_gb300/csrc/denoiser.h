@@ -3,7 +3,8 @@
 // nearest 2x upsampling, skip connections by channel concatenation, ReLU),
 // bf16 weights and activations with fp32 accumulation, trained with L1 on
 // log(1 + colour) and Adam. Inputs: 16 channels per pixel (log(1 + colour),
-// albedo, normal, depth / (1 + depth), six zeros); output: log(1 + colour)
+// albedo, normal, depth / (1 + depth), log(1 + standard error of the mean
+// luminance), 1 / sqrt(samples), four zeros); output: log(1 + colour)
 // in the first 3 of 16 fp32 channels, as the input's log(1 + colour) plus
 // the last convolution (a residual).
 #pragma once

@@ -57,19 +57,22 @@ __device__ __forceinline__ void mma16816(float (&d)[4], const uint32_t (&a)[4], 
 }
 
 // ------------------------------------------------------ convolution (GEMM)
-// CTA tile: 64 pixels x 64 output channels, k-step 16 (one tap, 16 input
-// channels); 4 warps as 2 x 2, each 32 x 32 (2 x 4 mma tiles). Two stages.
-constexpr int kBM = 64, kBN = 64, kBK = 16;
+// CTA tile: 64 pixels x BN output channels (64, or 32 for layers of at most
+// 32), k-step 16 (one tap, 16 input channels); 4 warps as 2 x 2, each 32 x
+// BN/2 (2 x BN/16 mma tiles). Two stages.
+constexpr int kBM = 64, kBK = 16;
 constexpr int kRowA = kBK + 8;  // padded smem row (48 B): conflict-free ldmatrix
 
+template <int BN>
 __global__ void __launch_bounds__(128) kConv3x3(ConvArgs a) {
+  constexpr int NT = BN / 16;  // n8 tiles per warp
   __shared__ __align__(128) bf16 As[2][kBM][kRowA];
-  __shared__ __align__(128) bf16 Bs[2][kBN][kRowA];
+  __shared__ __align__(128) bf16 Bs[2][BN][kRowA];
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int wm = warp >> 1, wn = warp & 1;
   const int P = a.N * a.H * a.W;
   const int pBase = blockIdx.x * kBM;
-  const int nBase = blockIdx.y * kBN;
+  const int nBase = blockIdx.y * BN;
   const int kChunks = a.Cin / kBK;  // per tap
   const int steps = 9 * kChunks;
   // this thread's loads: one 16-byte half-row of A and one of B
@@ -91,15 +94,17 @@ __global__ void __launch_bounds__(128) kConv3x3(ConvArgs a) {
     const bool ok = pIn && yy >= 0 && yy < a.H && xx >= 0 && xx < a.W;
     const bf16 *src = a.x + (ok ? (((size_t)pn * a.H + yy) * a.W + xx) * a.xC + a.xOff + c0 : 0);
     cpAsync16(&As[stage][lr][lh * 8], src, ok);
-    const bool wok = co < a.Cout;
-    const bf16 *wsrc = a.w + (wok ? ((size_t)co * 9 + tap) * a.Cin + c0 : 0);
-    cpAsync16(&Bs[stage][lr][lh * 8], wsrc, wok);
+    if (lr < BN) {
+      const bool wok = co < a.Cout;
+      const bf16 *wsrc = a.w + (wok ? ((size_t)co * 9 + tap) * a.Cin + c0 : 0);
+      cpAsync16(&Bs[stage][lr][lh * 8], wsrc, wok);
+    }
   };
-  float acc[2][4][4];
+  float acc[2][NT][4];
 #pragma unroll
   for (int i = 0; i < 2; ++i)
 #pragma unroll
-    for (int j = 0; j < 4; ++j)
+    for (int j = 0; j < NT; ++j)
 #pragma unroll
       for (int k = 0; k < 4; ++k) acc[i][j][k] = 0.f;
   load(0, 0);
@@ -110,18 +115,18 @@ __global__ void __launch_bounds__(128) kConv3x3(ConvArgs a) {
     cpAsyncCommit();
     cpAsyncWait<1>();
     __syncthreads();
-    uint32_t af[2][4], bfr[2][4];
+    uint32_t af[2][4], bfr[NT / 2][4];
 #pragma unroll
     for (int mt = 0; mt < 2; ++mt)
       ldsm4(af[mt], &As[cur][wm * 32 + mt * 16 + (lane & 15)][(lane >> 4) * 8]);
 #pragma unroll
-    for (int np = 0; np < 2; ++np)
-      ldsm4(bfr[np],
-            &Bs[cur][wn * 32 + np * 16 + (lane & 7) + (lane >> 4) * 8][((lane >> 3) & 1) * 8]);
+    for (int np = 0; np < NT / 2; ++np)
+      ldsm4(bfr[np], &Bs[cur][wn * (BN / 2) + np * 16 + (lane & 7) + (lane >> 4) * 8]
+                        [((lane >> 3) & 1) * 8]);
 #pragma unroll
     for (int mt = 0; mt < 2; ++mt)
 #pragma unroll
-      for (int nt = 0; nt < 4; ++nt)
+      for (int nt = 0; nt < NT; ++nt)
         mma16816(acc[mt][nt], af[mt], bfr[nt >> 1][(nt & 1) * 2], bfr[nt >> 1][(nt & 1) * 2 + 1]);
     __syncthreads();
   }
@@ -134,8 +139,8 @@ __global__ void __launch_bounds__(128) kConv3x3(ConvArgs a) {
       const int pp = pBase + wm * 32 + mt * 16 + g + half * 8;
       if (pp >= P) continue;
 #pragma unroll
-      for (int nt = 0; nt < 4; ++nt) {
-        const int c = nBase + wn * 32 + nt * 8 + t4 * 2;
+      for (int nt = 0; nt < NT; ++nt) {
+        const int c = nBase + wn * (BN / 2) + nt * 8 + t4 * 2;
         float v0 = acc[mt][nt][half * 2], v1 = acc[mt][nt][half * 2 + 1];
         if (a.bias) {
           if (c < a.Cout) v0 += a.bias[c];
@@ -446,11 +451,14 @@ __global__ void kAdam(float *w, float *m, float *v, const float *g, size_t n, fl
 }
 
 // Network input from a frame: log(1 + colour), albedo, normal (as stored),
-// depth mapped to [0, 1) by d / (1 + d) (0 for "no hit"), zero padding to
-// xC channels. The network image is Wp x Hp (multiples of 8); pixels
-// outside the frame are zero.
+// depth mapped to [0, 1) by d / (1 + d) (0 for "no hit"), the noise level:
+// log(1 + standard error of the mean luminance) from the variance channel
+// (0 without it) and 1 / sqrt(samples per pixel), zero padding to xC
+// channels. The network image is Wp x Hp (multiples of 8); pixels outside
+// the frame are zero.
 __global__ void kDenoiseInput(const float4 *color, const float *albedo, const float *normal,
-                              const float *depth, int W, int H, int Wp, int Hp, bf16 *x, int xC) {
+                              const float *depth, const float *var, float invSqrtN, int W, int H,
+                              int Wp, int Hp, bf16 *x, int xC) {
   const size_t np = (size_t)Wp * Hp;
   for (size_t j = blockIdx.x * (size_t)blockDim.x + threadIdx.x; j < np;
        j += (size_t)gridDim.x * blockDim.x) {
@@ -469,7 +477,10 @@ __global__ void kDenoiseInput(const float4 *color, const float *albedo, const fl
     for (int k = 0; k < 3; ++k) f[6 + k] = normal ? normal[3 * i + k] : 0.f;
     const float d = depth ? depth[i] : 1e31f;
     f[9] = d < 1e30f ? d / (1.f + d) : 0.f;
-    for (int k = 10; k < 16; ++k) f[k] = 0.f;
+    const float v = var ? var[i] : 0.f;
+    f[10] = v > 0.f && v < 1e30f ? log1pf(sqrtf(v)) : 0.f;
+    f[11] = invSqrtN;
+    for (int k = 12; k < 16; ++k) f[k] = 0.f;
     for (int k = 0; k < xC; ++k) x[j * xC + k] = __float2bfloat16(k < 16 ? f[k] : 0.f);
   }
 }
@@ -509,8 +520,11 @@ int gridFor(size_t n, int threads = 256) {
 cudaError_t launchConv3x3(const ConvArgs &a, cudaStream_t s) {
   if (a.Cin % 16 || a.Cout <= 0 || a.xC % 8 || a.xOff % 8) return cudaErrorInvalidValue;
   const int P = a.N * a.H * a.W;
-  dim3 grid((P + kBM - 1) / kBM, (a.Cout + kBN - 1) / kBN);
-  kConv3x3<<<grid, 128, 0, s>>>(a);
+  if (a.Cout <= 32) {
+    kConv3x3<32><<<dim3((P + kBM - 1) / kBM, 1), 128, 0, s>>>(a);
+  } else {
+    kConv3x3<64><<<dim3((P + kBM - 1) / kBM, (a.Cout + 63) / 64), 128, 0, s>>>(a);
+  }
   return cudaGetLastError();
 }
 
@@ -582,10 +596,10 @@ cudaError_t launchAdam(float *w, float *m, float *v, const float *g, size_t n, f
 }
 
 cudaError_t launchDenoiseInput(const float4 *color, const float *albedo, const float *normal,
-                               const float *depth, int W, int H, int Wp, int Hp,
-                               __nv_bfloat16 *x, int xC, cudaStream_t s) {
-  kDenoiseInput<<<gridFor((size_t)Wp * Hp), 256, 0, s>>>(color, albedo, normal, depth, W, H, Wp, Hp,
-                                                         x, xC);
+                               const float *depth, const float *var, float invSqrtN, int W, int H,
+                               int Wp, int Hp, __nv_bfloat16 *x, int xC, cudaStream_t s) {
+  kDenoiseInput<<<gridFor((size_t)Wp * Hp), 256, 0, s>>>(color, albedo, normal, depth, var,
+                                                         invSqrtN, W, H, Wp, Hp, x, xC);
   return cudaGetLastError();
 }
 

@@ -114,8 +114,8 @@ cudaError_t launchAdam(float *w, float *m, float *v, const float *g, size_t n, f
                        float b2, float eps, int step, __nv_bfloat16 *wb, __nv_bfloat16 *wt, int Cin,
                        int CoutT, cudaStream_t s);
 cudaError_t launchDenoiseInput(const float4 *color, const float *albedo, const float *normal,
-                               const float *depth, int W, int H, int Wp, int Hp,
-                               __nv_bfloat16 *x, int xC, cudaStream_t s);
+                               const float *depth, const float *var, float invSqrtN, int W, int H,
+                               int Wp, int Hp, __nv_bfloat16 *x, int xC, cudaStream_t s);
 cudaError_t launchDenoiseOutput(const float *out, int oC, int W, int H, int Wp, const float4 *mean,
                                 const float *var, float k, float floorAbs, float4 *result,
                                 uint8_t *retry, unsigned *numRetry, cudaStream_t s);

@@ -2027,6 +2027,13 @@ VSRStatus vsrDenoiserTrainStep(VSRDevice dv, VSRDenoiser nv, const void *input, 
   return st;
 }
 
+// 1 / sqrt(samples per pixel accumulated in the frame), a network input
+static float denoiseInvSqrtN(FrameObj *F) {
+  const int spp = F->renderer ? F->renderer->r.pixelSamples : 1;
+  const double n = (double)std::max(F->accumID, 1) * std::max(spp, 1);
+  return (float)(1.0 / std::sqrt(n));
+}
+
 VSRStatus vsrDenoiserFrameInput(VSRDevice dv, VSRFrame fv, void *input) {
   Device *d = asDev(dv);
   if (!d || !input) return VSR_ERROR_INVALID_ARGUMENT;
@@ -2037,7 +2044,8 @@ VSRStatus vsrDenoiserFrameInput(VSRDevice dv, VSRFrame fv, void *input) {
   if (!F->valid || !F->accum.p) return VSR_ERROR_INCOMPLETE;
   const int Wp = (F->width + 7) / 8 * 8, Hp = (F->height + 7) / 8 * 8;
   return cudaStatus(d, launchDenoiseInput(F->accum.as<float4>(), F->albedo.as<float>(),
-                                          F->normal.as<float>(), F->depth.as<float>(), F->width,
+                                          F->normal.as<float>(), F->depth.as<float>(),
+                                          F->variance.as<float>(), denoiseInvSqrtN(F), F->width,
                                           F->height, Wp, Hp, (__nv_bfloat16 *)input,
                                           Denoiser::kInC, d->stream),
                     "denoiser input");
@@ -2066,8 +2074,8 @@ VSRStatus vsrDenoiseFrame(VSRDevice dv, VSRDenoiser nv, VSRFrame fv, float k, fl
   const float4 *mean = F->accum.as<float4>();
   VSRStatus st = cudaStatus(
       d, launchDenoiseInput(mean, F->albedo.as<float>(), F->normal.as<float>(), F->depth.as<float>(),
-                            F->width, F->height, Wp, Hp, F->denoiseIn.as<__nv_bfloat16>(),
-                            Denoiser::kInC, s),
+                            F->variance.as<float>(), denoiseInvSqrtN(F), F->width, F->height, Wp,
+                            Hp, F->denoiseIn.as<__nv_bfloat16>(), Denoiser::kInC, s),
       "denoiser input");
   if (st == VSR_OK)
     st = cudaStatus(d, n->forward(F->denoiseIn.as<__nv_bfloat16>(), 1, Hp, Wp,

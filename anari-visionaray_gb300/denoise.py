@@ -111,7 +111,7 @@ def make_dataset(dev, seeds, res=256, ref_spp=1024, input_spp=(4,)):
     t = torch.zeros((n, res, res, 4), dtype=torch.float32, device="cuda")
     i = 0
     for seed in seeds:
-        h = build(dev, training_scene(seed, res, 4), variance=False)
+        h = build(dev, training_scene(seed, res, 4), variance=True)
         ref = torch.from_numpy(render_reference(dev, h, ref_spp)).cuda()
         done = 0
         for s in levels:
@@ -129,9 +129,12 @@ def make_dataset(dev, seeds, res=256, ref_spp=1024, input_spp=(4,)):
     return x, t
 
 
-def train(dn, x, t, steps, batch=16, crop=128, lr=1e-3, seed=0, log_every=0):
-    """Adam with cosine decay of the learning rate on random crops; returns
-    the logged (step, loss) pairs and the wall time."""
+def train(dn, x, t, steps, batch=16, crop=128, lr=1e-3, seed=0, log_every=0, warmup=None):
+    """Adam on random crops, the learning rate rising linearly over the first
+    `warmup` steps (default 5 %) and then decaying on a cosine; returns the
+    logged (step, loss) pairs and the wall time. Without the warm-up, Adam's
+    first steps (each weight moved by the full rate) can switch every ReLU
+    off, which leaves the residual network at the identity."""
     import torch
 
     g = torch.Generator(device="cpu")
@@ -150,7 +153,8 @@ def train(dn, x, t, steps, batch=16, crop=128, lr=1e-3, seed=0, log_every=0):
                           for i, a, b in zip(idx, oy, ox)]).contiguous()
         # torch made the crops on its own stream; the step runs on the device's
         torch.cuda.synchronize()
-        rate = lr * 0.5 * (1.0 + math.cos(math.pi * s / steps))
+        ramp = min(1.0, (s + 1) / max(1, warmup if warmup is not None else steps // 20))
+        rate = lr * ramp * 0.5 * (1.0 + math.cos(math.pi * s / steps))
         want = bool(log_every) and (s % log_every == 0 or s == steps - 1)
         loss = dn.train_step(xb.data_ptr(), tb.data_ptr(), 4, batch, crop, crop, rate,
                              want_loss=True)

@@ -57,9 +57,9 @@ def parse():
     p.add_argument("--volume-spp", type=int, default=256)
     p.add_argument("--no-denoise", dest="denoise", action="store_false",
                    help="skip the config-4 denoiser training and evaluation")
-    p.add_argument("--denoise-train-scenes", type=int, default=48)
+    p.add_argument("--denoise-train-scenes", type=int, default=64)
     p.add_argument("--denoise-eval-scenes", type=int, default=8)
-    p.add_argument("--denoise-steps", type=int, default=2000)
+    p.add_argument("--denoise-steps", type=int, default=4000)
     p.add_argument("--no-batch", dest="batch", action="store_false",
                    help="skip the config-3 batched-rendering measurement")
     return p.parse_args()
@@ -284,7 +284,7 @@ def measure_batch_config3(pkg, dev, steps=3, num_scenes=64):
             "timing": "host wall clock, first call to last frame done; synthetic seeded scenes"}
 
 
-def measure_denoiser_config4(pkg, dev, train_scenes=48, eval_scenes=8, steps=2000,
+def measure_denoiser_config4(pkg, dev, train_scenes=64, eval_scenes=8, steps=4000,
                              train_ref_spp=1024, eval_ref_spp=4096, res=256):
     """Config 4 (learned denoiser): train the U-Net on path-traced pairs
     (inputs after 4, 8, 16 and 32 spp, 1024-spp references, 256^2 images,
@@ -303,7 +303,7 @@ def measure_denoiser_config4(pkg, dev, train_scenes=48, eval_scenes=8, steps=200
     dn = pkg.vsr.Denoiser(dev, seed=1)
     losses, train_s = D.train(dn, x, t, steps, log_every=max(1, steps // 4))
     del x, t
-    levels = (4, 8, 16, 32, 64)
+    levels = (4, 8, 12, 16, 20, 24, 32, 64)  # frames accumulate 4 spp per render
     ev = D.evaluate(dev, dn, list(range(10001, 10001 + eval_scenes)), res=res,
                     ref_spp=eval_ref_spp, denoise_levels=levels)
     # 1920x1080: path-tracing time per sample per pixel, and the denoiser

@@ -194,7 +194,9 @@ VSR_API VSRStatus vsrRenderFrames(VSRDevice d, const VSRFrame *frames, uint32_t 
    weights and activations with fp32 accumulation, trained and run by this
    library's own kernels. Network images are N x H x W pixels, H and W
    multiples of 8, NHWC: input 16 bf16 channels (log(1 + colour), albedo,
-   normal, depth / (1 + depth), six zeros), output 16 fp32 channels whose
+   normal, depth / (1 + depth), log(1 + standard error of the mean
+   luminance) from the variance channel, 1 / sqrt(samples per pixel), four
+   zeros), output 16 fp32 channels whose
    first three are log(1 + colour): the input's plus a learned correction. Pointers to images are device pointers;
    work runs on the device's stream (vsrDeviceStream). */
 typedef struct VSRDenoiser_ *VSRDenoiser;

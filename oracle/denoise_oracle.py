@@ -228,8 +228,9 @@ def exact_loss(params, x, target):
 
 
 def init_params(seed):
-    """He-normal weights, zero biases, output channels 3..15 zero (the same
-    distribution as the GPU's initialisation; not the same numbers)."""
+    """He-normal weights, zero biases, output channels 3..15 zero. (The GPU's
+    own initialisation also zeroes the output layer's colour channels; tests
+    use this one so that every layer's gradient is non-zero.)"""
     rng = np.random.default_rng(seed)
     parts = []
     for i, (cin, cout) in enumerate(LAYERS):

@@ -301,7 +301,7 @@ def measure_denoiser_config4(pkg, dev, train_scenes=64, eval_scenes=8, steps=400
                           input_spp=(4, 8, 16, 32))
     data_s = time.perf_counter() - t0
     dn = pkg.vsr.Denoiser(dev, seed=1)
-    losses, train_s = D.train(dn, x, t, steps, log_every=max(1, steps // 4))
+    losses, train_s = D.train(dn, x, t, steps, lr=2e-3, log_every=max(1, steps // 4))
     del x, t
     levels = (4, 8, 12, 16, 20, 24, 32, 64)  # frames accumulate 4 spp per render
     ev = D.evaluate(dev, dn, list(range(10001, 10001 + eval_scenes)), res=res,

@@ -103,6 +103,51 @@ def test_raycast_triangles(pkg, device, oracle):
     assert float((ad <= 1e-5).mean()) >= 0.999
 
 
+def gl_matrices(eye, target, up, fovy, aspect, near=0.5, far=500.0):
+    """OpenGL-style view and projection matrices, column-major (the layout of
+    the matrix camera's 'view' and 'proj' parameters)."""
+    eye, target, up = (np.asarray(v, np.float64) for v in (eye, target, up))
+    f = target - eye
+    f /= np.linalg.norm(f)
+    s = np.cross(f, up)
+    s /= np.linalg.norm(s)
+    u = np.cross(s, f)
+    view = np.eye(4)
+    view[0, :3], view[1, :3], view[2, :3] = s, u, -f
+    view[:3, 3] = -view[:3, :3] @ eye
+    t = 1.0 / np.tan(fovy / 2)
+    proj = np.zeros((4, 4))
+    proj[0, 0], proj[1, 1] = t / aspect, t
+    proj[2, 2], proj[2, 3] = (far + near) / (near - far), 2 * far * near / (near - far)
+    proj[3, 2] = -1.0
+    return [float(v) for v in view.T.reshape(-1)], [float(v) for v in proj.T.reshape(-1)]
+
+
+@pytest.mark.parametrize("kind", ["orthographic", "omnidirectional", "matrix"])
+def test_raycast_camera_types(pkg, device, oracle, kind):
+    """The orthographic, omnidirectional and matrix cameras (DeviceCopyableObjects.h
+    :2510-2600) against the oracle's, through the raycast renderer."""
+    sc = small_spheres(pkg, res=128, renderer="raycast")
+    cam = dict(sc["camera"], type=kind)
+    if kind == "orthographic":
+        cam["height"] = 24.0
+    elif kind == "omnidirectional":
+        cam["position"] = [0.0, 2.0, 0.0]
+    else:
+        eye = np.asarray(cam["position"])
+        view, proj = gl_matrices(eye, eye + np.asarray(cam["direction"]), cam["up"],
+                                 cam["fovy"], 1.0)
+        cam["view"], cam["proj"] = view, proj
+    sc["camera"] = cam
+    gpu = render_gpu(pkg, device, sc)
+    _, F = render_oracle(oracle, sc)
+    good, frac = raycast_ok(gpu, F)
+    hit = F.depth < 1e30
+    print(kind, "within tolerance", frac, "hit share", float(hit.mean()))
+    assert hit.mean() > 0.05
+    assert good, frac
+
+
 @pytest.mark.parametrize("wavefront", [True, False])
 def test_pathtrace_same_stream(pkg, device, oracle, wavefront):
     """Same seeds: the GPU path tracer follows the oracle sample for sample,

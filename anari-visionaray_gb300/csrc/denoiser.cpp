@@ -64,7 +64,8 @@ Denoiser::Denoiser(uint64_t seed) {
   numWt_ = offT;
   ok_ = alloc(params_, off) == cudaSuccess && alloc(m_, off) == cudaSuccess &&
         alloc(v_, off) == cudaSuccess && alloc(grad_, off) == cudaSuccess &&
-        alloc(wbf_, off) == cudaSuccess && alloc(wt_, offT) == cudaSuccess;
+        alloc(wbf_, off) == cudaSuccess && alloc(wt_, offT) == cudaSuccess &&
+        alloc(loss_, 1) == cudaSuccess;
   if (!ok_) return;
   // He-normal weights (std sqrt(2 / fan_in)), zero biases. The output layer
   // starts at zero: the network begins as the identity on the input's
@@ -83,7 +84,8 @@ Denoiser::Denoiser(uint64_t seed) {
 }
 
 Denoiser::~Denoiser() {
-  for (void *p : {(void *)params_, (void *)m_, (void *)v_, (void *)grad_, (void *)wbf_, (void *)wt_})
+  for (void *p : {(void *)params_, (void *)m_, (void *)v_, (void *)grad_, (void *)wbf_, (void *)wt_,
+                  (void *)loss_})
     if (p) cudaFree(p);
   for (void *p : bufs_) cudaFree(p);
 }

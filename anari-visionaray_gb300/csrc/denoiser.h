@@ -45,6 +45,7 @@ class Denoiser {
   // one Adam step (beta 0.9 / 0.999, eps 1e-8) with the current gradients
   cudaError_t adam(float lr, cudaStream_t s);
   const float *grad() const { return grad_; }
+  float *lossDevice() const { return loss_; }  // one device float for the loss
   int steps() const { return step_; }
 
  private:
@@ -63,7 +64,7 @@ class Denoiser {
   bool ok_ = false;
   std::vector<DenoiseLayer> layers_;
   size_t numParams_ = 0, numWt_ = 0;
-  float *params_ = nullptr, *m_ = nullptr, *v_ = nullptr, *grad_ = nullptr;
+  float *params_ = nullptr, *m_ = nullptr, *v_ = nullptr, *grad_ = nullptr, *loss_ = nullptr;
   __nv_bfloat16 *wbf_ = nullptr, *wt_ = nullptr;
   int step_ = 0;
   // activations (and, for training, their gradients), sized for (N, H, W)

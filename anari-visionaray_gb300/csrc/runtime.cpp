@@ -1980,17 +1980,12 @@ VSRStatus vsrDenoiserForward(VSRDevice dv, VSRDenoiser nv, const void *input, ui
 // forward + backward; the loss (if wanted) is copied to the host
 static VSRStatus denoiserBackward(Device *d, Denoiser *n, const void *input, const float *target,
                                   uint32_t tC, uint32_t N, uint32_t H, uint32_t W, float *loss) {
-  static float *lossDev = nullptr;  // one float per process, guarded by the device mutex
-  if (!lossDev && cudaMalloc(&lossDev, sizeof(float)) != cudaSuccess) {
-    lossDev = nullptr;
-    return VSR_ERROR_OUT_OF_MEMORY;
-  }
   VSRStatus st = cudaStatus(d, n->backward((const __nv_bfloat16 *)input, target, (int)tC, (int)N,
-                                           (int)H, (int)W, lossDev, d->stream),
+                                           (int)H, (int)W, n->lossDevice(), d->stream),
                             "denoiser backward");
   if (st == VSR_OK && loss)
-    st = cudaStatus(d, cudaMemcpyAsync(loss, lossDev, sizeof(float), cudaMemcpyDeviceToHost,
-                                       d->stream),
+    st = cudaStatus(d, cudaMemcpyAsync(loss, n->lossDevice(), sizeof(float),
+                                       cudaMemcpyDeviceToHost, d->stream),
                     "denoiser loss");
   return st;
 }

@@ -65,7 +65,8 @@ Denoiser::Denoiser(uint64_t seed) {
   ok_ = alloc(params_, off) == cudaSuccess && alloc(m_, off) == cudaSuccess &&
         alloc(v_, off) == cudaSuccess && alloc(grad_, off) == cudaSuccess &&
         alloc(wbf_, off) == cudaSuccess && alloc(wt_, offT) == cudaSuccess &&
-        alloc(loss_, 1) == cudaSuccess;
+        alloc(loss_, 1) == cudaSuccess && alloc(err_, 1) == cudaSuccess &&
+        cudaMemset(err_, 0, sizeof(unsigned)) == cudaSuccess;
   if (!ok_) return;
   // He-normal weights (std sqrt(2 / fan_in)), zero biases. The output layer
   // starts at zero: the network begins as the identity on the input's
@@ -85,7 +86,7 @@ Denoiser::Denoiser(uint64_t seed) {
 
 Denoiser::~Denoiser() {
   for (void *p : {(void *)params_, (void *)m_, (void *)v_, (void *)grad_, (void *)wbf_, (void *)wt_,
-                  (void *)loss_})
+                  (void *)loss_, (void *)err_})
     if (p) cudaFree(p);
   for (void *p : bufs_) cudaFree(p);
 }
@@ -173,7 +174,8 @@ void Denoiser::conv(int li, const __nv_bfloat16 *x, int xC, __nv_bfloat16 *y, fl
   a.resid = resid;
   a.residC = kInC;
   a.residN = kColorC;
-  launchConv3x3(a, s);
+  if (tensorPath_ == 1) launchConv3x3Tc(a, err_, s);
+  else launchConv3x3(a, s);
 }
 
 // Weight and bias gradients of layer li from its pre-activation gradient dy
@@ -218,7 +220,8 @@ void Denoiser::convBack(int li, const __nv_bfloat16 *x, int xC, const __nv_bfloa
     a.N = N;
     a.H = H;
     a.W = W;
-    launchConv3x3(a, s);
+    if (tensorPath_ == 1) launchConv3x3Tc(a, err_, s);
+    else launchConv3x3(a, s);
   }
 }
 

@@ -46,6 +46,10 @@ class Denoiser {
   cudaError_t adam(float lr, cudaStream_t s);
   const float *grad() const { return grad_; }
   float *lossDevice() const { return loss_; }  // one device float for the loss
+  // 0: convolutions on mma.sync (kConv3x3), 1: on tcgen05 (kConv3x3Tc)
+  void setTensorPath(int path) { tensorPath_ = path; }
+  int tensorPath() const { return tensorPath_; }
+  unsigned *errorWord() const { return err_; }
   int steps() const { return step_; }
 
  private:
@@ -65,6 +69,8 @@ class Denoiser {
   std::vector<DenoiseLayer> layers_;
   size_t numParams_ = 0, numWt_ = 0;
   float *params_ = nullptr, *m_ = nullptr, *v_ = nullptr, *grad_ = nullptr, *loss_ = nullptr;
+  unsigned *err_ = nullptr;
+  int tensorPath_ = 0;
   __nv_bfloat16 *wbf_ = nullptr, *wt_ = nullptr;
   int step_ = 0;
   // activations (and, for training, their gradients), sized for (N, H, W)

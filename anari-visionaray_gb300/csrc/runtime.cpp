@@ -1944,6 +1944,29 @@ uint64_t vsrDenoiserParameterCount(VSRDevice dv, VSRDenoiser nv) {
   return n ? n->numParams() : 0;
 }
 
+VSRStatus vsrDenoiserSetTensorPath(VSRDevice dv, VSRDenoiser nv, int path) {
+  Device *d = asDev(dv);
+  if (!d || (path != 0 && path != 1)) return VSR_ERROR_INVALID_ARGUMENT;
+  std::lock_guard<std::recursive_mutex> lk(d->mtx);
+  Denoiser *n = asDenoiser(d, nv);
+  if (!n) return VSR_ERROR_INVALID_OBJECT;
+  cudaStreamSynchronize(d->stream);
+  n->setTensorPath(path);
+  return VSR_OK;
+}
+
+uint32_t vsrDenoiserErrors(VSRDevice dv, VSRDenoiser nv) {
+  Device *d = asDev(dv);
+  if (!d) return 0;
+  std::lock_guard<std::recursive_mutex> lk(d->mtx);
+  Denoiser *n = asDenoiser(d, nv);
+  if (!n) return 0;
+  uint32_t e = 0;
+  cudaMemcpyAsync(&e, n->errorWord(), sizeof(e), cudaMemcpyDeviceToHost, d->stream);
+  cudaStreamSynchronize(d->stream);
+  return e;
+}
+
 VSRStatus vsrDenoiserGetParameters(VSRDevice dv, VSRDenoiser nv, float *params, uint64_t count) {
   Device *d = asDev(dv);
   if (!d || !params) return VSR_ERROR_INVALID_ARGUMENT;

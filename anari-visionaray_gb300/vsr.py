@@ -64,6 +64,8 @@ _SIGNATURES = [
     ("vsrNewDenoiser", _P, [_P, ctypes.c_uint64]),
     ("vsrReleaseDenoiser", ctypes.c_int, [_P, _P]),
     ("vsrDenoiserParameterCount", ctypes.c_uint64, [_P, _P]),
+    ("vsrDenoiserSetTensorPath", ctypes.c_int, [_P, _P, ctypes.c_int]),
+    ("vsrDenoiserErrors", ctypes.c_uint32, [_P, _P]),
     ("vsrDenoiserGetParameters", ctypes.c_int, [_P, _P, ctypes.POINTER(ctypes.c_float), ctypes.c_uint64]),
     ("vsrDenoiserSetParameters", ctypes.c_int, [_P, _P, ctypes.POINTER(ctypes.c_float), ctypes.c_uint64]),
     ("vsrDenoiserForward", ctypes.c_int, [_P, _P, _P, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32, _P]),
@@ -168,6 +170,15 @@ class Denoiser:
         if self.handle:
             self.lib.vsrReleaseDenoiser(self.dev.handle, self.handle)
             self.handle = None
+
+    def set_tensor_path(self, path):
+        """0: mma.sync convolutions, 1: tcgen05 convolutions."""
+        rc = self.lib.vsrDenoiserSetTensorPath(self.dev.handle, self.handle, path)
+        if rc:
+            raise RuntimeError(f"vsrDenoiserSetTensorPath failed ({rc})")
+
+    def errors(self):
+        return int(self.lib.vsrDenoiserErrors(self.dev.handle, self.handle))
 
     def params(self):
         out = np.zeros(self.count, np.float32)

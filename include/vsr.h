@@ -208,6 +208,12 @@ VSR_API uint64_t vsrDenoiserParameterCount(VSRDevice d, VSRDenoiser n);
    the optimiser. */
 VSR_API VSRStatus vsrDenoiserGetParameters(VSRDevice d, VSRDenoiser n, float *params,
                                            uint64_t count);
+/* Which tensor-core path the convolutions take: 0 warp-level mma.sync
+   (default), 1 tcgen05 with the accumulator in tensor memory.
+   vsrDenoiserErrors returns the device error word of the tcgen05 path (bit
+   1: a bounded wait for the tensor core ran out), 0 when all is well. */
+VSR_API VSRStatus vsrDenoiserSetTensorPath(VSRDevice d, VSRDenoiser n, int path);
+VSR_API uint32_t vsrDenoiserErrors(VSRDevice d, VSRDenoiser n);
 VSR_API VSRStatus vsrDenoiserSetParameters(VSRDevice d, VSRDenoiser n, const float *params,
                                            uint64_t count);
 VSR_API VSRStatus vsrDenoiserForward(VSRDevice d, VSRDenoiser n, const void *input, uint32_t N,

@@ -101,6 +101,50 @@ def test_gradients_match_oracle(net):
             assert rel < 3e-2, f"layer {i} {what}"
 
 
+@pytest.mark.parametrize("shape", [(2, 16, 16), (1, 24, 40)])
+def test_tcgen05_path_matches_oracle(net, shape):
+    """The tcgen05 convolutions (accumulator in tensor memory) in forward and
+    in the backward's input gradients: the same output and parameter
+    gradients as the oracle, at a pixel count that fills 128-pixel tiles
+    and at one that leaves ragged tiles on every level (24 x 40: 960, 240,
+    60, 15 pixels)."""
+    import torch
+    n, h, w = shape
+    params = perturbed_params(5, 11)
+    net.set_params(params)
+    net.set_tensor_path(1)
+    x, target = make_case(6, n, h, w)
+    xd, td = to_device(x, target)
+    out = torch.zeros((n, h, w, 16), dtype=torch.float32, device="cuda")
+    net.forward(xd.data_ptr(), n, h, w, out.data_ptr())
+    torch.cuda.synchronize()
+    assert net.errors() == 0
+    ref = D.forward(params, x)["out"]
+    got = out.cpu().numpy()
+    scale = np.abs(ref[..., :3]).max()
+    err = np.abs(got[..., :3] - ref[..., :3]).max()
+    print("tcgen05 forward max err", err, "scale", scale)
+    assert err <= 2e-2 * scale + 1e-3
+    assert np.abs(got[..., 3:]).max() == 0.0
+
+    g, loss = net.gradients(xd.data_ptr(), td.data_ptr(), 4, n, h, w)
+    assert net.errors() == 0
+    ref_loss, ref_g, _ = D.loss_and_grads(params, x, target)
+    assert abs(loss - ref_loss) <= 1e-3 * ref_loss + 1e-5
+    for i, (ws, bs) in enumerate(layer_slices()):
+        for sl, what in ((ws, "weights"), (bs, "bias")):
+            a, b = g[sl], ref_g[sl]
+            if i == len(D.LAYERS) - 1:
+                cout = D.LAYERS[i][1]
+                keep = np.zeros(cout, bool)
+                keep[:3] = True
+                mask = np.repeat(keep, a.size // cout)
+                a, b = a[mask], b[mask]
+            rel = np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-12)
+            print(f"tcgen05 layer {i} {what}: rel err {rel:.2e}")
+            assert rel < 3e-2, f"layer {i} {what}"
+
+
 def test_adam_step(net):
     params = D.init_params(9)
     net.set_params(params)

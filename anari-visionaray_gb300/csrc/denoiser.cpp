@@ -174,8 +174,33 @@ void Denoiser::conv(int li, const __nv_bfloat16 *x, int xC, __nv_bfloat16 *y, fl
   a.resid = resid;
   a.residC = kInC;
   a.residN = kColorC;
-  if (tensorPath_ == 1) launchConv3x3Tc(a, err_, s);
+  if (useTc(W)) launchConv3x3Tc(a, err_, s);
   else launchConv3x3(a, s);
+}
+
+// a decoder convolution on [upsampled coarse level | skip connection],
+// read in place (tcgen05 path)
+void Denoiser::convCat(int li, const __nv_bfloat16 *coarse, int coarseC, const __nv_bfloat16 *skip,
+                       int skipC, __nv_bfloat16 *y, int yC, int N, int H, int W, cudaStream_t s) {
+  const DenoiseLayer &L = layers_[li];
+  ConvArgs a{};
+  a.x = coarse;
+  a.xC = coarseC;
+  a.up = 1;
+  a.x2 = skip;
+  a.x2C = skipC;
+  a.split = coarseC;
+  a.Cin = L.cin;
+  a.w = wbf_ + L.w;
+  a.bias = params_ + L.b;
+  a.Cout = L.cout;
+  a.y = y;
+  a.yC = yC;
+  a.relu = 1;
+  a.N = N;
+  a.H = H;
+  a.W = W;
+  launchConv3x3Tc(a, err_, s);
 }
 
 // Weight and bias gradients of layer li from its pre-activation gradient dy
@@ -220,12 +245,13 @@ void Denoiser::convBack(int li, const __nv_bfloat16 *x, int xC, const __nv_bfloa
     a.N = N;
     a.H = H;
     a.W = W;
-    if (tensorPath_ == 1) launchConv3x3Tc(a, err_, s);
+    if (useTc(W)) launchConv3x3Tc(a, err_, s);
     else launchConv3x3(a, s);
   }
 }
 
-cudaError_t Denoiser::run(const __nv_bfloat16 *x, int N, int H, int W, float *out, cudaStream_t s) {
+cudaError_t Denoiser::run(const __nv_bfloat16 *x, int N, int H, int W, float *out, cudaStream_t s,
+                          bool catOut) {
   const int H1 = H / 2, W1 = W / 2, H2 = H / 4, W2 = W / 4, H3 = H / 8, W3 = W / 8;
   const size_t P0 = (size_t)N * H * W, P1 = P0 / 4, P2 = P0 / 16;
   Act &A = act_;
@@ -240,17 +266,29 @@ cudaError_t Denoiser::run(const __nv_bfloat16 *x, int N, int H, int W, float *ou
   launchMaxPool(A.e2, 128, N, H2, W2, A.p2, s);
   conv(L_E3A, A.p2, 128, A.a3, nullptr, 256, N, H3, W3, true, s);
   conv(L_E3B, A.a3, 256, A.e3, nullptr, 256, N, H3, W3, true, s);
-  launchUpsample(A.e3, 256, N, H3, W3, A.cat2, 384, 0, s);
-  launchCopyChannels(A.e2, 128, 0, A.cat2, 384, 256, 128, P2, 0, s);
-  conv(L_D2A, A.cat2, 384, A.b2, nullptr, 128, N, H2, W2, true, s);
+  if (!catOut && useTc(W2)) {
+    convCat(L_D2A, A.e3, 256, A.e2, 128, A.b2, 128, N, H2, W2, s);
+  } else {
+    launchUpsample(A.e3, 256, N, H3, W3, A.cat2, 384, 0, s);
+    launchCopyChannels(A.e2, 128, 0, A.cat2, 384, 256, 128, P2, 0, s);
+    conv(L_D2A, A.cat2, 384, A.b2, nullptr, 128, N, H2, W2, true, s);
+  }
   conv(L_D2B, A.b2, 128, A.d2, nullptr, 128, N, H2, W2, true, s);
-  launchUpsample(A.d2, 128, N, H2, W2, A.cat1, 192, 0, s);
-  launchCopyChannels(A.e1, 64, 0, A.cat1, 192, 128, 64, P1, 0, s);
-  conv(L_D1A, A.cat1, 192, A.b1, nullptr, 64, N, H1, W1, true, s);
+  if (!catOut && useTc(W1)) {
+    convCat(L_D1A, A.d2, 128, A.e1, 64, A.b1, 64, N, H1, W1, s);
+  } else {
+    launchUpsample(A.d2, 128, N, H2, W2, A.cat1, 192, 0, s);
+    launchCopyChannels(A.e1, 64, 0, A.cat1, 192, 128, 64, P1, 0, s);
+    conv(L_D1A, A.cat1, 192, A.b1, nullptr, 64, N, H1, W1, true, s);
+  }
   conv(L_D1B, A.b1, 64, A.d1, nullptr, 64, N, H1, W1, true, s);
-  launchUpsample(A.d1, 64, N, H1, W1, A.cat0, 96, 0, s);
-  launchCopyChannels(A.e0, 32, 0, A.cat0, 96, 64, 32, P0, 0, s);
-  conv(L_D0A, A.cat0, 96, A.b0, nullptr, 32, N, H, W, true, s);
+  if (!catOut && useTc(W)) {
+    convCat(L_D0A, A.d1, 64, A.e0, 32, A.b0, 32, N, H, W, s);
+  } else {
+    launchUpsample(A.d1, 64, N, H1, W1, A.cat0, 96, 0, s);
+    launchCopyChannels(A.e0, 32, 0, A.cat0, 96, 64, 32, P0, 0, s);
+    conv(L_D0A, A.cat0, 96, A.b0, nullptr, 32, N, H, W, true, s);
+  }
   conv(L_D0B, A.b0, 32, A.d0, nullptr, 32, N, H, W, true, s);
   // the output is a correction of the input's log(1 + colour)
   conv(L_OUT, A.d0, 32, nullptr, out, kOutC, N, H, W, false, s, x);
@@ -262,7 +300,7 @@ cudaError_t Denoiser::forward(const __nv_bfloat16 *x, int N, int H, int W, float
   if (!ok_ || !x || N <= 0 || H <= 0 || W <= 0 || H % 8 || W % 8) return cudaErrorInvalidValue;
   cudaError_t e = ensure(N, H, W, false);
   if (e != cudaSuccess) return e;
-  return run(x, N, H, W, out ? out : out_, s);
+  return run(x, N, H, W, out ? out : out_, s, false);
 }
 
 cudaError_t Denoiser::backward(const __nv_bfloat16 *x, const float *target, int tC, int N, int H,
@@ -271,7 +309,7 @@ cudaError_t Denoiser::backward(const __nv_bfloat16 *x, const float *target, int 
     return cudaErrorInvalidValue;
   cudaError_t e = ensure(N, H, W, true);
   if (e != cudaSuccess) return e;
-  if ((e = run(x, N, H, W, out_, s)) != cudaSuccess) return e;
+  if ((e = run(x, N, H, W, out_, s, true)) != cudaSuccess) return e;
   const int H1 = H / 2, W1 = W / 2, H2 = H / 4, W2 = W / 4, H3 = H / 8, W3 = W / 8;
   const size_t P0 = (size_t)N * H * W, P1 = P0 / 4, P2 = P0 / 16;
   Act &A = act_, &G = grd_;

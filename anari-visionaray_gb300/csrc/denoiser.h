@@ -46,7 +46,9 @@ class Denoiser {
   cudaError_t adam(float lr, cudaStream_t s);
   const float *grad() const { return grad_; }
   float *lossDevice() const { return loss_; }  // one device float for the loss
-  // 0: convolutions on mma.sync (kConv3x3), 1: on tcgen05 (kConv3x3Tc)
+  // 0: convolutions on mma.sync (kConv3x3); 1: on tcgen05 (kConv3x3Tc) for
+  // images at least one 128-pixel tile wide, mma.sync below that; 2:
+  // tcgen05 at every width
   void setTensorPath(int path) { tensorPath_ = path; }
   int tensorPath() const { return tensorPath_; }
   unsigned *errorWord() const { return err_; }
@@ -58,7 +60,13 @@ class Denoiser {
         *b1, *d1, *cat0, *b0, *d0;
   };
   cudaError_t ensure(int N, int H, int W, bool train);
-  cudaError_t run(const __nv_bfloat16 *x, int N, int H, int W, float *out, cudaStream_t s);
+  // catOut: write the decoders' concatenated inputs (the backward reads
+  // them); without it the tcgen05 path reads the two parts directly
+  cudaError_t run(const __nv_bfloat16 *x, int N, int H, int W, float *out, cudaStream_t s,
+                  bool catOut);
+  bool useTc(int W) const { return tensorPath_ == 2 || (tensorPath_ == 1 && W >= 128); }
+  void convCat(int layer, const __nv_bfloat16 *coarse, int coarseC, const __nv_bfloat16 *skip,
+               int skipC, __nv_bfloat16 *y, int yC, int N, int H, int W, cudaStream_t s);
   void conv(int layer, const __nv_bfloat16 *x, int xC, __nv_bfloat16 *y, float *yf, int yC, int N,
             int H, int W, bool relu, cudaStream_t s, const __nv_bfloat16 *resid = nullptr);
   void convBack(int layer, const __nv_bfloat16 *x, int xC, const __nv_bfloat16 *dy,
@@ -70,7 +78,7 @@ class Denoiser {
   size_t numParams_ = 0, numWt_ = 0;
   float *params_ = nullptr, *m_ = nullptr, *v_ = nullptr, *grad_ = nullptr, *loss_ = nullptr;
   unsigned *err_ = nullptr;
-  int tensorPath_ = 0;
+  int tensorPath_ = 1;
   __nv_bfloat16 *wbf_ = nullptr, *wt_ = nullptr;
   int step_ = 0;
   // activations (and, for training, their gradients), sized for (N, H, W)

@@ -518,7 +518,8 @@ int gridFor(size_t n, int threads = 256) {
 }  // namespace
 
 cudaError_t launchConv3x3(const ConvArgs &a, cudaStream_t s) {
-  if (a.Cin % 16 || a.Cout <= 0 || a.xC % 8 || a.xOff % 8) return cudaErrorInvalidValue;
+  if (a.Cin % 16 || a.Cout <= 0 || a.xC % 8 || a.xOff % 8 || a.x2 || a.split || a.up)
+    return cudaErrorInvalidValue;
   const int P = a.N * a.H * a.W;
   if (a.Cout <= 32) {
     kConv3x3<32><<<dim3((P + kBM - 1) / kBM, 1), 128, 0, s>>>(a);

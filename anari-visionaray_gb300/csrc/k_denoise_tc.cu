@@ -32,6 +32,11 @@
 // mask of a previous ReLU, in the same order and with the same results as
 // kConv3x3.
 //
+// The input can be the concatenation of two tensors, the first one at half
+// resolution (a U-Net decoder's upsampled coarse level and its skip
+// connection): each 32-channel group is read from the tensor that holds it,
+// so neither the upsampled tensor nor the concatenation is written out.
+//
 // Every mbarrier wait is bounded (one second); a wait that runs out sets the
 // error word, and the CTA still waits (bounded) for its MMAs and releases its
 // tensor memory before it returns.
@@ -169,6 +174,13 @@ __global__ void __launch_bounds__(128) kConv3x3Tc(ConvArgs a, int tilesX, int ti
     }
     const int c0 = s * 8 * kChunks;
     const int chunks = min(kChunks, (a.Cin - c0) / 8);  // 4, or 2 for a last group of 16
+    // this group's source: x (upsampled or not) or the second input x2
+    const bool second = a.split > 0 && c0 >= a.split;
+    const bf16 *srcBase = second ? a.x2 : a.x;
+    const int srcC = second ? a.x2C : a.xC;
+    const int srcOff = second ? a.x2Off + c0 - a.split : a.xOff + c0;
+    const int sh = (!second && a.up) ? 1 : 0;
+    const int srcH = a.H >> sh, srcW = a.W >> sh;
     // the halo: chunk fastest, so that a pixel's channels are read together
     const int haloEntries = chunks * kHY * kHXUsed;
     for (int i = tid; i < haloEntries; i += 128) {
@@ -177,7 +189,8 @@ __global__ void __launch_bounds__(128) kConv3x3Tc(ConvArgs a, int tilesX, int ti
       const int hx = r % kHXUsed, hy = r / kHXUsed;
       const int y = y0 - 1 + hy, x = x0 - 1 + hx;
       const bool in = y >= 0 && y < a.H && x >= 0 && x < a.W;
-      const bf16 *src = a.x + (in ? (((size_t)n * a.H + y) * a.W + x) * a.xC + a.xOff + c0 + 8 * c : 0);
+      const size_t pix = ((size_t)n * srcH + (y >> sh)) * srcW + (x >> sh);
+      const bf16 *src = srcBase + (in ? pix * srcC + srcOff + 8 * c : 0);
       cpAsync16(haloBase + (uint32_t)(c * kPlane + (hy * kHX + hx) * 16), src, in);
     }
     // the weights of the nine taps
@@ -312,6 +325,10 @@ cudaError_t launchTc(const ConvArgs &a, unsigned *error, cudaStream_t s) {
 cudaError_t launchConv3x3Tc(const ConvArgs &a, unsigned *error, cudaStream_t s) {
   if (a.Cin <= 0 || a.Cin % 16 || a.Cout <= 0 || a.xC % 8 || a.xOff % 8 || !error)
     return cudaErrorInvalidValue;
+  if (a.split && (a.split < 0 || a.split % 32 || a.split >= a.Cin || !a.x2 || a.x2C % 8 ||
+                  a.x2Off % 8 || a.x2Off + a.Cin - a.split > a.x2C))
+    return cudaErrorInvalidValue;
+  if (a.up && (a.H % 2 || a.W % 2)) return cudaErrorInvalidValue;
   if (a.N <= 0 || a.H <= 0 || a.W <= 0) return cudaSuccess;
   return a.Cout <= 32 ? launchTc<32>(a, error, s) : launchTc<64>(a, error, s);
 }

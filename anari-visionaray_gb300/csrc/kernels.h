@@ -82,6 +82,12 @@ struct ConvArgs {
   int N, H, W;
   const __nv_bfloat16 *resid;  // added to output channels [0, residN), or null
   int residC, residN;
+  // tcgen05 path only: input channels [split, Cin) come from x2 (x2C
+  // channels per pixel, from x2Off), channels [0, split) from x; with up, x
+  // is at half resolution and is read at (y / 2, x / 2) (nearest 2x
+  // upsampling). split a multiple of 32; 0: every channel from x.
+  const __nv_bfloat16 *x2;
+  int x2C, x2Off, split, up;
 };
 struct WgradArgs {
   const __nv_bfloat16 *dy;  // output gradient (after the ReLU mask)

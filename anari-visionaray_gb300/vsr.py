@@ -172,7 +172,8 @@ class Denoiser:
             self.handle = None
 
     def set_tensor_path(self, path):
-        """0: mma.sync convolutions, 1: tcgen05 convolutions."""
+        """0: mma.sync convolutions; 1: tcgen05 where a level is at least 128
+        pixels wide, mma.sync below; 2: tcgen05 at every width."""
         rc = self.lib.vsrDenoiserSetTensorPath(self.dev.handle, self.handle, path)
         if rc:
             raise RuntimeError(f"vsrDenoiserSetTensorPath failed ({rc})")

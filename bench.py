@@ -356,7 +356,9 @@ def measure_denoiser_config4(pkg, dev, train_scenes=64, eval_scenes=8, steps=400
                      "unit": "TFLOP/s", "frac": flops / dn_s / 1e12 / peak[0],
                      "note": f"denoiser forward at 1920x1080 ({flops / 1e12:.3f} TFLOP incl. "
                              f"input and gate kernels in the time); peak bf16 {peak[1]}; "
-                             "mma.sync m16n8k16 bf16 implicit GEMM"},
+                             "tcgen05.mma kind::f16 (bf16 -> fp32 in tensor memory) on halo "
+                             "tiles of 4 x 128 pixels; decoders read upsampled level and skip "
+                             "in place"},
     }
 
 

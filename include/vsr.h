@@ -208,8 +208,11 @@ VSR_API uint64_t vsrDenoiserParameterCount(VSRDevice d, VSRDenoiser n);
    the optimiser. */
 VSR_API VSRStatus vsrDenoiserGetParameters(VSRDevice d, VSRDenoiser n, float *params,
                                            uint64_t count);
-/* Which tensor-core path the convolutions take: 0 warp-level mma.sync
-   (default), 1 tcgen05 with the accumulator in tensor memory.
+/* Which tensor-core path the convolutions take: 0 warp-level mma.sync,
+   1 (default) tcgen05 with the accumulators in tensor memory for levels at
+   least 128 pixels wide (mma.sync below), 2 tcgen05 at every width. On the
+   tcgen05 path the forward reads each decoder's upsampled input and skip
+   connection in place instead of writing their concatenation.
    vsrDenoiserErrors returns the device error word of the tcgen05 path (bit
    1: a bounded wait for the tensor core ran out), 0 when all is well. */
 VSR_API VSRStatus vsrDenoiserSetTensorPath(VSRDevice d, VSRDenoiser n, int path);

@@ -101,18 +101,21 @@ def test_gradients_match_oracle(net):
             assert rel < 3e-2, f"layer {i} {what}"
 
 
-@pytest.mark.parametrize("shape", [(2, 16, 16), (1, 24, 40)])
-def test_tcgen05_path_matches_oracle(net, shape):
-    """The tcgen05 convolutions (accumulator in tensor memory) in forward and
-    in the backward's input gradients: the same output and parameter
-    gradients as the oracle, at a pixel count that fills 128-pixel tiles
-    and at one that leaves ragged tiles on every level (24 x 40: 960, 240,
-    60, 15 pixels)."""
+@pytest.mark.parametrize("shape,path", [((2, 16, 16), 2), ((1, 24, 40), 2), ((1, 24, 136), 1),
+                                        ((2, 16, 256), 1)])
+def test_tcgen05_path_matches_oracle(net, shape, path):
+    """The tcgen05 convolutions (accumulators in tensor memory) in forward,
+    where the decoders read the upsampled level and the skip connection in
+    place, and in the backward's input gradients: the same output and
+    parameter gradients as the oracle. Path 2 runs every level on tcgen05
+    (tiles of 4 rows x 128 pixels far wider than these images, rows not a
+    multiple of 4 at 24 / 8 = 3); path 1 switches to mma.sync below 128
+    pixels (136: a second, nearly empty tile; 256: two levels on each)."""
     import torch
     n, h, w = shape
     params = perturbed_params(5, 11)
     net.set_params(params)
-    net.set_tensor_path(1)
+    net.set_tensor_path(path)
     x, target = make_case(6, n, h, w)
     xd, td = to_device(x, target)
     out = torch.zeros((n, h, w, 16), dtype=torch.float32, device="cuda")

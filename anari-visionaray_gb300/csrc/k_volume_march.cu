@@ -26,6 +26,8 @@
 #include "render_common.cuh"
 #include "kernels.h"
 
+#include <mutex>
+
 namespace vsr {
 namespace {
 
@@ -509,6 +511,34 @@ __global__ void __launch_bounds__(256) kVolumeCombine(DScene S, DRenderer R, DFr
 
 }  // namespace
 
+namespace {
+
+// resident blocks per SM of a persistent kernel at 256 threads, queried once
+// per (kernel, dynamic shared memory) and kept, so that a frame's launches
+// follow each other without host-side queries in between
+int persistentBlocksPerSM(const void *fn, size_t smem) {
+  struct Entry {
+    const void *fn;
+    size_t smem;
+    int perSM;
+  };
+  static Entry cache[16];
+  static int count = 0;
+  static std::mutex mtx;
+  std::lock_guard<std::mutex> lk(mtx);
+  for (int i = 0; i < count; ++i)
+    if (cache[i].fn == fn && cache[i].smem == smem) return cache[i].perSM;
+  if (smem > 48 * 1024)
+    cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  int perSM = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, fn, 256, smem);
+  perSM = perSM > 0 ? perSM : 1;
+  if (count < 16) cache[count++] = Entry{fn, smem, perSM};
+  return perSM;
+}
+
+}  // namespace
+
 cudaError_t launchVolumeMarch(const DScene &S, const DCamera &C, const DRenderer &R,
                               const DFrame &F, int stageTFSize, bool count,
                               const MarchScratch &M, cudaStream_t stream) {
@@ -525,11 +555,8 @@ cudaError_t launchVolumeMarch(const DScene &S, const DCamera &C, const DRenderer
   const int numPix = F.width * F.height;
   kVolumeSetup<<<min((numPix + 255) / 256, sms * 8), 256, 0, stream>>>(S, C, R, F, M);
   auto persistent = [&](auto kernel, auto... args) {
-    if (smem > 48 * 1024)
-      cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    int perSM = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, kernel, 256, smem);
-    kernel<<<sms * (perSM > 0 ? perSM : 1), 256, smem, stream>>>(args...);
+    const int perSM = persistentBlocksPerSM((const void *)kernel, smem);
+    kernel<<<sms * perSM, 256, smem, stream>>>(args...);
   };
   persistent(kVolumeSegments, S, R, M, stage);
   if (count) persistent(kVolumeCombine<true>, S, R, F, M, stage);

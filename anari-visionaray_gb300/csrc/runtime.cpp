@@ -1239,39 +1239,46 @@ VSRStatus renderFrame(Device *dev, FrameObj *F) {
     F->lastStamp = stampAll;
     F->nextReset = true;
   }
-  cudaEventRecord(F->evStart, s);
-  if (F->nextReset) {
-    launchFrameReset(F->accum.as<float4>(), F->depth.as<float>(), (size_t)F->width * F->height, s);
+  // host-side preparation first, so that the timed region between the
+  // frame's events holds GPU work only
+  const bool reset = F->nextReset;
+  if (reset) {
     F->accumID = 0;
     F->nextReset = false;
   }
+  const bool doRender = F->accumID < F->renderer->sampleLimit;
+  const DRenderer &R = F->renderer->r;
+  int stage = 0;
+  MarchScratch ms{};
+  bool segmented = false;
+  if (doRender && R.type == REND_RAYCAST) {
+    // stage the first volume's TF in shared memory when it fits (64 KB)
+    if (!W->volsHost.empty() && W->volsHost[0].tfSize <= 4096) stage = W->volsHost[0].tfSize;
+    segmented = !W->scene.hasSurfaces && R.pixelSamples == 1;
+    if (segmented && !F->ensureMarch()) {
+      dev->report(F, VSR_FRAME, VSR_SEVERITY_ERROR, VSR_ERROR_OUT_OF_MEMORY,
+                  "volume marcher scratch allocation failed");
+      return VSR_ERROR_OUT_OF_MEMORY;
+    }
+    if (segmented) ms = F->march();
+  } else if (doRender && F->renderer->wavefront && !F->ensureWave()) {
+    dev->report(F, VSR_FRAME, VSR_SEVERITY_ERROR, VSR_ERROR_OUT_OF_MEMORY,
+                "wavefront state allocation failed");
+    return VSR_ERROR_OUT_OF_MEMORY;
+  }
+  const DFrame fr = F->record();
+  cudaEventRecord(F->evStart, s);
+  if (reset)
+    launchFrameReset(F->accum.as<float4>(), F->depth.as<float>(), (size_t)F->width * F->height, s);
   cudaMemsetAsync(F->errFlags.p, 0, sizeof(uint32_t), s);
   if (F->countStats) cudaMemsetAsync(F->counters.p, 0, 24 * sizeof(unsigned long long), s);
   cudaEventRecord(F->evRender, s);
   cudaError_t e = cudaSuccess;
-  if (F->accumID < F->renderer->sampleLimit) {
-    DFrame fr = F->record();
-    const DRenderer &R = F->renderer->r;
+  if (doRender) {
     if (R.type == REND_RAYCAST) {
-      // stage the first volume's TF in shared memory when it fits (64 KB)
-      int stage = 0;
-      if (!W->volsHost.empty() && W->volsHost[0].tfSize <= 4096) stage = W->volsHost[0].tfSize;
-      MarchScratch ms{};
-      const bool segmented = !W->scene.hasSurfaces && R.pixelSamples == 1;
-      if (segmented && !F->ensureMarch()) {
-        dev->report(F, VSR_FRAME, VSR_SEVERITY_ERROR, VSR_ERROR_OUT_OF_MEMORY,
-                    "volume marcher scratch allocation failed");
-        return VSR_ERROR_OUT_OF_MEMORY;
-      }
-      if (segmented) ms = F->march();
       e = launchRaycast(W->scene, F->camera->c, R, fr, stage, F->countStats,
                         segmented ? &ms : nullptr, s);
     } else if (F->renderer->wavefront) {
-      if (!F->ensureWave()) {
-        dev->report(F, VSR_FRAME, VSR_SEVERITY_ERROR, VSR_ERROR_OUT_OF_MEMORY,
-                    "wavefront state allocation failed");
-        return VSR_ERROR_OUT_OF_MEMORY;
-      }
       e = launchPathtraceWavefront(W->scene, F->camera->c, R, fr, F->wave(), F->pinnedCount,
                                    F->countStats, s, &F->lastIterations);
     } else {

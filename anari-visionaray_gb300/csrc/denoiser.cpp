@@ -174,8 +174,12 @@ void Denoiser::conv(int li, const __nv_bfloat16 *x, int xC, __nv_bfloat16 *y, fl
   a.resid = resid;
   a.residC = kInC;
   a.residN = kColorC;
-  if (useTc(W)) launchConv3x3Tc(a, err_, s);
+  if (useTc(W)) launchTc(a, s);
   else launchConv3x3(a, s);
+}
+
+cudaError_t Denoiser::launchTc(const ConvArgs &a, cudaStream_t s) const {
+  return tensorPath_ == 3 ? launchConv3x3Ws(a, err_, s) : launchConv3x3Tc(a, err_, s);
 }
 
 // a decoder convolution on [upsampled coarse level | skip connection],
@@ -200,7 +204,7 @@ void Denoiser::convCat(int li, const __nv_bfloat16 *coarse, int coarseC, const _
   a.N = N;
   a.H = H;
   a.W = W;
-  launchConv3x3Tc(a, err_, s);
+  launchTc(a, s);
 }
 
 // Weight and bias gradients of layer li from its pre-activation gradient dy
@@ -245,7 +249,7 @@ void Denoiser::convBack(int li, const __nv_bfloat16 *x, int xC, const __nv_bfloa
     a.N = N;
     a.H = H;
     a.W = W;
-    if (useTc(W)) launchConv3x3Tc(a, err_, s);
+    if (useTc(W)) launchTc(a, s);
     else launchConv3x3(a, s);
   }
 }

@@ -16,6 +16,8 @@
 
 namespace vsr {
 
+struct ConvArgs;
+
 struct DenoiseLayer {
   int cin, cout;
   size_t w, b;  // offsets of weights [cout][9][cin] and bias [cout] in the parameter array
@@ -48,7 +50,7 @@ class Denoiser {
   float *lossDevice() const { return loss_; }  // one device float for the loss
   // 0: convolutions on mma.sync (kConv3x3); 1: on tcgen05 (kConv3x3Tc) for
   // images at least one 128-pixel tile wide, mma.sync below that; 2:
-  // tcgen05 at every width
+  // tcgen05 at every width; 3: as 1 with the warp-specialised kConv3x3Ws
   void setTensorPath(int path) { tensorPath_ = path; }
   int tensorPath() const { return tensorPath_; }
   unsigned *errorWord() const { return err_; }
@@ -64,7 +66,12 @@ class Denoiser {
   // them); without it the tcgen05 path reads the two parts directly
   cudaError_t run(const __nv_bfloat16 *x, int N, int H, int W, float *out, cudaStream_t s,
                   bool catOut);
-  bool useTc(int W) const { return tensorPath_ == 2 || (tensorPath_ == 1 && W >= 128); }
+  bool useTc(int W) const {
+    return tensorPath_ == 2 || ((tensorPath_ == 1 || tensorPath_ == 3) && W >= 128);
+  }
+  // the tcgen05 convolution: one tile per CTA (kConv3x3Tc), or on path 3
+  // the persistent warp-specialised kernel with TMA loads (kConv3x3Ws)
+  cudaError_t launchTc(const ConvArgs &a, cudaStream_t s) const;
   void convCat(int layer, const __nv_bfloat16 *coarse, int coarseC, const __nv_bfloat16 *skip,
                int skipC, __nv_bfloat16 *y, int yC, int N, int H, int W, cudaStream_t s);
   void conv(int layer, const __nv_bfloat16 *x, int xC, __nv_bfloat16 *y, float *yf, int yC, int N,

@@ -76,7 +76,7 @@ __device__ __forceinline__ uint32_t smemAddr(const void *p) {
 
 __device__ __forceinline__ void cpAsync16(uint32_t dst, const void *src, bool valid) {
   const int n = valid ? 16 : 0;
-  asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(dst), "l"(src), "r"(n));
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 16, %2;\n" ::"r"(dst), "l"(src), "r"(n));
 }
 
 // shared-memory matrix descriptor: start, leading and stride byte offsets

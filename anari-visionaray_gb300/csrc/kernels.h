@@ -102,6 +102,9 @@ cudaError_t launchConv3x3(const ConvArgs &a, cudaStream_t s);
 // the same convolution on tcgen05 (k_denoise_tc.cu); error: a device word
 // that gets bit 1 if a bounded wait ran out
 cudaError_t launchConv3x3Tc(const ConvArgs &a, unsigned *error, cudaStream_t s);
+// the same on a persistent warp-specialised kernel with TMA loads
+// (k_denoise_ws.cu); split requires up
+cudaError_t launchConv3x3Ws(const ConvArgs &a, unsigned *error, cudaStream_t s);
 cudaError_t launchConvWgrad(const WgradArgs &a, cudaStream_t s);
 cudaError_t launchBiasGrad(const __nv_bfloat16 *dy, int dyC, int dyOff, int C, int P, float *db,
                            cudaStream_t s);

@@ -173,7 +173,8 @@ class Denoiser:
 
     def set_tensor_path(self, path):
         """0: mma.sync convolutions; 1: tcgen05 where a level is at least 128
-        pixels wide, mma.sync below; 2: tcgen05 at every width."""
+        pixels wide, mma.sync below; 2: tcgen05 at every width; 3: as 1 on
+        the persistent warp-specialised kernel with TMA loads."""
         rc = self.lib.vsrDenoiserSetTensorPath(self.dev.handle, self.handle, path)
         if rc:
             raise RuntimeError(f"vsrDenoiserSetTensorPath failed ({rc})")

@@ -60,6 +60,9 @@ def parse():
     p.add_argument("--denoise-train-scenes", type=int, default=64)
     p.add_argument("--denoise-eval-scenes", type=int, default=8)
     p.add_argument("--denoise-steps", type=int, default=4000)
+    p.add_argument("--denoise-forward-only", action="store_true",
+                   help="config 4: time only the 1080p denoiser pass (untrained weights), "
+                        "no data, training or evaluation")
     p.add_argument("--no-batch", dest="batch", action="store_false",
                    help="skip the config-3 batched-rendering measurement")
     return p.parse_args()
@@ -284,6 +287,66 @@ def measure_batch_config3(pkg, dev, steps=3, num_scenes=64):
             "timing": "host wall clock, first call to last frame done; synthetic seeded scenes"}
 
 
+def time_denoiser_1080p(dev, dn, D):
+    """At 1920x1080: path-tracing seconds per sample per pixel, and the
+    median seconds of one denoiser pass (vsrDenoiseFrame: input assembly,
+    network, gate) after 3 warm-up passes."""
+    import torch
+
+    sc = D.training_scene(10001, res=1920, spp=16)
+    sc["frame"]["size"] = (1920, 1080)
+    sc["camera"]["aspect"] = 1920 / 1080
+    h = D.build(dev, sc, variance=True)
+    for _ in range(2):
+        dev.render(h["frame"])
+        dev.wait(h["frame"])
+    pt = []
+    for _ in range(3):
+        dev.render(h["frame"])
+        dev.wait(h["frame"])
+        pt.append(dev.get_float(h["frame"], "duration.render"))
+    pt_s_per_spp = statistics.median(pt) / 16
+    out = torch.zeros((1920 * 1080, 4), dtype=torch.float32, device="cuda")
+    for _ in range(3):
+        dn.denoise_frame(h["frame"], out.data_ptr())
+    ds = []
+    for _ in range(10):
+        tt = time.perf_counter()
+        dn.denoise_frame(h["frame"], out.data_ptr())  # synchronous: returns the retry count
+        ds.append(time.perf_counter() - tt)
+    D.release(dev, h)
+    return pt_s_per_spp, statistics.median(ds)
+
+
+DENOISER_LAYERS = [(16, 32, 0), (32, 32, 0), (32, 64, 1), (64, 64, 1), (64, 128, 2), (128, 128, 2),
+                   (128, 256, 3), (256, 256, 3), (384, 128, 2), (128, 128, 2), (192, 64, 1),
+                   (64, 64, 1), (96, 32, 0), (32, 32, 0), (32, 16, 0)]
+
+
+def denoiser_roofline(dn_s):
+    flops = sum(2.0 * ci * co * 9 * 1920 * 1080 / 4 ** lvl for ci, co, lvl in DENOISER_LAYERS)
+    peak = measured_peaks_tensor()
+    return {"bound": "tensor", "achieved": flops / dn_s / 1e12, "peak": peak[0],
+            "unit": "TFLOP/s", "frac": flops / dn_s / 1e12 / peak[0],
+            "note": f"denoiser forward at 1920x1080 ({flops / 1e12:.3f} TFLOP incl. "
+                    f"input and gate kernels in the time); peak bf16 {peak[1]}; "
+                    "tcgen05.mma kind::f16 (bf16 -> fp32 in tensor memory) on halo "
+                    "tiles of 4 x 128 pixels; decoders read upsampled level and skip "
+                    "in place"}
+
+
+def measure_denoiser_forward(pkg, dev):
+    """The 1080p denoiser pass alone (weights as initialised; the time does
+    not depend on their values), for profiling the network's kernels."""
+    D = importlib.import_module(pkg.__name__ + ".denoise")
+    dn = pkg.vsr.Denoiser(dev, seed=1)
+    pt_s_per_spp, dn_s = time_denoiser_1080p(dev, dn, D)
+    dn.close()
+    return {"workload": "config4 denoiser forward at 1920x1080 (untrained weights)",
+            "pt_ms_per_spp_1080p": 1e3 * pt_s_per_spp, "denoise_ms_1080p": 1e3 * dn_s,
+            "roofline": denoiser_roofline(dn_s)}
+
+
 def measure_denoiser_config4(pkg, dev, train_scenes=64, eval_scenes=8, steps=4000,
                              train_ref_spp=1024, eval_ref_spp=4096, res=256):
     """Config 4 (learned denoiser): train the U-Net on path-traced pairs
@@ -306,38 +369,10 @@ def measure_denoiser_config4(pkg, dev, train_scenes=64, eval_scenes=8, steps=400
     levels = (4, 8, 12, 16, 20, 24, 32, 64)  # frames accumulate 4 spp per render
     ev = D.evaluate(dev, dn, list(range(10001, 10001 + eval_scenes)), res=res,
                     ref_spp=eval_ref_spp, denoise_levels=levels)
-    # 1920x1080: path-tracing time per sample per pixel, and the denoiser
-    sc = D.training_scene(10001, res=1920, spp=16)
-    sc["frame"]["size"] = (1920, 1080)
-    sc["camera"]["aspect"] = 1920 / 1080
-    h = D.build(dev, sc, variance=True)
-    for _ in range(2):
-        dev.render(h["frame"])
-        dev.wait(h["frame"])
-    pt = []
-    for _ in range(3):
-        dev.render(h["frame"])
-        dev.wait(h["frame"])
-        pt.append(dev.get_float(h["frame"], "duration.render"))
-    pt_s_per_spp = statistics.median(pt) / 16
-    out = torch.zeros((1920 * 1080, 4), dtype=torch.float32, device="cuda")
-    for _ in range(3):
-        dn.denoise_frame(h["frame"], out.data_ptr())
-    ds = []
-    for _ in range(10):
-        tt = time.perf_counter()
-        dn.denoise_frame(h["frame"], out.data_ptr())  # synchronous: returns the retry count
-        ds.append(time.perf_counter() - tt)
-    dn_s = statistics.median(ds)
-    D.release(dev, h)
+    pt_s_per_spp, dn_s = time_denoiser_1080p(dev, dn, D)
     dn.close()
     goal, t_plain, s_dn, t_dn = D.time_to_rmse(ev["plain"]["rmse_tm"], ev["denoised"]["rmse_tm"],
                                                pt_s_per_spp, dn_s)
-    layers = [(16, 32, 0), (32, 32, 0), (32, 64, 1), (64, 64, 1), (64, 128, 2), (128, 128, 2),
-              (128, 256, 3), (256, 256, 3), (384, 128, 2), (128, 128, 2), (192, 64, 1), (64, 64, 1),
-              (96, 32, 0), (32, 32, 0), (32, 16, 0)]
-    flops = sum(2.0 * ci * co * 9 * 1920 * 1080 / 4 ** lvl for ci, co, lvl in layers)
-    peak = measured_peaks_tensor()
     return {
         "workload": f"config4 denoiser: {train_scenes} training scenes x 4 input spp levels "
                     f"({res}^2, {train_ref_spp}-spp references), {steps} Adam steps of 16 "
@@ -352,13 +387,7 @@ def measure_denoiser_config4(pkg, dev, train_scenes=64, eval_scenes=8, steps=400
         "pt_ms_per_spp_1080p": 1e3 * pt_s_per_spp, "denoise_ms_1080p": 1e3 * dn_s,
         "train_s": train_s, "train_ms_per_step": 1e3 * train_s / steps, "data_s": data_s,
         "loss": losses,
-        "roofline": {"bound": "tensor", "achieved": flops / dn_s / 1e12, "peak": peak[0],
-                     "unit": "TFLOP/s", "frac": flops / dn_s / 1e12 / peak[0],
-                     "note": f"denoiser forward at 1920x1080 ({flops / 1e12:.3f} TFLOP incl. "
-                             f"input and gate kernels in the time); peak bf16 {peak[1]}; "
-                             "tcgen05.mma kind::f16 (bf16 -> fp32 in tensor memory) on halo "
-                             "tiles of 4 x 128 pixels; decoders read upsampled level and skip "
-                             "in place"},
+        "roofline": denoiser_roofline(dn_s),
     }
 
 
@@ -526,9 +555,14 @@ def run_ours(args):
 
     raycast = measure_raycast_config0(pkg, dev, flush) if args.raycast else None
     batch = measure_batch_config3(pkg, dev) if args.batch else None
-    denoiser = (measure_denoiser_config4(pkg, dev, train_scenes=args.denoise_train_scenes,
-                                         eval_scenes=args.denoise_eval_scenes,
-                                         steps=args.denoise_steps) if args.denoise else None)
+    if not args.denoise:
+        denoiser = None
+    elif args.denoise_forward_only:
+        denoiser = measure_denoiser_forward(pkg, dev)
+    else:
+        denoiser = measure_denoiser_config4(pkg, dev, train_scenes=args.denoise_train_scenes,
+                                            eval_scenes=args.denoise_eval_scenes,
+                                            steps=args.denoise_steps)
     volume = (measure_volume_config2(pkg, dev, flush, res=args.volume_res, spp=args.volume_spp)
               if args.volume else None)
 

@@ -210,7 +210,8 @@ VSR_API VSRStatus vsrDenoiserGetParameters(VSRDevice d, VSRDenoiser n, float *pa
                                            uint64_t count);
 /* Which tensor-core path the convolutions take: 0 warp-level mma.sync,
    1 (default) tcgen05 with the accumulators in tensor memory for levels at
-   least 128 pixels wide (mma.sync below), 2 tcgen05 at every width. On the
+   least 128 pixels wide (mma.sync below), 2 tcgen05 at every width, 3 as 1
+   on a persistent warp-specialised kernel with TMA loads. On the
    tcgen05 path the forward reads each decoder's upsampled input and skip
    connection in place instead of writing their concatenation.
    vsrDenoiserErrors returns the device error word of the tcgen05 path (bit

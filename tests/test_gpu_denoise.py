@@ -102,7 +102,7 @@ def test_gradients_match_oracle(net):
 
 
 @pytest.mark.parametrize("shape,path", [((2, 16, 16), 2), ((1, 24, 40), 2), ((1, 24, 136), 1),
-                                        ((2, 16, 256), 1)])
+                                        ((2, 16, 256), 1), ((1, 24, 136), 3), ((2, 16, 256), 3)])
 def test_tcgen05_path_matches_oracle(net, shape, path):
     """The tcgen05 convolutions (accumulators in tensor memory) in forward,
     where the decoders read the upsampled level and the skip connection in
@@ -110,7 +110,8 @@ def test_tcgen05_path_matches_oracle(net, shape, path):
     parameter gradients as the oracle. Path 2 runs every level on tcgen05
     (tiles of 4 rows x 128 pixels far wider than these images, rows not a
     multiple of 4 at 24 / 8 = 3); path 1 switches to mma.sync below 128
-    pixels (136: a second, nearly empty tile; 256: two levels on each)."""
+    pixels (136: a second, nearly empty tile; 256: two levels on each);
+    path 3 is path 1 on the warp-specialised kernel with TMA loads."""
     import torch
     n, h, w = shape
     params = perturbed_params(5, 11)

@@ -47,7 +47,7 @@ cudaError_t alloc(T *&p, size_t n, std::vector<void *> *track = nullptr) {
 }  // namespace
 
 Denoiser::Denoiser(uint64_t seed) {
-  size_t off = 0, offT = 0;
+  size_t off = 0, offT = 0, offP = 0;
   for (auto &io : kLayerIO) {
     DenoiseLayer L;
     L.cin = io[0];
@@ -58,13 +58,19 @@ Denoiser::Denoiser(uint64_t seed) {
     off += L.cout;
     L.wt = offT;
     offT += (size_t)L.cout * 9 * L.cin;
+    L.wp = offP;
+    offP += packedConvWeights(L.cin, L.cout);
+    L.wtp = offP;
+    offP += packedConvWeights(L.cout, L.cin);
     layers_.push_back(L);
   }
   numParams_ = off;
   numWt_ = offT;
+  numPacked_ = offP;
   ok_ = alloc(params_, off) == cudaSuccess && alloc(m_, off) == cudaSuccess &&
         alloc(v_, off) == cudaSuccess && alloc(grad_, off) == cudaSuccess &&
         alloc(wbf_, off) == cudaSuccess && alloc(wt_, offT) == cudaSuccess &&
+        alloc(wpk_, offP) == cudaSuccess &&
         alloc(loss_, 1) == cudaSuccess && alloc(err_, 1) == cudaSuccess &&
         cudaMemset(err_, 0, sizeof(unsigned)) == cudaSuccess;
   if (!ok_) return;
@@ -86,7 +92,7 @@ Denoiser::Denoiser(uint64_t seed) {
 
 Denoiser::~Denoiser() {
   for (void *p : {(void *)params_, (void *)m_, (void *)v_, (void *)grad_, (void *)wbf_, (void *)wt_,
-                  (void *)loss_, (void *)err_})
+                  (void *)wpk_, (void *)loss_, (void *)err_})
     if (p) cudaFree(p);
   for (void *p : bufs_) cudaFree(p);
 }
@@ -112,7 +118,18 @@ cudaError_t Denoiser::setParams(const float *host, cudaStream_t s) {
     e = launchAdam(params_ + L.w, m_ + L.w, v_ + L.w, grad_ + L.w, (size_t)L.cout * 9 * L.cin, 0.f,
                    0.9f, 0.999f, 1e-8f, 1, wbf_ + L.w, wt_ + L.wt, L.cin, L.cout, s);
   }
+  if (e == cudaSuccess) e = pack(s);
   if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  return e;
+}
+
+cudaError_t Denoiser::pack(cudaStream_t s) {
+  cudaError_t e = cudaSuccess;
+  for (const DenoiseLayer &L : layers_) {
+    if (e == cudaSuccess) e = launchPackConvWeights(wbf_ + L.w, L.cin, L.cout, wpk_ + L.wp, s);
+    // the input gradient's weights: cout input channels, cin output channels
+    if (e == cudaSuccess) e = launchPackConvWeights(wt_ + L.wt, L.cout, L.cin, wpk_ + L.wtp, s);
+  }
   return e;
 }
 
@@ -129,7 +146,7 @@ cudaError_t Denoiser::ensure(int N, int H, int W, bool train) {
   struct Sz {
     __nv_bfloat16 *Act::*f;
     size_t n;
-  } sizes[] = {{&Act::a0, P0 * 32},   {&Act::e0, P0 * 32},   {&Act::p0, P1 * 32},
+  } sizes[] = {{&Act::x0, P0 * kInC}, {&Act::a0, P0 * 32},   {&Act::e0, P0 * 32},   {&Act::p0, P1 * 32},
                {&Act::a1, P1 * 64},   {&Act::e1, P1 * 64},   {&Act::p1, P2 * 64},
                {&Act::a2, P2 * 128},  {&Act::e2, P2 * 128},  {&Act::p2, P3 * 128},
                {&Act::a3, P3 * 256},  {&Act::e3, P3 * 256},  {&Act::cat2, P2 * 384},
@@ -162,6 +179,7 @@ void Denoiser::conv(int li, const __nv_bfloat16 *x, int xC, __nv_bfloat16 *y, fl
   a.xC = xC;
   a.Cin = L.cin;
   a.w = wbf_ + L.w;
+  a.wPacked = wpk_ + L.wp;
   a.bias = params_ + L.b;
   a.Cout = L.cout;
   a.y = y;
@@ -196,6 +214,7 @@ void Denoiser::convCat(int li, const __nv_bfloat16 *coarse, int coarseC, const _
   a.split = coarseC;
   a.Cin = L.cin;
   a.w = wbf_ + L.w;
+  a.wPacked = wpk_ + L.wp;
   a.bias = params_ + L.b;
   a.Cout = L.cout;
   a.y = y;
@@ -241,6 +260,7 @@ void Denoiser::convBack(int li, const __nv_bfloat16 *x, int xC, const __nv_bfloa
     a.xC = L.cout;
     a.Cin = L.cout;
     a.w = wt_ + L.wt;
+    a.wPacked = wpk_ + L.wtp;
     a.Cout = L.cin;
     a.y = dx;
     a.yC = L.cin;
@@ -259,7 +279,8 @@ cudaError_t Denoiser::run(const __nv_bfloat16 *x, int N, int H, int W, float *ou
   const int H1 = H / 2, W1 = W / 2, H2 = H / 4, W2 = W / 4, H3 = H / 8, W3 = W / 8;
   const size_t P0 = (size_t)N * H * W, P1 = P0 / 4, P2 = P0 / 16;
   Act &A = act_;
-  conv(L_E0A, x, kInC, A.a0, nullptr, 32, N, H, W, true, s);
+  launchToBlocked(x, kInC, P0, A.x0, s);
+  conv(L_E0A, A.x0, kInC, A.a0, nullptr, 32, N, H, W, true, s);
   conv(L_E0B, A.a0, 32, A.e0, nullptr, 32, N, H, W, true, s);
   launchMaxPool(A.e0, 32, N, H, W, A.p0, s);
   conv(L_E1A, A.p0, 32, A.a1, nullptr, 64, N, H1, W1, true, s);
@@ -295,7 +316,7 @@ cudaError_t Denoiser::run(const __nv_bfloat16 *x, int N, int H, int W, float *ou
   }
   conv(L_D0B, A.b0, 32, A.d0, nullptr, 32, N, H, W, true, s);
   // the output is a correction of the input's log(1 + colour)
-  conv(L_OUT, A.d0, 32, nullptr, out, kOutC, N, H, W, false, s, x);
+  conv(L_OUT, A.d0, 32, nullptr, out, kOutC, N, H, W, false, s, A.x0);
   return cudaGetLastError();
 }
 
@@ -348,7 +369,7 @@ cudaError_t Denoiser::backward(const __nv_bfloat16 *x, const float *target, int 
   launchMaxPoolGrad(A.e0, G.p0, 32, N, H, W, nullptr, G.e0, s);
   launchCopyChannels(G.cat0, 96, 64, G.e0, 32, 0, 32, P0, 1, s);
   convBack(L_E0B, A.a0, 32, G.e0, G.a0, A.a0, N, H, W, s);
-  convBack(L_E0A, x, kInC, G.a0, nullptr, nullptr, N, H, W, s);
+  convBack(L_E0A, A.x0, kInC, G.a0, nullptr, nullptr, N, H, W, s);
   return cudaGetLastError();
 }
 
@@ -363,6 +384,7 @@ cudaError_t Denoiser::adam(float lr, cudaStream_t s) {
       e = launchAdam(params_ + L.b, m_ + L.b, v_ + L.b, grad_ + L.b, L.cout, lr, 0.9f, 0.999f,
                      1e-8f, step_, nullptr, nullptr, 1, 1, s);
   }
+  if (e == cudaSuccess) e = pack(s);
   return e;
 }
 

@@ -22,6 +22,7 @@ struct DenoiseLayer {
   int cin, cout;
   size_t w, b;  // offsets of weights [cout][9][cin] and bias [cout] in the parameter array
   size_t wt;    // offset of the flipped, transposed bf16 copy [cin][9][cout]
+  size_t wp, wtp;  // offsets of the two copies packed for kConv3x3Ws (packConvWeights)
 };
 
 class Denoiser {
@@ -57,9 +58,11 @@ class Denoiser {
   int steps() const { return step_; }
 
  private:
+  // activations in channel-blocked planes (actAt, kernels.h); x0 is the
+  // network input, converted from the caller's NHWC
   struct Act {
-    __nv_bfloat16 *a0, *e0, *p0, *a1, *e1, *p1, *a2, *e2, *p2, *a3, *e3, *cat2, *b2, *d2, *cat1,
-        *b1, *d1, *cat0, *b0, *d0;
+    __nv_bfloat16 *x0, *a0, *e0, *p0, *a1, *e1, *p1, *a2, *e2, *p2, *a3, *e3, *cat2, *b2, *d2,
+        *cat1, *b1, *d1, *cat0, *b0, *d0;
   };
   cudaError_t ensure(int N, int H, int W, bool train);
   // catOut: write the decoders' concatenated inputs (the backward reads
@@ -86,7 +89,10 @@ class Denoiser {
   float *params_ = nullptr, *m_ = nullptr, *v_ = nullptr, *grad_ = nullptr, *loss_ = nullptr;
   unsigned *err_ = nullptr;
   int tensorPath_ = 1;
-  __nv_bfloat16 *wbf_ = nullptr, *wt_ = nullptr;
+  __nv_bfloat16 *wbf_ = nullptr, *wt_ = nullptr, *wpk_ = nullptr;
+  size_t numPacked_ = 0;
+  // refresh the packed weight copies from wbf_ and wt_
+  cudaError_t pack(cudaStream_t s);
   int step_ = 0;
   // activations (and, for training, their gradients), sized for (N, H, W)
   int n_ = 0, h_ = 0, w_ = 0;

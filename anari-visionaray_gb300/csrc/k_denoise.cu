@@ -1,5 +1,6 @@
-// Denoiser kernels: a U-Net of 3x3 convolutions over NHWC bf16 activations
-// with fp32 accumulation, its backward pass, and Adam.
+// Denoiser kernels: a U-Net of 3x3 convolutions over bf16 activations in
+// channel-blocked planes (actAt in kernels.h) with fp32 accumulation, its
+// backward pass, and Adam.
 //
 // Convolutions are implicit GEMMs on the tensor cores (mma.sync m16n8k16
 // bf16 -> fp32): the forward pass and the input gradient are one kernel
@@ -92,7 +93,7 @@ __global__ void __launch_bounds__(128) kConv3x3(ConvArgs a) {
     const int dy = tap / 3 - 1, dx = tap % 3 - 1;
     const int yy = py + dy, xx = px + dx;
     const bool ok = pIn && yy >= 0 && yy < a.H && xx >= 0 && xx < a.W;
-    const bf16 *src = a.x + (ok ? (((size_t)pn * a.H + yy) * a.W + xx) * a.xC + a.xOff + c0 : 0);
+    const bf16 *src = a.x + (ok ? actAt(P, ((size_t)pn * a.H + yy) * a.W + xx, a.xOff + c0) : 0);
     cpAsync16(&As[stage][lr][lh * 8], src, ok);
     if (lr < BN) {
       const bool wok = co < a.Cout;
@@ -151,20 +152,23 @@ __global__ void __launch_bounds__(128) kConv3x3(ConvArgs a) {
           v1 = fmaxf(v1, 0.f);
         }
         if (a.resid) {
-          const bf16 *r = a.resid + (size_t)pp * a.residC + c;
+          const bf16 *r = a.resid + actAt(P, pp, c);  // c, c + 1 in one 8-channel block
           if (c < a.residN) v0 += __bfloat162float(r[0]);
           if (c + 1 < a.residN) v1 += __bfloat162float(r[1]);
         }
         if (a.mask) {
-          const bf16 *m = a.mask + (size_t)pp * a.maskC + a.maskOff + c;
+          const bf16 *m = a.mask + actAt(P, pp, a.maskOff + c);
           if (c < a.Cout && !(__bfloat162float(m[0]) > 0.f)) v0 = 0.f;
           if (c + 1 < a.Cout && !(__bfloat162float(m[1]) > 0.f)) v1 = 0.f;
         }
-        const size_t o = (size_t)pp * a.yC + a.yOff + c;
-        if (a.yf) {
+        if (a.yf) {  // fp32 output: NHWC
+          const size_t o = (size_t)pp * a.yC + a.yOff + c;
           if (c < a.Cout) a.yf[o] = v0;
           if (c + 1 < a.Cout) a.yf[o + 1] = v1;
-        } else if (c + 1 < a.Cout) {
+          continue;
+        }
+        const size_t o = actAt(P, pp, a.yOff + c);
+        if (c + 1 < a.Cout) {
           *reinterpret_cast<__nv_bfloat162 *>(a.y + o) = __floats2bfloat162_rn(v0, v1);
         } else if (c < a.Cout) {
           a.y[o] = __float2bfloat16(v0);
@@ -192,8 +196,9 @@ __global__ void __launch_bounds__(128) kConvWgrad(WgradArgs a) {
   const int pStart = blockIdx.z * a.chunk;
   const int pEnd = min(P, pStart + a.chunk);
   const int steps = pEnd > pStart ? (pEnd - pStart + kBK - 1) / kBK : 0;
-  // loads: 16 pixels x 64 channels = 128 x 16 B for each of Ds and Xs
-  const int lr = tid >> 3, lc = (tid & 7) * 8;
+  // loads: 16 pixels x 64 channels = 128 x 16 B for each of Ds and Xs,
+  // consecutive threads on consecutive pixels of one 8-channel block
+  const int lr = tid & 15, lc = (tid >> 4) * 8;
   auto load = [&](int stage, int step) {
     const int p = pStart + step * kBK + lr;
     const bool pIn = p < pEnd;
@@ -205,12 +210,11 @@ __global__ void __launch_bounds__(128) kConvWgrad(WgradArgs a) {
       pn = t / a.H;
     }
     const bool dok = pIn && coBase + lc < a.Cout;
-    cpAsync16(&Ds[stage][lr][lc], a.dy + (dok ? (size_t)p * a.dyC + a.dyOff + coBase + lc : 0),
-              dok);
+    cpAsync16(&Ds[stage][lr][lc], a.dy + (dok ? actAt(P, p, a.dyOff + coBase + lc) : 0), dok);
     const int yy = py + dy, xx = px + dx;
     const bool xok = pIn && yy >= 0 && yy < a.H && xx >= 0 && xx < a.W && ciBase + lc < a.Cin;
     cpAsync16(&Xs[stage][lr][lc],
-              a.x + (xok ? (((size_t)pn * a.H + yy) * a.W + xx) * a.xC + a.xOff + ciBase + lc : 0),
+              a.x + (xok ? actAt(P, ((size_t)pn * a.H + yy) * a.W + xx, a.xOff + ciBase + lc) : 0),
               xok);
   };
   float acc[2][4][4];
@@ -266,35 +270,66 @@ __global__ void __launch_bounds__(128) kConvWgrad(WgradArgs a) {
     }
 }
 
-// db[c] += sum over pixels of dY[p][c]
-__global__ void kBiasGrad(const bf16 *dy, int dyC, int dyOff, int C, int P, float *db) {
-  const int c = blockIdx.y * 32 + (threadIdx.x & 31);
-  if (c >= C) return;
-  float s = 0.f;
-  for (int p = blockIdx.x * 8 + (threadIdx.x >> 5); p < P; p += gridDim.x * 8)
-    s += __bfloat162float(dy[(size_t)p * dyC + dyOff + c]);
-  atomicAdd(db + c, s);
+// db[c] += sum over pixels of dY[p][c]: one 8-channel block per blockIdx.y,
+// 16 bytes per thread and pixel
+__global__ void __launch_bounds__(256) kBiasGrad(const bf16 *dy, int dyOff, size_t P, float *db) {
+  const int blk = blockIdx.y;
+  const int c0 = dyOff + 8 * blk;
+  float s[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+  for (size_t p = blockIdx.x * (size_t)blockDim.x + threadIdx.x; p < P;
+       p += (size_t)gridDim.x * blockDim.x) {
+    const uint4 v = *reinterpret_cast<const uint4 *>(dy + actAt(P, p, c0));
+    const bf16 *e = reinterpret_cast<const bf16 *>(&v);
+#pragma unroll
+    for (int k = 0; k < 8; ++k) s[k] += __bfloat162float(e[k]);
+  }
+  __shared__ float red[8][256];
+#pragma unroll
+  for (int k = 0; k < 8; ++k) red[k][threadIdx.x] = s[k];
+  __syncthreads();
+  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+    if ((int)threadIdx.x < o)
+#pragma unroll
+      for (int k = 0; k < 8; ++k) red[k][threadIdx.x] += red[k][threadIdx.x + o];
+    __syncthreads();
+  }
+  if (threadIdx.x < 8) atomicAdd(db + 8 * blk + threadIdx.x, red[threadIdx.x][0]);
 }
 
 // --------------------------------------------------- layout and elementwise
+// Every thread below handles one 8-channel block of one pixel (16 bytes).
+__device__ __forceinline__ uint4 ld16(const bf16 *p) { return *reinterpret_cast<const uint4 *>(p); }
+__device__ __forceinline__ void st16(bf16 *p, uint4 v) { *reinterpret_cast<uint4 *>(p) = v; }
+__device__ __forceinline__ float el(const uint4 &v, int k) {
+  return __bfloat162float(reinterpret_cast<const bf16 *>(&v)[k]);
+}
+__device__ __forceinline__ void setEl(uint4 &v, int k, float f) {
+  reinterpret_cast<bf16 *>(&v)[k] = __float2bfloat16(f);
+}
+
 // 2x2 max pooling (H, W even)
 __global__ void kMaxPool(const bf16 *x, int C, int N, int H, int W, bf16 *y) {
   const int Ho = H / 2, Wo = W / 2;
-  const size_t n = (size_t)N * Ho * Wo * C;
+  const size_t Pi = (size_t)N * H * W, Po = (size_t)N * Ho * Wo;
+  const size_t n = Po * (C / 8);
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n;
        i += (size_t)gridDim.x * blockDim.x) {
-    const int c = (int)(i % C);
-    size_t q = i / C;
-    const int xo = (int)(q % Wo);
-    q /= Wo;
+    const int blk = (int)(i / Po);
+    const size_t po = i % Po;
+    const int xo = (int)(po % Wo);
+    const size_t q = po / Wo;
     const int yo = (int)(q % Ho);
     const int b = (int)(q / Ho);
-    const bf16 *s = x + (((size_t)b * H + 2 * yo) * W + 2 * xo) * C + c;
-    float m = __bfloat162float(s[0]);
-    m = fmaxf(m, __bfloat162float(s[C]));
-    m = fmaxf(m, __bfloat162float(s[(size_t)W * C]));
-    m = fmaxf(m, __bfloat162float(s[(size_t)W * C + C]));
-    y[i] = __float2bfloat16(m);
+    const size_t p0 = ((size_t)b * H + 2 * yo) * W + 2 * xo;
+    const size_t pin[4] = {p0, p0 + 1, p0 + W, p0 + W + 1};
+    uint4 v[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) v[k] = ld16(x + actAt(Pi, pin[k], 8 * blk));
+    uint4 o;
+#pragma unroll
+    for (int e = 0; e < 8; ++e)
+      setEl(o, e, fmaxf(fmaxf(el(v[0], e), el(v[1], e)), fmaxf(el(v[2], e), el(v[3], e))));
+    st16(y + actAt(Po, po, 8 * blk), o);
   }
 }
 
@@ -303,105 +338,166 @@ __global__ void kMaxPool(const bf16 *x, int C, int N, int H, int W, bf16 *y) {
 __global__ void kMaxPoolGrad(const bf16 *x, const bf16 *dy, int C, int N, int H, int W,
                              const bf16 *mask, bf16 *dx) {
   const int Ho = H / 2, Wo = W / 2;
-  const size_t n = (size_t)N * Ho * Wo * C;
+  const size_t Pi = (size_t)N * H * W, Po = (size_t)N * Ho * Wo;
+  const size_t n = Po * (C / 8);
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n;
        i += (size_t)gridDim.x * blockDim.x) {
-    const int c = (int)(i % C);
-    size_t q = i / C;
-    const int xo = (int)(q % Wo);
-    q /= Wo;
+    const int blk = (int)(i / Po);
+    const size_t po = i % Po;
+    const int xo = (int)(po % Wo);
+    const size_t q = po / Wo;
     const int yo = (int)(q % Ho);
     const int b = (int)(q / Ho);
-    const size_t base = (((size_t)b * H + 2 * yo) * W + 2 * xo) * C + c;
-    const size_t off[4] = {0, (size_t)C, (size_t)W * C, (size_t)W * C + C};
-    int arg = 0;
-    float m = __bfloat162float(x[base]);
-    for (int k = 1; k < 4; ++k) {
-      const float v = __bfloat162float(x[base + off[k]]);
-      if (v > m) {
-        m = v;
-        arg = k;
+    const size_t p0 = ((size_t)b * H + 2 * yo) * W + 2 * xo;
+    const size_t pin[4] = {p0, p0 + 1, p0 + W, p0 + W + 1};
+    uint4 v[4], m[4], d[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      v[k] = ld16(x + actAt(Pi, pin[k], 8 * blk));
+      if (mask) m[k] = ld16(mask + actAt(Pi, pin[k], 8 * blk));
+    }
+    const uint4 g = ld16(dy + actAt(Po, po, 8 * blk));
+#pragma unroll
+    for (int e = 0; e < 8; ++e) {
+      int arg = 0;
+      float mx = el(v[0], e);
+      for (int k = 1; k < 4; ++k) {
+        const float f = el(v[k], e);
+        if (f > mx) {
+          mx = f;
+          arg = k;
+        }
+      }
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        float f = k == arg ? el(g, e) : 0.f;
+        if (mask && !(el(m[k], e) > 0.f)) f = 0.f;
+        setEl(d[k], e, f);
       }
     }
-    const float g = __bfloat162float(dy[i]);
-    for (int k = 0; k < 4; ++k) {
-      float v = k == arg ? g : 0.f;
-      if (mask && !(__bfloat162float(mask[base + off[k]]) > 0.f)) v = 0.f;
-      dx[base + off[k]] = __float2bfloat16(v);
-    }
+#pragma unroll
+    for (int k = 0; k < 4; ++k) st16(dx + actAt(Pi, pin[k], 8 * blk), d[k]);
   }
 }
 
-// nearest 2x upsampling of x (C channels) into channels [yOff, yOff + C) of y
-__global__ void kUpsample(const bf16 *x, int C, int N, int H, int W, bf16 *y, int yC, int yOff) {
-  const size_t n = (size_t)N * 2 * H * 2 * W * C;
+// nearest 2x upsampling of x (C channels, N x H x W) into channels
+// [yOff, yOff + C) of y (N x 2H x 2W)
+__global__ void kUpsample(const bf16 *x, int C, int N, int H, int W, bf16 *y, int yOff) {
+  const size_t Pi = (size_t)N * H * W, Po = 4 * Pi;
+  const size_t n = Po * (C / 8);
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n;
        i += (size_t)gridDim.x * blockDim.x) {
-    const int c = (int)(i % C);
-    size_t q = i / C;
-    const int xo = (int)(q % (2 * W));
-    q /= 2 * W;
+    const int blk = (int)(i / Po);
+    const size_t po = i % Po;
+    const int xo = (int)(po % (2 * W));
+    const size_t q = po / (2 * W);
     const int yo = (int)(q % (2 * H));
     const int b = (int)(q / (2 * H));
-    y[(((size_t)b * 2 * H + yo) * 2 * W + xo) * yC + yOff + c] =
-        x[(((size_t)b * H + yo / 2) * W + xo / 2) * C + c];
+    const size_t pi = ((size_t)b * H + yo / 2) * W + xo / 2;
+    st16(y + actAt(Po, po, yOff + 8 * blk), ld16(x + actAt(Pi, pi, 8 * blk)));
   }
 }
 
 // gradient of kUpsample: sum of the four children; with mask, zero where
 // the mask (the upsampled input) is <= 0
-__global__ void kUpsampleGrad(const bf16 *dy, int dyC, int dyOff, int C, int N, int H, int W,
+__global__ void kUpsampleGrad(const bf16 *dy, int dyOff, int C, int N, int H, int W,
                               const bf16 *mask, bf16 *dx) {
-  const size_t n = (size_t)N * H * W * C;
+  const size_t Pi = (size_t)N * H * W, Po = 4 * Pi;
+  const size_t n = Pi * (C / 8);
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n;
        i += (size_t)gridDim.x * blockDim.x) {
-    const int c = (int)(i % C);
-    size_t q = i / C;
-    const int x = (int)(q % W);
-    q /= W;
+    const int blk = (int)(i / Pi);
+    const size_t pi = i % Pi;
+    const int x = (int)(pi % W);
+    const size_t q = pi / W;
     const int yv = (int)(q % H);
     const int b = (int)(q / H);
-    float s = 0.f;
+    float s[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
     for (int k = 0; k < 4; ++k) {
-      const int yy = 2 * yv + (k >> 1), xx = 2 * x + (k & 1);
-      s += __bfloat162float(dy[(((size_t)b * 2 * H + yy) * 2 * W + xx) * dyC + dyOff + c]);
+      const size_t po = ((size_t)b * 2 * H + 2 * yv + (k >> 1)) * 2 * W + 2 * x + (k & 1);
+      const uint4 v = ld16(dy + actAt(Po, po, dyOff + 8 * blk));
+#pragma unroll
+      for (int e = 0; e < 8; ++e) s[e] += el(v, e);
     }
-    if (mask && !(__bfloat162float(mask[i]) > 0.f)) s = 0.f;
-    dx[i] = __float2bfloat16(s);
+    uint4 m, o;
+    if (mask) m = ld16(mask + actAt(Pi, pi, 8 * blk));
+#pragma unroll
+    for (int e = 0; e < 8; ++e) setEl(o, e, (mask && !(el(m, e) > 0.f)) ? 0.f : s[e]);
+    st16(dx + actAt(Pi, pi, 8 * blk), o);
   }
 }
 
 // copy C channels: y[:, yOff:yOff+C] = x[:, xOff:xOff+C]; with add, y += x
-__global__ void kCopyChannels(const bf16 *x, int xC, int xOff, bf16 *y, int yC, int yOff, int C,
-                              size_t P, int add) {
-  const size_t n = P * C;
+__global__ void kCopyChannels(const bf16 *x, int xOff, bf16 *y, int yOff, int C, size_t P,
+                              int add) {
+  const size_t n = P * (C / 8);
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n;
        i += (size_t)gridDim.x * blockDim.x) {
-    const size_t p = i / C;
-    const int c = (int)(i % C);
-    float v = __bfloat162float(x[p * xC + xOff + c]);
-    if (add) v += __bfloat162float(y[p * yC + yOff + c]);
-    y[p * yC + yOff + c] = __float2bfloat16(v);
+    const int blk = (int)(i / P);
+    const size_t p = i % P;
+    uint4 v = ld16(x + actAt(P, p, xOff + 8 * blk));
+    bf16 *d = y + actAt(P, p, yOff + 8 * blk);
+    if (add) {
+      const uint4 w = ld16(d);
+#pragma unroll
+      for (int e = 0; e < 8; ++e) setEl(v, e, el(v, e) + el(w, e));
+    }
+    st16(d, v);
   }
 }
 
 // ReLU backward in place: d *= (post > 0)
-__global__ void kReluMask(bf16 *d, int dC, int dOff, const bf16 *post, int pC, int pOff, int C,
-                          size_t P) {
-  const size_t n = P * C;
+__global__ void kReluMask(bf16 *d, int dOff, const bf16 *post, int pOff, int C, size_t P) {
+  const size_t n = P * (C / 8);
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n;
        i += (size_t)gridDim.x * blockDim.x) {
-    const size_t p = i / C;
-    const int c = (int)(i % C);
-    if (!(__bfloat162float(post[p * pC + pOff + c]) > 0.f))
-      d[p * dC + dOff + c] = __float2bfloat16(0.f);
+    const int blk = (int)(i / P);
+    const size_t p = i % P;
+    bf16 *dp = d + actAt(P, p, dOff + 8 * blk);
+    uint4 v = ld16(dp);
+    const uint4 m = ld16(post + actAt(P, p, pOff + 8 * blk));
+#pragma unroll
+    for (int e = 0; e < 8; ++e)
+      if (!(el(m, e) > 0.f)) setEl(v, e, 0.f);
+    st16(dp, v);
+  }
+}
+
+// NHWC (C channels per pixel) -> channel-blocked planes
+__global__ void kToBlocked(const bf16 *x, int C, size_t P, bf16 *y) {
+  const size_t n = P * (C / 8);
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n;
+       i += (size_t)gridDim.x * blockDim.x) {
+    const int blk = (int)(i / P);
+    const size_t p = i % P;
+    st16(y + actAt(P, p, 8 * blk), ld16(x + p * C + 8 * blk));
+  }
+}
+
+// packed weights for kConv3x3Ws: [nTile][stage][tap][chunk 4][N][8]
+__global__ void kPackConvWeights(const bf16 *w, int Cin, int Cout, int N, int stages, size_t n,
+                                 bf16 *out) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n;
+       i += (size_t)gridDim.x * blockDim.x) {
+    const int e = (int)(i & 7);
+    size_t q = i >> 3;
+    const int co = (int)(q % N);
+    q /= N;
+    const int chunk = (int)(q % 4);
+    q /= 4;
+    const int tap = (int)(q % 9);
+    q /= 9;
+    const int st = (int)(q % stages);
+    const int nt = (int)(q / stages);
+    const int cog = nt * N + co, ci = st * 32 + chunk * 8 + e;
+    out[i] = (cog < Cout && ci < Cin) ? w[((size_t)cog * 9 + tap) * Cin + ci] : __float2bfloat16(0.f);
   }
 }
 
 // L1 loss between the first C channels of the output (fp32 log(1 + colour),
 // oC channels per pixel) and log(1 + target colour) (tC floats per pixel,
-// linear colour), and its gradient (sign / count) in bf16 with gC channels
-// per pixel (the others are left as they are)
+// linear colour), and its gradient (sign / count) in bf16 in blocked planes
+// of gC channels (the others are left as they are)
 __global__ void kL1(const float *out, int oC, const float *target, int tC, int C, size_t P,
                     bf16 *grad, int gC, float *loss) {
   __shared__ float red[256];
@@ -414,7 +510,7 @@ __global__ void kL1(const float *out, int oC, const float *target, int tC, int C
     const int c = (int)(i % C);
     const float d = out[p * oC + c] - log1pf(fmaxf(target[p * tC + c], 0.f));
     s += fabsf(d);
-    grad[p * gC + c] = __float2bfloat16(d > 0.f ? inv : (d < 0.f ? -inv : 0.f));
+    grad[actAt(P, p, c)] = __float2bfloat16(d > 0.f ? inv : (d < 0.f ? -inv : 0.f));
   }
   red[threadIdx.x] = s;
   __syncthreads();
@@ -538,47 +634,84 @@ cudaError_t launchConvWgrad(const WgradArgs &a, cudaStream_t s) {
   return cudaGetLastError();
 }
 
+// The channel-count arguments of views (dyC, yC, ...) only take part in the
+// checks: in blocked planes a view's address depends on its pixel count and
+// first channel.
+static bool blocks8(int C, int off) { return C > 0 && C % 8 == 0 && off % 8 == 0; }
+
 cudaError_t launchBiasGrad(const __nv_bfloat16 *dy, int dyC, int dyOff, int C, int P, float *db,
                            cudaStream_t s) {
-  dim3 grid(min(1024, (P + 7) / 8), (C + 31) / 32);
-  kBiasGrad<<<grid, 256, 0, s>>>(dy, dyC, dyOff, C, P, db);
+  if (!blocks8(C, dyOff) || dyOff + C > dyC) return cudaErrorInvalidValue;
+  dim3 grid(min(256, (P + 255) / 256), C / 8);
+  kBiasGrad<<<grid, 256, 0, s>>>(dy, dyOff, (size_t)P, db);
   return cudaGetLastError();
 }
 
 cudaError_t launchMaxPool(const __nv_bfloat16 *x, int C, int N, int H, int W, __nv_bfloat16 *y,
                           cudaStream_t s) {
-  kMaxPool<<<gridFor((size_t)N * (H / 2) * (W / 2) * C), 256, 0, s>>>(x, C, N, H, W, y);
+  if (!blocks8(C, 0) || H % 2 || W % 2) return cudaErrorInvalidValue;
+  kMaxPool<<<gridFor((size_t)N * (H / 2) * (W / 2) * (C / 8)), 256, 0, s>>>(x, C, N, H, W, y);
   return cudaGetLastError();
 }
 
 cudaError_t launchMaxPoolGrad(const __nv_bfloat16 *x, const __nv_bfloat16 *dy, int C, int N, int H,
                               int W, const __nv_bfloat16 *mask, __nv_bfloat16 *dx, cudaStream_t s) {
-  kMaxPoolGrad<<<gridFor((size_t)N * (H / 2) * (W / 2) * C), 256, 0, s>>>(x, dy, C, N, H, W, mask,
-                                                                        dx);
+  if (!blocks8(C, 0) || H % 2 || W % 2) return cudaErrorInvalidValue;
+  kMaxPoolGrad<<<gridFor((size_t)N * (H / 2) * (W / 2) * (C / 8)), 256, 0, s>>>(x, dy, C, N, H, W,
+                                                                              mask, dx);
   return cudaGetLastError();
 }
 
 cudaError_t launchUpsample(const __nv_bfloat16 *x, int C, int N, int H, int W, __nv_bfloat16 *y,
                            int yC, int yOff, cudaStream_t s) {
-  kUpsample<<<gridFor((size_t)N * 4 * H * W * C), 256, 0, s>>>(x, C, N, H, W, y, yC, yOff);
+  if (!blocks8(C, yOff) || yOff + C > yC) return cudaErrorInvalidValue;
+  kUpsample<<<gridFor((size_t)N * 4 * H * W * (C / 8)), 256, 0, s>>>(x, C, N, H, W, y, yOff);
   return cudaGetLastError();
 }
 
 cudaError_t launchUpsampleGrad(const __nv_bfloat16 *dy, int dyC, int dyOff, int C, int N, int H,
                                int W, const __nv_bfloat16 *mask, __nv_bfloat16 *dx, cudaStream_t s) {
-  kUpsampleGrad<<<gridFor((size_t)N * H * W * C), 256, 0, s>>>(dy, dyC, dyOff, C, N, H, W, mask, dx);
+  if (!blocks8(C, dyOff) || dyOff + C > dyC) return cudaErrorInvalidValue;
+  kUpsampleGrad<<<gridFor((size_t)N * H * W * (C / 8)), 256, 0, s>>>(dy, dyOff, C, N, H, W, mask,
+                                                                   dx);
   return cudaGetLastError();
 }
 
 cudaError_t launchCopyChannels(const __nv_bfloat16 *x, int xC, int xOff, __nv_bfloat16 *y, int yC,
                                int yOff, int C, size_t P, int add, cudaStream_t s) {
-  kCopyChannels<<<gridFor(P * C), 256, 0, s>>>(x, xC, xOff, y, yC, yOff, C, P, add);
+  if (!blocks8(C, xOff) || !blocks8(C, yOff) || xOff + C > xC || yOff + C > yC)
+    return cudaErrorInvalidValue;
+  kCopyChannels<<<gridFor(P * (C / 8)), 256, 0, s>>>(x, xOff, y, yOff, C, P, add);
   return cudaGetLastError();
 }
 
 cudaError_t launchReluMask(__nv_bfloat16 *d, int dC, int dOff, const __nv_bfloat16 *post, int pC,
                            int pOff, int C, size_t P, cudaStream_t s) {
-  kReluMask<<<gridFor(P * C), 256, 0, s>>>(d, dC, dOff, post, pC, pOff, C, P);
+  if (!blocks8(C, dOff) || !blocks8(C, pOff) || dOff + C > dC || pOff + C > pC)
+    return cudaErrorInvalidValue;
+  kReluMask<<<gridFor(P * (C / 8)), 256, 0, s>>>(d, dOff, post, pOff, C, P);
+  return cudaGetLastError();
+}
+
+cudaError_t launchToBlocked(const __nv_bfloat16 *x, int C, size_t P, __nv_bfloat16 *y,
+                            cudaStream_t s) {
+  if (!blocks8(C, 0)) return cudaErrorInvalidValue;
+  kToBlocked<<<gridFor(P * (C / 8)), 256, 0, s>>>(x, C, P, y);
+  return cudaGetLastError();
+}
+
+size_t packedConvWeights(int Cin, int Cout) {
+  const int N = Cout <= 32 ? 32 : 64;
+  const size_t nTiles = (size_t)(Cout + N - 1) / N, stages = (size_t)(Cin + 31) / 32;
+  return nTiles * stages * 9 * 4 * N * 8;
+}
+
+cudaError_t launchPackConvWeights(const __nv_bfloat16 *w, int Cin, int Cout, __nv_bfloat16 *packed,
+                                  cudaStream_t s) {
+  if (Cin <= 0 || Cout <= 0 || Cin % 16) return cudaErrorInvalidValue;
+  const int N = Cout <= 32 ? 32 : 64;
+  const size_t n = packedConvWeights(Cin, Cout);
+  kPackConvWeights<<<gridFor(n), 256, 0, s>>>(w, Cin, Cout, N, (Cin + 31) / 32, n, packed);
   return cudaGetLastError();
 }
 

@@ -30,7 +30,8 @@
 // the accumulators with tcgen05.ld (warp w: pixels 32w..32w+31 of the tile
 // row, one pixel per thread) and applies bias, ReLU, the residual and the
 // mask of a previous ReLU, in the same order and with the same results as
-// kConv3x3.
+// kConv3x3. Activations are channel-blocked planes (actAt, kernels.h): a
+// warp's halo loads and output stores cover contiguous rows of one block.
 //
 // The input can be the concatenation of two tensors, the first one at half
 // resolution (a U-Net decoder's upsampled coarse level and its skip
@@ -181,16 +182,18 @@ __global__ void __launch_bounds__(128) kConv3x3Tc(ConvArgs a, int tilesX, int ti
     const int srcOff = second ? a.x2Off + c0 - a.split : a.xOff + c0;
     const int sh = (!second && a.up) ? 1 : 0;
     const int srcH = a.H >> sh, srcW = a.W >> sh;
-    // the halo: chunk fastest, so that a pixel's channels are read together
+    const size_t srcP = (size_t)a.N * srcH * srcW;
+    // the halo: pixel fastest, so that a warp reads a row of one 8-channel
+    // block (contiguous in blocked planes)
     const int haloEntries = chunks * kHY * kHXUsed;
     for (int i = tid; i < haloEntries; i += 128) {
-      const int c = i % chunks;
-      const int r = i / chunks;
-      const int hx = r % kHXUsed, hy = r / kHXUsed;
+      const int hx = i % kHXUsed;
+      const int r = i / kHXUsed;
+      const int c = r % chunks, hy = r / chunks;
       const int y = y0 - 1 + hy, x = x0 - 1 + hx;
       const bool in = y >= 0 && y < a.H && x >= 0 && x < a.W;
       const size_t pix = ((size_t)n * srcH + (y >> sh)) * srcW + (x >> sh);
-      const bf16 *src = srcBase + (in ? pix * srcC + srcOff + 8 * c : 0);
+      const bf16 *src = srcBase + (in ? actAt(srcP, pix, srcOff + 8 * c) : 0);
       cpAsync16(haloBase + (uint32_t)(c * kPlane + (hy * kHX + hx) * 16), src, in);
     }
     // the weights of the nine taps
@@ -247,7 +250,7 @@ __global__ void __launch_bounds__(128) kConv3x3Tc(ConvArgs a, int tilesX, int ti
   asm volatile("tcgen05.fence::after_thread_sync;\n" ::);
   if (ok) {
     const int x = x0 + warp * 32 + lane;
-    const bool vec = a.yf == nullptr && (a.yC % 8) == 0 && (a.yOff % 8) == 0;
+    const size_t P = (size_t)a.N * a.H * a.W;
 #pragma unroll 1
     for (int r = 0; r < kR; ++r) {
       const int y = y0 + r;
@@ -272,30 +275,33 @@ __global__ void __launch_bounds__(128) kConv3x3Tc(ConvArgs a, int tilesX, int ti
           const int cb = nBase + c32 * 32 + g;
           if (cb >= a.Cout) break;
           float o[8];
+          // 16-byte blocks of the residual and the mask (blocked planes)
+          uint4 rv = make_uint4(0, 0, 0, 0), mv = make_uint4(0, 0, 0, 0);
+          if (a.resid && cb < a.residN) rv = *reinterpret_cast<const uint4 *>(a.resid + actAt(P, pp, cb));
+          if (a.mask) mv = *reinterpret_cast<const uint4 *>(a.mask + actAt(P, pp, a.maskOff + cb));
 #pragma unroll
           for (int k = 0; k < 8; ++k) {
             const int c = cb + k;
             float val = __uint_as_float(v[g + k]);
             if (a.bias && c < a.Cout) val += a.bias[c];
             if (a.relu) val = fmaxf(val, 0.f);
-            if (a.resid && c < a.residN) val += __bfloat162float(a.resid[pp * a.residC + c]);
-            if (a.mask && c < a.Cout && !(__bfloat162float(a.mask[pp * a.maskC + a.maskOff + c]) > 0.f))
+            if (a.resid && c < a.residN)
+              val += __bfloat162float(reinterpret_cast<const bf16 *>(&rv)[k]);
+            if (a.mask && !(__bfloat162float(reinterpret_cast<const bf16 *>(&mv)[k]) > 0.f))
               val = 0.f;
             o[k] = val;
           }
-          const size_t ob = pp * a.yC + a.yOff + cb;
-          if (vec && cb + 8 <= a.Cout) {
+          if (a.yf) {  // fp32 output: NHWC
+            const size_t ob = pp * a.yC + a.yOff + cb;
+#pragma unroll
+            for (int k = 0; k < 8; ++k)
+              if (cb + k < a.Cout) a.yf[ob + k] = o[k];
+          } else {
+            // Cout is a multiple of 16: whole 8-channel blocks
             __nv_bfloat162 h[4];
 #pragma unroll
             for (int k = 0; k < 4; ++k) h[k] = __floats2bfloat162_rn(o[2 * k], o[2 * k + 1]);
-            *reinterpret_cast<uint4 *>(a.y + ob) = *reinterpret_cast<const uint4 *>(h);
-          } else {
-#pragma unroll
-            for (int k = 0; k < 8; ++k) {
-              if (cb + k >= a.Cout) break;
-              if (a.yf) a.yf[ob + k] = o[k];
-              else a.y[ob + k] = __float2bfloat16(o[k]);
-            }
+            *reinterpret_cast<uint4 *>(a.y + actAt(P, pp, a.yOff + cb)) = *reinterpret_cast<const uint4 *>(h);
           }
         }
       }
@@ -324,6 +330,10 @@ cudaError_t launchTc(const ConvArgs &a, unsigned *error, cudaStream_t s) {
 
 cudaError_t launchConv3x3Tc(const ConvArgs &a, unsigned *error, cudaStream_t s) {
   if (a.Cin <= 0 || a.Cin % 16 || a.Cout <= 0 || a.xC % 8 || a.xOff % 8 || !error)
+    return cudaErrorInvalidValue;
+  // bf16 outputs, masks and residuals in whole 8-channel blocks
+  if ((!a.yf && (a.Cout % 8 || a.yOff % 8)) || (a.mask && a.maskOff % 8) ||
+      (a.resid && a.residN > 8 * ((a.residC + 7) / 8)))
     return cudaErrorInvalidValue;
   if (a.split && (a.split < 0 || a.split % 32 || a.split >= a.Cin || !a.x2 || a.x2C % 8 ||
                   a.x2Off % 8 || a.x2Off + a.Cin - a.split > a.x2C))

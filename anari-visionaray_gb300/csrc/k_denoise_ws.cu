@@ -6,32 +6,35 @@
 // channels in stages of 32. One CTA per SM walks its share of the tiles.
 // Three roles run concurrently, linked by mbarriers:
 //
-//   warp 0     producer: for each stage it waits for a free slot of a 2- or
-//              3-slot shared-memory ring, then loads the stage's weights
-//              (one TMA box of 8 channels x 1 tap x N output channels per
-//              tap and chunk) and its input halo (one TMA box of 8 channels
-//              x 130 pixels x 6 rows per chunk; the tensor map zero-fills
-//              outside the image). A decoder's upsampled input (read at
-//              (y / 2, x / 2) of the coarser level) cannot be one box: for
-//              those stages the 32 lanes gather the halo with cp.async
-//              instead. The slot's "full" barrier counts the TMA bytes and
-//              the lanes' cp.async completions.
-//   warp 1     MMA: one thread waits for a full slot, issues the stage's
-//              4 x 9 x 2 tcgen05.mma (bf16 x bf16 -> fp32) into one of two
-//              accumulator sets in tensor memory, and commits them to the
-//              slot's "empty" barrier, and after a tile's last stage to the
-//              set's "full" barrier.
-//   warps 2-5  epilogue: wait for an accumulator set, read it with
-//              tcgen05.ld (warp w reads lanes 32 (w % 4) ...), apply bias,
-//              ReLU, residual and mask like kConv3x3, store, and release
-//              the set; meanwhile the MMA thread fills the other set.
+//   warps 5-8  producer: for each stage they wait for a free slot of a 2- or
+//              3-slot shared-memory ring; one thread loads the stage's
+//              weights (one bulk copy of their packed shared-memory image,
+//              packConvWeights) and its input halo: activations are
+//              channel-blocked planes (actAt, kernels.h), so 4 blocks x 6
+//              rows x 130 pixels x 8 channels is one 5-d TMA box whose rows
+//              are contiguous; the tensor map zero-fills outside the image.
+//              A decoder's upsampled input (read at (y / 2, x / 2) of the
+//              coarser level) is not a box: for those stages the 128
+//              producer threads gather the halo with cp.async instead. The
+//              slot's "full" barrier counts the TMA bytes and the threads'
+//              cp.async completions.
+//   warp 4     MMA: one thread waits for a full slot, issues the stage's
+//              4 x 9 x 2 tcgen05.mma (bf16 x bf16 -> fp32; descriptors are
+//              the slot's base descriptor plus constant offsets) into one of
+//              two accumulator sets in tensor memory, and commits them to
+//              the slot's "empty" barrier, and after a tile's last stage to
+//              the set's "full" barrier.
+//   warps 0-3  epilogue: wait for an accumulator set, read it with
+//              tcgen05.ld (warp w reads lanes 32w..32w+31), apply bias,
+//              ReLU, residual and mask like kConv3x3, store 16-byte blocks,
+//              and release the set; meanwhile the MMA thread fills the other.
 //
 // Shared-memory operands use the tensor core's no-swizzle K-major layout
-// (core matrices of 8 rows x 16 bytes): the halo as [chunk][row][130
-// pixels][16 B] with chunk planes 12544 bytes apart (the LBO of A), 8-pixel
-// groups 128 bytes apart (SBO); the weights as [tap][chunk][N][16 B] (LBO
-// N x 16 B, SBO 128 B). Tap (dy, dx) of output row r is the halo view that
-// starts at row r + dy + 1, pixel dx + 1.
+// (core matrices of 8 rows x 16 bytes): the halo as [block][row][130
+// pixels][16 B] (the TMA box image; blocks 12480 bytes apart = the LBO of
+// A, 8-pixel groups 128 bytes apart = SBO); the weights as
+// [tap][block][N][16 B] (LBO N x 16 B, SBO 128 B). Tap (dy, dx) of output
+// row r is the halo view that starts at row r + dy + 1, pixel dx + 1.
 //
 // Every wait is bounded (one second). A role whose wait runs out sets the
 // error word and the CTA's abort flag, which ends the other roles' loops;
@@ -55,9 +58,10 @@ constexpr int kTX = 128;          // output pixels per tile row (tensor-core M)
 constexpr int kHY = kR + 2;       // halo rows
 constexpr int kHX = kTX + 2;      // halo pixels per row
 constexpr int kChunks = 4;        // 8-channel chunks per stage
-constexpr int kPlane = 12544;     // one chunk plane of the halo (6 x 130 x 16 = 12480, padded)
+constexpr int kPlane = kHY * kHX * 16;  // one 8-channel block of the halo: 12480 bytes
 constexpr int kHaloBytes = kChunks * kPlane;
-constexpr int kThreads = 192;
+constexpr int kThreads = 288;     // 4 epilogue warps, 1 MMA warp, 4 producer warps
+constexpr int kMmaWarp = 4, kProdWarp0 = 5, kProducers = 128;
 constexpr uint32_t kSpinLimit = 1u << 26;
 constexpr uint64_t kWaitNs = 1000000000ull;  // one second
 
@@ -65,7 +69,7 @@ template <int N>
 struct Cfg {
   static constexpr int kSlots = N == 64 ? 2 : 3;
   static constexpr int kWBytes = 9 * kChunks * N * 16;
-  static constexpr int kSlotBytes = kHaloBytes + kWBytes;
+  static constexpr int kSlotBytes = (kHaloBytes + kWBytes + 1023) / 1024 * 1024;
   static constexpr int kBarOff = kSlots * kSlotBytes;
   static constexpr int kSmem = kBarOff + 256;
   static constexpr int kCols = 2 * kR * N;  // two accumulator sets: 512 or 256 columns
@@ -124,21 +128,21 @@ __device__ __forceinline__ void cpAsync16(uint32_t dst, const void *src, bool va
   asm volatile("cp.async.ca.shared.global [%0], [%1], 16, %2;\n" ::"r"(dst), "l"(src), "r"(n));
 }
 
-__device__ __forceinline__ void tma3(uint32_t dst, const CUtensorMap *map, int c0, int c1, int c2,
-                                     uint32_t bar) {
+// one bulk copy of `bytes` (a multiple of 16) from global to shared memory
+__device__ __forceinline__ void bulkCopy(uint32_t dst, const void *src, uint32_t bytes, uint32_t bar) {
   asm volatile(
-      "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, "
-      "%3, %4}], [%5];\n" ::"r"(dst),
-      "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(c2), "r"(bar)
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];\n" ::"r"(
+          dst),
+      "l"(src), "r"(bytes), "r"(bar)
       : "memory");
 }
 
-__device__ __forceinline__ void tma4(uint32_t dst, const CUtensorMap *map, int c0, int c1, int c2,
-                                     int c3, uint32_t bar) {
+__device__ __forceinline__ void tma5(uint32_t dst, const CUtensorMap *map, int c0, int c1, int c2,
+                                     int c3, int c4, uint32_t bar) {
   asm volatile(
-      "cp.async.bulk.tensor.4d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, "
-      "%3, %4, %5}], [%6];\n" ::"r"(dst),
-      "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(bar)
+      "cp.async.bulk.tensor.5d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, "
+      "%3, %4, %5, %6}], [%7];\n" ::"r"(dst),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(c4), "r"(bar)
       : "memory");
 }
 
@@ -175,8 +179,8 @@ __device__ __forceinline__ Tile tileOf(int u, int tilesX, int tilesY, int nTiles
 
 template <int N>
 __global__ void __launch_bounds__(kThreads, 1)
-    kConv3x3Ws(const __grid_constant__ CUtensorMap mapX, const __grid_constant__ CUtensorMap mapW,
-               ConvArgs a, int tilesX, int tilesY, int nTiles, int units, unsigned *error) {
+    kConv3x3Ws(const __grid_constant__ CUtensorMap mapX, ConvArgs a, int tilesX, int tilesY,
+               int nTiles, int units, unsigned *error) {
   typedef Cfg<N> C;
   extern __shared__ __align__(1024) uint8_t smem[];
   uint64_t *bars = reinterpret_cast<uint64_t *>(smem + C::kBarOff);
@@ -191,7 +195,8 @@ __global__ void __launch_bounds__(kThreads, 1)
 
   if (threadIdx.x == 0) {
     for (int s = 0; s < C::kSlots; ++s) {
-      asm volatile("mbarrier.init.shared::cta.b64 [%0], 33;\n" ::"r"(fullBar + 8 * s));
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(fullBar + 8 * s),
+                   "r"(1 + kProducers));
       asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(emptyBar + 8 * s));
     }
     for (int b = 0; b < 2; ++b) {
@@ -201,7 +206,7 @@ __global__ void __launch_bounds__(kThreads, 1)
     *abort = 0;
     asm volatile("fence.mbarrier_init.release.cluster;\n" ::);
   }
-  if (warp == 1) {
+  if (warp == kMmaWarp) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(
                      smemAddr(tmemSlot)),
                  "r"(C::kCols));
@@ -212,10 +217,13 @@ __global__ void __launch_bounds__(kThreads, 1)
   asm volatile("tcgen05.fence::after_thread_sync;\n" ::);
   const uint32_t tmem = *tmemSlot;
 
-  if (warp == 0) {
+  if (warp >= kProdWarp0) {
     // ------------------------------------------------------------ producer
+    const int pt = threadIdx.x - kProdWarp0 * 32;  // 0..127
+    const bool leader = pt == 0;
     int g = 0;  // stages issued
     const bool up = a.split > 0;
+    const size_t Pc = (size_t)a.N * (a.H >> 1) * (a.W >> 1);  // pixels of an upsampled source
     for (int u = blockIdx.x; u < units && !*abort; u += gridDim.x) {
       const Tile T = tileOf(u, tilesX, tilesY, nTiles, N);
       for (int s = 0; s < stages; ++s, ++g) {
@@ -229,52 +237,46 @@ __global__ void __launch_bounds__(kThreads, 1)
         const int c0 = s * 8 * kChunks;
         const int chunks = min(kChunks, (a.Cin - c0) / 8);
         const bool gather = up && c0 < a.split;
-        __syncwarp();
-        if (lane == 0) {
-          const uint32_t bytes =
-              (uint32_t)(9 * chunks * N * 16 + (gather ? 0 : chunks * kHY * kHX * 16));
+        if (leader) {
+          const uint32_t bytes = (uint32_t)(C::kWBytes + (gather ? 0 : kHaloBytes));
           asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(full),
                        "r"(bytes)
                        : "memory");
-          for (int tap = 0; tap < 9; ++tap)
-            for (int c = 0; c < chunks; ++c)
-              tma3(sW + (uint32_t)((tap * chunks + c) * N * 16), &mapW, c0 + 8 * c, tap, T.nBase,
-                   full);
+          bulkCopy(sW, a.wPacked + ((size_t)(T.nBase / N) * stages + s) * (C::kWBytes / 2),
+                   (uint32_t)C::kWBytes, full);
           if (!gather) {
-            const int cOff = up ? a.x2Off + c0 - a.split : a.xOff + c0;
-            for (int c = 0; c < chunks; ++c)
-              tma4(sHalo + (uint32_t)(c * kPlane), &mapX, cOff + 8 * c, T.x0 - 1, T.y0 - 1, T.n,
-                   full);
+            const int blk = (up ? a.x2Off + c0 - a.split : a.xOff + c0) / 8;
+            tma5(sHalo, &mapX, 0, T.x0 - 1, T.y0 - 1, T.n, blk, full);
           }
         }
-        __syncwarp();
         if (gather) {
-          // the upsampled coarse level, zero outside the image
+          // the upsampled coarse level, zero outside the image; pixel
+          // fastest, so that a warp reads a row of one 8-channel block
           const int Hc = a.H >> 1, Wc = a.W >> 1;
           const int entries = chunks * kHY * kHX;
-          for (int i = lane; i < entries; i += 32) {
-            const int c = i % chunks;
-            const int r = i / chunks;
-            const int hx = r % kHX, hy = r / kHX;
+          for (int i = pt; i < entries; i += kProducers) {
+            const int hx = i % kHX;
+            const int r = i / kHX;
+            const int c = r % chunks, hy = r / chunks;
             const int y = T.y0 - 1 + hy, x = T.x0 - 1 + hx;
             const bool in = y >= 0 && y < a.H && x >= 0 && x < a.W;
             const size_t pix = ((size_t)T.n * Hc + (y >> 1)) * Wc + (x >> 1);
-            const bf16 *src = a.x + (in ? pix * a.xC + a.xOff + c0 + 8 * c : 0);
+            const bf16 *src = a.x + (in ? actAt(Pc, pix, a.xOff + c0 + 8 * c) : 0);
             cpAsync16(sHalo + (uint32_t)(c * kPlane + (hy * kHX + hx) * 16), src, in);
           }
         }
-        // each lane's cp.async (none outside gather stages) completes one arrival
+        // each thread's cp.async (none outside gather stages) completes one arrival
         asm volatile("cp.async.mbarrier.arrive.noinc.shared::cta.b64 [%0];\n" ::"r"(full) : "memory");
       }
       if (*abort) break;
     }
     // before the CTA ends: the loads issued complete
     asm volatile("cp.async.wait_all;\n" ::: "memory");
-    if (lane == 0)
+    if (leader)
       for (int k = max(0, g - C::kSlots); k < g; ++k)
         mbarWait(fullBar + 8 * (k % C::kSlots), (k / C::kSlots) & 1, nullptr);
     __syncwarp();
-  } else if (warp == 1) {
+  } else if (warp == kMmaWarp) {
     // ------------------------------------------------------------ MMA
     if (lane == 0) {
       int g = 0, j = 0;
@@ -302,15 +304,18 @@ __global__ void __launch_bounds__(kThreads, 1)
           asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
           asm volatile("tcgen05.fence::after_thread_sync;\n" ::);
           const uint32_t sHalo = slot0 + slot * C::kSlotBytes, sW = sHalo + kHaloBytes;
-#pragma unroll 1
+          // descriptors: the slot's base plus constant offsets in 16-byte units
+          const uint64_t da0 = smemDesc(sHalo, kPlane, 128), db0 = smemDesc(sW, N * 16, 128);
+#pragma unroll
           for (int r = 0; r < kR; ++r) {
-#pragma unroll 1
+#pragma unroll
             for (int tap = 0; tap < 9; ++tap) {
-              const uint32_t aRow = sHalo + (uint32_t)(((r + tap / 3) * kHX + tap % 3) * 16);
-              for (int k = 0; k < chunks; k += 2) {
-                const uint64_t da = smemDesc(aRow + (uint32_t)(k * kPlane), kPlane, 128);
-                const uint64_t db =
-                    smemDesc(sW + (uint32_t)((tap * chunks + k) * N * 16), N * 16, 128);
+#pragma unroll
+              for (int k = 0; k < kChunks; k += 2) {
+                if (k >= chunks) break;
+                const uint64_t da =
+                    da0 + (uint64_t)((((r + tap / 3) * kHX + tap % 3) * 16 + k * kPlane) >> 4);
+                const uint64_t db = db0 + (uint64_t)(((tap * kChunks + k) * N * 16) >> 4);
                 const uint32_t accum = (s > 0 || tap > 0 || k > 0) ? 1u : 0u;
                 asm volatile(
                     "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
@@ -337,8 +342,8 @@ __global__ void __launch_bounds__(kThreads, 1)
     __syncwarp();
   } else {
     // ------------------------------------------------------------ epilogue
-    const int q = warp & 3;  // the tensor-memory lane quarter this warp may read
-    const bool vec = a.yf == nullptr && (a.yC % 8) == 0 && (a.yOff % 8) == 0;
+    const int q = warp;  // warps 0-3: the tensor-memory lane quarter this warp may read
+    const size_t P = (size_t)a.N * a.H * a.W;
     int j = 0;
     for (int u = blockIdx.x; u < units && !*abort; u += gridDim.x, ++j) {
       const int b = j & 1;
@@ -374,31 +379,33 @@ __global__ void __launch_bounds__(kThreads, 1)
             const int cb = T.nBase + c32 * 32 + g8;
             if (cb >= a.Cout) break;
             float o[8];
+            uint4 rv = make_uint4(0, 0, 0, 0), mv = make_uint4(0, 0, 0, 0);
+            if (a.resid && cb < a.residN)
+              rv = *reinterpret_cast<const uint4 *>(a.resid + actAt(P, pp, cb));
+            if (a.mask) mv = *reinterpret_cast<const uint4 *>(a.mask + actAt(P, pp, a.maskOff + cb));
 #pragma unroll
             for (int k = 0; k < 8; ++k) {
               const int c = cb + k;
               float val = __uint_as_float(v[g8 + k]);
               if (a.bias && c < a.Cout) val += __ldg(a.bias + c);
               if (a.relu) val = fmaxf(val, 0.f);
-              if (a.resid && c < a.residN) val += __bfloat162float(a.resid[pp * a.residC + c]);
-              if (a.mask && c < a.Cout &&
-                  !(__bfloat162float(a.mask[pp * a.maskC + a.maskOff + c]) > 0.f))
+              if (a.resid && c < a.residN)
+                val += __bfloat162float(reinterpret_cast<const bf16 *>(&rv)[k]);
+              if (a.mask && !(__bfloat162float(reinterpret_cast<const bf16 *>(&mv)[k]) > 0.f))
                 val = 0.f;
               o[k] = val;
             }
-            const size_t ob = pp * a.yC + a.yOff + cb;
-            if (vec && cb + 8 <= a.Cout) {
+            if (a.yf) {  // fp32 output: NHWC
+              const size_t ob = pp * a.yC + a.yOff + cb;
+#pragma unroll
+              for (int k = 0; k < 8; ++k)
+                if (cb + k < a.Cout) a.yf[ob + k] = o[k];
+            } else {
               __nv_bfloat162 h[4];
 #pragma unroll
               for (int k = 0; k < 4; ++k) h[k] = __floats2bfloat162_rn(o[2 * k], o[2 * k + 1]);
-              *reinterpret_cast<uint4 *>(a.y + ob) = *reinterpret_cast<const uint4 *>(h);
-            } else {
-#pragma unroll
-              for (int k = 0; k < 8; ++k) {
-                if (cb + k >= a.Cout) break;
-                if (a.yf) a.yf[ob + k] = o[k];
-                else a.y[ob + k] = __float2bfloat16(o[k]);
-              }
+              *reinterpret_cast<uint4 *>(a.y + actAt(P, pp, a.yOff + cb)) =
+                  *reinterpret_cast<const uint4 *>(h);
             }
           }
         }
@@ -411,7 +418,7 @@ __global__ void __launch_bounds__(kThreads, 1)
   asm volatile("tcgen05.fence::before_thread_sync;\n" ::);
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;\n" ::);
-  if (warp == 1)
+  if (warp == kMmaWarp)
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem),
                  "r"(C::kCols));
 }
@@ -440,7 +447,7 @@ bool encodeBf16(CUtensorMap *map, const void *base, int rank, const cuuint64_t *
                 const cuuint64_t *strides, const cuuint32_t *box) {
   EncodeTiledFn fn = encodeTiled();
   if (!fn) return false;
-  const cuuint32_t ones[4] = {1, 1, 1, 1};
+  const cuuint32_t ones[5] = {1, 1, 1, 1, 1};
   return fn(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, (cuuint32_t)rank, const_cast<void *>(base), dims,
             strides, box, ones, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
             CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
@@ -454,16 +461,14 @@ cudaError_t launchWs(const ConvArgs &a, unsigned *error, cudaStream_t s) {
   const bool up = a.split > 0;
   const bf16 *src = up ? a.x2 : a.x;
   const int srcC = up ? a.x2C : a.xC;
-  CUtensorMap mapX, mapW;
-  const cuuint64_t xd[4] = {(cuuint64_t)srcC, (cuuint64_t)a.W, (cuuint64_t)a.H, (cuuint64_t)a.N};
-  const cuuint64_t xs[3] = {(cuuint64_t)srcC * 2, (cuuint64_t)a.W * srcC * 2,
-                            (cuuint64_t)a.H * a.W * srcC * 2};
-  const cuuint32_t xb[4] = {8, (cuuint32_t)kHX, (cuuint32_t)kHY, 1};
-  const cuuint64_t wd[3] = {(cuuint64_t)a.Cin, 9, (cuuint64_t)a.Cout};
-  const cuuint64_t ws[2] = {(cuuint64_t)a.Cin * 2, (cuuint64_t)a.Cin * 18};
-  const cuuint32_t wb[3] = {8, 1, (cuuint32_t)N};
-  if (!encodeBf16(&mapX, src, 4, xd, xs, xb) || !encodeBf16(&mapW, a.w, 3, wd, ws, wb))
-    return cudaErrorInvalidValue;
+  // blocked planes as a 5-d tensor: [block][n][y][x][8 channels]
+  CUtensorMap mapX;
+  const cuuint64_t P = (cuuint64_t)a.N * a.H * a.W;
+  const cuuint64_t xd[5] = {8, (cuuint64_t)a.W, (cuuint64_t)a.H, (cuuint64_t)a.N,
+                            (cuuint64_t)(srcC / 8)};
+  const cuuint64_t xs[4] = {16, (cuuint64_t)a.W * 16, (cuuint64_t)a.H * a.W * 16, P * 16};
+  const cuuint32_t xb[5] = {8, (cuuint32_t)kHX, (cuuint32_t)kHY, 1, (cuuint32_t)kChunks};
+  if (!encodeBf16(&mapX, src, 5, xd, xs, xb)) return cudaErrorInvalidValue;
   const int tilesX = (a.W + kTX - 1) / kTX, tilesY = (a.H + kR - 1) / kR;
   const int nTiles = (a.Cout + N - 1) / N;
   const long long units = (long long)a.N * tilesX * tilesY * nTiles;
@@ -479,15 +484,18 @@ cudaError_t launchWs(const ConvArgs &a, unsigned *error, cudaStream_t s) {
                                        C::kSmem);
   if (e != cudaSuccess) return e;
   const int grid = (int)std::min<long long>(units, sms);
-  kConv3x3Ws<N><<<grid, kThreads, C::kSmem, s>>>(mapX, mapW, a, tilesX, tilesY, nTiles, (int)units,
-                                                 error);
+  kConv3x3Ws<N><<<grid, kThreads, C::kSmem, s>>>(mapX, a, tilesX, tilesY, nTiles, (int)units, error);
   return cudaGetLastError();
 }
 
 }  // namespace
 
 cudaError_t launchConv3x3Ws(const ConvArgs &a, unsigned *error, cudaStream_t s) {
-  if (a.Cin <= 0 || a.Cin % 16 || a.Cout <= 0 || a.xC % 8 || a.xOff % 8 || !error || !a.x || !a.w)
+  if (a.Cin <= 0 || a.Cin % 16 || a.Cout <= 0 || a.xC % 8 || a.xOff % 8 || !error || !a.x ||
+      !a.wPacked)
+    return cudaErrorInvalidValue;
+  if ((!a.yf && (a.Cout % 8 || a.yOff % 8)) || (a.mask && a.maskOff % 8) ||
+      (a.resid && a.residN > 8 * ((a.residC + 7) / 8)))
     return cudaErrorInvalidValue;
   if (a.split && (a.split < 0 || a.split % 32 || a.split >= a.Cin || !a.x2 || a.x2C % 8 ||
                   a.x2Off % 8 || a.x2Off + a.Cin - a.split > a.x2C || !a.up))

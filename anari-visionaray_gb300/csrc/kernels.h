@@ -63,10 +63,17 @@ struct BatchLaunch {
 };
 cudaError_t launchBatch(const BatchLaunch &L, cudaStream_t stream);
 
-// Denoiser kernels (k_denoise.cu). Activations NHWC bf16; a tensor view is
-// (pointer, channels per pixel, first channel), both multiples of 8.
-// Convolution weights are [Cout][9][Cin] bf16 (tap = 3 (dy + 1) + dx + 1),
-// biases fp32.
+// Denoiser kernels (k_denoise.cu). Activations are bf16 in channel-blocked
+// planes: element (pixel p, channel c) of a tensor of P pixels (N x H x W,
+// row-major) is at ((c / 8) P + p) 8 + c % 8, so that 8 channels of a pixel
+// are 16 contiguous bytes and a row of pixels of one 8-channel block is
+// contiguous. A tensor view is (pointer, channels of the buffer, first
+// channel), both multiples of 8; the pixel count is that of the resolution
+// the view is used at. Convolution weights are [Cout][9][Cin] bf16 (tap =
+// 3 (dy + 1) + dx + 1), biases fp32.
+__host__ __device__ inline size_t actAt(size_t P, size_t p, int c) {
+  return ((size_t)(c >> 3) * P + p) * 8 + (size_t)(c & 7);
+}
 struct ConvArgs {
   const __nv_bfloat16 *x;
   int xC, xOff, Cin;  // Cin a multiple of 16
@@ -88,6 +95,8 @@ struct ConvArgs {
   // upsampling). split a multiple of 32; 0: every channel from x.
   const __nv_bfloat16 *x2;
   int x2C, x2Off, split, up;
+  // the weights packed for kConv3x3Ws (packConvWeights), or null
+  const __nv_bfloat16 *wPacked;
 };
 struct WgradArgs {
   const __nv_bfloat16 *dy;  // output gradient (after the ReLU mask)
@@ -125,6 +134,16 @@ cudaError_t launchL1(const float *out, int oC, const float *target, int tC, int 
 cudaError_t launchAdam(float *w, float *m, float *v, const float *g, size_t n, float lr, float b1,
                        float b2, float eps, int step, __nv_bfloat16 *wb, __nv_bfloat16 *wt, int Cin,
                        int CoutT, cudaStream_t s);
+// NHWC bf16 (C channels per pixel, a multiple of 8) -> channel-blocked planes
+cudaError_t launchToBlocked(const __nv_bfloat16 *x, int C, size_t P, __nv_bfloat16 *y,
+                            cudaStream_t s);
+// Weights of one layer packed for kConv3x3Ws: per block of N output channels
+// (N = 32 if Cout <= 32, else 64) and stage of 32 input channels, the nine
+// taps' [tap][chunk 0..3][N][8] image of shared memory, zero-padded; from
+// w [Cout][9][Cin]. packedConvWeights gives the element count.
+size_t packedConvWeights(int Cin, int Cout);
+cudaError_t launchPackConvWeights(const __nv_bfloat16 *w, int Cin, int Cout, __nv_bfloat16 *packed,
+                                  cudaStream_t s);
 cudaError_t launchDenoiseInput(const float4 *color, const float *albedo, const float *normal,
                                const float *depth, const float *var, float invSqrtN, int W, int H,
                                int Wp, int Hp, __nv_bfloat16 *x, int xC, cudaStream_t s);

@@ -197,7 +197,7 @@ void Denoiser::conv(int li, const __nv_bfloat16 *x, int xC, __nv_bfloat16 *y, fl
 }
 
 cudaError_t Denoiser::launchTc(const ConvArgs &a, cudaStream_t s) const {
-  return tensorPath_ == 3 ? launchConv3x3Ws(a, err_, s) : launchConv3x3Tc(a, err_, s);
+  return tensorPath_ == 3 ? launchConv3x3Tc(a, err_, s) : launchConv3x3Ws(a, err_, s);
 }
 
 // a decoder convolution on [upsampled coarse level | skip connection],

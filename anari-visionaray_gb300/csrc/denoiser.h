@@ -49,9 +49,10 @@ class Denoiser {
   cudaError_t adam(float lr, cudaStream_t s);
   const float *grad() const { return grad_; }
   float *lossDevice() const { return loss_; }  // one device float for the loss
-  // 0: convolutions on mma.sync (kConv3x3); 1: on tcgen05 (kConv3x3Tc) for
-  // images at least one 128-pixel tile wide, mma.sync below that; 2:
-  // tcgen05 at every width; 3: as 1 with the warp-specialised kConv3x3Ws
+  // 0: convolutions on mma.sync (kConv3x3); 1: on tcgen05 (the
+  // warp-specialised kConv3x3Ws with TMA loads) for images at least one
+  // 128-pixel tile wide, mma.sync below that; 2: kConv3x3Ws at every width;
+  // 3: as 1 with the one-tile-per-CTA kConv3x3Tc
   void setTensorPath(int path) { tensorPath_ = path; }
   int tensorPath() const { return tensorPath_; }
   unsigned *errorWord() const { return err_; }
@@ -72,8 +73,8 @@ class Denoiser {
   bool useTc(int W) const {
     return tensorPath_ == 2 || ((tensorPath_ == 1 || tensorPath_ == 3) && W >= 128);
   }
-  // the tcgen05 convolution: one tile per CTA (kConv3x3Tc), or on path 3
-  // the persistent warp-specialised kernel with TMA loads (kConv3x3Ws)
+  // the tcgen05 convolution: the persistent warp-specialised kernel with
+  // TMA loads (kConv3x3Ws), or on path 3 one tile per CTA (kConv3x3Tc)
   cudaError_t launchTc(const ConvArgs &a, cudaStream_t s) const;
   void convCat(int layer, const __nv_bfloat16 *coarse, int coarseC, const __nv_bfloat16 *skip,
                int skipC, __nv_bfloat16 *y, int yC, int N, int H, int W, cudaStream_t s);

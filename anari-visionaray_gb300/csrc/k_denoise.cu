@@ -131,8 +131,16 @@ __global__ void __launch_bounds__(128) kConv3x3(ConvArgs a) {
         mma16816(acc[mt][nt], af[mt], bfr[nt >> 1][(nt & 1) * 2], bfr[nt >> 1][(nt & 1) * 2 + 1]);
     __syncthreads();
   }
-  // epilogue: bias, ReLU, mask of a previous ReLU, store
+  // epilogue: bias, ReLU, mask of a previous ReLU, store; the biases of
+  // this thread's columns are loaded once
   const int g = lane >> 2, t4 = lane & 3;
+  float bias[NT][2];
+#pragma unroll
+  for (int nt = 0; nt < NT; ++nt) {
+    const int c = nBase + wn * (BN / 2) + nt * 8 + t4 * 2;
+    bias[nt][0] = (a.bias && c < a.Cout) ? a.bias[c] : 0.f;
+    bias[nt][1] = (a.bias && c + 1 < a.Cout) ? a.bias[c + 1] : 0.f;
+  }
 #pragma unroll
   for (int mt = 0; mt < 2; ++mt)
 #pragma unroll
@@ -142,11 +150,7 @@ __global__ void __launch_bounds__(128) kConv3x3(ConvArgs a) {
 #pragma unroll
       for (int nt = 0; nt < NT; ++nt) {
         const int c = nBase + wn * (BN / 2) + nt * 8 + t4 * 2;
-        float v0 = acc[mt][nt][half * 2], v1 = acc[mt][nt][half * 2 + 1];
-        if (a.bias) {
-          if (c < a.Cout) v0 += a.bias[c];
-          if (c + 1 < a.Cout) v1 += a.bias[c + 1];
-        }
+        float v0 = acc[mt][nt][half * 2] + bias[nt][0], v1 = acc[mt][nt][half * 2 + 1] + bias[nt][1];
         if (a.relu) {
           v0 = fmaxf(v0, 0.f);
           v1 = fmaxf(v1, 0.f);

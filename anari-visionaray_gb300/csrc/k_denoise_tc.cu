@@ -251,13 +251,20 @@ __global__ void __launch_bounds__(128) kConv3x3Tc(ConvArgs a, int tilesX, int ti
   if (ok) {
     const int x = x0 + warp * 32 + lane;
     const size_t P = (size_t)a.N * a.H * a.W;
-#pragma unroll 1
-    for (int r = 0; r < kR; ++r) {
-      const int y = y0 + r;
-      const bool pixIn = x < a.W && y < a.H;
-      const size_t pp = ((size_t)n * a.H + y) * a.W + x;
+    // columns outside, rows inside: a column group's biases are loaded once
 #pragma unroll
-      for (int c32 = 0; c32 < N / 32; ++c32) {
+    for (int c32 = 0; c32 < N / 32; ++c32) {
+      float bias[32];
+#pragma unroll
+      for (int k = 0; k < 32; ++k) {
+        const int c = nBase + c32 * 32 + k;
+        bias[k] = (a.bias && c < a.Cout) ? __ldg(a.bias + c) : 0.f;
+      }
+#pragma unroll 1
+      for (int r = 0; r < kR; ++r) {
+        const int y = y0 + r;
+        const bool pixIn = x < a.W && y < a.H;
+        const size_t pp = ((size_t)n * a.H + y) * a.W + x;
         uint32_t v[32];
         asm volatile(
             "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,"
@@ -283,7 +290,7 @@ __global__ void __launch_bounds__(128) kConv3x3Tc(ConvArgs a, int tilesX, int ti
           for (int k = 0; k < 8; ++k) {
             const int c = cb + k;
             float val = __uint_as_float(v[g + k]);
-            if (a.bias && c < a.Cout) val += a.bias[c];
+            val += bias[g + k];
             if (a.relu) val = fmaxf(val, 0.f);
             if (a.resid && c < a.residN)
               val += __bfloat162float(reinterpret_cast<const bf16 *>(&rv)[k]);

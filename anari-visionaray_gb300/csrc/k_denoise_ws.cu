@@ -354,13 +354,22 @@ __global__ void __launch_bounds__(kThreads, 1)
       asm volatile("tcgen05.fence::after_thread_sync;\n" ::);
       const Tile T = tileOf(u, tilesX, tilesY, nTiles, N);
       const int x = T.x0 + q * 32 + lane;
-#pragma unroll 1
-      for (int r = 0; r < kR; ++r) {
-        const int y = T.y0 + r;
-        const bool pixIn = x < a.W && y < a.H;
-        const size_t pp = ((size_t)T.n * a.H + y) * a.W + x;
+      // columns outside, rows inside: the 32 biases of a column group are
+      // loaded once per tile (loading them per element and row made the
+      // epilogue the pipeline's bottleneck)
 #pragma unroll
-        for (int c32 = 0; c32 < N / 32; ++c32) {
+      for (int c32 = 0; c32 < N / 32; ++c32) {
+        float bias[32];
+#pragma unroll
+        for (int k = 0; k < 32; ++k) {
+          const int c = T.nBase + c32 * 32 + k;
+          bias[k] = (a.bias && c < a.Cout) ? __ldg(a.bias + c) : 0.f;
+        }
+#pragma unroll 1
+        for (int r = 0; r < kR; ++r) {
+          const int y = T.y0 + r;
+          const bool pixIn = x < a.W && y < a.H;
+          const size_t pp = ((size_t)T.n * a.H + y) * a.W + x;
           uint32_t v[32];
           asm volatile(
               "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,"
@@ -387,7 +396,7 @@ __global__ void __launch_bounds__(kThreads, 1)
             for (int k = 0; k < 8; ++k) {
               const int c = cb + k;
               float val = __uint_as_float(v[g8 + k]);
-              if (a.bias && c < a.Cout) val += __ldg(a.bias + c);
+              val += bias[g8 + k];
               if (a.relu) val = fmaxf(val, 0.f);
               if (a.resid && c < a.residN)
                 val += __bfloat162float(reinterpret_cast<const bf16 *>(&rv)[k]);

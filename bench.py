@@ -330,9 +330,10 @@ def denoiser_roofline(dn_s):
             "unit": "TFLOP/s", "frac": flops / dn_s / 1e12 / peak[0],
             "note": f"denoiser forward at 1920x1080 ({flops / 1e12:.3f} TFLOP incl. "
                     f"input and gate kernels in the time); peak bf16 {peak[1]}; "
-                    "tcgen05.mma kind::f16 (bf16 -> fp32 in tensor memory) on halo "
-                    "tiles of 4 x 128 pixels; decoders read upsampled level and skip "
-                    "in place"}
+                    "tcgen05.mma kind::f16 (bf16 -> fp32 in tensor memory), persistent "
+                    "warp-specialised kernel (TMA producer, MMA thread, epilogue warps) "
+                    "on 4 x 128-pixel halo tiles of channel-blocked activations; "
+                    "decoders read upsampled level and skip in place"}
 
 
 def measure_denoiser_forward(pkg, dev):

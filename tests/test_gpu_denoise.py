@@ -107,11 +107,11 @@ def test_tcgen05_path_matches_oracle(net, shape, path):
     """The tcgen05 convolutions (accumulators in tensor memory) in forward,
     where the decoders read the upsampled level and the skip connection in
     place, and in the backward's input gradients: the same output and
-    parameter gradients as the oracle. Path 2 runs every level on tcgen05
-    (tiles of 4 rows x 128 pixels far wider than these images, rows not a
-    multiple of 4 at 24 / 8 = 3); path 1 switches to mma.sync below 128
-    pixels (136: a second, nearly empty tile; 256: two levels on each);
-    path 3 is path 1 on the warp-specialised kernel with TMA loads."""
+    parameter gradients as the oracle. Path 2 runs every level on the
+    warp-specialised TMA kernel (tiles of 4 rows x 128 pixels far wider than
+    these images, rows not a multiple of 4 at 24 / 8 = 3); path 1 switches
+    to mma.sync below 128 pixels (136: a second, nearly empty tile; 256: two
+    levels on each); path 3 is path 1 on the one-tile-per-CTA kernel."""
     import torch
     n, h, w = shape
     params = perturbed_params(5, 11)

@@ -6,7 +6,7 @@
 // channels in stages of 32. One CTA per SM walks its share of the tiles.
 // Three roles run concurrently, linked by mbarriers:
 //
-//   warps 5-8  producer: for each stage they wait for a free slot of a 2- or
+//   warps 9-12 producer: for each stage they wait for a free slot of a 2- or
 //              3-slot shared-memory ring; one thread loads the stage's
 //              weights (one bulk copy of their packed shared-memory image,
 //              packConvWeights) and its input halo: activations are
@@ -18,14 +18,15 @@
 //              producer threads gather the halo with cp.async instead. The
 //              slot's "full" barrier counts the TMA bytes and the threads'
 //              cp.async completions.
-//   warp 4     MMA: one thread waits for a full slot, issues the stage's
+//   warp 8     MMA: one thread waits for a full slot, issues the stage's
 //              4 x 9 x 2 tcgen05.mma (bf16 x bf16 -> fp32; descriptors are
 //              the slot's base descriptor plus constant offsets) into one of
 //              two accumulator sets in tensor memory, and commits them to
 //              the slot's "empty" barrier, and after a tile's last stage to
 //              the set's "full" barrier.
-//   warps 0-3  epilogue: wait for an accumulator set, read it with
-//              tcgen05.ld (warp w reads lanes 32w..32w+31), apply bias,
+//   warps 0-7  epilogue: wait for an accumulator set, read it with
+//              tcgen05.ld (warp w reads lanes 32 (w % 4) .. and rows
+//              2 (w / 4), 2 (w / 4) + 1 of the tile), apply bias,
 //              ReLU, residual and mask like kConv3x3, store 16-byte blocks,
 //              and release the set; meanwhile the MMA thread fills the other.
 //
@@ -60,8 +61,9 @@ constexpr int kHX = kTX + 2;      // halo pixels per row
 constexpr int kChunks = 4;        // 8-channel chunks per stage
 constexpr int kPlane = kHY * kHX * 16;  // one 8-channel block of the halo: 12480 bytes
 constexpr int kHaloBytes = kChunks * kPlane;
-constexpr int kThreads = 288;     // 4 epilogue warps, 1 MMA warp, 4 producer warps
-constexpr int kMmaWarp = 4, kProdWarp0 = 5, kProducers = 128;
+constexpr int kEpiWarps = 8;      // two per tensor-memory lane quarter, two rows each
+constexpr int kThreads = 32 * (kEpiWarps + 1 + 4);  // + 1 MMA warp + 4 producer warps
+constexpr int kMmaWarp = kEpiWarps, kProdWarp0 = kEpiWarps + 1, kProducers = 128;
 constexpr uint32_t kSpinLimit = 1u << 26;
 constexpr uint64_t kWaitNs = 1000000000ull;  // one second
 
@@ -201,7 +203,8 @@ __global__ void __launch_bounds__(kThreads, 1)
     }
     for (int b = 0; b < 2; ++b) {
       asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(accFullBar + 8 * b));
-      asm volatile("mbarrier.init.shared::cta.b64 [%0], 128;\n" ::"r"(accEmptyBar + 8 * b));
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(accEmptyBar + 8 * b),
+                   "r"(32 * kEpiWarps));
     }
     *abort = 0;
     asm volatile("fence.mbarrier_init.release.cluster;\n" ::);
@@ -342,7 +345,9 @@ __global__ void __launch_bounds__(kThreads, 1)
     __syncwarp();
   } else {
     // ------------------------------------------------------------ epilogue
-    const int q = warp;  // warps 0-3: the tensor-memory lane quarter this warp may read
+    // warp w reads tensor-memory lane quarter w % 4 (the only one it may
+    // access) and rows 2 (w / 4), 2 (w / 4) + 1 of the tile
+    const int q = warp & 3, rowBase = 2 * (warp >> 2);
     const size_t P = (size_t)a.N * a.H * a.W;
     int j = 0;
     for (int u = blockIdx.x; u < units && !*abort; u += gridDim.x, ++j) {
@@ -366,7 +371,7 @@ __global__ void __launch_bounds__(kThreads, 1)
           bias[k] = (a.bias && c < a.Cout) ? __ldg(a.bias + c) : 0.f;
         }
 #pragma unroll 1
-        for (int r = 0; r < kR; ++r) {
+        for (int r = rowBase; r < rowBase + 2; ++r) {
           const int y = T.y0 + r;
           const bool pixIn = x < a.W && y < a.H;
           const size_t pp = ((size_t)T.n * a.H + y) * a.W + x;

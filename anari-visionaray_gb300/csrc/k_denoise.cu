@@ -564,7 +564,7 @@ __global__ void kDenoiseInput(const float4 *color, const float *albedo, const fl
        j += (size_t)gridDim.x * blockDim.x) {
     const int px = (int)(j % Wp), py = (int)(j / Wp);
     if (px >= W || py >= H) {
-      for (int k = 0; k < xC; ++k) x[j * xC + k] = __float2bfloat16(0.f);
+      for (int k = 0; k < xC; k += 8) *reinterpret_cast<uint4 *>(x + j * xC + k) = make_uint4(0, 0, 0, 0);
       continue;
     }
     const size_t i = (size_t)py * W + px;
@@ -581,7 +581,15 @@ __global__ void kDenoiseInput(const float4 *color, const float *albedo, const fl
     f[10] = v > 0.f && v < 1e30f ? log1pf(sqrtf(v)) : 0.f;
     f[11] = invSqrtN;
     for (int k = 12; k < 16; ++k) f[k] = 0.f;
-    for (int k = 0; k < xC; ++k) x[j * xC + k] = __float2bfloat16(k < 16 ? f[k] : 0.f);
+    // 16-byte stores of 8 channels
+    for (int k = 0; k < xC; k += 8) {
+      __nv_bfloat162 h[4];
+#pragma unroll
+      for (int e = 0; e < 4; ++e)
+        h[e] = k < 16 ? __floats2bfloat162_rn(f[k + 2 * e], f[k + 2 * e + 1])
+                      : __floats2bfloat162_rn(0.f, 0.f);
+      *reinterpret_cast<uint4 *>(x + j * xC + k) = *reinterpret_cast<const uint4 *>(h);
+    }
   }
 }
 

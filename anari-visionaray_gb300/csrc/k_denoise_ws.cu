@@ -409,11 +409,16 @@ __global__ void __launch_bounds__(kThreads, 1)
                 val = 0.f;
               o[k] = val;
             }
-            if (a.yf) {  // fp32 output: NHWC
+            if (a.yf) {  // fp32 output: NHWC, two 16-byte stores per 8 channels
               const size_t ob = pp * a.yC + a.yOff + cb;
+              if (cb + 8 <= a.Cout && (ob & 3) == 0) {
+                reinterpret_cast<float4 *>(a.yf + ob)[0] = make_float4(o[0], o[1], o[2], o[3]);
+                reinterpret_cast<float4 *>(a.yf + ob)[1] = make_float4(o[4], o[5], o[6], o[7]);
+              } else {
 #pragma unroll
-              for (int k = 0; k < 8; ++k)
-                if (cb + k < a.Cout) a.yf[ob + k] = o[k];
+                for (int k = 0; k < 8; ++k)
+                  if (cb + k < a.Cout) a.yf[ob + k] = o[k];
+              }
             } else {
               __nv_bfloat162 h[4];
 #pragma unroll

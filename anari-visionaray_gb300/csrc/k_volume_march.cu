@@ -31,9 +31,6 @@
 namespace vsr {
 namespace {
 
-#ifndef VSR_SEG_SAMPLES
-#define VSR_SEG_SAMPLES 16
-#endif
 #ifndef VSR_SEG_MIN_BLOCKS
 #define VSR_SEG_MIN_BLOCKS 1
 #endif

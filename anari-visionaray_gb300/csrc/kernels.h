@@ -12,6 +12,11 @@ namespace vsr {
 // one sample per pixel (k_volume_march.cu): items 48 B per pixel, groups
 // 16 B per 32 pixels, counters 4 uint, and unitCap work units of 32
 // segments (unitGroup 4 B and segOut 1 KiB per unit).
+// samples per segment of the segmented volume marcher (k_volume_march.cu);
+// the work-unit capacity of MarchScratch scales with it
+#ifndef VSR_SEG_SAMPLES
+#define VSR_SEG_SAMPLES 12
+#endif
 struct MarchScratch {
   void *items;
   void *groups;

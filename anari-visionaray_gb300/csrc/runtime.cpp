@@ -1066,13 +1066,13 @@ struct FrameObj : Object {
   int batchTileW = 0, batchFetch = 0, batchTuned = 0;  // last batched render
 
   // scratch of the segmented volume marcher, made on first use: the ray list
-  // (48 B per pixel), groups (16 B per 32 pixels) and work units for 4
-  // segments of 16 samples per pixel (1 KiB per unit of 32 segments); rays
-  // beyond that are marched whole by the combining warps
+  // (48 B per pixel), groups (16 B per 32 pixels) and work units for
+  // 64 / VSR_SEG_SAMPLES segments per pixel (1 KiB per unit of 32 segments);
+  // rays beyond that are marched whole by the combining warps
   bool ensureMarch() {
     size_t np = (size_t)width * height;
     if (marchPixels == np) return true;
-    const size_t cap = std::max<size_t>(np / 8, 4096);
+    const size_t cap = std::max<size_t>(np * 2 / VSR_SEG_SAMPLES, 4096);
     const size_t numGroups = (np + 31) / 32;
     bool ok = marchItems.alloc(np * 48) == cudaSuccess &&
               marchGroups.alloc(numGroups * 16) == cudaSuccess &&

@@ -38,7 +38,7 @@ namespace {
 #define VSR_SETUP_MIN_BLOCKS 4
 #endif
 #ifndef VSR_COMBINE_PREFETCH
-#define VSR_COMBINE_PREFETCH 2
+#define VSR_COMBINE_PREFETCH 8
 #endif
 #ifndef VSR_SEG_DYNAMIC
 #define VSR_SEG_DYNAMIC 0

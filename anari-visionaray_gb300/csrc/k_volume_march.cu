@@ -66,6 +66,8 @@ struct SegOut {
 
 __global__ void __launch_bounds__(256, VSR_SETUP_MIN_BLOCKS) kVolumeSetup(DScene S, DCamera C, DRenderer R, DFrame F,
                                                     MarchScratch M) {
+  // the segments pass may launch now; it waits for this grid's results
+  asm volatile("griddepcontrol.launch_dependents;\n" ::);
   MarchItem *items = reinterpret_cast<MarchItem *>(M.items);
   MarchGroup *groups = reinterpret_cast<MarchGroup *>(M.groups);
   const int numPix = F.width * F.height;
@@ -477,6 +479,9 @@ __global__ void __launch_bounds__(256, VSR_SEG_MIN_BLOCKS)
     kVolumeSegments(DScene S, DRenderer R, MarchScratch M, int stageTF) {
   extern __shared__ float4 sTF[];
   stageTable(S, sTF, stageTF);
+  // the set-up pass's ray list and counters are complete and visible
+  asm volatile("griddepcontrol.wait;\n" ::: "memory");
+  asm volatile("griddepcontrol.launch_dependents;\n" ::);
   const int lane = threadIdx.x & 31;
   const unsigned numUnits = min(M.counters[2], M.unitCap);
   const unsigned warps = gridDim.x * (blockDim.x >> 5);
@@ -491,6 +496,8 @@ __global__ void __launch_bounds__(256) kVolumeCombine(DScene S, DRenderer R, DFr
                                                       MarchScratch M, int stageTF) {
   extern __shared__ float4 sTF[];
   stageTable(S, sTF, stageTF);
+  // the segment composites are complete and visible
+  asm volatile("griddepcontrol.wait;\n" ::: "memory");
   const int lane = threadIdx.x & 31;
   const unsigned numGroups = M.counters[3];
   const unsigned warps = gridDim.x * (blockDim.x >> 5);
@@ -551,9 +558,22 @@ cudaError_t launchVolumeMarch(const DScene &S, const DCamera &C, const DRenderer
   if (e != cudaSuccess) return e;
   const int numPix = F.width * F.height;
   kVolumeSetup<<<min((numPix + 255) / 256, sms * 8), 256, 0, stream>>>(S, C, R, F, M);
+  // programmatic dependent launch: a pass's blocks start (and stage the
+  // transfer function) while the previous pass drains, and wait for its
+  // results with griddepcontrol.wait
   auto persistent = [&](auto kernel, auto... args) {
     const int perSM = persistentBlocksPerSM((const void *)kernel, smem);
-    kernel<<<sms * perSM, 256, smem, stream>>>(args...);
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(sms * perSM);
+    cfg.blockDim = dim3(256);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = stream;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    cudaLaunchKernelEx(&cfg, kernel, args...);
   };
   persistent(kVolumeSegments, S, R, M, stage);
   if (count) persistent(kVolumeCombine<true>, S, R, F, M, stage);

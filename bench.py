@@ -220,7 +220,7 @@ def measure_raycast_config0(pkg, dev, flush, steps=20):
                          "frac": alg / t / 1e9 / peak,
                          "traffic": profiled_traffic("raycast_config0.txt"),
                          "note": f"32 B per trilinear sample + 20 B per pixel; peak {kind}; "
-                                 "segmented marcher (set-up, 16-sample segments, combine); "
+                                 "segmented marcher (set-up, 12-sample segments, combine; passes launched as programmatic dependents); "
                                  "the 8 MiB field is L2-resident, so DRAM traffic is far "
                                  "below the algorithmic bytes"}}
 

@@ -57,6 +57,9 @@ constexpr int kMaxSurfaceLayers = 1 << 12;
 #ifndef VSR_MEGA_MIN_BLOCKS
 #define VSR_MEGA_MIN_BLOCKS 12  // ~40 registers: latency hiding beats spill cost
 #endif
+#ifndef VSR_MEGA_MIN_BLOCKS_VOLUMES
+#define VSR_MEGA_MIN_BLOCKS_VOLUMES 8  // ~64 registers for worlds with volumes
+#endif
 #ifndef VSR_MEGA_BLOCK_Y
 #define VSR_MEGA_BLOCK_Y 8  // path-tracer megakernel tile: 16 x VSR_MEGA_BLOCK_Y pixels
 #endif

@@ -71,7 +71,9 @@ __device__ __forceinline__ void batchLoop(const DJob *jobs, const uint2 *items, 
   }
 }
 
-__global__ void __launch_bounds__(128, VSR_MEGA_MIN_BLOCKS)
+// the register budgets of kPathtrace: 64 registers when worlds have volumes
+template <bool Volumes>
+__global__ void __launch_bounds__(128, Volumes ? VSR_MEGA_MIN_BLOCKS_VOLUMES : VSR_MEGA_MIN_BLOCKS)
     kBatchPathtrace(const DJob *jobs, const uint2 *items, unsigned numItems, unsigned *next,
                     int tileW, int fetch) {
   __shared__ __align__(16) DJob sJob[4];
@@ -126,7 +128,9 @@ cudaError_t launchBatch(const BatchLaunch &L, cudaStream_t stream) {
   if (e != cudaSuccess) return e;
   kBatchPrepare<<<smCount() * 4, 256, 0, stream>>>(L.jobs, L.numJobs);
   if ((e = cudaGetLastError()) != cudaSuccess) return e;
-  if ((e = launchPersistent(kBatchPathtrace, L, JOB_PATHTRACE, stream)) != cudaSuccess) return e;
+  e = L.pathtraceVolumes ? launchPersistent(kBatchPathtrace<true>, L, JOB_PATHTRACE, stream)
+                         : launchPersistent(kBatchPathtrace<false>, L, JOB_PATHTRACE, stream);
+  if (e != cudaSuccess) return e;
   if ((e = launchPersistent(kBatchRaycastSurfaces, L, JOB_RAYCAST_SURFACES, stream)) != cudaSuccess)
     return e;
   return launchPersistent(kBatchRaycastVolume, L, JOB_RAYCAST_VOLUME, stream);

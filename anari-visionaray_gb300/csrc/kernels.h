@@ -65,6 +65,7 @@ struct BatchLaunch {
   unsigned *counters;  // kJobKinds work counters
   int tileW;           // 1..32, a divisor of 32
   int fetch;           // items per atomic
+  int pathtraceVolumes;  // a path-traced job's world has volumes: the 64-register kernel
 };
 cudaError_t launchBatch(const BatchLaunch &L, cudaStream_t stream);
 

@@ -1504,6 +1504,8 @@ VSRStatus renderFrames(Device *dev, FrameObj *const *frames, uint32_t count) {
     L.counters = B.counters.as<unsigned>();
     L.tileW = C.tileW;
     L.fetch = C.fetch;
+    for (const DJob &j : jobs)
+      if (j.kind == JOB_PATHTRACE && j.S.numVolumes > 0) L.pathtraceVolumes = 1;
     // one CUDA graph per frame set and configuration: the job records are
     // copied from the pinned staging buffer when the graph runs
     if (!B.graph) {

@@ -64,6 +64,13 @@ struct SegOut {
   float4 m;
 };
 
+// zeroes the set-up pass's counters; the set-up pass is its programmatic
+// dependent and computes its rays before it waits for this grid
+__global__ void kMarchReset(unsigned *counters) {
+  if (threadIdx.x < 4) counters[threadIdx.x] = 0u;
+  asm volatile("griddepcontrol.launch_dependents;\n" ::);
+}
+
 __global__ void __launch_bounds__(256, VSR_SETUP_MIN_BLOCKS) kVolumeSetup(DScene S, DCamera C, DRenderer R, DFrame F,
                                                     MarchScratch M) {
   // the segments pass may launch now; it waits for this grid's results
@@ -124,6 +131,8 @@ __global__ void __launch_bounds__(256, VSR_SETUP_MIN_BLOCKS) kVolumeSetup(DScene
       }
       if (!march) writeSample(F, x, y, false, bg, 1e31f, f3(0.f), f3(0.f));
     }
+    // the counters this block adds to were zeroed by kMarchReset
+    asm volatile("griddepcontrol.wait;\n" ::: "memory");
     const unsigned mask = __ballot_sync(kFull, march);
     const int numRays = __popc(mask);
     const int rank = __popc(mask & ((1u << lane) - 1u));
@@ -554,10 +563,20 @@ cudaError_t launchVolumeMarch(const DScene &S, const DCamera &C, const DRenderer
   }
   const size_t smem = stageTFSize > 0 ? sizeof(float4) * (size_t)stageTFSize : 0;
   const int stage = stageTFSize > 0;
-  cudaError_t e = cudaMemsetAsync(M.counters, 0, 4 * sizeof(unsigned), stream);
-  if (e != cudaSuccess) return e;
   const int numPix = F.width * F.height;
-  kVolumeSetup<<<min((numPix + 255) / 256, sms * 8), 256, 0, stream>>>(S, C, R, F, M);
+  kMarchReset<<<1, 32, 0, stream>>>(M.counters);
+  {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(min((numPix + 255) / 256, sms * 8));
+    cfg.blockDim = dim3(256);
+    cfg.stream = stream;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    cudaLaunchKernelEx(&cfg, kVolumeSetup, S, C, R, F, M);
+  }
   // programmatic dependent launch: a pass's blocks start (and stage the
   // transfer function) while the previous pass drains, and wait for its
   // results with griddepcontrol.wait

@@ -37,6 +37,15 @@ struct Normal {
   }
 };
 
+// keeps the first error of a sequence of launches (argument checks return
+// errors without setting CUDA's last error)
+struct FirstError {
+  cudaError_t e = cudaSuccess;
+  void operator()(cudaError_t r) {
+    if (e == cudaSuccess) e = r;
+  }
+};
+
 template <typename T>
 cudaError_t alloc(T *&p, size_t n, std::vector<void *> *track = nullptr) {
   cudaError_t e = cudaMalloc((void **)&p, std::max<size_t>(n, 1) * sizeof(T));
@@ -171,7 +180,7 @@ cudaError_t Denoiser::ensure(int N, int H, int W, bool train) {
   return cudaSuccess;
 }
 
-void Denoiser::conv(int li, const __nv_bfloat16 *x, int xC, __nv_bfloat16 *y, float *yf, int yC,
+cudaError_t Denoiser::conv(int li, const __nv_bfloat16 *x, int xC, __nv_bfloat16 *y, float *yf, int yC,
                     int N, int H, int W, bool relu, cudaStream_t s, const __nv_bfloat16 *resid) {
   const DenoiseLayer &L = layers_[li];
   ConvArgs a{};
@@ -192,8 +201,7 @@ void Denoiser::conv(int li, const __nv_bfloat16 *x, int xC, __nv_bfloat16 *y, fl
   a.resid = resid;
   a.residC = kInC;
   a.residN = kColorC;
-  if (useTc(W)) launchTc(a, s);
-  else launchConv3x3(a, s);
+  return useTc(W) ? launchTc(a, s) : launchConv3x3(a, s);
 }
 
 cudaError_t Denoiser::launchTc(const ConvArgs &a, cudaStream_t s) const {
@@ -202,7 +210,7 @@ cudaError_t Denoiser::launchTc(const ConvArgs &a, cudaStream_t s) const {
 
 // a decoder convolution on [upsampled coarse level | skip connection],
 // read in place (tcgen05 path)
-void Denoiser::convCat(int li, const __nv_bfloat16 *coarse, int coarseC, const __nv_bfloat16 *skip,
+cudaError_t Denoiser::convCat(int li, const __nv_bfloat16 *coarse, int coarseC, const __nv_bfloat16 *skip,
                        int skipC, __nv_bfloat16 *y, int yC, int N, int H, int W, cudaStream_t s) {
   const DenoiseLayer &L = layers_[li];
   ConvArgs a{};
@@ -223,7 +231,7 @@ void Denoiser::convCat(int li, const __nv_bfloat16 *coarse, int coarseC, const _
   a.N = N;
   a.H = H;
   a.W = W;
-  launchTc(a, s);
+  return launchTc(a, s);
 }
 
 // Weight and bias gradients of layer li from its pre-activation gradient dy
@@ -231,7 +239,7 @@ void Denoiser::convCat(int li, const __nv_bfloat16 *coarse, int coarseC, const _
 // layer's input, zeroed where `mask` (the input itself, a ReLU output) is
 // not positive, which makes it the pre-activation gradient of the layer
 // that produced the input.
-void Denoiser::convBack(int li, const __nv_bfloat16 *x, int xC, const __nv_bfloat16 *dy,
+cudaError_t Denoiser::convBack(int li, const __nv_bfloat16 *x, int xC, const __nv_bfloat16 *dy,
                         __nv_bfloat16 *dx, const __nv_bfloat16 *mask, int N, int H, int W,
                         cudaStream_t s) {
   const DenoiseLayer &L = layers_[li];
@@ -252,8 +260,8 @@ void Denoiser::convBack(int li, const __nv_bfloat16 *x, int xC, const __nv_bfloa
   const int chunks = std::max(1, std::min(2048 / tiles, P / 256));
   const int chunk = (P + chunks - 1) / chunks;
   g.chunk = (chunk + 15) / 16 * 16;
-  launchConvWgrad(g, s);
-  launchBiasGrad(dy, L.cout, 0, L.cout, P, grad_ + L.b, s);
+  cudaError_t e = launchConvWgrad(g, s);
+  if (e == cudaSuccess) e = launchBiasGrad(dy, L.cout, 0, L.cout, P, grad_ + L.b, s);
   if (dx) {
     ConvArgs a{};
     a.x = dy;
@@ -269,55 +277,57 @@ void Denoiser::convBack(int li, const __nv_bfloat16 *x, int xC, const __nv_bfloa
     a.N = N;
     a.H = H;
     a.W = W;
-    if (useTc(W)) launchTc(a, s);
-    else launchConv3x3(a, s);
+    if (e == cudaSuccess) e = useTc(W) ? launchTc(a, s) : launchConv3x3(a, s);
   }
+  return e;
 }
 
 cudaError_t Denoiser::run(const __nv_bfloat16 *x, int N, int H, int W, float *out, cudaStream_t s,
                           bool catOut) {
+  FirstError E;
   const int H1 = H / 2, W1 = W / 2, H2 = H / 4, W2 = W / 4, H3 = H / 8, W3 = W / 8;
   const size_t P0 = (size_t)N * H * W, P1 = P0 / 4, P2 = P0 / 16;
   Act &A = act_;
-  launchToBlocked(x, kInC, P0, A.x0, s);
-  conv(L_E0A, A.x0, kInC, A.a0, nullptr, 32, N, H, W, true, s);
-  conv(L_E0B, A.a0, 32, A.e0, nullptr, 32, N, H, W, true, s);
-  launchMaxPool(A.e0, 32, N, H, W, A.p0, s);
-  conv(L_E1A, A.p0, 32, A.a1, nullptr, 64, N, H1, W1, true, s);
-  conv(L_E1B, A.a1, 64, A.e1, nullptr, 64, N, H1, W1, true, s);
-  launchMaxPool(A.e1, 64, N, H1, W1, A.p1, s);
-  conv(L_E2A, A.p1, 64, A.a2, nullptr, 128, N, H2, W2, true, s);
-  conv(L_E2B, A.a2, 128, A.e2, nullptr, 128, N, H2, W2, true, s);
-  launchMaxPool(A.e2, 128, N, H2, W2, A.p2, s);
-  conv(L_E3A, A.p2, 128, A.a3, nullptr, 256, N, H3, W3, true, s);
-  conv(L_E3B, A.a3, 256, A.e3, nullptr, 256, N, H3, W3, true, s);
+  E(launchToBlocked(x, kInC, P0, A.x0, s));
+  E(conv(L_E0A, A.x0, kInC, A.a0, nullptr, 32, N, H, W, true, s));
+  E(conv(L_E0B, A.a0, 32, A.e0, nullptr, 32, N, H, W, true, s));
+  E(launchMaxPool(A.e0, 32, N, H, W, A.p0, s));
+  E(conv(L_E1A, A.p0, 32, A.a1, nullptr, 64, N, H1, W1, true, s));
+  E(conv(L_E1B, A.a1, 64, A.e1, nullptr, 64, N, H1, W1, true, s));
+  E(launchMaxPool(A.e1, 64, N, H1, W1, A.p1, s));
+  E(conv(L_E2A, A.p1, 64, A.a2, nullptr, 128, N, H2, W2, true, s));
+  E(conv(L_E2B, A.a2, 128, A.e2, nullptr, 128, N, H2, W2, true, s));
+  E(launchMaxPool(A.e2, 128, N, H2, W2, A.p2, s));
+  E(conv(L_E3A, A.p2, 128, A.a3, nullptr, 256, N, H3, W3, true, s));
+  E(conv(L_E3B, A.a3, 256, A.e3, nullptr, 256, N, H3, W3, true, s));
   if (!catOut && useTc(W2)) {
-    convCat(L_D2A, A.e3, 256, A.e2, 128, A.b2, 128, N, H2, W2, s);
+    E(convCat(L_D2A, A.e3, 256, A.e2, 128, A.b2, 128, N, H2, W2, s));
   } else {
-    launchUpsample(A.e3, 256, N, H3, W3, A.cat2, 384, 0, s);
-    launchCopyChannels(A.e2, 128, 0, A.cat2, 384, 256, 128, P2, 0, s);
-    conv(L_D2A, A.cat2, 384, A.b2, nullptr, 128, N, H2, W2, true, s);
+    E(launchUpsample(A.e3, 256, N, H3, W3, A.cat2, 384, 0, s));
+    E(launchCopyChannels(A.e2, 128, 0, A.cat2, 384, 256, 128, P2, 0, s));
+    E(conv(L_D2A, A.cat2, 384, A.b2, nullptr, 128, N, H2, W2, true, s));
   }
-  conv(L_D2B, A.b2, 128, A.d2, nullptr, 128, N, H2, W2, true, s);
+  E(conv(L_D2B, A.b2, 128, A.d2, nullptr, 128, N, H2, W2, true, s));
   if (!catOut && useTc(W1)) {
-    convCat(L_D1A, A.d2, 128, A.e1, 64, A.b1, 64, N, H1, W1, s);
+    E(convCat(L_D1A, A.d2, 128, A.e1, 64, A.b1, 64, N, H1, W1, s));
   } else {
-    launchUpsample(A.d2, 128, N, H2, W2, A.cat1, 192, 0, s);
-    launchCopyChannels(A.e1, 64, 0, A.cat1, 192, 128, 64, P1, 0, s);
-    conv(L_D1A, A.cat1, 192, A.b1, nullptr, 64, N, H1, W1, true, s);
+    E(launchUpsample(A.d2, 128, N, H2, W2, A.cat1, 192, 0, s));
+    E(launchCopyChannels(A.e1, 64, 0, A.cat1, 192, 128, 64, P1, 0, s));
+    E(conv(L_D1A, A.cat1, 192, A.b1, nullptr, 64, N, H1, W1, true, s));
   }
-  conv(L_D1B, A.b1, 64, A.d1, nullptr, 64, N, H1, W1, true, s);
+  E(conv(L_D1B, A.b1, 64, A.d1, nullptr, 64, N, H1, W1, true, s));
   if (!catOut && useTc(W)) {
-    convCat(L_D0A, A.d1, 64, A.e0, 32, A.b0, 32, N, H, W, s);
+    E(convCat(L_D0A, A.d1, 64, A.e0, 32, A.b0, 32, N, H, W, s));
   } else {
-    launchUpsample(A.d1, 64, N, H1, W1, A.cat0, 96, 0, s);
-    launchCopyChannels(A.e0, 32, 0, A.cat0, 96, 64, 32, P0, 0, s);
-    conv(L_D0A, A.cat0, 96, A.b0, nullptr, 32, N, H, W, true, s);
+    E(launchUpsample(A.d1, 64, N, H1, W1, A.cat0, 96, 0, s));
+    E(launchCopyChannels(A.e0, 32, 0, A.cat0, 96, 64, 32, P0, 0, s));
+    E(conv(L_D0A, A.cat0, 96, A.b0, nullptr, 32, N, H, W, true, s));
   }
-  conv(L_D0B, A.b0, 32, A.d0, nullptr, 32, N, H, W, true, s);
+  E(conv(L_D0B, A.b0, 32, A.d0, nullptr, 32, N, H, W, true, s));
   // the output is a correction of the input's log(1 + colour)
-  conv(L_OUT, A.d0, 32, nullptr, out, kOutC, N, H, W, false, s, A.x0);
-  return cudaGetLastError();
+  E(conv(L_OUT, A.d0, 32, nullptr, out, kOutC, N, H, W, false, s, A.x0));
+  E(cudaGetLastError());
+  return E.e;
 }
 
 cudaError_t Denoiser::forward(const __nv_bfloat16 *x, int N, int H, int W, float *out,
@@ -335,42 +345,44 @@ cudaError_t Denoiser::backward(const __nv_bfloat16 *x, const float *target, int 
   cudaError_t e = ensure(N, H, W, true);
   if (e != cudaSuccess) return e;
   if ((e = run(x, N, H, W, out_, s, true)) != cudaSuccess) return e;
+  FirstError E;
   const int H1 = H / 2, W1 = W / 2, H2 = H / 4, W2 = W / 4, H3 = H / 8, W3 = W / 8;
   const size_t P0 = (size_t)N * H * W, P1 = P0 / 4, P2 = P0 / 16;
   Act &A = act_, &G = grd_;
-  cudaMemsetAsync(grad_, 0, numParams_ * sizeof(float), s);
-  if (lossDevice) cudaMemsetAsync(lossDevice, 0, sizeof(float), s);
-  launchL1(out_, kOutC, target, tC, kColorC, P0, gout_, kOutC, lossDevice, s);
+  E(cudaMemsetAsync(grad_, 0, numParams_ * sizeof(float), s));
+  if (lossDevice) E(cudaMemsetAsync(lossDevice, 0, sizeof(float), s));
+  E(launchL1(out_, kOutC, target, tC, kColorC, P0, gout_, kOutC, lossDevice, s));
   // decoder, level 0
-  convBack(L_OUT, A.d0, 32, gout_, G.d0, A.d0, N, H, W, s);
-  convBack(L_D0B, A.b0, 32, G.d0, G.b0, A.b0, N, H, W, s);
-  convBack(L_D0A, A.cat0, 96, G.b0, G.cat0, A.cat0, N, H, W, s);
-  launchUpsampleGrad(G.cat0, 96, 0, 64, N, H1, W1, nullptr, G.d1, s);
+  E(convBack(L_OUT, A.d0, 32, gout_, G.d0, A.d0, N, H, W, s));
+  E(convBack(L_D0B, A.b0, 32, G.d0, G.b0, A.b0, N, H, W, s));
+  E(convBack(L_D0A, A.cat0, 96, G.b0, G.cat0, A.cat0, N, H, W, s));
+  E(launchUpsampleGrad(G.cat0, 96, 0, 64, N, H1, W1, nullptr, G.d1, s));
   // level 1
-  convBack(L_D1B, A.b1, 64, G.d1, G.b1, A.b1, N, H1, W1, s);
-  convBack(L_D1A, A.cat1, 192, G.b1, G.cat1, A.cat1, N, H1, W1, s);
-  launchUpsampleGrad(G.cat1, 192, 0, 128, N, H2, W2, nullptr, G.d2, s);
+  E(convBack(L_D1B, A.b1, 64, G.d1, G.b1, A.b1, N, H1, W1, s));
+  E(convBack(L_D1A, A.cat1, 192, G.b1, G.cat1, A.cat1, N, H1, W1, s));
+  E(launchUpsampleGrad(G.cat1, 192, 0, 128, N, H2, W2, nullptr, G.d2, s));
   // level 2
-  convBack(L_D2B, A.b2, 128, G.d2, G.b2, A.b2, N, H2, W2, s);
-  convBack(L_D2A, A.cat2, 384, G.b2, G.cat2, A.cat2, N, H2, W2, s);
-  launchUpsampleGrad(G.cat2, 384, 0, 256, N, H3, W3, nullptr, G.e3, s);
+  E(convBack(L_D2B, A.b2, 128, G.d2, G.b2, A.b2, N, H2, W2, s));
+  E(convBack(L_D2A, A.cat2, 384, G.b2, G.cat2, A.cat2, N, H2, W2, s));
+  E(launchUpsampleGrad(G.cat2, 384, 0, 256, N, H3, W3, nullptr, G.e3, s));
   // bottleneck, then the encoder: a pooled level gets its gradient from the
   // pooling and from its skip connection
-  convBack(L_E3B, A.a3, 256, G.e3, G.a3, A.a3, N, H3, W3, s);
-  convBack(L_E3A, A.p2, 128, G.a3, G.p2, A.p2, N, H3, W3, s);
-  launchMaxPoolGrad(A.e2, G.p2, 128, N, H2, W2, nullptr, G.e2, s);
-  launchCopyChannels(G.cat2, 384, 256, G.e2, 128, 0, 128, P2, 1, s);
-  convBack(L_E2B, A.a2, 128, G.e2, G.a2, A.a2, N, H2, W2, s);
-  convBack(L_E2A, A.p1, 64, G.a2, G.p1, A.p1, N, H2, W2, s);
-  launchMaxPoolGrad(A.e1, G.p1, 64, N, H1, W1, nullptr, G.e1, s);
-  launchCopyChannels(G.cat1, 192, 128, G.e1, 64, 0, 64, P1, 1, s);
-  convBack(L_E1B, A.a1, 64, G.e1, G.a1, A.a1, N, H1, W1, s);
-  convBack(L_E1A, A.p0, 32, G.a1, G.p0, A.p0, N, H1, W1, s);
-  launchMaxPoolGrad(A.e0, G.p0, 32, N, H, W, nullptr, G.e0, s);
-  launchCopyChannels(G.cat0, 96, 64, G.e0, 32, 0, 32, P0, 1, s);
-  convBack(L_E0B, A.a0, 32, G.e0, G.a0, A.a0, N, H, W, s);
-  convBack(L_E0A, A.x0, kInC, G.a0, nullptr, nullptr, N, H, W, s);
-  return cudaGetLastError();
+  E(convBack(L_E3B, A.a3, 256, G.e3, G.a3, A.a3, N, H3, W3, s));
+  E(convBack(L_E3A, A.p2, 128, G.a3, G.p2, A.p2, N, H3, W3, s));
+  E(launchMaxPoolGrad(A.e2, G.p2, 128, N, H2, W2, nullptr, G.e2, s));
+  E(launchCopyChannels(G.cat2, 384, 256, G.e2, 128, 0, 128, P2, 1, s));
+  E(convBack(L_E2B, A.a2, 128, G.e2, G.a2, A.a2, N, H2, W2, s));
+  E(convBack(L_E2A, A.p1, 64, G.a2, G.p1, A.p1, N, H2, W2, s));
+  E(launchMaxPoolGrad(A.e1, G.p1, 64, N, H1, W1, nullptr, G.e1, s));
+  E(launchCopyChannels(G.cat1, 192, 128, G.e1, 64, 0, 64, P1, 1, s));
+  E(convBack(L_E1B, A.a1, 64, G.e1, G.a1, A.a1, N, H1, W1, s));
+  E(convBack(L_E1A, A.p0, 32, G.a1, G.p0, A.p0, N, H1, W1, s));
+  E(launchMaxPoolGrad(A.e0, G.p0, 32, N, H, W, nullptr, G.e0, s));
+  E(launchCopyChannels(G.cat0, 96, 64, G.e0, 32, 0, 32, P0, 1, s));
+  E(convBack(L_E0B, A.a0, 32, G.e0, G.a0, A.a0, N, H, W, s));
+  E(convBack(L_E0A, A.x0, kInC, G.a0, nullptr, nullptr, N, H, W, s));
+  E(cudaGetLastError());
+  return E.e;
 }
 
 cudaError_t Denoiser::adam(float lr, cudaStream_t s) {

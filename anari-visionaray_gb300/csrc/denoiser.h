@@ -76,11 +76,11 @@ class Denoiser {
   // the tcgen05 convolution: the persistent warp-specialised kernel with
   // TMA loads (kConv3x3Ws), or on path 3 one tile per CTA (kConv3x3Tc)
   cudaError_t launchTc(const ConvArgs &a, cudaStream_t s) const;
-  void convCat(int layer, const __nv_bfloat16 *coarse, int coarseC, const __nv_bfloat16 *skip,
+  cudaError_t convCat(int layer, const __nv_bfloat16 *coarse, int coarseC, const __nv_bfloat16 *skip,
                int skipC, __nv_bfloat16 *y, int yC, int N, int H, int W, cudaStream_t s);
-  void conv(int layer, const __nv_bfloat16 *x, int xC, __nv_bfloat16 *y, float *yf, int yC, int N,
+  cudaError_t conv(int layer, const __nv_bfloat16 *x, int xC, __nv_bfloat16 *y, float *yf, int yC, int N,
             int H, int W, bool relu, cudaStream_t s, const __nv_bfloat16 *resid = nullptr);
-  void convBack(int layer, const __nv_bfloat16 *x, int xC, const __nv_bfloat16 *dy,
+  cudaError_t convBack(int layer, const __nv_bfloat16 *x, int xC, const __nv_bfloat16 *dy,
                 __nv_bfloat16 *dx, const __nv_bfloat16 *mask, int N, int H, int W,
                 cudaStream_t s);
 

@@ -163,6 +163,22 @@ def profiled_traffic(name="pathtrace_config1.txt"):
     return None
 
 
+def profiled_metric(name, metric):
+    """A metric's value from a committed ncu summary line '<metric>  <value> ...'."""
+    path = os.path.join(ROOT, "profiles", name)
+    if not os.path.exists(path):
+        return None
+    with open(path) as f:
+        for ln in f:
+            parts = ln.split()
+            if len(parts) >= 2 and parts[0] == metric:
+                try:
+                    return float(parts[1])
+                except ValueError:
+                    return None
+    return None
+
+
 def cpu_baseline(scene, rows, threads=0):
     """Time the oracle on a band of rows spread over the frame; Mpx*spp/s."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
@@ -622,6 +638,14 @@ def run_ours(args):
                      "frac": achieved / peak, "traffic": traffic,
                      "note": f"algorithmic bytes = BVH node fetches x64 B + triangle fetches x48 B "
                              f"+ frame bytes; peak {peak_kind}; most fetches hit L1/L2"},
+        # traversal and shading are issue- and latency-bound: the issue rate and
+        # the SIMT efficiency of the profiled launch (profiles/pathtrace_config1.txt)
+        "issue": {"issue_active_frac": (lambda v: v / 100 if v is not None else None)(
+                      profiled_metric("pathtrace_config1.txt",
+                                      "smsp__issue_active.avg.pct_of_peak_sustained_active")),
+                  "active_lanes_per_warp_instruction": profiled_metric(
+                      "pathtrace_config1.txt", "smsp__thread_inst_executed_per_inst_executed.ratio"),
+                  "source": "ncu, one 1-spp launch of the same kernel"},
         "traversal": {"rays": rays, "node_visits": nodes, "tri_tests": tris,
                       "node_visit_histogram_log2": counts[8:24],
                       "grays_per_s": rays / kernel_s / 1e9},

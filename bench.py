@@ -59,7 +59,7 @@ def parse():
     p.add_argument("--volume-spp", type=int, default=256)
     p.add_argument("--no-denoise", dest="denoise", action="store_false",
                    help="skip the config-4 denoiser training and evaluation")
-    p.add_argument("--denoise-train-scenes", type=int, default=64)
+    p.add_argument("--denoise-train-scenes", type=int, default=128)
     p.add_argument("--denoise-eval-scenes", type=int, default=8)
     p.add_argument("--denoise-steps", type=int, default=4000)
     p.add_argument("--denoise-forward-only", action="store_true",
@@ -366,7 +366,7 @@ def measure_denoiser_forward(pkg, dev):
             "roofline": denoiser_roofline(dn_s)}
 
 
-def measure_denoiser_config4(pkg, dev, train_scenes=64, eval_scenes=8, steps=4000,
+def measure_denoiser_config4(pkg, dev, train_scenes=128, eval_scenes=8, steps=4000,
                              train_ref_spp=1024, eval_ref_spp=4096, res=256):
     """Config 4 (learned denoiser): train the U-Net on path-traced pairs
     (inputs after 4, 8, 16 and 32 spp, 1024-spp references, 256^2 images,

@@ -32,16 +32,18 @@ __global__ void kBatchPrepare(const DJob *jobs, int numJobs) {
   }
 }
 
-template <int Kind>
+template <int Kind, bool Shade>
 __device__ __forceinline__ void renderItem(const DJob &J, int x, int y) {
-  if (Kind == JOB_PATHTRACE) pathtracePixel<false>(J.S, J.C, J.R, J.F, x, y);
+  if (Kind == JOB_PATHTRACE) pathtracePixel<false, Shade>(J.S, J.C, J.R, J.F, x, y);
   else if (Kind == JOB_RAYCAST_SURFACES) raycastPixel<false, true>(J.S, J.C, J.R, J.F, x, y, nullptr);
+  else if (Kind == JOB_RAYCAST_SHADED)
+    raycastPixel<false, true, true>(J.S, J.C, J.R, J.F, x, y, nullptr);
   else raycastPixel<false, false>(J.S, J.C, J.R, J.F, x, y, nullptr);
 }
 
 // Items are (job, tile) pairs; a tile is tileW x (32 / tileW) pixels. A warp
 // takes `fetch` consecutive items per atomic.
-template <int Kind>
+template <int Kind, bool Shade = false>
 __device__ __forceinline__ void batchLoop(const DJob *jobs, const uint2 *items, unsigned numItems,
                                           unsigned *next, int tileW, int fetch, DJob *sJob) {
   const int lane = threadIdx.x & 31;
@@ -66,18 +68,20 @@ __device__ __forceinline__ void batchLoop(const DJob *jobs, const uint2 *items, 
       }
       const int tx = (int)it.y % sJob->tilesX, ty = (int)it.y / sJob->tilesX;
       const int x = tx * tileW + px, y = ty * tileH + py;
-      if (x < sJob->F.width && y < sJob->F.height) renderItem<Kind>(*sJob, x, y);
+      if (x < sJob->F.width && y < sJob->F.height) renderItem<Kind, Shade>(*sJob, x, y);
     }
   }
 }
 
-// the register budgets of kPathtrace: 64 registers when worlds have volumes
-template <bool Volumes>
+// the register budgets of kPathtrace: 64 registers when worlds have volumes;
+// Shade: a job lights volume scatter events along the field gradient
+template <bool Volumes, bool Shade>
 __global__ void __launch_bounds__(128, Volumes ? VSR_MEGA_MIN_BLOCKS_VOLUMES : VSR_MEGA_MIN_BLOCKS)
     kBatchPathtrace(const DJob *jobs, const uint2 *items, unsigned numItems, unsigned *next,
                     int tileW, int fetch) {
   __shared__ __align__(16) DJob sJob[4];
-  batchLoop<JOB_PATHTRACE>(jobs, items, numItems, next, tileW, fetch, &sJob[threadIdx.x >> 5]);
+  batchLoop<JOB_PATHTRACE, Shade>(jobs, items, numItems, next, tileW, fetch,
+                                  &sJob[threadIdx.x >> 5]);
 }
 
 __global__ void __launch_bounds__(128)
@@ -93,6 +97,15 @@ __global__ void __launch_bounds__(128)
                         int tileW, int fetch) {
   __shared__ __align__(16) DJob sJob[4];
   batchLoop<JOB_RAYCAST_VOLUME>(jobs, items, numItems, next, tileW, fetch,
+                                &sJob[threadIdx.x >> 5]);
+}
+
+// raycast frames with gradient shading, any world
+__global__ void __launch_bounds__(128)
+    kBatchRaycastShaded(const DJob *jobs, const uint2 *items, unsigned numItems, unsigned *next,
+                        int tileW, int fetch) {
+  __shared__ __align__(16) DJob sJob[4];
+  batchLoop<JOB_RAYCAST_SHADED>(jobs, items, numItems, next, tileW, fetch,
                                 &sJob[threadIdx.x >> 5]);
 }
 
@@ -128,12 +141,15 @@ cudaError_t launchBatch(const BatchLaunch &L, cudaStream_t stream) {
   if (e != cudaSuccess) return e;
   kBatchPrepare<<<smCount() * 4, 256, 0, stream>>>(L.jobs, L.numJobs);
   if ((e = cudaGetLastError()) != cudaSuccess) return e;
-  e = L.pathtraceVolumes ? launchPersistent(kBatchPathtrace<true>, L, JOB_PATHTRACE, stream)
-                         : launchPersistent(kBatchPathtrace<false>, L, JOB_PATHTRACE, stream);
+  e = L.pathtraceVolumes == 2 ? launchPersistent(kBatchPathtrace<true, true>, L, JOB_PATHTRACE, stream)
+      : L.pathtraceVolumes    ? launchPersistent(kBatchPathtrace<true, false>, L, JOB_PATHTRACE, stream)
+                              : launchPersistent(kBatchPathtrace<false, false>, L, JOB_PATHTRACE, stream);
   if (e != cudaSuccess) return e;
   if ((e = launchPersistent(kBatchRaycastSurfaces, L, JOB_RAYCAST_SURFACES, stream)) != cudaSuccess)
     return e;
-  return launchPersistent(kBatchRaycastVolume, L, JOB_RAYCAST_VOLUME, stream);
+  if ((e = launchPersistent(kBatchRaycastVolume, L, JOB_RAYCAST_VOLUME, stream)) != cudaSuccess)
+    return e;
+  return launchPersistent(kBatchRaycastShaded, L, JOB_RAYCAST_SHADED, stream);
 }
 
 }  // namespace vsr

@@ -46,7 +46,13 @@ cudaError_t launchPathtraceWavefront(const DScene &S, const DCamera &C, const DR
 // Batched rendering (k_batch.cu). A job is one frame's records; kinds are
 // rendered by separate persistent kernels, each over its own work list of
 // (job, tile) items with tiles of tileW x (32 / tileW) pixels.
-enum JobKind { JOB_PATHTRACE = 0, JOB_RAYCAST_SURFACES = 1, JOB_RAYCAST_VOLUME = 2, kJobKinds = 3 };
+enum JobKind {
+  JOB_PATHTRACE = 0,
+  JOB_RAYCAST_SURFACES = 1,
+  JOB_RAYCAST_VOLUME = 2,
+  JOB_RAYCAST_SHADED = 3,  // raycast with gradient shading
+  kJobKinds = 4
+};
 struct DJob {
   DScene S;
   DCamera C;
@@ -65,7 +71,8 @@ struct BatchLaunch {
   unsigned *counters;  // kJobKinds work counters
   int tileW;           // 1..32, a divisor of 32
   int fetch;           // items per atomic
-  int pathtraceVolumes;  // a path-traced job's world has volumes: the 64-register kernel
+  int pathtraceVolumes;  // a path-traced job's world has volumes: the 64-register kernel;
+                         // 2: one of them also has gradient shading
 };
 cudaError_t launchBatch(const BatchLaunch &L, cudaStream_t stream);
 

@@ -689,6 +689,51 @@ __device__ __forceinline__ LightSample sampleLight(const DLight &L, Rng &rnd) {
   return s;
 }
 
+// Normalised central-difference gradient of the field at voxel-space point
+// P, one offset of `delta` per axis (sampleGradient,
+// DeviceCopyableObjects.h:582-597; a structured field is sampled
+// everywhere, so the difference is always taken). A zero difference
+// normalises to NaN components, as in the reference, and fails the length
+// tests that follow.
+__device__ __forceinline__ float fieldAt(const DVolume &V, float3 P, bool hw);
+__device__ __forceinline__ float3 fieldGradient(const DVolume &V, float3 P, float3 delta, bool hw) {
+  const float x1 = fieldAt(V, P + f3(delta.x, 0.f, 0.f), hw);
+  const float x0 = fieldAt(V, P - f3(delta.x, 0.f, 0.f), hw);
+  const float y1 = fieldAt(V, P + f3(0.f, delta.y, 0.f), hw);
+  const float y0 = fieldAt(V, P - f3(0.f, delta.y, 0.f), hw);
+  const float z1 = fieldAt(V, P + f3(0.f, 0.f, delta.z), hw);
+  const float z0 = fieldAt(V, P - f3(0.f, 0.f, delta.z), hw);
+  const float3 g = f3(x1, y1, z1) - f3(x0, y0, z0);
+  return g / sqrtf(dot(g, g));
+}
+
+// Gradient shading of one classified sample (rayMarchVolume<1>,
+// renderer/VolumeIntegration.h:420-460): a matte surface of the sample's
+// colour along the gradient, lit by every light, plus the ambient term.
+// Like the reference, the gradient is in voxel space and the light
+// directions in world space. viewDir need not be normalised. The raycast
+// renderer has no random stream (renderer/Raycast_impl.cpp:267): each light
+// is sampled with a zero-state generator, as for surfaces.
+__device__ __forceinline__ float3 gradientShade(const DScene &S, const DRenderer &R,
+                                                const DVolume &V, float3 P, float3 delta,
+                                                float3 viewDir, float3 rgb, bool hw) {
+  float3 gn = fieldGradient(V, P, delta, hw);
+  gn = faceforward(gn, viewDir, gn);
+  float3 shaded = f3(0.f);
+  if (length(gn) > 1e-10f) {
+    for (int li = 0; li < S.numLights; ++li) {
+      Rng none;
+      none.state = 0;
+      const LightSample ls = sampleLight(S.lights[li], none);
+      const float3 lightDir = normalize(ls.dir);
+      const float3 lightIntensity = ls.intensity * safeRcp(ls.dist2);
+      const float NdotL = fmaxf(0.f, dot(gn, lightDir));
+      shaded += rgb * kInvPi * lightIntensity * NdotL * safeRcp(ls.pdf);
+    }
+  }
+  return shaded + rgb * ld3(R.ambientColor) * R.ambientRadiance;
+}
+
 // ----------------------------------------------------------------- volumes
 // tex3D(normalized coords, linear, clamp) on the structured field,
 // sampleField DeviceCopyableObjects.h:478-481; texel i is centred at

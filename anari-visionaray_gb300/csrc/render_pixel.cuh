@@ -13,7 +13,10 @@ namespace vsr {
 
 // ------------------------------------------------------------------ raycast
 // renderSample, renderer/Raycast_impl.cpp:10-243 (default render mode).
-template <bool Count, bool Surfaces>
+// Shade = true is the gradient-shading variant (the shading code, with its
+// six extra field samples per step, stays out of the plain kernels'
+// register allocation).
+template <bool Count, bool Surfaces, bool Shade>
 __device__ void raycastSample(const DScene &S, const DRenderer &R, Ray ray, const float4 *sTF,
                               float4 &outColor, float &outDepth, float3 &outNg, float3 &outAlbedo,
                               uint32_t &err, unsigned long long *cnt) {
@@ -145,7 +148,10 @@ __device__ void raycastSample(const DScene &S, const DRenderer &R, Ray ray, cons
           // weights): use the fast pow there, the exact one otherwise
           const float stepTr = hw ? __powf(1.f - s.w, expo) : powf(1.f - s.w, expo);
           const float w = transmittance * (1.f - stepTr);
-          color += w * f3(s.x, s.y, s.z);
+          float3 rgb = f3(s.x, s.y, s.z);
+          if (Shade && R.gradientShading)
+            rgb = gradientShade(S, R, V, o + d * tk[k], Sv * V.cellSize, -d, rgb, hw);
+          color += w * rgb;
           alpha += w;
           transmittance *= stepTr;
           if (Count) ++samples;
@@ -166,7 +172,7 @@ __device__ void raycastSample(const DScene &S, const DRenderer &R, Ray ray, cons
 // One pixel of the raycast renderer: pixelSamples camera rays through the
 // pixel centre, averaged (renderer/Raycast_impl.cpp:282-322). sTF is the
 // first volume's TF staged in shared memory, or null.
-template <bool Count, bool Surfaces>
+template <bool Count, bool Surfaces, bool Shade = false>
 __device__ __forceinline__ void raycastPixel(const DScene &S, const DCamera &C, const DRenderer &R,
                                              const DFrame &F, int x, int y, const float4 *sTF) {
   uint32_t err = 0;
@@ -183,7 +189,7 @@ __device__ __forceinline__ void raycastPixel(const DScene &S, const DCamera &C, 
     float4 c;
     float dd;
     float3 nn, aa;
-    raycastSample<Count, Surfaces>(S, R, ray, sTF, c, dd, nn, aa, err, cnt);
+    raycastSample<Count, Surfaces, Shade>(S, R, ray, sTF, c, dd, nn, aa, err, cnt);
     acc.x += c.x; acc.y += c.y; acc.z += c.z; acc.w += c.w;
     if (s == 0) { c0 = c; d0 = dd; n0 = nn; a0 = aa; }
   }
@@ -203,6 +209,7 @@ struct HitRec {
   float volT;
   float3 volAlbedo;
   int volInst;
+  int volIdx;  // the volume hit
 };
 
 // intersectAll, renderer/common.h:1605-1620, with intersectSurfaces<1>
@@ -252,6 +259,7 @@ __device__ __forceinline__ void intersectAll(const DScene &S, const Ray &ray, bo
           h.volT = t;
           h.volAlbedo = alb;
           h.volInst = i;
+          h.volIdx = S.groupVolumes[k];
         }
       }
     }
@@ -262,7 +270,9 @@ __device__ __forceinline__ void intersectAll(const DScene &S, const Ray &ray, bo
 
 // Per-pixel body of VisionarayRendererPathtrace::renderFrame
 // (renderer/Pathtrace_impl.cpp:498-640) with shade() (:93-487) inlined.
-template <bool Count>
+// Shade = true is the variant with gradient shading of volume hits (kept out
+// of the plain kernels' register allocation).
+template <bool Count, bool Shade>
 __device__ __forceinline__ void pathtracePixel(const DScene &S, const DCamera &C,
                                                const DRenderer &R, const DFrame &F, int x, int y) {
   uint32_t err = 0;
@@ -333,7 +343,17 @@ __device__ __forceinline__ void pathtracePixel(const DScene &S, const DCamera &C
               hitPos = ray.o + hr.volT * ray.d;
               eps = epsilonFrom(hitPos, ray.d, hr.volT);
               gn = f3(0.f);
-              if (R.ambientSamples > 0) {
+              if (Shade && R.gradientShading) {
+                // the field gradient at the instance-local hit position in
+                // voxel space (renderer/Pathtrace_impl.cpp:204-212)
+                const DVolume &V = S.volumes[hr.volIdx];
+                float3 lo, ld;
+                localRay(I, ray.o, ray.d, lo, ld);
+                const float3 Sv = ld3(V.S);
+                gn = fieldGradient(V, Sv * (lo + hr.volT * ld + ld3(V.T)), Sv * V.cellSize,
+                                   R.hwFilter != 0);
+              }
+              if (R.ambientSamples > 0 && length(gn) < 1e-3f) {
                 const float u1 = rnd(), u2 = rnd();
                 gn = uniformSampleSphere(u1, u2);
               }
@@ -373,7 +393,11 @@ __device__ __forceinline__ void pathtracePixel(const DScene &S, const DCamera &C
             const float3 lightIntensity = ls.intensity * safeRcp(ls.dist2);
             const float NdotL = fmaxf(0.f, dot(sn, lightDir));
             if (hr.volumeHit) {
-              shadedColor = hr.volAlbedo * lightIntensity * safeRcp(ls.pdf) * safeRcp(ls.dist2);
+              if (Shade && R.gradientShading && length(gn) > 1e-10f)  // matte along the gradient
+                shadedColor = hr.volAlbedo * kInvPi * lightIntensity * NdotL * safeRcp(ls.pdf) *
+                              float(S.numLights);
+              else
+                shadedColor = hr.volAlbedo * lightIntensity * safeRcp(ls.pdf) * safeRcp(ls.dist2);
               const float u1 = rnd(), u2 = rnd();
               bsdf.dir = uniformSampleSphere(u1, u2);
               bsdf.f = hr.volAlbedo;

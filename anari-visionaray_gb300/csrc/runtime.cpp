@@ -710,15 +710,19 @@ struct Renderer : Object {
     getv("ambientColor", VSR_FLOAT32_VEC3, ac);
     float ar = 0.2f;
     getf("ambientRadiance", ar);
-    for (int k = 0; k < 3; ++k) r.ambient[k] = ac[k] * ar;
+    for (int k = 0; k < 3; ++k) {
+      r.ambient[k] = ac[k] * ar;
+      r.ambientColor[k] = ac[k];
+    }
+    r.ambientRadiance = ar;
     std::string mode = gets("mode", "default");
     if (mode != "default")
       dev->report(this, kind, VSR_SEVERITY_WARNING, VSR_ERROR_INVALID_ARGUMENT,
                   "render mode '%s' is not supported; using 'default'", mode.c_str());
     int b = 0;
-    if (geti("gradientShading", b) && b)
-      dev->report(this, kind, VSR_SEVERITY_WARNING, VSR_ERROR_INVALID_ARGUMENT,
-                  "'gradientShading' is not supported");
+    // Renderer.cpp:50: volume samples (raycast) and volume scatter events
+    // (path tracer) lit along the field gradient
+    r.gradientShading = geti("gradientShading", b) && b ? 1 : 0;
     if (geti("taa", b) && b)
       dev->report(this, kind, VSR_SEVERITY_WARNING, VSR_ERROR_INVALID_ARGUMENT, "'taa' is not supported");
     int v;
@@ -1254,14 +1258,16 @@ VSRStatus renderFrame(Device *dev, FrameObj *F) {
   if (doRender && R.type == REND_RAYCAST) {
     // stage the first volume's TF in shared memory when it fits (64 KB)
     if (!W->volsHost.empty() && W->volsHost[0].tfSize <= 4096) stage = W->volsHost[0].tfSize;
-    segmented = !W->scene.hasSurfaces && R.pixelSamples == 1;
+    // the segmented marcher composites unshaded samples; gradient shading
+    // takes the per-pixel kernel
+    segmented = !W->scene.hasSurfaces && R.pixelSamples == 1 && !R.gradientShading;
     if (segmented && !F->ensureMarch()) {
       dev->report(F, VSR_FRAME, VSR_SEVERITY_ERROR, VSR_ERROR_OUT_OF_MEMORY,
                   "volume marcher scratch allocation failed");
       return VSR_ERROR_OUT_OF_MEMORY;
     }
     if (segmented) ms = F->march();
-  } else if (doRender && F->renderer->wavefront && !F->ensureWave()) {
+  } else if (doRender && F->renderer->wavefront && !R.gradientShading && !F->ensureWave()) {
     dev->report(F, VSR_FRAME, VSR_SEVERITY_ERROR, VSR_ERROR_OUT_OF_MEMORY,
                 "wavefront state allocation failed");
     return VSR_ERROR_OUT_OF_MEMORY;
@@ -1278,7 +1284,9 @@ VSRStatus renderFrame(Device *dev, FrameObj *F) {
     if (R.type == REND_RAYCAST) {
       e = launchRaycast(W->scene, F->camera->c, R, fr, stage, F->countStats,
                         segmented ? &ms : nullptr, s);
-    } else if (F->renderer->wavefront) {
+    } else if (F->renderer->wavefront && !R.gradientShading) {
+      // (the wavefront shading kernel has no gradient shading: the
+      // megakernel takes such frames)
       e = launchPathtraceWavefront(W->scene, F->camera->c, R, fr, F->wave(), F->pinnedCount,
                                    F->countStats, s, &F->lastIterations);
     } else {
@@ -1354,7 +1362,7 @@ struct BatchState {
   std::vector<uint64_t> key;  // frame set and its work (sizes, kinds, sample counts)
   int config = -1;            // configuration of the items and the graph below
   DevBuf jobs, items[kJobKinds], counters;
-  unsigned numItems[kJobKinds] = {0, 0, 0};
+  unsigned numItems[kJobKinds] = {};
   DJob *jobsHost = nullptr;  // pinned staging, read by the graph's copy
   size_t jobsCap = 0;
   int numJobs = 0;
@@ -1436,16 +1444,17 @@ VSRStatus renderFrames(Device *dev, FrameObj *const *frames, uint32_t count) {
       F->nextReset = false;
     }
     j.F = F->record();
-    j.kind = j.R.type == REND_RAYCAST
-                 ? (j.S.hasSurfaces ? JOB_RAYCAST_SURFACES : JOB_RAYCAST_VOLUME)
-                 : JOB_PATHTRACE;
+    j.kind = j.R.type != REND_RAYCAST ? JOB_PATHTRACE
+             : j.R.gradientShading    ? JOB_RAYCAST_SHADED
+             : j.S.hasSurfaces        ? JOB_RAYCAST_SURFACES
+                                      : JOB_RAYCAST_VOLUME;
     // a frame past its sample limit only clears its error flags
     if (F->accumID >= F->renderer->sampleLimit) j.F.width = j.F.height = 0;
     jobs.push_back(j);
     batched.push_back(F);
     key.insert(key.end(), {(uint64_t)(uintptr_t)F, (uint64_t)j.F.width, (uint64_t)j.F.height,
                            (uint64_t)j.kind, (uint64_t)j.R.pixelSamples, (uint64_t)j.R.maxBounce,
-                           (uint64_t)j.S.numVolumes});
+                           (uint64_t)j.S.numVolumes, (uint64_t)j.R.gradientShading});
   }
   if (!batched.empty()) {
     BatchTuner &tuner = B.tuners[key];
@@ -1505,7 +1514,8 @@ VSRStatus renderFrames(Device *dev, FrameObj *const *frames, uint32_t count) {
     L.tileW = C.tileW;
     L.fetch = C.fetch;
     for (const DJob &j : jobs)
-      if (j.kind == JOB_PATHTRACE && j.S.numVolumes > 0) L.pathtraceVolumes = 1;
+      if (j.kind == JOB_PATHTRACE && j.S.numVolumes > 0)
+        L.pathtraceVolumes = std::max(L.pathtraceVolumes, j.R.gradientShading ? 2 : 1);
     // one CUDA graph per frame set and configuration: the job records are
     // copied from the pinned staging buffer when the graph runs
     if (!B.graph) {

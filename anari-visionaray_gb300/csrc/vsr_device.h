@@ -180,12 +180,15 @@ struct DRenderer {
   int type;
   float bg[4];
   float ambient[3];    // ambientColor * ambientRadiance
+  float ambientColor[3];
+  float ambientRadiance;
   float occlusionDistance;
   int ambientSamples;
   int maxBounce;
   int pixelSamples;
   float samplingRateInv;
   int hwFilter;        // 1: field samples through the texture unit's trilinear filter
+  int gradientShading; // volume samples lit along the normalised field gradient
   int numClipPlanes;
   float clip[kMaxClipPlanes][4];
 };

@@ -984,6 +984,43 @@ struct PixelSample {
 };
 
 // Raycast renderSample, renderer/Raycast_impl.cpp:10-243.
+// sampleGradient (DeviceCopyableObjects.h:582-597): central differences of
+// the field at voxel-space P, one offset of `delta` per axis, normalised as
+// the callers do (VolumeIntegration.h:424-425, Pathtrace_impl.cpp:209-210).
+// A zero difference normalises to NaN, as there.
+f3 fieldGradient(const OrVolume *v, f3 P, f3 delta) {
+  f3 g(sampleField(v, P + f3(delta.x, 0.f, 0.f)) - sampleField(v, P - f3(delta.x, 0.f, 0.f)),
+       sampleField(v, P + f3(0.f, delta.y, 0.f)) - sampleField(v, P - f3(0.f, delta.y, 0.f)),
+       sampleField(v, P + f3(0.f, 0.f, delta.z)) - sampleField(v, P - f3(0.f, 0.f, delta.z)));
+  return g / std::sqrt(dot(g, g));
+}
+
+// The voxel-space offsets of the gradient: cellSize times the diagonal of
+// the voxel-space transform (VolumeIntegration.h:398-401).
+f3 gradientDelta(const Vol &vol) { return vol.S * vol.cellSize; }
+
+// rayMarchVolume<1>'s shading of one classified sample
+// (VolumeIntegration.h:420-460): a matte surface of the sample's colour
+// along the face-forwarded gradient, lit by every light (zero-state
+// generator, as for surfaces), plus the ambient term.
+f3 gradientShade(const OrScene &S, const OrRenderer &R, const Vol &vol, f3 P, f3 viewDir, f3 rgb) {
+  f3 gn = fieldGradient(vol.v, P, gradientDelta(vol));
+  gn = faceforward(gn, viewDir, gn);
+  f3 shaded(0.f);
+  if (length(gn) > 1e-10f) {
+    for (int li = 0; li < S.numLights; ++li) {
+      LCG dummy(0, 0);
+      LightSample ls = sampleLight(S.lights[li], dummy);
+      f3 lightDir = normalize(ls.dir);
+      f3 lightIntensity = ls.intensity * safe_rcp(ls.dist2);
+      const float NdotL = std::fmax(0.f, dot(gn, lightDir));
+      shaded += rgb * kInvPi * lightIntensity * NdotL * safe_rcp(ls.pdf);
+    }
+  }
+  return shaded + rgb * f3(R.ambientColor[0], R.ambientColor[1], R.ambientColor[2]) *
+                      R.ambientRadiance;
+}
+
 PixelSample raycastSample(const Scene &sc, const OrRenderer &R, Ray ray, Counters &c) {
   PixelSample result;
   f4 bgColor(R.background[0], R.background[1], R.background[2], R.background[3]);
@@ -1080,7 +1117,9 @@ PixelSample raycastSample(const Scene &sc, const OrRenderer &R, Ray ray, Counter
       float v = sampleField(vol.v, P);
       f4 s = postClassify(vol.v, v);
       float stepTransmittance = std::pow(1.f - s.w, expo);
-      color += transmittance * (1.f - stepTransmittance) * s.xyz();
+      f3 rgb = s.xyz();
+      if (R.gradientShading) rgb = gradientShade(S, R, vol, P, -l.dir, rgb);
+      color += transmittance * (1.f - stepTransmittance) * rgb;
       alpha += transmittance * (1.f - stepTransmittance);
       transmittance *= stepTransmittance;
     }
@@ -1166,6 +1205,13 @@ void shade(const Scene &sc, const OrRenderer &R, LCG &rnd, const Ray &ray, RayTy
       hitPos = ray.ori + hv.t * ray.dir;
       eps = epsilonFrom(hitPos, ray.dir, hv.t);
       gn = f3(0.f);
+      if (R.gradientShading) {
+        // the gradient at the instance-local hit position in voxel space
+        // (Pathtrace_impl.cpp:203-211)
+        const Vol &vol = sc.vols[hv.vol];
+        Ray l = inst.toLocal(ray);
+        gn = fieldGradient(vol.v, vol.pointToVoxelSpace(l.ori + hv.t * l.dir), gradientDelta(vol));
+      }
       if (R.ambientSamples > 0 && length(gn) < 1e-3f) {
         float u1 = rnd(), u2 = rnd();
         gn = uniform_sample_sphere(u1, u2);
@@ -1211,7 +1257,11 @@ void shade(const Scene &sc, const OrRenderer &R, LCG &rnd, const Ray &ray, RayTy
     const float NdotL = std::fmax(0.f, dot(sn, lightDir));
     if (hitRec.volumeHit) {
       const f3 &alb = hitRec.volume.albedo;
-      ss.shadedColor = alb * lightIntensity * safe_rcp(ss.light.pdf) * safe_rcp(ss.light.dist2);
+      if (R.gradientShading && length(gn) > 1e-10f)  // matte along the gradient, :313-328
+        ss.shadedColor = alb * kInvPi * lightIntensity * NdotL * safe_rcp(ss.light.pdf) *
+                         float(S.numLights);
+      else
+        ss.shadedColor = alb * lightIntensity * safe_rcp(ss.light.pdf) * safe_rcp(ss.light.dist2);
       float u1 = rnd(), u2 = rnd();
       ss.bsdf.dir = uniform_sample_sphere(u1, u2);
       ss.bsdf.f = alb;

@@ -77,7 +77,8 @@ class OrRenderer(ctypes.Structure):
     _fields_ = [("type", c_int32), ("background", c_float * 4), ("ambientColor", c_float * 3),
                 ("ambientRadiance", c_float), ("occlusionDistance", c_float),
                 ("ambientSamples", c_int32), ("maxBounce", c_int32), ("pixelSamples", c_int32),
-                ("volumeSamplingRate", c_float), ("numClipPlanes", c_int32), ("clipPlanes", FP)]
+                ("volumeSamplingRate", c_float), ("numClipPlanes", c_int32), ("clipPlanes", FP),
+                ("gradientShading", c_int32)]
 
 
 class OrFrame(ctypes.Structure):
@@ -334,6 +335,7 @@ def renderer(r):
     orr.numClipPlanes = len(planes)
     orr._planes = np.ascontiguousarray(planes)
     orr.clipPlanes = fptr(orr._planes)
+    orr.gradientShading = 1 if r.get("gradientShading", False) else 0
     return orr
 
 

@@ -114,6 +114,7 @@ typedef struct OrRenderer {
   float volumeSamplingRate;
   int32_t numClipPlanes;
   const float *clipPlanes;   /* float4 (n.xyz, d) each */
+  int32_t gradientShading;   /* volume samples lit along the field gradient */
 } OrRenderer;
 
 typedef struct OrFrame {

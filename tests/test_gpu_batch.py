@@ -88,6 +88,41 @@ def test_batch_matches_single_frames(pkg, device):
             release(dev, h)
 
 
+def test_batch_gradient_shading(pkg, device):
+    """Raycast and path-traced frames with gradient shading batched beside an
+    unshaded raycast frame (the shaded frames take their own kernel variants):
+    the same images as rendered one at a time."""
+    dev = device
+    base = small_batch(pkg)
+
+    def shaded(s):
+        return dict(s, renderer=dict(s["renderer"], gradientShading=True))
+
+    scenes = [shaded(base[0]), shaded(base[1]), shaded(base[3]), base[0]]
+    single = [pkg.scenes.build(dev, s, channels=CHANNELS) for s in scenes]
+    batch = [pkg.scenes.build(dev, s, channels=CHANNELS) for s in scenes]
+    frames = [h["frame"] for h in batch]
+    try:
+        for it in range(3):
+            for h in single:
+                assert dev.render(h["frame"]) == 0
+            assert dev.render_batch(frames) == 0
+            for h in single + batch:
+                dev.wait(h["frame"])
+            for k, (a, b) in enumerate(zip(single, batch)):
+                assert dev.get_uint(b["frame"], "errorFlags") == 0
+                for ch in CHANNELS:
+                    x, y = dev.map(a["frame"], "channel." + ch), dev.map(b["frame"], "channel." + ch)
+                    same_bits(x, y, f"shaded frame {k} {ch} batch {it}")
+        # the shading changed the raycast image
+        a = dev.map(batch[0]["frame"], "channel.color")
+        b = dev.map(batch[3]["frame"], "channel.color")
+        assert np.abs(a[..., :3] - b[..., :3]).max() > 1e-2
+    finally:
+        for h in single + batch:
+            release(dev, h)
+
+
 def test_batch_commit_resets_accumulation(pkg, device):
     """A commit to one frame's camera restarts that frame's accumulation in
     the batch exactly as vsrRenderFrame does."""

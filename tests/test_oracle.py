@@ -148,6 +148,54 @@ def test_emission_absorption_slab(oracle):
     assert np.allclose(F.color[..., 3], alpha + (1 - alpha), rtol=1e-6)
 
 
+def ramp_volume_scene(gradient_shading, toward_camera):
+    """A 16^3 field that rises linearly along z (toward or away from an
+    orthographic camera looking down -z), one constant TF colour, a
+    directional light."""
+    n = 16
+    ramp = np.linspace(0.0, 1.0, n, dtype=np.float32)
+    if not toward_camera:
+        ramp = ramp[::-1].copy()
+    data = np.ascontiguousarray(np.broadcast_to(ramp[:, None, None], (n, n, n)))
+    tf = np.array([[0.8, 0.6, 0.4, 0.05]] * 4, np.float32)
+    return {
+        "surfaces": [],
+        "lights": [{"direction": [0.3, -0.4, -0.866], "color": [1.0, 1.0, 1.0],
+                    "irradiance": 2.0}],
+        "volumes": [{"data": data, "origin": [0, 0, 0], "spacing": [1, 1, 1],
+                     "color": tf[:, :3], "opacity": tf[:, 3], "valueRange": [0, 1],
+                     "unitDistance": 1.0}],
+        "camera": {"type": "orthographic", "position": [7.5, 7.5, 40.0],
+                   "direction": [0, 0, -1], "up": [0, 1, 0], "height": 10.0, "aspect": 1.0},
+        "renderer": {"type": "raycast", "volumeSamplingRate": 1.0, "background": [0, 0, 0, 1],
+                     "ambientColor": [1.0, 0.5, 0.25], "ambientRadiance": 0.3,
+                     "gradientShading": gradient_shading},
+        "frame": {"size": (8, 8)},
+    }
+
+
+@pytest.mark.parametrize("toward_camera", [True, False])
+def test_gradient_shading_closed_form(oracle, toward_camera):
+    """Raycast gradient shading (VolumeIntegration.h:420-460) of a linear
+    ramp: the face-forwarded gradient is +z (toward the viewer) at every
+    sample, so each sample's colour is scaled by the same
+    E/pi * max(0, N.L) + ambientColor * ambientRadiance, and so is the
+    composite (black background)."""
+    frames = {}
+    for g in (False, True):
+        S = oracle.Scene(ramp_volume_scene(g, toward_camera))
+        F = oracle.Frame(8, 8)
+        oracle.render(S, F)
+        frames[g] = F.color.copy()
+    plain, shaded = frames[False], frames[True]
+    L = -np.array([0.3, -0.4, -0.866])
+    L /= np.linalg.norm(L)
+    scale = 2.0 / math.pi * max(0.0, float(L[2])) + np.array([1.0, 0.5, 0.25]) * 0.3
+    assert plain[..., :3].min() > 1e-3  # every pixel sees the volume
+    assert np.allclose(shaded[..., :3], plain[..., :3] * scale, rtol=1e-4, atol=1e-7)
+    assert np.array_equal(shaded[..., 3], plain[..., 3])  # opacity is not shaded
+
+
 def test_bvh_closest_hit_matches_brute_force(oracle, pkg):
     lib = oracle.load()
     rng = np.random.default_rng(3)

@@ -32,18 +32,18 @@ __global__ void kBatchPrepare(const DJob *jobs, int numJobs) {
   }
 }
 
-template <int Kind, bool Shade>
+template <int Kind, bool Full>
 __device__ __forceinline__ void renderItem(const DJob &J, int x, int y) {
-  if (Kind == JOB_PATHTRACE) pathtracePixel<false, Shade>(J.S, J.C, J.R, J.F, x, y);
+  if (Kind == JOB_PATHTRACE) pathtracePixel<false, Full>(J.S, J.C, J.R, J.F, x, y);
   else if (Kind == JOB_RAYCAST_SURFACES) raycastPixel<false, true>(J.S, J.C, J.R, J.F, x, y, nullptr);
-  else if (Kind == JOB_RAYCAST_SHADED)
+  else if (Kind == JOB_RAYCAST_FULL)
     raycastPixel<false, true, true>(J.S, J.C, J.R, J.F, x, y, nullptr);
   else raycastPixel<false, false>(J.S, J.C, J.R, J.F, x, y, nullptr);
 }
 
 // Items are (job, tile) pairs; a tile is tileW x (32 / tileW) pixels. A warp
 // takes `fetch` consecutive items per atomic.
-template <int Kind, bool Shade = false>
+template <int Kind, bool Full = false>
 __device__ __forceinline__ void batchLoop(const DJob *jobs, const uint2 *items, unsigned numItems,
                                           unsigned *next, int tileW, int fetch, DJob *sJob) {
   const int lane = threadIdx.x & 31;
@@ -68,20 +68,20 @@ __device__ __forceinline__ void batchLoop(const DJob *jobs, const uint2 *items, 
       }
       const int tx = (int)it.y % sJob->tilesX, ty = (int)it.y / sJob->tilesX;
       const int x = tx * tileW + px, y = ty * tileH + py;
-      if (x < sJob->F.width && y < sJob->F.height) renderItem<Kind, Shade>(*sJob, x, y);
+      if (x < sJob->F.width && y < sJob->F.height) renderItem<Kind, Full>(*sJob, x, y);
     }
   }
 }
 
 // the register budgets of kPathtrace: 64 registers when worlds have volumes;
-// Shade: a job lights volume scatter events along the field gradient
-template <bool Volumes, bool Shade>
+// Full: a job uses gradient shading or point / spot lights
+template <bool Volumes, bool Full>
 __global__ void __launch_bounds__(128, Volumes ? VSR_MEGA_MIN_BLOCKS_VOLUMES : VSR_MEGA_MIN_BLOCKS)
     kBatchPathtrace(const DJob *jobs, const uint2 *items, unsigned numItems, unsigned *next,
                     int tileW, int fetch) {
   __shared__ __align__(16) DJob sJob[4];
-  batchLoop<JOB_PATHTRACE, Shade>(jobs, items, numItems, next, tileW, fetch,
-                                  &sJob[threadIdx.x >> 5]);
+  batchLoop<JOB_PATHTRACE, Full>(jobs, items, numItems, next, tileW, fetch,
+                                 &sJob[threadIdx.x >> 5]);
 }
 
 __global__ void __launch_bounds__(128)
@@ -100,13 +100,13 @@ __global__ void __launch_bounds__(128)
                                 &sJob[threadIdx.x >> 5]);
 }
 
-// raycast frames with gradient shading, any world
+// raycast frames with gradient shading or point / spot lights, any world
 __global__ void __launch_bounds__(128)
-    kBatchRaycastShaded(const DJob *jobs, const uint2 *items, unsigned numItems, unsigned *next,
-                        int tileW, int fetch) {
+    kBatchRaycastFull(const DJob *jobs, const uint2 *items, unsigned numItems, unsigned *next,
+                      int tileW, int fetch) {
   __shared__ __align__(16) DJob sJob[4];
-  batchLoop<JOB_RAYCAST_SHADED>(jobs, items, numItems, next, tileW, fetch,
-                                &sJob[threadIdx.x >> 5]);
+  batchLoop<JOB_RAYCAST_FULL>(jobs, items, numItems, next, tileW, fetch,
+                              &sJob[threadIdx.x >> 5]);
 }
 
 int smCount() {
@@ -141,15 +141,18 @@ cudaError_t launchBatch(const BatchLaunch &L, cudaStream_t stream) {
   if (e != cudaSuccess) return e;
   kBatchPrepare<<<smCount() * 4, 256, 0, stream>>>(L.jobs, L.numJobs);
   if ((e = cudaGetLastError()) != cudaSuccess) return e;
-  e = L.pathtraceVolumes == 2 ? launchPersistent(kBatchPathtrace<true, true>, L, JOB_PATHTRACE, stream)
-      : L.pathtraceVolumes    ? launchPersistent(kBatchPathtrace<true, false>, L, JOB_PATHTRACE, stream)
-                              : launchPersistent(kBatchPathtrace<false, false>, L, JOB_PATHTRACE, stream);
+  switch (L.pathtraceVariant) {
+    case 3: e = launchPersistent(kBatchPathtrace<true, true>, L, JOB_PATHTRACE, stream); break;
+    case 2: e = launchPersistent(kBatchPathtrace<false, true>, L, JOB_PATHTRACE, stream); break;
+    case 1: e = launchPersistent(kBatchPathtrace<true, false>, L, JOB_PATHTRACE, stream); break;
+    default: e = launchPersistent(kBatchPathtrace<false, false>, L, JOB_PATHTRACE, stream);
+  }
   if (e != cudaSuccess) return e;
   if ((e = launchPersistent(kBatchRaycastSurfaces, L, JOB_RAYCAST_SURFACES, stream)) != cudaSuccess)
     return e;
   if ((e = launchPersistent(kBatchRaycastVolume, L, JOB_RAYCAST_VOLUME, stream)) != cudaSuccess)
     return e;
-  return launchPersistent(kBatchRaycastShaded, L, JOB_RAYCAST_SHADED, stream);
+  return launchPersistent(kBatchRaycastFull, L, JOB_RAYCAST_FULL, stream);
 }
 
 }  // namespace vsr

@@ -9,8 +9,9 @@ namespace vsr {
 
 // Surfaces = false is the volume-only specialization (no traversal code,
 // fewer registers); the launcher picks it for worlds without surfaces.
-// Shade = true lights the volume samples along the field gradient.
-template <bool Count, bool Surfaces, bool Shade>
+// Full = true adds the optional features (gradient shading, point and spot
+// lights).
+template <bool Count, bool Surfaces, bool Full>
 __global__ void __launch_bounds__(VSR_RAYCAST_BLOCK_X * VSR_RAYCAST_BLOCK_Y, VSR_RAYCAST_MIN_BLOCKS)
     kRaycast(DScene S, DCamera C, DRenderer R, DFrame F, int stageTF) {
   extern __shared__ float4 sTF[];
@@ -23,22 +24,22 @@ __global__ void __launch_bounds__(VSR_RAYCAST_BLOCK_X * VSR_RAYCAST_BLOCK_Y, VSR
   const int x = blockIdx.x * blockDim.x + threadIdx.x;
   const int y = blockIdx.y * blockDim.y + threadIdx.y;
   if (x >= F.width || y >= F.height) return;
-  raycastPixel<Count, Surfaces, Shade>(S, C, R, F, x, y, stageTF ? sTF : nullptr);
+  raycastPixel<Count, Surfaces, Full>(S, C, R, F, x, y, stageTF ? sTF : nullptr);
 }
 
 // Two register budgets of the same body: worlds with volumes keep more path
 // state live during delta tracking and run faster with fewer resident
 // blocks and fewer spills (64 registers); surface-only worlds with more
-// blocks at 40 registers. Shade = true (worlds with volumes only) adds the
-// gradient shading of volume scatter events.
-template <bool Count, bool Volumes, bool Shade>
+// blocks at 40 registers. Full = true adds the optional features (gradient
+// shading of volume scatter events, point and spot lights).
+template <bool Count, bool Volumes, bool Full>
 __global__ void __launch_bounds__(16 * VSR_MEGA_BLOCK_Y,
                                  Volumes ? VSR_MEGA_MIN_BLOCKS_VOLUMES : VSR_MEGA_MIN_BLOCKS)
     kPathtrace(DScene S, DCamera C, DRenderer R, DFrame F) {
   const int x = blockIdx.x * blockDim.x + threadIdx.x;
   const int y = blockIdx.y * blockDim.y + threadIdx.y;
   if (x >= F.width || y >= F.height) return;
-  pathtracePixel<Count, Shade>(S, C, R, F, x, y);
+  pathtracePixel<Count, Full>(S, C, R, F, x, y);
 }
 
 static dim3 tileGrid(const DFrame &F, dim3 block) {
@@ -57,7 +58,7 @@ cudaError_t launchRaycast(const DScene &S, const DCamera &C, const DRenderer &R,
       cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     kernel<<<grid, block, smem, stream>>>(S, C, R, F, stage);
   };
-  if (R.gradientShading) {
+  if (R.gradientShading || S.positionalLights) {
     if (count) launch(kRaycast<true, true, true>);
     else launch(kRaycast<false, true, true>);
   } else if (S.hasSurfaces) {
@@ -77,15 +78,14 @@ cudaError_t launchPathtrace(const DScene &S, const DCamera &C, const DRenderer &
                             bool count, cudaStream_t stream) {
   dim3 block(16, VSR_MEGA_BLOCK_Y);
   const dim3 grid = tileGrid(F, block);
-  if (S.numVolumes > 0 && R.gradientShading) {
-    if (count) kPathtrace<true, true, true><<<grid, block, 0, stream>>>(S, C, R, F);
-    else kPathtrace<false, true, true><<<grid, block, 0, stream>>>(S, C, R, F);
-  } else if (S.numVolumes > 0) {
-    if (count) kPathtrace<true, true, false><<<grid, block, 0, stream>>>(S, C, R, F);
-    else kPathtrace<false, true, false><<<grid, block, 0, stream>>>(S, C, R, F);
+  const bool full = S.positionalLights || (S.numVolumes > 0 && R.gradientShading);
+  auto launch = [&](auto kernel) { kernel<<<grid, block, 0, stream>>>(S, C, R, F); };
+  if (S.numVolumes > 0) {
+    if (full) count ? launch(kPathtrace<true, true, true>) : launch(kPathtrace<false, true, true>);
+    else count ? launch(kPathtrace<true, true, false>) : launch(kPathtrace<false, true, false>);
   } else {
-    if (count) kPathtrace<true, false, false><<<grid, block, 0, stream>>>(S, C, R, F);
-    else kPathtrace<false, false, false><<<grid, block, 0, stream>>>(S, C, R, F);
+    if (full) count ? launch(kPathtrace<true, false, true>) : launch(kPathtrace<false, false, true>);
+    else count ? launch(kPathtrace<true, false, false>) : launch(kPathtrace<false, false, false>);
   }
   return cudaGetLastError();
 }

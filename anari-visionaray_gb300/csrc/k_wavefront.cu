@@ -340,7 +340,7 @@ __global__ void __launch_bounds__(256, VSR_WAVE_SHADE_MIN_BLOCKS) kWaveShade(
             if (S.numLights > 0) {
               int lightID = int(rnd() * S.numLights);
               if (lightID == S.numLights) lightID = 0;
-              ls = sampleLight(S.lights[lightID], rnd);
+              ls = sampleLight<true>(S.lights[lightID], hitPos, rnd);
             }
             lsDir = ls.dir;
             lsPdf = ls.pdf;

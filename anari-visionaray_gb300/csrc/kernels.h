@@ -50,7 +50,7 @@ enum JobKind {
   JOB_PATHTRACE = 0,
   JOB_RAYCAST_SURFACES = 1,
   JOB_RAYCAST_VOLUME = 2,
-  JOB_RAYCAST_SHADED = 3,  // raycast with gradient shading
+  JOB_RAYCAST_FULL = 3,  // raycast with gradient shading or point / spot lights
   kJobKinds = 4
 };
 struct DJob {
@@ -71,8 +71,8 @@ struct BatchLaunch {
   unsigned *counters;  // kJobKinds work counters
   int tileW;           // 1..32, a divisor of 32
   int fetch;           // items per atomic
-  int pathtraceVolumes;  // a path-traced job's world has volumes: the 64-register kernel;
-                         // 2: one of them also has gradient shading
+  int pathtraceVariant;  // bit 0: a path-traced job's world has volumes (the 64-register
+                         // kernel); bit 1: a job uses gradient shading or point / spot lights
 };
 cudaError_t launchBatch(const BatchLaunch &L, cudaStream_t stream);
 

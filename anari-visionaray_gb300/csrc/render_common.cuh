@@ -662,15 +662,43 @@ __device__ inline BSDFSample sampleMaterial(const DMaterial &m, float3 Ng, float
 }
 
 // ------------------------------------------------------------------ light
-// Directional light: scene/light/Directional.cpp:30-40 and sampleLight,
-// renderer/common.h:1432-1466 (dist2 = 1, pdf = 1, dist = FLT_MAX).
+// sampleLight, renderer/common.h:1432-1466, towards reference point P.
+// Directional (scene/light/Directional.cpp:30-40): dist2 = 1, pdf = 1,
+// dist = FLT_MAX; a positive angular diameter samples a uniform cone (two
+// draws). Point (scene/light/Point.cpp:28-37: constant attenuation 1) and
+// spot (DeviceCopyableObjects.h:2286-2321): direction P -> position, dist
+// its length, dist2 = dist^2, pdf 1, three draws for a random light normal
+// that delta lights do not use; the spot's intensity falls off with a
+// smoothstep between the outer and inner cone cosines.
 struct LightSample {
   float3 intensity, dir;
   float pdf, dist, dist2;
 };
 
-__device__ __forceinline__ LightSample sampleLight(const DLight &L, Rng &rnd) {
+// Positional = false compiles the directional light only (the kernels
+// that run near their register budget, for worlds without point or spot
+// lights).
+template <bool Positional>
+__device__ __forceinline__ LightSample sampleLight(const DLight &L, float3 P, Rng &rnd) {
   LightSample s;
+  if (Positional && L.type != LIGHT_DIRECTIONAL) {
+    s.intensity = ld3(L.intensity);
+    s.pdf = 1.f;
+    s.dir = ld3(L.pos) - P;
+    s.dist = length(s.dir);
+    s.dist2 = s.dist * s.dist;
+    (void)rnd(); (void)rnd(); (void)rnd();
+    if (L.type == LIGHT_SPOT) {
+      float spot = dot(normalize(ld3(L.dir)), normalize(-s.dir));
+      if (spot < L.cosOuter) {
+        s.intensity = f3(0.f);
+      } else if (!(spot > L.cosInner)) {
+        spot = (spot - L.cosOuter) / (L.cosInner - L.cosOuter);
+        s.intensity = s.intensity * (spot * spot * (3.f - 2.f * spot));
+      }
+    }
+    return s;
+  }
   float3 d = ld3(L.dir);
   if (L.cosHalfAngle < 1.f) {
     float u1 = rnd(), u2 = rnd();
@@ -710,10 +738,11 @@ __device__ __forceinline__ float3 fieldGradient(const DVolume &V, float3 P, floa
 // Gradient shading of one classified sample (rayMarchVolume<1>,
 // renderer/VolumeIntegration.h:420-460): a matte surface of the sample's
 // colour along the gradient, lit by every light, plus the ambient term.
-// Like the reference, the gradient is in voxel space and the light
-// directions in world space. viewDir need not be normalised. The raycast
-// renderer has no random stream (renderer/Raycast_impl.cpp:267): each light
-// is sampled with a zero-state generator, as for surfaces.
+// Like the reference, the gradient and P are in voxel space and the light
+// directions in world space (a point or spot light is sampled towards the
+// voxel-space P, VolumeIntegration.h:435). viewDir need not be normalised.
+// The raycast renderer has no random stream (renderer/Raycast_impl.cpp:267):
+// each light is sampled with a zero-state generator, as for surfaces.
 __device__ __forceinline__ float3 gradientShade(const DScene &S, const DRenderer &R,
                                                 const DVolume &V, float3 P, float3 delta,
                                                 float3 viewDir, float3 rgb, bool hw) {
@@ -724,7 +753,7 @@ __device__ __forceinline__ float3 gradientShade(const DScene &S, const DRenderer
     for (int li = 0; li < S.numLights; ++li) {
       Rng none;
       none.state = 0;
-      const LightSample ls = sampleLight(S.lights[li], none);
+      const LightSample ls = sampleLight<true>(S.lights[li], P, none);
       const float3 lightDir = normalize(ls.dir);
       const float3 lightIntensity = ls.intensity * safeRcp(ls.dist2);
       const float NdotL = fmaxf(0.f, dot(gn, lightDir));

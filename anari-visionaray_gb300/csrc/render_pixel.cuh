@@ -13,10 +13,10 @@ namespace vsr {
 
 // ------------------------------------------------------------------ raycast
 // renderSample, renderer/Raycast_impl.cpp:10-243 (default render mode).
-// Shade = true is the gradient-shading variant (the shading code, with its
-// six extra field samples per step, stays out of the plain kernels'
-// register allocation).
-template <bool Count, bool Surfaces, bool Shade>
+// Full = true is the variant with the optional features (gradient shading,
+// with its six extra field samples per step; point and spot lights), kept
+// out of the plain kernels' register allocation.
+template <bool Count, bool Surfaces, bool Full>
 __device__ void raycastSample(const DScene &S, const DRenderer &R, Ray ray, const float4 *sTF,
                               float4 &outColor, float &outDepth, float3 &outNg, float3 &outAlbedo,
                               uint32_t &err, unsigned long long *cnt) {
@@ -55,7 +55,7 @@ __device__ void raycastSample(const DScene &S, const DRenderer &R, Ray ray, cons
       for (int li = 0; li < S.numLights; ++li) {
         Rng dummy;
         dummy.state = 0;
-        LightSample ls = sampleLight(S.lights[li], dummy);
+        LightSample ls = sampleLight<Full>(S.lights[li], hitPos, dummy);
         const float3 lightDir = normalize(ls.dir);
         const float3 li3 = ls.intensity * safeRcp(ls.dist2);
         const float NdotL = fmaxf(0.f, dot(sn, lightDir));
@@ -149,7 +149,7 @@ __device__ void raycastSample(const DScene &S, const DRenderer &R, Ray ray, cons
           const float stepTr = hw ? __powf(1.f - s.w, expo) : powf(1.f - s.w, expo);
           const float w = transmittance * (1.f - stepTr);
           float3 rgb = f3(s.x, s.y, s.z);
-          if (Shade && R.gradientShading)
+          if (Full && R.gradientShading)
             rgb = gradientShade(S, R, V, o + d * tk[k], Sv * V.cellSize, -d, rgb, hw);
           color += w * rgb;
           alpha += w;
@@ -172,7 +172,7 @@ __device__ void raycastSample(const DScene &S, const DRenderer &R, Ray ray, cons
 // One pixel of the raycast renderer: pixelSamples camera rays through the
 // pixel centre, averaged (renderer/Raycast_impl.cpp:282-322). sTF is the
 // first volume's TF staged in shared memory, or null.
-template <bool Count, bool Surfaces, bool Shade = false>
+template <bool Count, bool Surfaces, bool Full = false>
 __device__ __forceinline__ void raycastPixel(const DScene &S, const DCamera &C, const DRenderer &R,
                                              const DFrame &F, int x, int y, const float4 *sTF) {
   uint32_t err = 0;
@@ -189,7 +189,7 @@ __device__ __forceinline__ void raycastPixel(const DScene &S, const DCamera &C, 
     float4 c;
     float dd;
     float3 nn, aa;
-    raycastSample<Count, Surfaces, Shade>(S, R, ray, sTF, c, dd, nn, aa, err, cnt);
+    raycastSample<Count, Surfaces, Full>(S, R, ray, sTF, c, dd, nn, aa, err, cnt);
     acc.x += c.x; acc.y += c.y; acc.z += c.z; acc.w += c.w;
     if (s == 0) { c0 = c; d0 = dd; n0 = nn; a0 = aa; }
   }
@@ -270,9 +270,9 @@ __device__ __forceinline__ void intersectAll(const DScene &S, const Ray &ray, bo
 
 // Per-pixel body of VisionarayRendererPathtrace::renderFrame
 // (renderer/Pathtrace_impl.cpp:498-640) with shade() (:93-487) inlined.
-// Shade = true is the variant with gradient shading of volume hits (kept out
-// of the plain kernels' register allocation).
-template <bool Count, bool Shade>
+// Full = true is the variant with gradient shading of volume hits and point
+// and spot lights (kept out of the plain kernels' register allocation).
+template <bool Count, bool Full>
 __device__ __forceinline__ void pathtracePixel(const DScene &S, const DCamera &C,
                                                const DRenderer &R, const DFrame &F, int x, int y) {
   uint32_t err = 0;
@@ -343,7 +343,7 @@ __device__ __forceinline__ void pathtracePixel(const DScene &S, const DCamera &C
               hitPos = ray.o + hr.volT * ray.d;
               eps = epsilonFrom(hitPos, ray.d, hr.volT);
               gn = f3(0.f);
-              if (Shade && R.gradientShading) {
+              if (Full && R.gradientShading) {
                 // the field gradient at the instance-local hit position in
                 // voxel space (renderer/Pathtrace_impl.cpp:204-212)
                 const DVolume &V = S.volumes[hr.volIdx];
@@ -387,13 +387,13 @@ __device__ __forceinline__ void pathtracePixel(const DScene &S, const DCamera &C
             if (S.numLights > 0) {
               int lightID = int(rnd() * S.numLights);
               if (lightID == S.numLights) lightID = 0;
-              ls = sampleLight(S.lights[lightID], rnd);
+              ls = sampleLight<Full>(S.lights[lightID], hitPos, rnd);
             }
             const float3 lightDir = normalize(ls.dir);
             const float3 lightIntensity = ls.intensity * safeRcp(ls.dist2);
             const float NdotL = fmaxf(0.f, dot(sn, lightDir));
             if (hr.volumeHit) {
-              if (Shade && R.gradientShading && length(gn) > 1e-10f)  // matte along the gradient
+              if (Full && R.gradientShading && length(gn) > 1e-10f)  // matte along the gradient
                 shadedColor = hr.volAlbedo * kInvPi * lightIntensity * NdotL * safeRcp(ls.pdf) *
                               float(S.numLights);
               else

@@ -21,6 +21,7 @@
 #include <atomic>
 #include <chrono>
 #include <cmath>
+#include <limits>
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
@@ -502,24 +503,53 @@ struct Material : Object {
   }
 };
 
-// directional light, scene/light/Directional.cpp:17-40 and Light.cpp:27-28
+// Lights: Light.cpp:27-35 (color, visible) and the subtypes'
+// commitParameters: directional (Directional.cpp:17-28), point (Point.cpp:
+// 18-24), spot (Spot.cpp:19-47; the cone cosines are taken of the angles as
+// given).
 struct Light : Object {
-  float direction[3] = {0, 0, -1}, color[3] = {1, 1, 1};
-  float irradiance = 1.f, angularDiameter = 0.f;
+  int type = LIGHT_DIRECTIONAL;
+  float direction[3] = {0, 0, -1}, color[3] = {1, 1, 1}, position[3] = {0, 0, 0};
+  float irradiance = 1.f, angularDiameter = 0.f, intensity = 1.f;
+  float cosOuter = -1.f, cosInner = -1.f;
   int visible = 1;
   using Object::Object;
   void commit() override {
-    direction[0] = 0; direction[1] = 0; direction[2] = -1;
-    getv("direction", VSR_FLOAT32_VEC3, direction);
-    float l = std::sqrt(direction[0] * direction[0] + direction[1] * direction[1] + direction[2] * direction[2]);
-    for (float &d : direction) d /= l;
+    type = subtype == "point" ? LIGHT_POINT : subtype == "spot" ? LIGHT_SPOT : LIGHT_DIRECTIONAL;
     color[0] = color[1] = color[2] = 1.f;
     getv("color", VSR_FLOAT32_VEC3, color);
-    irradiance = 1.f; getf("irradiance", irradiance);
-    irradiance = std::max(irradiance, 0.f);
-    angularDiameter = 0.f; getf("angularDiameter", angularDiameter);
-    angularDiameter = std::max(angularDiameter, 0.f);
     visible = 1; geti("visible", visible);
+    const float maxF = std::numeric_limits<float>::max();
+    if (type == LIGHT_DIRECTIONAL) {
+      direction[0] = 0; direction[1] = 0; direction[2] = -1;
+      getv("direction", VSR_FLOAT32_VEC3, direction);
+      float l = std::sqrt(direction[0] * direction[0] + direction[1] * direction[1] +
+                          direction[2] * direction[2]);
+      for (float &d : direction) d /= l;
+      irradiance = 1.f; getf("irradiance", irradiance);
+      irradiance = std::max(irradiance, 0.f);
+      angularDiameter = 0.f; getf("angularDiameter", angularDiameter);
+      angularDiameter = std::max(angularDiameter, 0.f);
+    } else if (type == LIGHT_POINT) {
+      position[0] = 0; position[1] = 0; position[2] = -1;
+      getv("position", VSR_FLOAT32_VEC3, position);
+      intensity = 1.f; getf("intensity", intensity);
+      intensity = std::min(std::max(intensity, 0.f), maxF);
+    } else {
+      position[0] = position[1] = position[2] = 0.f;
+      getv("position", VSR_FLOAT32_VEC3, position);
+      direction[0] = 0; direction[1] = 0; direction[2] = -1;
+      getv("direction", VSR_FLOAT32_VEC3, direction);
+      float opening = (float)M_PI, falloff = 0.1f;
+      getf("openingAngle", opening);
+      getf("falloffAngle", falloff);
+      intensity = 1.f; getf("intensity", intensity);
+      intensity = std::min(std::max(intensity, 0.f), maxF);
+      const float inner = opening - 2.f * falloff;
+      if (inner < 0.f) warn("falloffAngle should be smaller than half of openingAngle");
+      cosOuter = std::cos(opening);
+      cosInner = std::cos(inner);
+    }
     valid = true;
   }
 };
@@ -987,19 +1017,34 @@ struct World : Object {
       dinst.push_back(di);
       for (Light *L : r.g->lights) {
         if (!L->valid) continue;
+        // xfmLight (DeviceCopyableObjects.h:2398-2430): positions by the
+        // instance's affine transform, directions by its linear part
+        auto linear = [&](const float *v, float *o) {
+          for (int k = 0; k < 3; ++k) o[k] = m[k] * v[0] + m[3 + k] * v[1] + m[6 + k] * v[2];
+        };
         DLight dl{};
-        // direction transformed by the instance's linear part
-        float d[3];
-        for (int k = 0; k < 3; ++k)
-          d[k] = m[k] * L->direction[0] + m[3 + k] * L->direction[1] + m[6 + k] * L->direction[2];
-        float l = std::sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
-        for (int k = 0; k < 3; ++k) {
-          dl.dir[k] = -d[k] / l;
-          dl.intensity[k] = L->color[k] * L->irradiance;
-        }
-        dl.cosHalfAngle = L->angularDiameter > 0.f ? std::cos(0.5f * L->angularDiameter) : 1.f;
-        dl.type = 0;
+        dl.type = L->type;
         dl.visible = L->visible;
+        if (L->type == LIGHT_DIRECTIONAL) {
+          float d[3];
+          linear(L->direction, d);
+          float l = std::sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
+          for (int k = 0; k < 3; ++k) {
+            dl.dir[k] = -d[k] / l;
+            dl.intensity[k] = L->color[k] * L->irradiance;
+          }
+          dl.cosHalfAngle = L->angularDiameter > 0.f ? std::cos(0.5f * L->angularDiameter) : 1.f;
+        } else {
+          linear(L->position, dl.pos);
+          for (int k = 0; k < 3; ++k) {
+            dl.pos[k] += m[9 + k];
+            dl.intensity[k] = L->color[k] * L->intensity;
+          }
+          if (L->type == LIGHT_SPOT) linear(L->direction, dl.dir);
+          dl.cosHalfAngle = 1.f;
+          dl.cosOuter = L->cosOuter;
+          dl.cosInner = L->cosInner;
+        }
         lights.push_back(dl);
       }
     }
@@ -1024,6 +1069,8 @@ struct World : Object {
     scene.numInstances = (int)dinst.size();
     scene.numGroups = (int)dgroups.size();
     scene.numLights = (int)lights.size();
+    scene.positionalLights = 0;
+    for (const DLight &l : lights) scene.positionalLights += l.type != LIGHT_DIRECTIONAL;
     scene.numVolumes = (int)vols.size();
     scene.allOpaque = allOpaque ? 1 : 0;
     scene.hasSurfaces = anySurf ? 1 : 0;
@@ -1445,7 +1492,7 @@ VSRStatus renderFrames(Device *dev, FrameObj *const *frames, uint32_t count) {
     }
     j.F = F->record();
     j.kind = j.R.type != REND_RAYCAST ? JOB_PATHTRACE
-             : j.R.gradientShading    ? JOB_RAYCAST_SHADED
+             : (j.R.gradientShading || j.S.positionalLights) ? JOB_RAYCAST_FULL
              : j.S.hasSurfaces        ? JOB_RAYCAST_SURFACES
                                       : JOB_RAYCAST_VOLUME;
     // a frame past its sample limit only clears its error flags
@@ -1454,7 +1501,8 @@ VSRStatus renderFrames(Device *dev, FrameObj *const *frames, uint32_t count) {
     batched.push_back(F);
     key.insert(key.end(), {(uint64_t)(uintptr_t)F, (uint64_t)j.F.width, (uint64_t)j.F.height,
                            (uint64_t)j.kind, (uint64_t)j.R.pixelSamples, (uint64_t)j.R.maxBounce,
-                           (uint64_t)j.S.numVolumes, (uint64_t)j.R.gradientShading});
+                           (uint64_t)j.S.numVolumes, (uint64_t)j.R.gradientShading,
+                           (uint64_t)j.S.positionalLights});
   }
   if (!batched.empty()) {
     BatchTuner &tuner = B.tuners[key];
@@ -1514,8 +1562,11 @@ VSRStatus renderFrames(Device *dev, FrameObj *const *frames, uint32_t count) {
     L.tileW = C.tileW;
     L.fetch = C.fetch;
     for (const DJob &j : jobs)
-      if (j.kind == JOB_PATHTRACE && j.S.numVolumes > 0)
-        L.pathtraceVolumes = std::max(L.pathtraceVolumes, j.R.gradientShading ? 2 : 1);
+      if (j.kind == JOB_PATHTRACE) {
+        if (j.S.numVolumes > 0) L.pathtraceVariant |= 1;
+        if (j.S.positionalLights || (j.S.numVolumes > 0 && j.R.gradientShading))
+          L.pathtraceVariant |= 2;
+      }
     // one CUDA graph per frame set and configuration: the job records are
     // copied from the pinned staging buffer when the graph runs
     if (!B.graph) {
@@ -1733,7 +1784,7 @@ VSRObject vsrNewMaterial(VSRDevice d, const char *s) {
   return newObj<Material>(d, VSR_MATERIAL, s, {"matte", "physicallyBased"});
 }
 VSRObject vsrNewLight(VSRDevice d, const char *s) {
-  return newObj<Light>(d, VSR_LIGHT, s, {"directional"});
+  return newObj<Light>(d, VSR_LIGHT, s, {"directional", "point", "spot"});
 }
 VSRObject vsrNewSurface(VSRDevice d) { return newObj<Surface>(d, VSR_SURFACE, "", {}); }
 VSRObject vsrNewGroup(VSRDevice d) { return newObj<Group>(d, VSR_GROUP, "", {}); }

@@ -98,13 +98,20 @@ struct DMaterial {
   float pad[3];
 };
 
+enum LightType { LIGHT_DIRECTIONAL = 0, LIGHT_POINT = 1, LIGHT_SPOT = 2 };
+
+// One light in world space (instance transforms applied on the host).
 struct DLight {
-  float dir[3];        // unit vector towards the light (-direction)
-  float intensity[3];  // color * irradiance
-  float cosHalfAngle;  // cos(angularDiameter/2); 1 = delta light
-  int type;
+  float dir[3];        // directional: unit vector towards the light (-direction);
+                       // spot: the cone axis (instance-transformed, normalised at use)
+  float intensity[3];  // color * irradiance (directional) or color * intensity
+  float cosHalfAngle;  // directional: cos(angularDiameter/2); 1 = delta light
+  int type;            // LightType
   int visible;
-  int pad;
+  float pos[3];        // point / spot position
+  float cosOuter;      // spot: cos(openingAngle)
+  float cosInner;      // spot: cos(openingAngle - 2 falloffAngle)
+  float pad[2];
 };
 
 struct DVolume {
@@ -160,6 +167,7 @@ struct DScene {
   int numInstances;
   int numGroups;
   int numLights;
+  int positionalLights;  // point and spot lights among them: the kernels' full variants
   int numVolumes;
   int allOpaque;
   int hasSurfaces;

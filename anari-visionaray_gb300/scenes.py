@@ -8,7 +8,10 @@ is fixed in each generator. A scene is a plain dict:
   surfaces : [{"vertices": (V,3) f32, "indices": (T,3) u32, "material": {...}}]
   volumes  : [{"data": (nz,ny,nx) f32, "origin", "spacing", "color": (N,3),
                "opacity": (N,), "valueRange", "unitDistance"}]
-  lights   : [{"direction", "color", "irradiance"}]
+  lights   : [{"type": "directional" (default), "direction", "color", "irradiance",
+                "angularDiameter"} | {"type": "point", "position", "color", "intensity"} |
+              {"type": "spot", "position", "direction", "openingAngle", "falloffAngle",
+               "color", "intensity"}]
   instances: [{"transform": 12 floats (column-major 3x4), "surfaces": [...],
                "volumes": [...], "lights": [...]}]   (optional)
   camera   : {"type": "perspective", "position", "direction", "up", "fovy", "aspect"}
@@ -347,10 +350,21 @@ def _volumes(dev, vols, keep):
 def _lights(dev, lights, keep):
     out = []
     for L in lights:
-        lt = dev.light("directional")
-        dev.set(lt, "direction", L["direction"], vsr.FLOAT32_VEC3)
+        kind = L.get("type", "directional")
+        lt = dev.light(kind)
         dev.set(lt, "color", L.get("color", [1, 1, 1]), vsr.FLOAT32_VEC3)
-        dev.set(lt, "irradiance", float(L.get("irradiance", 1.0)))
+        if kind == "directional":
+            dev.set(lt, "direction", L["direction"], vsr.FLOAT32_VEC3)
+            dev.set(lt, "irradiance", float(L.get("irradiance", 1.0)))
+            if "angularDiameter" in L:
+                dev.set(lt, "angularDiameter", float(L["angularDiameter"]))
+        else:
+            for k in ("position", "direction"):
+                if k in L:
+                    dev.set(lt, k, L[k], vsr.FLOAT32_VEC3)
+            for k in ("intensity", "openingAngle", "falloffAngle"):
+                if k in L:
+                    dev.set(lt, k, float(L[k]))
         dev.commit(lt)
         out.append(lt)
     return out

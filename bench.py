@@ -200,12 +200,21 @@ def cpu_baseline(scene, rows, threads=0):
     return px * spp / dt / MPX, dt, px, cores
 
 
-def measure_raycast_config0(pkg, dev, flush, steps=20):
+def measure_raycast_config0(pkg, dev, flush, steps=20, gradient=False):
     """Config 0 (raycast, 128^3 blob volume, 512x512, 1 spp): Mpx/s and the
-    marcher's roofline (32 B per trilinear sample + 20 B per pixel written)."""
+    marcher's roofline (32 B per trilinear sample + 20 B per pixel written).
+    gradient: the same volume lit by a directional light with gradient
+    shading (6 more trilinear samples per step for the central differences:
+    7 x 32 B per step)."""
     import torch
 
     scene = pkg.scenes.config0()
+    fetches = 1
+    if gradient:
+        scene["lights"] = [{"direction": [-0.3, -0.87, -0.39], "color": [1.0, 1.0, 1.0],
+                            "irradiance": 2.5}]
+        scene["renderer"]["gradientShading"] = True
+        fetches = 7
     h = pkg.scenes.build(dev, scene, channels=("color", "depth"))
     frame = h["frame"]
     dev.set(frame, "collectStatistics", True)
@@ -227,10 +236,19 @@ def measure_raycast_config0(pkg, dev, flush, steps=20):
         ds.append(dev.get_float(frame, "duration.render"))
     t = statistics.mean(ds)
     W, H = scene["frame"]["size"]
-    alg = samples * 32 + W * H * 20
+    alg = samples * 32 * fetches + W * H * 20
     peak, kind = measured_peaks()
     for o in (frame, h["renderer"], h["camera"], h["world"], *h["keep"]):
         dev.release(o)
+    if gradient:
+        return {"value": W * H / t / MPX, "unit": "Mpx*spp/s", "ms_per_frame": 1e3 * t,
+                "workload": "config0 volume with a directional light and gradient shading, "
+                            "512x512 1spp, per-pixel raycast kernel",
+                "march_samples": samples,
+                "roofline": {"bound": "hbm", "achieved": alg / t / 1e9, "peak": peak,
+                             "unit": "GB/s", "frac": alg / t / 1e9 / peak, "traffic": None,
+                             "note": f"7 x 32 B per step (the sample and its 6 central "
+                                     f"differences) + 20 B per pixel; peak {kind}"}}
     return {"value": W * H / t / MPX, "unit": "Mpx*spp/s", "ms_per_frame": 1e3 * t,
             "workload": "config0 raycast 512x512 1spp, 128^3 float32 blobs, dt 0.5 voxel",
             "march_samples": samples,
@@ -595,6 +613,7 @@ def run_ours(args):
         dev.commit(h["renderer"])
 
     raycast = measure_raycast_config0(pkg, dev, flush) if args.raycast else None
+    shaded = measure_raycast_config0(pkg, dev, flush, gradient=True) if args.raycast else None
     batch = measure_batch_config3(pkg, dev) if args.batch else None
     if not args.denoise:
         denoiser = None
@@ -651,6 +670,7 @@ def run_ours(args):
                       "grays_per_s": rays / kernel_s / 1e9},
         "config1_accumulated_1spp": accum,
         "commit_s": commit_s, "bvh_build_s": bvh_s, "raycast_config0": raycast,
+        "raycast_config0_gradient_shading": shaded,
         "volume_pathtracer_config2": volume, "batch_config3": batch,
         "denoiser_config4": denoiser,
         "wall_s_timed": wall, "clocks": clk, "error_flags": err,

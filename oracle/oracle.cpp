@@ -947,31 +947,58 @@ BSDFSample sampleMaterial(const OrMaterial &m, f3 Ng, f3 Ns, f3 viewDir, LCG &rn
 }
 
 // ---------------------------------------------------------------------------
-// Lights: directional (scene/light/Directional.cpp:30-40; sampleLight,
-// renderer/common.h:1432-1466). The stored direction is -direction; with
-// angularDiameter == 0 no random number is drawn, dist = FLT_MAX, pdf = 1,
-// dist2 = 1. A positive angular diameter samples a uniform cone (2 draws).
+// Lights: sampleLight (renderer/common.h:1432-1466) towards reference point
+// P. Directional (scene/light/Directional.cpp:30-40): the stored direction
+// is -direction; with angularDiameter == 0 no random number is drawn,
+// dist = FLT_MAX, pdf = 1, dist2 = 1; a positive angular diameter samples a
+// uniform cone (2 draws). Point (scene/light/Point.cpp:28-37, Visionaray's
+// point_light with constant attenuation 1) and spot
+// (DeviceCopyableObjects.h:2286-2321): dir = position - P, dist = |dir|,
+// dist2 = dist^2, pdf = 1, three draws for a light normal that delta lights
+// do not use; intensity = color * intensity, for the spot times a
+// smoothstep between cos(openingAngle) and cos(openingAngle - 2 falloff)
+// (Spot.cpp:34-45).
 // ---------------------------------------------------------------------------
 struct LightSample { f3 intensity, dir; float pdf = 0.f, dist = 0.f, dist2 = 0.f; };
 
-LightSample sampleLight(const OrLight &L, LCG &rnd) {
+LightSample sampleLight(const OrLight &L, f3 P, LCG &rnd) {
   LightSample s;
-  f3 d = -normalize(f3(L.direction[0], L.direction[1], L.direction[2]));
-  if (L.angularDiameter > 0.f) {
-    float cosMax = std::cos(0.5f * L.angularDiameter);
-    float u1 = rnd(), u2 = rnd();
-    float cz = 1.f - u1 * (1.f - cosMax);
-    float sz = std::sqrt(std::fmax(0.f, 1.f - cz * cz));
-    float phi = kTwoPi * u2;
-    f3 a, b;
-    make_orthonormal_basis(a, b, d);
-    d = normalize(a * (sz * std::cos(phi)) + b * (sz * std::sin(phi)) + d * cz);
-  }
-  s.dir = d;
-  s.dist = FLT_MAX;
   s.pdf = 1.f;
-  s.dist2 = 1.f;
-  s.intensity = f3(L.color[0], L.color[1], L.color[2]) * L.irradiance;
+  if (L.type == 0) {
+    f3 d = -normalize(f3(L.direction[0], L.direction[1], L.direction[2]));
+    if (L.angularDiameter > 0.f) {
+      float cosMax = std::cos(0.5f * L.angularDiameter);
+      float u1 = rnd(), u2 = rnd();
+      float cz = 1.f - u1 * (1.f - cosMax);
+      float sz = std::sqrt(std::fmax(0.f, 1.f - cz * cz));
+      float phi = kTwoPi * u2;
+      f3 a, b;
+      make_orthonormal_basis(a, b, d);
+      d = normalize(a * (sz * std::cos(phi)) + b * (sz * std::sin(phi)) + d * cz);
+    }
+    s.dir = d;
+    s.dist = FLT_MAX;
+    s.dist2 = 1.f;
+    s.intensity = f3(L.color[0], L.color[1], L.color[2]) * L.irradiance;
+    return s;
+  }
+  s.dir = f3(L.position[0], L.position[1], L.position[2]) - P;
+  s.dist = length(s.dir);
+  s.dist2 = s.dist * s.dist;
+  for (int k = 0; k < 3; ++k) (void)rnd();
+  s.intensity = f3(L.color[0], L.color[1], L.color[2]) * L.intensity;
+  if (L.type == 2) {
+    const float cosOuter = std::cos(L.openingAngle);
+    const float cosInner = std::cos(L.openingAngle - 2.f * L.falloffAngle);
+    float spot = dot(normalize(f3(L.direction[0], L.direction[1], L.direction[2])),
+                     normalize(-s.dir));
+    if (spot < cosOuter) {
+      s.intensity = f3(0.f);
+    } else if (!(spot > cosInner)) {
+      spot = (spot - cosOuter) / (cosInner - cosOuter);
+      s.intensity = s.intensity * (spot * spot * (3.f - 2.f * spot));
+    }
+  }
   return s;
 }
 
@@ -1010,7 +1037,7 @@ f3 gradientShade(const OrScene &S, const OrRenderer &R, const Vol &vol, f3 P, f3
   if (length(gn) > 1e-10f) {
     for (int li = 0; li < S.numLights; ++li) {
       LCG dummy(0, 0);
-      LightSample ls = sampleLight(S.lights[li], dummy);
+      LightSample ls = sampleLight(S.lights[li], P, dummy);
       f3 lightDir = normalize(ls.dir);
       f3 lightIntensity = ls.intensity * safe_rcp(ls.dist2);
       const float NdotL = std::fmax(0.f, dot(gn, lightDir));
@@ -1050,7 +1077,7 @@ PixelSample raycastSample(const Scene &sc, const OrRenderer &R, Ray ray, Counter
     f3 viewDir = -ray.dir;
     for (int li = 0; li < S.numLights; ++li) {
       LCG dummy(0, 0);
-      LightSample ls = sampleLight(S.lights[li], dummy);
+      LightSample ls = sampleLight(S.lights[li], hitPos, dummy);
       f3 lightDir = normalize(ls.dir);
       f3 lightIntensity = ls.intensity * safe_rcp(ls.dist2);
       const float NdotL = std::fmax(0.f, dot(sn, lightDir));
@@ -1250,7 +1277,7 @@ void shade(const Scene &sc, const OrRenderer &R, LCG &rnd, const Ray &ray, RayTy
       float r = rnd();
       lightID = int(r * S.numLights);
       if (lightID == S.numLights) lightID = 0;
-      ss.light = sampleLight(S.lights[lightID], rnd);
+      ss.light = sampleLight(S.lights[lightID], hitPos, rnd);
     }
     f3 lightDir = normalize(ss.light.dir);
     f3 lightIntensity = ss.light.intensity * safe_rcp(ss.light.dist2);

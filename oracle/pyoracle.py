@@ -53,7 +53,9 @@ class OrInstance(ctypes.Structure):
 
 class OrLight(ctypes.Structure):
     _fields_ = [("type", c_int32), ("direction", c_float * 3), ("color", c_float * 3),
-                ("irradiance", c_float), ("angularDiameter", c_float), ("visible", c_int32)]
+                ("irradiance", c_float), ("angularDiameter", c_float), ("visible", c_int32),
+                ("position", c_float * 3), ("intensity", c_float), ("openingAngle", c_float),
+                ("falloffAngle", c_float)]
 
 
 class OrScene(ctypes.Structure):
@@ -247,14 +249,31 @@ class Scene:
             oi.userID = 0xffffffff
             oinsts.append(oi)
             lin = np.asarray(xfm, np.float64)[:9].reshape(3, 3).T  # column-major -> matrix
+            tr = np.asarray(xfm, np.float32)[9:12]
             for L in lts:
                 ol = OrLight()
-                d = lin @ np.asarray(L["direction"], np.float64)
-                ol.direction = farr(3, d / np.linalg.norm(d))
+                kind = L.get("type", "directional")
+                ol.type = {"directional": 0, "point": 1, "spot": 2}[kind]
                 ol.color = farr(3, L.get("color", [1, 1, 1]))
-                ol.irradiance = float(L.get("irradiance", 1.0))
-                ol.angularDiameter = float(L.get("angularDiameter", 0.0))
                 ol.visible = 1
+                if kind == "directional":
+                    d = lin @ np.asarray(L["direction"], np.float64)
+                    ol.direction = farr(3, d / np.linalg.norm(d))
+                    ol.irradiance = float(L.get("irradiance", 1.0))
+                    ol.angularDiameter = float(L.get("angularDiameter", 0.0))
+                else:
+                    # positions by the instance's affine transform, the spot
+                    # axis by its linear part, in float32 as the device does
+                    lin32 = lin.astype(np.float32)
+                    p0 = np.asarray(L.get("position", [0, 0, -1] if kind == "point" else [0, 0, 0]),
+                                    np.float32)
+                    ol.position = farr(3, lin32 @ p0 + tr)
+                    ol.intensity = float(min(max(L.get("intensity", 1.0), 0.0), 3.4e38))
+                    if kind == "spot":
+                        ol.direction = farr(3, lin32 @ np.asarray(L.get("direction", [0, 0, -1]),
+                                                                  np.float32))
+                        ol.openingAngle = float(L.get("openingAngle", math.pi))
+                        ol.falloffAngle = float(L.get("falloffAngle", 0.1))
                 lights.append(ol)
         tri = np.ascontiguousarray(np.concatenate(verts) if verts else np.zeros((0, 9), np.float32))
         ts = np.ascontiguousarray(np.concatenate(tsurf) if tsurf else np.zeros(0, np.uint32))

@@ -65,12 +65,17 @@ typedef struct OrInstance {
 } OrInstance;
 
 typedef struct OrLight {
-  int32_t type;             /* 0 = directional */
-  float direction[3];       /* direction the light travels (ANARI "direction") */
+  int32_t type;             /* 0 = directional, 1 = point, 2 = spot */
+  float direction[3];       /* directional: direction the light travels (ANARI
+                               "direction"); spot: cone axis, world space */
   float color[3];
   float irradiance;
   float angularDiameter;
   int32_t visible;
+  float position[3];        /* point / spot, world space */
+  float intensity;          /* point / spot */
+  float openingAngle;       /* spot */
+  float falloffAngle;       /* spot */
 } OrLight;
 
 typedef struct OrScene {

@@ -384,6 +384,80 @@ def test_volume_pathtrace_gradient_shading_same_stream(pkg, device, oracle, wave
     assert float((d <= 1e-3).mean()) >= 0.95, float((d <= 1e-3).mean())
 
 
+def point_and_spot_lights():
+    """A point light above the sphere set and a spot aimed at its centre."""
+    spot_pos = np.array([4.0, 14.0, 10.0])
+    axis = np.array([0.0, -1.0, 0.0]) - spot_pos
+    axis /= np.linalg.norm(axis)
+    return [{"type": "point", "position": [0.0, 12.0, 5.0], "intensity": 300.0,
+             "color": [1.0, 0.9, 0.8]},
+            {"type": "spot", "position": spot_pos.tolist(), "direction": axis.tolist(),
+             "openingAngle": 0.6, "falloffAngle": 0.15, "intensity": 400.0,
+             "color": [0.7, 0.8, 1.0]}]
+
+
+def test_raycast_point_and_spot_lights(pkg, device, oracle):
+    """Point and spot lights (sampleLight towards the hit point, inverse-square
+    falloff, the spot's smoothstep cone) in the raycast renderer."""
+    sc = small_spheres(pkg, res=128, renderer="raycast")
+    sc["lights"] = point_and_spot_lights()
+    gpu = render_gpu(pkg, device, sc)
+    _, F = render_oracle(oracle, sc)
+    _, P = render_oracle(oracle, dict(sc, lights=sc["lights"][:1]))
+    assert gpu["errorFlags"] == 0
+    assert float(np.abs(F.color - P.color).max()) > 0.05  # the spot lights part of the view
+    good, frac = raycast_ok(gpu, F)
+    assert good, frac
+
+
+@pytest.mark.parametrize("wavefront", [True, False])
+def test_pathtrace_point_and_spot_same_stream(pkg, device, oracle, wavefront):
+    """Next-event estimation towards point and spot lights (three draws per
+    light sample, shadow rays ending at the light), same stream as the
+    oracle, in both execution modes."""
+    sc = small_spheres(pkg, res=96, spp=8)
+    sc["lights"] = point_and_spot_lights()
+    sc["renderer"]["wavefront"] = wavefront
+    gpu = render_gpu(pkg, device, sc)
+    _, F = render_oracle(oracle, sc)
+    assert gpu["errorFlags"] == 0
+    assert not np.isnan(gpu["color"]).any()
+    d = np.abs(gpu["color"][..., :3] - F.color[..., :3]).max(axis=-1)
+    assert float((d <= 1e-3).mean()) >= 0.97, float((d <= 1e-3).mean())
+
+
+def test_instanced_lights(pkg, device, oracle):
+    """Lights inside an instanced group: positions by the instance's affine
+    transform, directions by its linear part (xfmLight)."""
+    base = small_spheres(pkg, res=96, renderer="raycast", n=10)
+    c, s = np.cos(0.4), np.sin(0.4)
+    xfm = [c * 1.2, 0.0, -s * 1.2, 0.0, 1.2, 0.0, s * 1.2, 0.0, c * 1.2, 1.0, -0.5, 2.0]
+    sc = dict(base)
+    sc["lights"] = []
+    sc["instances"] = [{"transform": xfm, "surfaces": base["surfaces"][:5],
+                        "lights": point_and_spot_lights() + base["lights"]}]
+    sc["surfaces"] = base["surfaces"][5:]
+    gpu = render_gpu(pkg, device, sc)
+    _, F = render_oracle(oracle, sc)
+    assert gpu["errorFlags"] == 0
+    good, frac = raycast_ok(gpu, F)
+    assert good, frac
+
+
+def test_volume_pathtrace_point_light_gradient_shading(pkg, device, oracle):
+    """A point light inside the config-2 style volume with gradient shading:
+    scatter events lit towards the light, same stream as the oracle."""
+    sc = small_volume_scene(pkg)
+    sc["lights"] = [{"type": "point", "position": [2.0, 6.0, 4.0], "intensity": 200.0}]
+    sc["renderer"].update(gradientShading=True, volumeFilter="exact")
+    gpu = render_gpu(pkg, device, sc)
+    _, F = render_oracle(oracle, sc, grid=oracle.GRID_BRICK)
+    assert gpu["errorFlags"] == 0
+    assert not np.isnan(gpu["color"]).any()
+    d = np.abs(gpu["color"][..., :3] - F.color[..., :3]).max(axis=-1)
+    assert float((d <= 1e-3).mean()) >= 0.95, float((d <= 1e-3).mean())
+
+
 def test_wavefront_equals_megakernel(pkg, device):
     """The two execution modes produce the same frame (same stream, same math)."""
     sc = small_spheres(pkg, res=96, spp=4, n=16)

@@ -121,6 +121,43 @@ def test_lambertian_plane_closed_form(oracle):
     assert np.allclose(F.albedo, c, atol=1e-6)
 
 
+@pytest.mark.parametrize("kind", ["point", "spot"])
+def test_point_and_spot_lights_closed_form(oracle, kind):
+    """Raycast of a matte plane under a point or spot light (orthographic
+    view from above): c/pi * color * intensity / d^2 * cos(theta) +
+    c * ambient, times the spot's smoothstep between cos(openingAngle) and
+    cos(openingAngle - 2 falloffAngle) of the angle to its axis."""
+    pos = np.array([1.0, -0.5, 3.0])
+    col, inten = np.array([1.0, 0.8, 0.6]), 5.0
+    light = {"type": kind, "position": pos.tolist(), "intensity": inten, "color": col.tolist()}
+    if kind == "spot":
+        light.update(direction=[0.0, 0.0, -1.0], openingAngle=0.9, falloffAngle=0.2)
+    sc = plane_scene()
+    sc["lights"] = [light]
+    sc["camera"] = {"type": "orthographic", "position": [0.0, 0.0, 10.0],
+                    "direction": [0.0, 0.0, -1.0], "up": [0.0, 1.0, 0.0], "height": 8.0,
+                    "aspect": 1.0}
+    S = oracle.Scene(sc)
+    F = oracle.Frame(16, 16)
+    oracle.render(S, F)
+    xs = ((np.arange(16) + 0.5) / 16 - 0.5) * 8.0
+    X, Y = np.meshgrid(xs, xs)  # rows are image y (up)
+    L = pos[None, None, :] - np.stack([X, Y, np.zeros_like(X)], axis=-1)
+    d2 = (L * L).sum(-1)
+    cos = np.maximum(0.0, L[..., 2] / np.sqrt(d2))
+    factor = np.ones_like(d2)
+    if kind == "spot":
+        spot = L[..., 2] / np.sqrt(d2)  # axis (0,0,-1) against the direction light -> point
+        co, ci = math.cos(0.9), math.cos(0.9 - 0.4)
+        u = np.clip((spot - co) / (ci - co), 0.0, 1.0)
+        factor = np.where(spot < co, 0.0, np.where(spot > ci, 1.0, u * u * (3 - 2 * u)))
+        assert (factor == 0).any() and (factor == 1).any() and ((factor > 0) & (factor < 1)).any()
+    c = np.array([0.6, 0.5, 0.4])
+    expect = (c / math.pi)[None, None, :] * (col * inten)[None, None, :] * \
+        (cos * factor / d2)[..., None] + c * 0.2
+    assert np.allclose(F.color[..., :3], expect, rtol=1e-4, atol=1e-5)
+
+
 def test_emission_absorption_slab(oracle):
     """Constant field, TF alpha a: alpha after k steps is 1 - (1-a)^(k dt/ud)."""
     n = 16

@@ -208,13 +208,33 @@ __device__ __forceinline__ void localRay(const DInstance &I, float3 o, float3 d,
   ld = mat3mul(I.affineInv, d);
 }
 
+// Ray/sphere test in the form of Visionaray's basic_sphere intersection
+// (used by the reference through intersect(ray, bls.asSphere),
+// DeviceCopyableObjects.h:1486-1507): the two roots of
+// |o + t d - c|^2 = r^2 from the cancellation-free quadratic formula, the
+// smaller one returned (a ray starting inside the sphere reports the
+// negative root and so misses it).
+__device__ __forceinline__ float sphereHitT(float3 o, float3 d, float4 sph) {
+  const float3 oc = o - f3(sph.x, sph.y, sph.z);
+  const float A = dot(d, d);
+  const float B = 2.f * dot(d, oc);
+  const float C = dot(oc, oc) - sph.w * sph.w;
+  const float disc = B * B - 4.f * A * C;
+  if (!(disc >= 0.f)) return -1.f;
+  const float rd = sqrtf(disc);
+  const float q = B < 0.f ? -0.5f * (B - rd) : -0.5f * (B + rd);
+  const float t1 = q / A, t2 = C / q;
+  return t1 > t2 ? t2 : t1;
+}
+
 // Stack-based BVH2 traversal, near child first, in the while-while form
 // (an inner-node loop, then a leaf loop) so the lanes of a warp stay in
 // step. One loop serves closest-hit and any-hit rays (anyHit stops at the
 // first accepted hit), so shadow/AO rays and radiance rays in one warp share
 // the same instructions. Closest hits are ordered by (t, instance, triangle),
 // the order the CPU restatement uses, so any valid BVH gives the same hit.
-template <bool Count>
+// Spheres = true walks the group's sphere BVH with sphere leaves.
+template <bool Count, bool Spheres = false>
 __device__ __forceinline__ bool traverseGroup(const DGroup &G, float3 o, float3 d, float tmin,
                                               int inst, bool anyHit, Hit &best, uint32_t &err,
                                               unsigned long long *cnt) {
@@ -228,7 +248,7 @@ __device__ __forceinline__ bool traverseGroup(const DGroup &G, float3 o, float3 
   while (!done) {
     // inner nodes until a leaf comes up or nothing is left
     while (node >= 0) {
-      const float4 *N = G.nodes + 4 * (size_t)node;
+      const float4 *N = (Spheres ? G.sphNodes : G.nodes) + 4 * (size_t)node;
       const float4 n0 = __ldg(N), n1 = __ldg(N + 1), n2 = __ldg(N + 2);
       const int4 n3 = __ldg(reinterpret_cast<const int4 *>(N + 3));
       if (Count) ++nodeVisits;
@@ -267,6 +287,20 @@ __device__ __forceinline__ bool traverseGroup(const DGroup &G, float3 o, float3 
       const int first = (int)(code & kLeafFirstMask);
       const int count = (int)(code >> kLeafCountShift) + 1;
       for (int k = 0; k < count; ++k) {
+        if constexpr (Spheres) {
+          if (Count) ++triTests;
+          const float t = sphereHitT(o, d, __ldg(G.spheres + first + k));
+          if (!(t >= tmin)) continue;
+          const int local = G.numTris + (int)__ldg(G.sphLocal + first + k);
+          const bool closer =
+              t < best.t || (t == best.t && best.inst >= 0 &&
+                             (inst < best.inst || (inst == best.inst && local < best.tri)));
+          if (!closer) continue;
+          best.t = t; best.u = 0.f; best.v = 0.f; best.inst = inst; best.tri = local;
+          best.leaf = first + k;
+          found = true;
+          continue;
+        }
         const float4 *T = G.tris + 3 * (size_t)(first + k);
         const float4 ta = __ldg(T), tbv = __ldg(T + 1), tc = __ldg(T + 2);
         if (Count) ++triTests;
@@ -430,7 +464,7 @@ __device__ __forceinline__ bool traverseGroup4(const DGroup &G, float3 o, float3
 
 // intersectSurfaces(Ray, TLS, shadow), DeviceCopyableObjects.h:1826-1839,
 // with intersect(Ray, Instance) :1772-1814 for the instance transform.
-template <bool Count>
+template <bool Count, bool Full = false>
 __device__ __forceinline__ bool traceSurfaces(const DScene &S, const Ray &r, bool anyHit, Hit &h,
                                               uint32_t &err, unsigned long long *cnt) {
   h.t = r.tmax;
@@ -443,11 +477,15 @@ __device__ __forceinline__ bool traceSurfaces(const DScene &S, const Ray &r, boo
   for (int i = 0; i < S.numInstances; ++i) {
     const DInstance &I = S.instances[i];
     const DGroup &G = S.groups[I.group];
-    if (G.numNodes == 0) continue;
+    if (!Full && G.numNodes == 0) continue;
     float3 lo, ld;
     localRay(I, r.o, r.d, lo, ld);
-    const bool f = G.width == 4 ? traverseGroup4<Count>(G, lo, ld, r.tmin, i, anyHit, h, err, cnt)
-                                : traverseGroup<Count>(G, lo, ld, r.tmin, i, anyHit, h, err, cnt);
+    bool f = false;
+    if (!Full || G.numNodes > 0)
+      f = G.width == 4 ? traverseGroup4<Count>(G, lo, ld, r.tmin, i, anyHit, h, err, cnt)
+                       : traverseGroup<Count>(G, lo, ld, r.tmin, i, anyHit, h, err, cnt);
+    if (Full && G.sphNumNodes > 0 && !(anyHit && f))
+      f = traverseGroup<Count, true>(G, lo, ld, r.tmin, i, anyHit, h, err, cnt) || f;
     if (f) {
       any = true;
       if (anyHit) break;
@@ -455,6 +493,30 @@ __device__ __forceinline__ bool traceSurfaces(const DScene &S, const Ray &r, boo
   }
   if (!any) h.t = FLT_MAX;
   return any;
+}
+
+// Surface index of a hit (a triangle's, or with Full a sphere's).
+template <bool Full>
+__device__ __forceinline__ uint32_t hitSurface(const DGroup &G, const Hit &h) {
+  if (Full && h.tri >= G.numTris) return __ldg(G.sphSurface + (h.tri - G.numTris));
+  return __ldg(G.triSurface + h.tri);
+}
+
+// Object-space geometric normal of a hit, getNormals (renderer/common.h:
+// 241-275): normalize(e1 x e2) for a triangle, normalize((P - c) / r) at
+// the instance-local hit position P for a sphere.
+template <bool Full>
+__device__ __forceinline__ float3 hitNormal(const DGroup &G, const DInstance &I, const Hit &h,
+                                            float3 o, float3 d) {
+  if (Full && h.tri >= G.numTris) {
+    const float4 sp = __ldg(G.spheres + h.leaf);
+    float3 lo, ld;
+    localRay(I, o, d, lo, ld);
+    return normalize((lo + h.t * ld - f3(sp.x, sp.y, sp.z)) / sp.w);
+  }
+  const float4 *E = G.tris + 3 * (size_t)h.leaf;
+  const float4 e1 = __ldg(E + 1), e2 = __ldg(E + 2);
+  return normalize(cross(f3(e1.x, e1.y, e1.z), f3(e2.x, e2.y, e2.z)));
 }
 
 // --------------------------------------------------------------- materials

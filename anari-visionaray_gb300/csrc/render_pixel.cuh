@@ -30,7 +30,7 @@ __device__ void raycastSample(const DScene &S, const DRenderer &R, Ray ray, cons
   float surfaceAlpha = 0.f;
   if (Surfaces && S.hasSurfaces) {
     Hit hr;
-    bool hit = traceSurfaces<Count>(S, ray, false, hr, err, cnt);
+    bool hit = traceSurfaces<Count, Full>(S, ray, false, hr, err, cnt);
     bool first = true;
     int layers = 0;
     while (hit) {
@@ -40,12 +40,10 @@ __device__ void raycastSample(const DScene &S, const DRenderer &R, Ray ray, cons
       }
       const DInstance &I = S.instances[hr.inst];
       const DGroup &G = S.groups[I.group];
-      const DMaterial &mat = S.materials[__ldg(G.triSurface + hr.tri)];
+      const DMaterial &mat = S.materials[hitSurface<Full>(G, hr)];
       const float3 hitPos = ray.o + hr.t * ray.d;
-      // getNormals (renderer/common.h:241-264): Ng = normalize(e1 x e2)
-      const float4 *E = G.tris + 3 * (size_t)hr.leaf;
-      const float4 e1 = __ldg(E + 1), e2 = __ldg(E + 2);
-      float3 gn = normalize(cross(f3(e1.x, e1.y, e1.z), f3(e2.x, e2.y, e2.z)));
+      // getNormals (renderer/common.h:241-275)
+      float3 gn = hitNormal<Full>(G, I, hr, ray.o, ray.d);
       float3 sn = gn;
       gn = normalize(mat3mul(I.normalXfm, gn));
       sn = normalize(mat3mul(I.normalXfm, sn));
@@ -75,7 +73,7 @@ __device__ void raycastSample(const DScene &S, const DRenderer &R, Ray ray, cons
       if (surfaceAlpha < 0.999f) {
         const float eps = epsilonFrom(hitPos, ray.d, hr.t);
         ray.tmin = hr.t + eps;
-        hit = traceSurfaces<Count>(S, ray, false, hr, err, cnt);
+        hit = traceSurfaces<Count, Full>(S, ray, false, hr, err, cnt);
       } else {
         ray.tmax = hr.t;
         break;
@@ -215,7 +213,7 @@ struct HitRec {
 // intersectAll, renderer/common.h:1605-1620, with intersectSurfaces<1>
 // (:1502-1543: one draw per surface hit) and the volume free-flight
 // sampling of every volume in the world.
-template <bool Count>
+template <bool Count, bool Full>
 __device__ __forceinline__ void intersectAll(const DScene &S, const Ray &ray, bool shadow, Rng &rnd,
                                              HitRec &h, uint32_t &err, unsigned long long *cnt,
                                              bool hwFilter) {
@@ -223,16 +221,16 @@ __device__ __forceinline__ void intersectAll(const DScene &S, const Ray &ray, bo
   if (S.hasSurfaces) {
     Ray r = ray;
     const bool anyHit = shadow && S.allOpaque;
-    bool hit = traceSurfaces<Count>(S, r, anyHit, h.surf, err, cnt);
+    bool hit = traceSurfaces<Count, Full>(S, r, anyHit, h.surf, err, cnt);
     int guard = 1 << 16;
     while (hit) {
       const DGroup &G = S.groups[S.instances[h.surf.inst].group];
-      const float opacity = materialOpacity(S.materials[__ldg(G.triSurface + h.surf.tri)]);
+      const float opacity = materialOpacity(S.materials[hitSurface<Full>(G, h.surf)]);
       const float u = rnd();
       if (u > opacity && --guard > 0) {
         const float3 hp = r.o + h.surf.t * r.d;
         r.tmin = h.surf.t + epsilonFrom(hp, r.d, h.surf.t);
-        hit = traceSurfaces<Count>(S, r, false, h.surf, err, cnt);
+        hit = traceSurfaces<Count, Full>(S, r, false, h.surf, err, cnt);
       } else {
         break;
       }
@@ -320,7 +318,7 @@ __device__ __forceinline__ void pathtracePixel(const DScene &S, const DCamera &C
           // cannot hit anything: skip the traversal
           hr.surfHit = hr.volHit = hr.hit = hr.volumeHit = false;
         } else {
-          intersectAll<Count>(S, ray, rayType == RT_SHADOW || rayType == RT_AO, rnd, hr, err, cnt,
+          intersectAll<Count, Full>(S, ray, rayType == RT_SHADOW || rayType == RT_AO, rnd, hr, err, cnt,
                               R.hwFilter != 0);
         }
         int nextType = RT_MISS;
@@ -368,10 +366,8 @@ __device__ __forceinline__ void pathtracePixel(const DScene &S, const DCamera &C
               const DGroup &G = S.groups[I.group];
               hitPos = ray.o + hr.surf.t * ray.d;
               eps = epsilonFrom(hitPos, ray.d, hr.surf.t);
-              mat = &S.materials[__ldg(G.triSurface + hr.surf.tri)];
-              const float4 *E = G.tris + 3 * (size_t)hr.surf.leaf;
-              const float4 e1 = __ldg(E + 1), e2 = __ldg(E + 2);
-              gn = normalize(cross(f3(e1.x, e1.y, e1.z), f3(e2.x, e2.y, e2.z)));
+              mat = &S.materials[hitSurface<Full>(G, hr.surf)];
+              gn = hitNormal<Full>(G, I, hr.surf, ray.o, ray.d);
               sn = normalize(mat3mul(I.normalXfm, gn));
               gn = sn;
               sn = faceforward(sn, viewDir, gn);

@@ -424,10 +424,16 @@ struct Volume : Object {
 // triangle geometry, scene/surface/geometry/Triangle.cpp:46-133
 struct Geometry : Object {
   std::vector<float> v1, e1, e2;  // per triangle, float3 packed
+  std::vector<float> spheres;     // per sphere: center, radius
   using Object::Object;
   void commit() override {
     valid = false;
     v1.clear(); e1.clear(); e2.clear();
+    spheres.clear();
+    if (subtype == "sphere") {
+      commitSpheres();
+      return;
+    }
     Array *pos = geto<Array>("vertex.position", VSR_ARRAY1D);
     Array *idx = geto<Array>("primitive.index", VSR_ARRAY1D);
     if (!pos || pos->elemType != VSR_FLOAT32_VEC3) {
@@ -465,7 +471,49 @@ struct Geometry : Object {
                   "'vertex.normal' is not used: shading uses the geometric normal");
     valid = true;
   }
+  // Sphere.cpp:19-83: centers from vertex.position (through primitive.index
+  // when given), radius from vertex.radius indexed by the sphere (not by the
+  // vertex), else the global 'radius' (default 0.01)
+  void commitSpheres() {
+    Array *pos = geto<Array>("vertex.position", VSR_ARRAY1D);
+    Array *idx = geto<Array>("primitive.index", VSR_ARRAY1D);
+    Array *rad = geto<Array>("vertex.radius", VSR_ARRAY1D);
+    if (!pos || pos->elemType != VSR_FLOAT32_VEC3) {
+      warn("missing required parameter 'vertex.position' on sphere geometry");
+      return;
+    }
+    if (idx && idx->elemType != VSR_UINT32) {
+      warn("unsupported type for 'primitive.index' on sphere geometry");
+      return;
+    }
+    if (rad && rad->elemType != VSR_FLOAT32) {
+      warn("unsupported type for 'vertex.radius' on sphere geometry");
+      return;
+    }
+    float globalRadius = 0.01f;
+    getf("radius", globalRadius);
+    const float *P = pos->as<float>();
+    const size_t nv = pos->size();
+    const size_t n = idx ? idx->size() : nv;
+    if (rad && rad->size() < n) {
+      warn("'vertex.radius' shorter than the number of spheres");
+      return;
+    }
+    spheres.resize(4 * n);
+    for (size_t i = 0; i < n; ++i) {
+      const size_t v = idx ? idx->as<uint32_t>()[i] : i;
+      if (v >= nv) {
+        warn("'primitive.index' out of range on sphere geometry");
+        spheres.clear();
+        return;
+      }
+      for (int k = 0; k < 3; ++k) spheres[4 * i + k] = P[3 * v + k];
+      spheres[4 * i + 3] = rad ? rad->as<float>()[i] : globalRadius;
+    }
+    valid = true;
+  }
   size_t numTris() const { return v1.size() / 3; }
+  size_t numSpheres() const { return spheres.size() / 4; }
 };
 
 // matte / physicallyBased, scene/surface/material/{Matte,PBM}.cpp
@@ -799,7 +847,9 @@ struct Renderer : Object {
 // ----------------------------------------------------------------- world
 struct GroupGPU {
   DevBuf v1, e1, e2, nodes, nodes4, tris, triSurface, triPrim;
+  DevBuf sphSrc, sphNodes, sphLeaf, spheres, sphLocal, sphSurface;
   int numTris = 0, numNodes = 0, width = 2;
+  int numSpheres = 0, sphNumNodes = 0;
   float buildMs = 0.f;
 };
 
@@ -852,6 +902,57 @@ struct World : Object {
     valid = true;
   }
 
+  // The group's spheres get their own BVH2 from the triangle builder: each
+  // sphere enters as a triangle spanning its bounding box (v1 = c - r,
+  // v1 + e1 = c + r, v1 + e2 another box corner), then a gather puts the
+  // spheres and their group indices in leaf order.
+  bool buildSpheres(GroupGPU &gg, const std::vector<float> &sph,
+                    const std::vector<uint32_t> &sphSurf, cudaStream_t s) {
+    const int ns = (int)sphSurf.size();
+    std::vector<float> v1(3 * ns), e1(3 * ns), e2(3 * ns);
+    for (int k = 0; k < ns; ++k) {
+      const float r = sph[4 * k + 3];
+      for (int a = 0; a < 3; ++a) {
+        v1[3 * k + a] = sph[4 * k + a] - r;
+        e1[3 * k + a] = 2.f * r;
+        e2[3 * k + a] = a == 1 ? 0.f : 2.f * r;
+      }
+    }
+    const size_t fb = (size_t)ns * 3 * sizeof(float);
+    DevBuf bv1, be1, be2;
+    if (bv1.upload(v1.data(), fb, s) || be1.upload(e1.data(), fb, s) ||
+        be2.upload(e2.data(), fb, s) ||
+        gg.sphSrc.upload(sph.data(), (size_t)ns * sizeof(float4), s) ||
+        gg.sphSurface.upload(sphSurf.data(), (size_t)ns * sizeof(uint32_t), s) ||
+        gg.sphNodes.alloc((size_t)std::max(ns - 1, 1) * 4 * sizeof(float4)) ||
+        gg.sphLeaf.alloc((size_t)ns * 3 * sizeof(float4)) ||
+        gg.spheres.alloc((size_t)ns * sizeof(float4)) ||
+        gg.sphLocal.alloc((size_t)ns * sizeof(uint32_t))) {
+      dev->report(this, kind, VSR_SEVERITY_ERROR, VSR_ERROR_OUT_OF_MEMORY, "scene upload failed");
+      return false;
+    }
+    BvhBuildStats st{};
+    auto build = fastBuild ? buildGroupBVH : buildGroupBVHQuality;
+    cudaError_t e = build(bv1.as<float>(), be1.as<float>(), be2.as<float>(), ns,
+                          gg.sphNodes.as<float4>(), gg.sphLeaf.as<float4>(), &st, s);
+    if (e == cudaSuccess)
+      e = launchGatherSpheres(gg.sphLeaf.as<float4>(), gg.sphSrc.as<float4>(), ns,
+                              gg.spheres.as<float4>(), gg.sphLocal.as<uint32_t>(), s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) {
+      dev->report(this, kind, VSR_SEVERITY_ERROR, VSR_ERROR_CUDA, "sphere BVH build failed: %s",
+                  cudaGetErrorString(e));
+      return false;
+    }
+    gg.sphLeaf.release();
+    gg.sphSrc.release();
+    gg.numSpheres = ns;
+    gg.sphNumNodes = st.numNodes;
+    gg.buildMs += st.buildMs;
+    bvhNodes += (uint64_t)st.numNodes;
+    return true;
+  }
+
   bool buildScene(uint64_t deep) {
     auto t0 = std::chrono::steady_clock::now();
     cudaStream_t s = dev->stream;
@@ -879,11 +980,14 @@ struct World : Object {
     groupsGPU.clear();
     bvhNodes = bvhTris = 0;
     bool allOpaque = true, anySurf = false;
+    int numSpheres = 0;
     for (size_t gi = 0; gi < groups.size(); ++gi) {
       Group *g = groups[gi];
       auto gg = std::make_unique<GroupGPU>();
       std::vector<float> v1, e1, e2;
       std::vector<uint32_t> triSurf, triPrim;
+      std::vector<float> sph;
+      std::vector<uint32_t> sphSurf;
       float lo[3] = {1e30f, 1e30f, 1e30f}, hi[3] = {-1e30f, -1e30f, -1e30f};
       for (Surface *sf : g->surfaces) {
         if (!sf->valid || !sf->geom->valid || !sf->mat->valid) continue;
@@ -891,6 +995,18 @@ struct World : Object {
         mats.push_back(sf->mat->m);
         if (sf->mat->m.alphaMode != ALPHA_OPAQUE) allOpaque = false;
         Geometry *G = sf->geom;
+        if (G->numSpheres()) {
+          sph.insert(sph.end(), G->spheres.begin(), G->spheres.end());
+          for (size_t k = 0; k < G->numSpheres(); ++k) {
+            sphSurf.push_back(sid);
+            for (int a = 0; a < 3; ++a) {
+              const float c = G->spheres[4 * k + a], r = G->spheres[4 * k + 3];
+              lo[a] = std::min(lo[a], c - r);
+              hi[a] = std::max(hi[a], c + r);
+            }
+          }
+          continue;
+        }
         size_t nt = G->numTris();
         v1.insert(v1.end(), G->v1.begin(), G->v1.end());
         e1.insert(e1.end(), G->e1.begin(), G->e1.end());
@@ -970,6 +1086,21 @@ struct World : Object {
         bvhNodes += (uint64_t)st.numNodes;
         bvhTris += (uint64_t)nt;
       }
+      const int ns = (int)sphSurf.size();
+      if (ns >= (1 << 27)) {
+        dev->report(this, kind, VSR_SEVERITY_ERROR, VSR_ERROR_INVALID_ARGUMENT,
+                    "group has more than 2^27 spheres");
+        return false;
+      }
+      if (ns > 0 && !buildSpheres(*gg, sph, sphSurf, s)) return false;
+      if (ns > 0) anySurf = true;
+      dg.sphNodes = gg->sphNodes.as<float4>();
+      dg.spheres = gg->spheres.as<float4>();
+      dg.sphLocal = gg->sphLocal.as<uint32_t>();
+      dg.sphSurface = gg->sphSurface.as<uint32_t>();
+      dg.numSpheres = gg->numSpheres;
+      dg.sphNumNodes = gg->sphNumNodes;
+      numSpheres += ns;
       dg.nodes = gg->nodes.as<float4>();
       dg.tris = gg->tris.as<float4>();
       dg.triSurface = gg->triSurface.as<uint32_t>();
@@ -1074,6 +1205,7 @@ struct World : Object {
     scene.numVolumes = (int)vols.size();
     scene.allOpaque = allOpaque ? 1 : 0;
     scene.hasSurfaces = anySurf ? 1 : 0;
+    scene.numSpheres = numSpheres;
     builtStamp = deep;
     commitMs = std::chrono::duration<float, std::milli>(std::chrono::steady_clock::now() - t0).count();
     return true;
@@ -1299,6 +1431,9 @@ VSRStatus renderFrame(Device *dev, FrameObj *F) {
   }
   const bool doRender = F->accumID < F->renderer->sampleLimit;
   const DRenderer &R = F->renderer->r;
+  // the wavefront kernels have neither gradient shading nor spheres: the
+  // megakernel takes such frames
+  const bool wave = F->renderer->wavefront && !R.gradientShading && !W->scene.numSpheres;
   int stage = 0;
   MarchScratch ms{};
   bool segmented = false;
@@ -1314,7 +1449,7 @@ VSRStatus renderFrame(Device *dev, FrameObj *F) {
       return VSR_ERROR_OUT_OF_MEMORY;
     }
     if (segmented) ms = F->march();
-  } else if (doRender && F->renderer->wavefront && !R.gradientShading && !F->ensureWave()) {
+  } else if (doRender && wave && !F->ensureWave()) {
     dev->report(F, VSR_FRAME, VSR_SEVERITY_ERROR, VSR_ERROR_OUT_OF_MEMORY,
                 "wavefront state allocation failed");
     return VSR_ERROR_OUT_OF_MEMORY;
@@ -1331,9 +1466,7 @@ VSRStatus renderFrame(Device *dev, FrameObj *F) {
     if (R.type == REND_RAYCAST) {
       e = launchRaycast(W->scene, F->camera->c, R, fr, stage, F->countStats,
                         segmented ? &ms : nullptr, s);
-    } else if (F->renderer->wavefront && !R.gradientShading) {
-      // (the wavefront shading kernel has no gradient shading: the
-      // megakernel takes such frames)
+    } else if (wave) {
       e = launchPathtraceWavefront(W->scene, F->camera->c, R, fr, F->wave(), F->pinnedCount,
                                    F->countStats, s, &F->lastIterations);
     } else {
@@ -1492,7 +1625,8 @@ VSRStatus renderFrames(Device *dev, FrameObj *const *frames, uint32_t count) {
     }
     j.F = F->record();
     j.kind = j.R.type != REND_RAYCAST ? JOB_PATHTRACE
-             : (j.R.gradientShading || j.S.positionalLights) ? JOB_RAYCAST_FULL
+             : (j.R.gradientShading ||
+                (j.S.hasSurfaces && (j.S.positionalLights || j.S.numSpheres))) ? JOB_RAYCAST_FULL
              : j.S.hasSurfaces        ? JOB_RAYCAST_SURFACES
                                       : JOB_RAYCAST_VOLUME;
     // a frame past its sample limit only clears its error flags
@@ -1502,7 +1636,7 @@ VSRStatus renderFrames(Device *dev, FrameObj *const *frames, uint32_t count) {
     key.insert(key.end(), {(uint64_t)(uintptr_t)F, (uint64_t)j.F.width, (uint64_t)j.F.height,
                            (uint64_t)j.kind, (uint64_t)j.R.pixelSamples, (uint64_t)j.R.maxBounce,
                            (uint64_t)j.S.numVolumes, (uint64_t)j.R.gradientShading,
-                           (uint64_t)j.S.positionalLights});
+                           (uint64_t)j.S.positionalLights, (uint64_t)j.S.numSpheres});
   }
   if (!batched.empty()) {
     BatchTuner &tuner = B.tuners[key];
@@ -1564,7 +1698,7 @@ VSRStatus renderFrames(Device *dev, FrameObj *const *frames, uint32_t count) {
     for (const DJob &j : jobs)
       if (j.kind == JOB_PATHTRACE) {
         if (j.S.numVolumes > 0) L.pathtraceVariant |= 1;
-        if (j.S.positionalLights || (j.S.numVolumes > 0 && j.R.gradientShading))
+        if (j.S.positionalLights || j.S.numSpheres || (j.S.numVolumes > 0 && j.R.gradientShading))
           L.pathtraceVariant |= 2;
       }
     // one CUDA graph per frame set and configuration: the job records are
@@ -1778,7 +1912,7 @@ VSRObject vsrNewVolume(VSRDevice d, const char *s) {
   return newObj<Volume>(d, VSR_VOLUME, s, {"transferFunction1D"});
 }
 VSRObject vsrNewGeometry(VSRDevice d, const char *s) {
-  return newObj<Geometry>(d, VSR_GEOMETRY, s, {"triangle"});
+  return newObj<Geometry>(d, VSR_GEOMETRY, s, {"triangle", "sphere"});
 }
 VSRObject vsrNewMaterial(VSRDevice d, const char *s) {
   return newObj<Material>(d, VSR_MATERIAL, s, {"matte", "physicallyBased"});

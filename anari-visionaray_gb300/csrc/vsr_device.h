@@ -147,6 +147,16 @@ struct DGroup {
   int width;              // 2: BVH2 nodes (64 B), 4: BVH4 nodes (128 B)
   int volBegin, volEnd;   // range in DScene::groupVolumes
   float boundsLo[3], boundsHi[3];
+  // spheres (all sphere geometries of the group), their own BVH2: leaves
+  // index `spheres` (center, radius) in leaf order; sphLocal maps a leaf
+  // to the sphere's index in the group, sphSurface a sphere to its surface.
+  // A hit on sphere k carries Hit::tri = numTris + k.
+  const float4 *sphNodes;
+  const float4 *spheres;
+  const uint32_t *sphLocal;
+  const uint32_t *sphSurface;
+  int numSpheres;
+  int sphNumNodes;
 };
 
 struct DInstance {
@@ -168,6 +178,7 @@ struct DScene {
   int numGroups;
   int numLights;
   int positionalLights;  // point and spot lights among them: the kernels' full variants
+  int numSpheres;        // spheres in all groups: the kernels' full variants
   int numVolumes;
   int allOpaque;
   int hasSurfaces;

@@ -5,7 +5,10 @@ No public dataset is involved: each configuration is generated from a
 numpy PCG64 stream seeded with 0x5EED0000 + config index; the draw order
 is fixed in each generator. A scene is a plain dict:
 
-  surfaces : [{"vertices": (V,3) f32, "indices": (T,3) u32, "material": {...}}]
+  surfaces : [{"vertices": (V,3) f32, "indices": (T,3) u32, "material": {...}} |
+              {"geometry": "sphere", "vertices": (V,3) f32 centres, "indices": (N,) u32
+               (optional), "radii": (N,) f32 (optional), "radius": f32 (default 0.01),
+               "material": {...}}]
   volumes  : [{"data": (nz,ny,nx) f32, "origin", "spacing", "color": (N,3),
                "opacity": (N,), "valueRange", "unitDistance"}]
   lights   : [{"type": "directional" (default), "direction", "color", "irradiance",
@@ -306,18 +309,33 @@ def _material(dev, m):
 def _surfaces(dev, surfs, keep):
     out = []
     for s in surfs:
-        g = dev.geometry("triangle")
+        kind = s.get("geometry", "triangle")
+        g = dev.geometry(kind)
         va = dev.array1d(np.asarray(s["vertices"], np.float32))
-        ia = dev.array1d(np.asarray(s["indices"], np.uint32))
         dev.set(g, "vertex.position", va)
-        dev.set(g, "primitive.index", ia)
+        keep += [va]
+        ia = None
+        if kind == "sphere":
+            if "indices" in s:
+                ia = dev.array1d(np.asarray(s["indices"], np.uint32).reshape(-1))
+            if "radii" in s:
+                ra = dev.array1d(np.asarray(s["radii"], np.float32).reshape(-1))
+                dev.set(g, "vertex.radius", ra)
+                keep += [ra]
+            if "radius" in s:
+                dev.set(g, "radius", float(s["radius"]))
+        else:
+            ia = dev.array1d(np.asarray(s["indices"], np.uint32))
+        if ia is not None:
+            dev.set(g, "primitive.index", ia)
+            keep += [ia]
         dev.commit(g)
         mat = _material(dev, s["material"])
         sf = dev.surface()
         dev.set(sf, "geometry", g)
         dev.set(sf, "material", mat)
         dev.commit(sf)
-        keep += [g, va, ia, mat]
+        keep += [g, mat]
         out.append(sf)
     return out
 

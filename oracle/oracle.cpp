@@ -373,9 +373,28 @@ BoxHit intersectBox(const Ray &r, const Box &b) {
 struct SurfHit {
   bool hit = false;
   float t = FLT_MAX, u = 0, v = 0;
-  int inst = -1, tri = -1;
-  f3 isect_pos;
+  int inst = -1, tri = -1;  // tri: global triangle index, -1 for a sphere
+  int sph = -1;             // global sphere index, -1 for a triangle
+  int key = -1;             // order within the instance: triangles, then spheres
+  f3 isect_pos;             // instance-local hit position
 };
+
+// Ray/sphere test as Visionaray's basic_sphere intersection (the reference's
+// intersect(ray, bls.asSphere), DeviceCopyableObjects.h:1486-1507): the
+// smaller root of |o + t d - c|^2 = r^2 from the cancellation-free
+// quadratic formula; -1 without real roots.
+inline float hitSphere(const Ray &r, const float *sph) {
+  f3 oc = r.ori - f3(sph[0], sph[1], sph[2]);
+  float A = dot(r.dir, r.dir);
+  float B = 2.f * dot(r.dir, oc);
+  float C = dot(oc, oc) - sph[3] * sph[3];
+  float disc = B * B - 4.f * A * C;
+  if (!(disc >= 0.f)) return -1.f;
+  float rd = std::sqrt(disc);
+  float q = B < 0.f ? -0.5f * (B - rd) : -0.5f * (B + rd);
+  float t1 = q / A, t2 = C / q;
+  return t1 > t2 ? t2 : t1;
+}
 
 // Ray/triangle test in the basic_triangle (Moller-Trumbore) form; u,v are
 // the barycentrics of v2 and v3.
@@ -406,8 +425,23 @@ SurfHit traceSurfaces(const Scene &sc, const Ray &ray, Counters &c) {
   for (size_t ii = 0; ii < sc.insts.size(); ++ii) {
     const Inst &inst = sc.insts[ii];
     const GroupBVH &bvh = sc.bvh[inst.group];
-    if (bvh.nodes.empty()) continue;
+    const OrGroup &og = sc.src->groups[inst.group];
     Ray l = inst.toLocal(ray);
+    // spheres: every one of the group's (no acceleration structure)
+    for (int k = og.sphBegin; k < og.sphEnd; ++k) {
+      c.tris++;
+      float t = hitSphere(l, sc.src->spheres + 4 * (size_t)k);
+      if (!(t >= l.tmin)) continue;
+      int key = (og.triEnd - og.triBegin) + (k - og.sphBegin);
+      bool closer = t < best.t ||
+                    (t == best.t && best.hit &&
+                     ((int)ii < best.inst || ((int)ii == best.inst && key < best.key)));
+      if (!closer) continue;
+      best.hit = true; best.t = t; best.u = 0.f; best.v = 0.f;
+      best.inst = (int)ii; best.tri = -1; best.sph = k; best.key = key;
+      best.isect_pos = l.ori + t * l.dir;
+    }
+    if (bvh.nodes.empty()) continue;
     f3 inv = f3(1.f) / l.dir;
     int stack[128];
     int sp = 0;
@@ -425,12 +459,13 @@ SurfHit traceSurfaces(const Scene &sc, const Ray &ray, Counters &c) {
           c.tris++;
           float t, u, v;
           if (!hitTri(l, sc.tris[tri], l.tmin, t, u, v)) continue;
+          int key = tri - og.triBegin;
           bool closer = t < best.t ||
                         (t == best.t && best.hit &&
-                         ((int)ii < best.inst || ((int)ii == best.inst && tri < best.tri)));
+                         ((int)ii < best.inst || ((int)ii == best.inst && key < best.key)));
           if (!closer) continue;
           best.hit = true; best.t = t; best.u = u; best.v = v;
-          best.inst = (int)ii; best.tri = tri;
+          best.inst = (int)ii; best.tri = tri; best.sph = -1; best.key = key;
           best.isect_pos = l.ori + t * l.dir;
         }
       } else {
@@ -441,6 +476,22 @@ SurfHit traceSurfaces(const Scene &sc, const Ray &ray, Counters &c) {
   }
   if (!best.hit) best.t = FLT_MAX;
   return best;
+}
+
+// Surface index and object-space geometric normal of a surface hit
+// (getNormals, renderer/common.h:241-275): normalize(e1 x e2) for a
+// triangle, normalize((P - c) / r) at the local hit position for a sphere.
+uint32_t hitSurface(const OrScene &S, const SurfHit &h) {
+  return h.sph >= 0 ? S.sphereSurface[h.sph] : S.triSurface[h.tri];
+}
+
+f3 hitNormal(const Scene &sc, const SurfHit &h) {
+  if (h.sph >= 0) {
+    const float *s = sc.src->spheres + 4 * (size_t)h.sph;
+    return normalize((h.isect_pos - f3(s[0], s[1], s[2])) / s[3]);
+  }
+  const Tri &T = sc.tris[h.tri];
+  return normalize(cross(T.e1, T.e2));
 }
 
 // ---------------------------------------------------------------------------
@@ -1064,11 +1115,10 @@ PixelSample raycastSample(const Scene &sc, const OrRenderer &R, Ray ray, Counter
     if (!hr.hit) break;
     if (++layers > (1 << 12)) break;  // same bound as the GPU path (zero epsilon would loop)
     const Inst &inst = sc.insts[hr.inst];
-    uint32_t surf = S.triSurface[hr.tri];
+    uint32_t surf = hitSurface(S, hr);
     const OrMaterial &mat = S.surfMaterial[surf];
     f3 hitPos = ray.ori + hr.t * ray.dir;
-    const Tri &T = sc.tris[hr.tri];
-    f3 gn = normalize(cross(T.e1, T.e2));
+    f3 gn = hitNormal(sc, hr);
     f3 sn = gn;
     gn = normalize(inst.normalXfm * gn);
     sn = normalize(inst.normalXfm * sn);
@@ -1174,7 +1224,7 @@ HitRec intersectAll(const Scene &sc, const Ray &ray, LCG &rnd, Counters &c) {
   Ray r = ray;
   SurfHit hr = traceSurfaces(sc, r, c);
   while (hr.hit) {
-    const OrMaterial &mat = S.surfMaterial[S.triSurface[hr.tri]];
+    const OrMaterial &mat = S.surfMaterial[hitSurface(S, hr)];
     float opacity = materialOpacity(mat);
     float u = rnd();
     if (u > opacity) {
@@ -1255,9 +1305,8 @@ void shade(const Scene &sc, const OrRenderer &R, LCG &rnd, const Ray &ray, RayTy
       const Inst &inst = sc.insts[hr.inst];
       hitPos = ray.ori + hr.t * ray.dir;
       eps = epsilonFrom(hitPos, ray.dir, hr.t);
-      mat = &S.surfMaterial[S.triSurface[hr.tri]];
-      const Tri &T = sc.tris[hr.tri];
-      gn = normalize(cross(T.e1, T.e2));
+      mat = &S.surfMaterial[hitSurface(S, hr)];
+      gn = hitNormal(sc, hr);
       sn = gn;
       gn = normalize(inst.normalXfm * gn);
       sn = normalize(inst.normalXfm * sn);

@@ -44,7 +44,8 @@ class OrVolume(ctypes.Structure):
 
 
 class OrGroup(ctypes.Structure):
-    _fields_ = [("triBegin", c_int32), ("triEnd", c_int32), ("volBegin", c_int32), ("volEnd", c_int32)]
+    _fields_ = [("triBegin", c_int32), ("triEnd", c_int32), ("volBegin", c_int32), ("volEnd", c_int32),
+                ("sphBegin", c_int32), ("sphEnd", c_int32)]
 
 
 class OrInstance(ctypes.Structure):
@@ -64,7 +65,8 @@ class OrScene(ctypes.Structure):
                 ("surfObjID", UP), ("numVolumes", c_int32), ("volumes", ctypes.POINTER(OrVolume)),
                 ("numGroups", c_int32), ("groups", ctypes.POINTER(OrGroup)),
                 ("numInstances", c_int32), ("instances", ctypes.POINTER(OrInstance)),
-                ("numLights", c_int32), ("lights", ctypes.POINTER(OrLight))]
+                ("numLights", c_int32), ("lights", ctypes.POINTER(OrLight)),
+                ("numSpheres", c_int32), ("spheres", FP), ("sphereSurface", UP)]
 
 
 class OrCamera(ctypes.Structure):
@@ -208,11 +210,26 @@ class Scene:
             groups.append((inst.get("surfaces", []), inst.get("volumes", []),
                            inst.get("lights", []), inst["transform"]))
         verts, tsurf, tprim, mats, vols, ogroups, oinsts, lights = [], [], [], [], [], [], [], []
-        ntri = 0
+        sphs, ssurf = [], []
+        ntri = nsph = 0
         for gi, (surfs, vls, lts, xfm) in enumerate(groups):
             g = OrGroup()
             g.triBegin = ntri
+            g.sphBegin = nsph
             for s in surfs:
+                if s.get("geometry", "triangle") == "sphere":
+                    # Sphere.cpp:46-75: centres through primitive.index when
+                    # given; vertex.radius indexed by the sphere, else 'radius'
+                    c = np.asarray(s["vertices"], np.float32).reshape(-1, 3)
+                    if "indices" in s:
+                        c = c[np.asarray(s["indices"], np.int64).reshape(-1)]
+                    r = (np.asarray(s["radii"], np.float32).reshape(-1)[:len(c)] if "radii" in s
+                         else np.full(len(c), s.get("radius", 0.01), np.float32))
+                    sphs.append(np.concatenate([c, r[:, None]], axis=1))
+                    ssurf.append(np.full(len(c), len(mats), np.uint32))
+                    mats.append(material(s["material"]))
+                    nsph += len(c)
+                    continue
                 v = np.asarray(s["vertices"], np.float32)
                 t = np.asarray(s["indices"], np.uint32)
                 verts.append(v[t].reshape(-1, 9))
@@ -222,6 +239,7 @@ class Scene:
                 tprim.append(np.arange(len(t), dtype=np.uint32))
                 ntri += len(t)
             g.triEnd = ntri
+            g.sphEnd = nsph
             g.volBegin = len(vols)
             for v in vls:
                 ov = OrVolume()
@@ -278,7 +296,10 @@ class Scene:
         tri = np.ascontiguousarray(np.concatenate(verts) if verts else np.zeros((0, 9), np.float32))
         ts = np.ascontiguousarray(np.concatenate(tsurf) if tsurf else np.zeros(0, np.uint32))
         tp = np.ascontiguousarray(np.concatenate(tprim) if tprim else np.zeros(0, np.uint32))
-        self._keep += [tri, ts, tp]
+        sp = np.ascontiguousarray(np.concatenate(sphs) if sphs else np.zeros((0, 4), np.float32),
+                                  np.float32)
+        ss = np.ascontiguousarray(np.concatenate(ssurf) if ssurf else np.zeros(0, np.uint32))
+        self._keep += [tri, ts, tp, sp, ss]
         self.mats = (OrMaterial * max(1, len(mats)))(*mats)
         self.vols = (OrVolume * max(1, len(vols)))(*vols)
         self.groups = (OrGroup * max(1, len(ogroups)))(*ogroups)
@@ -302,6 +323,9 @@ class Scene:
         sc.instances = self.insts
         sc.numLights = len(lights)
         sc.lights = self.lights
+        sc.numSpheres = len(sp)
+        sc.spheres = fptr(sp)
+        sc.sphereSurface = ss.ctypes.data_as(UP)
         self.scene = sc
         self.handle = lib.or_scene_commit(ctypes.byref(sc))
         self.camera = camera(scene["camera"])

@@ -56,6 +56,7 @@ typedef struct OrVolume {
 typedef struct OrGroup {
   int32_t triBegin, triEnd; /* range in the scene's triangle array */
   int32_t volBegin, volEnd; /* range in the scene's volume array */
+  int32_t sphBegin, sphEnd; /* range in the scene's sphere array */
 } OrGroup;
 
 typedef struct OrInstance {
@@ -94,6 +95,9 @@ typedef struct OrScene {
   const OrInstance *instances;
   int32_t numLights;
   const OrLight *lights;
+  int32_t numSpheres;
+  const float *spheres;          /* center, radius (object space) */
+  const uint32_t *sphereSurface; /* surface index per sphere */
 } OrScene;
 
 typedef struct OrCamera {

@@ -98,7 +98,13 @@ def test_batch_gradient_shading(pkg, device):
     def shaded(s):
         return dict(s, renderer=dict(s["renderer"], gradientShading=True))
 
-    scenes = [shaded(base[0]), shaded(base[1]), shaded(base[3]), base[0]]
+    # and a frame of each renderer over sphere geometry (full variants too)
+    rng = np.random.default_rng(5)
+    balls = {"geometry": "sphere", "vertices": rng.uniform(-10.0, 10.0, (24, 3)).astype(np.float32),
+             "radii": rng.uniform(1.0, 4.0, 24).astype(np.float32),
+             "material": {"type": "matte", "color": [0.7, 0.6, 0.5]}}
+    with_balls = [dict(base[k], surfaces=list(base[k]["surfaces"]) + [balls]) for k in (0, 3)]
+    scenes = [shaded(base[0]), shaded(base[1]), shaded(base[3]), base[0]] + with_balls
     single = [pkg.scenes.build(dev, s, channels=CHANNELS) for s in scenes]
     batch = [pkg.scenes.build(dev, s, channels=CHANNELS) for s in scenes]
     frames = [h["frame"] for h in batch]

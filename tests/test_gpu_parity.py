@@ -458,6 +458,72 @@ def test_volume_pathtrace_point_light_gradient_shading(pkg, device, oracle):
     assert float((d <= 1e-3).mean()) >= 0.95, float((d <= 1e-3).mean())
 
 
+def sphere_surfaces(base, n=40, seed=3):
+    """Two sphere geometries over the sphere-set volume: one with per-sphere
+    radii, one placed through primitive.index; the materials of the first
+    two surfaces of `base`."""
+    rng = np.random.default_rng(seed)
+    centres = rng.uniform(-10.0, 10.0, (n, 3)).astype(np.float32)
+    radii = rng.uniform(0.3, 1.5, n).astype(np.float32)
+    h = n // 2
+    return [{"geometry": "sphere", "vertices": centres[:h], "radii": radii[:h],
+             "material": base["surfaces"][0]["material"]},
+            {"geometry": "sphere", "vertices": centres, "indices": np.arange(h, n, dtype=np.uint32),
+             "radii": radii[h:], "material": base["surfaces"][1]["material"]}]
+
+
+def test_raycast_spheres(pkg, device, oracle):
+    """Sphere geometry (their own BVH per group, the smaller root of the
+    quadratic, normal (P - c) / r) beside triangle meshes, raycast."""
+    sc = small_spheres(pkg, res=128, renderer="raycast")
+    sc["surfaces"] = sc["surfaces"] + sphere_surfaces(sc)
+    sc["lights"] = sc["lights"] + point_and_spot_lights()[:1]
+    gpu = render_gpu(pkg, device, sc)
+    _, F = render_oracle(oracle, sc)
+    assert gpu["errorFlags"] == 0
+    good, frac = raycast_ok(gpu, F)
+    assert good, frac
+    hit = (F.depth < 1e30) & (gpu["depth"] < 1e30)
+    rel = np.abs(gpu["depth"][hit] - F.depth[hit]) / F.depth[hit]
+    assert float((rel <= 1e-4).mean()) >= 0.999
+    nd = np.abs(gpu["normal"] - F.normal).max(axis=-1)
+    assert float((nd <= 1e-3).mean()) >= 0.999
+    # the spheres are in view: the image differs from the one without them
+    _, P = render_oracle(oracle, dict(sc, surfaces=sc["surfaces"][:-2]))
+    assert float((np.abs(F.color - P.color).max(axis=-1) > 1e-3).mean()) > 0.02
+
+
+@pytest.mark.parametrize("wavefront", [True, False])
+def test_pathtrace_spheres_same_stream(pkg, device, oracle, wavefront):
+    """Path tracing over spheres and triangles with the same stream as the
+    oracle (a wavefront renderer hands worlds with spheres to the
+    megakernel)."""
+    sc = small_spheres(pkg, res=96, spp=8)
+    sc["surfaces"] = sc["surfaces"] + sphere_surfaces(sc)
+    sc["renderer"]["wavefront"] = wavefront
+    gpu = render_gpu(pkg, device, sc)
+    _, F = render_oracle(oracle, sc)
+    assert gpu["errorFlags"] == 0
+    assert not np.isnan(gpu["color"]).any()
+    d = np.abs(gpu["color"][..., :3] - F.color[..., :3]).max(axis=-1)
+    assert float((d <= 1e-3).mean()) >= 0.97, float((d <= 1e-3).mean())
+
+
+def test_instanced_spheres(pkg, device, oracle):
+    """A sphere-only group placed by an instance transform (rotation, scale,
+    translation), next to world-level triangles."""
+    base = small_spheres(pkg, res=96, renderer="raycast", n=10)
+    c, s = np.cos(0.4), np.sin(0.4)
+    xfm = [c * 1.2, 0.0, -s * 1.2, 0.0, 1.2, 0.0, s * 1.2, 0.0, c * 1.2, 1.0, -0.5, 2.0]
+    sc = dict(base)
+    sc["instances"] = [{"transform": xfm, "surfaces": sphere_surfaces(base, n=16)}]
+    gpu = render_gpu(pkg, device, sc)
+    _, F = render_oracle(oracle, sc)
+    assert gpu["errorFlags"] == 0
+    good, frac = raycast_ok(gpu, F)
+    assert good, frac
+
+
 def test_wavefront_equals_megakernel(pkg, device):
     """The two execution modes produce the same frame (same stream, same math)."""
     sc = small_spheres(pkg, res=96, spp=4, n=16)

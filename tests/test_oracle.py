@@ -158,6 +158,41 @@ def test_point_and_spot_lights_closed_form(oracle, kind):
     assert np.allclose(F.color[..., :3], expect, rtol=1e-4, atol=1e-5)
 
 
+def test_sphere_closed_form(oracle):
+    """Raycast of a matte sphere (centre (0.5, -0.25, 0), radius 2, placed
+    through primitive.index with a per-sphere radius) seen from above by an
+    orthographic camera under a directional light: each covered pixel is
+    c/pi E max(0, n.L) + c ambient with n the analytic sphere normal at the
+    pixel; the rest is background."""
+    centre, r = np.array([0.5, -0.25, 0.0]), 2.0
+    sc = plane_scene()
+    sc["surfaces"] = [{"geometry": "sphere",
+                       "vertices": np.array([[9.0, 9.0, 9.0], centre], np.float32),
+                       "indices": np.array([1], np.uint32), "radii": np.array([r], np.float32),
+                       "material": {"type": "matte", "color": [0.6, 0.5, 0.4]}}]
+    sc["camera"] = {"type": "orthographic", "position": [0.0, 0.0, 10.0],
+                    "direction": [0.0, 0.0, -1.0], "up": [0.0, 1.0, 0.0], "height": 6.0,
+                    "aspect": 1.0}
+    S = oracle.Scene(sc)
+    F = oracle.Frame(24, 24)
+    oracle.render(S, F)
+    xs = ((np.arange(24) + 0.5) / 24 - 0.5) * 6.0
+    X, Y = np.meshgrid(xs, xs)
+    dx, dy = X - centre[0], Y - centre[1]
+    q = r * r - dx * dx - dy * dy
+    inside, outside = q > 1e-3, q < -1e-3
+    n = np.stack([dx, dy, np.sqrt(np.maximum(q, 0.0))], axis=-1) / r
+    L = -np.array([0.0, -0.6, -0.8])
+    L /= np.linalg.norm(L)
+    c = np.array([0.6, 0.5, 0.4])
+    expect = c / math.pi * 2.0 * np.maximum(0.0, n @ L)[..., None] + c * 0.2
+    assert inside.sum() > 100 and outside.sum() > 50
+    assert np.allclose(F.color[inside][:, :3], expect[inside], atol=2e-5)
+    assert np.all(F.color[outside][:, :3] == 0.0)
+    assert np.allclose(F.depth[inside], 10.0 - np.sqrt(q[inside]), rtol=1e-4)
+    assert np.allclose(F.normal[inside], n[inside], atol=1e-4)
+
+
 def test_emission_absorption_slab(oracle):
     """Constant field, TF alpha a: alpha after k steps is 1 - (1-a)^(k dt/ud)."""
     n = 16

@@ -105,27 +105,31 @@ cleanup:
   return err;
 }
 
-// Sphere leaves: the builder ran over each sphere's bounding triangle and
-// wrote the leaf-ordered triangles with the group index in the first
-// float4's w; the sphere records follow that order.
-__global__ void kGatherSpheres(const float4 *leafTris, const float4 *src, int n,
-                               float4 *spheresOut, uint32_t *localOut) {
+// Analytic-primitive leaves: the builder ran over each primitive's
+// bounding triangle and wrote the leaf-ordered triangles with the group
+// index in the first float4's w; the primitive records follow that order.
+__global__ void kGatherAnalytic(const float4 *leafTris, const float4 *src, const uint32_t *kinds,
+                                int n, float4 *primsOut, uint32_t *localOut) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const int k = __float_as_int(leafTris[3 * (size_t)i].w);
-  if (k < 0 || k >= n) {  // not a valid group index: an empty sphere
-    spheresOut[i] = make_float4(__int_as_float(0x7fffffff), 0.f, 0.f, 0.f);  // NaN: never hit
+  if (k < 0 || k >= n) {  // not a valid group index: a sphere that is never hit
+    primsOut[2 * (size_t)i] = make_float4(__int_as_float(0x7fffffff), 0.f, 0.f, 0.f);
+    primsOut[2 * (size_t)i + 1] = make_float4(0.f, 0.f, 0.f, 0.f);
     localOut[i] = 0;
     return;
   }
-  spheresOut[i] = src[k];
-  localOut[i] = (uint32_t)k;
+  primsOut[2 * (size_t)i] = src[2 * (size_t)k];
+  primsOut[2 * (size_t)i + 1] = src[2 * (size_t)k + 1];
+  localOut[i] = (uint32_t)k | (kinds[k] << kApKindShift);
 }
 
-cudaError_t launchGatherSpheres(const float4 *leafTris, const float4 *src, int n,
-                                float4 *spheresOut, uint32_t *localOut, cudaStream_t stream) {
+cudaError_t launchGatherAnalytic(const float4 *leafTris, const float4 *src, const uint32_t *kinds,
+                                 int n, float4 *primsOut, uint32_t *localOut,
+                                 cudaStream_t stream) {
   if (n <= 0) return cudaSuccess;
-  kGatherSpheres<<<(n + 255) / 256, 256, 0, stream>>>(leafTris, src, n, spheresOut, localOut);
+  kGatherAnalytic<<<(n + 255) / 256, 256, 0, stream>>>(leafTris, src, kinds, n, primsOut,
+                                                       localOut);
   return cudaGetLastError();
 }
 

@@ -213,18 +213,99 @@ __device__ __forceinline__ void localRay(const DInstance &I, float3 o, float3 d,
 // DeviceCopyableObjects.h:1486-1507): the two roots of
 // |o + t d - c|^2 = r^2 from the cancellation-free quadratic formula, the
 // smaller one returned (a ray starting inside the sphere reports the
-// negative root and so misses it).
+// negative root and so misses it). Misses return -FLT_MAX.
 __device__ __forceinline__ float sphereHitT(float3 o, float3 d, float4 sph) {
   const float3 oc = o - f3(sph.x, sph.y, sph.z);
   const float A = dot(d, d);
   const float B = 2.f * dot(d, oc);
   const float C = dot(oc, oc) - sph.w * sph.w;
   const float disc = B * B - 4.f * A * C;
-  if (!(disc >= 0.f)) return -1.f;
+  if (!(disc >= 0.f)) return -FLT_MAX;
   const float rd = sqrtf(disc);
   const float q = B < 0.f ? -0.5f * (B - rd) : -0.5f * (B + rd);
   const float t1 = q / A, t2 = C / q;
   return t1 > t2 ? t2 : t1;
+}
+
+// Capped cone from (v1, r1) to (v2, r2), intersect(Ray, Cone),
+// DeviceCopyableObjects.h:933-1007 (after Quilez's cone intersector): the
+// cap discs first (the one the origin lies behind), then the body as the
+// smaller root of the quadratic; u = 0 / 1 on the caps and y / |v2-v1|^2 on
+// the body, v = y (the unnormalised axis parameter the normal needs).
+__device__ __forceinline__ float coneHitT(float3 ro, float3 rd, float4 A, float4 B, float &u,
+                                          float &v) {
+  const float3 pa = f3(A.x, A.y, A.z), pb = f3(B.x, B.y, B.z);
+  const float ra = A.w, rb = B.w;
+  const float3 ba = pb - pa, oa = ro - pa, ob = ro - pb;
+  const float m0 = dot(ba, ba), m1 = dot(oa, ba), m2 = dot(rd, ba);
+  const float m3 = dot(rd, oa), m5 = dot(oa, oa), m9 = dot(ob, ba);
+  if (m1 < 0.f) {
+    const float3 w = oa * m2 - rd * m1;
+    if (dot(w, w) < ra * ra * m2 * m2) {
+      u = 0.f;
+      v = 0.f;
+      return -m1 / m2;
+    }
+  } else if (m9 > 0.f) {
+    const float t = -m9 / m2;
+    const float3 w = ob + rd * t;
+    if (dot(w, w) < rb * rb) {
+      u = 1.f;
+      v = 0.f;
+      return t;
+    }
+  }
+  const float rr = ra - rb;
+  const float hy = m0 + rr * rr;
+  const float k2 = m0 * m0 - m2 * m2 * hy;
+  const float k1 = m0 * m0 * m3 - m1 * m2 * hy + m0 * ra * (rr * m2 * 1.f);
+  const float k0 = m0 * m0 * m5 - m1 * m1 * hy + m0 * ra * (rr * m1 * 2.f - m0 * ra);
+  const float h = k1 * k1 - k2 * k0;
+  if (h < 0.f) return -FLT_MAX;
+  const float t = (-k1 - sqrtf(h)) / k2;
+  const float y = m1 + t * m2;
+  if (y > 0.f && y < m0) {
+    u = y / m0;
+    v = y;
+    return t;
+  }
+  return -FLT_MAX;
+}
+
+// Capped cylinder from v1 to v2 of radius r (Visionaray's basic_cylinder
+// test is not part of the reference; this is Quilez's published capped-
+// cylinder intersector): the body as the smaller root of the quadratic in
+// the plane normal to the axis, else the cap plane the body root falls
+// beyond, accepted inside the radius.
+__device__ __forceinline__ float cylinderHitT(float3 ro, float3 rd, float4 A, float4 B) {
+  const float3 pa = f3(A.x, A.y, A.z), pb = f3(B.x, B.y, B.z);
+  const float ra = A.w;
+  const float3 ba = pb - pa, oc = ro - pa;
+  const float baba = dot(ba, ba), bard = dot(ba, rd), baoc = dot(ba, oc);
+  const float k2 = baba - bard * bard;
+  const float k1 = baba * dot(oc, rd) - baoc * bard;
+  const float k0 = baba * dot(oc, oc) - baoc * baoc - ra * ra * baba;
+  float h = k1 * k1 - k2 * k0;
+  if (h < 0.f) return -FLT_MAX;
+  h = sqrtf(h);
+  float t = (-k1 - h) / k2;
+  const float y = baoc + t * bard;
+  if (y > 0.f && y < baba) return t;
+  t = ((y < 0.f ? 0.f : baba) - baoc) / bard;
+  if (fabsf(k1 + k2 * t) < h) return t;
+  return -FLT_MAX;
+}
+
+// One analytic-primitive leaf: its hit parameter (-FLT_MAX on a miss) and
+// the (u, v) the normal needs.
+__device__ __forceinline__ float analyticHitT(const DGroup &G, int leaf, uint32_t kind, float3 o,
+                                              float3 d, float &u, float &v) {
+  const float4 A = __ldg(G.apPrims + 2 * (size_t)leaf);
+  u = 0.f;
+  v = 0.f;
+  if (kind == AP_SPHERE) return sphereHitT(o, d, A);
+  const float4 B = __ldg(G.apPrims + 2 * (size_t)leaf + 1);
+  return kind == AP_CONE ? coneHitT(o, d, A, B, u, v) : cylinderHitT(o, d, A, B);
 }
 
 // Stack-based BVH2 traversal, near child first, in the while-while form
@@ -233,8 +314,8 @@ __device__ __forceinline__ float sphereHitT(float3 o, float3 d, float4 sph) {
 // first accepted hit), so shadow/AO rays and radiance rays in one warp share
 // the same instructions. Closest hits are ordered by (t, instance, triangle),
 // the order the CPU restatement uses, so any valid BVH gives the same hit.
-// Spheres = true walks the group's sphere BVH with sphere leaves.
-template <bool Count, bool Spheres = false>
+// Analytic = true walks the group's BVH of spheres, cones and cylinders.
+template <bool Count, bool Analytic = false>
 __device__ __forceinline__ bool traverseGroup(const DGroup &G, float3 o, float3 d, float tmin,
                                               int inst, bool anyHit, Hit &best, uint32_t &err,
                                               unsigned long long *cnt) {
@@ -248,7 +329,7 @@ __device__ __forceinline__ bool traverseGroup(const DGroup &G, float3 o, float3 
   while (!done) {
     // inner nodes until a leaf comes up or nothing is left
     while (node >= 0) {
-      const float4 *N = (Spheres ? G.sphNodes : G.nodes) + 4 * (size_t)node;
+      const float4 *N = (Analytic ? G.apNodes : G.nodes) + 4 * (size_t)node;
       const float4 n0 = __ldg(N), n1 = __ldg(N + 1), n2 = __ldg(N + 2);
       const int4 n3 = __ldg(reinterpret_cast<const int4 *>(N + 3));
       if (Count) ++nodeVisits;
@@ -287,16 +368,18 @@ __device__ __forceinline__ bool traverseGroup(const DGroup &G, float3 o, float3 
       const int first = (int)(code & kLeafFirstMask);
       const int count = (int)(code >> kLeafCountShift) + 1;
       for (int k = 0; k < count; ++k) {
-        if constexpr (Spheres) {
+        if constexpr (Analytic) {
           if (Count) ++triTests;
-          const float t = sphereHitT(o, d, __ldg(G.spheres + first + k));
+          const uint32_t lk = __ldg(G.apLocal + first + k);
+          float u, v;
+          const float t = analyticHitT(G, first + k, lk >> kApKindShift, o, d, u, v);
           if (!(t >= tmin)) continue;
-          const int local = G.numTris + (int)__ldg(G.sphLocal + first + k);
+          const int local = G.numTris + (int)(lk & kApLocalMask);
           const bool closer =
               t < best.t || (t == best.t && best.inst >= 0 &&
                              (inst < best.inst || (inst == best.inst && local < best.tri)));
           if (!closer) continue;
-          best.t = t; best.u = 0.f; best.v = 0.f; best.inst = inst; best.tri = local;
+          best.t = t; best.u = u; best.v = v; best.inst = inst; best.tri = local;
           best.leaf = first + k;
           found = true;
           continue;
@@ -484,7 +567,7 @@ __device__ __forceinline__ bool traceSurfaces(const DScene &S, const Ray &r, boo
     if (!Full || G.numNodes > 0)
       f = G.width == 4 ? traverseGroup4<Count>(G, lo, ld, r.tmin, i, anyHit, h, err, cnt)
                        : traverseGroup<Count>(G, lo, ld, r.tmin, i, anyHit, h, err, cnt);
-    if (Full && G.sphNumNodes > 0 && !(anyHit && f))
+    if (Full && G.apNumNodes > 0 && !(anyHit && f))
       f = traverseGroup<Count, true>(G, lo, ld, r.tmin, i, anyHit, h, err, cnt) || f;
     if (f) {
       any = true;
@@ -495,24 +578,47 @@ __device__ __forceinline__ bool traceSurfaces(const DScene &S, const Ray &r, boo
   return any;
 }
 
-// Surface index of a hit (a triangle's, or with Full a sphere's).
+// Surface index of a hit (a triangle's, or with Full an analytic
+// primitive's).
 template <bool Full>
 __device__ __forceinline__ uint32_t hitSurface(const DGroup &G, const Hit &h) {
-  if (Full && h.tri >= G.numTris) return __ldg(G.sphSurface + (h.tri - G.numTris));
+  if (Full && h.tri >= G.numTris) return __ldg(G.apSurface + (h.tri - G.numTris));
   return __ldg(G.triSurface + h.tri);
 }
 
-// Object-space geometric normal of a hit, getNormals (renderer/common.h:
-// 241-275): normalize(e1 x e2) for a triangle, normalize((P - c) / r) at
-// the instance-local hit position P for a sphere.
+// Object-space geometric normal of a hit at the instance-local hit position
+// P, getNormals (renderer/common.h:241-303): normalize(e1 x e2) for a
+// triangle; normalize((P - c) / r) for a sphere; for a cone the cap axis
+// (u <= 0, u >= 1) or the body normal from the axis parameter v; for a
+// cylinder the cap axis within the radius of an end point, else P minus
+// its projection on the axis.
 template <bool Full>
 __device__ __forceinline__ float3 hitNormal(const DGroup &G, const DInstance &I, const Hit &h,
                                             float3 o, float3 d) {
   if (Full && h.tri >= G.numTris) {
-    const float4 sp = __ldg(G.spheres + h.leaf);
     float3 lo, ld;
     localRay(I, o, d, lo, ld);
-    return normalize((lo + h.t * ld - f3(sp.x, sp.y, sp.z)) / sp.w);
+    const float3 P = lo + h.t * ld;
+    const uint32_t kind = __ldg(G.apLocal + h.leaf) >> kApKindShift;
+    const float4 A = __ldg(G.apPrims + 2 * (size_t)h.leaf);
+    const float3 v1 = f3(A.x, A.y, A.z);
+    if (kind == AP_SPHERE) return normalize((P - v1) / A.w);
+    const float4 B = __ldg(G.apPrims + 2 * (size_t)h.leaf + 1);
+    const float3 v2 = f3(B.x, B.y, B.z);
+    if (kind == AP_CONE) {
+      const float3 ba = v2 - v1;
+      const float m0 = dot(ba, ba);
+      if (h.u <= 0.f) return -ba * (1.f / sqrtf(m0));
+      if (h.u >= 1.f) return ba * (1.f / sqrtf(m0));
+      const float ra = A.w, rr = A.w - B.w;
+      const float hy = m0 + rr * rr;
+      return normalize(m0 * (m0 * (P - v1) + rr * ba * ra) - ba * hy * h.v);
+    }
+    const float3 axis = normalize(v2 - v1);
+    if (length(P - v1) < A.w) return -axis;
+    if (length(P - v2) < A.w) return axis;
+    const float s = dot(P - v1, axis);
+    return normalize(P - (v1 + s * axis));
   }
   const float4 *E = G.tris + 3 * (size_t)h.leaf;
   const float4 e1 = __ldg(E + 1), e2 = __ldg(E + 2);

@@ -424,14 +424,21 @@ struct Volume : Object {
 // triangle geometry, scene/surface/geometry/Triangle.cpp:46-133
 struct Geometry : Object {
   std::vector<float> v1, e1, e2;  // per triangle, float3 packed
-  std::vector<float> spheres;     // per sphere: center, radius
+  // spheres, cones, cylinders: 8 floats per primitive, (p0, r0, p1, r1)
+  // (a sphere uses (center, radius) and zeros), all of kind apKind
+  std::vector<float> prims;
+  int apKind = AP_SPHERE;
   using Object::Object;
   void commit() override {
     valid = false;
     v1.clear(); e1.clear(); e2.clear();
-    spheres.clear();
+    prims.clear();
     if (subtype == "sphere") {
       commitSpheres();
+      return;
+    }
+    if (subtype == "cone" || subtype == "cylinder") {
+      commitConesCylinders(subtype == "cone");
       return;
     }
     Array *pos = geto<Array>("vertex.position", VSR_ARRAY1D);
@@ -475,6 +482,7 @@ struct Geometry : Object {
   // when given), radius from vertex.radius indexed by the sphere (not by the
   // vertex), else the global 'radius' (default 0.01)
   void commitSpheres() {
+    apKind = AP_SPHERE;
     Array *pos = geto<Array>("vertex.position", VSR_ARRAY1D);
     Array *idx = geto<Array>("primitive.index", VSR_ARRAY1D);
     Array *rad = geto<Array>("vertex.radius", VSR_ARRAY1D);
@@ -499,21 +507,74 @@ struct Geometry : Object {
       warn("'vertex.radius' shorter than the number of spheres");
       return;
     }
-    spheres.resize(4 * n);
+    prims.assign(8 * n, 0.f);
     for (size_t i = 0; i < n; ++i) {
       const size_t v = idx ? idx->as<uint32_t>()[i] : i;
       if (v >= nv) {
         warn("'primitive.index' out of range on sphere geometry");
-        spheres.clear();
+        prims.clear();
         return;
       }
-      for (int k = 0; k < 3; ++k) spheres[4 * i + k] = P[3 * v + k];
-      spheres[4 * i + 3] = rad ? rad->as<float>()[i] : globalRadius;
+      for (int k = 0; k < 3; ++k) prims[8 * i + k] = P[3 * v + k];
+      prims[8 * i + 3] = rad ? rad->as<float>()[i] : globalRadius;
+    }
+    valid = true;
+  }
+
+  // Cone.cpp:31-82 and Cylinder.cpp:31-82: end points from vertex.position
+  // pairs (primitive.index as UINT32_VEC2, else consecutive vertices). A
+  // cone's radii are vertex.radius at the two end vertices (required); a
+  // cylinder's is primitive.radius indexed by the cylinder, else the global
+  // 'radius' (default 1).
+  void commitConesCylinders(bool cone) {
+    apKind = cone ? AP_CONE : AP_CYLINDER;
+    const char *what = cone ? "cone" : "cylinder";
+    Array *pos = geto<Array>("vertex.position", VSR_ARRAY1D);
+    Array *idx = geto<Array>("primitive.index", VSR_ARRAY1D);
+    Array *rad = geto<Array>(cone ? "vertex.radius" : "primitive.radius", VSR_ARRAY1D);
+    if (!pos || pos->elemType != VSR_FLOAT32_VEC3) {
+      warn("missing required parameter 'vertex.position' on %s geometry", what);
+      return;
+    }
+    if (cone && !rad) {
+      warn("missing required parameter 'vertex.radius' on cone geometry");
+      return;
+    }
+    if (idx && idx->elemType != VSR_UINT32_VEC2) {
+      warn("unsupported type for 'primitive.index' on %s geometry", what);
+      return;
+    }
+    if (rad && rad->elemType != VSR_FLOAT32) {
+      warn("unsupported type for the radius array on %s geometry", what);
+      return;
+    }
+    float globalRadius = 1.f;
+    if (!cone) getf("radius", globalRadius);
+    const float *P = pos->as<float>();
+    const size_t nv = pos->size();
+    const size_t n = idx ? idx->size() : nv / 2;
+    const size_t nr = rad ? rad->size() : 0;
+    prims.assign(8 * n, 0.f);
+    for (size_t i = 0; i < n; ++i) {
+      const size_t a = idx ? idx->as<uint32_t>()[2 * i] : 2 * i;
+      const size_t b = idx ? idx->as<uint32_t>()[2 * i + 1] : 2 * i + 1;
+      const size_t ra = cone ? a : i, rb = cone ? b : i;
+      if (a >= nv || b >= nv || (rad && (ra >= nr || rb >= nr))) {
+        warn("'primitive.index' or the radius array out of range on %s geometry", what);
+        prims.clear();
+        return;
+      }
+      for (int k = 0; k < 3; ++k) {
+        prims[8 * i + k] = P[3 * a + k];
+        prims[8 * i + 4 + k] = P[3 * b + k];
+      }
+      prims[8 * i + 3] = rad ? rad->as<float>()[ra] : globalRadius;
+      prims[8 * i + 7] = rad ? rad->as<float>()[rb] : globalRadius;
     }
     valid = true;
   }
   size_t numTris() const { return v1.size() / 3; }
-  size_t numSpheres() const { return spheres.size() / 4; }
+  size_t numAnalytic() const { return prims.size() / 8; }
 };
 
 // matte / physicallyBased, scene/surface/material/{Matte,PBM}.cpp
@@ -847,9 +908,9 @@ struct Renderer : Object {
 // ----------------------------------------------------------------- world
 struct GroupGPU {
   DevBuf v1, e1, e2, nodes, nodes4, tris, triSurface, triPrim;
-  DevBuf sphSrc, sphNodes, sphLeaf, spheres, sphLocal, sphSurface;
+  DevBuf apSrc, apKinds, apNodes, apLeaf, apPrims, apLocal, apSurface;
   int numTris = 0, numNodes = 0, width = 2;
-  int numSpheres = 0, sphNumNodes = 0;
+  int numAP = 0, apNumNodes = 0;
   float buildMs = 0.f;
 };
 
@@ -902,52 +963,62 @@ struct World : Object {
     valid = true;
   }
 
-  // The group's spheres get their own BVH2 from the triangle builder: each
-  // sphere enters as a triangle spanning its bounding box (v1 = c - r,
-  // v1 + e1 = c + r, v1 + e2 another box corner), then a gather puts the
-  // spheres and their group indices in leaf order.
-  bool buildSpheres(GroupGPU &gg, const std::vector<float> &sph,
-                    const std::vector<uint32_t> &sphSurf, cudaStream_t s) {
-    const int ns = (int)sphSurf.size();
-    std::vector<float> v1(3 * ns), e1(3 * ns), e2(3 * ns);
-    for (int k = 0; k < ns; ++k) {
-      const float r = sph[4 * k + 3];
+  // The group's spheres, cones and cylinders get their own BVH2 from the
+  // triangle builder: each enters as a triangle spanning its bounding box
+  // (get_bounds, DeviceCopyableObjects.h:1009-1018: the end points grown by
+  // their radii), then a gather puts the primitives, their group indices
+  // and kinds in leaf order.
+  bool buildAnalytic(GroupGPU &gg, const std::vector<float> &prims,
+                     const std::vector<uint32_t> &kinds, const std::vector<uint32_t> &surf,
+                     cudaStream_t s) {
+    const int n = (int)surf.size();
+    std::vector<float> v1(3 * n), e1(3 * n), e2(3 * n);
+    for (int k = 0; k < n; ++k) {
+      const float *q = &prims[8 * k];
       for (int a = 0; a < 3; ++a) {
-        v1[3 * k + a] = sph[4 * k + a] - r;
-        e1[3 * k + a] = 2.f * r;
-        e2[3 * k + a] = a == 1 ? 0.f : 2.f * r;
+        float lo = q[a] - q[3], hi = q[a] + q[3];
+        if (kinds[k] != AP_SPHERE) {
+          lo = std::min(lo, q[4 + a] - q[7]);
+          hi = std::max(hi, q[4 + a] + q[7]);
+        }
+        v1[3 * k + a] = lo;
+        e1[3 * k + a] = hi - lo;
+        e2[3 * k + a] = a == 1 ? 0.f : hi - lo;
       }
     }
-    const size_t fb = (size_t)ns * 3 * sizeof(float);
+    const size_t fb = (size_t)n * 3 * sizeof(float);
     DevBuf bv1, be1, be2;
     if (bv1.upload(v1.data(), fb, s) || be1.upload(e1.data(), fb, s) ||
         be2.upload(e2.data(), fb, s) ||
-        gg.sphSrc.upload(sph.data(), (size_t)ns * sizeof(float4), s) ||
-        gg.sphSurface.upload(sphSurf.data(), (size_t)ns * sizeof(uint32_t), s) ||
-        gg.sphNodes.alloc((size_t)std::max(ns - 1, 1) * 4 * sizeof(float4)) ||
-        gg.sphLeaf.alloc((size_t)ns * 3 * sizeof(float4)) ||
-        gg.spheres.alloc((size_t)ns * sizeof(float4)) ||
-        gg.sphLocal.alloc((size_t)ns * sizeof(uint32_t))) {
+        gg.apSrc.upload(prims.data(), (size_t)n * 2 * sizeof(float4), s) ||
+        gg.apKinds.upload(kinds.data(), (size_t)n * sizeof(uint32_t), s) ||
+        gg.apSurface.upload(surf.data(), (size_t)n * sizeof(uint32_t), s) ||
+        gg.apNodes.alloc((size_t)std::max(n - 1, 1) * 4 * sizeof(float4)) ||
+        gg.apLeaf.alloc((size_t)n * 3 * sizeof(float4)) ||
+        gg.apPrims.alloc((size_t)n * 2 * sizeof(float4)) ||
+        gg.apLocal.alloc((size_t)n * sizeof(uint32_t))) {
       dev->report(this, kind, VSR_SEVERITY_ERROR, VSR_ERROR_OUT_OF_MEMORY, "scene upload failed");
       return false;
     }
     BvhBuildStats st{};
     auto build = fastBuild ? buildGroupBVH : buildGroupBVHQuality;
-    cudaError_t e = build(bv1.as<float>(), be1.as<float>(), be2.as<float>(), ns,
-                          gg.sphNodes.as<float4>(), gg.sphLeaf.as<float4>(), &st, s);
+    cudaError_t e = build(bv1.as<float>(), be1.as<float>(), be2.as<float>(), n,
+                          gg.apNodes.as<float4>(), gg.apLeaf.as<float4>(), &st, s);
     if (e == cudaSuccess)
-      e = launchGatherSpheres(gg.sphLeaf.as<float4>(), gg.sphSrc.as<float4>(), ns,
-                              gg.spheres.as<float4>(), gg.sphLocal.as<uint32_t>(), s);
+      e = launchGatherAnalytic(gg.apLeaf.as<float4>(), gg.apSrc.as<float4>(),
+                               gg.apKinds.as<uint32_t>(), n, gg.apPrims.as<float4>(),
+                               gg.apLocal.as<uint32_t>(), s);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
     if (e != cudaSuccess) {
-      dev->report(this, kind, VSR_SEVERITY_ERROR, VSR_ERROR_CUDA, "sphere BVH build failed: %s",
-                  cudaGetErrorString(e));
+      dev->report(this, kind, VSR_SEVERITY_ERROR, VSR_ERROR_CUDA,
+                  "sphere / cone / cylinder BVH build failed: %s", cudaGetErrorString(e));
       return false;
     }
-    gg.sphLeaf.release();
-    gg.sphSrc.release();
-    gg.numSpheres = ns;
-    gg.sphNumNodes = st.numNodes;
+    gg.apLeaf.release();
+    gg.apSrc.release();
+    gg.apKinds.release();
+    gg.numAP = n;
+    gg.apNumNodes = st.numNodes;
     gg.buildMs += st.buildMs;
     bvhNodes += (uint64_t)st.numNodes;
     return true;
@@ -980,14 +1051,14 @@ struct World : Object {
     groupsGPU.clear();
     bvhNodes = bvhTris = 0;
     bool allOpaque = true, anySurf = false;
-    int numSpheres = 0;
+    int numAnalytic = 0;
     for (size_t gi = 0; gi < groups.size(); ++gi) {
       Group *g = groups[gi];
       auto gg = std::make_unique<GroupGPU>();
       std::vector<float> v1, e1, e2;
       std::vector<uint32_t> triSurf, triPrim;
-      std::vector<float> sph;
-      std::vector<uint32_t> sphSurf;
+      std::vector<float> apPrims;
+      std::vector<uint32_t> apKinds, apSurf;
       float lo[3] = {1e30f, 1e30f, 1e30f}, hi[3] = {-1e30f, -1e30f, -1e30f};
       for (Surface *sf : g->surfaces) {
         if (!sf->valid || !sf->geom->valid || !sf->mat->valid) continue;
@@ -995,14 +1066,19 @@ struct World : Object {
         mats.push_back(sf->mat->m);
         if (sf->mat->m.alphaMode != ALPHA_OPAQUE) allOpaque = false;
         Geometry *G = sf->geom;
-        if (G->numSpheres()) {
-          sph.insert(sph.end(), G->spheres.begin(), G->spheres.end());
-          for (size_t k = 0; k < G->numSpheres(); ++k) {
-            sphSurf.push_back(sid);
+        if (G->numAnalytic()) {
+          apPrims.insert(apPrims.end(), G->prims.begin(), G->prims.end());
+          for (size_t k = 0; k < G->numAnalytic(); ++k) {
+            apSurf.push_back(sid);
+            apKinds.push_back((uint32_t)G->apKind);
+            const float *q = &G->prims[8 * k];
             for (int a = 0; a < 3; ++a) {
-              const float c = G->spheres[4 * k + a], r = G->spheres[4 * k + 3];
-              lo[a] = std::min(lo[a], c - r);
-              hi[a] = std::max(hi[a], c + r);
+              lo[a] = std::min(lo[a], q[a] - q[3]);
+              hi[a] = std::max(hi[a], q[a] + q[3]);
+              if (G->apKind != AP_SPHERE) {
+                lo[a] = std::min(lo[a], q[4 + a] - q[7]);
+                hi[a] = std::max(hi[a], q[4 + a] + q[7]);
+              }
             }
           }
           continue;
@@ -1086,21 +1162,21 @@ struct World : Object {
         bvhNodes += (uint64_t)st.numNodes;
         bvhTris += (uint64_t)nt;
       }
-      const int ns = (int)sphSurf.size();
-      if (ns >= (1 << 27)) {
+      const int na = (int)apSurf.size();
+      if (na >= (1 << kApKindShift)) {
         dev->report(this, kind, VSR_SEVERITY_ERROR, VSR_ERROR_INVALID_ARGUMENT,
-                    "group has more than 2^27 spheres");
+                    "group has more than 2^28 spheres, cones and cylinders");
         return false;
       }
-      if (ns > 0 && !buildSpheres(*gg, sph, sphSurf, s)) return false;
-      if (ns > 0) anySurf = true;
-      dg.sphNodes = gg->sphNodes.as<float4>();
-      dg.spheres = gg->spheres.as<float4>();
-      dg.sphLocal = gg->sphLocal.as<uint32_t>();
-      dg.sphSurface = gg->sphSurface.as<uint32_t>();
-      dg.numSpheres = gg->numSpheres;
-      dg.sphNumNodes = gg->sphNumNodes;
-      numSpheres += ns;
+      if (na > 0 && !buildAnalytic(*gg, apPrims, apKinds, apSurf, s)) return false;
+      if (na > 0) anySurf = true;
+      dg.apNodes = gg->apNodes.as<float4>();
+      dg.apPrims = gg->apPrims.as<float4>();
+      dg.apLocal = gg->apLocal.as<uint32_t>();
+      dg.apSurface = gg->apSurface.as<uint32_t>();
+      dg.numAP = gg->numAP;
+      dg.apNumNodes = gg->apNumNodes;
+      numAnalytic += na;
       dg.nodes = gg->nodes.as<float4>();
       dg.tris = gg->tris.as<float4>();
       dg.triSurface = gg->triSurface.as<uint32_t>();
@@ -1205,7 +1281,7 @@ struct World : Object {
     scene.numVolumes = (int)vols.size();
     scene.allOpaque = allOpaque ? 1 : 0;
     scene.hasSurfaces = anySurf ? 1 : 0;
-    scene.numSpheres = numSpheres;
+    scene.numAnalytic = numAnalytic;
     builtStamp = deep;
     commitMs = std::chrono::duration<float, std::milli>(std::chrono::steady_clock::now() - t0).count();
     return true;
@@ -1431,9 +1507,10 @@ VSRStatus renderFrame(Device *dev, FrameObj *F) {
   }
   const bool doRender = F->accumID < F->renderer->sampleLimit;
   const DRenderer &R = F->renderer->r;
-  // the wavefront kernels have neither gradient shading nor spheres: the
+  // the wavefront kernels have neither gradient shading nor spheres, cones
+  // and cylinders: the
   // megakernel takes such frames
-  const bool wave = F->renderer->wavefront && !R.gradientShading && !W->scene.numSpheres;
+  const bool wave = F->renderer->wavefront && !R.gradientShading && !W->scene.numAnalytic;
   int stage = 0;
   MarchScratch ms{};
   bool segmented = false;
@@ -1626,7 +1703,7 @@ VSRStatus renderFrames(Device *dev, FrameObj *const *frames, uint32_t count) {
     j.F = F->record();
     j.kind = j.R.type != REND_RAYCAST ? JOB_PATHTRACE
              : (j.R.gradientShading ||
-                (j.S.hasSurfaces && (j.S.positionalLights || j.S.numSpheres))) ? JOB_RAYCAST_FULL
+                (j.S.hasSurfaces && (j.S.positionalLights || j.S.numAnalytic))) ? JOB_RAYCAST_FULL
              : j.S.hasSurfaces        ? JOB_RAYCAST_SURFACES
                                       : JOB_RAYCAST_VOLUME;
     // a frame past its sample limit only clears its error flags
@@ -1636,7 +1713,7 @@ VSRStatus renderFrames(Device *dev, FrameObj *const *frames, uint32_t count) {
     key.insert(key.end(), {(uint64_t)(uintptr_t)F, (uint64_t)j.F.width, (uint64_t)j.F.height,
                            (uint64_t)j.kind, (uint64_t)j.R.pixelSamples, (uint64_t)j.R.maxBounce,
                            (uint64_t)j.S.numVolumes, (uint64_t)j.R.gradientShading,
-                           (uint64_t)j.S.positionalLights, (uint64_t)j.S.numSpheres});
+                           (uint64_t)j.S.positionalLights, (uint64_t)j.S.numAnalytic});
   }
   if (!batched.empty()) {
     BatchTuner &tuner = B.tuners[key];
@@ -1698,7 +1775,7 @@ VSRStatus renderFrames(Device *dev, FrameObj *const *frames, uint32_t count) {
     for (const DJob &j : jobs)
       if (j.kind == JOB_PATHTRACE) {
         if (j.S.numVolumes > 0) L.pathtraceVariant |= 1;
-        if (j.S.positionalLights || j.S.numSpheres || (j.S.numVolumes > 0 && j.R.gradientShading))
+        if (j.S.positionalLights || j.S.numAnalytic || (j.S.numVolumes > 0 && j.R.gradientShading))
           L.pathtraceVariant |= 2;
       }
     // one CUDA graph per frame set and configuration: the job records are
@@ -1912,7 +1989,7 @@ VSRObject vsrNewVolume(VSRDevice d, const char *s) {
   return newObj<Volume>(d, VSR_VOLUME, s, {"transferFunction1D"});
 }
 VSRObject vsrNewGeometry(VSRDevice d, const char *s) {
-  return newObj<Geometry>(d, VSR_GEOMETRY, s, {"triangle", "sphere"});
+  return newObj<Geometry>(d, VSR_GEOMETRY, s, {"triangle", "sphere", "cone", "cylinder"});
 }
 VSRObject vsrNewMaterial(VSRDevice d, const char *s) {
   return newObj<Material>(d, VSR_MATERIAL, s, {"matte", "physicallyBased"});

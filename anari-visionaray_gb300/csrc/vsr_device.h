@@ -137,6 +137,10 @@ struct DVolume {
 //       leaf code as for BVH2   [7] unused
 constexpr int kEmptyChild = 0x7fffffff;
 
+enum AnalyticKind { AP_SPHERE = 0, AP_CONE = 1, AP_CYLINDER = 2 };
+constexpr int kApKindShift = 28;
+constexpr uint32_t kApLocalMask = (1u << kApKindShift) - 1u;
+
 struct DGroup {
   const float4 *nodes;
   const float4 *tris;
@@ -147,16 +151,18 @@ struct DGroup {
   int width;              // 2: BVH2 nodes (64 B), 4: BVH4 nodes (128 B)
   int volBegin, volEnd;   // range in DScene::groupVolumes
   float boundsLo[3], boundsHi[3];
-  // spheres (all sphere geometries of the group), their own BVH2: leaves
-  // index `spheres` (center, radius) in leaf order; sphLocal maps a leaf
-  // to the sphere's index in the group, sphSurface a sphere to its surface.
-  // A hit on sphere k carries Hit::tri = numTris + k.
-  const float4 *sphNodes;
-  const float4 *spheres;
-  const uint32_t *sphLocal;
-  const uint32_t *sphSurface;
-  int numSpheres;
-  int sphNumNodes;
+  // analytic primitives (all sphere, cone and cylinder geometries of the
+  // group) with their own BVH2: leaf i is apPrims[2i], apPrims[2i+1]
+  // (sphere: (center, radius), unused; cone / cylinder: (v1, r1), (v2, r2)),
+  // apLocal[i] = the primitive's index in the group | kind << kApKindShift,
+  // apSurface maps a group index to its surface. A hit on primitive k
+  // carries Hit::tri = numTris + k.
+  const float4 *apNodes;
+  const float4 *apPrims;
+  const uint32_t *apLocal;
+  const uint32_t *apSurface;
+  int numAP;
+  int apNumNodes;
 };
 
 struct DInstance {
@@ -178,7 +184,7 @@ struct DScene {
   int numGroups;
   int numLights;
   int positionalLights;  // point and spot lights among them: the kernels' full variants
-  int numSpheres;        // spheres in all groups: the kernels' full variants
+  int numAnalytic;       // spheres, cones, cylinders in all groups: the kernels' full variants
   int numVolumes;
   int allOpaque;
   int hasSurfaces;

@@ -8,7 +8,11 @@ is fixed in each generator. A scene is a plain dict:
   surfaces : [{"vertices": (V,3) f32, "indices": (T,3) u32, "material": {...}} |
               {"geometry": "sphere", "vertices": (V,3) f32 centres, "indices": (N,) u32
                (optional), "radii": (N,) f32 (optional), "radius": f32 (default 0.01),
-               "material": {...}}]
+               "material": {...}} |
+              {"geometry": "cone" | "cylinder", "vertices": (V,3) f32 end points,
+               "indices": (N,2) u32 (optional, else consecutive pairs), "radii": per
+               vertex (cone, required) or per cylinder (optional), "radius": f32
+               (cylinder, default 1), "material": {...}}]
   volumes  : [{"data": (nz,ny,nx) f32, "origin", "spacing", "color": (N,3),
                "opacity": (N,), "valueRange", "unitDistance"}]
   lights   : [{"type": "directional" (default), "direction", "color", "irradiance",
@@ -315,12 +319,13 @@ def _surfaces(dev, surfs, keep):
         dev.set(g, "vertex.position", va)
         keep += [va]
         ia = None
-        if kind == "sphere":
+        if kind in ("sphere", "cone", "cylinder"):
             if "indices" in s:
-                ia = dev.array1d(np.asarray(s["indices"], np.uint32).reshape(-1))
+                ia = np.asarray(s["indices"], np.uint32)
+                ia = dev.array1d(ia.reshape(-1) if kind == "sphere" else ia.reshape(-1, 2))
             if "radii" in s:
                 ra = dev.array1d(np.asarray(s["radii"], np.float32).reshape(-1))
-                dev.set(g, "vertex.radius", ra)
+                dev.set(g, "primitive.radius" if kind == "cylinder" else "vertex.radius", ra)
                 keep += [ra]
             if "radius" in s:
                 dev.set(g, "radius", float(s["radius"]))

@@ -144,6 +144,7 @@ _ARRAY_TYPES = {
     (np.dtype(np.float32), 3): FLOAT32_VEC3,
     (np.dtype(np.float32), 4): FLOAT32_VEC4,
     (np.dtype(np.uint32), 1): UINT32,
+    (np.dtype(np.uint32), 2): UINT32_VEC2,
     (np.dtype(np.uint32), 3): UINT32_VEC3,
     (np.dtype(np.uint8), 1): UFIXED8,
     (np.dtype(np.uint16), 1): UFIXED16,

@@ -373,8 +373,8 @@ BoxHit intersectBox(const Ray &r, const Box &b) {
 struct SurfHit {
   bool hit = false;
   float t = FLT_MAX, u = 0, v = 0;
-  int inst = -1, tri = -1;  // tri: global triangle index, -1 for a sphere
-  int sph = -1;             // global sphere index, -1 for a triangle
+  int inst = -1, tri = -1;  // tri: global triangle index, -1 otherwise
+  int prim = -1;            // global sphere / cone / cylinder index, -1 otherwise
   int key = -1;             // order within the instance: triangles, then spheres
   f3 isect_pos;             // instance-local hit position
 };
@@ -382,18 +382,72 @@ struct SurfHit {
 // Ray/sphere test as Visionaray's basic_sphere intersection (the reference's
 // intersect(ray, bls.asSphere), DeviceCopyableObjects.h:1486-1507): the
 // smaller root of |o + t d - c|^2 = r^2 from the cancellation-free
-// quadratic formula; -1 without real roots.
+// quadratic formula; -FLT_MAX without real roots.
 inline float hitSphere(const Ray &r, const float *sph) {
   f3 oc = r.ori - f3(sph[0], sph[1], sph[2]);
   float A = dot(r.dir, r.dir);
   float B = 2.f * dot(r.dir, oc);
   float C = dot(oc, oc) - sph[3] * sph[3];
   float disc = B * B - 4.f * A * C;
-  if (!(disc >= 0.f)) return -1.f;
+  if (!(disc >= 0.f)) return -FLT_MAX;
   float rd = std::sqrt(disc);
   float q = B < 0.f ? -0.5f * (B - rd) : -0.5f * (B + rd);
   float t1 = q / A, t2 = C / q;
   return t1 > t2 ? t2 : t1;
+}
+
+// Capped cone (v1, r1) -> (v2, r2): intersect(Ray, Cone),
+// DeviceCopyableObjects.h:933-1007 (Quilez's cone intersector). Caps first
+// (the one the origin lies behind), then the body's smaller root; u = 0 / 1
+// on the caps and y / |v2-v1|^2 on the body, v = y.
+inline float hitCone(const Ray &r, const float *q, float &u, float &v) {
+  f3 pa(q[0], q[1], q[2]), pb(q[4], q[5], q[6]);
+  float ra = q[3], rb = q[7];
+  f3 ba = pb - pa, oa = r.ori - pa, ob = r.ori - pb;
+  float m0 = dot(ba, ba), m1 = dot(oa, ba), m2 = dot(r.dir, ba);
+  float m3 = dot(r.dir, oa), m5 = dot(oa, oa), m9 = dot(ob, ba);
+  if (m1 < 0.f) {
+    f3 w = oa * m2 - r.dir * m1;
+    if (dot(w, w) < ra * ra * m2 * m2) { u = 0.f; v = 0.f; return -m1 / m2; }
+  } else if (m9 > 0.f) {
+    float t = -m9 / m2;
+    f3 w = ob + r.dir * t;
+    if (dot(w, w) < rb * rb) { u = 1.f; v = 0.f; return t; }
+  }
+  float rr = ra - rb;
+  float hy = m0 + rr * rr;
+  float k2 = m0 * m0 - m2 * m2 * hy;
+  float k1 = m0 * m0 * m3 - m1 * m2 * hy + m0 * ra * (rr * m2 * 1.f);
+  float k0 = m0 * m0 * m5 - m1 * m1 * hy + m0 * ra * (rr * m1 * 2.f - m0 * ra);
+  float h = k1 * k1 - k2 * k0;
+  if (h < 0.f) return -FLT_MAX;
+  float t = (-k1 - std::sqrt(h)) / k2;
+  float y = m1 + t * m2;
+  if (y > 0.f && y < m0) { u = y / m0; v = y; return t; }
+  return -FLT_MAX;
+}
+
+// Capped cylinder v1 -> v2 of radius r1 (Quilez's published capped-cylinder
+// intersector; Visionaray's basic_cylinder test is not part of the
+// reference): the body's smaller root, else the cap plane the body root
+// falls beyond, accepted inside the radius.
+inline float hitCylinder(const Ray &r, const float *q) {
+  f3 pa(q[0], q[1], q[2]), pb(q[4], q[5], q[6]);
+  float ra = q[3];
+  f3 ba = pb - pa, oc = r.ori - pa;
+  float baba = dot(ba, ba), bard = dot(ba, r.dir), baoc = dot(ba, oc);
+  float k2 = baba - bard * bard;
+  float k1 = baba * dot(oc, r.dir) - baoc * bard;
+  float k0 = baba * dot(oc, oc) - baoc * baoc - ra * ra * baba;
+  float h = k1 * k1 - k2 * k0;
+  if (h < 0.f) return -FLT_MAX;
+  h = std::sqrt(h);
+  float t = (-k1 - h) / k2;
+  float y = baoc + t * bard;
+  if (y > 0.f && y < baba) return t;
+  t = ((y < 0.f ? 0.f : baba) - baoc) / bard;
+  if (std::fabs(k1 + k2 * t) < h) return t;
+  return -FLT_MAX;
 }
 
 // Ray/triangle test in the basic_triangle (Moller-Trumbore) form; u,v are
@@ -427,18 +481,25 @@ SurfHit traceSurfaces(const Scene &sc, const Ray &ray, Counters &c) {
     const GroupBVH &bvh = sc.bvh[inst.group];
     const OrGroup &og = sc.src->groups[inst.group];
     Ray l = inst.toLocal(ray);
-    // spheres: every one of the group's (no acceleration structure)
-    for (int k = og.sphBegin; k < og.sphEnd; ++k) {
+    // spheres, cones, cylinders: every one of the group's (no acceleration
+    // structure)
+    for (int k = og.apBegin; k < og.apEnd; ++k) {
       c.tris++;
-      float t = hitSphere(l, sc.src->spheres + 4 * (size_t)k);
+      const float *q = sc.src->prims + 8 * (size_t)k;
+      float u = 0.f, v = 0.f, t;
+      switch (sc.src->primKind[k]) {
+        case 0: t = hitSphere(l, q); break;
+        case 1: t = hitCone(l, q, u, v); break;
+        default: t = hitCylinder(l, q);
+      }
       if (!(t >= l.tmin)) continue;
-      int key = (og.triEnd - og.triBegin) + (k - og.sphBegin);
+      int key = (og.triEnd - og.triBegin) + (k - og.apBegin);
       bool closer = t < best.t ||
                     (t == best.t && best.hit &&
                      ((int)ii < best.inst || ((int)ii == best.inst && key < best.key)));
       if (!closer) continue;
-      best.hit = true; best.t = t; best.u = 0.f; best.v = 0.f;
-      best.inst = (int)ii; best.tri = -1; best.sph = k; best.key = key;
+      best.hit = true; best.t = t; best.u = u; best.v = v;
+      best.inst = (int)ii; best.tri = -1; best.prim = k; best.key = key;
       best.isect_pos = l.ori + t * l.dir;
     }
     if (bvh.nodes.empty()) continue;
@@ -465,7 +526,7 @@ SurfHit traceSurfaces(const Scene &sc, const Ray &ray, Counters &c) {
                          ((int)ii < best.inst || ((int)ii == best.inst && key < best.key)));
           if (!closer) continue;
           best.hit = true; best.t = t; best.u = u; best.v = v;
-          best.inst = (int)ii; best.tri = tri; best.sph = -1; best.key = key;
+          best.inst = (int)ii; best.tri = tri; best.prim = -1; best.key = key;
           best.isect_pos = l.ori + t * l.dir;
         }
       } else {
@@ -478,17 +539,36 @@ SurfHit traceSurfaces(const Scene &sc, const Ray &ray, Counters &c) {
   return best;
 }
 
-// Surface index and object-space geometric normal of a surface hit
-// (getNormals, renderer/common.h:241-275): normalize(e1 x e2) for a
-// triangle, normalize((P - c) / r) at the local hit position for a sphere.
+// Surface index and object-space geometric normal of a surface hit at its
+// local position P (getNormals, renderer/common.h:241-303): normalize(e1 x
+// e2) for a triangle; normalize((P - c) / r) for a sphere; for a cone the
+// cap axis (u <= 0, u >= 1) or the body normal from the axis parameter v;
+// for a cylinder the cap axis within the radius of an end point, else P
+// minus its projection on the axis.
 uint32_t hitSurface(const OrScene &S, const SurfHit &h) {
-  return h.sph >= 0 ? S.sphereSurface[h.sph] : S.triSurface[h.tri];
+  return h.prim >= 0 ? S.primSurface[h.prim] : S.triSurface[h.tri];
 }
 
 f3 hitNormal(const Scene &sc, const SurfHit &h) {
-  if (h.sph >= 0) {
-    const float *s = sc.src->spheres + 4 * (size_t)h.sph;
-    return normalize((h.isect_pos - f3(s[0], s[1], s[2])) / s[3]);
+  if (h.prim >= 0) {
+    const float *q = sc.src->prims + 8 * (size_t)h.prim;
+    const f3 P = h.isect_pos, v1(q[0], q[1], q[2]), v2(q[4], q[5], q[6]);
+    const int kind = sc.src->primKind[h.prim];
+    if (kind == 0) return normalize((P - v1) / q[3]);
+    if (kind == 1) {
+      f3 ba = v2 - v1;
+      float m0 = dot(ba, ba);
+      if (h.u <= 0.f) return -ba * (1.f / std::sqrt(m0));
+      if (h.u >= 1.f) return ba * (1.f / std::sqrt(m0));
+      float ra = q[3], rr = q[3] - q[7];
+      float hy = m0 + rr * rr;
+      return normalize(m0 * (m0 * (P - v1) + rr * ba * ra) - ba * hy * h.v);
+    }
+    f3 axis = normalize(v2 - v1);
+    if (length(P - v1) < q[3]) return -axis;
+    if (length(P - v2) < q[3]) return axis;
+    float s = dot(P - v1, axis);
+    return normalize(P - (v1 + s * axis));
   }
   const Tri &T = sc.tris[h.tri];
   return normalize(cross(T.e1, T.e2));

@@ -45,7 +45,7 @@ class OrVolume(ctypes.Structure):
 
 class OrGroup(ctypes.Structure):
     _fields_ = [("triBegin", c_int32), ("triEnd", c_int32), ("volBegin", c_int32), ("volEnd", c_int32),
-                ("sphBegin", c_int32), ("sphEnd", c_int32)]
+                ("apBegin", c_int32), ("apEnd", c_int32)]
 
 
 class OrInstance(ctypes.Structure):
@@ -66,7 +66,8 @@ class OrScene(ctypes.Structure):
                 ("numGroups", c_int32), ("groups", ctypes.POINTER(OrGroup)),
                 ("numInstances", c_int32), ("instances", ctypes.POINTER(OrInstance)),
                 ("numLights", c_int32), ("lights", ctypes.POINTER(OrLight)),
-                ("numSpheres", c_int32), ("spheres", FP), ("sphereSurface", UP)]
+                ("numPrims", c_int32), ("prims", FP), ("primKind", ctypes.POINTER(c_int32)),
+                ("primSurface", UP)]
 
 
 class OrCamera(ctypes.Structure):
@@ -196,6 +197,39 @@ def build_tf(color, opacity):
     return out
 
 
+def analytic_prims(s):
+    """(N, 8) float32 records (p0, r0, p1, r1) of a sphere, cone or cylinder
+    surface, following Sphere.cpp:46-75, Cone.cpp:49-82, Cylinder.cpp:49-82:
+    sphere centres through 'indices' when given, per-sphere 'radii' (else
+    'radius', default 0.01); cone / cylinder end points from 'indices' pairs
+    (else consecutive vertices), cone radii per end vertex ('radii' required),
+    cylinder radii per cylinder ('radii') else 'radius' (default 1)."""
+    kind = s["geometry"]
+    pos = np.asarray(s["vertices"], np.float32).reshape(-1, 3)
+    if kind == "sphere":
+        c = pos[np.asarray(s["indices"], np.int64).reshape(-1)] if "indices" in s else pos
+        r = (np.asarray(s["radii"], np.float32).reshape(-1)[:len(c)] if "radii" in s
+             else np.full(len(c), s.get("radius", 0.01), np.float32))
+        q = np.zeros((len(c), 8), np.float32)
+        q[:, :3], q[:, 3] = c, r
+        return q
+    if "indices" in s:
+        ab = np.asarray(s["indices"], np.int64).reshape(-1, 2)
+    else:
+        n = len(pos) // 2
+        ab = np.stack([2 * np.arange(n), 2 * np.arange(n) + 1], axis=1)
+    q = np.zeros((len(ab), 8), np.float32)
+    q[:, :3], q[:, 4:7] = pos[ab[:, 0]], pos[ab[:, 1]]
+    if kind == "cone":
+        radii = np.asarray(s["radii"], np.float32).reshape(-1)
+        q[:, 3], q[:, 7] = radii[ab[:, 0]], radii[ab[:, 1]]
+    else:
+        r = (np.asarray(s["radii"], np.float32).reshape(-1)[:len(ab)] if "radii" in s
+             else np.full(len(ab), s.get("radius", 1.0), np.float32))
+        q[:, 3], q[:, 7] = r, r
+    return q
+
+
 class Scene:
     """A scene dict committed to the oracle (owns all buffers it points to)."""
 
@@ -210,25 +244,22 @@ class Scene:
             groups.append((inst.get("surfaces", []), inst.get("volumes", []),
                            inst.get("lights", []), inst["transform"]))
         verts, tsurf, tprim, mats, vols, ogroups, oinsts, lights = [], [], [], [], [], [], [], []
-        sphs, ssurf = [], []
-        ntri = nsph = 0
+        aps, akind, asurf = [], [], []
+        ntri = nap = 0
         for gi, (surfs, vls, lts, xfm) in enumerate(groups):
             g = OrGroup()
             g.triBegin = ntri
-            g.sphBegin = nsph
+            g.apBegin = nap
             for s in surfs:
-                if s.get("geometry", "triangle") == "sphere":
-                    # Sphere.cpp:46-75: centres through primitive.index when
-                    # given; vertex.radius indexed by the sphere, else 'radius'
-                    c = np.asarray(s["vertices"], np.float32).reshape(-1, 3)
-                    if "indices" in s:
-                        c = c[np.asarray(s["indices"], np.int64).reshape(-1)]
-                    r = (np.asarray(s["radii"], np.float32).reshape(-1)[:len(c)] if "radii" in s
-                         else np.full(len(c), s.get("radius", 0.01), np.float32))
-                    sphs.append(np.concatenate([c, r[:, None]], axis=1))
-                    ssurf.append(np.full(len(c), len(mats), np.uint32))
+                kind = s.get("geometry", "triangle")
+                if kind != "triangle":
+                    q = analytic_prims(s)
+                    aps.append(q)
+                    akind.append(np.full(len(q), {"sphere": 0, "cone": 1, "cylinder": 2}[kind],
+                                         np.int32))
+                    asurf.append(np.full(len(q), len(mats), np.uint32))
                     mats.append(material(s["material"]))
-                    nsph += len(c)
+                    nap += len(q)
                     continue
                 v = np.asarray(s["vertices"], np.float32)
                 t = np.asarray(s["indices"], np.uint32)
@@ -239,7 +270,7 @@ class Scene:
                 tprim.append(np.arange(len(t), dtype=np.uint32))
                 ntri += len(t)
             g.triEnd = ntri
-            g.sphEnd = nsph
+            g.apEnd = nap
             g.volBegin = len(vols)
             for v in vls:
                 ov = OrVolume()
@@ -296,10 +327,11 @@ class Scene:
         tri = np.ascontiguousarray(np.concatenate(verts) if verts else np.zeros((0, 9), np.float32))
         ts = np.ascontiguousarray(np.concatenate(tsurf) if tsurf else np.zeros(0, np.uint32))
         tp = np.ascontiguousarray(np.concatenate(tprim) if tprim else np.zeros(0, np.uint32))
-        sp = np.ascontiguousarray(np.concatenate(sphs) if sphs else np.zeros((0, 4), np.float32),
+        ap = np.ascontiguousarray(np.concatenate(aps) if aps else np.zeros((0, 8), np.float32),
                                   np.float32)
-        ss = np.ascontiguousarray(np.concatenate(ssurf) if ssurf else np.zeros(0, np.uint32))
-        self._keep += [tri, ts, tp, sp, ss]
+        ak = np.ascontiguousarray(np.concatenate(akind) if akind else np.zeros(0, np.int32))
+        asf = np.ascontiguousarray(np.concatenate(asurf) if asurf else np.zeros(0, np.uint32))
+        self._keep += [tri, ts, tp, ap, ak, asf]
         self.mats = (OrMaterial * max(1, len(mats)))(*mats)
         self.vols = (OrVolume * max(1, len(vols)))(*vols)
         self.groups = (OrGroup * max(1, len(ogroups)))(*ogroups)
@@ -323,9 +355,10 @@ class Scene:
         sc.instances = self.insts
         sc.numLights = len(lights)
         sc.lights = self.lights
-        sc.numSpheres = len(sp)
-        sc.spheres = fptr(sp)
-        sc.sphereSurface = ss.ctypes.data_as(UP)
+        sc.numPrims = len(ap)
+        sc.prims = fptr(ap)
+        sc.primKind = ak.ctypes.data_as(ctypes.POINTER(c_int32))
+        sc.primSurface = asf.ctypes.data_as(UP)
         self.scene = sc
         self.handle = lib.or_scene_commit(ctypes.byref(sc))
         self.camera = camera(scene["camera"])

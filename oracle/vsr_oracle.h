@@ -56,7 +56,7 @@ typedef struct OrVolume {
 typedef struct OrGroup {
   int32_t triBegin, triEnd; /* range in the scene's triangle array */
   int32_t volBegin, volEnd; /* range in the scene's volume array */
-  int32_t sphBegin, sphEnd; /* range in the scene's sphere array */
+  int32_t apBegin, apEnd;   /* range in the scene's sphere / cone / cylinder array */
 } OrGroup;
 
 typedef struct OrInstance {
@@ -95,9 +95,11 @@ typedef struct OrScene {
   const OrInstance *instances;
   int32_t numLights;
   const OrLight *lights;
-  int32_t numSpheres;
-  const float *spheres;          /* center, radius (object space) */
-  const uint32_t *sphereSurface; /* surface index per sphere */
+  int32_t numPrims;              /* spheres, cones, cylinders */
+  const float *prims;            /* 8 floats each, object space: sphere (center, radius, -);
+                                    cone / cylinder (v1, r1, v2, r2) */
+  const int32_t *primKind;       /* 0 sphere, 1 cone, 2 cylinder */
+  const uint32_t *primSurface;   /* surface index per primitive */
 } OrScene;
 
 typedef struct OrCamera {

@@ -472,11 +472,30 @@ def sphere_surfaces(base, n=40, seed=3):
              "radii": radii[h:], "material": base["surfaces"][1]["material"]}]
 
 
-def test_raycast_spheres(pkg, device, oracle):
-    """Sphere geometry (their own BVH per group, the smaller root of the
-    quadratic, normal (P - c) / r) beside triangle meshes, raycast."""
+def cone_cylinder_surfaces(base, n=16, seed=4):
+    """A cone geometry (index pairs, radii per vertex) and a cylinder
+    geometry (consecutive end points, radius per cylinder) over the
+    sphere-set volume."""
+    rng = np.random.default_rng(seed)
+    a = rng.uniform(-9.0, 9.0, (n, 3)).astype(np.float32)
+    b = (a + rng.uniform(-3.0, 3.0, (n, 3))).astype(np.float32)
+    ends = np.stack([a, b], axis=1).reshape(-1, 3)
+    return [{"geometry": "cone", "vertices": ends,
+             "indices": np.arange(2 * n, dtype=np.uint32).reshape(-1, 2)[::-1].copy(),
+             "radii": rng.uniform(0.2, 1.2, 2 * n).astype(np.float32),
+             "material": base["surfaces"][2]["material"]},
+            {"geometry": "cylinder", "vertices": ends,
+             "radii": rng.uniform(0.2, 0.8, n).astype(np.float32),
+             "material": base["surfaces"][3]["material"]}]
+
+
+@pytest.mark.parametrize("kinds", ["spheres", "cones_cylinders"])
+def test_raycast_analytic_primitives(pkg, device, oracle, kinds):
+    """Spheres, cones and cylinders (their own BVH per group, each kind's
+    intersection and normal) beside triangle meshes, raycast."""
     sc = small_spheres(pkg, res=128, renderer="raycast")
-    sc["surfaces"] = sc["surfaces"] + sphere_surfaces(sc)
+    extra = sphere_surfaces(sc) if kinds == "spheres" else cone_cylinder_surfaces(sc)
+    sc["surfaces"] = sc["surfaces"] + extra
     sc["lights"] = sc["lights"] + point_and_spot_lights()[:1]
     gpu = render_gpu(pkg, device, sc)
     _, F = render_oracle(oracle, sc)
@@ -494,12 +513,12 @@ def test_raycast_spheres(pkg, device, oracle):
 
 
 @pytest.mark.parametrize("wavefront", [True, False])
-def test_pathtrace_spheres_same_stream(pkg, device, oracle, wavefront):
-    """Path tracing over spheres and triangles with the same stream as the
-    oracle (a wavefront renderer hands worlds with spheres to the
+def test_pathtrace_analytic_primitives_same_stream(pkg, device, oracle, wavefront):
+    """Path tracing over spheres, cones, cylinders and triangles with the
+    same stream as the oracle (a wavefront renderer hands such worlds to the
     megakernel)."""
     sc = small_spheres(pkg, res=96, spp=8)
-    sc["surfaces"] = sc["surfaces"] + sphere_surfaces(sc)
+    sc["surfaces"] = sc["surfaces"] + sphere_surfaces(sc) + cone_cylinder_surfaces(sc)
     sc["renderer"]["wavefront"] = wavefront
     gpu = render_gpu(pkg, device, sc)
     _, F = render_oracle(oracle, sc)
@@ -509,14 +528,15 @@ def test_pathtrace_spheres_same_stream(pkg, device, oracle, wavefront):
     assert float((d <= 1e-3).mean()) >= 0.97, float((d <= 1e-3).mean())
 
 
-def test_instanced_spheres(pkg, device, oracle):
-    """A sphere-only group placed by an instance transform (rotation, scale,
-    translation), next to world-level triangles."""
+def test_instanced_analytic_primitives(pkg, device, oracle):
+    """A group of spheres, cones and cylinders placed by an instance
+    transform (rotation, scale, translation), next to world-level triangles."""
     base = small_spheres(pkg, res=96, renderer="raycast", n=10)
     c, s = np.cos(0.4), np.sin(0.4)
     xfm = [c * 1.2, 0.0, -s * 1.2, 0.0, 1.2, 0.0, s * 1.2, 0.0, c * 1.2, 1.0, -0.5, 2.0]
     sc = dict(base)
-    sc["instances"] = [{"transform": xfm, "surfaces": sphere_surfaces(base, n=16)}]
+    sc["instances"] = [{"transform": xfm,
+                        "surfaces": sphere_surfaces(base, n=16) + cone_cylinder_surfaces(base, 8)}]
     gpu = render_gpu(pkg, device, sc)
     _, F = render_oracle(oracle, sc)
     assert gpu["errorFlags"] == 0

@@ -193,6 +193,64 @@ def test_sphere_closed_form(oracle):
     assert np.allclose(F.normal[inside], n[inside], atol=1e-4)
 
 
+def _lit(n, c=np.array([0.6, 0.5, 0.4])):
+    """Matte shading of plane_scene's light: c/pi E max(0, n.L) + c ambient."""
+    L = -np.array([0.0, -0.6, -0.8])
+    L /= np.linalg.norm(L)
+    return c / math.pi * 2.0 * np.maximum(0.0, n @ L)[..., None] + c * 0.2
+
+
+def _top_view(oracle, surface, size=32, height=6.0):
+    sc = plane_scene()
+    sc["surfaces"] = [dict(surface, material={"type": "matte", "color": [0.6, 0.5, 0.4]})]
+    sc["camera"] = {"type": "orthographic", "position": [0.0, 0.0, 10.0],
+                    "direction": [0.0, 0.0, -1.0], "up": [0.0, 1.0, 0.0], "height": height,
+                    "aspect": 1.0}
+    S = oracle.Scene(sc)
+    F = oracle.Frame(size, size)
+    oracle.render(S, F)
+    xs = ((np.arange(size) + 0.5) / size - 0.5) * height
+    X, Y = np.meshgrid(xs, xs)
+    return F, X, Y
+
+
+def test_cylinder_closed_form(oracle):
+    """A cylinder along x (radius 1, from x = -2 to 2, placed through
+    primitive.index) seen from above: the body's top half, normal
+    (0, y, sqrt(1 - y^2)), shaded as a matte surface; nothing past the ends."""
+    F, X, Y = _top_view(oracle, {"geometry": "cylinder",
+                                 "vertices": np.array([[5, 5, 5], [-2, 0, 0], [2, 0, 0]],
+                                                      np.float32),
+                                 "indices": np.array([[1, 2]], np.uint32), "radius": 1.0})
+    body = (np.abs(X) < 1.9) & (np.abs(Y) < 0.95)
+    miss = (np.abs(X) > 2.1) | (np.abs(Y) > 1.05)
+    z = np.sqrt(np.maximum(0.0, 1.0 - Y * Y))
+    n = np.stack([np.zeros_like(Y), Y, z], axis=-1)
+    assert body.sum() > 100 and miss.sum() > 100
+    assert np.allclose(F.color[body][:, :3], _lit(n)[body], atol=2e-5)
+    assert np.allclose(F.depth[body], 10.0 - z[body], rtol=1e-4)
+    assert np.all(F.color[miss][:, :3] == 0.0)
+
+
+def test_cone_closed_form(oracle):
+    """A cone frustum along z (radius 2 at z = 0 to radius 1 at z = 3) seen
+    from above: the top cap (normal +z) inside radius 1, the body between
+    radius 1 and 2 at height 3 (2 - rho) with normal along (x/rho, y/rho, 1/3)."""
+    F, X, Y = _top_view(oracle, {"geometry": "cone",
+                                 "vertices": np.array([[0, 0, 0], [0, 0, 3]], np.float32),
+                                 "radii": np.array([2.0, 1.0], np.float32)})
+    rho = np.sqrt(X * X + Y * Y)
+    cap, body, miss = rho < 0.95, (rho > 1.05) & (rho < 1.95), rho > 2.05
+    nb = np.stack([X / rho, Y / rho, np.full_like(rho, 1.0 / 3.0)], axis=-1)
+    nb /= np.linalg.norm(nb, axis=-1, keepdims=True)
+    assert cap.sum() > 20 and body.sum() > 100 and miss.sum() > 50
+    assert np.allclose(F.color[cap][:, :3], _lit(np.array([0.0, 0.0, 1.0]))[None, :], atol=2e-5)
+    assert np.allclose(F.depth[cap], 7.0, rtol=1e-5)
+    assert np.allclose(F.color[body][:, :3], _lit(nb)[body], atol=5e-5)
+    assert np.allclose(F.depth[body], 10.0 - 3.0 * (2.0 - rho[body]), rtol=1e-4)
+    assert np.all(F.color[miss][:, :3] == 0.0)
+
+
 def test_emission_absorption_slab(oracle):
     """Constant field, TF alpha a: alpha after k steps is 1 - (1-a)^(k dt/ud)."""
     n = 16

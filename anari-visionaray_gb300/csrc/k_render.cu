@@ -58,10 +58,11 @@ cudaError_t launchRaycast(const DScene &S, const DCamera &C, const DRenderer &R,
       cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     kernel<<<grid, block, smem, stream>>>(S, C, R, F, stage);
   };
-  // the full variant for gradient shading, and for point / spot lights or
-  // spheres on surfaces (volume-only worlds light nothing without gradient
+  // the full variant for gradient shading, and for point / spot lights,
+  // spheres, cones, cylinders or quads on surfaces (volume-only worlds light nothing without gradient
   // shading)
-  if (R.gradientShading || (S.hasSurfaces && (S.positionalLights || S.numAnalytic))) {
+  if (R.gradientShading ||
+      (S.hasSurfaces && (S.positionalLights || S.numAnalytic || S.quadGroups))) {
     if (count) launch(kRaycast<true, true, true>);
     else launch(kRaycast<false, true, true>);
   } else if (S.hasSurfaces) {
@@ -81,7 +82,8 @@ cudaError_t launchPathtrace(const DScene &S, const DCamera &C, const DRenderer &
                             bool count, cudaStream_t stream) {
   dim3 block(16, VSR_MEGA_BLOCK_Y);
   const dim3 grid = tileGrid(F, block);
-  const bool full = S.positionalLights || S.numAnalytic || (S.numVolumes > 0 && R.gradientShading);
+  const bool full = S.positionalLights || S.numAnalytic || S.quadGroups ||
+                    (S.numVolumes > 0 && R.gradientShading);
   auto launch = [&](auto kernel) { kernel<<<grid, block, 0, stream>>>(S, C, R, F); };
   if (S.numVolumes > 0) {
     if (full) count ? launch(kPathtrace<true, true, true>) : launch(kPathtrace<false, true, true>);

@@ -602,7 +602,7 @@ __device__ __forceinline__ uint32_t hitSurface(const DGroup &G, const Hit &h) {
 
 // Object-space geometric normal of a hit at the instance-local hit position
 // P, getNormals (renderer/common.h:241-303): normalize(e1 x e2) for a
-// triangle; normalize((P - c) / r) for a sphere; for a cone the cap axis
+// triangle (for a quad's triangles the stored normal of the quad); normalize((P - c) / r) for a sphere; for a cone the cap axis
 // (u <= 0, u >= 1) or the body normal from the axis parameter v; for a
 // cylinder the cap axis within the radius of an end point, else P minus
 // its projection on the axis.
@@ -633,6 +633,10 @@ __device__ __forceinline__ float3 hitNormal(const DGroup &G, const DInstance &I,
     if (length(P - v2) < A.w) return axis;
     const float s = dot(P - v1, axis);
     return normalize(P - (v1 + s * axis));
+  }
+  if (Full && G.triNormal) {  // quads: the normal getNormals picks for the quad
+    const float4 n = __ldg(G.triNormal + h.tri);
+    if (n.w != 0.f) return f3(n.x, n.y, n.z);
   }
   const float4 *E = G.tris + 3 * (size_t)h.leaf;
   const float4 e1 = __ldg(E + 1), e2 = __ldg(E + 2);

@@ -97,7 +97,7 @@ static size_t typeSize(VSRDataType t) {
   case VSR_UFIXED16: return 2;
   case VSR_INT32_VEC2: case VSR_UINT32_VEC2: case VSR_FLOAT32_VEC2: case VSR_FLOAT32_BOX1: return 8;
   case VSR_UINT32_VEC3: case VSR_FLOAT32_VEC3: return 12;
-  case VSR_FLOAT32_VEC4: return 16;
+  case VSR_FLOAT32_VEC4: case VSR_UINT32_VEC4: return 16;
   case VSR_UFIXED8_VEC4: case VSR_UFIXED8_RGBA_SRGB: return 4;
   case VSR_FLOAT32_MAT4: return 64;
   case VSR_FLOAT32_MAT3x4: return 48;
@@ -428,11 +428,18 @@ struct Geometry : Object {
   // (a sphere uses (center, radius) and zeros), all of kind apKind
   std::vector<float> prims;
   int apKind = AP_SPHERE;
+  // quads: the object-space shading normal of each tessellated triangle
+  std::vector<float> quadNormals;
   using Object::Object;
   void commit() override {
     valid = false;
     v1.clear(); e1.clear(); e2.clear();
     prims.clear();
+    quadNormals.clear();
+    if (subtype == "quad") {
+      commitQuads();
+      return;
+    }
     if (subtype == "sphere") {
       commitSpheres();
       return;
@@ -478,6 +485,58 @@ struct Geometry : Object {
                   "'vertex.normal' is not used: shading uses the geometric normal");
     valid = true;
   }
+  // Quad.cpp:46-110: each quad (v1..v4, from primitive.index as UINT32_VEC4
+  // or consecutive vertices) becomes the triangles (v1, v2-v1, v4-v1) and
+  // (v3, v4-v3, v2-v3). Shading normals follow getNormals
+  // (renderer/common.h:266-267), which takes the triangle whose position in
+  // the geometry's triangle list equals the quad's index: quad q is shaded
+  // with the normal of triangle q (of quad q / 2), not of the one hit.
+  void commitQuads() {
+    Array *pos = geto<Array>("vertex.position", VSR_ARRAY1D);
+    Array *idx = geto<Array>("primitive.index", VSR_ARRAY1D);
+    if (!pos || pos->elemType != VSR_FLOAT32_VEC3) {
+      warn("missing required parameter 'vertex.position' on quad geometry");
+      return;
+    }
+    if (idx && idx->elemType != VSR_UINT32_VEC4) {
+      warn("unsupported type for 'primitive.index' on quad geometry");
+      return;
+    }
+    const float *P = pos->as<float>();
+    const size_t nv = pos->size();
+    const size_t nq = idx ? idx->size() : nv / 4;
+    auto tri = [&](size_t a, size_t b, size_t c) {
+      for (int k = 0; k < 3; ++k) {
+        const float p1 = P[3 * a + k];
+        v1.push_back(p1);
+        e1.push_back(P[3 * b + k] - p1);
+        e2.push_back(P[3 * c + k] - p1);
+      }
+    };
+    for (size_t q = 0; q < nq; ++q) {
+      size_t i[4];
+      for (int k = 0; k < 4; ++k) i[k] = idx ? idx->as<uint32_t>()[4 * q + k] : 4 * q + k;
+      if (i[0] >= nv || i[1] >= nv || i[2] >= nv || i[3] >= nv) {
+        warn("'primitive.index' out of range on quad geometry");
+        v1.clear(); e1.clear(); e2.clear();
+        return;
+      }
+      tri(i[0], i[1], i[3]);
+      tri(i[2], i[3], i[1]);
+    }
+    const size_t nt = 2 * nq;
+    quadNormals.resize(3 * nt);
+    for (size_t t = 0; t < nt; ++t) {
+      const size_t src = 3 * (t / 2);  // triangle number (quad index), float offset
+      const float *a = &e1[src], *b = &e2[src];
+      float n[3] = {a[1] * b[2] - a[2] * b[1], a[2] * b[0] - a[0] * b[2],
+                    a[0] * b[1] - a[1] * b[0]};
+      const float l = std::sqrt(n[0] * n[0] + n[1] * n[1] + n[2] * n[2]);
+      for (int k = 0; k < 3; ++k) quadNormals[3 * t + k] = n[k] / l;
+    }
+    valid = true;
+  }
+
   // Sphere.cpp:19-83: centers from vertex.position (through primitive.index
   // when given), radius from vertex.radius indexed by the sphere (not by the
   // vertex), else the global 'radius' (default 0.01)
@@ -908,7 +967,7 @@ struct Renderer : Object {
 // ----------------------------------------------------------------- world
 struct GroupGPU {
   DevBuf v1, e1, e2, nodes, nodes4, tris, triSurface, triPrim;
-  DevBuf apSrc, apKinds, apNodes, apLeaf, apPrims, apLocal, apSurface;
+  DevBuf apSrc, apKinds, apNodes, apLeaf, apPrims, apLocal, apSurface, triNormal;
   int numTris = 0, numNodes = 0, width = 2;
   int numAP = 0, apNumNodes = 0;
   float buildMs = 0.f;
@@ -1051,7 +1110,7 @@ struct World : Object {
     groupsGPU.clear();
     bvhNodes = bvhTris = 0;
     bool allOpaque = true, anySurf = false;
-    int numAnalytic = 0;
+    int numAnalytic = 0, quadGroups = 0;
     for (size_t gi = 0; gi < groups.size(); ++gi) {
       Group *g = groups[gi];
       auto gg = std::make_unique<GroupGPU>();
@@ -1059,6 +1118,8 @@ struct World : Object {
       std::vector<uint32_t> triSurf, triPrim;
       std::vector<float> apPrims;
       std::vector<uint32_t> apKinds, apSurf;
+      std::vector<float> triNormal;  // 4 floats per triangle, w = 1 where set
+      bool anyQuad = false;
       float lo[3] = {1e30f, 1e30f, 1e30f}, hi[3] = {-1e30f, -1e30f, -1e30f};
       for (Surface *sf : g->surfaces) {
         if (!sf->valid || !sf->geom->valid || !sf->mat->valid) continue;
@@ -1084,6 +1145,15 @@ struct World : Object {
           continue;
         }
         size_t nt = G->numTris();
+        triNormal.resize(4 * (triSurf.size() + nt), 0.f);
+        if (!G->quadNormals.empty()) {
+          anyQuad = true;
+          for (size_t t = 0; t < nt; ++t) {
+            float *n = &triNormal[4 * (triSurf.size() + t)];
+            for (int k = 0; k < 3; ++k) n[k] = G->quadNormals[3 * t + k];
+            n[3] = 1.f;
+          }
+        }
         v1.insert(v1.end(), G->v1.begin(), G->v1.end());
         e1.insert(e1.end(), G->e1.begin(), G->e1.end());
         e2.insert(e2.end(), G->e2.begin(), G->e2.end());
@@ -1170,6 +1240,15 @@ struct World : Object {
       }
       if (na > 0 && !buildAnalytic(*gg, apPrims, apKinds, apSurf, s)) return false;
       if (na > 0) anySurf = true;
+      if (anyQuad) {
+        if (gg->triNormal.upload(triNormal.data(), triNormal.size() * sizeof(float), s)) {
+          dev->report(this, kind, VSR_SEVERITY_ERROR, VSR_ERROR_OUT_OF_MEMORY,
+                      "scene upload failed");
+          return false;
+        }
+        ++quadGroups;
+      }
+      dg.triNormal = anyQuad ? gg->triNormal.as<float4>() : nullptr;
       dg.apNodes = gg->apNodes.as<float4>();
       dg.apPrims = gg->apPrims.as<float4>();
       dg.apLocal = gg->apLocal.as<uint32_t>();
@@ -1282,6 +1361,7 @@ struct World : Object {
     scene.allOpaque = allOpaque ? 1 : 0;
     scene.hasSurfaces = anySurf ? 1 : 0;
     scene.numAnalytic = numAnalytic;
+    scene.quadGroups = quadGroups;
     builtStamp = deep;
     commitMs = std::chrono::duration<float, std::milli>(std::chrono::steady_clock::now() - t0).count();
     return true;
@@ -1507,10 +1587,11 @@ VSRStatus renderFrame(Device *dev, FrameObj *F) {
   }
   const bool doRender = F->accumID < F->renderer->sampleLimit;
   const DRenderer &R = F->renderer->r;
-  // the wavefront kernels have neither gradient shading nor spheres, cones
-  // and cylinders: the
+  // the wavefront kernels have neither gradient shading nor spheres, cones,
+  // cylinders and quads: the
   // megakernel takes such frames
-  const bool wave = F->renderer->wavefront && !R.gradientShading && !W->scene.numAnalytic;
+  const bool wave = F->renderer->wavefront && !R.gradientShading && !W->scene.numAnalytic &&
+                    !W->scene.quadGroups;
   int stage = 0;
   MarchScratch ms{};
   bool segmented = false;
@@ -1703,7 +1784,8 @@ VSRStatus renderFrames(Device *dev, FrameObj *const *frames, uint32_t count) {
     j.F = F->record();
     j.kind = j.R.type != REND_RAYCAST ? JOB_PATHTRACE
              : (j.R.gradientShading ||
-                (j.S.hasSurfaces && (j.S.positionalLights || j.S.numAnalytic))) ? JOB_RAYCAST_FULL
+                (j.S.hasSurfaces && (j.S.positionalLights || j.S.numAnalytic || j.S.quadGroups)))
+                 ? JOB_RAYCAST_FULL
              : j.S.hasSurfaces        ? JOB_RAYCAST_SURFACES
                                       : JOB_RAYCAST_VOLUME;
     // a frame past its sample limit only clears its error flags
@@ -1713,7 +1795,8 @@ VSRStatus renderFrames(Device *dev, FrameObj *const *frames, uint32_t count) {
     key.insert(key.end(), {(uint64_t)(uintptr_t)F, (uint64_t)j.F.width, (uint64_t)j.F.height,
                            (uint64_t)j.kind, (uint64_t)j.R.pixelSamples, (uint64_t)j.R.maxBounce,
                            (uint64_t)j.S.numVolumes, (uint64_t)j.R.gradientShading,
-                           (uint64_t)j.S.positionalLights, (uint64_t)j.S.numAnalytic});
+                           (uint64_t)j.S.positionalLights, (uint64_t)j.S.numAnalytic,
+                           (uint64_t)j.S.quadGroups});
   }
   if (!batched.empty()) {
     BatchTuner &tuner = B.tuners[key];
@@ -1775,7 +1858,8 @@ VSRStatus renderFrames(Device *dev, FrameObj *const *frames, uint32_t count) {
     for (const DJob &j : jobs)
       if (j.kind == JOB_PATHTRACE) {
         if (j.S.numVolumes > 0) L.pathtraceVariant |= 1;
-        if (j.S.positionalLights || j.S.numAnalytic || (j.S.numVolumes > 0 && j.R.gradientShading))
+        if (j.S.positionalLights || j.S.numAnalytic || j.S.quadGroups ||
+            (j.S.numVolumes > 0 && j.R.gradientShading))
           L.pathtraceVariant |= 2;
       }
     // one CUDA graph per frame set and configuration: the job records are
@@ -1989,7 +2073,7 @@ VSRObject vsrNewVolume(VSRDevice d, const char *s) {
   return newObj<Volume>(d, VSR_VOLUME, s, {"transferFunction1D"});
 }
 VSRObject vsrNewGeometry(VSRDevice d, const char *s) {
-  return newObj<Geometry>(d, VSR_GEOMETRY, s, {"triangle", "sphere", "cone", "cylinder"});
+  return newObj<Geometry>(d, VSR_GEOMETRY, s, {"triangle", "quad", "sphere", "cone", "cylinder"});
 }
 VSRObject vsrNewMaterial(VSRDevice d, const char *s) {
   return newObj<Material>(d, VSR_MATERIAL, s, {"matte", "physicallyBased"});

@@ -157,6 +157,10 @@ struct DGroup {
   // apLocal[i] = the primitive's index in the group | kind << kApKindShift,
   // apSurface maps a group index to its surface. A hit on primitive k
   // carries Hit::tri = numTris + k.
+  // per local triangle: an object-space shading normal (w = 1) that
+  // replaces normalize(e1 x e2), set for quad geometries; null when the
+  // group has none
+  const float4 *triNormal;
   const float4 *apNodes;
   const float4 *apPrims;
   const uint32_t *apLocal;
@@ -185,6 +189,7 @@ struct DScene {
   int numLights;
   int positionalLights;  // point and spot lights among them: the kernels' full variants
   int numAnalytic;       // spheres, cones, cylinders in all groups: the kernels' full variants
+  int quadGroups;        // groups with quad geometry (triNormal set): the full variants
   int numVolumes;
   int allOpaque;
   int hasSurfaces;

@@ -9,6 +9,8 @@ is fixed in each generator. A scene is a plain dict:
               {"geometry": "sphere", "vertices": (V,3) f32 centres, "indices": (N,) u32
                (optional), "radii": (N,) f32 (optional), "radius": f32 (default 0.01),
                "material": {...}} |
+              {"geometry": "quad", "vertices": (V,3) f32, "indices": (Q,4) u32 (optional,
+               else consecutive quadruples), "material": {...}} |
               {"geometry": "cone" | "cylinder", "vertices": (V,3) f32 end points,
                "indices": (N,2) u32 (optional, else consecutive pairs), "radii": per
                vertex (cone, required) or per cylinder (optional), "radius": f32
@@ -329,6 +331,9 @@ def _surfaces(dev, surfs, keep):
                 keep += [ra]
             if "radius" in s:
                 dev.set(g, "radius", float(s["radius"]))
+        elif kind == "quad":
+            if "indices" in s:
+                ia = dev.array1d(np.asarray(s["indices"], np.uint32).reshape(-1, 4))
         else:
             ia = dev.array1d(np.asarray(s["indices"], np.uint32))
         if ia is not None:

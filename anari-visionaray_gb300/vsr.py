@@ -19,7 +19,7 @@ UNKNOWN, STRING, OBJECT, ARRAY1D, ARRAY2D, ARRAY3D, CAMERA, FRAME, GEOMETRY, GRO
     LIGHT, MATERIAL, RENDERER, SURFACE, SPATIAL_FIELD, VOLUME, WORLD, DATA_TYPE, BOOL, INT32, \
     UINT32, INT32_VEC2, UINT32_VEC2, UINT32_VEC3, FLOAT32, FLOAT32_VEC2, FLOAT32_VEC3, \
     FLOAT32_VEC4, FLOAT32_BOX1, FLOAT32_MAT4, FLOAT32_MAT3x4, UFIXED8, UFIXED8_VEC4, \
-    UFIXED8_RGBA_SRGB, UFIXED16, FLOAT64_BOX1, UINT64, FLOAT64 = range(39)
+    UFIXED8_RGBA_SRGB, UFIXED16, FLOAT64_BOX1, UINT64, FLOAT64, UINT32_VEC4 = range(40)
 
 OK = 0
 WAIT, NO_WAIT = 1, 0
@@ -146,6 +146,7 @@ _ARRAY_TYPES = {
     (np.dtype(np.uint32), 1): UINT32,
     (np.dtype(np.uint32), 2): UINT32_VEC2,
     (np.dtype(np.uint32), 3): UINT32_VEC3,
+    (np.dtype(np.uint32), 4): UINT32_VEC4,
     (np.dtype(np.uint8), 1): UFIXED8,
     (np.dtype(np.uint16), 1): UFIXED16,
 }
@@ -348,7 +349,7 @@ class Device:
                          12: FLOAT32_MAT3x4}[n]
         if type_ in (BOOL, INT32, UINT32, DATA_TYPE):
             buf = np.array([int(value)], dtype=np.int64).astype(np.uint32 if type_ == UINT32 else np.int32)
-        elif type_ in (UINT32_VEC2, UINT32_VEC3):
+        elif type_ in (UINT32_VEC2, UINT32_VEC3, UINT32_VEC4):
             buf = np.asarray(value, dtype=np.uint32)
         elif type_ == INT32_VEC2:
             buf = np.asarray(value, dtype=np.int32)

@@ -94,7 +94,8 @@ typedef enum VSRDataType {
   VSR_UFIXED16 = 35,
   VSR_FLOAT64_BOX1 = 36,
   VSR_UINT64 = 37,
-  VSR_FLOAT64 = 38
+  VSR_FLOAT64 = 38,
+  VSR_UINT32_VEC4 = 39
 } VSRDataType;
 
 typedef enum VSRWaitMask { VSR_NO_WAIT = 0, VSR_WAIT = 1 } VSRWaitMask;

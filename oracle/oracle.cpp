@@ -351,6 +351,8 @@ void buildMajorants(Vol &vol) {
 struct Scene {
   const OrScene *src;
   std::vector<Tri> tris;
+  std::vector<f3> triNormal;   // quads: the shading normal per triangle (empty if none)
+  std::vector<char> hasNormal;
   std::vector<GroupBVH> bvh;
   std::vector<Vol> vols;
   std::vector<Inst> insts;
@@ -582,6 +584,7 @@ f3 hitNormal(const Scene &sc, const SurfHit &h) {
     float s = dot(P - v1, axis);
     return normalize(P - (v1 + s * axis));
   }
+  if (!sc.hasNormal.empty() && sc.hasNormal[h.tri]) return sc.triNormal[h.tri];
   const Tri &T = sc.tris[h.tri];
   return normalize(cross(T.e1, T.e2));
 }
@@ -1657,6 +1660,22 @@ Scene *commit(const OrScene *s) {
     const float *p = s->triVerts + 9 * i;
     f3 v1(p[0], p[1], p[2]), v2(p[3], p[4], p[5]), v3(p[6], p[7], p[8]);
     sc->tris[i] = Tri{v1, v2 - v1, v3 - v1};
+  }
+  // quad geometries (Quad.cpp:69-110 tessellation; getNormals,
+  // renderer/common.h:266-267): a quad's triangles are shaded with the normal
+  // of the triangle whose position in the geometry's list is the quad's index
+  if (s->triNormalFrom) {
+    sc->triNormal.resize(s->numTriangles);
+    sc->hasNormal.assign(s->numTriangles, 0);
+    for (int i = 0; i < s->numTriangles; ++i) {
+      const int from = s->triNormalFrom[i];
+      if (from < 0) continue;
+      const Tri &T = sc->tris[from];
+      f3 n = cross(T.e1, T.e2);
+      const float l = std::sqrt(n.x * n.x + n.y * n.y + n.z * n.z);
+      sc->triNormal[i] = f3(n.x / l, n.y / l, n.z / l);
+      sc->hasNormal[i] = 1;
+    }
   }
   sc->bvh.resize(s->numGroups);
   for (int g = 0; g < s->numGroups; ++g)

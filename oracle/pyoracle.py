@@ -67,7 +67,7 @@ class OrScene(ctypes.Structure):
                 ("numInstances", c_int32), ("instances", ctypes.POINTER(OrInstance)),
                 ("numLights", c_int32), ("lights", ctypes.POINTER(OrLight)),
                 ("numPrims", c_int32), ("prims", FP), ("primKind", ctypes.POINTER(c_int32)),
-                ("primSurface", UP)]
+                ("primSurface", UP), ("triNormalFrom", ctypes.POINTER(c_int32))]
 
 
 class OrCamera(ctypes.Structure):
@@ -245,6 +245,7 @@ class Scene:
                            inst.get("lights", []), inst["transform"]))
         verts, tsurf, tprim, mats, vols, ogroups, oinsts, lights = [], [], [], [], [], [], [], []
         aps, akind, asurf = [], [], []
+        nfrom, has_quads = [], False
         ntri = nap = 0
         for gi, (surfs, vls, lts, xfm) in enumerate(groups):
             g = OrGroup()
@@ -252,7 +253,7 @@ class Scene:
             g.apBegin = nap
             for s in surfs:
                 kind = s.get("geometry", "triangle")
-                if kind != "triangle":
+                if kind in ("sphere", "cone", "cylinder"):
                     q = analytic_prims(s)
                     aps.append(q)
                     akind.append(np.full(len(q), {"sphere": 0, "cone": 1, "cylinder": 2}[kind],
@@ -262,7 +263,17 @@ class Scene:
                     nap += len(q)
                     continue
                 v = np.asarray(s["vertices"], np.float32)
-                t = np.asarray(s["indices"], np.uint32)
+                if kind == "quad":
+                    # Quad.cpp:69-110: (v1, v2, v4) and (v3, v4, v2) per quad;
+                    # triangle k of the list shades quad k's two triangles
+                    q = (np.asarray(s["indices"], np.int64).reshape(-1, 4) if "indices" in s
+                         else np.arange(len(v) // 4 * 4).reshape(-1, 4))
+                    t = np.stack([q[:, [0, 1, 3]], q[:, [2, 3, 1]]], axis=1).reshape(-1, 3)
+                    nfrom.append(ntri + np.arange(len(t)) // 2)
+                    has_quads = True
+                else:
+                    t = np.asarray(s["indices"], np.uint32)
+                    nfrom.append(np.full(len(t), -1, np.int64))
                 verts.append(v[t].reshape(-1, 9))
                 sid = len(mats)
                 mats.append(material(s["material"]))
@@ -331,7 +342,8 @@ class Scene:
                                   np.float32)
         ak = np.ascontiguousarray(np.concatenate(akind) if akind else np.zeros(0, np.int32))
         asf = np.ascontiguousarray(np.concatenate(asurf) if asurf else np.zeros(0, np.uint32))
-        self._keep += [tri, ts, tp, ap, ak, asf]
+        nf = np.ascontiguousarray(np.concatenate(nfrom) if nfrom else np.zeros(0), np.int32)
+        self._keep += [tri, ts, tp, ap, ak, asf, nf]
         self.mats = (OrMaterial * max(1, len(mats)))(*mats)
         self.vols = (OrVolume * max(1, len(vols)))(*vols)
         self.groups = (OrGroup * max(1, len(ogroups)))(*ogroups)
@@ -359,6 +371,8 @@ class Scene:
         sc.prims = fptr(ap)
         sc.primKind = ak.ctypes.data_as(ctypes.POINTER(c_int32))
         sc.primSurface = asf.ctypes.data_as(UP)
+        sc.triNormalFrom = (nf.ctypes.data_as(ctypes.POINTER(c_int32)) if has_quads
+                            else ctypes.POINTER(c_int32)())
         self.scene = sc
         self.handle = lib.or_scene_commit(ctypes.byref(sc))
         self.camera = camera(scene["camera"])

@@ -100,6 +100,8 @@ typedef struct OrScene {
                                     cone / cylinder (v1, r1, v2, r2) */
   const int32_t *primKind;       /* 0 sphere, 1 cone, 2 cylinder */
   const uint32_t *primSurface;   /* surface index per primitive */
+  const int32_t *triNormalFrom;  /* per triangle: the triangle whose e1 x e2 is its shading
+                                    normal (quads), -1 for its own; may be null */
 } OrScene;
 
 typedef struct OrCamera {

@@ -495,12 +495,43 @@ def cone_cylinder_surfaces(base, n=16, seed=4):
              "material": base["surfaces"][3]["material"]}]
 
 
-@pytest.mark.parametrize("kinds", ["spheres", "cones_cylinders"])
+def quad_surfaces(base, n=24, seed=6, flat=False):
+    """Planar quads of random orientation and size over the sphere-set
+    volume, half through primitive.index (as UINT32_VEC4), half as
+    consecutive vertices; each quad k is shaded with the normal of
+    tessellated triangle k, i.e. mostly another quad's. flat: horizontal
+    quads facing up, for which that normal is each quad's own."""
+    rng = np.random.default_rng(seed)
+    c = rng.uniform(-9.0, 9.0, (n, 3))
+    u = rng.normal(size=(n, 3))
+    w = rng.normal(size=(n, 3))
+    if flat:
+        u[:, 1] = 0.0
+        w = np.cross(np.array([0.0, 1.0, 0.0]), u)
+    u *= rng.uniform(0.8, 2.5, (n, 1)) / np.linalg.norm(u, axis=1, keepdims=True)
+    w -= (w * u).sum(1, keepdims=True) * u / (u * u).sum(1, keepdims=True)
+    w *= rng.uniform(0.8, 2.5, (n, 1)) / np.linalg.norm(w, axis=1, keepdims=True)
+    v = np.stack([c - u - w, c + u - w, c + u + w, c - u + w], axis=1).astype(np.float32)
+    h = n // 2
+    second = v[h:].reshape(-1, 3)[::-1].copy()
+    order = np.arange(4 * (n - h), dtype=np.uint32).reshape(-1, 4)[:, ::-1]
+    if flat:  # keep the winding (and so the facing) of the second half
+        second = v[h:].reshape(-1, 3).copy()
+        order = np.arange(4 * (n - h), dtype=np.uint32).reshape(-1, 4)
+    return [{"geometry": "quad", "vertices": v[:h].reshape(-1, 3),
+             "material": base["surfaces"][0]["material"]},
+            {"geometry": "quad", "vertices": second, "indices": order.copy(),
+             "material": base["surfaces"][1]["material"]}]
+
+
+@pytest.mark.parametrize("kinds", ["spheres", "cones_cylinders", "quads"])
 def test_raycast_analytic_primitives(pkg, device, oracle, kinds):
     """Spheres, cones and cylinders (their own BVH per group, each kind's
-    intersection and normal) beside triangle meshes, raycast."""
+    intersection and normal), and quads (two triangles each, the reference's
+    normal rule) beside triangle meshes, raycast."""
     sc = small_spheres(pkg, res=128, renderer="raycast")
-    extra = sphere_surfaces(sc) if kinds == "spheres" else cone_cylinder_surfaces(sc)
+    extra = {"spheres": sphere_surfaces, "cones_cylinders": cone_cylinder_surfaces,
+             "quads": quad_surfaces}[kinds](sc)
     sc["surfaces"] = sc["surfaces"] + extra
     sc["lights"] = sc["lights"] + point_and_spot_lights()[:1]
     gpu = render_gpu(pkg, device, sc)
@@ -526,6 +557,24 @@ def test_pathtrace_analytic_primitives_same_stream(pkg, device, oracle, wavefron
     sc = small_spheres(pkg, res=96, spp=8)
     sc["surfaces"] = sc["surfaces"] + sphere_surfaces(sc) + cone_cylinder_surfaces(sc)
     sc["renderer"]["wavefront"] = wavefront
+    gpu = render_gpu(pkg, device, sc)
+    _, F = render_oracle(oracle, sc)
+    assert gpu["errorFlags"] == 0
+    assert not np.isnan(gpu["color"]).any()
+    d = np.abs(gpu["color"][..., :3] - F.color[..., :3]).max(axis=-1)
+    assert float((d <= 1e-3).mean()) >= 0.97, float((d <= 1e-3).mean())
+
+
+def test_pathtrace_quads_same_stream(pkg, device, oracle):
+    """Path tracing over quads and triangles, same stream as the oracle. The
+    quads are horizontal and face one way, so the reference's normal rule
+    (quad k shaded with triangle k's normal) gives each its own normal; with
+    mixed orientations a quad can be shaded, and its bounce rays offset, along
+    another quad's normal, so that rays start on the wrong side of their
+    surface and self-hits turn on rounding (the raycast test covers that
+    rule)."""
+    sc = small_spheres(pkg, res=96, spp=8)
+    sc["surfaces"] = sc["surfaces"] + quad_surfaces(sc, flat=True)
     gpu = render_gpu(pkg, device, sc)
     _, F = render_oracle(oracle, sc)
     assert gpu["errorFlags"] == 0

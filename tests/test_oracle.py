@@ -251,6 +251,27 @@ def test_cone_closed_form(oracle):
     assert np.all(F.color[miss][:, :3] == 0.0)
 
 
+def test_quad_closed_form(oracle):
+    """Two quads seen from above: a flat one at z = 0 and a tilted one
+    (z = 0.5 x) beside it. Quad k is shaded with the normal of triangle k of
+    the geometry's tessellated list (Quad.cpp tessellation, getNormals
+    taking the geometry's primitive at the quad's index), so the tilted quad
+    (k = 1) takes triangle 1, the second triangle of the flat quad: it is
+    shaded as if flat, with depth from its own tilted plane."""
+    v = np.array([[-3, -2, 0], [-1, -2, 0], [-1, 2, 0], [-3, 2, 0],
+                  [1, -2, 0.5], [3, -2, 1.5], [3, 2, 1.5], [1, 2, 0.5]], np.float32)
+    F, X, Y = _top_view(oracle, {"geometry": "quad", "vertices": v,
+                                 "indices": np.array([[0, 1, 2, 3], [4, 5, 6, 7]], np.uint32)},
+                        size=32, height=8.0)
+    flat = (X > -2.9) & (X < -1.1) & (np.abs(Y) < 1.9)
+    tilt = (X > 1.1) & (X < 2.9) & (np.abs(Y) < 1.9)
+    up = _lit(np.array([0.0, 0.0, 1.0]))
+    assert flat.sum() > 20 and tilt.sum() > 20
+    assert np.allclose(F.color[flat][:, :3], up[None, :], atol=2e-5)
+    assert np.allclose(F.color[tilt][:, :3], up[None, :], atol=2e-5)
+    assert np.allclose(F.depth[tilt], 10.0 - 0.5 * X[tilt], rtol=1e-5)
+
+
 def test_emission_absorption_slab(oracle):
     """Constant field, TF alpha a: alpha after k steps is 1 - (1-a)^(k dt/ud)."""
     n = 16

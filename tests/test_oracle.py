@@ -272,6 +272,102 @@ def test_quad_closed_form(oracle):
     assert np.allclose(F.depth[tilt], 10.0 - 0.5 * X[tilt], rtol=1e-5)
 
 
+def _entry_t(o, d, kind, q):
+    """Float64 entry distance of the ray o + t d (t >= 0, o outside) into a
+    sphere, or into the solid capped cone / cylinder (v1, r1, v2, r2): the
+    nearest of the body's roots inside the slab and the cap discs; inf on a
+    miss. Written from the geometry, independently of the intersectors."""
+    p1, r1, p2, r2 = q[:3], q[3], q[4:7], q[7]
+    if kind == "sphere":
+        oc = o - p1
+        b, c = oc @ d, oc @ oc - r1 * r1
+        disc = b * b - c
+        if disc < 0:
+            return np.inf
+        t = -b - np.sqrt(disc)
+        return t if t >= 0 else np.inf
+    axis = p2 - p1
+    L = np.linalg.norm(axis)
+    a = axis / L
+    cands = []
+    for centre, r in ((p1, r1), (p2, r2)):  # caps
+        den = d @ a
+        if abs(den) > 1e-12:
+            t = ((centre - o) @ a) / den
+            x = o + t * d - centre
+            if t >= 0 and x @ x < r * r:
+                cands.append(t)
+    # body: |w - (w.a) a| = r1 + (r2 - r1) (w.a) / L with w = o + t d - p1
+    k = (r2 - r1) / L
+    w0 = o - p1
+    da, wa = d @ a, w0 @ a
+    dp, wp = d - da * a, w0 - wa * a
+    A = dp @ dp - (k * da) ** 2
+    B = 2 * (dp @ wp - k * da * (r1 + k * wa))
+    C = wp @ wp - (r1 + k * wa) ** 2
+    disc = B * B - 4 * A * C
+    if abs(A) > 1e-12 and disc >= 0:
+        for t in ((-B - np.sqrt(disc)) / (2 * A), (-B + np.sqrt(disc)) / (2 * A)):
+            y = wa + t * da
+            if t >= 0 and 0 < y < L and r1 + k * y >= 0:
+                cands.append(t)
+    return min(cands) if cands else np.inf
+
+
+@pytest.mark.parametrize("kind", ["sphere", "cone", "cylinder"])
+def test_analytic_intersectors_against_float64(oracle, kind):
+    """The oracle's sphere, cone and cylinder tests (the reference's cone
+    intersector, the capped-cylinder and sphere quadratics, with the origin
+    moved next to cones and cylinders) against a float64 evaluation of the
+    entry point, for rays from outside: the same hit or miss, and t within
+    1e-4 relative, except for rays grazing a silhouette."""
+    lib = oracle.load()
+    rng = np.random.default_rng({"sphere": 1, "cone": 2, "cylinder": 3}[kind])
+    n = 40
+    a = rng.uniform(-8.0, 8.0, (n, 3)).astype(np.float32)
+    b = (a + rng.uniform(-3.0, 3.0, (n, 3))).astype(np.float32)
+    if kind == "sphere":
+        surf = {"geometry": "sphere", "vertices": a, "radii": rng.uniform(0.3, 1.5, n).astype(np.float32)}
+        q = np.zeros((n, 8))
+        q[:, :3], q[:, 3] = a, surf["radii"]
+    else:
+        ends = np.stack([a, b], axis=1).reshape(-1, 3)
+        radii = rng.uniform(0.2, 1.2, 2 * n).astype(np.float32)
+        surf = {"geometry": kind, "vertices": ends}
+        q = np.zeros((n, 8))
+        q[:, :3], q[:, 4:7] = a, b
+        if kind == "cone":
+            surf["radii"] = radii
+            q[:, 3], q[:, 7] = radii[0::2], radii[1::2]
+        else:
+            surf["radii"] = radii[:n]
+            q[:, 3] = q[:, 7] = radii[:n]
+    sc = plane_scene()
+    sc["surfaces"] = [dict(surf, material={"type": "matte", "color": [0.5, 0.5, 0.5]})]
+    S = oracle.Scene(sc)
+    mismatch, checked = 0, 0
+    for _ in range(400):
+        o = rng.normal(size=3)
+        o = o / np.linalg.norm(o) * 30.0
+        target = q[rng.integers(n), :3] + rng.uniform(-1.5, 1.5, 3)
+        d = target - o
+        d /= np.linalg.norm(d)
+        o32, d32 = o.astype(np.float32), d.astype(np.float32)
+        of, df = (ctypes.c_float * 3)(*o32), (ctypes.c_float * 3)(*d32)
+        tt = ctypes.c_float(0)
+        ins, tri = ctypes.c_uint32(0), ctypes.c_uint32(0)
+        uv = (ctypes.c_float * 2)()
+        hit = lib.or_trace(S.handle, of, df, 0.0, 3.0e38, ctypes.byref(tt), ctypes.byref(ins),
+                           ctypes.byref(tri), uv)
+        ts = [_entry_t(o32.astype(np.float64), d32.astype(np.float64), kind, q[k]) for k in range(n)]
+        t64 = min(ts)
+        checked += 1
+        if hit != np.isfinite(t64) or (hit and abs(tt.value - t64) > 1e-4 * t64):
+            mismatch += 1
+    print(kind, "mismatches", mismatch, "of", checked)
+    assert checked == 400 and mismatch <= 2
+
+
 def test_emission_absorption_slab(oracle):
     """Constant field, TF alpha a: alpha after k steps is 1 - (1-a)^(k dt/ud)."""
     n = 16

@@ -12,7 +12,8 @@ namespace vsr {
 // Full = true adds the optional features (gradient shading, point and spot
 // lights).
 template <bool Count, bool Surfaces, bool Full>
-__global__ void __launch_bounds__(VSR_RAYCAST_BLOCK_X * VSR_RAYCAST_BLOCK_Y, VSR_RAYCAST_MIN_BLOCKS)
+__global__ void __launch_bounds__(VSR_RAYCAST_BLOCK_X * VSR_RAYCAST_BLOCK_Y,
+                                 Full ? VSR_RAYCAST_FULL_MIN_BLOCKS : VSR_RAYCAST_MIN_BLOCKS)
     kRaycast(DScene S, DCamera C, DRenderer R, DFrame F, int stageTF) {
   extern __shared__ float4 sTF[];
   if (stageTF) {
@@ -59,10 +60,10 @@ cudaError_t launchRaycast(const DScene &S, const DCamera &C, const DRenderer &R,
     kernel<<<grid, block, smem, stream>>>(S, C, R, F, stage);
   };
   // the full variant for gradient shading, and for point / spot lights,
-  // spheres, cones, cylinders or quads on surfaces (volume-only worlds light nothing without gradient
+  // spheres, cones, cylinders, quads or iso-surfaces on surfaces (volume-only worlds light nothing without gradient
   // shading)
   if (R.gradientShading ||
-      (S.hasSurfaces && (S.positionalLights || S.numAnalytic || S.quadGroups))) {
+      (S.hasSurfaces && (S.positionalLights || S.numAnalytic || S.quadGroups || S.numIso))) {
     if (count) launch(kRaycast<true, true, true>);
     else launch(kRaycast<false, true, true>);
   } else if (S.hasSurfaces) {
@@ -82,7 +83,7 @@ cudaError_t launchPathtrace(const DScene &S, const DCamera &C, const DRenderer &
                             bool count, cudaStream_t stream) {
   dim3 block(16, VSR_MEGA_BLOCK_Y);
   const dim3 grid = tileGrid(F, block);
-  const bool full = S.positionalLights || S.numAnalytic || S.quadGroups ||
+  const bool full = S.positionalLights || S.numAnalytic || S.quadGroups || S.numIso ||
                     (S.numVolumes > 0 && R.gradientShading);
   auto launch = [&](auto kernel) { kernel<<<grid, block, 0, stream>>>(S, C, R, F); };
   if (S.numVolumes > 0) {

@@ -559,6 +559,68 @@ __device__ __forceinline__ bool traverseGroup4(const DGroup &G, float3 o, float3
   return found;
 }
 
+// Iso-surface test, intersect(Ray, ISOSurface), DeviceCopyableObjects.h:
+// 825-911, as the reference's CPU device runs it but without its 16^3
+// empty-space grid (which only skips cells that hold no crossing): in voxel
+// space with the direction normalised, samples on the lattice anchored at
+// tmin - dt/2 (by repeated addition, dt = step * |S d|) over [tmin, tmax]
+// clipped to the field box; the first lattice interval whose two values
+// bracket an iso value (inclusive) gives the hit by linear interpolation
+// (the smallest over the iso values bracketed there; an interval bracketing
+// one with equal ends stops the march without a hit, as there). Samples use
+// the exact fp32 filter. Returns the object-space t, or -FLT_MAX. Kept out
+// of line: inlined at every surface-trace site it would take the
+// full-feature kernels from about 150 to 254 registers.
+__device__ __forceinline__ float fieldAt(const DVolume &V, float3 P, bool hw);
+static __device__ __noinline__ float isoHitT(const DIso &I, float3 o, float3 d, float tmin, float tmax,
+                                      uint32_t &err) {
+  const DVolume &V = I.field;
+  const float3 inv = f3(1.f / d.x, 1.f / d.y, 1.f / d.z);
+  const float3 t1b = (ld3(V.boundsLo) - o) * inv, t2b = (ld3(V.boundsHi) - o) * inv;
+  const float tnear = maxe(min3(t1b, t2b)), tfar = mine(max3(t1b, t2b));
+  if (!(tnear <= tfar)) return -FLT_MAX;
+  tmin = fmaxf(tmin, tnear);
+  tmax = fminf(tmax, tfar);
+  const float3 Sv = ld3(V.S);
+  const float3 ov = Sv * (o + ld3(V.T));
+  float3 dv = Sv * d;
+  const float scale = length(dv);
+  dv = normalize(dv);
+  const float t0v = tmin * scale, t1v = tmax * scale;
+  const float dt = scale * I.step;
+  if (!(dt > 0.f)) return -FLT_MAX;
+  int budget = 1 << 22;
+  float t0 = t0v - dt / 2.f, t1 = t0v - dt / 2.f;
+  while (t0 < t0v) {
+    t0 += dt;
+    if (--budget <= 0) { err |= ERR_MARCH_LIMIT; return -FLT_MAX; }
+  }
+  while (t1 < t1v) {
+    t1 += dt;
+    if (--budget <= 0) { err |= ERR_MARCH_LIMIT; return -FLT_MAX; }
+  }
+  float v1 = fieldAt(V, ov + dv * t0, false);
+  for (float t = t0; t < t1; t += dt) {
+    if (--budget <= 0) { err |= ERR_MARCH_LIMIT; return -FLT_MAX; }
+    const float v2 = fieldAt(V, ov + dv * (t + dt), false);
+    const float lo = fminf(v1, v2), hi = fmaxf(v1, v2);
+    bool hit = false;
+    float best = FLT_MAX;
+    for (int i = 0; i < I.numValues; ++i) {
+      const float iso = __ldg(I.values + i);
+      if (iso >= lo && iso <= hi) {
+        const float f = (iso - v1) / (v2 - v1);
+        const float tHit = t + dt * f;
+        if (tHit < best) best = tHit;
+        hit = true;
+      }
+    }
+    if (hit) return best < FLT_MAX ? best / scale : -FLT_MAX;
+    v1 = v2;
+  }
+  return -FLT_MAX;
+}
+
 // intersectSurfaces(Ray, TLS, shadow), DeviceCopyableObjects.h:1826-1839,
 // with intersect(Ray, Instance) :1772-1814 for the instance transform.
 template <bool Count, bool Full = false>
@@ -583,6 +645,18 @@ __device__ __forceinline__ bool traceSurfaces(const DScene &S, const Ray &r, boo
                        : traverseGroup<Count>(G, lo, ld, r.tmin, i, anyHit, h, err, cnt);
     if (Full && G.apNumNodes > 0 && !(anyHit && f))
       f = traverseGroup<Count, true>(G, lo, ld, r.tmin, i, anyHit, h, err, cnt) || f;
+    if (Full && G.numIso > 0) {
+      for (int k = 0; k < G.numIso && !(anyHit && f); ++k) {
+        const float t = isoHitT(G.isos[k], lo, ld, r.tmin, h.t, err);
+        if (!(t >= r.tmin)) continue;
+        const int local = G.numTris + G.numAP + k;
+        const bool closer = t < h.t || (t == h.t && h.inst >= 0 &&
+                                        (i < h.inst || (i == h.inst && local < h.tri)));
+        if (!closer) continue;
+        h.t = t; h.u = 0.f; h.v = 0.f; h.inst = i; h.tri = local; h.leaf = k;
+        f = true;
+      }
+    }
     if (f) {
       any = true;
       if (anyHit) break;
@@ -596,6 +670,7 @@ __device__ __forceinline__ bool traceSurfaces(const DScene &S, const Ray &r, boo
 // primitive's).
 template <bool Full>
 __device__ __forceinline__ uint32_t hitSurface(const DGroup &G, const Hit &h) {
+  if (Full && h.tri >= G.numTris + G.numAP) return G.isos[h.leaf].surface;
   if (Full && h.tri >= G.numTris) return __ldg(G.apSurface + (h.tri - G.numTris));
   return __ldg(G.triSurface + h.tri);
 }
@@ -605,10 +680,24 @@ __device__ __forceinline__ uint32_t hitSurface(const DGroup &G, const Hit &h) {
 // triangle (for a quad's triangles the stored normal of the quad); normalize((P - c) / r) for a sphere; for a cone the cap axis
 // (u <= 0, u >= 1) or the body normal from the axis parameter v; for a
 // cylinder the cap axis within the radius of an end point, else P minus
-// its projection on the axis.
+// its projection on the axis; for an iso-surface the normalised central-
+// difference field gradient (renderer/common.h:304-314; NaN where the
+// difference is zero, as there).
+__device__ __forceinline__ float3 fieldGradient(const DVolume &V, float3 P, float3 delta, bool hw);
+// (out of line for the same reason as isoHitT)
+static __device__ __noinline__ float3 isoNormal(const DIso &I, float3 P) {
+  const DVolume &V = I.field;
+  const float3 Sv = ld3(V.S);
+  return fieldGradient(V, Sv * (P + ld3(V.T)), Sv * V.cellSize, false);
+}
 template <bool Full>
 __device__ __forceinline__ float3 hitNormal(const DGroup &G, const DInstance &I, const Hit &h,
                                             float3 o, float3 d) {
+  if (Full && h.tri >= G.numTris + G.numAP) {  // iso-surface: the field gradient
+    float3 lo, ld;
+    localRay(I, o, d, lo, ld);
+    return isoNormal(G.isos[h.leaf], lo + h.t * ld);
+  }
   if (Full && h.tri >= G.numTris) {
     float3 lo, ld;
     localRay(I, o, d, lo, ld);

@@ -307,6 +307,23 @@ struct SpatialField : Object {
       hi[i] = origin[i] + ((float)dims[i] - 1.f) * spacing[i];
     }
   }
+  // the sampling part of a volume record: data, texture, bounds, voxel
+  // space (S * (p + T) maps the bounds to [0,1]^3), cellSize = min spacing
+  DVolume fieldRecord() const {
+    DVolume v{};
+    v.tex = tex;
+    v.data = data.as<float>();
+    for (int a = 0; a < 3; ++a) v.dims[a] = dims[a];
+    bounds(v.boundsLo, v.boundsHi);
+    float minSp = spacing[0];
+    for (int a = 0; a < 3; ++a) {
+      v.S[a] = 1.f / (v.boundsHi[a] - v.boundsLo[a]);
+      v.T[a] = -v.boundsLo[a];
+      minSp = std::min(minSp, spacing[a]);
+    }
+    v.cellSize = minSp;
+    return v;
+  }
 };
 
 // transferFunction1D volume, scene/volume/TransferFunction1D.cpp:22-165
@@ -430,14 +447,23 @@ struct Geometry : Object {
   int apKind = AP_SPHERE;
   // quads: the object-space shading normal of each tessellated triangle
   std::vector<float> quadNormals;
+  // iso-surface: the field and its iso values
+  SpatialField *isoField = nullptr;
+  std::vector<float> isoValues;
   using Object::Object;
   void commit() override {
     valid = false;
     v1.clear(); e1.clear(); e2.clear();
     prims.clear();
     quadNormals.clear();
+    isoField = nullptr;
+    isoValues.clear();
     if (subtype == "quad") {
       commitQuads();
+      return;
+    }
+    if (subtype == "isosurface") {
+      commitIso();
       return;
     }
     if (subtype == "sphere") {
@@ -485,6 +511,29 @@ struct Geometry : Object {
                   "'vertex.normal' is not used: shading uses the geometric normal");
     valid = true;
   }
+  // ISOSurface.cpp:19-60: a structured field ('field') and its iso values
+  // ('isovalue', FLOAT32 array)
+  void commitIso() {
+    isoField = geto<SpatialField>("field", VSR_SPATIAL_FIELD);
+    Array *iv = geto<Array>("isovalue", VSR_ARRAY1D);
+    if (!isoField) {
+      warn("no spatial field provided to isosurface geometry");
+      return;
+    }
+    if (!iv || iv->size() == 0 || iv->elemType != VSR_FLOAT32) {
+      warn("no iso values (FLOAT32 'isovalue') provided to isosurface geometry");
+      return;
+    }
+    if (!isoField->valid) {
+      warn("spatial field not valid on isosurface geometry");
+      isoField = nullptr;
+      return;
+    }
+    isoValues.assign(iv->as<float>(), iv->as<float>() + iv->size());
+    valid = true;
+  }
+  bool isIso() const { return isoField != nullptr; }
+
   // Quad.cpp:46-110: each quad (v1..v4, from primitive.index as UINT32_VEC4
   // or consecutive vertices) becomes the triangles (v1, v2-v1, v4-v1) and
   // (v3, v4-v3, v2-v3). Shading normals follow getNormals
@@ -968,6 +1017,7 @@ struct Renderer : Object {
 struct GroupGPU {
   DevBuf v1, e1, e2, nodes, nodes4, tris, triSurface, triPrim;
   DevBuf apSrc, apKinds, apNodes, apLeaf, apPrims, apLocal, apSurface, triNormal;
+  DevBuf isos, isoValues;
   int numTris = 0, numNodes = 0, width = 2;
   int numAP = 0, apNumNodes = 0;
   float buildMs = 0.f;
@@ -1110,7 +1160,7 @@ struct World : Object {
     groupsGPU.clear();
     bvhNodes = bvhTris = 0;
     bool allOpaque = true, anySurf = false;
-    int numAnalytic = 0, quadGroups = 0;
+    int numAnalytic = 0, quadGroups = 0, numIso = 0;
     for (size_t gi = 0; gi < groups.size(); ++gi) {
       Group *g = groups[gi];
       auto gg = std::make_unique<GroupGPU>();
@@ -1120,6 +1170,9 @@ struct World : Object {
       std::vector<uint32_t> apKinds, apSurf;
       std::vector<float> triNormal;  // 4 floats per triangle, w = 1 where set
       bool anyQuad = false;
+      std::vector<DIso> isos;
+      std::vector<float> isoVals;
+      std::vector<size_t> isoValOffset;
       float lo[3] = {1e30f, 1e30f, 1e30f}, hi[3] = {-1e30f, -1e30f, -1e30f};
       for (Surface *sf : g->surfaces) {
         if (!sf->valid || !sf->geom->valid || !sf->mat->valid) continue;
@@ -1127,6 +1180,21 @@ struct World : Object {
         mats.push_back(sf->mat->m);
         if (sf->mat->m.alphaMode != ALPHA_OPAQUE) allOpaque = false;
         Geometry *G = sf->geom;
+        if (G->isIso()) {
+          DIso di{};
+          di.field = G->isoField->fieldRecord();
+          di.numValues = (int)G->isoValues.size();
+          di.surface = sid;
+          di.step = 0.5f * di.field.cellSize;
+          isoValOffset.push_back(isoVals.size());
+          isoVals.insert(isoVals.end(), G->isoValues.begin(), G->isoValues.end());
+          isos.push_back(di);
+          for (int a = 0; a < 3; ++a) {
+            lo[a] = std::min(lo[a], di.field.boundsLo[a]);
+            hi[a] = std::max(hi[a], di.field.boundsHi[a]);
+          }
+          continue;
+        }
         if (G->numAnalytic()) {
           apPrims.insert(apPrims.end(), G->prims.begin(), G->prims.end());
           for (size_t k = 0; k < G->numAnalytic(); ++k) {
@@ -1249,6 +1317,24 @@ struct World : Object {
         ++quadGroups;
       }
       dg.triNormal = anyQuad ? gg->triNormal.as<float4>() : nullptr;
+      if (!isos.empty()) {
+        if (gg->isoValues.upload(isoVals.data(), isoVals.size() * sizeof(float), s)) {
+          dev->report(this, kind, VSR_SEVERITY_ERROR, VSR_ERROR_OUT_OF_MEMORY,
+                      "scene upload failed");
+          return false;
+        }
+        for (size_t k = 0; k < isos.size(); ++k)
+          isos[k].values = gg->isoValues.as<float>() + isoValOffset[k];
+        if (gg->isos.upload(isos.data(), isos.size() * sizeof(DIso), s)) {
+          dev->report(this, kind, VSR_SEVERITY_ERROR, VSR_ERROR_OUT_OF_MEMORY,
+                      "scene upload failed");
+          return false;
+        }
+        anySurf = true;
+        numIso += (int)isos.size();
+      }
+      dg.isos = gg->isos.as<DIso>();
+      dg.numIso = (int)isos.size();
       dg.apNodes = gg->apNodes.as<float4>();
       dg.apPrims = gg->apPrims.as<float4>();
       dg.apLocal = gg->apLocal.as<uint32_t>();
@@ -1362,6 +1448,7 @@ struct World : Object {
     scene.hasSurfaces = anySurf ? 1 : 0;
     scene.numAnalytic = numAnalytic;
     scene.quadGroups = quadGroups;
+    scene.numIso = numIso;
     builtStamp = deep;
     commitMs = std::chrono::duration<float, std::milli>(std::chrono::steady_clock::now() - t0).count();
     return true;
@@ -1588,10 +1675,10 @@ VSRStatus renderFrame(Device *dev, FrameObj *F) {
   const bool doRender = F->accumID < F->renderer->sampleLimit;
   const DRenderer &R = F->renderer->r;
   // the wavefront kernels have neither gradient shading nor spheres, cones,
-  // cylinders and quads: the
+  // cylinders, quads and iso-surfaces: the
   // megakernel takes such frames
   const bool wave = F->renderer->wavefront && !R.gradientShading && !W->scene.numAnalytic &&
-                    !W->scene.quadGroups;
+                    !W->scene.quadGroups && !W->scene.numIso;
   int stage = 0;
   MarchScratch ms{};
   bool segmented = false;
@@ -1784,7 +1871,8 @@ VSRStatus renderFrames(Device *dev, FrameObj *const *frames, uint32_t count) {
     j.F = F->record();
     j.kind = j.R.type != REND_RAYCAST ? JOB_PATHTRACE
              : (j.R.gradientShading ||
-                (j.S.hasSurfaces && (j.S.positionalLights || j.S.numAnalytic || j.S.quadGroups)))
+                (j.S.hasSurfaces &&
+                 (j.S.positionalLights || j.S.numAnalytic || j.S.quadGroups || j.S.numIso)))
                  ? JOB_RAYCAST_FULL
              : j.S.hasSurfaces        ? JOB_RAYCAST_SURFACES
                                       : JOB_RAYCAST_VOLUME;
@@ -1796,7 +1884,7 @@ VSRStatus renderFrames(Device *dev, FrameObj *const *frames, uint32_t count) {
                            (uint64_t)j.kind, (uint64_t)j.R.pixelSamples, (uint64_t)j.R.maxBounce,
                            (uint64_t)j.S.numVolumes, (uint64_t)j.R.gradientShading,
                            (uint64_t)j.S.positionalLights, (uint64_t)j.S.numAnalytic,
-                           (uint64_t)j.S.quadGroups});
+                           (uint64_t)j.S.quadGroups, (uint64_t)j.S.numIso});
   }
   if (!batched.empty()) {
     BatchTuner &tuner = B.tuners[key];
@@ -1858,7 +1946,7 @@ VSRStatus renderFrames(Device *dev, FrameObj *const *frames, uint32_t count) {
     for (const DJob &j : jobs)
       if (j.kind == JOB_PATHTRACE) {
         if (j.S.numVolumes > 0) L.pathtraceVariant |= 1;
-        if (j.S.positionalLights || j.S.numAnalytic || j.S.quadGroups ||
+        if (j.S.positionalLights || j.S.numAnalytic || j.S.quadGroups || j.S.numIso ||
             (j.S.numVolumes > 0 && j.R.gradientShading))
           L.pathtraceVariant |= 2;
       }
@@ -2073,7 +2161,8 @@ VSRObject vsrNewVolume(VSRDevice d, const char *s) {
   return newObj<Volume>(d, VSR_VOLUME, s, {"transferFunction1D"});
 }
 VSRObject vsrNewGeometry(VSRDevice d, const char *s) {
-  return newObj<Geometry>(d, VSR_GEOMETRY, s, {"triangle", "quad", "sphere", "cone", "cylinder"});
+  return newObj<Geometry>(d, VSR_GEOMETRY, s,
+                         {"triangle", "quad", "sphere", "cone", "cylinder", "isosurface"});
 }
 VSRObject vsrNewMaterial(VSRDevice d, const char *s) {
   return newObj<Material>(d, VSR_MATERIAL, s, {"matte", "physicallyBased"});

@@ -69,6 +69,9 @@ constexpr int kMaxSurfaceLayers = 1 << 12;
 #ifndef VSR_RAYCAST_MIN_BLOCKS
 #define VSR_RAYCAST_MIN_BLOCKS 1
 #endif
+#ifndef VSR_RAYCAST_FULL_MIN_BLOCKS
+#define VSR_RAYCAST_FULL_MIN_BLOCKS 3  // the full-feature variant: at most 168 registers
+#endif
 #ifndef VSR_RAYCAST_BLOCK_X
 #define VSR_RAYCAST_BLOCK_X 16  // raycast tile: VSR_RAYCAST_BLOCK_X x VSR_RAYCAST_BLOCK_Y pixels
 #endif
@@ -138,6 +141,16 @@ struct DVolume {
 constexpr int kEmptyChild = 0x7fffffff;
 
 enum AnalyticKind { AP_SPHERE = 0, AP_CONE = 1, AP_CYLINDER = 2 };
+
+// An iso-surface of a structured field (ISOSurface.cpp): the field as a
+// volume record (its TF fields unused), the iso values, the surface index.
+struct DIso {
+  DVolume field;
+  const float *values;
+  int numValues;
+  uint32_t surface;
+  float step;  // march step in world units: min(spacing) / 2
+};
 constexpr int kApKindShift = 28;
 constexpr uint32_t kApLocalMask = (1u << kApKindShift) - 1u;
 
@@ -167,6 +180,10 @@ struct DGroup {
   const uint32_t *apSurface;
   int numAP;
   int apNumNodes;
+  // iso-surfaces of the group; a hit on iso-surface k carries
+  // Hit::tri = numTris + numAP + k and Hit::leaf = k
+  const DIso *isos;
+  int numIso;
 };
 
 struct DInstance {
@@ -190,6 +207,7 @@ struct DScene {
   int positionalLights;  // point and spot lights among them: the kernels' full variants
   int numAnalytic;       // spheres, cones, cylinders in all groups: the kernels' full variants
   int quadGroups;        // groups with quad geometry (triNormal set): the full variants
+  int numIso;            // iso-surfaces in all groups: the full variants
   int numVolumes;
   int allOpaque;
   int hasSurfaces;

@@ -9,6 +9,8 @@ is fixed in each generator. A scene is a plain dict:
               {"geometry": "sphere", "vertices": (V,3) f32 centres, "indices": (N,) u32
                (optional), "radii": (N,) f32 (optional), "radius": f32 (default 0.01),
                "material": {...}} |
+              {"geometry": "isosurface", "data": (nz,ny,nx) f32, "origin", "spacing",
+               "isovalues": [...], "material": {...}} |
               {"geometry": "quad", "vertices": (V,3) f32, "indices": (Q,4) u32 (optional,
                else consecutive quadruples), "material": {...}} |
               {"geometry": "cone" | "cylinder", "vertices": (V,3) f32 end points,
@@ -317,6 +319,26 @@ def _surfaces(dev, surfs, keep):
     for s in surfs:
         kind = s.get("geometry", "triangle")
         g = dev.geometry(kind)
+        if kind == "isosurface":
+            f = dev.spatial_field("structuredRegular")
+            da = dev.array3d(np.asarray(s["data"], np.float32))
+            dev.set(f, "data", da)
+            dev.set(f, "origin", s.get("origin", [0.0, 0.0, 0.0]), vsr.FLOAT32_VEC3)
+            dev.set(f, "spacing", s.get("spacing", [1.0, 1.0, 1.0]), vsr.FLOAT32_VEC3)
+            dev.commit(f)
+            iv = dev.array1d(np.asarray(s["isovalues"], np.float32).reshape(-1))
+            dev.set(g, "field", f)
+            dev.set(g, "isovalue", iv)
+            dev.commit(g)
+            keep += [f, da, iv]
+            mat = _material(dev, s["material"])
+            sf = dev.surface()
+            dev.set(sf, "geometry", g)
+            dev.set(sf, "material", mat)
+            dev.commit(sf)
+            keep += [g, mat]
+            out.append(sf)
+            continue
         va = dev.array1d(np.asarray(s["vertices"], np.float32))
         dev.set(g, "vertex.position", va)
         keep += [va]

@@ -351,6 +351,7 @@ void buildMajorants(Vol &vol) {
 struct Scene {
   const OrScene *src;
   std::vector<Tri> tris;
+  std::vector<Vol> isoFields;  // the iso-surfaces' fields (bounds and voxel space)
   std::vector<f3> triNormal;   // quads: the shading normal per triangle (empty if none)
   std::vector<char> hasNormal;
   std::vector<GroupBVH> bvh;
@@ -377,6 +378,7 @@ struct SurfHit {
   float t = FLT_MAX, u = 0, v = 0;
   int inst = -1, tri = -1;  // tri: global triangle index, -1 otherwise
   int prim = -1;            // global sphere / cone / cylinder index, -1 otherwise
+  int iso = -1;             // global iso-surface index, -1 otherwise
   int key = -1;             // order within the instance: triangles, then spheres
   f3 isect_pos;             // instance-local hit position
 };
@@ -471,6 +473,53 @@ inline bool hitTri(const Ray &r, const Tri &T, float tmin, float &t, float &u, f
   return true;
 }
 
+// Iso-surface test, intersect(Ray, ISOSurface), DeviceCopyableObjects.h:
+// 825-911, as the reference's CPU device runs it but without its 16^3
+// empty-space grid (which only skips cells that hold no crossing): in voxel
+// space with the direction normalised, samples on the lattice anchored at
+// tmin - dt/2 (by repeated addition, dt = (min spacing / 2) |S d|) over
+// [tmin, tmax] clipped to the field box; the first lattice interval whose
+// values bracket an iso value (inclusive) gives the hit by linear
+// interpolation (the smallest over the values bracketed there; an interval
+// bracketing one with equal ends stops the march without a hit). Returns
+// the object-space t or -FLT_MAX.
+float hitIso(const Vol &vol, const OrIso &iso, const Ray &l, float tmax) {
+  BoxHit bh = intersectBox(l, vol.bounds);
+  if (!bh.hit) return -FLT_MAX;
+  const float tmin = std::fmax(l.tmin, bh.tnear);
+  tmax = std::fmin(tmax, bh.tfar);
+  f3 ov = vol.pointToVoxelSpace(l.ori), dv = vol.vectorToVoxelSpace(l.dir);
+  const float scale = length(dv);
+  dv = normalize(dv);
+  const float t0v = tmin * scale, t1v = tmax * scale;
+  const float dt = scale * (0.5f * vol.cellSize);
+  if (!(dt > 0.f)) return -FLT_MAX;
+  long budget = 1 << 22;
+  float t0 = t0v - dt / 2.f, t1 = t0v - dt / 2.f;
+  while (t0 < t0v) { t0 += dt; if (--budget <= 0) return -FLT_MAX; }
+  while (t1 < t1v) { t1 += dt; if (--budget <= 0) return -FLT_MAX; }
+  float v1 = sampleField(vol.v, ov + dv * t0);
+  for (float t = t0; t < t1; t += dt) {
+    if (--budget <= 0) return -FLT_MAX;
+    float v2 = sampleField(vol.v, ov + dv * (t + dt));
+    float lo = std::fmin(v1, v2), hi = std::fmax(v1, v2);
+    bool hit = false;
+    float best = FLT_MAX;
+    for (int i = 0; i < iso.numValues; ++i) {
+      float x = iso.values[i];
+      if (x >= lo && x <= hi) {
+        float f = (x - v1) / (v2 - v1);
+        float tHit = t + dt * f;
+        if (tHit < best) best = tHit;
+        hit = true;
+      }
+    }
+    if (hit) return best < FLT_MAX ? best / scale : -FLT_MAX;
+    v1 = v2;
+  }
+  return -FLT_MAX;
+}
+
 // Closest hit over all instances: intersectSurfaces(Ray,TLS) with the
 // instance transform of intersect(Ray, Instance), DeviceCopyableObjects.h:
 // 1772-1839. Hits are ordered by (t, instance, triangle).
@@ -513,7 +562,21 @@ SurfHit traceSurfaces(const Scene &sc, const Ray &ray, Counters &c) {
                      ((int)ii < best.inst || ((int)ii == best.inst && key < best.key)));
       if (!closer) continue;
       best.hit = true; best.t = t; best.u = u; best.v = v;
-      best.inst = (int)ii; best.tri = -1; best.prim = k; best.key = key;
+      best.inst = (int)ii; best.tri = -1; best.prim = k; best.iso = -1; best.key = key;
+      best.isect_pos = l.ori + t * l.dir;
+    }
+    // iso-surfaces of the group, after its triangles and analytic primitives
+    for (int k = og.isoBegin; k < og.isoEnd; ++k) {
+      c.tris++;
+      float t = hitIso(sc.isoFields[k], sc.src->isos[k], l, best.t);
+      if (!(t >= l.tmin)) continue;
+      int key = (og.triEnd - og.triBegin) + (og.apEnd - og.apBegin) + (k - og.isoBegin);
+      bool closer = t < best.t ||
+                    (t == best.t && best.hit &&
+                     ((int)ii < best.inst || ((int)ii == best.inst && key < best.key)));
+      if (!closer) continue;
+      best.hit = true; best.t = t; best.u = 0.f; best.v = 0.f;
+      best.inst = (int)ii; best.tri = -1; best.prim = -1; best.iso = k; best.key = key;
       best.isect_pos = l.ori + t * l.dir;
     }
     if (bvh.nodes.empty()) continue;
@@ -540,7 +603,7 @@ SurfHit traceSurfaces(const Scene &sc, const Ray &ray, Counters &c) {
                          ((int)ii < best.inst || ((int)ii == best.inst && key < best.key)));
           if (!closer) continue;
           best.hit = true; best.t = t; best.u = u; best.v = v;
-          best.inst = (int)ii; best.tri = tri; best.prim = -1; best.key = key;
+          best.inst = (int)ii; best.tri = tri; best.prim = -1; best.iso = -1; best.key = key;
           best.isect_pos = l.ori + t * l.dir;
         }
       } else {
@@ -560,10 +623,18 @@ SurfHit traceSurfaces(const Scene &sc, const Ray &ray, Counters &c) {
 // for a cylinder the cap axis within the radius of an end point, else P
 // minus its projection on the axis.
 uint32_t hitSurface(const OrScene &S, const SurfHit &h) {
+  if (h.iso >= 0) return S.isos[h.iso].surface;
   return h.prim >= 0 ? S.primSurface[h.prim] : S.triSurface[h.tri];
 }
 
+f3 fieldGradient(const OrVolume *v, f3 P, f3 delta);
+f3 gradientDelta(const Vol &vol);
+
 f3 hitNormal(const Scene &sc, const SurfHit &h) {
+  if (h.iso >= 0) {  // the normalised field gradient (NaN for a zero difference)
+    const Vol &vol = sc.isoFields[h.iso];
+    return fieldGradient(vol.v, vol.pointToVoxelSpace(h.isect_pos), gradientDelta(vol));
+  }
   if (h.prim >= 0) {
     const float *q = sc.src->prims + 8 * (size_t)h.prim;
     const f3 P = h.isect_pos, v1(q[0], q[1], q[2]), v2(q[4], q[5], q[6]);
@@ -1693,6 +1764,19 @@ Scene *commit(const OrScene *s) {
     v.T = -v.bounds.lo;
     v.cellSize = min_element(sp);
     buildMajorants(v);
+  }
+  sc->isoFields.resize(s->numIsos);
+  for (int i = 0; i < s->numIsos; ++i) {
+    Vol &v = sc->isoFields[i];
+    v.v = &s->isoFields[s->isos[i].field];
+    f3 org(v.v->origin[0], v.v->origin[1], v.v->origin[2]);
+    f3 sp(v.v->spacing[0], v.v->spacing[1], v.v->spacing[2]);
+    f3 dims((float)v.v->dims[0], (float)v.v->dims[1], (float)v.v->dims[2]);
+    v.bounds.lo = org;
+    v.bounds.hi = org + (dims - f3(1.f)) * sp;
+    v.S = f3(1.f) / (v.bounds.hi - v.bounds.lo);
+    v.T = -v.bounds.lo;
+    v.cellSize = min_element(sp);
   }
   sc->insts.resize(s->numInstances);
   for (int i = 0; i < s->numInstances; ++i) {

@@ -45,7 +45,12 @@ class OrVolume(ctypes.Structure):
 
 class OrGroup(ctypes.Structure):
     _fields_ = [("triBegin", c_int32), ("triEnd", c_int32), ("volBegin", c_int32), ("volEnd", c_int32),
-                ("apBegin", c_int32), ("apEnd", c_int32)]
+                ("apBegin", c_int32), ("apEnd", c_int32), ("isoBegin", c_int32),
+                ("isoEnd", c_int32)]
+
+
+class OrIso(ctypes.Structure):
+    _fields_ = [("field", c_int32), ("numValues", c_int32), ("values", FP), ("surface", c_uint32)]
 
 
 class OrInstance(ctypes.Structure):
@@ -67,7 +72,9 @@ class OrScene(ctypes.Structure):
                 ("numInstances", c_int32), ("instances", ctypes.POINTER(OrInstance)),
                 ("numLights", c_int32), ("lights", ctypes.POINTER(OrLight)),
                 ("numPrims", c_int32), ("prims", FP), ("primKind", ctypes.POINTER(c_int32)),
-                ("primSurface", UP), ("triNormalFrom", ctypes.POINTER(c_int32))]
+                ("primSurface", UP), ("triNormalFrom", ctypes.POINTER(c_int32)),
+                ("numIsos", c_int32), ("isos", ctypes.POINTER(OrIso)),
+                ("isoFields", ctypes.POINTER(OrVolume))]
 
 
 class OrCamera(ctypes.Structure):
@@ -246,12 +253,33 @@ class Scene:
         verts, tsurf, tprim, mats, vols, ogroups, oinsts, lights = [], [], [], [], [], [], [], []
         aps, akind, asurf = [], [], []
         nfrom, has_quads = [], False
+        isos, iso_fields = [], []
         ntri = nap = 0
         for gi, (surfs, vls, lts, xfm) in enumerate(groups):
             g = OrGroup()
             g.triBegin = ntri
             g.apBegin = nap
+            g.isoBegin = len(isos)
             for s in surfs:
+                if s.get("geometry") == "isosurface":
+                    data = np.ascontiguousarray(s["data"], np.float32)
+                    vals = np.ascontiguousarray(s["isovalues"], np.float32).reshape(-1)
+                    self._keep += [data, vals]
+                    ov = OrVolume()
+                    ov.data = fptr(data)
+                    nz, ny, nx = data.shape
+                    ov.dims = (c_int32 * 3)(nx, ny, nz)
+                    ov.origin = farr(3, s.get("origin", [0, 0, 0]))
+                    ov.spacing = farr(3, s.get("spacing", [1, 1, 1]))
+                    oi = OrIso()
+                    oi.field = len(iso_fields)
+                    oi.numValues = len(vals)
+                    oi.values = fptr(vals)
+                    oi.surface = len(mats)
+                    mats.append(material(s["material"]))
+                    iso_fields.append(ov)
+                    isos.append(oi)
+                    continue
                 kind = s.get("geometry", "triangle")
                 if kind in ("sphere", "cone", "cylinder"):
                     q = analytic_prims(s)
@@ -282,6 +310,7 @@ class Scene:
                 ntri += len(t)
             g.triEnd = ntri
             g.apEnd = nap
+            g.isoEnd = len(isos)
             g.volBegin = len(vols)
             for v in vls:
                 ov = OrVolume()
@@ -373,6 +402,11 @@ class Scene:
         sc.primSurface = asf.ctypes.data_as(UP)
         sc.triNormalFrom = (nf.ctypes.data_as(ctypes.POINTER(c_int32)) if has_quads
                             else ctypes.POINTER(c_int32)())
+        self.isos = (OrIso * max(1, len(isos)))(*isos)
+        self.iso_fields = (OrVolume * max(1, len(iso_fields)))(*iso_fields)
+        sc.numIsos = len(isos)
+        sc.isos = self.isos
+        sc.isoFields = self.iso_fields
         self.scene = sc
         self.handle = lib.or_scene_commit(ctypes.byref(sc))
         self.camera = camera(scene["camera"])

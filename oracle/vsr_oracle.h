@@ -57,7 +57,15 @@ typedef struct OrGroup {
   int32_t triBegin, triEnd; /* range in the scene's triangle array */
   int32_t volBegin, volEnd; /* range in the scene's volume array */
   int32_t apBegin, apEnd;   /* range in the scene's sphere / cone / cylinder array */
+  int32_t isoBegin, isoEnd; /* range in the scene's iso-surface array */
 } OrGroup;
+
+typedef struct OrIso {
+  int32_t field;            /* index into OrScene::isoFields (TF fields unused) */
+  int32_t numValues;
+  const float *values;
+  uint32_t surface;         /* surface index */
+} OrIso;
 
 typedef struct OrInstance {
   float xfm[12];            /* column-major 3x4 affine: 3 columns + translation */
@@ -102,6 +110,9 @@ typedef struct OrScene {
   const uint32_t *primSurface;   /* surface index per primitive */
   const int32_t *triNormalFrom;  /* per triangle: the triangle whose e1 x e2 is its shading
                                     normal (quads), -1 for its own; may be null */
+  int32_t numIsos;
+  const OrIso *isos;
+  const OrVolume *isoFields;     /* one per iso-surface */
 } OrScene;
 
 typedef struct OrCamera {

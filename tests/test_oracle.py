@@ -368,6 +368,61 @@ def test_analytic_intersectors_against_float64(oracle, kind):
     assert checked == 400 and mismatch <= 2
 
 
+def test_isosurface_plane_closed_form(oracle):
+    """A field rising linearly along z (16^3 nodes over [0,15]^3) with iso
+    value 0.5 seen from above: with texel centres at (i + 0.5) / N the level
+    set is the mid plane z = 7.5 exactly, linear interpolation along the ray
+    is exact there, and the normal is the gradient direction +z."""
+    n = 16
+    ramp = np.linspace(0.0, 1.0, n, dtype=np.float32)
+    data = np.ascontiguousarray(np.broadcast_to(ramp[:, None, None], (n, n, n)))
+    sc = plane_scene()
+    sc["surfaces"] = [{"geometry": "isosurface", "data": data, "origin": [0.0, 0.0, 0.0],
+                       "spacing": [1.0, 1.0, 1.0], "isovalues": [0.5],
+                       "material": {"type": "matte", "color": [0.6, 0.5, 0.4]}}]
+    sc["camera"] = {"type": "orthographic", "position": [7.5, 7.5, 40.0],
+                    "direction": [0.0, 0.0, -1.0], "up": [0.0, 1.0, 0.0], "height": 12.0,
+                    "aspect": 1.0}
+    S = oracle.Scene(sc)
+    F = oracle.Frame(16, 16)
+    oracle.render(S, F)
+    assert np.allclose(F.depth, 40.0 - 7.5, rtol=1e-5)
+    assert np.allclose(F.normal, [0.0, 0.0, 1.0], atol=1e-5)
+    assert np.allclose(F.color[..., :3], _lit(np.array([0.0, 0.0, 1.0]))[None, None, :], atol=2e-5)
+
+
+def test_isosurface_sphere(oracle):
+    """A distance field |p - c| (sampled at the texel centres of a 32^3 field
+    over [0,31]^3) with two iso values 6 and 9: seen from above, the hits lie
+    on the radius-9 sphere (the outer level set is met first) to trilinear
+    accuracy, with radial normals; rays missing it hit nothing."""
+    n, c = 32, np.array([15.5, 15.5, 15.5])
+    w = (np.arange(n) + 0.5) / n * 31.0
+    Z, Y, X = np.meshgrid(w, w, w, indexing="ij")
+    data = np.sqrt((X - c[0]) ** 2 + (Y - c[1]) ** 2 + (Z - c[2]) ** 2).astype(np.float32)
+    sc = plane_scene()
+    sc["surfaces"] = [{"geometry": "isosurface", "data": data, "origin": [0.0, 0.0, 0.0],
+                       "spacing": [1.0, 1.0, 1.0], "isovalues": [6.0, 9.0],
+                       "material": {"type": "matte", "color": [0.6, 0.5, 0.4]}}]
+    sc["camera"] = {"type": "orthographic", "position": [15.5, 15.5, 60.0],
+                    "direction": [0.0, 0.0, -1.0], "up": [0.0, 1.0, 0.0], "height": 24.0,
+                    "aspect": 1.0}
+    S = oracle.Scene(sc)
+    F = oracle.Frame(24, 24)
+    oracle.render(S, F)
+    xs = 15.5 + ((np.arange(24) + 0.5) / 24 - 0.5) * 24.0
+    X2, Y2 = np.meshgrid(xs, xs)
+    rho2 = (X2 - c[0]) ** 2 + (Y2 - c[1]) ** 2
+    inside, outside = rho2 < 8.0 ** 2, rho2 > 9.6 ** 2
+    P = np.stack([X2, Y2, 60.0 - F.depth], axis=-1)
+    r = np.linalg.norm(P - c, axis=-1)
+    assert inside.sum() > 100 and outside.sum() > 50
+    assert np.all(np.abs(r[inside] - 9.0) < 0.05)
+    radial = (P - c) / r[..., None]
+    assert np.all(np.abs(F.normal[inside] - radial[inside]) < 0.02)
+    assert np.all(F.depth[outside] > 1e30)
+
+
 def test_emission_absorption_slab(oracle):
     """Constant field, TF alpha a: alpha after k steps is 1 - (1-a)^(k dt/ud)."""
     n = 16

@@ -599,6 +599,42 @@ def test_instanced_analytic_primitives(pkg, device, oracle):
     assert good, frac
 
 
+def iso_surface(pkg, seed=7):
+    """A two-level iso-surface of a 40^3 blob field over [-8,8]^3."""
+    rng = np.random.default_rng(seed)
+    return {"geometry": "isosurface", "data": pkg.scenes.blob_field(40, rng),
+            "origin": [-8.0, -8.0, -8.0], "spacing": [16.0 / 39] * 3, "isovalues": [0.3, 0.6],
+            "material": {"type": "matte", "color": [0.3, 0.7, 0.4]}}
+
+
+def test_raycast_isosurface(pkg, device, oracle):
+    """Iso-surfaces of a structured field (the lattice march and the
+    gradient normal) beside triangle meshes, raycast."""
+    sc = small_spheres(pkg, res=96, renderer="raycast")
+    sc["surfaces"] = sc["surfaces"] + [iso_surface(pkg)]
+    gpu = render_gpu(pkg, device, sc)
+    _, F = render_oracle(oracle, sc)
+    assert gpu["errorFlags"] == 0
+    good, frac = raycast_ok(gpu, F)
+    assert good, frac
+    hit = (F.depth < 1e30) & (gpu["depth"] < 1e30)
+    rel = np.abs(gpu["depth"][hit] - F.depth[hit]) / F.depth[hit]
+    assert float((rel <= 1e-4).mean()) >= 0.999
+
+
+def test_pathtrace_isosurface_same_stream(pkg, device, oracle):
+    """Path tracing over an iso-surface and triangles, same stream as the
+    oracle."""
+    sc = small_spheres(pkg, res=96, spp=8)
+    sc["surfaces"] = sc["surfaces"] + [iso_surface(pkg)]
+    gpu = render_gpu(pkg, device, sc)
+    _, F = render_oracle(oracle, sc)
+    assert gpu["errorFlags"] == 0
+    assert not np.isnan(gpu["color"]).any()
+    d = np.abs(gpu["color"][..., :3] - F.color[..., :3]).max(axis=-1)
+    assert float((d <= 1e-3).mean()) >= 0.97, float((d <= 1e-3).mean())
+
+
 def test_wavefront_equals_megakernel(pkg, device):
     """The two execution modes produce the same frame (same stream, same math)."""
     sc = small_spheres(pkg, res=96, spp=4, n=16)

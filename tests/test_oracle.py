@@ -423,6 +423,36 @@ def test_isosurface_sphere(oracle):
     assert np.all(F.depth[outside] > 1e30)
 
 
+def test_instanced_lights_match_transformed_world_lights(oracle):
+    """xfmLight (DeviceCopyableObjects.h:2398-2430): a point and a spot light
+    inside an instance (rotation about z, scale 1.5, translation) light the
+    scene as world-level lights at the transformed position and axis."""
+    c, s_ = np.cos(0.7), np.sin(0.7)
+    R = np.array([[c, -s_, 0.0], [s_, c, 0.0], [0.0, 0.0, 1.0]]) * 1.5
+    t = np.array([0.5, -1.0, 0.25])
+    xfm = list(R.T.reshape(-1)) + list(t)  # column-major 3x4
+    lights = [{"type": "point", "position": [0.4, 0.2, 2.0], "intensity": 6.0},
+              {"type": "spot", "position": [-0.3, 0.1, 2.5], "direction": [0.1, 0.0, -1.0],
+               "openingAngle": 0.8, "falloffAngle": 0.2, "intensity": 9.0}]
+    moved = []
+    for L in lights:
+        L2 = dict(L, position=list(R @ np.array(L["position"]) + t))
+        if "direction" in L:
+            L2["direction"] = list(R @ np.array(L["direction"]))
+        moved.append(L2)
+    images = []
+    for world, inst in ((moved, []), ([], lights)):
+        sc = plane_scene()
+        sc["lights"] = world
+        sc["instances"] = [{"transform": xfm, "lights": inst}] if inst else []
+        S = oracle.Scene(sc)
+        F = oracle.Frame(16, 16)
+        oracle.render(S, F)
+        images.append(F.color.copy())
+    assert images[0][..., :3].max() > 0.2
+    assert np.allclose(images[0], images[1], atol=1e-5)
+
+
 def test_emission_absorption_slab(oracle):
     """Constant field, TF alpha a: alpha after k steps is 1 - (1-a)^(k dt/ud)."""
     n = 16

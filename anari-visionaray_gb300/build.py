@@ -1,4 +1,5 @@
-"""Build the renderer core library (libvsr.so) in-tree for sm_103a.
+"""Build the renderer core library (libvsr.so) in-tree for sm_103a, and
+libvsr_probe.so (single device functions behind test entry points).
 
 Compiles the CUDA translation units with nvcc and the host runtime with g++
 in parallel, then links one shared library next to this file. Objects go to
@@ -14,6 +15,9 @@ ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 OBJ = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libvsr.so")
+# probe entry points of single device functions, loaded by tests only
+PROBE_LIB = os.path.join(HERE, "libvsr_probe.so")
+PROBE_SOURCES = ["probe.cu"]
 INCLUDE = os.path.join(ROOT, "include")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
@@ -65,6 +69,12 @@ def build(verbose=False):
         objs.append(obj)
         if _stale(src, obj, dep):
             jobs.append([nvcc, *NVCC_FLAGS, "-c", src, "-o", obj])
+    probe_objs = []
+    for s in PROBE_SOURCES:
+        src, obj = os.path.join(CSRC, s), os.path.join(OBJ, s + ".o")
+        probe_objs.append(obj)
+        if _stale(src, obj, dep):
+            jobs.append([nvcc, *NVCC_FLAGS, "-c", src, "-o", obj])
     for s in CPP_SOURCES:
         src, obj = os.path.join(CSRC, s), os.path.join(OBJ, s + ".o")
         objs.append(obj)
@@ -75,6 +85,8 @@ def build(verbose=False):
             f.result()
     if jobs or not os.path.exists(LIB):
         _run([nvcc, "-shared", *ARCH, "-o", LIB, *objs], verbose)
+    if jobs or not os.path.exists(PROBE_LIB):
+        _run([nvcc, "-shared", *ARCH, "-o", PROBE_LIB, *probe_objs], verbose)
     return LIB
 
 

@@ -1121,6 +1121,70 @@ __device__ __forceinline__ int projectOnGrid1(float v, float lo, float hi, int n
   return min(max(c, 0), n - 1);
 }
 
+// dda3, renderer/DDA.h:12-113, with projectOnGrid and linearIndex
+// (scene/volume/spatial_field/GridAccel-common.h:9-25): walks the cells of
+// a gx x gy x gz grid spanning [blo, bhi] that the ray o + t d crosses from
+// tmin on, calling cell(id, t0, t1) with id = (z gy + y) gx + x for each
+// until it returns false or the walk leaves the grid (t1 is clipped to
+// tmax; the walk itself goes on past tmax, as the reference's does). A walk
+// of more than 4 (gx + gy + gz) + 16 cells sets ERR_DDA_LIMIT and stops.
+// The two products that a compiler would fuse into multiply-adds (the
+// moved origin and the first cell boundaries) are rounded separately, as
+// in the reference's own (uncontracted) arithmetic, so the walk visits the
+// same cells at the same parameters bit for bit.
+template <typename CellFn>
+__device__ __forceinline__ void ddaWalk(float3 o, float3 d, float tmin, float tmax, float3 blo,
+                                        float3 bhi, int gx, int gy, int gz, uint32_t &err,
+                                        CellFn &&cell) {
+  const float ray_tmin = tmin;
+  const float3 ro = f3(__fadd_rn(o.x, __fmul_rn(tmin, d.x)), __fadd_rn(o.y, __fmul_rn(tmin, d.y)),
+                       __fadd_rn(o.z, __fmul_rn(tmin, d.z)));
+  const float rtmax = tmax - ray_tmin;
+  const float3 rcp = f3(1.f) / d;
+  const float3 lo = (blo - ro) * rcp;
+  const float3 hi = (bhi - ro) * rcp;
+  float3 tnear = min3(lo, hi);
+  const float3 tfar = max3(lo, hi);
+  if (d.x == 0.f) tnear.x = FLT_MAX;
+  if (d.y == 0.f) tnear.y = FLT_MAX;
+  if (d.z == 0.f) tnear.z = FLT_MAX;
+  int cx = projectOnGrid1(ro.x, blo.x, bhi.x, gx);
+  int cy = projectOnGrid1(ro.y, blo.y, bhi.y, gy);
+  int cz = projectOnGrid1(ro.z, blo.z, bhi.z, gz);
+  const float3 dist = max3(f3(0.f), (tfar - tnear) / f3((float)gx, (float)gy, (float)gz));
+  const int stx = d.x > 0.f ? 1 : -1, sty = d.y > 0.f ? 1 : -1, stz = d.z > 0.f ? 1 : -1;
+  const int spx = d.x > 0.f ? gx : -1, spy = d.y > 0.f ? gy : -1, spz = d.z > 0.f ? gz : -1;
+  float3 tnext;
+  tnext.x = __fadd_rn(tnear.x, __fmul_rn(float(d.x > 0.f ? cx + 1 : gx - cx), dist.x));
+  tnext.y = __fadd_rn(tnear.y, __fmul_rn(float(d.y > 0.f ? cy + 1 : gy - cy), dist.y));
+  tnext.z = __fadd_rn(tnear.z, __fmul_rn(float(d.z > 0.f ? cz + 1 : gz - cz), dist.z));
+  float t0 = 0.f;
+  int steps = 4 * (gx + gy + gz) + 16;
+  while (true) {
+    if (--steps < 0) { err |= ERR_DDA_LIMIT; break; }
+    const float t1 = fminf(mine(tnext), rtmax);
+    const int id = (cz * gy + cy) * gx + cx;
+    if (!cell(id, ray_tmin + t0, ray_tmin + t1)) break;
+    const float tc = mine(tnext);
+    if (tnext.x == tc) {
+      tnext.x += dist.x;
+      cx += stx;
+      if (cx == spx) break;
+    }
+    if (tnext.y == tc) {
+      tnext.y += dist.y;
+      cy += sty;
+      if (cy == spy) break;
+    }
+    if (tnext.z == tc) {
+      tnext.z += dist.z;
+      cz += stz;
+      if (cz == spz) break;
+    }
+    t0 = t1;
+  }
+}
+
 // Delta tracking through one volume: intersect(Ray, Volume),
 // DeviceCopyableObjects.h:680-796, with the DDA of renderer/DDA.h:12-113
 // over the majorant grid (voxel-space bounds [0,1]^3). Returns true on a
@@ -1172,53 +1236,7 @@ __device__ bool deltaTrack(const DVolume &V, float3 o, float3 d, float tmin, flo
 
   if (V.majorant) {
     // dda3 with modelBounds = [0,1]^3 in voxel space
-    const float ray_tmin = tmin;
-    const float3 ro = o + tmin * d;
-    const float rtmax = tmax - ray_tmin;
-    const float3 rcp = f3(1.f) / d;
-    const float3 lo = (f3(0.f) - ro) * rcp;
-    const float3 hi = (f3(1.f) - ro) * rcp;
-    float3 tnear = min3(lo, hi);
-    const float3 tfar = max3(lo, hi);
-    if (d.x == 0.f) tnear.x = FLT_MAX;
-    if (d.y == 0.f) tnear.y = FLT_MAX;
-    if (d.z == 0.f) tnear.z = FLT_MAX;
-    const int gx = V.gdims[0], gy = V.gdims[1], gz = V.gdims[2];
-    int cx = projectOnGrid1(ro.x, 0.f, 1.f, gx);
-    int cy = projectOnGrid1(ro.y, 0.f, 1.f, gy);
-    int cz = projectOnGrid1(ro.z, 0.f, 1.f, gz);
-    const float3 dist = max3(f3(0.f), (tfar - tnear) / f3((float)gx, (float)gy, (float)gz));
-    const int stx = d.x > 0.f ? 1 : -1, sty = d.y > 0.f ? 1 : -1, stz = d.z > 0.f ? 1 : -1;
-    const int spx = d.x > 0.f ? gx : -1, spy = d.y > 0.f ? gy : -1, spz = d.z > 0.f ? gz : -1;
-    float3 tnext;
-    tnext.x = d.x > 0.f ? tnear.x + float(cx + 1) * dist.x : tnear.x + float(gx - cx) * dist.x;
-    tnext.y = d.y > 0.f ? tnear.y + float(cy + 1) * dist.y : tnear.y + float(gy - cy) * dist.y;
-    tnext.z = d.z > 0.f ? tnear.z + float(cz + 1) * dist.z : tnear.z + float(gz - cz) * dist.z;
-    float t0 = 0.f;
-    int steps = 4 * (gx + gy + gz) + 16;
-    while (true) {
-      if (--steps < 0) { err |= ERR_DDA_LIMIT; break; }
-      const float t1 = fminf(mine(tnext), rtmax);
-      const int id = (cz * gy + cy) * gx + cx;
-      if (!woodcock(id, ray_tmin + t0, ray_tmin + t1)) break;
-      const float tc = mine(tnext);
-      if (tnext.x == tc) {
-        tnext.x += dist.x;
-        cx += stx;
-        if (cx == spx) break;
-      }
-      if (tnext.y == tc) {
-        tnext.y += dist.y;
-        cy += sty;
-        if (cy == spy) break;
-      }
-      if (tnext.z == tc) {
-        tnext.z += dist.z;
-        cz += stz;
-        if (cz == spz) break;
-      }
-      t0 = t1;
-    }
+    ddaWalk(o, d, tmin, tmax, f3(0.f), f3(1.f), V.gdims[0], V.gdims[1], V.gdims[2], err, woodcock);
   } else {
     woodcock(-1, tmin, tmax);
   }
@@ -1238,6 +1256,12 @@ __device__ __forceinline__ float linearToSrgb(float x) {
 }
 __device__ __forceinline__ uint32_t cvtU8(float f) {
   return (uint32_t)(255.f * fminf(fmaxf(f, 0.f), 1.f));
+}
+// cvt_uint32 (srgb = false) / cvt_uint32_srgb (srgb = true) of one colour.
+__device__ __forceinline__ uint32_t packRGBA8(float4 color, bool srgb) {
+  float r = color.x, g = color.y, b = color.z;
+  if (srgb) { r = linearToSrgb(r); g = linearToSrgb(g); b = linearToSrgb(b); }
+  return cvtU8(r) | (cvtU8(g) << 8) | (cvtU8(b) << 16) | (cvtU8(color.w) << 24);
 }
 
 // lumSqMean: the mean over this frame's samples of the squared sample
@@ -1278,10 +1302,7 @@ __device__ __forceinline__ void writeSample(const DFrame &F, int x, int y, bool 
   if (F.colorType == COLOR_FLOAT4) {
     reinterpret_cast<float4 *>(F.color)[idx] = color;
   } else if (F.colorType == COLOR_UFIXED8 || F.colorType == COLOR_SRGB8) {
-    float r = color.x, g = color.y, b = color.z;
-    if (F.colorType == COLOR_SRGB8) { r = linearToSrgb(r); g = linearToSrgb(g); b = linearToSrgb(b); }
-    reinterpret_cast<uint32_t *>(F.color)[idx] =
-        cvtU8(r) | (cvtU8(g) << 8) | (cvtU8(b) << 16) | (cvtU8(color.w) << 24);
+    reinterpret_cast<uint32_t *>(F.color)[idx] = packRGBA8(color, F.colorType == COLOR_SRGB8);
   }
 }
 

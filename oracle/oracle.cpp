@@ -1581,6 +1581,14 @@ struct Ctx {
   OrFrame *F;
 };
 
+// cvt_uint32 / cvt_uint32_srgb, frame/common.h:31-48: clamp to [0,1],
+// scale by 255 and truncate, RGBA in bytes 0..3 (sRGB encodes rgb only).
+uint32_t cvtColor(f4 c, bool srgb) {
+  auto cv = [](float f) { return (uint32_t)(255.f * std::min(std::max(f, 0.f), 1.f)); };
+  if (srgb) c = f4(linear_to_srgb1(c.x), linear_to_srgb1(c.y), linear_to_srgb1(c.z), c.w);
+  return cv(c.x) | (cv(c.y) << 8) | (cv(c.z) << 16) | (cv(c.w) << 24);
+}
+
 // Per-pixel body of VisionarayRendererPathtrace::renderFrame,
 // renderer/Pathtrace_impl.cpp:498-640, followed by dco::Frame::writeSample.
 void pathtracePixel(const Ctx &cx, int x, int y, Counters &c) {
@@ -1667,11 +1675,7 @@ void pathtracePixel(const Ctx &cx, int x, int y, Counters &c) {
       float *o = (float *)F.color + 4 * idx;
       o[0] = fin.color.x; o[1] = fin.color.y; o[2] = fin.color.z; o[3] = fin.color.w;
     } else {
-      auto cv = [](float f) { return (uint32_t)(255.f * std::min(std::max(f, 0.f), 1.f)); };
-      f4 cc = fin.color;
-      if (F.colorType == OR_COLOR_SRGB8)
-        cc = f4(linear_to_srgb1(cc.x), linear_to_srgb1(cc.y), linear_to_srgb1(cc.z), cc.w);
-      ((uint32_t *)F.color)[idx] = cv(cc.x) | (cv(cc.y) << 8) | (cv(cc.z) << 16) | (cv(cc.w) << 24);
+      ((uint32_t *)F.color)[idx] = cvtColor(fin.color, F.colorType == OR_COLOR_SRGB8);
     }
   }
 }
@@ -1714,11 +1718,7 @@ void raycastPixel(const Ctx &cx, int x, int y, Counters &c) {
       float *o = (float *)F.color + 4 * idx;
       o[0] = fin.color.x; o[1] = fin.color.y; o[2] = fin.color.z; o[3] = fin.color.w;
     } else {
-      auto cv = [](float f) { return (uint32_t)(255.f * std::min(std::max(f, 0.f), 1.f)); };
-      f4 cc = fin.color;
-      if (F.colorType == OR_COLOR_SRGB8)
-        cc = f4(linear_to_srgb1(cc.x), linear_to_srgb1(cc.y), linear_to_srgb1(cc.z), cc.w);
-      ((uint32_t *)F.color)[idx] = cv(cc.x) | (cv(cc.y) << 8) | (cv(cc.z) << 16) | (cv(cc.w) << 24);
+      ((uint32_t *)F.color)[idx] = cvtColor(fin.color, F.colorType == OR_COLOR_SRGB8);
     }
   }
 }
@@ -1898,6 +1898,11 @@ int or_majorants(void *scene, int vol, int32_t *dims, float *out, int maxCells) 
   int n = (int)v.maxOpacity.size();
   for (int i = 0; i < n && i < maxCells; ++i) out[i] = v.maxOpacity[i];
   return n;
+}
+
+void or_cvt(const float *rgba, int n, int srgb, uint32_t *out) {
+  for (int i = 0; i < n; ++i)
+    out[i] = cvtColor(f4(rgba[4 * i], rgba[4 * i + 1], rgba[4 * i + 2], rgba[4 * i + 3]), srgb != 0);
 }
 
 int or_dda(const float *ori, const float *dir, float tmin, float tmax, const int32_t *dims,

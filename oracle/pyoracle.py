@@ -142,6 +142,7 @@ def load():
         lib.or_dda.restype = ctypes.c_int
         lib.or_dda.argtypes = [FP, FP, c_float, c_float, ctypes.POINTER(c_int32), FP, FP,
                                ctypes.POINTER(c_int32), FP, ctypes.c_int]
+        lib.or_cvt.argtypes = [FP, ctypes.c_int, ctypes.c_int, UP]
         lib.or_trace.restype = ctypes.c_int
         lib.or_trace.argtypes = [c_void_p, FP, FP, c_float, c_float, FP, UP, UP, FP]
         _lib = lib

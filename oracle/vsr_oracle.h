@@ -196,6 +196,9 @@ int or_majorants(void *scene, int vol, int32_t *dims, float *out, int maxCells);
 int or_dda(const float *ori, const float *dir, float tmin, float tmax,
            const int32_t *dims, const float *boundsLo, const float *boundsHi,
            int32_t *cells, float *t01, int maxCells);
+/* Colour conversion of n float4 colours to packed RGBA8 (srgb != 0: the
+   sRGB-encoded variant), as the frame's UFIXED8 / sRGB8 colour formats. */
+void or_cvt(const float *rgba, int n, int srgb, uint32_t *out);
 /* Closest hit through the committed scene: returns 1 on hit. */
 int or_trace(void *scene, const float *ori, const float *dir, float tmin, float tmax,
              float *t, uint32_t *inst, uint32_t *tri, float *uv);

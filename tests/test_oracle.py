@@ -1,8 +1,10 @@
 """The CPU oracle pinned against known answers (no GPU).
 
 The reference ships no tests, golden images or fixtures, so the oracle is
-pinned by (a) golden vectors of the in-reference LCG computed by an
-independent restatement (tests/golden/lcg.json), (b) closed-form cases:
+pinned by (a) golden vectors of the reference's LCG<4>, made by the
+reference's own code compiled here (tests/golden/lcg.json; the DDA and
+colour-conversion fixtures are checked in test_reference_pins.py), (b)
+closed-form cases:
 texel-centred trilinear sampling, a Lambertian plane under a directional
 light, an emission-absorption slab, (c) brute-force cross-checks of the BVH
 and of the majorant grid, and (d) invariants of the DDA and the BSDF

@@ -1816,8 +1816,8 @@ int or_render_frame(void *scene, const OrCamera *cam, const OrRenderer *rend, Or
   int r0 = frame->rowBegin, r1 = frame->rowEnd;
   if (r0 == 0 && r1 == 0) r1 = H;
   // 64x64 tiles on a pool of hardware_concurrency() threads (for_each.h:71-85,
-  // SyncContext.cpp:21).
-  const int T = 64;
+  // SyncContext.cpp:21); tests may ask for smaller tiles.
+  const int T = frame->tileSize > 0 ? frame->tileSize : 64;
   const int tx = (W + T - 1) / T, ty = (r1 - r0 + T - 1) / T;
   const int ntiles = tx * ty;
   if (numThreads <= 0) numThreads = (int)std::max(1u, std::thread::hardware_concurrency());

@@ -97,7 +97,7 @@ class OrFrame(ctypes.Structure):
     _fields_ = [("width", c_int32), ("height", c_int32), ("accumID", c_int32),
                 ("colorType", c_int32), ("color", c_void_p), ("depth", FP), ("normal", FP),
                 ("albedo", FP), ("accum", FP), ("sampleSum", DP), ("sampleSumSq", DP),
-                ("rowBegin", c_int32), ("rowEnd", c_int32)]
+                ("rowBegin", c_int32), ("rowEnd", c_int32), ("tileSize", c_int32)]
 
 
 class OrStats(ctypes.Structure):
@@ -491,10 +491,14 @@ class Frame:
         load().or_frame_reset(ctypes.byref(f))
 
 
-def render(sc, frame, num_threads=0, rows=None, stats=None):
-    """Render one frame of committed scene `sc` into `frame` (accumulating)."""
+def render(sc, frame, num_threads=0, rows=None, stats=None, tile=None):
+    """Render one frame of committed scene `sc` into `frame` (accumulating).
+    tile: pixel tile edge handed to each thread (default 64, the reference
+    CPU device's); smaller tiles spread small frames over more threads."""
     if rows is not None:
         frame.f.rowBegin, frame.f.rowEnd = rows
+    if tile is not None:
+        frame.f.tileSize = int(tile)
     st = stats if stats is not None else OrStats()
     load().or_render_frame(sc.handle, ctypes.byref(sc.camera), ctypes.byref(sc.renderer),
                            ctypes.byref(frame.f), num_threads, ctypes.byref(st))

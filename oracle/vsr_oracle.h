@@ -153,6 +153,8 @@ typedef struct OrFrame {
   double *sampleSum;         /* optional: per-pixel sum of sample rgb (3 doubles) */
   double *sampleSumSq;       /* optional: per-pixel sum of squares (3 doubles) */
   int32_t rowBegin, rowEnd;  /* render rows [rowBegin,rowEnd) only (0,0 = all) */
+  int32_t tileSize;          /* square pixel tiles handed to the threads (0 = 64, as
+                                the reference CPU device); results do not depend on it */
 } OrFrame;
 
 typedef struct OrStats {

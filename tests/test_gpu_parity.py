@@ -32,14 +32,14 @@ def render_gpu(pkg, dev, scene, frames=1, accum_offset=0):
     return out
 
 
-def render_oracle(oracle, scene, frames=1, accum_start=0, stats=False, grid=None):
+def render_oracle(oracle, scene, frames=1, accum_start=0, stats=False, grid=None, tile=None):
     kw = {} if grid is None else {"grid_method": grid}
     S = oracle.Scene(scene, **kw)
     W, H = scene["frame"]["size"]
     F = oracle.Frame(W, H, stats=stats)
     F.f.accumID = accum_start
     for _ in range(frames):
-        oracle.render(S, F)
+        oracle.render(S, F, tile=tile)
     return S, F
 
 
@@ -659,3 +659,177 @@ def test_bvh_build_policies_give_the_same_image(pkg, device, build, width):
     assert np.array_equal(a["depth"], b["depth"])
     d = np.abs(a["color"] - b["color"]).max(axis=-1)
     assert float((d <= 1e-6).mean()) >= 0.995
+
+
+def translucent_spheres(pkg, renderer, res=96, spp=8, n=16):
+    """The sphere set with non-opaque materials: a third "blend" with opacity
+    0.25..0.75, a third "mask" with opacity either side of its cutoff (0.5),
+    the rest (and the ground) opaque, so that the stochastic-opacity loop
+    (one draw per surface hit, re-trace past a rejected hit) and the
+    closest-hit shadow rays of a non-opaque world both run."""
+    sc = small_spheres(pkg, res=res, spp=spp, n=n, renderer=renderer)
+    rng = np.random.default_rng(21)
+    for k, s in enumerate(sc["surfaces"][:-1]):
+        m = dict(s["material"])
+        if k % 3 == 0:
+            m.update(alphaMode="blend", opacity=float(rng.uniform(0.25, 0.75)))
+        elif k % 3 == 1:
+            m.update(alphaMode="mask", opacity=float(rng.choice([0.3, 0.7])), alphaCutoff=0.5)
+        s["material"] = m
+    return sc
+
+
+def test_raycast_nonopaque_materials(pkg, device, oracle):
+    """Raycast through blend / mask materials (surface layers composited
+    front to back until alpha reaches 0.999, Raycast_impl.cpp:100-156)."""
+    sc = translucent_spheres(pkg, "raycast", res=128)
+    gpu = render_gpu(pkg, device, sc)
+    _, F = render_oracle(oracle, sc)
+    opaque = {k: v for k, v in sc.items()}
+    opaque["surfaces"] = [dict(s, material={kk: vv for kk, vv in s["material"].items()
+                                            if kk not in ("alphaMode", "opacity", "alphaCutoff")})
+                          for s in sc["surfaces"]]
+    _, P = render_oracle(oracle, opaque)
+    assert gpu["errorFlags"] == 0
+    # the materials change the image
+    assert float((np.abs(F.color - P.color).max(axis=-1) > 1e-2).mean()) > 0.02
+    good, frac = raycast_ok(gpu, F)
+    assert good, frac
+    hit = (F.depth < 1e30) & (gpu["depth"] < 1e30)
+    rel = np.abs(gpu["depth"][hit] - F.depth[hit]) / F.depth[hit]
+    assert float((rel <= 1e-4).mean()) >= 0.999
+
+
+@pytest.mark.parametrize("wavefront", [True, False])
+def test_pathtrace_nonopaque_materials_same_stream(pkg, device, oracle, wavefront):
+    """Stochastic opacity (intersectSurfaces<EvalOpacity>, renderer/common.h
+    :1502-1543): a hit is rejected when a uniform draw exceeds the material's
+    opacity and the ray is traced on from just past it; same stream as the
+    oracle, in both execution modes."""
+    sc = translucent_spheres(pkg, "pathtrace")
+    sc["renderer"]["wavefront"] = wavefront
+    gpu = render_gpu(pkg, device, sc)
+    _, F = render_oracle(oracle, sc)
+    assert gpu["errorFlags"] == 0
+    assert not np.isnan(gpu["color"]).any()
+    d = np.abs(gpu["color"][..., :3] - F.color[..., :3]).max(axis=-1)
+    frac = float((d <= 1e-3).mean())
+    print("non-opaque same-stream within 1e-3:", frac)
+    assert frac >= 0.97, frac
+
+
+def surfaces_and_volume(pkg, res=128, n=64, spheres=12):
+    """A raycast world with triangle meshes inside a blob volume: the config-0
+    field and transfer function over the sphere set's box [-12, 12]^3 (unit
+    distance one voxel spacing), the config-1 camera."""
+    sc = small_spheres(pkg, res=res, renderer="raycast", n=spheres)
+    v = pkg.scenes.config0(res=32, n=n)["volumes"][0]
+    spacing = 24.0 / (n - 1)
+    v = dict(v, origin=[-12.0] * 3, spacing=[spacing] * 3, unitDistance=spacing)
+    sc["volumes"] = [v]
+    sc["renderer"]["volumeSamplingRate"] = 2.0
+    return sc
+
+
+@pytest.mark.parametrize("filt", ["hardware", "exact"])
+def test_raycast_surfaces_and_volume(pkg, device, oracle, filt):
+    """Raycast compositing with surfaces and a volume (Raycast_impl.cpp
+    :158-240): the surface over the background, then the volume marched up
+    to the surface hit and composited over that; a pixel whose ray meets the
+    volume keeps the surface's depth but zero normal and albedo."""
+    sc = surfaces_and_volume(pkg)
+    sc["renderer"]["volumeFilter"] = filt
+    gpu = render_gpu(pkg, device, sc)
+    _, F = render_oracle(oracle, sc)
+    _, P = render_oracle(oracle, dict(sc, volumes=[]))
+    assert gpu["errorFlags"] == 0
+    assert float((np.abs(F.color - P.color).max(axis=-1) > 1e-2).mean()) > 0.1
+    good, frac = raycast_ok(gpu, F)
+    print(filt, "within 2e-3:", frac)
+    assert good, frac
+    hit = (F.depth < 1e30) & (gpu["depth"] < 1e30)
+    assert hit.mean() > 0.1
+    assert np.array_equal(F.depth < 1e30, gpu["depth"] < 1e30)
+    rel = np.abs(gpu["depth"][hit] - F.depth[hit]) / F.depth[hit]
+    assert float((rel <= 1e-4).mean()) >= 0.999
+    assert np.array_equal(gpu["normal"] == 0, F.normal == 0)
+    if filt == "exact":
+        assert float(np.abs(gpu["color"] - F.color).max()) < 1e-3
+
+
+def test_pathtrace_1024spp_band_config1_scene(pkg, device, oracle):
+    """The path-tracer bar: the config-1 scene (all 256 spheres, 64x32
+    segments, ground quad, depth 5) at 128x128, 1024 spp on each side with
+    independent random streams (GPU accumulation IDs 0..15, oracle 1000..).
+    The GPU's 1024-spp mean must lie inside the 3-sigma band of the
+    difference of the two means (sigma from the oracle's per-sample variance
+    and the variance of the GPU's 16 frame means) on >= 98.5 % of pixels;
+    the RMSE between the two means and the share inside the oracle's own
+    3-sigma band are printed."""
+    frames, spp = 16, 64
+    sc = pkg.scenes.config1(res=128, spp=spp)
+    h = pkg.scenes.build(device, sc)
+    prev, fms = None, []
+    for k in range(frames):
+        assert device.render(h["frame"]) == 0
+        assert device.wait(h["frame"])
+        acc = device.map(h["frame"], "channel.color")[..., :3].astype(np.float64)
+        fms.append(acc if prev is None else (k + 1) * acc - k * prev)
+        prev = acc
+    assert device.get_uint(h["frame"], "errorFlags") == 0
+    for o in (h["frame"], h["renderer"], h["camera"], h["world"], *h["keep"]):
+        device.release(o)
+    gpu_mean = prev
+    var_gpu_mean = np.stack(fms).var(axis=0, ddof=1) / frames
+    _, F = render_oracle(oracle, sc, frames=frames, accum_start=1000, stats=True, tile=16)
+    n = frames * spp
+    mean = F.sum / n
+    var = np.maximum(F.sumsq / n - mean * mean, 0.0) * n / (n - 1)
+    sigma_ref = np.sqrt(var / n)
+    sigma = np.sqrt(var_gpu_mean + var / n)
+    inside = float((np.abs(gpu_mean - mean) <= 3.0 * sigma + 1e-6).all(axis=-1).mean())
+    inside_ref = float((np.abs(gpu_mean - mean) <= 3.0 * sigma_ref + 1e-6).all(axis=-1).mean())
+    rmse = float(np.sqrt(np.mean((gpu_mean - mean) ** 2)))
+    print(f"1024 spp, 128x128: inside combined 3-sigma band {inside:.4f}, inside the oracle's "
+          f"own band {inside_ref:.4f}, RMSE {rmse:.5f}, mean {float(mean.mean()):.4f}")
+    assert inside >= 0.985, inside
+    assert abs(float(gpu_mean.mean() - mean.mean())) < 0.01 * float(mean.mean()) + 1e-3
+
+
+@pytest.mark.parametrize("case", ["band", "crop"])
+def test_volume_pathtrace_config2_settings_same_stream(pkg, device, oracle, case):
+    """Config 2 at its own settings: the 512^3 value-noise field with the
+    default 16^3-voxel brick majorants (32^3 bricks walked by the DDA), the
+    clip plane (0,0,1,0), depth 8, the config-1 spheres; same random stream
+    as the oracle at 16 spp. band: the full 1920x1080 frame on the GPU, rows
+    538..541 against the oracle; crop: a 256x256 frame of the same world."""
+    spp = 16
+    if case == "band":
+        sc = pkg.scenes.config2(spp=spp)
+        rows = (538, 542)
+    else:
+        sc = pkg.scenes.config2(res=(256, 256), spp=spp)
+        rows = None
+    assert sc["volumes"][0]["majorantBrickSize"] == 16
+    assert sc["renderer"]["clipPlanes"] == [[0.0, 0.0, 1.0, 0.0]]
+    h = pkg.scenes.build(device, sc)
+    assert device.render(h["frame"]) == 0
+    assert device.wait(h["frame"])
+    color = device.map(h["frame"], "channel.color")
+    err = device.get_uint(h["frame"], "errorFlags")
+    for o in (h["frame"], h["renderer"], h["camera"], h["world"], *h["keep"]):
+        device.release(o)
+    assert err == 0
+    assert not np.isnan(color).any()
+    W, H = sc["frame"]["size"]
+    S = oracle.Scene(sc, grid_method=oracle.GRID_BRICK)
+    F = oracle.Frame(W, H)
+    oracle.render(S, F, rows=rows)
+    r0, r1 = rows if rows else (0, H)
+    g, o = color[r0:r1, :, :3], F.color[r0:r1, :, :3]
+    assert float(o.max()) > 0.05  # the band sees the volume and the spheres
+    d = np.abs(g - o).max(axis=-1)
+    frac = float((d <= 1e-3).mean())
+    print(f"config2 {case}: {frac:.4f} of pixels within 1e-3, mean |d| {float(d.mean()):.2e}")
+    assert frac >= 0.95, frac
+    assert float(np.abs(g.mean() - o.mean())) < 2e-3

@@ -204,7 +204,10 @@ cudaError_t Denoiser::conv(int li, const __nv_bfloat16 *x, int xC, __nv_bfloat16
   return useTc(W) ? launchTc(a, s) : launchConv3x3(a, s);
 }
 
-cudaError_t Denoiser::launchTc(const ConvArgs &a, cudaStream_t s) const {
+cudaError_t Denoiser::launchTc(const ConvArgs &args, cudaStream_t s) const {
+  ConvArgs a = args;
+  a.testStall = stallNext_ ? 1 : 0;
+  stallNext_ = false;
   return tensorPath_ == 3 ? launchConv3x3Tc(a, err_, s) : launchConv3x3Ws(a, err_, s);
 }
 

@@ -56,6 +56,9 @@ class Denoiser {
   void setTensorPath(int path) { tensorPath_ = path; }
   int tensorPath() const { return tensorPath_; }
   unsigned *errorWord() const { return err_; }
+  // timeout test: the next tcgen05 convolution launch runs with
+  // ConvArgs::testStall set (one launch only)
+  void armWaitTimeoutTest() { stallNext_ = true; }
   int steps() const { return step_; }
 
  private:
@@ -90,6 +93,7 @@ class Denoiser {
   float *params_ = nullptr, *m_ = nullptr, *v_ = nullptr, *grad_ = nullptr, *loss_ = nullptr;
   unsigned *err_ = nullptr;
   int tensorPath_ = 1;
+  mutable bool stallNext_ = false;
   __nv_bfloat16 *wbf_ = nullptr, *wt_ = nullptr, *wpk_ = nullptr;
   size_t numPacked_ = 0;
   // refresh the packed weight copies from wbf_ and wt_

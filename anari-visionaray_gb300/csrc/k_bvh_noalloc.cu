@@ -75,19 +75,30 @@ __global__ void kClearScratch(uint32_t *bounds, int *flags, int numFlags) {
 std::mutex g_setupMutex;
 void *g_scratch[256] = {};
 
-// Set-up, once per device, with that device current: the device address of
-// the static buffer.
-cudaError_t scratchOfCurrentDevice(void **out) {
+// The device address of the static buffer on the current device. The
+// address belongs to the device's current context: a cudaDeviceReset (or a
+// released and re-created primary context) reloads the module and may move
+// it. So every call made outside stream capture looks it up again (a
+// lookup, no allocation) and refreshes the per-device copy; while `stream`
+// is being captured the copy from the device's last uncaptured call is
+// used (the first lookup may load the module, so the first call on a
+// device must come before any capture; without a copy the call fails).
+cudaError_t scratchOfCurrentDevice(cudaStream_t stream, void **out) {
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return e;
   if (dev < 0 || dev >= 256) return cudaErrorInvalidDevice;
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  e = cudaStreamIsCapturing(stream, &cap);
+  if (e != cudaSuccess) return e;
   std::lock_guard<std::mutex> lock(g_setupMutex);
-  if (!g_scratch[dev]) {
+  if (cap == cudaStreamCaptureStatusNone) {
     void *ptr = nullptr;
     e = cudaGetSymbolAddress((void **)&ptr, g_bvhScratch);
     if (e != cudaSuccess) return e;
     g_scratch[dev] = ptr;
+  } else if (!g_scratch[dev]) {
+    return cudaErrorStreamCaptureUnsupported;
   }
   *out = g_scratch[dev];
   return cudaSuccess;
@@ -112,7 +123,7 @@ extern "C" VSRStatus vsrBuildTriangleBVHNoAlloc(const float *v1, const float *e1
     return cudaGetLastError() == cudaSuccess ? VSR_OK : VSR_ERROR_CUDA;
   }
   void *base = nullptr;
-  if (scratchOfCurrentDevice(&base) != cudaSuccess) return VSR_ERROR_CUDA;
+  if (scratchOfCurrentDevice(stream, &base) != cudaSuccess) return VSR_ERROR_CUDA;
   ScratchLayout L;
   if (layoutFor(n, stream, L) != cudaSuccess) return VSR_ERROR_CUDA;
   if (L.total > kScratchBytes) return VSR_ERROR_LIMIT_EXCEEDED;

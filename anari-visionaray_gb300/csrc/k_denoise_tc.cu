@@ -158,6 +158,8 @@ __global__ void __launch_bounds__(128) kConv3x3Tc(ConvArgs a, int tilesX, int ti
   }
   if (tid == 0) {
     asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smemAddr(bar)));
+    // a barrier nothing arrives on, waited on only by the timeout test
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smemAddr(bar + 3)));
     asm volatile("fence.mbarrier_init.release.cluster;\n" ::);
   }
   asm volatile("tcgen05.fence::before_thread_sync;\n" ::);
@@ -167,8 +169,10 @@ __global__ void __launch_bounds__(128) kConv3x3Tc(ConvArgs a, int tilesX, int ti
   const uint32_t haloBase = smemAddr(sHalo), wBase = smemAddr(sW);
   bool ok = true;
   int issued = 0;  // stages whose MMAs were committed
+  // timeout test: nothing is in flight yet when this wait runs out
+  if (a.testStall) ok = blockWait(smemAddr(bar + 3), 0, waitFlag);
 
-  for (int s = 0; s < stages; ++s) {
+  for (int s = 0; ok && s < stages; ++s) {
     if (s > 0) {
       ok = blockWait(smemAddr(bar), (s - 1) & 1, waitFlag);  // the MMAs of stage s - 1
       if (!ok) break;

@@ -74,6 +74,8 @@ struct Cfg {
   static constexpr int kSlotBytes = (kHaloBytes + kWBytes + 1023) / 1024 * 1024;
   static constexpr int kBarOff = kSlots * kSlotBytes;
   static constexpr int kSmem = kBarOff + 256;
+  // barriers (2 kSlots + 4), tensor-memory slot, abort flag, timeout-test barrier
+  static_assert(8 * (2 * kSlots + 7) <= 256, "barrier area");
   static constexpr int kCols = 2 * kR * N;  // two accumulator sets: 512 or 256 columns
 };
 static_assert(Cfg<64>::kSmem <= 227 * 1024 && Cfg<32>::kSmem <= 227 * 1024, "shared memory");
@@ -191,6 +193,7 @@ __global__ void __launch_bounds__(kThreads, 1)
   const uint32_t accFullBar = emptyBar + 8 * C::kSlots, accEmptyBar = accFullBar + 16;
   uint32_t *tmemSlot = reinterpret_cast<uint32_t *>(bars + 2 * C::kSlots + 4);
   volatile int *abort = reinterpret_cast<volatile int *>(bars + 2 * C::kSlots + 5);
+  const uint32_t stallBar = smemAddr(bars + 2 * C::kSlots + 6);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int stages = (a.Cin + 8 * kChunks - 1) / (8 * kChunks);
   const uint32_t slot0 = smemAddr(smem);
@@ -206,6 +209,8 @@ __global__ void __launch_bounds__(kThreads, 1)
       asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(accEmptyBar + 8 * b),
                    "r"(32 * kEpiWarps));
     }
+    // a barrier nothing arrives on, waited on only by the timeout test
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(stallBar));
     *abort = 0;
     asm volatile("fence.mbarrier_init.release.cluster;\n" ::);
   }
@@ -285,6 +290,9 @@ __global__ void __launch_bounds__(kThreads, 1)
       int g = 0, j = 0;
       int lastSlot = -1, lastRound = 0;
       constexpr uint32_t idesc = instrDesc(N, kTX);
+      // timeout test: the MMA thread has issued nothing when this wait runs
+      // out; the producer drains the loads it started before the CTA ends
+      if (a.testStall && !mbarWait(stallBar, 0, abort)) fail(error, abort);
       for (int u = blockIdx.x; u < units && !*abort; u += gridDim.x, ++j) {
         const int b = j & 1;
         if (!mbarWait(accEmptyBar + 8 * b, ((j >> 1) & 1) ^ 1, abort)) {

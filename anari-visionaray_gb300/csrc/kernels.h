@@ -110,6 +110,11 @@ struct ConvArgs {
   int x2C, x2Off, split, up;
   // the weights packed for kConv3x3Ws (packConvWeights), or null
   const __nv_bfloat16 *wPacked;
+  // tcgen05 kernels, for tests of the timeout path only (0 otherwise): the
+  // MMA role of every CTA first waits on a barrier that nothing completes,
+  // so that its bounded wait runs out and the launch ends early with error
+  // word 1 and no output
+  int testStall;
 };
 struct WgradArgs {
   const __nv_bfloat16 *dy;  // output gradient (after the ReLU mask)

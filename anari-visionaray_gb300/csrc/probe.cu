@@ -114,4 +114,21 @@ int vsrProbeCvt(const float *rgba, int n, int srgb, uint32_t *out) {
   return (int)cudaMemcpy(out, dout.p, 4 * (size_t)n, cudaMemcpyDeviceToHost);
 }
 
+// Bytes in use and reserved in the current device's default stream-ordered
+// memory pool (the pool cudaMallocAsync draws from), for tests that check
+// that an entry point allocates nothing.
+int vsrProbeMemPoolUsage(uint64_t *used, uint64_t *reserved) {
+  int dev = 0;
+  cudaMemPool_t pool;
+  cudaError_t e;
+  if ((e = cudaGetDevice(&dev)) || (e = cudaDeviceGetDefaultMemPool(&pool, dev))) return (int)e;
+  unsigned long long u = 0, r = 0;  // the attributes are 64-bit counts
+  if ((e = cudaMemPoolGetAttribute(pool, cudaMemPoolAttrUsedMemCurrent, &u)) ||
+      (e = cudaMemPoolGetAttribute(pool, cudaMemPoolAttrReservedMemCurrent, &r)))
+    return (int)e;
+  *used = u;
+  *reserved = r;
+  return 0;
+}
+
 } // extern "C"

@@ -2416,9 +2416,22 @@ uint32_t vsrDenoiserErrors(VSRDevice dv, VSRDenoiser nv) {
   Denoiser *n = asDenoiser(d, nv);
   if (!n) return 0;
   uint32_t e = 0;
-  cudaMemcpyAsync(&e, n->errorWord(), sizeof(e), cudaMemcpyDeviceToHost, d->stream);
-  cudaStreamSynchronize(d->stream);
+  if (cudaMemcpyAsync(&e, n->errorWord(), sizeof(e), cudaMemcpyDeviceToHost, d->stream) !=
+          cudaSuccess ||
+      cudaMemsetAsync(n->errorWord(), 0, sizeof(e), d->stream) != cudaSuccess ||
+      cudaStreamSynchronize(d->stream) != cudaSuccess)
+    return 0xffffffffu;
   return e;
+}
+
+VSRStatus vsrDenoiserTestWaitTimeout(VSRDevice dv, VSRDenoiser nv) {
+  Device *d = asDev(dv);
+  if (!d) return VSR_ERROR_INVALID_ARGUMENT;
+  std::lock_guard<std::recursive_mutex> lk(d->mtx);
+  Denoiser *n = asDenoiser(d, nv);
+  if (!n) return VSR_ERROR_INVALID_OBJECT;
+  n->armWaitTimeoutTest();
+  return VSR_OK;
 }
 
 VSRStatus vsrDenoiserGetParameters(VSRDevice dv, VSRDenoiser nv, float *params, uint64_t count) {
@@ -2562,10 +2575,21 @@ VSRStatus vsrDenoiseFrame(VSRDevice dv, VSRDenoiser nv, VSRFrame fv, float k, fl
                                            F->denoiseCount.as<unsigned>(), s),
                     "denoiser output");
   if (st == VSR_OK && numRetry) {
+    uint32_t word = 0;
     st = cudaStatus(d, cudaMemcpyAsync(numRetry, F->denoiseCount.p, sizeof(unsigned),
                                        cudaMemcpyDeviceToHost, s),
                     "denoiser retry count");
+    if (st == VSR_OK)
+      st = cudaStatus(d, cudaMemcpyAsync(&word, n->errorWord(), sizeof(word),
+                                         cudaMemcpyDeviceToHost, s),
+                      "denoiser error word");
     if (st == VSR_OK) st = cudaStatus(d, cudaStreamSynchronize(s), "denoiser");
+    if (st == VSR_OK && word) {
+      // a bounded wait of a tcgen05 convolution ran out: the image is not valid
+      d->report(F, VSR_FRAME, VSR_SEVERITY_ERROR, VSR_ERROR_TIMEOUT,
+                "denoiser: a tensor-core wait ran out (error word 0x%x)", word);
+      st = VSR_ERROR_TIMEOUT;
+    }
   }
   return st;
 }
@@ -2637,12 +2661,23 @@ const void *vsrMapFrame(VSRDevice dv, VSRFrame fv, const char *channel, uint32_t
     return nullptr;
   }
   void *&host = F->pinned[channel];
+  if (width) *width = 0;
+  if (height) *height = 0;
+  if (pixelType) *pixelType = VSR_UNKNOWN;
   if (!host && cudaMallocHost(&host, bytes) != cudaSuccess) {
     host = nullptr;
+    d->report(F, VSR_FRAME, VSR_SEVERITY_ERROR, VSR_ERROR_OUT_OF_MEMORY,
+              "map of channel '%s': no pinned host buffer of %zu bytes", channel, bytes);
     return nullptr;
   }
-  cudaMemcpyAsync(host, p, bytes, cudaMemcpyDeviceToHost, d->stream);
-  cudaStreamSynchronize(d->stream);
+  // a failed copy must not hand back the previous frame's pixels
+  cudaError_t e = cudaMemcpyAsync(host, p, bytes, cudaMemcpyDeviceToHost, d->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(d->stream);
+  if (e != cudaSuccess) {
+    d->report(F, VSR_FRAME, VSR_SEVERITY_ERROR, VSR_ERROR_CUDA, "map of channel '%s' failed: %s",
+              channel, cudaGetErrorString(e));
+    return nullptr;
+  }
   if (width) *width = (uint32_t)F->width;
   if (height) *height = (uint32_t)F->height;
   if (pixelType) *pixelType = t;

@@ -66,6 +66,7 @@ _SIGNATURES = [
     ("vsrDenoiserParameterCount", ctypes.c_uint64, [_P, _P]),
     ("vsrDenoiserSetTensorPath", ctypes.c_int, [_P, _P, ctypes.c_int]),
     ("vsrDenoiserErrors", ctypes.c_uint32, [_P, _P]),
+    ("vsrDenoiserTestWaitTimeout", ctypes.c_int, [_P, _P]),
     ("vsrDenoiserGetParameters", ctypes.c_int, [_P, _P, ctypes.POINTER(ctypes.c_float), ctypes.c_uint64]),
     ("vsrDenoiserSetParameters", ctypes.c_int, [_P, _P, ctypes.POINTER(ctypes.c_float), ctypes.c_uint64]),
     ("vsrDenoiserForward", ctypes.c_int, [_P, _P, _P, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32, _P]),
@@ -183,7 +184,16 @@ class Denoiser:
             raise RuntimeError(f"vsrDenoiserSetTensorPath failed ({rc})")
 
     def errors(self):
+        """The tcgen05 path's device error word (1: a bounded wait ran out);
+        reading clears it."""
         return int(self.lib.vsrDenoiserErrors(self.dev.handle, self.handle))
+
+    def test_wait_timeout(self):
+        """Arm the timeout-path test for the next tcgen05 convolution launch
+        (its waits run out after one second; error word 1)."""
+        rc = self.lib.vsrDenoiserTestWaitTimeout(self.dev.handle, self.handle)
+        if rc:
+            raise RuntimeError(f"vsrDenoiserTestWaitTimeout failed ({rc})")
 
     def params(self):
         out = np.zeros(self.count, np.float32)

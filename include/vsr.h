@@ -216,10 +216,18 @@ VSR_API VSRStatus vsrDenoiserGetParameters(VSRDevice d, VSRDenoiser n, float *pa
    1 on a kernel that stages one tile per CTA with cp.async. On the
    tcgen05 path the forward reads each decoder's upsampled input and skip
    connection in place instead of writing their concatenation.
-   vsrDenoiserErrors returns the device error word of the tcgen05 path (bit
-   1: a bounded wait for the tensor core ran out), 0 when all is well. */
+   vsrDenoiserErrors returns the device error word of the tcgen05 path
+   (value 1: a bounded wait on the tensor core, a load or another role ran
+   out; that launch ended early and its layer's output is undefined), 0
+   when all is well, and clears it (0xffffffff if it cannot be read).
+   vsrDenoiserTestWaitTimeout arms a test of that failure path for the next
+   tcgen05 convolution launch only: the MMA thread of each CTA first waits
+   on a barrier that nothing completes, its wait runs out after one second,
+   and the launch ends early with error word 1 (no GPU fault; the device
+   stays usable). Not in the reference (it has no denoiser). */
 VSR_API VSRStatus vsrDenoiserSetTensorPath(VSRDevice d, VSRDenoiser n, int path);
 VSR_API uint32_t vsrDenoiserErrors(VSRDevice d, VSRDenoiser n);
+VSR_API VSRStatus vsrDenoiserTestWaitTimeout(VSRDevice d, VSRDenoiser n);
 VSR_API VSRStatus vsrDenoiserSetParameters(VSRDevice d, VSRDenoiser n, const float *params,
                                            uint64_t count);
 VSR_API VSRStatus vsrDenoiserForward(VSRDevice d, VSRDenoiser n, const void *input, uint32_t N,
@@ -246,7 +254,10 @@ VSR_API VSRStatus vsrDenoiserFrameInput(VSRDevice d, VSRFrame f, void *input);
    and is marked for more samples (retry: one byte per pixel, device, may be
    null). Without a variance channel on the frame every pixel takes the
    denoised colour. colorOut: device float4 per pixel; numRetry: host, may be
-   null. */
+   null. With numRetry the call waits for the pass and returns
+   VSR_ERROR_TIMEOUT (also through the status callback) when a bounded wait
+   of a tcgen05 convolution ran out (vsrDenoiserErrors); without it the call
+   returns once the work is enqueued. */
 VSR_API VSRStatus vsrDenoiseFrame(VSRDevice d, VSRDenoiser n, VSRFrame f, float k,
                                   float floorAbs, float *colorOut, uint8_t *retry,
                                   uint32_t *numRetry);
@@ -264,7 +275,10 @@ VSR_API uint64_t vsrPlanBatch(const uint32_t *width, const uint32_t *height,
 /* Mapping; replaces anariMapFrame / anariUnmapFrame (frame/Frame.cpp:399-447).
    Channels: "channel.color", "channel.depth", "channel.normal",
    "channel.albedo". Returns a host pointer valid until the next render or
-   unmap; the copy from device memory happens inside this call. */
+   unmap; the copy from device memory happens inside this call. On failure
+   (channel not enabled, no pinned host buffer, a failed copy) returns NULL
+   with width = height = 0, reported through the status callback
+   (VSR_ERROR_INVALID_ARGUMENT, VSR_ERROR_OUT_OF_MEMORY, VSR_ERROR_CUDA). */
 VSR_API const void *vsrMapFrame(VSRDevice d, VSRFrame f, const char *channel, uint32_t *width,
                                 uint32_t *height, VSRDataType *pixelType);
 VSR_API VSRStatus vsrUnmapFrame(VSRDevice d, VSRFrame f, const char *channel);
@@ -310,8 +324,11 @@ VSR_API VSRStatus vsrBuildTriangleBVH(const float *v1, const float *e1, const fl
    device share it and it keeps the last call's contents (each call clears
    what must start at zero). Calls that overlap on the GPU race on the buffer
    and corrupt each other's result: order them (one stream, or events).
-   The first call on each device, made with that device current, looks up the
-   buffer's device address; make that first call before any stream capture. */
+   The first call on each device, made with that device current, looks up
+   the buffer's device address; make that first call before any stream
+   capture. Every later call made outside stream capture looks the address
+   up again (a lookup, no allocation), so a cudaDeviceReset or a re-created
+   primary context between calls does not leave a stale address. */
 #define VSR_BVH_NOALLOC_MAX_TRIANGLES 65536u
 VSR_API VSRStatus vsrBuildTriangleBVHNoAlloc(const float *v1, const float *e1, const float *e2,
                                              uint32_t n, void *nodesOut, void *trisOut,

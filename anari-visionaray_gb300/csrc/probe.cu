@@ -51,6 +51,36 @@ __global__ void kProbeCvt(const float4 *rgba, int n, int srgb, uint32_t *out) {
   if (i < n) out[i] = packRGBA8(rgba[i], srgb != 0);
 }
 
+// Streaming read of `bytes` (a multiple of 16) `repeats` times: every
+// thread sums 16-byte loads of a grid-stride walk; one partial sum per block
+// keeps the loads live. With a buffer that fits the L2 cache (e.g. 8 MiB)
+// this measures the achievable L2 read bandwidth.
+__global__ void kProbeRead(const float4 *buf, size_t n16, int repeats, float *sink) {
+  float acc = 0.f;
+  const size_t stride = (size_t)gridDim.x * blockDim.x;
+  for (int r = 0; r < repeats; ++r) {
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n16; i += 4 * stride) {
+      float4 v[4];
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        const size_t j = i + k * stride;
+        v[k] = j < n16 ? __ldcg(buf + j) : make_float4(0.f, 0.f, 0.f, 0.f);
+      }
+#pragma unroll
+      for (int k = 0; k < 4; ++k) acc += v[k].x + v[k].y + v[k].z + v[k].w;
+    }
+  }
+  __shared__ float red[32];
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    float t = 0.f;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += red[w];
+    sink[blockIdx.x] = t;
+  }
+}
+
 struct DevBuf {
   void *p = nullptr;
   cudaError_t alloc(size_t bytes) { return cudaMalloc(&p, bytes > 0 ? bytes : 4); }
@@ -112,6 +142,23 @@ int vsrProbeCvt(const float *rgba, int n, int srgb, uint32_t *out) {
   kProbeCvt<<<(n + 127) / 128, 128>>>((const float4 *)di.p, n, srgb, (uint32_t *)dout.p);
   if ((e = cudaGetLastError()) || (e = cudaDeviceSynchronize())) return (int)e;
   return (int)cudaMemcpy(out, dout.p, 4 * (size_t)n, cudaMemcpyDeviceToHost);
+}
+
+// Enqueue kProbeRead on `stream` over the device buffer `buf` (`bytes`, a
+// multiple of 16, 16-byte aligned) `repeats` times; `sink`: device floats,
+// one per block of the grid (blocksPerSM x the SM count). Asynchronous.
+int vsrProbeReadBandwidth(const void *buf, size_t bytes, int repeats, int blocksPerSM, float *sink,
+                          void *stream) {
+  if (!buf || !sink || bytes % 16 || ((uintptr_t)buf & 15) || repeats <= 0 || blocksPerSM <= 0)
+    return (int)cudaErrorInvalidValue;
+  int dev = 0, sms = 0;
+  cudaError_t e;
+  if ((e = cudaGetDevice(&dev)) ||
+      (e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)))
+    return (int)e;
+  kProbeRead<<<sms * blocksPerSM, 512, 0, (cudaStream_t)stream>>>((const float4 *)buf, bytes / 16,
+                                                                   repeats, sink);
+  return (int)cudaGetLastError();
 }
 
 // Bytes in use and reserved in the current device's default stream-ordered

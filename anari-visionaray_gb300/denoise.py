@@ -239,3 +239,35 @@ def time_to_rmse(plain, dn, pt_s_per_spp, dn_s, target_spp=256):
         return goal, t_plain, None, None
     s = ok[0]
     return goal, t_plain, s, s * pt_s_per_spp + dn_s
+
+
+def plain_spp_for(plain, err):
+    """Samples per pixel plain path tracing needs for the error `err`, from
+    its measured error curve (spp -> error): log-log interpolation between
+    the measured levels, beyond the last one the Monte-Carlo rate error ~
+    1/sqrt(spp) from the last level."""
+    pts = sorted(plain.items())
+    if err >= pts[0][1]:
+        return float(pts[0][0])
+    for (s0, e0), (s1, e1) in zip(pts, pts[1:]):
+        if e1 <= err <= e0:
+            if e0 == e1:
+                return float(s0)
+            f = math.log(e0 / err) / math.log(e0 / e1)
+            return float(math.exp(math.log(s0) + f * math.log(s1 / s0)))
+    s_last, e_last = pts[-1]
+    return float(s_last * (e_last / err) ** 2)
+
+
+def at_input_spp(plain, dn, pt_s_per_spp, dn_s, spp=4):
+    """What denoising `spp` input samples buys: its error, the plain sample
+    count with the same error, and the time ratio of the two at that error
+    (plain spp_equal x per-sample time vs spp x per-sample time + the
+    denoiser pass)."""
+    e = dn[spp]
+    s_eq = plain_spp_for(plain, e)
+    t_plain = s_eq * pt_s_per_spp
+    t_dn = spp * pt_s_per_spp + dn_s
+    return {"input_spp": spp, "denoised_rmse_tm": e, "plain_spp_same_rmse": s_eq,
+            "plain_s_1080p": t_plain, "denoised_s_1080p": t_dn,
+            "speedup_at_that_rmse": t_plain / t_dn}

@@ -28,6 +28,8 @@ import sys
 import threading
 import time
 
+import numpy as np
+
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
@@ -42,7 +44,7 @@ def parse():
     p.add_argument("--impl", choices=["ours", "reference"], default="ours")
     p.add_argument("--res", type=int, default=1024)
     p.add_argument("--spp", type=int, default=64)
-    p.add_argument("--e2e-steps", type=int, default=3)
+    p.add_argument("--e2e-steps", type=int, default=8)
     p.add_argument("--cpu-rows", type=int, default=48,
                    help="rows of the frame the CPU baseline renders (bounded sample)")
     p.add_argument("--no-cpu-baseline", action="store_true")
@@ -179,8 +181,9 @@ def profiled_metric(name, metric):
     return None
 
 
-def cpu_baseline(scene, rows, threads=0):
-    """Time the oracle on a band of rows spread over the frame; Mpx*spp/s."""
+def cpu_baseline(scene, rows, threads=0, keep=False):
+    """Time the oracle on a band of rows spread over the frame; Mpx*spp/s.
+    keep: also return the row ranges and the oracle's colour image."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import pyoracle as po
 
@@ -194,13 +197,86 @@ def cpu_baseline(scene, rows, threads=0):
     t0 = time.perf_counter()
     for s in starts:
         po.render(S, F, num_threads=threads, rows=(s, s + per))
+        F.f.accumID = 0  # every band is the frame's first (the row ranges are disjoint)
     dt = time.perf_counter() - t0
     px = W * per * bands
     cores = threads if threads > 0 else os.cpu_count()
+    if keep:
+        return px * spp / dt / MPX, dt, px, cores, [(s, s + per) for s in starts], F.color
     return px * spp / dt / MPX, dt, px, cores
 
 
-def measure_raycast_config0(pkg, dev, flush, steps=20, gradient=False):
+def issue_roofline(kernel_s, spp, res, sms=None):
+    """The path tracer's issue roofline: thread instructions per second of
+    the 64-spp frame (warp instructions x active lanes per warp instruction
+    of the profiled 1-spp launch at the same resolution, times spp, over the
+    live kernel time) against the SMs' peak (SMs x 4 schedulers x 32 lanes x
+    the maximum SM clock): frac = issue rate x SIMT efficiency."""
+    inst = profiled_metric("pathtrace_config1.txt", "smsp__inst_executed.sum")
+    lanes = profiled_metric("pathtrace_config1.txt",
+                            "smsp__thread_inst_executed_per_inst_executed.ratio")
+    active = profiled_metric("pathtrace_config1.txt",
+                             "smsp__issue_active.avg.pct_of_peak_sustained_active")
+    if not inst or not lanes or res != 1024:
+        return None
+    if sms is None:
+        import torch
+
+        sms = torch.cuda.get_device_properties(0).multi_processor_count
+    mhz = 2070.0
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            mhz = json.load(f).get("sm_max_mhz", mhz)
+    peak = sms * 4 * 32 * mhz * 1e6 / 1e9
+    achieved = inst * lanes * spp / kernel_s / 1e9
+    return {"bound": "issue", "achieved": achieved, "peak": peak, "unit": "Gthread-inst/s",
+            "frac": achieved / peak,
+            "issue_active_frac": active / 100 if active is not None else None,
+            "active_lanes_per_warp_instruction": lanes,
+            "note": f"thread instructions of the profiled 1-spp launch ({inst:.4g} warp "
+                    f"instructions x {lanes:.2f} lanes) x {spp} spp / live kernel time, against "
+                    f"{sms} SMs x 4 schedulers x 32 lanes x {mhz:.0f} MHz; frac = issue-active "
+                    "share x SIMT efficiency"}
+
+
+def measure_l2_read_peak(pkg, mib=8, repeats=64, trials=5):
+    """Achievable L2 read bandwidth on this GPU, measured in this run: a
+    streaming read (16-byte L2-only loads, every SM) of a `mib` MiB buffer
+    (config 0's field is 8 MiB) `repeats` times per launch, timed with CUDA
+    events on torch's current stream (the one the read is launched on);
+    best of `trials` launches. GB/s."""
+    import ctypes
+    import torch
+
+    probe = ctypes.CDLL(os.path.join(os.path.dirname(pkg.__file__), "libvsr_probe.so"))
+    probe.vsrProbeReadBandwidth.argtypes = [ctypes.c_void_p, ctypes.c_size_t, ctypes.c_int,
+                                            ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p]
+    nbytes = mib << 20
+    buf = torch.ones(nbytes // 4, dtype=torch.float32, device="cuda")
+    blocks = 4
+    sink = torch.zeros(torch.cuda.get_device_properties(0).multi_processor_count * blocks,
+                       dtype=torch.float32, device="cuda")
+    stream = torch.cuda.current_stream()
+    best = 0.0
+    for t in range(trials + 1):
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        a.record(stream)
+        rc = probe.vsrProbeReadBandwidth(buf.data_ptr(), nbytes, repeats, blocks,
+                                         sink.data_ptr(), stream.cuda_stream)
+        b.record(stream)
+        torch.cuda.synchronize()
+        if rc:
+            return None
+        if t > 0:  # the first launch is a warm-up
+            best = max(best, nbytes * repeats / (a.elapsed_time(b) * 1e-3) / 1e9)
+    return {"gbs": best, "buffer_mib": mib, "repeats": repeats,
+            "how": "streaming 16-byte ld.global.cg reads over every SM, CUDA events, best of "
+                   f"{trials}"}
+
+
+def measure_raycast_config0(pkg, dev, flush, steps=20, gradient=False, l2=None):
     """Config 0 (raycast, 128^3 blob volume, 512x512, 1 spp): Mpx/s and the
     marcher's roofline (32 B per trilinear sample + 20 B per pixel written).
     gradient: the same volume lit by a directional light with gradient
@@ -249,16 +325,25 @@ def measure_raycast_config0(pkg, dev, flush, steps=20, gradient=False):
                              "unit": "GB/s", "frac": alg / t / 1e9 / peak, "traffic": None,
                              "note": f"7 x 32 B per step (the sample and its 6 central "
                                      f"differences) + 20 B per pixel; peak {kind}"}}
+    achieved = alg / t / 1e9
+    l2_roof = None
+    if l2:
+        l2_roof = {"bound": "l2", "achieved": achieved, "peak": l2["gbs"], "unit": "GB/s",
+                   "frac": achieved / l2["gbs"],
+                   "note": f"the same algorithmic bytes against the L2 read bandwidth "
+                           f"measured in this run ({l2['buffer_mib']} MiB buffer; the field "
+                           f"is L2-resident)"}
     return {"value": W * H / t / MPX, "unit": "Mpx*spp/s", "ms_per_frame": 1e3 * t,
             "workload": "config0 raycast 512x512 1spp, 128^3 float32 blobs, dt 0.5 voxel",
             "march_samples": samples,
-            "roofline": {"bound": "hbm", "achieved": alg / t / 1e9, "peak": peak, "unit": "GB/s",
-                         "frac": alg / t / 1e9 / peak,
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak,
                          "traffic": profiled_traffic("raycast_config0.txt"),
                          "note": f"32 B per trilinear sample + 20 B per pixel; peak {kind}; "
                                  "segmented marcher (set-up, 12-sample segments, combine; passes launched as programmatic dependents); "
                                  "the 8 MiB field is L2-resident, so DRAM traffic is far "
-                                 "below the algorithmic bytes"}}
+                                 "below the algorithmic bytes"},
+            "roofline_l2": l2_roof}
 
 
 def measure_batch_config3(pkg, dev, steps=3, num_scenes=64):
@@ -410,6 +495,8 @@ def measure_denoiser_config4(pkg, dev, train_scenes=128, eval_scenes=8, steps=40
     dn.close()
     goal, t_plain, s_dn, t_dn = D.time_to_rmse(ev["plain"]["rmse_tm"], ev["denoised"]["rmse_tm"],
                                                pt_s_per_spp, dn_s)
+    four = D.at_input_spp(ev["plain"]["rmse_tm"], ev["denoised"]["rmse_tm"], pt_s_per_spp, dn_s, 4)
+    four["reaches_plain256_rmse"] = four["denoised_rmse_tm"] <= goal
     return {
         "workload": f"config4 denoiser: {train_scenes} training scenes x 4 input spp levels "
                     f"({res}^2, {train_ref_spp}-spp references), {steps} Adam steps of 16 "
@@ -421,6 +508,7 @@ def measure_denoiser_config4(pkg, dev, train_scenes=128, eval_scenes=8, steps=40
         "goal_rmse_tm_plain256": goal, "plain256_s_1080p": t_plain,
         "denoised_input_spp": s_dn, "denoised_s_1080p": t_dn,
         "speedup_to_equal_rmse": (t_plain / t_dn) if t_dn else None,
+        "at_4_input_spp": four,
         "pt_ms_per_spp_1080p": 1e3 * pt_s_per_spp, "denoise_ms_1080p": 1e3 * dn_s,
         "train_s": train_s, "train_ms_per_step": 1e3 * train_s / steps, "data_s": data_s,
         "loss": losses,
@@ -495,7 +583,9 @@ def run_reference(args):
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic",
         "config": {"workload": f"config1 pathtracer {args.res}x{args.res} {args.spp}spp depth5 "
-                               "1015810 tris", "sample": f"{px} pixels per step"},
+                               f"1015810 tris; each step renders a bounded sample of it: {rows} "
+                               f"rows in 8 bands ({px} pixels) x {args.spp} spp, throughput "
+                               "scaled per pixel-sample", "sample": f"{px} pixels per step"},
         "cpu_baseline": {"value": value, "unit": unit, "cores": cores, "kind": "port",
                          "sample": f"{px} of {args.res * args.res} pixels ({rows} rows in 8 bands) "
                                    f"x {args.spp} spp per step"},
@@ -589,6 +679,13 @@ def run_ours(args):
         if i > 0:
             e2e_times.append(time.perf_counter() - t)
     h2d = 3 * 4 + 4 * 4 * 0  # the camera position crosses to the device as kernel parameters
+    # one frame at the scene's own camera, accumulation restarted: the same
+    # random stream as the oracle's first frame (compared in the CPU leg)
+    dev.set(cam, "position", list(c["position"]), vsr.FLOAT32_VEC3)
+    dev.commit(cam)
+    dev.render(frame)
+    dev.wait(frame)
+    first_frame = dev.map(frame, "channel.color") if world == 1 else None
 
     # the same samples as accumulated 1-spp frames (the reference's other way
     # to reach 64 spp): one frame per sample, L2 flushed before each
@@ -612,7 +709,8 @@ def run_ours(args):
         dev.set(h["renderer"], "pixelSamples", args.spp)
         dev.commit(h["renderer"])
 
-    raycast = measure_raycast_config0(pkg, dev, flush) if args.raycast else None
+    l2peak = measure_l2_read_peak(pkg) if args.raycast else None
+    raycast = measure_raycast_config0(pkg, dev, flush, l2=l2peak) if args.raycast else None
     shaded = measure_raycast_config0(pkg, dev, flush, gradient=True) if args.raycast else None
     batch = measure_batch_config3(pkg, dev) if args.batch else None
     if not args.denoise:
@@ -643,6 +741,7 @@ def run_ours(args):
     peak, peak_kind = measured_peaks()
     achieved = alg_bytes / kernel_s / 1e9
     traffic = profiled_traffic()
+    issue = issue_roofline(kernel_s, args.spp, args.res)
     line = {
         "metric": "pathtracer Mpx*spp/s (config 1)",
         "value": value, "unit": "Mpx*spp/s", "n_gpus": world, "steps": args.steps,
@@ -653,18 +752,17 @@ def run_ours(args):
         "e2e": {"value": e2e_value, "unit": "Mpx*spp/s", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h},
         "gpu_launches": args.steps,
-        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak, "traffic": traffic,
-                     "note": f"algorithmic bytes = BVH node fetches x64 B + triangle fetches x48 B "
-                             f"+ frame bytes; peak {peak_kind}; most fetches hit L1/L2"},
-        # traversal and shading are issue- and latency-bound: the issue rate and
-        # the SIMT efficiency of the profiled launch (profiles/pathtrace_config1.txt)
-        "issue": {"issue_active_frac": (lambda v: v / 100 if v is not None else None)(
-                      profiled_metric("pathtrace_config1.txt",
-                                      "smsp__issue_active.avg.pct_of_peak_sustained_active")),
-                  "active_lanes_per_warp_instruction": profiled_metric(
-                      "pathtrace_config1.txt", "smsp__thread_inst_executed_per_inst_executed.ratio"),
-                  "source": "ncu, one 1-spp launch of the same kernel"},
+        # traversal and shading are issue- and latency-bound: thread
+        # instructions per second against the SMs' lane-issue peak
+        "roofline": dict(issue, traffic=traffic) if issue else
+        {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+         "frac": achieved / peak, "traffic": traffic},
+        "roofline_memory": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                            "frac": achieved / peak, "traffic": traffic,
+                            "note": f"algorithmic bytes = BVH node fetches x64 B + triangle "
+                                    f"fetches x48 B + frame bytes; peak {peak_kind}; most "
+                                    "fetches hit L1/L2, so this is traversal memory work, not "
+                                    "DRAM traffic"},
         "traversal": {"rays": rays, "node_visits": nodes, "tri_tests": tris,
                       "node_visit_histogram_log2": counts[8:24],
                       "grays_per_s": rays / kernel_s / 1e9},
@@ -677,10 +775,22 @@ def run_ours(args):
         "wavefront_iterations": iterations,
     }
     if world == 1 and not args.no_cpu_baseline:
-        v, dt, px, cores = cpu_baseline(scene, args.cpu_rows)
+        v, dt, px, cores, rows, colour = cpu_baseline(scene, args.cpu_rows, keep=True)
         line["cpu_baseline"] = {"value": v, "unit": "Mpx*spp/s", "cores": cores, "kind": "port",
                                 "sample": f"{px} of {W * H} pixels ({args.cpu_rows} rows in 8 bands) "
                                           f"x {args.spp} spp, {dt:.1f} s"}
+        if first_frame is not None:
+            # the CPU sample is the oracle's first frame of the same rows: the
+            # GPU's first frame follows the same random streams
+            g = np.concatenate([first_frame[a:b, :, :3] for a, b in rows])
+            o = np.concatenate([colour[a:b, :, :3] for a, b in rows])
+            d = np.abs(g.astype(np.float64) - o)
+            line["cpu_baseline"]["parity"] = {
+                "pixels": int(d.shape[0] * d.shape[1]),
+                "within_1e-3": float((d.max(axis=-1) <= 1e-3).mean()),
+                "rmse": float(np.sqrt(np.mean(d * d))), "mean_abs": float(d.mean()),
+                "how": "GPU first frame vs the oracle's frame on the sampled rows, same "
+                       "per-pixel random streams (accumulation restarted)"}
     print(json.dumps(line), flush=True)
     dev.close()
 

@@ -36,3 +36,16 @@ def test_every_profile_names_its_command():
         with open(os.path.join(ROOT, "profiles", name)) as f:
             text = f.read()
         assert "python bench.py" in text and "ncu " in text, name
+
+
+def test_issue_roofline_from_profile():
+    """frac = thread instructions per second / lane-issue peak; with the
+    profile's own launch time (1 spp) it equals issue-active share x active
+    lanes / 32 up to the elapsed-vs-active difference, so it lies in (0, 1]."""
+    bench = load_bench()
+    t1 = bench.profiled_metric("pathtrace_config1.txt", "gpu__time_duration.sum")
+    r = bench.issue_roofline(t1 * 1e-3 * 64, 64, 1024, sms=152)
+    assert r is not None and r["bound"] == "issue" and r["unit"] == "Gthread-inst/s"
+    assert 0 < r["frac"] <= 1.0
+    assert abs(r["frac"] - r["achieved"] / r["peak"]) < 1e-12
+    assert bench.issue_roofline(1.0, 64, 512, sms=152) is None  # other sizes: no profile

@@ -40,6 +40,7 @@ __global__ void __launch_bounds__(16 * VSR_MEGA_BLOCK_Y,
   const int x = blockIdx.x * blockDim.x + threadIdx.x;
   const int y = blockIdx.y * blockDim.y + threadIdx.y;
   if (x >= F.width || y >= F.height) return;
+  if (F.sampleMask && !F.sampleMask[(size_t)y * F.width + x]) return;
   pathtracePixel<Count, Full>(S, C, R, F, x, y);
 }
 

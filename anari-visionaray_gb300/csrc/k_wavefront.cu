@@ -137,7 +137,7 @@ __global__ void __launch_bounds__(256) kWaveInit(DScene S, DCamera C, DRenderer 
   for (uint32_t base = (blockIdx.x * blockDim.x + threadIdx.x) & ~31u; base < n; base += stride) {
     const uint32_t p = base + (threadIdx.x & 31);
     bool active = false;
-    if (p < n) {
+    if (p < n && (!F.sampleMask || F.sampleMask[p])) {
       const int x = (int)(p % F.width), y = (int)(p / F.width);
       Rng rng;
       rng.init(p, (uint32_t)F.accumID);

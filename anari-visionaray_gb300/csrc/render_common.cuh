@@ -340,13 +340,18 @@ __device__ __forceinline__ bool traverseGroup(const DGroup &G, float3 o, float3 
   int node = 0;
   bool found = false, done = false;
   unsigned nodeVisits = 0, triTests = 0;
+  unsigned long long innerW = 0, leafW = 0;
+  unsigned leafL = 0;
   while (!done) {
     // inner nodes until a leaf comes up or nothing is left
     while (node >= 0) {
       const float4 *N = (Analytic ? G.apNodes : G.nodes) + 4 * (size_t)node;
       const float4 n0 = __ldg(N), n1 = __ldg(N + 1), n2 = __ldg(N + 2);
       const int4 n3 = __ldg(reinterpret_cast<const int4 *>(N + 3));
-      if (Count) ++nodeVisits;
+      if (Count) {
+        ++nodeVisits;
+        innerW += 65536u / (unsigned)__popc(__activemask());
+      }
       const float tb = best.t;
       float a0 = fmaf(n0.x, inv.x, oi.x), b0 = fmaf(n0.y, inv.x, oi.x);
       float a1 = fmaf(n0.z, inv.y, oi.y), b1 = fmaf(n0.w, inv.y, oi.y);
@@ -378,6 +383,10 @@ __device__ __forceinline__ bool traverseGroup(const DGroup &G, float3 o, float3 
     }
     // leaves until an inner node comes up or nothing is left
     while (!done && node < 0) {
+      if (Count) {
+        ++leafL;
+        leafW += 65536u / (unsigned)__popc(__activemask());
+      }
       const uint32_t code = ~(uint32_t)node;
       const int first = (int)(code & kLeafFirstMask);
       const int count = (int)(code >> kLeafCountShift) + 1;
@@ -437,6 +446,9 @@ __device__ __forceinline__ bool traverseGroup(const DGroup &G, float3 o, float3 
     // histogram of inner-node visits per traversal, bins [2^k, 2^(k+1))
     const int bin = nodeVisits ? min(31 - __clz(nodeVisits), 15) : 0;
     atomicAdd(&cnt[8 + bin], 1ull);
+    atomicAdd(&cnt[27], innerW);
+    atomicAdd(&cnt[28], (unsigned long long)leafL);
+    atomicAdd(&cnt[29], leafW);
   }
   return found;
 }
@@ -561,8 +573,15 @@ __device__ __forceinline__ bool traverseGroup4(const DGroup &G, float3 o, float3
 
 // Iso-surface test, intersect(Ray, ISOSurface), DeviceCopyableObjects.h:
 // 825-911, as the reference's CPU device runs it but without its 16^3
-// empty-space grid (which only skips cells that hold no crossing): in voxel
-// space with the direction normalised, samples on the lattice anchored at
+// empty-space grid. That is a known divergence, not an equivalence: the
+// reference walks the grid's cells by DDA and restarts the march in each
+// cell whose value range holds an iso value, so a lattice interval that
+// straddles the boundary between such a cell and an empty one is not
+// sampled there, while this march samples it; a crossing right next to an
+// empty macro-cell can therefore come out at a slightly different t (the
+// reference CUDA device builds no grid at all and marches 1 world unit per
+// step). Here: in voxel space with the direction normalised, samples on
+// the lattice anchored at
 // tmin - dt/2 (by repeated addition, dt = step * |S d|) over [tmin, tmax]
 // clipped to the field box; the first lattice interval whose two values
 // bracket an iso value (inclusive) gives the hit by linear interpolation

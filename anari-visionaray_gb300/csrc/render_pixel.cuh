@@ -218,6 +218,8 @@ __device__ __forceinline__ void intersectAll(const DScene &S, const Ray &ray, bo
                                              HitRec &h, uint32_t &err, unsigned long long *cnt,
                                              bool hwFilter) {
   h.surfHit = false;
+  long long tc0 = 0;
+  if (Count) tc0 = clock64();
   if (S.hasSurfaces) {
     Ray r = ray;
     const bool anyHit = shadow && S.allOpaque;
@@ -238,6 +240,11 @@ __device__ __forceinline__ void intersectAll(const DScene &S, const Ray &ray, bo
     h.surfHit = hit;
   } else {
     h.surf.t = FLT_MAX;
+  }
+  if (Count) {
+    const long long tc1 = clock64();
+    atomicAdd(&cnt[25], (unsigned long long)(tc1 - tc0));
+    tc0 = tc1;
   }
   h.volHit = false;
   h.volT = FLT_MAX;
@@ -262,6 +269,7 @@ __device__ __forceinline__ void intersectAll(const DScene &S, const Ray &ray, bo
       }
     }
   }
+  if (Count && S.numVolumes > 0) atomicAdd(&cnt[26], (unsigned long long)(clock64() - tc0));
   h.hit = h.surfHit || h.volHit;
   h.volumeHit = h.volHit && (!h.surfHit || h.volT < h.surf.t);
 }
@@ -275,6 +283,8 @@ __device__ __forceinline__ void pathtracePixel(const DScene &S, const DCamera &C
                                                const DRenderer &R, const DFrame &F, int x, int y) {
   uint32_t err = 0;
   unsigned long long *cnt = F.counters;
+  long long tStart = 0;
+  if (Count) tStart = clock64();
   const int W = F.width, H = F.height;
   Rng rng;
   rng.init((uint32_t)(x + W * y), (uint32_t)F.accumID);
@@ -492,6 +502,7 @@ __device__ __forceinline__ void pathtracePixel(const DScene &S, const DCamera &C
     }
   }
   const float inv = 1.f / R.pixelSamples;
+  if (Count) atomicAdd(&cnt[24], (unsigned long long)(clock64() - tStart));
   writeSample(F, x, y, true, make_float4(accum.x * inv, accum.y * inv, accum.z * inv, accum.w * inv),
               cDepth, cNg, cAlb, lumSq * inv);
   if (err) atomicOr(F.errorFlags, err);

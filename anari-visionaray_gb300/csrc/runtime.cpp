@@ -1482,7 +1482,7 @@ struct FrameObj : Object {
   bool nextReset = true;
   bool countStats = false;
   DevBuf counters;
-  unsigned long long countersHost[24] = {0};
+  unsigned long long countersHost[kStatCounters] = {0};
   // wavefront path-tracer state (allocated on first wavefront render)
   static constexpr int kWaveF4 = 15;
   DevBuf waveF4[kWaveF4], waveMeta, waveHit, waveQueue[2], waveCount;
@@ -1490,6 +1490,7 @@ struct FrameObj : Object {
   uint32_t *pinnedCount = nullptr;
   int lastIterations = 0;
   int batchTileW = 0, batchFetch = 0, batchTuned = 0;  // last batched render
+  const uint8_t *sampleMask = nullptr;  // caller's device mask (vsrFrameSampleMask)
 
   // scratch of the segmented volume marcher, made on first use: the ray list
   // (48 B per pixel), groups (16 B per 32 pixels) and work units for
@@ -1596,7 +1597,7 @@ struct FrameObj : Object {
                 albedo.alloc(np * 3 * sizeof(float)) == cudaSuccess &&
                 color.alloc(np * (colorType == VSR_FLOAT32_VEC4 ? 16 : 4)) == cudaSuccess &&
                 errFlags.alloc(sizeof(uint32_t)) == cudaSuccess &&
-                counters.alloc(24 * sizeof(unsigned long long)) == cudaSuccess;
+                counters.alloc(kStatCounters * sizeof(unsigned long long)) == cudaSuccess;
       if (varianceType == VSR_FLOAT32) {
         ok = ok && variance.alloc(np * sizeof(float)) == cudaSuccess &&
              accumSq.alloc(np * sizeof(float)) == cudaSuccess;
@@ -1639,6 +1640,7 @@ struct FrameObj : Object {
     f.accumSq = accumSq.as<float>();
     f.variance = variance.as<float>();
     f.pixelSamples = renderer ? renderer->r.pixelSamples : 1;
+    f.sampleMask = sampleMask;
     return f;
   }
 };
@@ -1704,7 +1706,8 @@ VSRStatus renderFrame(Device *dev, FrameObj *F) {
   if (reset)
     launchFrameReset(F->accum.as<float4>(), F->depth.as<float>(), (size_t)F->width * F->height, s);
   cudaMemsetAsync(F->errFlags.p, 0, sizeof(uint32_t), s);
-  if (F->countStats) cudaMemsetAsync(F->counters.p, 0, 24 * sizeof(unsigned long long), s);
+  if (F->countStats)
+    cudaMemsetAsync(F->counters.p, 0, kStatCounters * sizeof(unsigned long long), s);
   cudaEventRecord(F->evRender, s);
   cudaError_t e = cudaSuccess;
   if (doRender) {
@@ -1722,7 +1725,7 @@ VSRStatus renderFrame(Device *dev, FrameObj *F) {
   cudaEventRecord(F->evStop, s);
   cudaMemcpyAsync(F->errHost, F->errFlags.p, sizeof(uint32_t), cudaMemcpyDeviceToHost, s);
   if (F->countStats)
-    cudaMemcpyAsync(F->countersHost, F->counters.p, 24 * sizeof(unsigned long long),
+    cudaMemcpyAsync(F->countersHost, F->counters.p, kStatCounters * sizeof(unsigned long long),
                     cudaMemcpyDeviceToHost, s);
   F->rendered = true;
   if (e != cudaSuccess) {
@@ -2315,7 +2318,7 @@ int vsrGetProperty(VSRDevice dv, VSRObject ov, const char *name, VSRDataType typ
       return 1;
     }
     if (n == "statistics" && type == VSR_UINT64 && size >= 8 * sizeof(uint64_t)) {
-      memcpy(mem, F->countersHost, std::min<size_t>(size, 24 * sizeof(uint64_t)));
+      memcpy(mem, F->countersHost, std::min<size_t>(size, kStatCounters * sizeof(uint64_t)));
       return 1;
     }
   }
@@ -2633,6 +2636,16 @@ int vsrFrameReady(VSRDevice dv, VSRFrame fv, VSRWaitMask mask) {
     d->report(F, VSR_FRAME, VSR_SEVERITY_WARNING, VSR_OK, "device error flags 0x%x in last render",
               *F->errHost);
   return 1;
+}
+
+VSRStatus vsrFrameSampleMask(VSRDevice dv, VSRFrame fv, const uint8_t *mask) {
+  Device *d = asDev(dv);
+  if (!d) return VSR_ERROR_INVALID_ARGUMENT;
+  std::lock_guard<std::recursive_mutex> lk(d->mtx);
+  Object *o = asObj(fv);
+  if (!checkObj(d, o) || o->kind != VSR_FRAME) return VSR_ERROR_INVALID_OBJECT;
+  static_cast<FrameObj *>(o)->sampleMask = mask;
+  return VSR_OK;
 }
 
 VSRStatus vsrDiscardFrame(VSRDevice dv, VSRFrame fv) {

@@ -86,6 +86,19 @@ constexpr int kMaxSurfaceLayers = 1 << 12;
 #endif
 
 constexpr int kTraversalStack = 64;
+// Frame statistics (frame property "statistics", uint64 each, filled by the
+// counting kernel variants when "collectStatistics" is on):
+//   0 rays traced, 1 BVH inner-node visits, 2 primitive tests, 3 ray-march
+//   samples, 4 delta-tracking samples, 5 majorant cells visited,
+//   8..23 histogram of inner-node visits per traversal (bins [2^k, 2^(k+1))),
+//   path tracer only: 24 clock cycles per pixel thread from its start to
+//   its frame write (summed over threads), 25 of them inside surface
+//   traversal, 26 inside delta tracking; 27 warp iterations of the
+//   traversal's inner-node loop x 65536 (each active lane adds
+//   65536 / active lanes), 28 leaf-loop lane iterations, 29 leaf-loop warp
+//   iterations x 65536. SIMT efficiency of the inner-node loop =
+//   [1] / (32 [27] / 65536), of the leaf loop [28] / (32 [29] / 65536).
+constexpr int kStatCounters = 32;
 constexpr int kMaxClipPlanes = 8;
 constexpr uint32_t kLeafCountShift = 27;
 constexpr uint32_t kLeafFirstMask = (1u << kLeafCountShift) - 1u;
@@ -257,6 +270,9 @@ struct DFrame {
   float *accumSq;
   float *variance;
   int pixelSamples;  // samples per frame
+  // optional (null = every pixel): one byte per pixel; the path tracer
+  // leaves pixels whose byte is 0 untouched (no samples, no writes)
+  const uint8_t *sampleMask;
 };
 
 // Wavefront path-tracer state: one slot per pixel, structure of arrays

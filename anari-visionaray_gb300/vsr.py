@@ -80,6 +80,7 @@ _SIGNATURES = [
                                        ctypes.POINTER(ctypes.c_uint32)]),
     ("vsrFrameReady", ctypes.c_int, [_P, _P, ctypes.c_int]),
     ("vsrDiscardFrame", ctypes.c_int, [_P, _P]),
+    ("vsrFrameSampleMask", ctypes.c_int, [_P, _P, _P]),
     ("vsrMapFrame", _P, [_P, _P, ctypes.c_char_p, ctypes.POINTER(ctypes.c_uint32),
                          ctypes.POINTER(ctypes.c_uint32), ctypes.POINTER(ctypes.c_int)]),
     ("vsrUnmapFrame", ctypes.c_int, [_P, _P, ctypes.c_char_p]),
@@ -389,6 +390,13 @@ class Device:
         rc = self.lib.vsrDenoiserFrameInput(self.handle, frame.ptr, x_ptr)
         if rc:
             raise RuntimeError(f"vsrDenoiserFrameInput failed ({rc})")
+
+    def sample_mask(self, frame, mask_ptr):
+        """Restrict the frame's path tracer to pixels whose mask byte is
+        nonzero (a device pointer, one byte per pixel; None or 0 for all)."""
+        rc = self.lib.vsrFrameSampleMask(self.handle, frame.ptr, mask_ptr or None)
+        if rc:
+            raise RuntimeError(f"vsrFrameSampleMask failed ({rc})")
 
     def render_batch(self, frames):
         """Render several frames as one batch (vsrRenderFrames)."""

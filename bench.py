@@ -45,7 +45,7 @@ def parse():
     p.add_argument("--res", type=int, default=1024)
     p.add_argument("--spp", type=int, default=64)
     p.add_argument("--e2e-steps", type=int, default=8)
-    p.add_argument("--cpu-rows", type=int, default=48,
+    p.add_argument("--cpu-rows", type=int, default=192,
                    help="rows of the frame the CPU baseline renders (bounded sample)")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--accum-frames", type=int, default=64,
@@ -204,6 +204,22 @@ def cpu_baseline(scene, rows, threads=0, keep=False):
     if keep:
         return px * spp / dt / MPX, dt, px, cores, [(s, s + per) for s in starts], F.color
     return px * spp / dt / MPX, dt, px, cores
+
+
+def phase_split(c):
+    """From the counting frame's statistics: the share of the path tracer's
+    per-thread time spent in surface traversal and in delta tracking, and
+    the SIMT efficiency (active lanes / 32) of the traversal's inner-node
+    and leaf loops."""
+    if len(c) < 30 or not c[24]:
+        return {}
+    out = {"time_share_surface_traversal": c[25] / c[24],
+           "time_share_delta_tracking": c[26] / c[24]}
+    if c[27]:
+        out["simt_inner_node_loop"] = c[1] / (32.0 * c[27] / 65536.0)
+    if c[29]:
+        out["simt_leaf_loop"] = c[28] / (32.0 * c[29] / 65536.0)
+    return out
 
 
 def issue_roofline(kernel_s, spp, res, sms=None):
@@ -634,7 +650,7 @@ def run_ours(args):
     dev.commit(frame)
     dev.render(frame)
     dev.wait(frame)
-    counts = dev.get_u64(frame, "statistics", 24) or [0] * 24
+    counts = dev.get_u64(frame, "statistics", 32) or [0] * 32
     dev.set(frame, "collectStatistics", False)
     dev.commit(frame)
 
@@ -765,7 +781,8 @@ def run_ours(args):
                                     "DRAM traffic"},
         "traversal": {"rays": rays, "node_visits": nodes, "tri_tests": tris,
                       "node_visit_histogram_log2": counts[8:24],
-                      "grays_per_s": rays / kernel_s / 1e9},
+                      "grays_per_s": rays / kernel_s / 1e9,
+                      **phase_split(counts)},
         "config1_accumulated_1spp": accum,
         "commit_s": commit_s, "bvh_build_s": bvh_s, "raycast_config0": raycast,
         "raycast_config0_gradient_shading": shaded,

@@ -262,6 +262,18 @@ VSR_API VSRStatus vsrDenoiseFrame(VSRDevice d, VSRDenoiser n, VSRFrame f, float 
                                   float floorAbs, float *colorOut, uint8_t *retry,
                                   uint32_t *numRetry);
 
+/* Per-pixel sample mask of a frame's path tracer (no counterpart in the
+   reference): one byte per pixel in device memory (the caller's, e.g. the
+   retry mask of vsrDenoiseFrame), null for every pixel. Following renders
+   of the path tracer take samples only for pixels whose byte is nonzero;
+   the others keep their colour, accumulation and G-buffer. Setting it does
+   not restart accumulation. The running mean weights every frame since the
+   last reset, so keep a mask fixed while accumulating: a pixel is exact if
+   it was rendered in every frame since then (the variance gate's loop:
+   all pixels once, then only the rejected ones). The raycast renderer
+   ignores it. The buffer must stay valid while renders that use it run. */
+VSR_API VSRStatus vsrFrameSampleMask(VSRDevice d, VSRFrame f, const uint8_t *mask);
+
 /* Work list of a batch, without a device (vsrPlanBatch has no counterpart in
    the reference): tiles of tileWidth x (32 / tileWidth) pixels for jobs of
    the given sizes, as (job, tile) uint32 pairs ordered by cost per pixel,

@@ -1,5 +1,8 @@
 import importlib
 import os
+import platform
+import shutil
+import subprocess
 import sys
 
 import pytest
@@ -31,3 +34,21 @@ def device(pkg):
     dev = pkg.vsr.Device()
     yield dev
     dev.close()
+
+
+@pytest.fixture(scope="session")
+def contracted(oracle, tmp_path_factory):
+    """Path of a second liboracle.so built with multiply-add contraction
+    (-ffp-contract=fast): it rounds like a compiler that fuses multiplies
+    and adds, so comparing it with the plain oracle measures how sensitive a
+    scene is to last-bit differences."""
+    cxx = shutil.which("g++")
+    if cxx is None:
+        pytest.skip("no C++ compiler")
+    out = str(tmp_path_factory.mktemp("fma") / "liboracle.so")
+    flags = ["-std=c++17", "-O3", "-fPIC", "-pthread", "-shared", "-ffp-contract=fast"]
+    if platform.machine() in ("x86_64", "AMD64"):
+        flags.append("-mfma")  # x86 needs FMA enabled; aarch64 has it
+    src = os.path.join(ROOT, "oracle", "oracle.cpp")
+    subprocess.run([cxx, *flags, "-o", out, src], check=True)
+    return out

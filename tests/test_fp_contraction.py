@@ -10,11 +10,7 @@ Each check asks for a clear margin above the bar of the GPU test that uses
 the scene (raycast: 2e-3 on 99.9 % of pixels; path tracer with the same
 stream: 1e-3 on 97 %).
 """
-import ctypes
 import os
-import platform
-import shutil
-import subprocess
 import sys
 
 import numpy as np
@@ -22,21 +18,6 @@ import pytest
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, HERE)
-
-
-@pytest.fixture(scope="module")
-def contracted(oracle, tmp_path_factory):
-    """Path of a liboracle.so built with multiply-add contraction."""
-    cxx = shutil.which("g++")
-    if cxx is None:
-        pytest.skip("no C++ compiler")
-    out = str(tmp_path_factory.mktemp("fma") / "liboracle.so")
-    flags = ["-std=c++17", "-O3", "-fPIC", "-pthread", "-shared", "-ffp-contract=fast"]
-    if platform.machine() in ("x86_64", "AMD64"):
-        flags.append("-mfma")  # x86 needs FMA enabled; aarch64 has it
-    src = os.path.join(os.path.dirname(HERE), "oracle", "oracle.cpp")
-    subprocess.run([cxx, *flags, "-o", out, src], check=True)
-    return out
 
 
 def render_both(oracle, contracted, scene):

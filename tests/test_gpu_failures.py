@@ -37,7 +37,7 @@ def test_march_step_limit_sets_error_flag(pkg, device, oracle, surfaces):
                            "indices": np.array([[0, 1, 2]], np.uint32),
                            "material": {"type": "matte", "color": [0.5, 0.5, 0.5]}}]
     sc["renderer"]["volumeSamplingRate"] = 2.0e7  # dt = 5e-8 voxel: ~6e8 steps per ray
-    h = pkg.scenes.build(device, sc, channels=("depth",))
+    h = pkg.scenes.build(device, sc, channels=("color", "depth"))
     n0 = len(device.messages)
     assert device.render(h["frame"]) == 0
     assert device.wait(h["frame"])

@@ -66,6 +66,12 @@ __global__ void kFrameReset(float4 *accum, float *depth, size_t n) {
   }
 }
 
+__global__ void kFillU32(uint32_t *p, uint32_t v, size_t n) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n;
+       i += (size_t)gridDim.x * blockDim.x)
+    p[i] = v;
+}
+
 } // namespace
 
 cudaError_t launchBrickMajorants(const float *field, const int dims[3], int brick,
@@ -87,6 +93,15 @@ cudaError_t launchFrameReset(float4 *accum, float *depth, size_t n, cudaStream_t
   const int blocks = (int)((n + threads - 1) / threads < 152 * 16 ? (n + threads - 1) / threads
                                                                    : 152 * 16);
   kFrameReset<<<blocks, threads, 0, stream>>>(accum, depth, n);
+  return cudaGetLastError();
+}
+
+cudaError_t launchFillU32(uint32_t *p, uint32_t value, size_t n, cudaStream_t stream) {
+  if (n == 0) return cudaSuccess;
+  const int threads = 256;
+  const size_t want = (n + threads - 1) / threads;
+  const int blocks = (int)(want < 152 * 16 ? want : 152 * 16);
+  kFillU32<<<blocks, threads, 0, stream>>>(p, value, n);
   return cudaGetLastError();
 }
 

@@ -171,6 +171,8 @@ cudaError_t launchDenoiseOutput(const float *out, int oC, int W, int H, int Wp, 
 
 // Accumulation reset: accum = 0, depth = 1e31 (frame/Frame.cpp:287-312).
 cudaError_t launchFrameReset(float4 *accum, float *depth, size_t numPixels, cudaStream_t stream);
+// p[0 .. n) = value
+cudaError_t launchFillU32(uint32_t *p, uint32_t value, size_t n, cudaStream_t stream);
 
 // Brick majorant grid of a structured volume: one cell per brick of
 // `brick` voxels per edge; majorant = max TF alpha over the TF bins that the

@@ -1304,7 +1304,12 @@ __device__ __forceinline__ void writeSample(const DFrame &F, int x, int y, bool 
     }
   }
   if (stochastic) {
-    const float a = 1.f / (F.accumID + 1);
+    int frames = F.accumID;  // frames already in this pixel's mean
+    if (F.pixelFrames) {
+      frames = (int)F.pixelFrames[idx];
+      F.pixelFrames[idx] = (uint32_t)frames + 1u;
+    }
+    const float a = 1.f / (frames + 1);
     const float4 acc = F.accum[idx];
     color = make_float4((1 - a) * acc.x + a * color.x, (1 - a) * acc.y + a * color.y,
                         (1 - a) * acc.z + a * color.z, (1 - a) * acc.w + a * color.w);
@@ -1314,7 +1319,7 @@ __device__ __forceinline__ void writeSample(const DFrame &F, int x, int y, bool 
       const float m2 = (1 - a) * F.accumSq[idx] + a * lumSqMean;
       F.accumSq[idx] = m2;
       const float lm = 0.3f * color.x + 0.59f * color.y + 0.11f * color.z;
-      const float n = (float)(F.accumID + 1) * (float)F.pixelSamples;
+      const float n = (float)(frames + 1) * (float)F.pixelSamples;
       F.variance[idx] = n > 1.f ? fmaxf(m2 - lm * lm, 0.f) / (n - 1.f) : FLT_MAX;
     }
   }

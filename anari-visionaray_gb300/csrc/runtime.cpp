@@ -1491,6 +1491,7 @@ struct FrameObj : Object {
   int lastIterations = 0;
   int batchTileW = 0, batchFetch = 0, batchTuned = 0;  // last batched render
   const uint8_t *sampleMask = nullptr;  // caller's device mask (vsrFrameSampleMask)
+  DevBuf pixelFrames;  // frames per pixel, made by the first sample mask
 
   // scratch of the segmented volume marcher, made on first use: the ray list
   // (48 B per pixel), groups (16 B per 32 pixels) and work units for
@@ -1590,6 +1591,11 @@ struct FrameObj : Object {
     width = (int)sz[0];
     height = (int)sz[1];
     size_t np = (size_t)width * height;
+    if (pixelFrames.p && pixelFrames.bytes != np * sizeof(uint32_t)) {
+      // a mask of the old size does not fit the new one
+      pixelFrames.release();
+      sampleMask = nullptr;
+    }
     {
       bool ok = accum.alloc(np * sizeof(float4)) == cudaSuccess &&
                 depth.alloc(np * sizeof(float)) == cudaSuccess &&
@@ -1641,6 +1647,7 @@ struct FrameObj : Object {
     f.variance = variance.as<float>();
     f.pixelSamples = renderer ? renderer->r.pixelSamples : 1;
     f.sampleMask = sampleMask;
+    f.pixelFrames = pixelFrames.as<uint32_t>();
     return f;
   }
 };
@@ -1703,8 +1710,10 @@ VSRStatus renderFrame(Device *dev, FrameObj *F) {
   }
   const DFrame fr = F->record();
   cudaEventRecord(F->evStart, s);
-  if (reset)
+  if (reset) {
     launchFrameReset(F->accum.as<float4>(), F->depth.as<float>(), (size_t)F->width * F->height, s);
+    if (F->pixelFrames.p) cudaMemsetAsync(F->pixelFrames.p, 0, (size_t)F->width * F->height * 4, s);
+  }
   cudaMemsetAsync(F->errFlags.p, 0, sizeof(uint32_t), s);
   if (F->countStats)
     cudaMemsetAsync(F->counters.p, 0, kStatCounters * sizeof(unsigned long long), s);
@@ -2644,7 +2653,21 @@ VSRStatus vsrFrameSampleMask(VSRDevice dv, VSRFrame fv, const uint8_t *mask) {
   std::lock_guard<std::recursive_mutex> lk(d->mtx);
   Object *o = asObj(fv);
   if (!checkObj(d, o) || o->kind != VSR_FRAME) return VSR_ERROR_INVALID_OBJECT;
-  static_cast<FrameObj *>(o)->sampleMask = mask;
+  FrameObj *F = static_cast<FrameObj *>(o);
+  if (mask && !F->pixelFrames.p) {
+    // from now on each pixel counts its own frames, starting from the
+    // frames accumulated so far
+    const size_t np = (size_t)F->width * F->height;
+    if (F->pixelFrames.alloc(np * sizeof(uint32_t)) != cudaSuccess) {
+      d->report(F, VSR_FRAME, VSR_SEVERITY_ERROR, VSR_ERROR_OUT_OF_MEMORY,
+                "sample mask: per-pixel frame counts could not be allocated");
+      return VSR_ERROR_OUT_OF_MEMORY;
+    }
+    const uint32_t start = F->nextReset ? 0u : (uint32_t)F->accumID;
+    if (launchFillU32(F->pixelFrames.as<uint32_t>(), start, np, d->stream) != cudaSuccess)
+      return VSR_ERROR_CUDA;
+  }
+  F->sampleMask = mask;
   return VSR_OK;
 }
 

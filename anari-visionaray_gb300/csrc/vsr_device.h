@@ -273,6 +273,10 @@ struct DFrame {
   // optional (null = every pixel): one byte per pixel; the path tracer
   // leaves pixels whose byte is 0 untouched (no samples, no writes)
   const uint8_t *sampleMask;
+  // optional (null = every pixel has accumID frames): frames accumulated
+  // per pixel, kept once a frame has had a sample mask; the running mean
+  // and the variance then weight each pixel by its own count
+  uint32_t *pixelFrames;
 };
 
 // Wavefront path-tracer state: one slot per pixel, structure of arrays

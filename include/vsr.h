@@ -267,11 +267,13 @@ VSR_API VSRStatus vsrDenoiseFrame(VSRDevice d, VSRDenoiser n, VSRFrame f, float 
    retry mask of vsrDenoiseFrame), null for every pixel. Following renders
    of the path tracer take samples only for pixels whose byte is nonzero;
    the others keep their colour, accumulation and G-buffer. Setting it does
-   not restart accumulation. The running mean weights every frame since the
-   last reset, so keep a mask fixed while accumulating: a pixel is exact if
-   it was rendered in every frame since then (the variance gate's loop:
-   all pixels once, then only the rejected ones). The raycast renderer
-   ignores it. The buffer must stay valid while renders that use it run. */
+   not restart accumulation. From the first mask on, the frame counts the
+   frames accumulated in each pixel (starting from those accumulated so
+   far), and each pixel's running mean and variance weight its own count,
+   so masks may change between renders. A committed frame size change drops
+   the mask. The denoiser's 1/sqrt(samples) input stays the frame-wide
+   value. The raycast renderer ignores the mask. The buffer must stay valid
+   while renders that use it run. */
 VSR_API VSRStatus vsrFrameSampleMask(VSRDevice d, VSRFrame f, const uint8_t *mask);
 
 /* Work list of a batch, without a device (vsrPlanBatch has no counterpart in

@@ -303,8 +303,6 @@ __device__ __forceinline__ void pathtracePixel(const DScene &S, const DCamera &C
     yf += jy;
     Ray ray = primaryRay<true>(C, rnd, xf, yf, (float)W, (float)H);
     float4 pc = make_float4(R.bg[0], R.bg[1], R.bg[2], R.bg[3]);
-    float pDepth = 1e31f;
-    float3 pNg = f3(0.f), pAlb = f3(0.f);
     if (S.numInstances > 0) {
       bool firstHit = false;
       int rayType = RT_RADIANCE;
@@ -315,13 +313,15 @@ __device__ __forceinline__ void pathtracePixel(const DScene &S, const DCamera &C
       float aoWeights = 0.f, aoCount = 0.f;
       BSDFSample bsdf;
       bsdf.dir = f3(0.f); bsdf.f = f3(0.f); bsdf.pdf = 0.f; bsdf.cosT = 0.f;
-      LightSample ls;
-      ls.intensity = f3(0.f); ls.dir = f3(0.f); ls.pdf = 0.f; ls.dist = 0.f; ls.dist2 = 0.f;
       float misWeightNEE = 0.f, visLight = 1.f, visAO = 1.f;
       unsigned bounceID = 0;
       for (int passID = 0; true; ++passID) {
         if (passID >= maxPasses) { err |= ERR_PATH_LIMIT; break; }
         clipRay(ray, R);
+        // the pass's light sample (zero when the scene has no light): it is
+        // used by this pass only, so it is not carried across the traversal
+        LightSample ls;
+        ls.intensity = f3(0.f); ls.dir = f3(0.f); ls.pdf = 0.f; ls.dist = 0.f; ls.dist2 = 0.f;
         HitRec hr;
         if (rayType == RT_SHADOW && S.numLights == 0) {
           // the shadow ray of a light-less scene has a NaN direction and
@@ -370,7 +370,6 @@ __device__ __forceinline__ void pathtracePixel(const DScene &S, const DCamera &C
               sn = faceforward(sn, viewDir, gn);
               gn = faceforward(gn, viewDir, gn);
               color = hr.volAlbedo;
-              if (bounceID == 0) pDepth = hr.volT;
             } else {
               const DInstance &I = S.instances[hr.surf.inst];
               const DGroup &G = S.groups[I.group];
@@ -383,11 +382,16 @@ __device__ __forceinline__ void pathtracePixel(const DScene &S, const DCamera &C
               sn = faceforward(sn, viewDir, gn);
               gn = faceforward(gn, viewDir, gn);
               color = materialColor(*mat);
-              if (bounceID == 0) pDepth = hr.surf.t;
             }
             if (bounceID == 0) {
-              pNg = gn;
-              pAlb = color;
+              // the closest first hit over the pixel's samples feeds the
+              // G-buffer (Pathtrace_impl.cpp:616-618), merged right here
+              const float d0 = hr.volumeHit ? hr.volT : hr.surf.t;
+              if (d0 < cDepth) {
+                cDepth = d0;
+                cNg = gn;
+                cAlb = color;
+              }
             }
             hitPosOff = hitPos + sn * eps;
             if (S.numLights > 0) {
@@ -495,11 +499,6 @@ __device__ __forceinline__ void pathtracePixel(const DScene &S, const DCamera &C
     accum.x += pc.x; accum.y += pc.y; accum.z += pc.z; accum.w += pc.w;
     const float lum = 0.3f * pc.x + 0.59f * pc.y + 0.11f * pc.z;
     lumSq += lum * lum;
-    if (pDepth < cDepth) {
-      cDepth = pDepth;
-      cNg = pNg;
-      cAlb = pAlb;
-    }
   }
   const float inv = 1.f / R.pixelSamples;
   if (Count) atomicAdd(&cnt[24], (unsigned long long)(clock64() - tStart));

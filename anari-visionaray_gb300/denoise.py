@@ -271,3 +271,67 @@ def at_input_spp(plain, dn, pt_s_per_spp, dn_s, spp=4):
     return {"input_spp": spp, "denoised_rmse_tm": e, "plain_spp_same_rmse": s_eq,
             "plain_s_1080p": t_plain, "denoised_s_1080p": t_dn,
             "speedup_at_that_rmse": t_plain / t_dn}
+
+
+def evaluate_gated_loop(dev, dn, seeds, res=256, ref_spp=4096, input_spp=4, rounds=4,
+                        frames_per_round=4, k=3.0, floor=0.01):
+    """The variance gate as a loop: after input_spp samples per pixel (one
+    frame of 4 spp per 4 samples), denoise and gate; the pixels the gate
+    rejects get frames_per_round more frames (4 spp each) through the
+    frame's sample mask (vsrFrameSampleMask), then the frame is denoised and
+    gated again, up to `rounds` times. Per round r (0 = after the input
+    samples only), pooled over the scenes: the tone-mapped RMSE of the gated
+    image against ref_spp references, the share of pixels the gate sent
+    back, and the samples per pixel spent so far (all pixels' input samples
+    plus the rejected pixels' extra ones, divided by the pixel count)."""
+    import torch
+
+    npx = res * res
+    sq = {}
+    spent = {}
+    retried = {}
+    mask = torch.zeros(npx, dtype=torch.uint8, device="cuda")
+    out = torch.zeros((npx, 4), dtype=torch.float32, device="cuda")
+    for seed in seeds:
+        h = build(dev, training_scene(seed, res, 4), variance=True)
+        ref = render_reference(dev, h, ref_spp)
+        for _ in range(max(1, input_spp // 4)):
+            dev.render(h["frame"])
+        dev.wait(h["frame"])
+        px_spp = float(npx * input_spp)
+        for r in range(rounds + 1):
+            nret = dn.denoise_frame(h["frame"], out.data_ptr(), k=k, floor=floor,
+                                    retry_ptr=mask.data_ptr())
+            img = out.cpu().numpy().reshape(res, res, 4)
+            sq[r] = sq.get(r, 0.0) + sq_errors(img, ref)[1]
+            spent[r] = spent.get(r, 0.0) + px_spp
+            retried[r] = retried.get(r, 0) + nret
+            if r == rounds:
+                break
+            dev.sample_mask(h["frame"], mask.data_ptr())
+            for _ in range(frames_per_round):
+                dev.render(h["frame"])
+            dev.wait(h["frame"])
+            px_spp += float(nret) * 4 * frames_per_round
+        dev.sample_mask(h["frame"], None)
+        release(dev, h)
+    n = len(seeds)
+    return [{"round": r, "rmse_tm": math.sqrt(sq[r] / (3.0 * npx * n)),
+             "retry_share": retried[r] / (npx * n), "spp_per_pixel": spent[r] / (npx * n)}
+            for r in sorted(sq)]
+
+
+def gated_loop_times(loop, pt_s_per_spp, dn_s, masked_s_per_px_spp, px_1080p=1920 * 1080,
+                     frames_per_round=4):
+    """Seconds at 1920x1080 to reach each round of evaluate_gated_loop: the
+    input samples over every pixel, the rejected pixels' extra samples at
+    the measured per-pixel-sample cost of masked frames, and one denoiser
+    pass per round."""
+    out = []
+    for e in loop:
+        r = e["round"]
+        t = loop[0]["spp_per_pixel"] * pt_s_per_spp + (r + 1) * dn_s
+        for q in loop[:r]:
+            t += q["retry_share"] * px_1080p * 4 * frames_per_round * masked_s_per_px_spp
+        out.append(dict(e, s_1080p=t))
+    return out

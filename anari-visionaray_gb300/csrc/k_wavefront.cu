@@ -193,6 +193,187 @@ __global__ void __launch_bounds__(256, VSR_WAVE_TRACE_MIN_BLOCKS) kWaveTrace(
   if (err) atomicOr(errFlags, err);
 }
 
+// Persistent traversal with dynamic ray fetch (Aila and Laine's scheme):
+// each lane traverses one queued ray over BVH2 groups, keeping its
+// traversal state (node, stack, closest hit, instance) across iterations
+// of the warp's loop; whenever kRefill or more lanes of the warp are idle,
+// the warp takes that many new queue entries with one atomic, so lanes do
+// not wait for the warp's longest ray. Hits follow the same closest-hit
+// order (t, instance, triangle) and any-hit rule as traceSurfaces, so the
+// hit records equal kWaveTrace's. Queue entries are handed out through a
+// per-parity counter in Wv.count[2 + cur], zeroed by the previous trace
+// launch (and by the frame's initial memset).
+constexpr unsigned kFullMask = 0xffffffffu;
+#ifndef VSR_WAVE_REFILL
+#define VSR_WAVE_REFILL 8  // idle lanes of a warp that trigger a fetch of new rays
+#endif
+constexpr int kRefill = VSR_WAVE_REFILL;
+
+template <bool Count>
+__global__ void __launch_bounds__(128, VSR_WAVE_DYN_MIN_BLOCKS) kWaveTraceDyn(
+    DScene S, DWave Wv, int cur, uint32_t *errFlags, unsigned long long *cnt) {
+  const uint32_t n = Wv.count[cur];
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    Wv.count[cur ^ 1] = 0;
+    Wv.count[2 + (cur ^ 1)] = 0;
+  }
+  const uint32_t *q = Wv.queue[cur];
+  uint32_t *fetch = &Wv.count[2 + cur];
+  const int lane = threadIdx.x & 31;
+  const unsigned below = (1u << lane) - 1u;
+  uint32_t err = 0;
+  bool active = false, exhausted = false;
+  uint32_t p = 0;
+  // the lane's ray in its current instance's object space
+  float3 o = f3(0.f), d = f3(0.f), inv = f3(0.f), oi = f3(0.f);
+  float tmin = 0.f;
+  const float4 *nodes = nullptr, *tris = nullptr;
+  Hit best;
+  best.t = 0.f; best.u = best.v = 0.f; best.inst = best.tri = best.leaf = -1;
+  int node = 0, sp = 0, inst = 0;
+  bool anyHit = false, found = false, done = true;
+  int stack[kTraversalStack];
+  unsigned nodeVisits = 0, triTests = 0;
+
+  // first instance at or after `inst` with triangles: transform the ray
+  auto enterInstance = [&]() -> bool {
+    while (inst < S.numInstances && S.groups[S.instances[inst].group].numNodes == 0) ++inst;
+    if (inst >= S.numInstances) return false;
+    const DInstance &I = S.instances[inst];
+    const DGroup &G = S.groups[I.group];
+    const float4 a = Wv.rayO[p], b = Wv.rayD[p];
+    localRay(I, xyz(a), xyz(b), o, d);
+    inv = f3(1.f / d.x, 1.f / d.y, 1.f / d.z);
+    oi = f3(-o.x * inv.x, -o.y * inv.y, -o.z * inv.z);
+    nodes = G.nodes;
+    tris = G.tris;
+    node = 0;
+    sp = 0;
+    done = false;
+    return true;
+  };
+  auto finish = [&]() {
+    Wv.hit[p] = found ? make_int4(__float_as_int(best.t), best.inst, best.tri, best.leaf)
+                      : make_int4(__float_as_int(FLT_MAX), -1, -1, -1);
+    if (Count) {
+      atomicAdd(&cnt[0], 1ull);
+      atomicAdd(&cnt[1], (unsigned long long)nodeVisits);
+      atomicAdd(&cnt[2], (unsigned long long)triTests);
+      const int bin = nodeVisits ? min(31 - __clz(nodeVisits), 15) : 0;
+      atomicAdd(&cnt[8 + bin], 1ull);
+    }
+    active = false;
+  };
+
+  while (true) {
+    // ---- dynamic fetch
+    const unsigned idle = __ballot_sync(kFullMask, !active);
+    if (!exhausted && idle && (__popc(idle) >= kRefill || idle == kFullMask)) {
+      const int leader = __ffs(idle) - 1;
+      uint32_t base = 0;
+      if (lane == leader) base = atomicAdd(fetch, (uint32_t)__popc(idle));
+      base = __shfl_sync(kFullMask, base, leader);
+      if (base + (uint32_t)__popc(idle) >= n) exhausted = true;
+      if (!active) {
+        const uint32_t i = base + (uint32_t)__popc(idle & below);
+        if (i < n) {
+          p = q[i];
+          const uint32_t flags = Wv.meta[p].z;
+          const uint32_t rt = fRayType(flags);
+          tmin = Wv.rayO[p].w;
+          best.t = Wv.rayD[p].w;
+          best.u = best.v = 0.f;
+          best.inst = best.tri = best.leaf = -1;
+          found = false;
+          nodeVisits = triTests = 0;
+          inst = 0;
+          anyHit = (rt == RT_SHADOW || rt == RT_AO) && S.allOpaque && !fRetrace(flags);
+          const bool skip = (rt == RT_SHADOW && S.numLights == 0) || !S.hasSurfaces;
+          active = true;
+          if (skip || !enterInstance()) finish();
+        }
+      }
+    }
+    if (!__any_sync(kFullMask, active)) {
+      if (exhausted) break;
+      continue;
+    }
+    if (!active) continue;
+    // ---- one while-while step of the lane's traversal
+    while (!done && node >= 0) {
+      const float4 *N = nodes + 4 * (size_t)node;
+      const float4 n0 = __ldg(N), n1 = __ldg(N + 1), n2 = __ldg(N + 2);
+      const int4 n3 = __ldg(reinterpret_cast<const int4 *>(N + 3));
+      if (Count) ++nodeVisits;
+      const float tb = best.t;
+      float a0 = fmaf(n0.x, inv.x, oi.x), b0 = fmaf(n0.y, inv.x, oi.x);
+      float a1 = fmaf(n0.z, inv.y, oi.y), b1 = fmaf(n0.w, inv.y, oi.y);
+      float a2 = fmaf(n2.x, inv.z, oi.z), b2 = fmaf(n2.y, inv.z, oi.z);
+      const float c0min = fmaxf(fmaxf(fminf(a0, b0), fminf(a1, b1)), fmaxf(fminf(a2, b2), tmin));
+      const float c0max = fminf(fminf(fmaxf(a0, b0), fmaxf(a1, b1)), fminf(fmaxf(a2, b2), tb));
+      a0 = fmaf(n1.x, inv.x, oi.x); b0 = fmaf(n1.y, inv.x, oi.x);
+      a1 = fmaf(n1.z, inv.y, oi.y); b1 = fmaf(n1.w, inv.y, oi.y);
+      a2 = fmaf(n2.z, inv.z, oi.z); b2 = fmaf(n2.w, inv.z, oi.z);
+      const float c1min = fmaxf(fmaxf(fminf(a0, b0), fminf(a1, b1)), fmaxf(fminf(a2, b2), tmin));
+      const float c1max = fminf(fminf(fmaxf(a0, b0), fmaxf(a1, b1)), fminf(fmaxf(a2, b2), tb));
+      const bool h0 = c0min <= c0max, h1 = c1min <= c1max;
+      if (!h0 && !h1) {
+        if (sp == 0) done = true;
+        else node = stack[--sp];
+      } else {
+        int near = h0 ? n3.x : n3.y;
+        if (h0 && h1) {
+          int far = n3.y;
+          if (c1min < c0min) { near = n3.y; far = n3.x; }
+          if (sp < kTraversalStack) stack[sp++] = far;
+          else err |= ERR_STACK_OVERFLOW;
+        }
+        node = near;
+      }
+    }
+    while (!done && node < 0) {
+      const uint32_t code = ~(uint32_t)node;
+      const int first = (int)(code & kLeafFirstMask);
+      const int count = (int)(code >> kLeafCountShift) + 1;
+      for (int k = 0; k < count; ++k) {
+        const float4 *T = tris + 3 * (size_t)(first + k);
+        const float4 ta = __ldg(T), tbv = __ldg(T + 1), tc = __ldg(T + 2);
+        if (Count) ++triTests;
+        const float3 v1 = f3(ta.x, ta.y, ta.z), e1 = f3(tbv.x, tbv.y, tbv.z),
+                     e2 = f3(tc.x, tc.y, tc.z);
+        const float3 s1 = cross(d, e2);
+        const float div = dot(s1, e1);
+        if (div == 0.f) continue;
+        const float idiv = 1.f / div;
+        const float3 dd = o - v1;
+        const float bb1 = dot(dd, s1) * idiv;
+        if (bb1 < 0.f || bb1 > 1.f) continue;
+        const float3 s2 = cross(dd, e1);
+        const float bb2 = dot(d, s2) * idiv;
+        if (bb2 < 0.f || bb1 + bb2 > 1.f) continue;
+        const float t = dot(e2, s2) * idiv;
+        if (!(t >= tmin)) continue;
+        const int local = __float_as_int(ta.w);
+        const bool closer =
+            t < best.t || (t == best.t && best.inst >= 0 &&
+                           (inst < best.inst || (inst == best.inst && local < best.tri)));
+        if (!closer) continue;
+        best.t = t; best.u = bb1; best.v = bb2; best.inst = inst; best.tri = local;
+        best.leaf = first + k;
+        found = true;
+      }
+      if ((anyHit && found) || sp == 0) done = true;
+      else node = stack[--sp];
+    }
+    if (done) {
+      // this instance is through: the next one, or the ray is finished
+      ++inst;
+      if ((anyHit && found) || !enterInstance()) finish();
+    }
+  }
+  if (err) atomicOr(errFlags, err);
+}
+
 template <bool Count>
 __global__ void __launch_bounds__(256, VSR_WAVE_SHADE_MIN_BLOCKS) kWaveShade(
     DScene S, DCamera C, DRenderer R, DFrame F, DWave Wv, int cur) {
@@ -503,14 +684,17 @@ cudaError_t launchPathtraceWavefront(const DScene &S, const DCamera &C, const DR
                                      const DFrame &F, const DWave &Wv, uint32_t *pinnedCount,
                                      bool count, cudaStream_t stream, int *iterations) {
   const int B = 256;
-  cudaError_t e = cudaMemsetAsync(Wv.count, 0, 2 * sizeof(uint32_t), stream);
+  cudaError_t e = cudaMemsetAsync(Wv.count, 0, 4 * sizeof(uint32_t), stream);
   if (e != cudaSuccess) return e;
   const int gInit = gridFor((const void *)kWaveInit, B);
   kWaveInit<<<gInit, B, 0, stream>>>(S, C, R, F, Wv);
   if ((e = cudaGetLastError()) != cudaSuccess) return e;
   const void *tk = count ? (const void *)kWaveTrace<true> : (const void *)kWaveTrace<false>;
   const void *sk = count ? (const void *)kWaveShade<true> : (const void *)kWaveShade<false>;
-  const int gTrace = gridFor(tk, B), gShade = gridFor(sk, B);
+  const void *dk = count ? (const void *)kWaveTraceDyn<true> : (const void *)kWaveTraceDyn<false>;
+  const int gTrace = gridFor(tk, B), gShade = gridFor(sk, B), gDyn = gridFor(dk, 128);
+  // persistent dynamic-fetch traversal for worlds of 2-wide BVHs
+  const bool dyn = S.maxGroupWidth == 2;
   int cur = 0, iters = 0;
   const int batch = 16;
   // every pixel finishes after at most spp * maxPasses iterations (plus
@@ -521,10 +705,12 @@ cudaError_t launchPathtraceWavefront(const DScene &S, const DCamera &C, const DR
   while (iters < maxIters) {
     for (int b = 0; b < batch; ++b) {
       if (count) {
-        kWaveTrace<true><<<gTrace, B, 0, stream>>>(S, Wv, cur, F.errorFlags, F.counters);
+        if (dyn) kWaveTraceDyn<true><<<gDyn, 128, 0, stream>>>(S, Wv, cur, F.errorFlags, F.counters);
+        else kWaveTrace<true><<<gTrace, B, 0, stream>>>(S, Wv, cur, F.errorFlags, F.counters);
         kWaveShade<true><<<gShade, B, 0, stream>>>(S, C, R, F, Wv, cur);
       } else {
-        kWaveTrace<false><<<gTrace, B, 0, stream>>>(S, Wv, cur, F.errorFlags, F.counters);
+        if (dyn) kWaveTraceDyn<false><<<gDyn, 128, 0, stream>>>(S, Wv, cur, F.errorFlags, F.counters);
+        else kWaveTrace<false><<<gTrace, B, 0, stream>>>(S, Wv, cur, F.errorFlags, F.counters);
         kWaveShade<false><<<gShade, B, 0, stream>>>(S, C, R, F, Wv, cur);
       }
       cur ^= 1;

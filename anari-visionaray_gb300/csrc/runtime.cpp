@@ -1449,6 +1449,8 @@ struct World : Object {
     scene.numAnalytic = numAnalytic;
     scene.quadGroups = quadGroups;
     scene.numIso = numIso;
+    scene.maxGroupWidth = 2;
+    for (const DGroup &g : dgroups) scene.maxGroupWidth = std::max(scene.maxGroupWidth, g.width);
     builtStamp = deep;
     commitMs = std::chrono::duration<float, std::milli>(std::chrono::steady_clock::now() - t0).count();
     return true;
@@ -1524,7 +1526,7 @@ struct FrameObj : Object {
          waveHit.alloc(np * sizeof(int4)) == cudaSuccess &&
          waveQueue[0].alloc(np * sizeof(uint32_t)) == cudaSuccess &&
          waveQueue[1].alloc(np * sizeof(uint32_t)) == cudaSuccess &&
-         waveCount.alloc(2 * sizeof(uint32_t)) == cudaSuccess;
+         waveCount.alloc(4 * sizeof(uint32_t)) == cudaSuccess;
     if (!pinnedCount) ok = ok && cudaMallocHost((void **)&pinnedCount, sizeof(uint32_t)) == cudaSuccess;
     wavePixels = ok ? np : 0;
     return ok;

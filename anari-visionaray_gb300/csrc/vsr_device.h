@@ -84,6 +84,9 @@ constexpr int kMaxSurfaceLayers = 1 << 12;
 #ifndef VSR_WAVE_SHADE_MIN_BLOCKS
 #define VSR_WAVE_SHADE_MIN_BLOCKS 1
 #endif
+#ifndef VSR_WAVE_DYN_MIN_BLOCKS
+#define VSR_WAVE_DYN_MIN_BLOCKS 8  // persistent traversal: 128-thread blocks, <= 64 registers
+#endif
 
 constexpr int kTraversalStack = 64;
 // Frame statistics (frame property "statistics", uint64 each, filled by the
@@ -224,6 +227,7 @@ struct DScene {
   int numVolumes;
   int allOpaque;
   int hasSurfaces;
+  int maxGroupWidth;  // widest group BVH (2 or 4)
 };
 
 struct DCamera {
@@ -301,7 +305,7 @@ struct DWave {
   uint4 *meta;
   int4 *hit;
   uint32_t *queue[2];
-  uint32_t *count;  // [0], [1]
+  uint32_t *count;  // [0], [1] queue lengths; [2], [3] entries handed out by the traversal
 };
 
 } // namespace vsr

@@ -398,6 +398,21 @@ def measure_batch_config3(pkg, dev, steps=3, num_scenes=64):
         return time.perf_counter() - t
 
     sequential()  # commits, BVH builds, first-use allocations
+    # what caps batching: each frame's own device time in a sequential pass;
+    # if a frame kind already fills the GPU at its best rate, a batch can
+    # save at most the difference to that rate
+    sequential()
+    per = []
+    for sc, f in zip(scenes, frames):
+        W, H = sc["frame"]["size"]
+        spp = sc["renderer"]["pixelSamples"] if sc["renderer"]["type"] == "pathtrace" else 1
+        per.append((sc["renderer"]["type"], W * H * spp, dev.get_float(f, "duration.render")))
+    best = {}
+    for kind, w, t in per:
+        if t > 0:
+            best[kind] = max(best.get(kind, 0.0), w / t)
+    t_seq_dev = sum(t for _, _, t in per)
+    t_ideal = sum(w / best[kind] for kind, w, t in per if t > 0)
     tune = 0
     while not dev.get_int(frames[0], "batch.tuned") and tune < 32:
         batched()
@@ -421,6 +436,13 @@ def measure_batch_config3(pkg, dev, steps=3, num_scenes=64):
                         f"{kinds['pathtrace']} pathtrace), {px_spp / 1e6:.0f} Mpx*spp per pass",
             "tile": f"{tile_w}x{32 // max(tile_w, 1)}", "fetch": fetch, "tuning_batches": tune,
             "error_flags": err, "generate_s": gen_s,
+            "cap_analysis": {
+                "sum_frame_device_ms": 1e3 * t_seq_dev,
+                "ideal_ms_every_frame_at_its_kinds_best_rate": 1e3 * t_ideal,
+                "max_speedup_from_filling_the_gpu": t_seq_dev / t_ideal if t_ideal else None,
+                "best_rate_mpxspp": {k: v / MPX for k, v in best.items()},
+                "how": "each frame's device time in a sequential pass; a batch can at best run "
+                       "every frame at the best rate any frame of its kind reaches alone"},
             "timing": "host wall clock, first call to last frame done; synthetic seeded scenes"}
 
 

@@ -41,7 +41,16 @@ __global__ void __launch_bounds__(16 * VSR_MEGA_BLOCK_Y,
   const int y = blockIdx.y * blockDim.y + threadIdx.y;
   if (x >= F.width || y >= F.height) return;
   if (F.sampleMask && !F.sampleMask[(size_t)y * F.width + x]) return;
-  pathtracePixel<Count, Full>(S, C, R, F, x, y);
+  // grid z: the frame's sample chunks (1: the whole frame in one stream)
+  pathtracePixel<Count, Full>(S, C, R, F, x, y, R.sampleChunks > 1 ? (int)blockIdx.z : -1);
+}
+
+__global__ void __launch_bounds__(256) kCombineChunks(DRenderer R, DFrame F) {
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  const int y = blockIdx.y * blockDim.y + threadIdx.y;
+  if (x >= F.width || y >= F.height) return;
+  if (F.sampleMask && !F.sampleMask[(size_t)y * F.width + x]) return;
+  combineChunks(R, F, x, y);
 }
 
 static dim3 tileGrid(const DFrame &F, dim3 block) {
@@ -83,7 +92,13 @@ cudaError_t launchRaycast(const DScene &S, const DCamera &C, const DRenderer &R,
 cudaError_t launchPathtrace(const DScene &S, const DCamera &C, const DRenderer &R, const DFrame &F,
                             bool count, cudaStream_t stream) {
   dim3 block(16, VSR_MEGA_BLOCK_Y);
-  const dim3 grid = tileGrid(F, block);
+  dim3 grid = tileGrid(F, block);
+  const int chunks = R.sampleChunks > 1 ? R.sampleChunks : 1;
+  if (chunks > 1 && !F.chunkOut) return cudaErrorInvalidValue;
+  // chunked frames: every chunk of every pixel is a thread of one launch, so
+  // the grid is chunks times longer and each thread's path loop chunks
+  // times shorter (a shorter tail when the last blocks finish)
+  grid.z = (unsigned)chunks;
   const bool full = S.positionalLights || S.numAnalytic || S.quadGroups || S.numIso ||
                     (S.numVolumes > 0 && R.gradientShading);
   auto launch = [&](auto kernel) { kernel<<<grid, block, 0, stream>>>(S, C, R, F); };
@@ -93,6 +108,10 @@ cudaError_t launchPathtrace(const DScene &S, const DCamera &C, const DRenderer &
   } else {
     if (full) count ? launch(kPathtrace<true, false, true>) : launch(kPathtrace<false, false, true>);
     else count ? launch(kPathtrace<true, false, false>) : launch(kPathtrace<false, false, false>);
+  }
+  if (chunks > 1) {
+    const dim3 cb(32, 8);
+    kCombineChunks<<<tileGrid(F, cb), cb, 0, stream>>>(R, F);
   }
   return cudaGetLastError();
 }

@@ -278,16 +278,24 @@ __device__ __forceinline__ void intersectAll(const DScene &S, const Ray &ray, bo
 // (renderer/Pathtrace_impl.cpp:498-640) with shade() (:93-487) inlined.
 // Full = true is the variant with gradient shading of volume hits and point
 // and spot lights (kept out of the plain kernels' register allocation).
+// chunk >= 0: sample chunk `chunk` of R.sampleChunks: R.pixelSamples /
+// R.sampleChunks samples seeded as accumulation ID sampleChunks * accumID +
+// chunk, written to F.chunkOut for kCombineChunks instead of the frame.
 template <bool Count, bool Full>
 __device__ __forceinline__ void pathtracePixel(const DScene &S, const DCamera &C,
-                                               const DRenderer &R, const DFrame &F, int x, int y) {
+                                               const DRenderer &R, const DFrame &F, int x, int y,
+                                               int chunk = -1) {
   uint32_t err = 0;
   unsigned long long *cnt = F.counters;
   long long tStart = 0;
   if (Count) tStart = clock64();
   const int W = F.width, H = F.height;
+  const int spp = chunk >= 0 ? R.pixelSamples / R.sampleChunks : R.pixelSamples;
+  const uint32_t seedFrame =
+      chunk >= 0 ? (uint32_t)F.accumID * (uint32_t)R.sampleChunks + (uint32_t)chunk
+                 : (uint32_t)F.accumID;
   Rng rng;
-  rng.init((uint32_t)(x + W * y), (uint32_t)F.accumID);
+  rng.init((uint32_t)(x + W * y), seedFrame);
   Rng rnd = rng;
   const float3 ambient = ld3(R.ambient);
   float4 accum = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -295,7 +303,7 @@ __device__ __forceinline__ void pathtracePixel(const DScene &S, const DCamera &C
   float cDepth = 1e31f;
   float3 cNg = f3(0.f), cAlb = f3(0.f);
   const int maxPasses = (R.maxBounce + 2) * (2 + R.ambientSamples) + 8;
-  for (int sampleID = 0; sampleID < R.pixelSamples; ++sampleID) {
+  for (int sampleID = 0; sampleID < spp; ++sampleID) {
     float xf = (float)x, yf = (float)y;
     const float jx = rnd() - .5f;
     const float jy = rnd() - .5f;
@@ -500,11 +508,39 @@ __device__ __forceinline__ void pathtracePixel(const DScene &S, const DCamera &C
     const float lum = 0.3f * pc.x + 0.59f * pc.y + 0.11f * pc.z;
     lumSq += lum * lum;
   }
-  const float inv = 1.f / R.pixelSamples;
+  const float inv = 1.f / spp;
   if (Count) atomicAdd(&cnt[24], (unsigned long long)(clock64() - tStart));
-  writeSample(F, x, y, true, make_float4(accum.x * inv, accum.y * inv, accum.z * inv, accum.w * inv),
-              cDepth, cNg, cAlb, lumSq * inv);
+  const float4 mean = make_float4(accum.x * inv, accum.y * inv, accum.z * inv, accum.w * inv);
+  if (chunk >= 0) {
+    const size_t np = (size_t)W * H, i = (size_t)chunk * np + (size_t)y * W + x;
+    const size_t plane = (size_t)R.sampleChunks * np;
+    F.chunkOut[i] = mean;
+    F.chunkOut[plane + i] = make_float4(lumSq * inv, cDepth, cNg.x, cNg.y);
+    F.chunkOut[2 * plane + i] = make_float4(cNg.z, cAlb.x, cAlb.y, cAlb.z);
+  } else {
+    writeSample(F, x, y, true, mean, cDepth, cNg, cAlb, lumSq * inv);
+  }
   if (err) atomicOr(F.errorFlags, err);
+}
+
+// The frame write of a chunked path-traced frame: per pixel, the chunks'
+// results accumulated in chunk order as consecutive sub-frames
+// (dco::Frame::writeSample for each, accumulation ID sampleChunks *
+// accumID + c, pixelSamples / sampleChunks samples each), as the reference
+// accumulates that many frames.
+__device__ __forceinline__ void combineChunks(const DRenderer &R, const DFrame &F, int x, int y) {
+  const int K = R.sampleChunks;
+  const size_t np = (size_t)F.width * F.height, p = (size_t)y * F.width + x;
+  const size_t plane = (size_t)K * np;
+  DFrame Fc = F;
+  Fc.pixelSamples = R.pixelSamples / K;
+  for (int c = 0; c < K; ++c) {
+    const float4 col = F.chunkOut[(size_t)c * np + p];
+    const float4 a = F.chunkOut[plane + (size_t)c * np + p];
+    const float4 b = F.chunkOut[2 * plane + (size_t)c * np + p];
+    Fc.accumID = F.accumID * K + c;
+    writeSample(Fc, x, y, true, col, a.y, f3(a.z, a.w, b.x), f3(b.y, b.z, b.w), a.x);
+  }
 }
 
 } // namespace vsr

@@ -981,6 +981,17 @@ struct Renderer : Object {
     if (geti("ambientSamples", v)) r.ambientSamples = std::min(std::max(v, 0), 256);
     r.pixelSamples = 1;
     if (r.type == REND_PATHTRACE && geti("pixelSamples", v)) r.pixelSamples = std::min(std::max(v, 1), 256);
+    // sample chunks (path tracer): a divisor of pixelSamples, at most 16
+    r.sampleChunks = 1;
+    if (r.type == REND_PATHTRACE && geti("sampleChunks", v)) {
+      int k = std::min(std::max(v, 1), std::min(16, r.pixelSamples));
+      while (r.pixelSamples % k) --k;
+      if (k != v)
+        dev->report(this, kind, VSR_SEVERITY_WARNING, VSR_ERROR_INVALID_ARGUMENT,
+                    "sampleChunks %d does not divide pixelSamples %d (or is above 16): using %d",
+                    v, r.pixelSamples, k);
+      r.sampleChunks = k;
+    }
     sampleLimit = 1024;
     if (geti("sampleLimit", v)) sampleLimit = std::max(v, 1);
     // path tracer execution: one thread per pixel for the whole frame
@@ -1494,6 +1505,12 @@ struct FrameObj : Object {
   int batchTileW = 0, batchFetch = 0, batchTuned = 0;  // last batched render
   const uint8_t *sampleMask = nullptr;  // caller's device mask (vsrFrameSampleMask)
   DevBuf pixelFrames;  // frames per pixel, made by the first sample mask
+  DevBuf chunkOut;     // per-chunk results of chunked path tracing (3 float4 per pixel and chunk)
+  bool ensureChunks(int chunks) {
+    const size_t bytes = 3 * (size_t)chunks * width * height * sizeof(float4);
+    if (chunkOut.bytes >= bytes) return true;
+    return chunkOut.alloc(bytes) == cudaSuccess;
+  }
 
   // scratch of the segmented volume marcher, made on first use: the ray list
   // (48 B per pixel), groups (16 B per 32 pixels) and work units for
@@ -1650,6 +1667,7 @@ struct FrameObj : Object {
     f.pixelSamples = renderer ? renderer->r.pixelSamples : 1;
     f.sampleMask = sampleMask;
     f.pixelFrames = pixelFrames.as<uint32_t>();
+    f.chunkOut = chunkOut.as<float4>();
     return f;
   }
 };
@@ -1689,7 +1707,7 @@ VSRStatus renderFrame(Device *dev, FrameObj *F) {
   // cylinders, quads and iso-surfaces: the
   // megakernel takes such frames
   const bool wave = F->renderer->wavefront && !R.gradientShading && !W->scene.numAnalytic &&
-                    !W->scene.quadGroups && !W->scene.numIso;
+                    !W->scene.quadGroups && !W->scene.numIso && R.sampleChunks <= 1;
   int stage = 0;
   MarchScratch ms{};
   bool segmented = false;
@@ -1708,6 +1726,10 @@ VSRStatus renderFrame(Device *dev, FrameObj *F) {
   } else if (doRender && wave && !F->ensureWave()) {
     dev->report(F, VSR_FRAME, VSR_SEVERITY_ERROR, VSR_ERROR_OUT_OF_MEMORY,
                 "wavefront state allocation failed");
+    return VSR_ERROR_OUT_OF_MEMORY;
+  } else if (doRender && !wave && R.sampleChunks > 1 && !F->ensureChunks(R.sampleChunks)) {
+    dev->report(F, VSR_FRAME, VSR_SEVERITY_ERROR, VSR_ERROR_OUT_OF_MEMORY,
+                "sample-chunk buffer allocation failed");
     return VSR_ERROR_OUT_OF_MEMORY;
   }
   const DFrame fr = F->record();
@@ -1858,7 +1880,10 @@ VSRStatus renderFrames(Device *dev, FrameObj *const *frames, uint32_t count) {
       status = VSR_ERROR_INCOMPLETE;
       continue;
     }
-    if (F->countStats) {  // statistics are collected by the per-frame kernels
+    // statistics are collected by the per-frame kernels; chunked path tracing
+    // and sample masks are per-frame launches too
+    if (F->countStats || F->sampleMask ||
+        (F->renderer->r.type == REND_PATHTRACE && F->renderer->r.sampleChunks > 1)) {
       single.push_back(F);
       continue;
     }

@@ -251,6 +251,11 @@ struct DRenderer {
   int ambientSamples;
   int maxBounce;
   int pixelSamples;
+  // path tracer: a frame's pixelSamples are taken as sampleChunks streams of
+  // pixelSamples / sampleChunks samples, defined as that many accumulated
+  // sub-frames (accumulation IDs sampleChunks * accumID + c), rendered at
+  // once; 1 = the reference's single stream per pixel and frame
+  int sampleChunks;
   float samplingRateInv;
   int hwFilter;        // 1: field samples through the texture unit's trilinear filter
   int gradientShading; // volume samples lit along the normalised field gradient
@@ -281,6 +286,10 @@ struct DFrame {
   // per pixel, kept once a frame has had a sample mask; the running mean
   // and the variance then weight each pixel by its own count
   uint32_t *pixelFrames;
+  // per sample chunk and pixel, [3][chunks][pixels] (sampleChunks > 1):
+  // the chunk's mean colour; (mean squared luminance, closest depth, Ng.xy);
+  // (Ng.z, albedo)
+  float4 *chunkOut;
 };
 
 // Wavefront path-tracer state: one slot per pixel, structure of arrays

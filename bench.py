@@ -50,6 +50,9 @@ def parse():
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--accum-frames", type=int, default=64,
                    help="config 1 also as this many accumulated 1-spp frames (0: skip)")
+    p.add_argument("--sample-chunks", type=int, default=4,
+                   help="config 1: the frame's samples as this many concurrent per-pixel streams "
+                        "(accumulated sub-frames); 1 = one stream per pixel and frame")
     p.add_argument("--wavefront", action="store_true",
                    help="path tracer with wavefront queues instead of one thread per pixel")
     p.add_argument("--no-raycast", dest="raycast", action="store_false",
@@ -684,6 +687,7 @@ def run_ours(args):
 
     scene = pkg.scenes.config1(res=args.res, spp=args.spp)
     scene["renderer"]["wavefront"] = args.wavefront
+    scene["renderer"]["sampleChunks"] = args.sample_chunks
     ntris = pkg.scenes.triangle_count(scene)
     dev = vsr.Device()
     h = pkg.scenes.build(dev, scene)
@@ -762,6 +766,7 @@ def run_ours(args):
     accum = None
     if args.accum_frames > 0 and world == 1:
         dev.set(h["renderer"], "pixelSamples", 1)
+        dev.set(h["renderer"], "sampleChunks", 1)
         dev.commit(h["renderer"])
         dev.render(frame)  # accumulation restarts after the commit
         dev.wait(frame)
@@ -777,6 +782,7 @@ def run_ours(args):
                  "workload": f"config1 pathtracer {W}x{H}, {args.accum_frames} accumulated "
                              f"1-spp frames, L2 flushed before each"}
         dev.set(h["renderer"], "pixelSamples", args.spp)
+        dev.set(h["renderer"], "sampleChunks", args.sample_chunks)
         dev.commit(h["renderer"])
 
     l2peak = measure_l2_read_peak(pkg) if args.raycast else None
@@ -818,6 +824,7 @@ def run_ours(args):
         "warmup": args.warmup, "ms_per_step": 1e3 * kernel_s, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": f"config1 pathtracer {W}x{H} {args.spp}spp depth5 {ntris} tris",
+                   "sample_chunks": args.sample_chunks,
                    "l2": "flushed (256 MiB write) between steps", "parallelism": f"replicas{world}"},
         "e2e": {"value": e2e_value, "unit": "Mpx*spp/s", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h},

@@ -412,6 +412,7 @@ class Scene:
         self.handle = lib.or_scene_commit(ctypes.byref(sc))
         self.camera = camera(scene["camera"])
         self.renderer = renderer(scene["renderer"])
+        self.sample_chunks = sample_chunks(scene["renderer"])
         self.size = tuple(scene["frame"]["size"])
 
     def close(self):
@@ -443,6 +444,18 @@ def camera(c):
     oc.view = farr(16, c.get("view", np.eye(4).reshape(-1)))
     oc.proj = farr(16, c.get("proj", np.eye(4).reshape(-1)))
     return oc
+
+
+def sample_chunks(r):
+    """The renderer's sample chunks as the renderer core resolves them: a
+    divisor of pixelSamples, at most 16 (path tracer only)."""
+    if r.get("type", "pathtrace") == "raycast":
+        return 1
+    spp = int(r.get("pixelSamples", 1))
+    k = min(max(int(r.get("sampleChunks", 1)), 1), min(16, spp))
+    while spp % k:
+        k -= 1
+    return k
 
 
 def renderer(r):
@@ -499,6 +512,25 @@ def render(sc, frame, num_threads=0, rows=None, stats=None, tile=None):
         frame.f.rowBegin, frame.f.rowEnd = rows
     if tile is not None:
         frame.f.tileSize = int(tile)
+    k = getattr(sc, "sample_chunks", 1)
+    if k > 1:
+        # a frame of K sample chunks is K accumulated sub-frames of spp / K
+        # samples with accumulation IDs K * accumID + c
+        spp = sc.renderer.pixelSamples
+        base = frame.f.accumID
+        sc.renderer.pixelSamples = spp // k
+        try:
+            for c in range(k):
+                frame.f.accumID = base * k + c
+                render_once(sc, frame, num_threads, stats)
+        finally:
+            sc.renderer.pixelSamples = spp
+        frame.f.accumID = base + 1
+        return stats
+    return render_once(sc, frame, num_threads, stats)
+
+
+def render_once(sc, frame, num_threads=0, stats=None):
     st = stats if stats is not None else OrStats()
     load().or_render_frame(sc.handle, ctypes.byref(sc.camera), ctypes.byref(sc.renderer),
                            ctypes.byref(frame.f), num_threads, ctypes.byref(st))

@@ -268,9 +268,12 @@ def test_incomplete_frame_reports_error(pkg, device):
     device.release(f)
 
 
-def test_full_config1_rows_against_oracle(pkg, device, oracle):
-    """Config 1 at full size on the GPU; a band of rows checked against the oracle."""
+@pytest.mark.parametrize("chunks", [1, 4])
+def test_full_config1_rows_against_oracle(pkg, device, oracle, chunks):
+    """Config 1 at full size on the GPU; a band of rows checked against the
+    oracle (chunks 4: the benchmark's setting)."""
     sc = pkg.scenes.config1()
+    sc["renderer"]["sampleChunks"] = chunks
     h = pkg.scenes.build(device, sc)
     device.render(h["frame"])
     device.wait(h["frame"])
@@ -757,7 +760,32 @@ def test_raycast_surfaces_and_volume(pkg, device, oracle, filt):
         assert float(np.abs(gpu["color"] - F.color).max()) < 1e-3
 
 
-def test_pathtrace_1024spp_band_config1_scene(pkg, device, oracle):
+@pytest.mark.parametrize("chunks", [1, 4])
+def test_pathtrace_sample_chunks_same_stream(pkg, device, oracle, chunks):
+    """Sample chunks: a frame's samples as `chunks` concurrent streams, each
+    seeded and accumulated as a sub-frame (accumulation IDs chunks * accumID
+    + c); over two frames the GPU follows the oracle, which renders the same
+    sub-frames one after another."""
+    sc = small_spheres(pkg, res=96, spp=8, n=16)
+    sc["renderer"]["sampleChunks"] = chunks
+    gpu = render_gpu(pkg, device, sc, frames=2)
+    _, F = render_oracle(oracle, sc, frames=2)
+    assert gpu["errorFlags"] == 0
+    d = np.abs(gpu["color"][..., :3] - F.color[..., :3]).max(axis=-1)
+    frac = float((d <= 1e-3).mean())
+    print(f"sample chunks {chunks}: {frac:.4f} of pixels within 1e-3")
+    assert frac >= 0.97, frac
+    hit = (F.depth < 1e30) & (gpu["depth"] < 1e30)
+    rel = np.abs(gpu["depth"][hit] - F.depth[hit]) / F.depth[hit]
+    assert float((rel <= 1e-4).mean()) >= 0.99
+    if chunks > 1:  # the streams differ from the single-stream frame
+        sc1 = dict(sc, renderer=dict(sc["renderer"], sampleChunks=1))
+        _, F1 = render_oracle(oracle, sc1, frames=2)
+        assert float(np.abs(F1.color - F.color).max()) > 1e-3
+
+
+@pytest.mark.parametrize("chunks", [1, 4])
+def test_pathtrace_1024spp_band_config1_scene(pkg, device, oracle, chunks):
     """The path-tracer bar: the config-1 scene (all 256 spheres, 64x32
     segments, ground quad, depth 5) at 128x128, 1024 spp on each side with
     independent random streams (GPU accumulation IDs 0..15, oracle 1000..).
@@ -768,6 +796,7 @@ def test_pathtrace_1024spp_band_config1_scene(pkg, device, oracle):
     3-sigma band are printed."""
     frames, spp = 16, 64
     sc = pkg.scenes.config1(res=128, spp=spp)
+    sc["renderer"]["sampleChunks"] = chunks
     h = pkg.scenes.build(device, sc)
     prev, fms = None, []
     for k in range(frames):
@@ -790,7 +819,8 @@ def test_pathtrace_1024spp_band_config1_scene(pkg, device, oracle):
     inside = float((np.abs(gpu_mean - mean) <= 3.0 * sigma + 1e-6).all(axis=-1).mean())
     inside_ref = float((np.abs(gpu_mean - mean) <= 3.0 * sigma_ref + 1e-6).all(axis=-1).mean())
     rmse = float(np.sqrt(np.mean((gpu_mean - mean) ** 2)))
-    print(f"1024 spp, 128x128: inside combined 3-sigma band {inside:.4f}, inside the oracle's "
+    print(f"1024 spp, 128x128, {chunks} chunks: inside combined 3-sigma band {inside:.4f}, "
+          f"inside the oracle's "
           f"own band {inside_ref:.4f}, RMSE {rmse:.5f}, mean {float(mean.mean()):.4f}")
     assert inside >= 0.985, inside
     assert abs(float(gpu_mean.mean() - mean.mean())) < 0.01 * float(mean.mean()) + 1e-3

@@ -55,7 +55,7 @@ constexpr int kMaxSurfaceLayers = 1 << 12;
 // Launch-bound tunables (minimum resident blocks per SM) of the path-tracer
 // kernels; they trade registers for occupancy.
 #ifndef VSR_MEGA_MIN_BLOCKS
-#define VSR_MEGA_MIN_BLOCKS 12  // ~40 registers: latency hiding beats spill cost
+#define VSR_MEGA_MIN_BLOCKS 16  // 32 registers, 64 warps per SM: latency hiding beats spill cost
 #endif
 #ifndef VSR_MEGA_MIN_BLOCKS_VOLUMES
 #define VSR_MEGA_MIN_BLOCKS_VOLUMES 8  // ~64 registers for worlds with volumes

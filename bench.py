@@ -50,7 +50,7 @@ def parse():
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--accum-frames", type=int, default=64,
                    help="config 1 also as this many accumulated 1-spp frames (0: skip)")
-    p.add_argument("--sample-chunks", type=int, default=4,
+    p.add_argument("--sample-chunks", type=int, default=8,
                    help="config 1: the frame's samples as this many concurrent per-pixel streams "
                         "(accumulated sub-frames); 1 = one stream per pixel and frame")
     p.add_argument("--wavefront", action="store_true",

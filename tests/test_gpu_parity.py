@@ -268,10 +268,10 @@ def test_incomplete_frame_reports_error(pkg, device):
     device.release(f)
 
 
-@pytest.mark.parametrize("chunks", [1, 4])
+@pytest.mark.parametrize("chunks", [1, 8])
 def test_full_config1_rows_against_oracle(pkg, device, oracle, chunks):
     """Config 1 at full size on the GPU; a band of rows checked against the
-    oracle (chunks 4: the benchmark's setting)."""
+    oracle (chunks 8: the benchmark's setting)."""
     sc = pkg.scenes.config1()
     sc["renderer"]["sampleChunks"] = chunks
     h = pkg.scenes.build(device, sc)
@@ -784,7 +784,7 @@ def test_pathtrace_sample_chunks_same_stream(pkg, device, oracle, chunks):
         assert float(np.abs(F1.color - F.color).max()) > 1e-3
 
 
-@pytest.mark.parametrize("chunks", [1, 4])
+@pytest.mark.parametrize("chunks", [1, 8])
 def test_pathtrace_1024spp_band_config1_scene(pkg, device, oracle, chunks):
     """The path-tracer bar: the config-1 scene (all 256 spheres, 64x32
     segments, ground quad, depth 5) at 128x128, 1024 spp on each side with

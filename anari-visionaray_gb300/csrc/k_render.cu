@@ -45,6 +45,13 @@ __global__ void __launch_bounds__(16 * VSR_MEGA_BLOCK_Y,
   pathtracePixel<Count, Full>(S, C, R, F, x, y, R.sampleChunks > 1 ? (int)blockIdx.z : -1);
 }
 
+__global__ void __launch_bounds__(256) kTaaResolve(DRenderer R, DFrame F) {
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  const int y = blockIdx.y * blockDim.y + threadIdx.y;
+  if (x >= F.width || y >= F.height) return;
+  taaResolvePixel(R, F, x, y);
+}
+
 __global__ void __launch_bounds__(256) kCombineChunks(DRenderer R, DFrame F) {
   const int x = blockIdx.x * blockDim.x + threadIdx.x;
   const int y = blockIdx.y * blockDim.y + threadIdx.y;
@@ -100,7 +107,9 @@ cudaError_t launchPathtrace(const DScene &S, const DCamera &C, const DRenderer &
   // times shorter (a shorter tail when the last blocks finish)
   grid.z = (unsigned)chunks;
   const bool full = S.positionalLights || S.numAnalytic || S.quadGroups || S.numIso ||
-                    (S.numVolumes > 0 && R.gradientShading);
+                    (S.numVolumes > 0 && R.gradientShading) || R.taa;
+  if (R.taa && (!F.taaCurr || !F.taaPrev || !F.motionVec || chunks > 1))
+    return cudaErrorInvalidValue;
   auto launch = [&](auto kernel) { kernel<<<grid, block, 0, stream>>>(S, C, R, F); };
   if (S.numVolumes > 0) {
     if (full) count ? launch(kPathtrace<true, true, true>) : launch(kPathtrace<false, true, true>);
@@ -112,6 +121,18 @@ cudaError_t launchPathtrace(const DScene &S, const DCamera &C, const DRenderer &
   if (chunks > 1) {
     const dim3 cb(32, 8);
     kCombineChunks<<<tileGrid(F, cb), cb, 0, stream>>>(R, F);
+  }
+  if (R.taa) {
+    // resolve, then this frame becomes the next one's history
+    const dim3 cb(32, 8);
+    kTaaResolve<<<tileGrid(F, cb), cb, 0, stream>>>(R, F);
+    const size_t np = (size_t)F.width * F.height;
+    cudaError_t e = cudaMemcpyAsync(F.taaPrev, F.taaCurr, np * sizeof(float4),
+                                    cudaMemcpyDeviceToDevice, stream);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(F.taaPrevAlbedo, F.taaCurrAlbedo, np * 3 * sizeof(float),
+                          cudaMemcpyDeviceToDevice, stream);
+    if (e != cudaSuccess) return e;
   }
   return cudaGetLastError();
 }

@@ -1283,6 +1283,83 @@ __device__ __forceinline__ uint32_t packRGBA8(float4 color, bool srgb) {
   return cvtU8(r) | (cvtU8(g) << 8) | (cvtU8(b) << 16) | (cvtU8(color.w) << 24);
 }
 
+// Window position of a world point under a column-major view-projection
+// matrix M (Visionaray's project, the gluProject convention: clip = M (p, 1),
+// ndc = clip / w, win = size (ndc + 1) / 2), for motion vectors
+// (Pathtrace_impl.cpp:290-297). Every product and sum is rounded on its own,
+// in a fixed order, so the oracle's arithmetic gives the same bits.
+__device__ __forceinline__ float2 projectWin(const float *M, float3 p, float W, float H) {
+  auto row = [&](int r) {
+    return __fadd_rn(__fadd_rn(__fadd_rn(__fmul_rn(M[r], p.x), __fmul_rn(M[4 + r], p.y)),
+                               __fmul_rn(M[8 + r], p.z)),
+                     M[12 + r]);
+  };
+  const float cx = row(0), cy = row(1), cw = row(3);
+  const float nx = __fdiv_rn(cx, cw), ny = __fdiv_rn(cy, cw);
+  return make_float2(__fmul_rn(__fmul_rn(W, __fadd_rn(nx, 1.f)), 0.5f),
+                     __fmul_rn(__fmul_rn(H, __fadd_rn(ny, 1.f)), 0.5f));
+}
+
+// The path tracer's frame write with temporal anti-aliasing
+// (dco::Frame::fillGBuffer, DeviceCopyableObjects.h:2745-2773): motion
+// vector, this frame's colour and the closest sample's albedo for the
+// resolve pass, then the depth-tested G-buffer; the accumulation buffer and
+// the colour channel are left to the resolve pass.
+__device__ __forceinline__ void fillGBufferTaa(const DFrame &F, int x, int y, float4 color,
+                                               float depth, float3 Ng, float3 albedo, float2 mv) {
+  const size_t idx = (size_t)y * F.width + x;
+  F.motionVec[idx] = mv;
+  F.taaCurr[idx] = color;
+  F.taaCurrAlbedo[3 * idx] = albedo.x;
+  F.taaCurrAlbedo[3 * idx + 1] = albedo.y;
+  F.taaCurrAlbedo[3 * idx + 2] = albedo.z;
+  if (F.depth && !(depth > F.depth[idx])) {
+    F.depth[idx] = depth;
+    if (F.normal) {
+      F.normal[3 * idx] = Ng.x;
+      F.normal[3 * idx + 1] = Ng.y;
+      F.normal[3 * idx + 2] = Ng.z;
+    }
+    if (F.albedo) {
+      F.albedo[3 * idx] = albedo.x;
+      F.albedo[3 * idx + 1] = albedo.y;
+      F.albedo[3 * idx + 2] = albedo.z;
+    }
+  }
+}
+
+// The TAA history: the previous resolved image read at normalised
+// coordinates (u, v) with clamp addressing and a cardinal-spline (Catmull-
+// Rom) filter over 4x4 texels, texel centres at (i + 0.5) / size, as the
+// reference's history texture is set up (frame/Frame.cpp:541-545).
+__device__ __forceinline__ void catmullRomWeights(float f, float w[4]) {
+  const float f2 = f * f, f3 = f2 * f;
+  w[0] = 0.5f * (-f3 + 2.f * f2 - f);
+  w[1] = 0.5f * (3.f * f3 - 5.f * f2 + 2.f);
+  w[2] = 0.5f * (-3.f * f3 + 4.f * f2 + f);
+  w[3] = 0.5f * (f3 - f2);
+}
+__device__ __forceinline__ float4 historyAt(const float4 *img, int W, int H, float u, float v) {
+  const float tx = u * (float)W - 0.5f, ty = v * (float)H - 0.5f;
+  const float fx0 = floorf(tx), fy0 = floorf(ty);
+  float wx[4], wy[4];
+  catmullRomWeights(tx - fx0, wx);
+  catmullRomWeights(ty - fy0, wy);
+  const int x0 = (int)fx0 - 1, y0 = (int)fy0 - 1;
+  float4 r = make_float4(0.f, 0.f, 0.f, 0.f);
+  for (int j = 0; j < 4; ++j) {
+    const int yy = min(max(y0 + j, 0), H - 1);
+    float4 row = make_float4(0.f, 0.f, 0.f, 0.f);
+    for (int i = 0; i < 4; ++i) {
+      const int xx = min(max(x0 + i, 0), W - 1);
+      const float4 t = img[(size_t)yy * W + xx];
+      row.x += wx[i] * t.x; row.y += wx[i] * t.y; row.z += wx[i] * t.z; row.w += wx[i] * t.w;
+    }
+    r.x += wy[j] * row.x; r.y += wy[j] * row.y; r.z += wy[j] * row.z; r.w += wy[j] * row.w;
+  }
+  return r;
+}
+
 // lumSqMean: the mean over this frame's samples of the squared sample
 // luminance (0.3 r + 0.59 g + 0.11 b), for the optional variance channel;
 // negative when the caller does not track it.

@@ -302,8 +302,15 @@ __device__ __forceinline__ void pathtracePixel(const DScene &S, const DCamera &C
   float lumSq = 0.f;  // sum of squared sample luminances (variance channel)
   float cDepth = 1e31f;
   float3 cNg = f3(0.f), cAlb = f3(0.f);
+  // TAA (Full variant): the motion vector of the closest sample; a sample's
+  // is that of its path's last radiance hit, as the reference overwrites it
+  // at every radiance hit (Pathtrace_impl.cpp:290-297)
+  float2 cMV = make_float2(0.f, 0.f);
+  const bool taa = Full && R.taa && chunk < 0;
   const int maxPasses = (R.maxBounce + 2) * (2 + R.ambientSamples) + 8;
   for (int sampleID = 0; sampleID < spp; ++sampleID) {
+    float2 pMV = make_float2(0.f, 0.f);
+    bool closestNow = false;
     float xf = (float)x, yf = (float)y;
     const float jx = rnd() - .5f;
     const float jy = rnd() - .5f;
@@ -399,9 +406,15 @@ __device__ __forceinline__ void pathtracePixel(const DScene &S, const DCamera &C
                 cDepth = d0;
                 cNg = gn;
                 cAlb = color;
+                closestNow = true;
               }
             }
             hitPosOff = hitPos + sn * eps;
+            if (taa) {
+              const float2 a = projectWin(F.prevMVP, hitPos, (float)W, (float)H);
+              const float2 b = projectWin(F.currMVP, hitPos, (float)W, (float)H);
+              pMV = make_float2(a.x - b.x, a.y - b.y);
+            }
             if (S.numLights > 0) {
               int lightID = int(rnd() * S.numLights);
               if (lightID == S.numLights) lightID = 0;
@@ -507,6 +520,7 @@ __device__ __forceinline__ void pathtracePixel(const DScene &S, const DCamera &C
     accum.x += pc.x; accum.y += pc.y; accum.z += pc.z; accum.w += pc.w;
     const float lum = 0.3f * pc.x + 0.59f * pc.y + 0.11f * pc.z;
     lumSq += lum * lum;
+    if (closestNow) cMV = pMV;
   }
   const float inv = 1.f / spp;
   if (Count) atomicAdd(&cnt[24], (unsigned long long)(clock64() - tStart));
@@ -517,6 +531,8 @@ __device__ __forceinline__ void pathtracePixel(const DScene &S, const DCamera &C
     F.chunkOut[i] = mean;
     F.chunkOut[plane + i] = make_float4(lumSq * inv, cDepth, cNg.x, cNg.y);
     F.chunkOut[2 * plane + i] = make_float4(cNg.z, cAlb.x, cAlb.y, cAlb.z);
+  } else if (taa) {
+    fillGBufferTaa(F, x, y, mean, cDepth, cNg, cAlb, cMV);
   } else {
     writeSample(F, x, y, true, mean, cDepth, cNg, cAlb, lumSq * inv);
   }
@@ -541,6 +557,38 @@ __device__ __forceinline__ void combineChunks(const DRenderer &R, const DFrame &
     Fc.accumID = F.accumID * K + c;
     writeSample(Fc, x, y, true, col, a.y, f3(a.z, a.w, b.x), f3(b.y, b.z, b.w), a.x);
   }
+}
+
+// The TAA resolve pass of one pixel (frame/Frame.cpp:339-381 with
+// dco::Frame::accumSample, DeviceCopyableObjects.h:2692-2720): the previous
+// resolved image is read at the pixel moved by its motion vector with the
+// history filter; the blend weight is taaAlpha, or 1 where the albedo at
+// the reprojected pixel differs from this pixel's (by 1e-2 or more in a
+// channel); the result replaces this frame's colour and is converted into
+// the frame's colour channel.
+__device__ __forceinline__ void taaResolvePixel(const DRenderer &R, const DFrame &F, int x, int y) {
+  const int W = F.width, H = F.height;
+  const size_t idx = (size_t)y * W + x;
+  const float2 mv = F.motionVec[idx];
+  int px = (int)((float)x + mv.x), py = (int)((float)y + mv.y);
+  px = min(max(px, 0), W - 1);
+  py = min(max(py, 0), H - 1);
+  const size_t pidx = (size_t)py * W + px;
+  float alpha = R.taaAlpha;
+  const float *pa = F.taaPrevAlbedo + 3 * pidx, *ca = F.taaCurrAlbedo + 3 * idx;
+  if (!(fabsf(pa[0] - ca[0]) < 1e-2f && fabsf(pa[1] - ca[1]) < 1e-2f &&
+        fabsf(pa[2] - ca[2]) < 1e-2f))
+    alpha = 1.f;
+  const float u = ((float)x + mv.x + 0.5f) / (float)W, v = ((float)y + mv.y + 0.5f) / (float)H;
+  const float4 h = historyAt(F.taaPrev, W, H, u, v);
+  const float4 c = F.taaCurr[idx];
+  const float4 o = make_float4((1.f - alpha) * h.x + alpha * c.x, (1.f - alpha) * h.y + alpha * c.y,
+                               (1.f - alpha) * h.z + alpha * c.z, (1.f - alpha) * h.w + alpha * c.w);
+  F.taaCurr[idx] = o;
+  if (F.colorType == COLOR_FLOAT4)
+    reinterpret_cast<float4 *>(F.color)[idx] = o;
+  else if (F.colorType == COLOR_UFIXED8 || F.colorType == COLOR_SRGB8)
+    reinterpret_cast<uint32_t *>(F.color)[idx] = packRGBA8(o, F.colorType == COLOR_SRGB8);
 }
 
 } // namespace vsr

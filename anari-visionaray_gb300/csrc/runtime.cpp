@@ -827,8 +827,58 @@ struct Instance : Object {
   }
 };
 
+// perspective(fovy, aspect, 0.001, 1000) * lookAt(eye, eye + dir, up),
+// column-major, evaluated in double from dir and up as given (normalised
+// here) and rounded once to float.
+static void perspectiveViewProj(const float *eye, const float *dir, const float *up, float fovy,
+                                float aspect, float *out) {
+  const double n = 0.001, f = 1000.0;
+  double F[3] = {dir[0], dir[1], dir[2]}, Up[3] = {up[0], up[1], up[2]};
+  const double fl = std::sqrt(F[0] * F[0] + F[1] * F[1] + F[2] * F[2]);
+  const double ul = std::sqrt(Up[0] * Up[0] + Up[1] * Up[1] + Up[2] * Up[2]);
+  for (int k = 0; k < 3; ++k) {
+    F[k] /= fl;
+    Up[k] /= ul;
+  }
+  double S[3] = {F[1] * Up[2] - F[2] * Up[1], F[2] * Up[0] - F[0] * Up[2],
+                 F[0] * Up[1] - F[1] * Up[0]};
+  const double sl = std::sqrt(S[0] * S[0] + S[1] * S[1] + S[2] * S[2]);
+  for (double &v : S) v /= sl;
+  const double U[3] = {S[1] * F[2] - S[2] * F[1], S[2] * F[0] - S[0] * F[2],
+                       S[0] * F[1] - S[1] * F[0]};
+  double V[16] = {0};  // column-major view matrix
+  for (int k = 0; k < 3; ++k) {
+    V[4 * k + 0] = S[k];
+    V[4 * k + 1] = U[k];
+    V[4 * k + 2] = -F[k];
+  }
+  V[12] = -(S[0] * eye[0] + S[1] * eye[1] + S[2] * eye[2]);
+  V[13] = -(U[0] * eye[0] + U[1] * eye[1] + U[2] * eye[2]);
+  V[14] = F[0] * eye[0] + F[1] * eye[1] + F[2] * eye[2];
+  V[15] = 1.0;
+  const double t = 1.0 / std::tan(0.5 * (double)fovy);
+  double P[16] = {0};
+  P[0] = t / aspect;
+  P[5] = t;
+  P[10] = (f + n) / (n - f);
+  P[11] = -1.0;
+  P[14] = 2.0 * f * n / (n - f);
+  for (int col = 0; col < 4; ++col)
+    for (int row = 0; row < 4; ++row) {
+      double acc = 0.0;
+      for (int k = 0; k < 4; ++k) acc += P[4 * k + row] * V[4 * col + k];
+      out[4 * col + row] = (float)acc;
+    }
+}
+
 struct Camera : Object {
   DCamera c{};
+  // view-projection matrix (column-major) for the TAA motion vectors:
+  // perspective cameras as Visionaray's pinhole camera (look-at view,
+  // perspective projection with near 0.001 and far 1000, Perspective.cpp:
+  // 35-40), matrix cameras proj * view; none for the others
+  float mvp[16];
+  bool hasMVP = false;
   using Object::Object;
   static void normalize3(float *v) {
     float l = std::sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
@@ -873,6 +923,7 @@ struct Camera : Object {
     getv("position", VSR_FLOAT32_VEC3, pos);
     getv("direction", VSR_FLOAT32_VEC3, dir);
     getv("up", VSR_FLOAT32_VEC3, up);
+    const float rawDir[3] = {dir[0], dir[1], dir[2]}, rawUp[3] = {up[0], up[1], up[2]};
     normalize3(dir);
     normalize3(up);
     float region[4] = {0, 0, 1, 1};
@@ -887,10 +938,13 @@ struct Camera : Object {
     float aspect = 1.f;
     getf("aspect", aspect);
     valid = true;
+    hasMVP = false;
     if (subtype == "perspective") {
       c.type = CAM_PERSPECTIVE;
       float fovy = 60.f * 3.14159265358979f / 180.f;
       getf("fovy", fovy);
+      perspectiveViewProj(pos, rawDir, rawUp, fovy, aspect, mvp);
+      hasMVP = true;
       c.lensRadius = 0.f; getf("apertureRadius", c.lensRadius);
       c.focusDistance = 1.f; getf("focusDistance", c.focusDistance);
       float th = std::tan(0.5f * fovy);
@@ -937,6 +991,8 @@ struct Camera : Object {
         warn("singular proj*view on matrix camera");
         valid = false;
       }
+      memcpy(mvp, pv, sizeof(pv));
+      hasMVP = true;
     }
   }
 };
@@ -945,6 +1001,11 @@ struct Renderer : Object {
   DRenderer r{};
   int sampleLimit = 1024;
   bool wavefront = false;
+  // TAA: the view-projection matrices of the previous and the current frame
+  // rendered with this renderer (rendererState.prevMV/currMV and PR,
+  // renderer/common.h:75-78; identity at first, as there)
+  float prevMVP[16] = {1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1};
+  float currMVP[16] = {1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1};
   using Object::Object;
   // Renderer.cpp:34-45, Raycast.cpp:16-20, Pathtrace.cpp:16-28
   void commit() override {
@@ -970,8 +1031,10 @@ struct Renderer : Object {
     // Renderer.cpp:50: volume samples (raycast) and volume scatter events
     // (path tracer) lit along the field gradient
     r.gradientShading = geti("gradientShading", b) && b ? 1 : 0;
-    if (geti("taa", b) && b)
-      dev->report(this, kind, VSR_SEVERITY_WARNING, VSR_ERROR_INVALID_ARGUMENT, "'taa' is not supported");
+    // Pathtrace.cpp:24-25: taa (path tracer only), taaAlpha
+    r.taa = r.type == REND_PATHTRACE && geti("taa", b) && b ? 1 : 0;
+    r.taaAlpha = 0.3f;
+    getf("taaAlpha", r.taaAlpha);
     int v;
     r.maxBounce = 7;
     if (geti("maxBounce", v)) r.maxBounce = std::min(std::max(v, 0), 256);
@@ -991,6 +1054,11 @@ struct Renderer : Object {
                     "sampleChunks %d does not divide pixelSamples %d (or is above 16): using %d",
                     v, r.pixelSamples, k);
       r.sampleChunks = k;
+    }
+    if (r.taa && r.sampleChunks > 1) {
+      dev->report(this, kind, VSR_SEVERITY_WARNING, VSR_ERROR_INVALID_ARGUMENT,
+                  "sampleChunks is not used with taa");
+      r.sampleChunks = 1;
     }
     sampleLimit = 1024;
     if (geti("sampleLimit", v)) sampleLimit = std::max(v, 1);
@@ -1506,6 +1574,23 @@ struct FrameObj : Object {
   const uint8_t *sampleMask = nullptr;  // caller's device mask (vsrFrameSampleMask)
   DevBuf pixelFrames;  // frames per pixel, made by the first sample mask
   DevBuf chunkOut;     // per-chunk results of chunked path tracing (3 float4 per pixel and chunk)
+  // TAA buffers (frame/Frame.cpp:535-540), zeroed when (re)made
+  DevBuf taaCurr, taaPrev, taaCurrAlb, taaPrevAlb, motionVec;
+  bool ensureTaa() {
+    const size_t np = (size_t)width * height;
+    if (taaCurr.bytes == np * sizeof(float4)) return true;
+    bool ok = taaCurr.alloc(np * sizeof(float4)) == cudaSuccess &&
+              taaPrev.alloc(np * sizeof(float4)) == cudaSuccess &&
+              taaCurrAlb.alloc(np * 3 * sizeof(float)) == cudaSuccess &&
+              taaPrevAlb.alloc(np * 3 * sizeof(float)) == cudaSuccess &&
+              motionVec.alloc(np * sizeof(float2)) == cudaSuccess;
+    if (ok) {
+      for (DevBuf *b : {&taaCurr, &taaPrev, &taaCurrAlb, &taaPrevAlb, &motionVec})
+        ok = ok && cudaMemset(b->p, 0, b->bytes) == cudaSuccess;
+    }
+    if (!ok) taaCurr.release();
+    return ok;
+  }
   bool ensureChunks(int chunks) {
     const size_t bytes = 3 * (size_t)chunks * width * height * sizeof(float4);
     if (chunkOut.bytes >= bytes) return true;
@@ -1668,6 +1753,11 @@ struct FrameObj : Object {
     f.sampleMask = sampleMask;
     f.pixelFrames = pixelFrames.as<uint32_t>();
     f.chunkOut = chunkOut.as<float4>();
+    f.taaCurr = taaCurr.as<float4>();
+    f.taaPrev = taaPrev.as<float4>();
+    f.taaCurrAlbedo = taaCurrAlb.as<float>();
+    f.taaPrevAlbedo = taaPrevAlb.as<float>();
+    f.motionVec = motionVec.as<float2>();
     return f;
   }
 };
@@ -1707,7 +1797,7 @@ VSRStatus renderFrame(Device *dev, FrameObj *F) {
   // cylinders, quads and iso-surfaces: the
   // megakernel takes such frames
   const bool wave = F->renderer->wavefront && !R.gradientShading && !W->scene.numAnalytic &&
-                    !W->scene.quadGroups && !W->scene.numIso && R.sampleChunks <= 1;
+                    !W->scene.quadGroups && !W->scene.numIso && R.sampleChunks <= 1 && !R.taa;
   int stage = 0;
   MarchScratch ms{};
   bool segmented = false;
@@ -1732,7 +1822,22 @@ VSRStatus renderFrame(Device *dev, FrameObj *F) {
                 "sample-chunk buffer allocation failed");
     return VSR_ERROR_OUT_OF_MEMORY;
   }
-  const DFrame fr = F->record();
+  if (doRender && R.type == REND_PATHTRACE && R.taa && !F->ensureTaa()) {
+    dev->report(F, VSR_FRAME, VSR_SEVERITY_ERROR, VSR_ERROR_OUT_OF_MEMORY,
+                "TAA buffer allocation failed");
+    return VSR_ERROR_OUT_OF_MEMORY;
+  }
+  DFrame fr = F->record();
+  if (doRender && R.type == REND_PATHTRACE) {
+    // Frame.cpp:315-334: the current view-projection comes from the camera
+    // (perspective and matrix cameras), the previous one is the last
+    // frame's; after the render the current one becomes the previous one
+    Renderer *rn = F->renderer;
+    if (F->camera->hasMVP) memcpy(rn->currMVP, F->camera->mvp, sizeof(rn->currMVP));
+    memcpy(fr.prevMVP, rn->prevMVP, sizeof(fr.prevMVP));
+    memcpy(fr.currMVP, rn->currMVP, sizeof(fr.currMVP));
+    memcpy(rn->prevMVP, rn->currMVP, sizeof(rn->prevMVP));
+  }
   cudaEventRecord(F->evStart, s);
   if (reset) {
     launchFrameReset(F->accum.as<float4>(), F->depth.as<float>(), (size_t)F->width * F->height, s);
@@ -1883,7 +1988,8 @@ VSRStatus renderFrames(Device *dev, FrameObj *const *frames, uint32_t count) {
     // statistics are collected by the per-frame kernels; chunked path tracing
     // and sample masks are per-frame launches too
     if (F->countStats || F->sampleMask ||
-        (F->renderer->r.type == REND_PATHTRACE && F->renderer->r.sampleChunks > 1)) {
+        (F->renderer->r.type == REND_PATHTRACE &&
+         (F->renderer->r.sampleChunks > 1 || F->renderer->r.taa))) {
       single.push_back(F);
       continue;
     }

@@ -261,6 +261,11 @@ struct DRenderer {
   int gradientShading; // volume samples lit along the normalised field gradient
   int numClipPlanes;
   float clip[kMaxClipPlanes][4];
+  // temporal anti-aliasing of the path tracer (Pathtrace.cpp:24-37): a frame
+  // writes its own mean colour and motion vectors, and a resolve pass
+  // blends it with the reprojected previous result (weight taaAlpha)
+  int taa;
+  float taaAlpha;
 };
 
 struct DFrame {
@@ -290,6 +295,15 @@ struct DFrame {
   // the chunk's mean colour; (mean squared luminance, closest depth, Ng.xy);
   // (Ng.z, albedo)
   float4 *chunkOut;
+  // temporal anti-aliasing (renderer taa): this frame's mean colour, the
+  // albedo of its closest sample and its motion vector per pixel (the resolve
+  // pass reads the previous frame's from taaPrev / taaPrevAlbedo), and the
+  // previous and current view-projection matrices (column-major) that the
+  // motion vectors are projected with
+  float4 *taaCurr, *taaPrev;
+  float *taaCurrAlbedo, *taaPrevAlbedo;  // float3 packed
+  float2 *motionVec;
+  float prevMVP[16], currMVP[16];
 };
 
 // Wavefront path-tracer state: one slot per pixel, structure of arrays

@@ -1225,7 +1225,66 @@ struct PixelSample {
   f4 color;
   float depth = 1e31f;
   f3 Ng, albedo;
+  float mvx = 0.f, mvy = 0.f;  // motion vector (TAA), Pathtrace_impl.cpp:290-297
 };
+
+// Window position of P under a column-major view-projection matrix
+// (Visionaray's project, the gluProject convention; viewport = the frame):
+// clip = M (P, 1), ndc = clip / w, win = size (ndc + 1) / 2, each operation
+// rounded in this order.
+void projectWin(const float *M, f3 P, float W, float H, float &wx, float &wy) {
+  auto row = [&](int r) { return ((M[r] * P.x + M[4 + r] * P.y) + M[8 + r] * P.z) + M[12 + r]; };
+  const float cx = row(0), cy = row(1), cw = row(3);
+  const float nx = cx / cw, ny = cy / cw;
+  wx = (W * (nx + 1.f)) * 0.5f;
+  wy = (H * (ny + 1.f)) * 0.5f;
+}
+
+// The view-projection matrix of a perspective camera as Visionaray's
+// pinhole camera sets it up (Perspective.cpp:35-40: perspective(fovy,
+// aspect, 0.001, 1000) and a look-at view from eye along dir with up), in
+// double from the camera's direction and up as given (normalised here),
+// rounded once to float; matrix cameras: proj * view.
+void perspectiveViewProj(const float *eye, const float *dir, const float *up, float fovy,
+                         float aspect, float *out) {
+  const double n = 0.001, f = 1000.0;
+  double F[3] = {dir[0], dir[1], dir[2]}, Up[3] = {up[0], up[1], up[2]};
+  const double fl = std::sqrt(F[0] * F[0] + F[1] * F[1] + F[2] * F[2]);
+  const double ul = std::sqrt(Up[0] * Up[0] + Up[1] * Up[1] + Up[2] * Up[2]);
+  for (int k = 0; k < 3; ++k) {
+    F[k] /= fl;
+    Up[k] /= ul;
+  }
+  double S[3] = {F[1] * Up[2] - F[2] * Up[1], F[2] * Up[0] - F[0] * Up[2],
+                 F[0] * Up[1] - F[1] * Up[0]};
+  const double sl = std::sqrt(S[0] * S[0] + S[1] * S[1] + S[2] * S[2]);
+  for (double &v : S) v /= sl;
+  const double U[3] = {S[1] * F[2] - S[2] * F[1], S[2] * F[0] - S[0] * F[2],
+                       S[0] * F[1] - S[1] * F[0]};
+  double V[16] = {0};
+  for (int k = 0; k < 3; ++k) {
+    V[4 * k + 0] = S[k];
+    V[4 * k + 1] = U[k];
+    V[4 * k + 2] = -F[k];
+  }
+  V[12] = -(S[0] * eye[0] + S[1] * eye[1] + S[2] * eye[2]);
+  V[13] = -(U[0] * eye[0] + U[1] * eye[1] + U[2] * eye[2]);
+  V[14] = F[0] * eye[0] + F[1] * eye[1] + F[2] * eye[2];
+  V[15] = 1.0;
+  const double t = 1.0 / std::tan(0.5 * (double)fovy);
+  double P[16] = {0};
+  P[0] = t / aspect;
+  P[5] = t;
+  P[10] = (f + n) / (n - f);
+  P[11] = -1.0;
+  P[14] = 2.0 * f * n / (n - f);
+  for (int col = 0; col < 4; ++col)
+    for (int row = 0; row < 4; ++row) {
+      double acc = 0.0;
+      for (int k = 0; k < 4; ++k) acc += P[4 * k + row] * V[4 * col + k];
+      out[4 * col + row] = (float)acc;
+    }
+}
 
 // Raycast renderSample, renderer/Raycast_impl.cpp:10-243.
 // sampleGradient (DeviceCopyableObjects.h:582-597): central differences of
@@ -1422,8 +1481,9 @@ struct ShadeState {
 };
 
 // shade(), renderer/Pathtrace_impl.cpp:93-487 (default render mode).
-void shade(const Scene &sc, const OrRenderer &R, LCG &rnd, const Ray &ray, RayType rayType,
-           const HitRec &hitRec, ShadeState &ss, PixelSample &result, unsigned bounceID) {
+void shade(const Scene &sc, const OrRenderer &R, const OrFrame &F, LCG &rnd, const Ray &ray,
+           RayType rayType, const HitRec &hitRec, ShadeState &ss, PixelSample &result,
+           unsigned bounceID) {
   const OrScene &S = *sc.src;
   ss.nextType = Miss;
   if (rayType == Radiance) {
@@ -1487,6 +1547,14 @@ void shade(const Scene &sc, const OrRenderer &R, LCG &rnd, const Ray &ray, RayTy
     }
     ss.sn = sn;
     ss.hitPosOff = hitPos + sn * eps;
+    if (R.taa) {
+      // every radiance hit overwrites the sample's motion vector
+      float px, py, cx, cy;
+      projectWin(F.prevMVP, hitPos, (float)F.width, (float)F.height, px, py);
+      projectWin(F.currMVP, hitPos, (float)F.width, (float)F.height, cx, cy);
+      result.mvx = px - cx;
+      result.mvy = py - cy;
+    }
     int lightID = -1;
     if (S.numLights > 0) {
       float r = rnd();
@@ -1622,7 +1690,7 @@ void pathtracePixel(const Ctx &cx, int x, int y, Counters &c) {
       for (unsigned passID = 0, bounceID = 0; true; ++passID) {
         ray = clipRay(ray, R);
         HitRec hitRec = intersectAll(sc, ray, rnd, c);
-        shade(sc, R, rnd, ray, rayType, hitRec, ss, ps, bounceID);
+        shade(sc, R, F, rnd, ray, rayType, hitRec, ss, ps, bounceID);
         if (passID == 0 && bounceID == 0) firstHit = hitRec.hit;
         ray = ss.nextRay;
         rayType = ss.nextType;
@@ -1658,6 +1726,24 @@ void pathtracePixel(const Ctx &cx, int x, int y, Counters &c) {
   fin.color = accumColor * (1.f / spp);
   // writeSample = fillGBuffer + accumSample + toneMap (DeviceCopyableObjects.h:2692-2781)
   size_t idx = size_t(y) * W + x;
+  if (R.taa) {
+    // fillGBuffer only (Pathtrace_impl.cpp:636-637); the resolve pass blends
+    F.motionVec[2 * idx] = fin.mvx;
+    F.motionVec[2 * idx + 1] = fin.mvy;
+    F.taaCurr[4 * idx] = fin.color.x;
+    F.taaCurr[4 * idx + 1] = fin.color.y;
+    F.taaCurr[4 * idx + 2] = fin.color.z;
+    F.taaCurr[4 * idx + 3] = fin.color.w;
+    F.taaCurrAlbedo[3 * idx] = fin.albedo.x;
+    F.taaCurrAlbedo[3 * idx + 1] = fin.albedo.y;
+    F.taaCurrAlbedo[3 * idx + 2] = fin.albedo.z;
+    if (F.depth && !(fin.depth > F.depth[idx])) {
+      F.depth[idx] = fin.depth;
+      if (F.normal) { F.normal[3 * idx] = fin.Ng.x; F.normal[3 * idx + 1] = fin.Ng.y; F.normal[3 * idx + 2] = fin.Ng.z; }
+      if (F.albedo) { F.albedo[3 * idx] = fin.albedo.x; F.albedo[3 * idx + 1] = fin.albedo.y; F.albedo[3 * idx + 2] = fin.albedo.z; }
+    }
+    return;
+  }
   if (F.depth && !(fin.depth > F.depth[idx])) {
     F.depth[idx] = fin.depth;
     if (F.normal) { F.normal[3 * idx] = fin.Ng.x; F.normal[3 * idx + 1] = fin.Ng.y; F.normal[3 * idx + 2] = fin.Ng.z; }
@@ -1809,8 +1895,95 @@ void or_frame_reset(OrFrame *F) {
   F->accumID = 0;
 }
 
+// The history read of the TAA resolve pass: the previous resolved image at
+// normalised (u, v), clamp addressing, cardinal-spline (Catmull-Rom) filter
+// over 4x4 texels with texel centres at (i + 0.5) / size (the reference's
+// history texture, frame/Frame.cpp:541-545).
+void catmullRomWeights(float f, float *w) {
+  const float f2 = f * f, f3v = f2 * f;
+  w[0] = 0.5f * (-f3v + 2.f * f2 - f);
+  w[1] = 0.5f * (3.f * f3v - 5.f * f2 + 2.f);
+  w[2] = 0.5f * (-3.f * f3v + 4.f * f2 + f);
+  w[3] = 0.5f * (f3v - f2);
+}
+
+f4 historyAt(const float *img, int W, int H, float u, float v) {
+  const float tx = u * (float)W - 0.5f, ty = v * (float)H - 0.5f;
+  const float fx0 = std::floor(tx), fy0 = std::floor(ty);
+  float wx[4], wy[4];
+  catmullRomWeights(tx - fx0, wx);
+  catmullRomWeights(ty - fy0, wy);
+  const int x0 = (int)fx0 - 1, y0 = (int)fy0 - 1;
+  f4 r(0.f);
+  for (int j = 0; j < 4; ++j) {
+    const int yy = std::min(std::max(y0 + j, 0), H - 1);
+    f4 row(0.f);
+    for (int i = 0; i < 4; ++i) {
+      const int xx = std::min(std::max(x0 + i, 0), W - 1);
+      const float *t = img + 4 * (size_t(yy) * W + xx);
+      row.x += wx[i] * t[0]; row.y += wx[i] * t[1]; row.z += wx[i] * t[2]; row.w += wx[i] * t[3];
+    }
+    r.x += wy[j] * row.x; r.y += wy[j] * row.y; r.z += wy[j] * row.z; r.w += wy[j] * row.w;
+  }
+  return r;
+}
+
+// The TAA resolve pass (frame/Frame.cpp:339-381, dco::Frame::accumSample,
+// DeviceCopyableObjects.h:2692-2720) over rows [r0, r1): reproject by the
+// motion vector, blend with weight taaAlpha (1 where the albedo moved by
+// 1e-2 or more), convert into the colour channel; then the frame becomes
+// the next one's history.
+void taaResolve(const OrRenderer &R, OrFrame &F, int r0, int r1) {
+  const int W = F.width, H = F.height;
+  for (int y = r0; y < r1; ++y)
+    for (int x = 0; x < W; ++x) {
+      const size_t idx = size_t(y) * W + x;
+      const float mvx = F.motionVec[2 * idx], mvy = F.motionVec[2 * idx + 1];
+      int px = (int)((float)x + mvx), py = (int)((float)y + mvy);
+      px = std::min(std::max(px, 0), W - 1);
+      py = std::min(std::max(py, 0), H - 1);
+      const size_t pidx = size_t(py) * W + px;
+      float alpha = R.taaAlpha;
+      const float *pa = F.taaPrevAlbedo + 3 * pidx, *ca = F.taaCurrAlbedo + 3 * idx;
+      if (!(std::fabs(pa[0] - ca[0]) < 1e-2f && std::fabs(pa[1] - ca[1]) < 1e-2f &&
+            std::fabs(pa[2] - ca[2]) < 1e-2f))
+        alpha = 1.f;
+      const float u = ((float)x + mvx + 0.5f) / (float)W, v = ((float)y + mvy + 0.5f) / (float)H;
+      const f4 h = historyAt(F.taaPrev, W, H, u, v);
+      float *c = F.taaCurr + 4 * idx;
+      const f4 o((1.f - alpha) * h.x + alpha * c[0], (1.f - alpha) * h.y + alpha * c[1],
+                 (1.f - alpha) * h.z + alpha * c[2], (1.f - alpha) * h.w + alpha * c[3]);
+      c[0] = o.x; c[1] = o.y; c[2] = o.z; c[3] = o.w;
+      if (F.color) {
+        if (F.colorType == OR_COLOR_FLOAT4) {
+          float *d = (float *)F.color + 4 * idx;
+          d[0] = o.x; d[1] = o.y; d[2] = o.z; d[3] = o.w;
+        } else {
+          ((uint32_t *)F.color)[idx] = cvtColor(o, F.colorType == OR_COLOR_SRGB8);
+        }
+      }
+    }
+  const size_t n = size_t(W) * H;
+  std::copy(F.taaCurr, F.taaCurr + 4 * n, F.taaPrev);
+  std::copy(F.taaCurrAlbedo, F.taaCurrAlbedo + 3 * n, F.taaPrevAlbedo);
+}
+
 int or_render_frame(void *scene, const OrCamera *cam, const OrRenderer *rend, OrFrame *frame,
                     int numThreads, OrStats *stats) {
+  if (rend->type == OR_PATHTRACE) {
+    // Frame.cpp:315-334: the current view-projection from a perspective or
+    // matrix camera; the previous one is the last frame's
+    if (cam->type == OR_CAM_PERSPECTIVE) {
+      perspectiveViewProj(cam->position, cam->direction, cam->up, cam->fovy, cam->aspect,
+                          frame->currMVP);
+    } else if (cam->type == OR_CAM_MATRIX) {
+      mul44(cam->proj, cam->view, frame->currMVP);
+    }
+  }
+  if (rend->taa && rend->type == OR_PATHTRACE &&
+      (!frame->taaCurr || !frame->taaPrev || !frame->taaCurrAlbedo || !frame->taaPrevAlbedo ||
+       !frame->motionVec))
+    return 1;
   Ctx cx{(const Scene *)scene, makeCam(*cam), rend, frame};
   const int W = frame->width, H = frame->height;
   int r0 = frame->rowBegin, r1 = frame->rowEnd;
@@ -1846,6 +2019,8 @@ int or_render_frame(void *scene, const OrCamera *cam, const OrRenderer *rend, Or
       stats->marchSamples += c.march; stats->trackingSamples += c.track; stats->cellsVisited += c.cells;
     }
   }
+  if (rend->taa && rend->type == OR_PATHTRACE) taaResolve(*rend, *frame, r0, r1);
+  if (rend->type == OR_PATHTRACE) std::copy(frame->currMVP, frame->currMVP + 16, frame->prevMVP);
   frame->accumID++;
   return 0;
 }

@@ -90,14 +90,16 @@ class OrRenderer(ctypes.Structure):
                 ("ambientRadiance", c_float), ("occlusionDistance", c_float),
                 ("ambientSamples", c_int32), ("maxBounce", c_int32), ("pixelSamples", c_int32),
                 ("volumeSamplingRate", c_float), ("numClipPlanes", c_int32), ("clipPlanes", FP),
-                ("gradientShading", c_int32)]
+                ("gradientShading", c_int32), ("taa", c_int32), ("taaAlpha", c_float)]
 
 
 class OrFrame(ctypes.Structure):
     _fields_ = [("width", c_int32), ("height", c_int32), ("accumID", c_int32),
                 ("colorType", c_int32), ("color", c_void_p), ("depth", FP), ("normal", FP),
                 ("albedo", FP), ("accum", FP), ("sampleSum", DP), ("sampleSumSq", DP),
-                ("rowBegin", c_int32), ("rowEnd", c_int32), ("tileSize", c_int32)]
+                ("rowBegin", c_int32), ("rowEnd", c_int32), ("tileSize", c_int32),
+                ("taaCurr", FP), ("taaPrev", FP), ("taaCurrAlbedo", FP), ("taaPrevAlbedo", FP),
+                ("motionVec", FP), ("prevMVP", c_float * 16), ("currMVP", c_float * 16)]
 
 
 class OrStats(ctypes.Structure):
@@ -449,7 +451,7 @@ def camera(c):
 def sample_chunks(r):
     """The renderer's sample chunks as the renderer core resolves them: a
     divisor of pixelSamples, at most 16 (path tracer only)."""
-    if r.get("type", "pathtrace") == "raycast":
+    if r.get("type", "pathtrace") == "raycast" or r.get("taa", False):
         return 1
     spp = int(r.get("pixelSamples", 1))
     k = min(max(int(r.get("sampleChunks", 1)), 1), min(16, spp))
@@ -474,13 +476,15 @@ def renderer(r):
     orr._planes = np.ascontiguousarray(planes)
     orr.clipPlanes = fptr(orr._planes)
     orr.gradientShading = 1 if r.get("gradientShading", False) else 0
+    orr.taa = 1 if (r.get("taa", False) and orr.type == PATHTRACE) else 0
+    orr.taaAlpha = float(r.get("taaAlpha", 0.3))
     return orr
 
 
 class Frame:
     """Frame buffers of the oracle (float4 colour, depth, normal, albedo)."""
 
-    def __init__(self, w, h, stats=False):
+    def __init__(self, w, h, stats=False, taa=False):
         self.w, self.h = w, h
         self.color = np.zeros((h, w, 4), np.float32)
         self.depth = np.zeros((h, w), np.float32)
@@ -500,6 +504,21 @@ class Frame:
         if stats:
             f.sampleSum = self.sum.ctypes.data_as(DP)
             f.sampleSumSq = self.sumsq.ctypes.data_as(DP)
+        eye = [1.0 if i % 5 == 0 else 0.0 for i in range(16)]
+        f.prevMVP = (c_float * 16)(*eye)
+        f.currMVP = (c_float * 16)(*eye)
+        if taa:
+            # TAA buffers, zero at first (frame/Frame.cpp:535-540)
+            self.taa_curr = np.zeros((h, w, 4), np.float32)
+            self.taa_prev = np.zeros((h, w, 4), np.float32)
+            self.taa_curr_albedo = np.zeros((h, w, 3), np.float32)
+            self.taa_prev_albedo = np.zeros((h, w, 3), np.float32)
+            self.motion_vec = np.zeros((h, w, 2), np.float32)
+            f.taaCurr = fptr(self.taa_curr)
+            f.taaPrev = fptr(self.taa_prev)
+            f.taaCurrAlbedo = fptr(self.taa_curr_albedo)
+            f.taaPrevAlbedo = fptr(self.taa_prev_albedo)
+            f.motionVec = fptr(self.motion_vec)
         self.f = f
         load().or_frame_reset(ctypes.byref(f))
 

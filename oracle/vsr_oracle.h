@@ -139,6 +139,8 @@ typedef struct OrRenderer {
   int32_t numClipPlanes;
   const float *clipPlanes;   /* float4 (n.xyz, d) each */
   int32_t gradientShading;   /* volume samples lit along the field gradient */
+  int32_t taa;               /* temporal anti-aliasing (path tracer) */
+  float taaAlpha;            /* weight of the new frame in the TAA blend */
 } OrRenderer;
 
 typedef struct OrFrame {
@@ -155,6 +157,13 @@ typedef struct OrFrame {
   int32_t rowBegin, rowEnd;  /* render rows [rowBegin,rowEnd) only (0,0 = all) */
   int32_t tileSize;          /* square pixel tiles handed to the threads (0 = 64, as
                                 the reference CPU device); results do not depend on it */
+  /* TAA (renderer taa): this frame's colour, the previous resolved image,
+     the closest samples' albedo (float3) now and before, motion vectors
+     (float2) per pixel; the previous and current view-projection matrices
+     (column-major, in/out: the current one becomes the previous one after
+     each frame; identity at first) */
+  float *taaCurr, *taaPrev, *taaCurrAlbedo, *taaPrevAlbedo, *motionVec;
+  float prevMVP[16], currMVP[16];
 } OrFrame;
 
 typedef struct OrStats {

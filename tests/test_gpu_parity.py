@@ -973,3 +973,44 @@ def test_sample_mask_renders_only_masked_pixels(pkg, device, oracle, wavefront):
     untouched = cnt[..., 0] == 1
     assert untouched.any() and (cnt[..., 0] == 2).any() and (cnt[..., 0] >= 3).any()
     assert float((d[untouched] <= 1e-3).mean()) >= 0.97
+
+
+@pytest.mark.parametrize("move", [False, True])
+def test_pathtrace_taa_same_stream(pkg, device, oracle, move):
+    """Temporal anti-aliasing (renderer taa, taaAlpha; frame/Frame.cpp
+    :339-381): each frame's own mean colour and motion vectors, then the
+    resolve pass blends the reprojected previous result (cardinal-spline
+    history read, albedo test). Four frames, with the camera still (the
+    frames accumulate seeds, motion vectors are zero) or moving sideways
+    (each camera commit restarts accumulation but keeps the history); every
+    frame's resolved colour follows the oracle's."""
+    import ctypes
+    sc = small_spheres(pkg, res=96, spp=4, n=16)
+    sc["renderer"].update(taa=True, taaAlpha=0.3)
+    h = pkg.scenes.build(device, sc)
+    S = oracle.Scene(sc)
+    F = oracle.Frame(96, 96, taa=True)
+    cam = dict(sc["camera"])
+    right = np.cross(np.asarray(cam["direction"]), np.asarray(cam["up"]))
+    right /= np.linalg.norm(right)
+    vsr = pkg.vsr
+    try:
+        for k in range(4):
+            if move and k > 0:
+                cam["position"] = [float(p + 0.4 * r) for p, r in zip(cam["position"], right)]
+                device.set(h["camera"], "position", cam["position"], vsr.FLOAT32_VEC3)
+                device.commit(h["camera"])
+                S = oracle.Scene(dict(sc, camera=dict(cam)))
+                oracle.load().or_frame_reset(ctypes.byref(F.f))
+            assert device.render(h["frame"]) == 0
+            assert device.wait(h["frame"])
+            got = device.map(h["frame"], "channel.color")
+            oracle.render(S, F)
+            d = np.abs(got[..., :3] - F.color[..., :3]).max(axis=-1)
+            frac = float((d <= 1e-3).mean())
+            print(f"taa move={move} frame {k}: {frac:.4f} within 1e-3")
+            assert frac >= 0.97, (k, frac)
+        assert device.get_uint(h["frame"], "errorFlags") == 0
+    finally:
+        for o in (h["frame"], h["renderer"], h["camera"], h["world"], *h["keep"]):
+            device.release(o)

@@ -655,3 +655,58 @@ def test_render_is_thread_count_independent(oracle, pkg):
     oracle.render(S, b, num_threads=4)
     assert np.array_equal(a.color, b.color)
     assert np.array_equal(a.depth, b.depth)
+
+
+def test_taa_resolve_closed_form(oracle, pkg):
+    """TAA on pixels that see only the background (a camera looking away
+    from the geometry): the frame colour is the background b, the motion
+    vector 0 and the albedo 0 in every frame, so the resolve pass blends the
+    history (the Catmull-Rom read of a constant image, weights summing to
+    one) with weight alpha: after k frames from the zero history the colour
+    is b (1 - (1 - alpha)^k). With a static camera the motion vectors are
+    exactly zero."""
+    sc = pkg.scenes.config1(res=24, spp=2, num_spheres=4, nu=8, nv=4)
+    cam = dict(sc["camera"])
+    cam["direction"] = [-v for v in cam["direction"]]  # away from the spheres
+    cam["position"] = [0.0, 40.0, 60.0]
+    sc["camera"] = cam
+    bg = [0.2, 0.5, 0.8, 1.0]
+    alpha = 0.3
+    sc["renderer"].update(background=bg, taa=True, taaAlpha=alpha)
+    S = oracle.Scene(sc)
+    F = oracle.Frame(24, 24, taa=True)
+    for k in range(1, 5):
+        oracle.render(S, F)
+        want = np.asarray(bg, np.float64) * (1.0 - (1.0 - alpha) ** k)
+        assert np.abs(F.color - want).max() < 1e-5, k
+        assert np.array_equal(F.taa_prev, F.taa_curr)  # the frame became the history
+        assert not F.motion_vec.any()
+    assert np.all(F.depth == np.float32(1e31))
+
+
+def test_taa_motion_vectors_follow_the_camera(oracle, pkg):
+    """A camera moved sideways between two frames: on pixels that see the
+    ground plane, the motion vector points back to where the hit projected in
+    the previous frame (its x component has the sign of the camera's move in
+    screen space and no pixel moves more than the shift of the nearest
+    point), and pixels that see nothing keep a zero vector."""
+    sc = pkg.scenes.config1(res=48, spp=1, num_spheres=6, nu=8, nv=4)
+    sc["renderer"].update(taa=True, maxBounce=0)
+    S = oracle.Scene(sc)
+    F = oracle.Frame(48, 48, taa=True)
+    oracle.render(S, F)
+    cam = dict(sc["camera"])
+    right = np.cross(np.asarray(cam["direction"]), np.asarray(cam["up"]))
+    right /= np.linalg.norm(right)
+    cam["position"] = [float(p + 0.5 * r) for p, r in zip(cam["position"], right)]
+    S2 = oracle.Scene(dict(sc, camera=cam))
+    # a camera commit restarts accumulation and the depth buffer, not TAA
+    oracle.load().or_frame_reset(ctypes.byref(F.f))
+    oracle.render(S2, F)
+    hit = F.depth < 1e30
+    mv = F.motion_vec
+    assert hit.mean() > 0.2
+    # the camera moved right: points move left on screen, so the previous
+    # window position is to the right of the current one
+    assert float((mv[hit][:, 0] > 0).mean()) > 0.999
+    assert not mv[~hit].any()

@@ -79,14 +79,14 @@ cudaError_t launchRaycast(const DScene &S, const DCamera &C, const DRenderer &R,
   // the full variant for gradient shading, and for point / spot lights,
   // spheres, cones, cylinders, quads or iso-surfaces on surfaces (volume-only worlds light nothing without gradient
   // shading)
-  if (R.gradientShading ||
+  if (R.gradientShading || S.areaLights ||
       (S.hasSurfaces && (S.positionalLights || S.numAnalytic || S.quadGroups || S.numIso))) {
     if (count) launch(kRaycast<true, true, true>);
     else launch(kRaycast<false, true, true>);
   } else if (S.hasSurfaces) {
     if (count) launch(kRaycast<true, true, false>);
     else launch(kRaycast<false, true, false>);
-  } else if (R.pixelSamples == 1 && scratch) {
+  } else if (R.pixelSamples == 1 && scratch && !S.areaLights) {
     // volume-only world: set-up, segments, combination (k_volume_march.cu)
     return launchVolumeMarch(S, C, R, F, stageTFSize, count, *scratch, stream);
   } else {

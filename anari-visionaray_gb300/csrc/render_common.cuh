@@ -975,6 +975,31 @@ struct LightSample {
 template <bool Positional>
 __device__ __forceinline__ LightSample sampleLight(const DLight &L, float3 P, Rng &rnd) {
   LightSample s;
+  if (Positional && L.type == LIGHT_QUAD) {
+    // Quad light (the reference's area_light<float, dco::Quad>; Visionaray's
+    // sampling is not in the reference, so its conventions are restated):
+    // sample_surface(Quad) picks the first triangle when A1 / (A1 + A2) < r
+    // (DeviceCopyableObjects.h:2258-2271), then a uniform point of the
+    // triangle from two draws (v1 + sqrt(u1) (1 - u2) a + sqrt(u1) u2 b);
+    // intensity = color * intensity; the pdf is the area density over the
+    // light-side cosine, 1 / (A |cos|), so that intensity / dist^2 / pdf
+    // is the light's contribution per unit solid angle as renderer/
+    // common.h:1441-1464 and Pathtrace_impl.cpp:343-354 use it.
+    const float r = rnd();
+    const float3 e1 = ld3(L.e1), e2 = ld3(L.e2), d = e1 + e2;
+    float3 a = d, b = e2;
+    if (L.area1 / (L.area1 + L.area2) < r) { a = e1; b = d; }
+    const float u1 = rnd(), u2 = rnd();
+    const float su = sqrtf(u1);
+    const float3 pos = ld3(L.pos) + a * (su * (1.f - u2)) + b * (su * u2);
+    s.dir = pos - P;
+    s.dist = length(s.dir);
+    s.dist2 = s.dist * s.dist;
+    const float cosL = fabsf(dot(s.dir, ld3(L.normal))) / s.dist;
+    s.pdf = 1.f / ((L.area1 + L.area2) * cosL);
+    s.intensity = ld3(L.intensity);
+    return s;
+  }
   if (Positional && L.type != LIGHT_DIRECTIONAL) {
     s.intensity = ld3(L.intensity);
     s.pdf = 1.f;
@@ -1009,6 +1034,55 @@ __device__ __forceinline__ LightSample sampleLight(const DLight &L, float3 P, Rn
   s.dist2 = 1.f;
   s.intensity = ld3(L.intensity);
   return s;
+}
+
+// power_heuristic(a, b) = a^2 / (a^2 + b^2) (the MIS weight of
+// renderer/Pathtrace_impl.cpp:175, :367-369).
+__device__ __forceinline__ float powerHeuristic(float a, float b) {
+  const float a2 = a * a;
+  return a2 / (a2 + b * b);
+}
+
+// The nearest quad light the ray meets (intersectLights, renderer/common.h
+// :1566-1603, quad branch; both sides lit): intersect(Ray, Quad) tests the
+// two tessellated triangles with the triangle test and keeps the nearer hit
+// (DeviceCopyableObjects.h:2211-2237); at bounce 0 invisible lights are
+// skipped. Returns the light's index or -1, and its distance.
+__device__ __forceinline__ bool quadLightTriT(float3 o, float3 d, float3 v1, float3 e1, float3 e2,
+                                              float tmin, float tmax, float &t) {
+  const float3 s1 = cross(d, e2);
+  const float div = dot(s1, e1);
+  if (div == 0.f) return false;
+  const float idiv = 1.f / div;
+  const float3 dd = o - v1;
+  const float bb1 = dot(dd, s1) * idiv;
+  if (bb1 < 0.f || bb1 > 1.f) return false;
+  const float3 s2 = cross(dd, e1);
+  const float bb2 = dot(d, s2) * idiv;
+  if (bb2 < 0.f || bb1 + bb2 > 1.f) return false;
+  t = dot(e2, s2) * idiv;
+  return t >= tmin && t <= tmax;
+}
+__device__ __forceinline__ int intersectQuadLights(const DScene &S, float3 o, float3 d, float tmin,
+                                                   float tmax, unsigned bounceID, float &tl) {
+  int id = -1;
+  tl = FLT_MAX;
+  for (int i = 0; i < S.numLights; ++i) {
+    const DLight &L = S.lights[i];
+    if (L.type != LIGHT_QUAD || (bounceID == 0 && !L.visible)) continue;
+    const float3 v1 = ld3(L.pos), e1 = ld3(L.e1), e2 = ld3(L.e2), dd = e1 + e2;
+    float t1 = FLT_MAX, t2 = FLT_MAX;
+    const bool h1 = quadLightTriT(o, d, v1, e1, dd, tmin, tmax, t1);
+    const bool h2 = quadLightTriT(o, d, v1, dd, e2, tmin, tmax, t2);
+    float t = FLT_MAX;
+    if (h1) t = t1;
+    if (h2 && t2 < t) t = t2;
+    if ((h1 || h2) && t < tl) {
+      tl = t;
+      id = i;
+    }
+  }
+  return id;
 }
 
 // Normalised central-difference gradient of the field at voxel-space point

@@ -80,10 +80,21 @@ __device__ void raycastSample(const DScene &S, const DRenderer &R, Ray ray, cons
       }
     }
   }
-  float4 result = make_float4(surfaceColor.x + (1.f - surfaceAlpha) * bg.x,
-                              surfaceColor.y + (1.f - surfaceAlpha) * bg.y,
-                              surfaceColor.z + (1.f - surfaceAlpha) * bg.z,
-                              surfaceAlpha + (1.f - surfaceAlpha) * bg.w);
+  // behind the surfaces: a quad light the ray meets (its intensity, alpha
+  // 1), else the background (Raycast_impl.cpp:158-172)
+  float4 back = bg;
+  if (Full && S.areaLights) {
+    float tl;
+    const int li = intersectQuadLights(S, ray.o, ray.d, ray.tmin, ray.tmax, 0, tl);
+    if (li >= 0) {
+      const float3 I = ld3(S.lights[li].intensity);
+      back = make_float4(I.x, I.y, I.z, 1.f);
+    }
+  }
+  float4 result = make_float4(surfaceColor.x + (1.f - surfaceAlpha) * back.x,
+                              surfaceColor.y + (1.f - surfaceAlpha) * back.y,
+                              surfaceColor.z + (1.f - surfaceAlpha) * back.z,
+                              surfaceAlpha + (1.f - surfaceAlpha) * back.w);
   // intersectVolumeBounds: closest volume box entry.
   int vInst = -1, vIdx = -1;
   float vT = FLT_MAX;
@@ -203,11 +214,14 @@ enum RayType { RT_RADIANCE = 0, RT_SHADOW = 1, RT_AO = 2, RT_MISS = 3 };
 
 struct HitRec {
   bool surfHit, volHit, hit, volumeHit;
+  bool lightHit;  // a quad light is the nearest hit (Full variants)
   Hit surf;
   float volT;
   float3 volAlbedo;
   int volInst;
   int volIdx;  // the volume hit
+  int lightID;
+  float lightT;
 };
 
 // intersectAll, renderer/common.h:1605-1620, with intersectSurfaces<1>
@@ -216,8 +230,11 @@ struct HitRec {
 template <bool Count, bool Full>
 __device__ __forceinline__ void intersectAll(const DScene &S, const Ray &ray, bool shadow, Rng &rnd,
                                              HitRec &h, uint32_t &err, unsigned long long *cnt,
-                                             bool hwFilter) {
+                                             bool hwFilter, unsigned bounceID = 0) {
   h.surfHit = false;
+  h.lightHit = false;
+  h.lightID = -1;
+  h.lightT = FLT_MAX;
   long long tc0 = 0;
   if (Count) tc0 = clock64();
   if (S.hasSurfaces) {
@@ -270,8 +287,17 @@ __device__ __forceinline__ void intersectAll(const DScene &S, const Ray &ray, bo
     }
   }
   if (Count && S.numVolumes > 0) atomicAdd(&cnt[26], (unsigned long long)(clock64() - tc0));
-  h.hit = h.surfHit || h.volHit;
-  h.volumeHit = h.volHit && (!h.surfHit || h.volT < h.surf.t);
+  bool lh = false;
+  if (Full && S.areaLights) {
+    h.lightID = intersectQuadLights(S, ray.o, ray.d, ray.tmin, ray.tmax, bounceID, h.lightT);
+    lh = h.lightID >= 0;
+  }
+  // renderer/common.h:1605-1620: a light hit takes precedence over surface
+  // and volume hits at equal distance (<=), a volume over a surface only
+  // when nearer
+  h.hit = h.surfHit || h.volHit || lh;
+  h.lightHit = lh && (!h.surfHit || h.lightT <= h.surf.t) && (!h.volHit || h.lightT <= h.volT);
+  h.volumeHit = h.volHit && (!h.surfHit || h.volT < h.surf.t) && (!lh || h.volT < h.lightT);
 }
 
 // Per-pixel body of VisionarayRendererPathtrace::renderFrame
@@ -341,12 +367,16 @@ __device__ __forceinline__ void pathtracePixel(const DScene &S, const DCamera &C
         if (rayType == RT_SHADOW && S.numLights == 0) {
           // the shadow ray of a light-less scene has a NaN direction and
           // cannot hit anything: skip the traversal
-          hr.surfHit = hr.volHit = hr.hit = hr.volumeHit = false;
+          hr.surfHit = hr.volHit = hr.hit = hr.volumeHit = hr.lightHit = false;
         } else {
-          intersectAll<Count, Full>(S, ray, rayType == RT_SHADOW || rayType == RT_AO, rnd, hr, err, cnt,
-                              R.hwFilter != 0);
+          // every ray type tests the quad lights (a radiance ray's emission,
+          // an AO ray's occluder; a shadow ray's volume hit beyond the light
+          // does not count)
+          intersectAll<Count, Full>(S, ray, rayType == RT_SHADOW || rayType == RT_AO, rnd, hr, err,
+                                    cnt, R.hwFilter != 0, bounceID);
         }
         int nextType = RT_MISS;
+        bool lightHitNow = false;
         if (rayType == RT_RADIANCE) {
           baseColor = f3(0.f);
           visLight = 1.f;
@@ -356,6 +386,23 @@ __device__ __forceinline__ void pathtracePixel(const DScene &S, const DCamera &C
           aoCount = 0.f;
           if (!hr.hit) {
             shadedColor = f3(0.f);
+          } else if (Full && hr.lightHit) {
+            // a quad light seen by the ray: its intensity, weighted after a
+            // bounce by the BSDF sample's MIS weight against the light's
+            // solid-angle density, ends the path (Pathtrace_impl.cpp:139-182)
+            const DLight &L = S.lights[hr.lightID];
+            shadedColor = ld3(L.intensity);
+            misWeightNEE = 1.f;
+            if (bounceID > 0) {
+              const float3 hp = ray.o + hr.lightT * ray.d;
+              const float ld = length(hp - ray.o);
+              const float3 Ld = normalize(hp - ray.o);
+              const float LdotNl = fabsf(dot(-Ld, ld3(L.normal)));
+              const float solidAngle = (LdotNl * (L.area1 + L.area2)) / (ld * ld);
+              const float lightPDF = 1.f / solidAngle;
+              shadedColor = shadedColor * powerHeuristic(bsdf.pdf, lightPDF / float(S.numLights));
+            }
+            lightHitNow = true;
           } else {
             const float3 viewDir = -normalize(ray.d);
             float3 hitPos, gn, color;
@@ -415,10 +462,12 @@ __device__ __forceinline__ void pathtracePixel(const DScene &S, const DCamera &C
               const float2 b = projectWin(F.currMVP, hitPos, (float)W, (float)H);
               pMV = make_float2(a.x - b.x, a.y - b.y);
             }
+            bool areaSample = false;
             if (S.numLights > 0) {
               int lightID = int(rnd() * S.numLights);
               if (lightID == S.numLights) lightID = 0;
               ls = sampleLight<Full>(S.lights[lightID], hitPos, rnd);
+              areaSample = Full && S.lights[lightID].type == LIGHT_QUAD;
             }
             const float3 lightDir = normalize(ls.dir);
             const float3 lightIntensity = ls.intensity * safeRcp(ls.dist2);
@@ -439,7 +488,10 @@ __device__ __forceinline__ void pathtracePixel(const DScene &S, const DCamera &C
               shadedColor = f * lightIntensity * NdotL * safeRcp(ls.pdf) * float(S.numLights);
               bsdf = sampleMaterial(*mat, gn, sn, viewDir, rnd);
             }
+            // Pathtrace_impl.cpp:365-375: MIS weight of the light sample
+            // against the BSDF sample for area lights, 1 for delta lights
             misWeightNEE = S.numLights > 0 ? 1.f : 0.f;
+            if (areaSample) misWeightNEE = powerHeuristic(ls.pdf / float(S.numLights), bsdf.pdf);
             baseColor = color;
           }
         } else if (rayType == RT_SHADOW) {
@@ -453,7 +505,7 @@ __device__ __forceinline__ void pathtracePixel(const DScene &S, const DCamera &C
           if (weight > 0.f && hr.hit) aoCount += weight;
         }
         // advance the state machine (prepareNextRay, :37-90)
-        const bool radianceHit = rayType == RT_RADIANCE && hr.hit;
+        const bool radianceHit = rayType == RT_RADIANCE && hr.hit && !lightHitNow;
         bool wantShadow = radianceHit && ls.pdf >= 0.f;
         bool wantAO = false, wantBounce = false;
         if (radianceHit && !wantShadow) {

@@ -727,12 +727,16 @@ struct Material : Object {
 struct Light : Object {
   int type = LIGHT_DIRECTIONAL;
   float direction[3] = {0, 0, -1}, color[3] = {1, 1, 1}, position[3] = {0, 0, 0};
+  float edge1[3] = {1, 0, 0}, edge2[3] = {0, 1, 0};  // quad (Quad.cpp:18-27)
   float irradiance = 1.f, angularDiameter = 0.f, intensity = 1.f;
   float cosOuter = -1.f, cosInner = -1.f;
   int visible = 1;
   using Object::Object;
   void commit() override {
-    type = subtype == "point" ? LIGHT_POINT : subtype == "spot" ? LIGHT_SPOT : LIGHT_DIRECTIONAL;
+    type = subtype == "point"  ? LIGHT_POINT
+           : subtype == "spot" ? LIGHT_SPOT
+           : subtype == "quad" ? LIGHT_QUAD
+                               : LIGHT_DIRECTIONAL;
     color[0] = color[1] = color[2] = 1.f;
     getv("color", VSR_FLOAT32_VEC3, color);
     visible = 1; geti("visible", visible);
@@ -747,6 +751,31 @@ struct Light : Object {
       irradiance = std::max(irradiance, 0.f);
       angularDiameter = 0.f; getf("angularDiameter", angularDiameter);
       angularDiameter = std::max(angularDiameter, 0.f);
+    } else if (type == LIGHT_QUAD) {
+      // Quad.cpp:18-55: position, edge1, edge2, intensity (clamped to >= 0),
+      // side (read and checked; the reference lights both sides)
+      position[0] = position[1] = position[2] = 0.f;
+      getv("position", VSR_FLOAT32_VEC3, position);
+      const float d1[3] = {1, 0, 0}, d2[3] = {0, 1, 0};
+      memcpy(edge1, d1, sizeof(edge1));
+      memcpy(edge2, d2, sizeof(edge2));
+      getv("edge1", VSR_FLOAT32_VEC3, edge1);
+      getv("edge2", VSR_FLOAT32_VEC3, edge2);
+      intensity = 1.f; getf("intensity", intensity);
+      intensity = std::min(std::max(intensity, 0.f), maxF);
+      const std::string side = gets("side", "front");
+      const float l1 = std::sqrt(edge1[0] * edge1[0] + edge1[1] * edge1[1] + edge1[2] * edge1[2]);
+      const float l2 = std::sqrt(edge2[0] * edge2[0] + edge2[1] * edge2[1] + edge2[2] * edge2[2]);
+      if (l1 == 0.f || l2 == 0.f) {
+        warn("quad light has zero-length edges");
+        valid = false;
+        return;
+      }
+      if (side != "front" && side != "back" && side != "both") {
+        warn("quad light has invalid side");
+        valid = false;
+        return;
+      }
     } else if (type == LIGHT_POINT) {
       position[0] = 0; position[1] = 0; position[2] = -1;
       getv("position", VSR_FLOAT32_VEC3, position);
@@ -1495,6 +1524,26 @@ struct World : Object {
           dl.cosHalfAngle = 1.f;
           dl.cosOuter = L->cosOuter;
           dl.cosInner = L->cosInner;
+          if (L->type == LIGHT_QUAD) {
+            // the quad in world space (xfmLight); the areas and normal of
+            // its tessellation (DeviceCopyableObjects.h:2191-2257)
+            linear(L->edge1, dl.e1);
+            linear(L->edge2, dl.e2);
+            float d[3], c1[3], c2[3];
+            for (int k = 0; k < 3; ++k) d[k] = dl.e1[k] + dl.e2[k];
+            auto cross = [](const float *a, const float *b, float *o) {
+              o[0] = a[1] * b[2] - a[2] * b[1];
+              o[1] = a[2] * b[0] - a[0] * b[2];
+              o[2] = a[0] * b[1] - a[1] * b[0];
+            };
+            cross(dl.e1, d, c1);
+            cross(d, dl.e2, c2);
+            const float n1 = std::sqrt(c1[0] * c1[0] + c1[1] * c1[1] + c1[2] * c1[2]);
+            const float n2 = std::sqrt(c2[0] * c2[0] + c2[1] * c2[1] + c2[2] * c2[2]);
+            dl.area1 = 0.5f * n1;
+            dl.area2 = 0.5f * n2;
+            for (int k = 0; k < 3; ++k) dl.normal[k] = c1[k] / n1;
+          }
         }
         lights.push_back(dl);
       }
@@ -1521,7 +1570,11 @@ struct World : Object {
     scene.numGroups = (int)dgroups.size();
     scene.numLights = (int)lights.size();
     scene.positionalLights = 0;
-    for (const DLight &l : lights) scene.positionalLights += l.type != LIGHT_DIRECTIONAL;
+    scene.areaLights = 0;
+    for (const DLight &l : lights) {
+      scene.positionalLights += l.type != LIGHT_DIRECTIONAL;
+      scene.areaLights += l.type == LIGHT_QUAD;
+    }
     scene.numVolumes = (int)vols.size();
     scene.allOpaque = allOpaque ? 1 : 0;
     scene.hasSurfaces = anySurf ? 1 : 0;
@@ -1797,7 +1850,8 @@ VSRStatus renderFrame(Device *dev, FrameObj *F) {
   // cylinders, quads and iso-surfaces: the
   // megakernel takes such frames
   const bool wave = F->renderer->wavefront && !R.gradientShading && !W->scene.numAnalytic &&
-                    !W->scene.quadGroups && !W->scene.numIso && R.sampleChunks <= 1 && !R.taa;
+                    !W->scene.quadGroups && !W->scene.numIso && R.sampleChunks <= 1 && !R.taa &&
+                    !W->scene.areaLights;
   int stage = 0;
   MarchScratch ms{};
   bool segmented = false;
@@ -1806,7 +1860,8 @@ VSRStatus renderFrame(Device *dev, FrameObj *F) {
     if (!W->volsHost.empty() && W->volsHost[0].tfSize <= 4096) stage = W->volsHost[0].tfSize;
     // the segmented marcher composites unshaded samples; gradient shading
     // takes the per-pixel kernel
-    segmented = !W->scene.hasSurfaces && R.pixelSamples == 1 && !R.gradientShading;
+    segmented = !W->scene.hasSurfaces && R.pixelSamples == 1 && !R.gradientShading &&
+                !W->scene.areaLights;
     if (segmented && !F->ensureMarch()) {
       dev->report(F, VSR_FRAME, VSR_SEVERITY_ERROR, VSR_ERROR_OUT_OF_MEMORY,
                   "volume marcher scratch allocation failed");
@@ -2015,7 +2070,7 @@ VSRStatus renderFrames(Device *dev, FrameObj *const *frames, uint32_t count) {
     }
     j.F = F->record();
     j.kind = j.R.type != REND_RAYCAST ? JOB_PATHTRACE
-             : (j.R.gradientShading ||
+             : (j.R.gradientShading || j.S.areaLights ||
                 (j.S.hasSurfaces &&
                  (j.S.positionalLights || j.S.numAnalytic || j.S.quadGroups || j.S.numIso)))
                  ? JOB_RAYCAST_FULL
@@ -2313,7 +2368,7 @@ VSRObject vsrNewMaterial(VSRDevice d, const char *s) {
   return newObj<Material>(d, VSR_MATERIAL, s, {"matte", "physicallyBased"});
 }
 VSRObject vsrNewLight(VSRDevice d, const char *s) {
-  return newObj<Light>(d, VSR_LIGHT, s, {"directional", "point", "spot"});
+  return newObj<Light>(d, VSR_LIGHT, s, {"directional", "point", "spot", "quad"});
 }
 VSRObject vsrNewSurface(VSRDevice d) { return newObj<Surface>(d, VSR_SURFACE, "", {}); }
 VSRObject vsrNewGroup(VSRDevice d) { return newObj<Group>(d, VSR_GROUP, "", {}); }

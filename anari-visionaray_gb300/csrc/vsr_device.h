@@ -117,7 +117,7 @@ struct DMaterial {
   float pad[3];
 };
 
-enum LightType { LIGHT_DIRECTIONAL = 0, LIGHT_POINT = 1, LIGHT_SPOT = 2 };
+enum LightType { LIGHT_DIRECTIONAL = 0, LIGHT_POINT = 1, LIGHT_SPOT = 2, LIGHT_QUAD = 3 };
 
 // One light in world space (instance transforms applied on the host).
 struct DLight {
@@ -131,6 +131,13 @@ struct DLight {
   float cosOuter;      // spot: cos(openingAngle)
   float cosInner;      // spot: cos(openingAngle - 2 falloffAngle)
   float pad[2];
+  // quad: corner pos, edges e1, e2 (the parallelogram pos + a e1 + b e2,
+  // tessellated as (pos, e1, e1 + e2) and (pos, e1 + e2, e2)), the two
+  // triangles' areas and the unit normal of the first
+  float e1[3], e2[3];
+  float area1, area2;
+  float normal[3];
+  float pad2;
 };
 
 struct DVolume {
@@ -220,7 +227,8 @@ struct DScene {
   int numInstances;
   int numGroups;
   int numLights;
-  int positionalLights;  // point and spot lights among them: the kernels' full variants
+  int positionalLights;  // point, spot and quad lights among them: the kernels' full variants
+  int areaLights;        // quad lights among them (hit by rays; no wavefront mode)
   int numAnalytic;       // spheres, cones, cylinders in all groups: the kernels' full variants
   int quadGroups;        // groups with quad geometry (triNormal set): the full variants
   int numIso;            // iso-surfaces in all groups: the full variants

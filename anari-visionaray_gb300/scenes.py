@@ -22,7 +22,8 @@ is fixed in each generator. A scene is a plain dict:
   lights   : [{"type": "directional" (default), "direction", "color", "irradiance",
                 "angularDiameter"} | {"type": "point", "position", "color", "intensity"} |
               {"type": "spot", "position", "direction", "openingAngle", "falloffAngle",
-               "color", "intensity"}]
+               "color", "intensity"} | {"type": "quad", "position", "edge1", "edge2",
+               "color", "intensity", "side"}; any light may carry "visible" (bool)]
   instances: [{"transform": 12 floats (column-major 3x4), "surfaces": [...],
                "volumes": [...], "lights": [...]}]   (optional)
   camera   : {"type": "perspective", "position", "direction", "up", "fovy", "aspect"}
@@ -403,15 +404,19 @@ def _lights(dev, lights, keep):
         kind = L.get("type", "directional")
         lt = dev.light(kind)
         dev.set(lt, "color", L.get("color", [1, 1, 1]), vsr.FLOAT32_VEC3)
+        if "visible" in L:
+            dev.set(lt, "visible", bool(L["visible"]))
         if kind == "directional":
             dev.set(lt, "direction", L["direction"], vsr.FLOAT32_VEC3)
             dev.set(lt, "irradiance", float(L.get("irradiance", 1.0)))
             if "angularDiameter" in L:
                 dev.set(lt, "angularDiameter", float(L["angularDiameter"]))
         else:
-            for k in ("position", "direction"):
+            for k in ("position", "direction", "edge1", "edge2"):
                 if k in L:
                     dev.set(lt, k, L[k], vsr.FLOAT32_VEC3)
+            if "side" in L:
+                dev.set(lt, "side", L["side"])
             for k in ("intensity", "openingAngle", "falloffAngle"):
                 if k in L:
                     dev.set(lt, k, float(L[k]))

@@ -1178,9 +1178,53 @@ BSDFSample sampleMaterial(const OrMaterial &m, f3 Ng, f3 Ns, f3 viewDir, LCG &rn
 // ---------------------------------------------------------------------------
 struct LightSample { f3 intensity, dir; float pdf = 0.f, dist = 0.f, dist2 = 0.f; };
 
+// Quad light geometry (dco::Quad, DeviceCopyableObjects.h:2187-2257): the
+// parallelogram v1 + a e1 + b e2 tessellated as the triangles
+// (v1, e1, e1 + e2) and (v1, e1 + e2, e2); each triangle's area is half the
+// length of its edges' cross product, the light's normal the first
+// triangle's unit normal.
+struct QuadGeom { f3 v1, e1, e2, d, n; float A1, A2; };
+QuadGeom quadGeom(const OrLight &L) {
+  QuadGeom q;
+  q.v1 = f3(L.position[0], L.position[1], L.position[2]);
+  q.e1 = f3(L.edge1[0], L.edge1[1], L.edge1[2]);
+  q.e2 = f3(L.edge2[0], L.edge2[1], L.edge2[2]);
+  q.d = q.e1 + q.e2;
+  const f3 c1 = cross(q.e1, q.d), c2 = cross(q.d, q.e2);
+  const float n1 = length(c1);
+  q.A1 = 0.5f * n1;
+  q.A2 = 0.5f * length(c2);
+  q.n = c1 / n1;
+  return q;
+}
+
 LightSample sampleLight(const OrLight &L, f3 P, LCG &rnd) {
   LightSample s;
   s.pdf = 1.f;
+  if (L.type == 3) {
+    // area_light<float, dco::Quad> (Visionaray, not vendored; conventions
+    // restated): sample_surface(Quad) takes the first triangle when
+    // A1 / (A1 + A2) < r (DeviceCopyableObjects.h:2258-2271), then the
+    // triangle point v1 + sqrt(u1)(1 - u2) e1 + sqrt(u1) u2 e2 of two more
+    // draws; intensity = color * intensity; pdf = 1 / (A |cos|) with the
+    // cosine between the sample direction and the light's normal, so that
+    // intensity / dist^2 / pdf is the area light's estimator as
+    // renderer/common.h:1441-1464 and Pathtrace_impl.cpp:343-354 use it.
+    const QuadGeom q = quadGeom(L);
+    const float r = rnd();
+    f3 a = q.d, b = q.e2;
+    if (q.A1 / (q.A1 + q.A2) < r) { a = q.e1; b = q.d; }
+    const float u1 = rnd(), u2 = rnd();
+    const float su = std::sqrt(u1);
+    const f3 pos = q.v1 + a * (su * (1.f - u2)) + b * (su * u2);
+    s.dir = pos - P;
+    s.dist = length(s.dir);
+    s.dist2 = s.dist * s.dist;
+    const float cosL = std::fabs(dot(s.dir, q.n)) / s.dist;
+    s.pdf = 1.f / ((q.A1 + q.A2) * cosL);
+    s.intensity = f3(L.color[0], L.color[1], L.color[2]) * L.intensity;
+    return s;
+  }
   if (L.type == 0) {
     f3 d = -normalize(f3(L.direction[0], L.direction[1], L.direction[2]));
     if (L.angularDiameter > 0.f) {
@@ -1220,6 +1264,44 @@ LightSample sampleLight(const OrLight &L, f3 P, LCG &rnd) {
 }
 
 inline float safe_rcp(float f) { return f > 0.f ? 1.f / f : 0.f; }
+
+// intersectLights (renderer/common.h:1566-1603), quad branch: each quad
+// light is tested as its two triangles with the ray's [tmin, tmax]
+// (intersect(Ray, Quad), DeviceCopyableObjects.h:2211-2237, the nearer hit
+// kept); both sides are lit (Quad.cpp:48-51 fixes the side to Both); at
+// bounce 0 invisible lights are skipped; the nearest light wins, the first
+// on ties. Returns the light's index or -1 and its distance in tl.
+int intersectQuadLights(const OrScene &S, const Ray &ray, unsigned bounceID, float &tl) {
+  auto tri = [&](f3 v1, f3 e1, f3 e2, float &t) {
+    f3 s1 = cross(ray.dir, e2);
+    float div = dot(s1, e1);
+    if (div == 0.f) return false;
+    float inv = 1.f / div;
+    f3 d = ray.ori - v1;
+    float b1 = dot(d, s1) * inv;
+    if (b1 < 0.f || b1 > 1.f) return false;
+    f3 s2 = cross(d, e1);
+    float b2 = dot(ray.dir, s2) * inv;
+    if (b2 < 0.f || b1 + b2 > 1.f) return false;
+    t = dot(e2, s2) * inv;
+    return t >= ray.tmin && t <= ray.tmax;
+  };
+  int id = -1;
+  tl = FLT_MAX;
+  for (int i = 0; i < S.numLights; ++i) {
+    const OrLight &L = S.lights[i];
+    if (L.type != 3 || (bounceID == 0 && !L.visible)) continue;
+    const QuadGeom q = quadGeom(L);
+    float t1 = FLT_MAX, t2 = FLT_MAX;
+    const bool h1 = tri(q.v1, q.e1, q.d, t1);
+    const bool h2 = tri(q.v1, q.d, q.e2, t2);
+    float t = FLT_MAX;
+    if (h1) t = t1;
+    if (h2 && t2 < t) t = t2;
+    if ((h1 || h2) && t < tl) { tl = t; id = i; }
+  }
+  return id;
+}
 
 struct PixelSample {
   f4 color;
@@ -1312,7 +1394,7 @@ f3 gradientShade(const OrScene &S, const OrRenderer &R, const Vol &vol, f3 P, f3
   f3 shaded(0.f);
   if (length(gn) > 1e-10f) {
     for (int li = 0; li < S.numLights; ++li) {
-      LCG dummy(0, 0);
+      LCG dummy;  // state 0: the reference's raycast stream is never seeded
       LightSample ls = sampleLight(S.lights[li], P, dummy);
       f3 lightDir = normalize(ls.dir);
       f3 lightIntensity = ls.intensity * safe_rcp(ls.dist2);
@@ -1351,7 +1433,7 @@ PixelSample raycastSample(const Scene &sc, const OrRenderer &R, Ray ray, Counter
     f3 shadedColor(0.f);
     f3 viewDir = -ray.dir;
     for (int li = 0; li < S.numLights; ++li) {
-      LCG dummy(0, 0);
+      LCG dummy;  // state 0: the reference's raycast stream is never seeded
       LightSample ls = sampleLight(S.lights[li], hitPos, dummy);
       f3 lightDir = normalize(ls.dir);
       f3 lightIntensity = ls.intensity * safe_rcp(ls.dist2);
@@ -1379,7 +1461,18 @@ PixelSample raycastSample(const Scene &sc, const OrRenderer &R, Ray ray, Counter
       break;
     }
   }
-  result.color = over(f4(surfaceColor, surfaceAlpha), bgColor);
+  // behind the surfaces: the quad light the ray meets (its intensity,
+  // alpha 1), else the background (Raycast_impl.cpp:158-172)
+  f4 back = bgColor;
+  {
+    float tl;
+    const int li = intersectQuadLights(S, ray, 0, tl);
+    if (li >= 0) {
+      const OrLight &L = S.lights[li];
+      back = f4(f3(L.color[0], L.color[1], L.color[2]) * L.intensity, 1.f);
+    }
+  }
+  result.color = over(f4(surfaceColor, surfaceAlpha), back);
 
   // intersectVolumeBounds: closest volume box entry.
   int vInst = -1, vIdx = -1;
@@ -1438,12 +1531,15 @@ struct HitRec {
   SurfHit surface;
   VolHit volume;
   bool hit = false, volumeHit = false;
+  bool lightHit = false;  // a quad light is the nearest hit
+  int lightID = -1;
+  float lightT = FLT_MAX;
 };
 
 // intersectAll (renderer/common.h:1605-1620) with intersectSurfaces<1>
 // (:1502-1543): one random number is drawn per surface hit for stochastic
 // opacity, then the volumes are tracked with the same generator.
-HitRec intersectAll(const Scene &sc, const Ray &ray, LCG &rnd, Counters &c) {
+HitRec intersectAll(const Scene &sc, const Ray &ray, LCG &rnd, Counters &c, unsigned bounceID) {
   HitRec h;
   const OrScene &S = *sc.src;
   Ray r = ray;
@@ -1463,8 +1559,15 @@ HitRec intersectAll(const Scene &sc, const Ray &ray, LCG &rnd, Counters &c) {
   }
   h.surface = hr;
   h.volume = traceVolumes(sc, ray, rnd, c);
-  h.hit = h.surface.hit || h.volume.hit;
-  h.volumeHit = h.volume.hit && (!h.surface.hit || h.volume.t < h.surface.t);
+  h.lightID = intersectQuadLights(S, ray, bounceID, h.lightT);
+  const bool lh = h.lightID >= 0;
+  // a light hit takes precedence over surface and volume hits at equal
+  // distance, a volume over a surface only when nearer
+  h.hit = h.surface.hit || h.volume.hit || lh;
+  h.lightHit = lh && (!h.surface.hit || h.lightT <= h.surface.t) &&
+               (!h.volume.hit || h.lightT <= h.volume.t);
+  h.volumeHit = h.volume.hit && (!h.surface.hit || h.volume.t < h.surface.t) &&
+                (!lh || h.volume.t < h.lightT);
   return h;
 }
 
@@ -1495,6 +1598,27 @@ void shade(const Scene &sc, const OrRenderer &R, const OrFrame &F, LCG &rnd, con
     ss.aoCount = 0.f;
     if (!hitRec.hit) {
       ss.shadedColor = f3(0.f);
+      ss.nextType = Miss;
+      return;
+    }
+    if (hitRec.lightHit) {
+      // a quad light seen by the ray: its intensity, after a bounce weighted
+      // by the BSDF sample's MIS weight against the light's solid-angle
+      // density (the light pdf over the number of lights); the path ends
+      // (Pathtrace_impl.cpp:139-182)
+      const OrLight &L = S.lights[hitRec.lightID];
+      const QuadGeom q = quadGeom(L);
+      ss.shadedColor = f3(L.color[0], L.color[1], L.color[2]) * L.intensity;
+      ss.misWeightNEE = 1.f;
+      if (bounceID > 0) {
+        const f3 hp = ray.ori + hitRec.lightT * ray.dir;
+        const float ld = length(hp - ray.ori);
+        const f3 Ld = normalize(hp - ray.ori);
+        const float LdotNl = std::fabs(dot(-Ld, q.n));
+        const float solidAngle = (LdotNl * (q.A1 + q.A2)) / (ld * ld);
+        const float lightPDF = 1.f / solidAngle;
+        ss.shadedColor = ss.shadedColor * power_heuristic(ss.bsdf.pdf, lightPDF / float(S.numLights));
+      }
       ss.nextType = Miss;
       return;
     }
@@ -1556,11 +1680,13 @@ void shade(const Scene &sc, const OrRenderer &R, const OrFrame &F, LCG &rnd, con
       result.mvy = py - cy;
     }
     int lightID = -1;
+    bool areaSample = false;
     if (S.numLights > 0) {
       float r = rnd();
       lightID = int(r * S.numLights);
       if (lightID == S.numLights) lightID = 0;
       ss.light = sampleLight(S.lights[lightID], hitPos, rnd);
+      areaSample = S.lights[lightID].type == 3;
     }
     f3 lightDir = normalize(ss.light.dir);
     f3 lightIntensity = ss.light.intensity * safe_rcp(ss.light.dist2);
@@ -1582,8 +1708,11 @@ void shade(const Scene &sc, const OrRenderer &R, const OrFrame &F, LCG &rnd, con
       ss.shadedColor = f * lightIntensity * NdotL * safe_rcp(ss.light.pdf) * float(S.numLights);
       ss.bsdf = sampleMaterial(*mat, gn, sn, viewDir, rnd);
     }
+    // Pathtrace_impl.cpp:365-375: the light sample's MIS weight against the
+    // BSDF sample for an area light, 1 for a delta light
     ss.misWeightNEE = 0.f;
-    if (S.numLights > 0) ss.misWeightNEE = 1.f; // delta light (directional)
+    if (S.numLights > 0) ss.misWeightNEE = 1.f;
+    if (areaSample) ss.misWeightNEE = power_heuristic(ss.light.pdf / float(S.numLights), ss.bsdf.pdf);
     ss.baseColor = color;
   }
 
@@ -1689,7 +1818,7 @@ void pathtracePixel(const Ctx &cx, int x, int y, Counters &c) {
       f3 throughput(1.f), intensity(0.f);
       for (unsigned passID = 0, bounceID = 0; true; ++passID) {
         ray = clipRay(ray, R);
-        HitRec hitRec = intersectAll(sc, ray, rnd, c);
+        HitRec hitRec = intersectAll(sc, ray, rnd, c, bounceID);
         shade(sc, R, F, rnd, ray, rayType, hitRec, ss, ps, bounceID);
         if (passID == 0 && bounceID == 0) firstHit = hitRec.hit;
         ray = ss.nextRay;

@@ -57,11 +57,20 @@ class OrInstance(ctypes.Structure):
     _fields_ = [("xfm", c_float * 12), ("group", c_int32), ("userID", c_uint32)]
 
 
+def _linear32(m, v):
+    """m v in float32, each row summed left to right without contraction
+    (the order the runtime uses to move light positions and edges)."""
+    v = np.asarray(v, np.float32)
+    f = np.float32
+    return np.array([(f(m[k, 0]) * v[0] + f(m[k, 1]) * v[1]) + f(m[k, 2]) * v[2] for k in range(3)],
+                    np.float32)
+
+
 class OrLight(ctypes.Structure):
     _fields_ = [("type", c_int32), ("direction", c_float * 3), ("color", c_float * 3),
                 ("irradiance", c_float), ("angularDiameter", c_float), ("visible", c_int32),
                 ("position", c_float * 3), ("intensity", c_float), ("openingAngle", c_float),
-                ("falloffAngle", c_float)]
+                ("falloffAngle", c_float), ("edge1", c_float * 3), ("edge2", c_float * 3)]
 
 
 class OrScene(ctypes.Structure):
@@ -345,9 +354,9 @@ class Scene:
             for L in lts:
                 ol = OrLight()
                 kind = L.get("type", "directional")
-                ol.type = {"directional": 0, "point": 1, "spot": 2}[kind]
+                ol.type = {"directional": 0, "point": 1, "spot": 2, "quad": 3}[kind]
                 ol.color = farr(3, L.get("color", [1, 1, 1]))
-                ol.visible = 1
+                ol.visible = 1 if L.get("visible", True) else 0
                 if kind == "directional":
                     d = lin @ np.asarray(L["direction"], np.float64)
                     ol.direction = farr(3, d / np.linalg.norm(d))
@@ -359,7 +368,10 @@ class Scene:
                     lin32 = lin.astype(np.float32)
                     p0 = np.asarray(L.get("position", [0, 0, -1] if kind == "point" else [0, 0, 0]),
                                     np.float32)
-                    ol.position = farr(3, lin32 @ p0 + tr)
+                    ol.position = farr(3, _linear32(lin32, p0) + tr)
+                    if kind == "quad":
+                        ol.edge1 = farr(3, _linear32(lin32, L.get("edge1", [1, 0, 0])))
+                        ol.edge2 = farr(3, _linear32(lin32, L.get("edge2", [0, 1, 0])))
                     ol.intensity = float(min(max(L.get("intensity", 1.0), 0.0), 3.4e38))
                     if kind == "spot":
                         ol.direction = farr(3, lin32 @ np.asarray(L.get("direction", [0, 0, -1]),

@@ -74,17 +74,19 @@ typedef struct OrInstance {
 } OrInstance;
 
 typedef struct OrLight {
-  int32_t type;             /* 0 = directional, 1 = point, 2 = spot */
+  int32_t type;             /* 0 = directional, 1 = point, 2 = spot, 3 = quad */
   float direction[3];       /* directional: direction the light travels (ANARI
                                "direction"); spot: cone axis, world space */
   float color[3];
   float irradiance;
   float angularDiameter;
   int32_t visible;
-  float position[3];        /* point / spot, world space */
-  float intensity;          /* point / spot */
+  float position[3];        /* point / spot / quad, world space */
+  float intensity;          /* point / spot / quad */
   float openingAngle;       /* spot */
   float falloffAngle;       /* spot */
+  float edge1[3], edge2[3]; /* quad: the parallelogram position + a edge1 +
+                               b edge2, world space */
 } OrLight;
 
 typedef struct OrScene {

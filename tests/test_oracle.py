@@ -455,6 +455,116 @@ def test_instanced_lights_match_transformed_world_lights(oracle):
     assert np.allclose(images[0], images[1], atol=1e-5)
 
 
+def _quad_light(visible=False, intensity=3.0, color=(1.0, 0.9, 0.8)):
+    """A unit square light 2 above the origin, facing the z = 0 plane."""
+    return {"type": "quad", "position": [-0.5, -0.5, 2.0], "edge1": [1.0, 0.0, 0.0],
+            "edge2": [0.0, 1.0, 0.0], "intensity": intensity, "color": list(color),
+            "visible": visible}
+
+
+def _ortho_down(height=0.01):
+    return {"type": "orthographic", "position": [0.0, 0.0, 10.0], "direction": [0.0, 0.0, -1.0],
+            "up": [0.0, 1.0, 0.0], "height": height, "aspect": 1.0}
+
+
+def _lcg_zero_state_draws(n):
+    """The first n draws of the reference's LCG<4> from state 0."""
+    state, out = 0, []
+    for _ in range(n):
+        state = (1664525 * state + 1013904223) & 0xFFFFFFFF
+        out.append(np.float32(state & 0xFFFFFF) / np.float32(1 << 24))
+    return out
+
+
+def test_quad_light_raycast_closed_form(oracle):
+    """Raycast of the matte plane under an invisible quad light: the light is
+    sampled once (zero-state stream: triangle pick r, then the point
+    v1 + sqrt(u1)(1 - u2) a + sqrt(u1) u2 b of that triangle) and shades
+    as c/pi * I * cos_s * A cos_l / d^2, plus the ambient term."""
+    sc = plane_scene()
+    sc["lights"] = [_quad_light()]
+    sc["camera"] = _ortho_down(8.0)
+    S = oracle.Scene(sc)
+    F = oracle.Frame(16, 16)
+    oracle.render(S, F)
+    r, u1, u2 = (float(x) for x in _lcg_zero_state_draws(3))
+    v1, e1, e2 = np.array([-0.5, -0.5, 2.0]), np.array([1.0, 0, 0]), np.array([0, 1.0, 0])
+    a, b = (e1, e1 + e2) if 0.5 < r else (e1 + e2, e2)
+    y = v1 + math.sqrt(u1) * (1 - u2) * a + math.sqrt(u1) * u2 * b
+    xs = ((np.arange(16) + 0.5) / 16 - 0.5) * 8.0
+    X, Y = np.meshgrid(xs, xs)
+    L = y[None, None, :] - np.stack([X, Y, np.zeros_like(X)], axis=-1)
+    d2 = (L * L).sum(-1)
+    cos_s = np.maximum(0.0, L[..., 2] / np.sqrt(d2))
+    cos_l = np.abs(L[..., 2]) / np.sqrt(d2)
+    c = np.array([0.6, 0.5, 0.4])
+    I = 3.0 * np.array([1.0, 0.9, 0.8])
+    expect = (c / math.pi) * I * (cos_s * cos_l / d2)[..., None] + c * 0.2
+    assert np.allclose(F.color[..., :3], expect, rtol=2e-4, atol=1e-5)
+
+
+@pytest.mark.parametrize("renderer", ["raycast", "pathtrace"])
+def test_quad_light_seen_by_the_camera(oracle, renderer):
+    """A visible quad light in front of the camera shows its intensity with
+    alpha 1 in both renderers; an invisible one is skipped by camera rays
+    (the background shows)."""
+    sc = plane_scene(renderer=renderer)
+    sc["camera"] = {"type": "orthographic", "position": [0.0, 0.0, 1.0],
+                    "direction": [0.0, 0.0, 1.0], "up": [0.0, 1.0, 0.0], "height": 0.5,
+                    "aspect": 1.0}
+    sc["renderer"]["background"] = [0.1, 0.2, 0.3, 0.5]
+    for visible in (True, False):
+        sc["lights"] = [_quad_light(visible=visible)]
+        S = oracle.Scene(sc)
+        F = oracle.Frame(8, 8)
+        oracle.render(S, F)
+        expect = [3.0, 2.7, 2.4, 1.0] if visible else [0.1, 0.2, 0.3, 0.5]
+        assert np.allclose(F.color, np.array(expect, np.float32), atol=1e-6), visible
+
+
+def test_quad_light_pathtrace_mis_closed_form(oracle):
+    """Path-traced matte plane under an invisible quad light: next-event
+    estimation weighted by power_heuristic(pdf_light / n, pdf_bsdf) plus
+    emission of BSDF-sampled rays that hit the light weighted by
+    power_heuristic(pdf_bsdf, pdf_solid_angle / n) (Pathtrace_impl.cpp:
+    139-182, :365-375). The weights do not sum to 1, as the reference
+    writes them: the light sample's weight takes the pdf of the BSDF sample
+    drawn at the same hit (cos_r / pi of a cosine-distributed direction,
+    whose expectation over cos_r^2 ~ U(0,1) is a^2 ln(1 + 1/a^2) with
+    a = pi pdf_light), not of the light direction, and its pdf is
+    1 / (A cos_l) against the hit's d^2 / (A cos_l). The expectation is
+    c/pi * I * int cos_s cos_l / d^2 (w_nee + w_bsdf) dA, integrated here
+    by the midpoint rule."""
+    sc = plane_scene(renderer="pathtrace")
+    sc["lights"] = [_quad_light()]
+    sc["camera"] = _ortho_down()
+    sc["renderer"].update(pixelSamples=16, maxBounce=3, ambientRadiance=0.0, ambientSamples=0)
+    S = oracle.Scene(sc)
+    F = oracle.Frame(16, 16, stats=True)
+    frames = 4
+    for _ in range(frames):
+        oracle.render(S, F)
+    n = 16 * 16 * 16 * frames
+    mean = F.sum.reshape(-1, 3).sum(0) / n
+    var = F.sumsq.reshape(-1, 3).sum(0) / n - mean * mean
+    k = 400
+    g = (np.arange(k) + 0.5) / k - 0.5
+    U, V = np.meshgrid(g, g)
+    d = np.sqrt(U * U + V * V + 4.0)
+    cos_s = cos_l = 2.0 / d
+    geo = cos_s * cos_l / (d * d)
+    p_nee, p_bsdf, p_hit = 1.0 / cos_l, cos_s / math.pi, d * d / cos_l
+    a2 = (math.pi * p_nee) ** 2
+    w_nee = a2 * np.log1p(1.0 / a2)
+    w_bsdf = p_bsdf ** 2 / (p_bsdf ** 2 + p_hit ** 2)
+    c = np.array([0.6, 0.5, 0.4])
+    I = 3.0 * np.array([1.0, 0.9, 0.8])
+    expect = c / math.pi * I * float((geo * (w_nee + w_bsdf)).mean())
+    unweighted = c / math.pi * I * float(geo.mean())
+    assert np.all(np.abs(mean - expect) <= 5 * np.sqrt(var / n) + 1e-4 * expect), (mean, expect)
+    assert np.all(np.abs(mean - unweighted) > 10 * np.sqrt(var / n))  # the quirk is visible
+
+
 def test_emission_absorption_slab(oracle):
     """Constant field, TF alpha a: alpha after k steps is 1 - (1-a)^(k dt/ud)."""
     n = 16

@@ -72,6 +72,10 @@ def parse():
                         "no data, training or evaluation")
     p.add_argument("--no-batch", dest="batch", action="store_false",
                    help="skip the config-3 batched-rendering measurement")
+    p.add_argument("--batch-only", action="store_true",
+                   help="profiling aid: run only the config-3 measurement and print its record "
+                        "(no config-1 metric line); its second sequential pass is bracketed by "
+                        "cudaProfilerStart/Stop for ncu --profile-from-start off")
     return p.parse_args()
 
 
@@ -153,19 +157,24 @@ def measured_peaks_tensor():
     return 1900.0, "fallback"
 
 
-def profiled_traffic(name="pathtrace_config1.txt"):
-    """DRAM bytes per launch (per frame) from a committed ncu summary."""
+def profiled_value(name, key):
+    """A 'key = value' line's value from a committed ncu summary."""
     path = os.path.join(ROOT, "profiles", name)
     if not os.path.exists(path):
         return None
     with open(path) as f:
         for ln in f:
-            if ln.strip().startswith("traffic_bytes_per_launch"):
+            if ln.strip().startswith(key + " "):
                 try:
                     return float(ln.split("=")[1].split()[0])
                 except (IndexError, ValueError):
                     return None
     return None
+
+
+def profiled_traffic(name="pathtrace_config1.txt"):
+    """DRAM bytes per launch (per frame) from a committed ncu summary."""
+    return profiled_value(name, "traffic_bytes_per_launch")
 
 
 def profiled_metric(name, metric):
@@ -227,11 +236,13 @@ def phase_split(c):
 
 def issue_roofline(kernel_s, spp, res, sms=None):
     """The path tracer's issue roofline: thread instructions per second of
-    the 64-spp frame (warp instructions x active lanes per warp instruction
-    of the profiled 1-spp launch at the same resolution, times spp, over the
-    live kernel time) against the SMs' peak (SMs x 4 schedulers x 32 lanes x
-    the maximum SM clock): frac = issue rate x SIMT efficiency."""
+    the frame (warp instructions x active lanes per warp instruction of the
+    profiled launch at the same resolution, scaled by spp over the profiled
+    launch's spp, over the live kernel time) against the SMs' peak (SMs x 4
+    schedulers x 32 lanes x the maximum SM clock): frac = issue rate x SIMT
+    efficiency."""
     inst = profiled_metric("pathtrace_config1.txt", "smsp__inst_executed.sum")
+    pspp = profiled_value("pathtrace_config1.txt", "profiled_spp_per_launch") or 1.0
     lanes = profiled_metric("pathtrace_config1.txt",
                             "smsp__thread_inst_executed_per_inst_executed.ratio")
     active = profiled_metric("pathtrace_config1.txt",
@@ -248,13 +259,13 @@ def issue_roofline(kernel_s, spp, res, sms=None):
         with open(path) as f:
             mhz = json.load(f).get("sm_max_mhz", mhz)
     peak = sms * 4 * 32 * mhz * 1e6 / 1e9
-    achieved = inst * lanes * spp / kernel_s / 1e9
+    achieved = inst * lanes * (spp / pspp) / kernel_s / 1e9
     return {"bound": "issue", "achieved": achieved, "peak": peak, "unit": "Gthread-inst/s",
             "frac": achieved / peak,
             "issue_active_frac": active / 100 if active is not None else None,
             "active_lanes_per_warp_instruction": lanes,
-            "note": f"thread instructions of the profiled 1-spp launch ({inst:.4g} warp "
-                    f"instructions x {lanes:.2f} lanes) x {spp} spp / live kernel time, against "
+            "note": f"thread instructions of the profiled {pspp:.0f}-spp launch ({inst:.4g} warp "
+                    f"instructions x {lanes:.2f} lanes) x {spp}/{pspp:.0f} / live kernel time, against "
                     f"{sms} SMs x 4 schedulers x 32 lanes x {mhz:.0f} MHz; frac = issue-active "
                     "share x SIMT efficiency"}
 
@@ -365,7 +376,7 @@ def measure_raycast_config0(pkg, dev, flush, steps=20, gradient=False, l2=None):
             "roofline_l2": l2_roof}
 
 
-def measure_batch_config3(pkg, dev, steps=3, num_scenes=64):
+def measure_batch_config3(pkg, dev, steps=3, num_scenes=64, profile_range=False):
     """Config 3 (64 independent scenes: blob volumes of side 64..384, optional
     10k..500k-triangle sphere sets, images 256^2..1024^2, 1..64 spp, raycast
     and path tracing): the 64 frames as one batch (vsrRenderFrames, CUDA
@@ -404,7 +415,14 @@ def measure_batch_config3(pkg, dev, steps=3, num_scenes=64):
     # what caps batching: each frame's own device time in a sequential pass;
     # if a frame kind already fills the GPU at its best rate, a batch can
     # save at most the difference to that rate
+    if profile_range:
+        import torch
+
+        torch.cuda.synchronize()
+        torch.cuda.cudart().cudaProfilerStart()
     sequential()
+    if profile_range:
+        torch.cuda.cudart().cudaProfilerStop()
     per = []
     for sc, f in zip(scenes, frames):
         W, H = sc["frame"]["size"]
@@ -873,10 +891,20 @@ def run_ours(args):
     dev.close()
 
 
+def run_batch_only():
+    pkg = importlib.import_module("anari-visionaray_gb300")
+    dev = pkg.vsr.Device()
+    rec = measure_batch_config3(pkg, dev, profile_range=True)
+    print(json.dumps({"batch_config3": rec}))
+    dev.close()
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         run_reference(args)
+    elif args.batch_only:
+        run_batch_only()
     else:
         run_ours(args)
 

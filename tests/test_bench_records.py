@@ -40,11 +40,12 @@ def test_every_profile_names_its_command():
 
 def test_issue_roofline_from_profile():
     """frac = thread instructions per second / lane-issue peak; with the
-    profile's own launch time (1 spp) it equals issue-active share x active
+    profile's own launch time (scaled to 64 spp) it equals issue-active share x active
     lanes / 32 up to the elapsed-vs-active difference, so it lies in (0, 1]."""
     bench = load_bench()
     t1 = bench.profiled_metric("pathtrace_config1.txt", "gpu__time_duration.sum")
-    r = bench.issue_roofline(t1 * 1e-3 * 64, 64, 1024, sms=152)
+    pspp = bench.profiled_value("pathtrace_config1.txt", "profiled_spp_per_launch") or 1.0
+    r = bench.issue_roofline(t1 * 1e-3 * 64 / pspp, 64, 1024, sms=152)
     assert r is not None and r["bound"] == "issue" and r["unit"] == "Gthread-inst/s"
     assert 0 < r["frac"] <= 1.0
     assert abs(r["frac"] - r["achieved"] / r["peak"]) < 1e-12

@@ -969,6 +969,113 @@ struct LightSample {
   float pdf, dist, dist2;
 };
 
+// ------------------------------------------------------------ HDRI light
+// pi in double: the reference writes M_PI in these formulas
+constexpr double kPiD = 3.14159265358979323846;
+
+// upper_bound and sample_cdf of sampleCDF.h:16-55: the first bin whose CDF
+// value exceeds x and that bin's probability. Past the table's end the
+// reference reads an unset value; here the probability is 0 there.
+__device__ __forceinline__ unsigned cdfBin(const float *d, unsigned n, float x, float &pdf) {
+  unsigned first = 0;
+  int count = (int)n;
+  while (count > 0) {
+    const int step = count / 2;
+    const unsigned it = first + step;
+    if (!(x < d[it])) {
+      first = it + 1;
+      count -= step + 1;
+    } else {
+      count = step;
+    }
+  }
+  if (first == 0) pdf = d[0];
+  else if (first < n) pdf = d[first] - d[first - 1];
+  else pdf = 0.f;
+  return first;
+}
+
+// sampleCDF (sampleCDF.h:84-94): the row from the CDF of row sums, then the
+// column from that row's CDF. The light record's table named `rows` holds
+// the row sums and `lastCol` the per-row tables (scene/light/HDRI.cpp:
+// 156-157 assigns them crosswise, and sampleCDF takes them in that order),
+// so the lookup is the usual marginal-then-conditional one.
+__device__ __forceinline__ void hdriSampleCdf(const DLight &L, float rx, float ry, unsigned &x,
+                                              unsigned &y, float &pdfx, float &pdfy) {
+  const unsigned W = (unsigned)L.hdriW, H = (unsigned)L.hdriH;
+  y = cdfBin(L.hdriLastCol, H, ry, pdfy);
+  y = min(y, H - 1);
+  x = cdfBin(L.hdriRows + (size_t)y * W, W, rx, pdfx);
+}
+
+// toPolar / toUV (sampleCDF.h:57-82); the angle arithmetic runs in double
+// as the reference's M_PI constants make it, rounded to float where the
+// reference stores a float.
+__device__ __forceinline__ float3 hdriToPolar(float u, float v) {
+  const float theta = (float)(2.0f * kPiD * (double)u + -kPiD / 2.0f);
+  const float phi = (float)(kPiD * (double)v);
+  float3 n;
+  n.x = cosf(theta) * sinf(phi);
+  n.z = sinf(theta) * sinf(phi);
+  n.y = cosf(phi);
+  n.x = -n.x;
+  return n;
+}
+__device__ __forceinline__ float2 hdriToUV(float3 n) {
+  float2 uv;
+  uv.x = atan2f(n.x, n.z);
+  uv.x = (float)(((double)uv.x + kPiD / 2.0f) / (kPiD * 2.0f) + kPiD * (double)(28.670f / 360.0f));
+  uv.y = fminf(fmaxf((float)((double)acosf(n.y) / kPiD), .001f), .999f);
+  return uv;
+}
+
+__device__ __forceinline__ float3 mat3mulCM(const float *m, float3 v) {
+  return make_float3((m[0] * v.x + m[3] * v.y) + m[6] * v.z, (m[1] * v.x + m[4] * v.y) + m[7] * v.z,
+                     (m[2] * v.x + m[5] * v.y) + m[8] * v.z);
+}
+
+// tex2D over the radiance image: normalized coordinates, texel centres at
+// (i + 0.5) / n, bilinear, clamp (HDRI.cpp:129-131), filtered in software
+// as the reference's CPU device does.
+__device__ __forceinline__ float3 hdriTex(const DLight &L, float2 uv) {
+  const int W = L.hdriW, H = L.hdriH;
+  const float x = uv.x * W - 0.5f, y = uv.y * H - 0.5f;
+  const float fx0 = floorf(x), fy0 = floorf(y);
+  const float fx = x - fx0, fy = y - fy0;
+  auto cl = [](float f, int n) { return !(f >= 0.f) ? 0 : (f > (float)(n - 1) ? n - 1 : (int)f); };
+  const int x0 = cl(fx0, W), x1 = cl(fx0 + 1.f, W), y0 = cl(fy0, H), y1 = cl(fy0 + 1.f, H);
+  const float4 a = L.hdriTex[(size_t)y0 * W + x0], b = L.hdriTex[(size_t)y0 * W + x1];
+  const float4 c = L.hdriTex[(size_t)y1 * W + x0], d = L.hdriTex[(size_t)y1 * W + x1];
+  auto lerp3 = [](float4 p, float4 q, float t) {
+    return make_float3(p.x + t * (q.x - p.x), p.y + t * (q.y - p.y), p.z + t * (q.z - p.z));
+  };
+  const float3 r0 = lerp3(a, b, fx), r1 = lerp3(c, d, fx);
+  return r0 + fy * (r1 - r0);
+}
+
+// intensity(dir) = tex2D(radiance, toUV(toLocal dir)).xyz * scale
+// (DeviceCopyableObjects.h:2384-2388).
+__device__ __forceinline__ float3 hdriIntensity(const DLight &L, float3 dir) {
+  return hdriTex(L, hdriToUV(mat3mulCM(L.toLocal, dir))) * L.scale;
+}
+
+// The density the reference gives a direction that hits the HDRI light, for
+// the MIS weight of a BSDF sample (Pathtrace_impl.cpp:160-172): the CDF is
+// looked up with the direction's (u, v) as if they were random numbers,
+// and the bin probabilities are divided by 2 pi^2 sin(theta) / (W H).
+__device__ __forceinline__ float hdriHitPdf(const DLight &L, float3 rayDir) {
+  const float3 dir = mat3mulCM(L.toLocal, rayDir);
+  const float2 uv = hdriToUV(dir);
+  unsigned x, y;
+  float pdfx, pdfy;
+  hdriSampleCdf(L, uv.x, uv.y, x, y, pdfx, pdfy);
+  const float theta = acosf(fminf(fmaxf(dir.y, -1.f), 1.f));
+  const float sinTheta = sinf(theta);
+  if (sinTheta == 0.f) return 0.f;
+  return (pdfx * pdfy) * (float)((unsigned)L.hdriW * (unsigned)L.hdriH) /
+         (2.0f * kPi * kPi * sinTheta);
+}
+
 // Positional = false compiles the directional light only (the kernels
 // that run near their register budget, for worlds without point or spot
 // lights).
@@ -998,6 +1105,28 @@ __device__ __forceinline__ LightSample sampleLight(const DLight &L, float3 P, Rn
     const float cosL = fabsf(dot(s.dir, ld3(L.normal))) / s.dist;
     s.pdf = 1.f / ((L.area1 + L.area2) * cosL);
     s.intensity = ld3(L.intensity);
+    return s;
+  }
+  if (Positional && L.type == LIGHT_HDRI) {
+    // HDRI light (DeviceCopyableObjects.h:2371-2382): a texel from the
+    // CDFs, its corner's direction through toPolar into world space,
+    // pdf = pdfx pdfy W H / (4 pi), dist = FLT_MAX, dist2 = 1
+    // (renderer/common.h:1459-1461), intensity looked up along that
+    // direction. The two draws are arguments of one call, which C++ leaves
+    // unordered; GCC, which builds the reference's CPU device, evaluates
+    // them right to left, so the row's draw comes first.
+    const float ry = rnd();
+    const float rx = rnd();
+    unsigned x, y;
+    float pdfx, pdfy;
+    hdriSampleCdf(L, rx, ry, x, y, pdfx, pdfy);
+    const float invJacobian = (float)((unsigned)L.hdriW * (unsigned)L.hdriH) / (float)(4 * kPiD);
+    const float3 Lp = hdriToPolar(x / (float)L.hdriW, y / (float)L.hdriH);
+    s.dir = mat3mulCM(L.toWorld, Lp);
+    s.dist = FLT_MAX;
+    s.dist2 = 1.f;
+    s.pdf = pdfx * pdfy * invJacobian;
+    s.intensity = hdriIntensity(L, s.dir);
     return s;
   }
   if (Positional && L.type != LIGHT_DIRECTIONAL) {
@@ -1043,11 +1172,14 @@ __device__ __forceinline__ float powerHeuristic(float a, float b) {
   return a2 / (a2 + b * b);
 }
 
-// The nearest quad light the ray meets (intersectLights, renderer/common.h
-// :1566-1603, quad branch; both sides lit): intersect(Ray, Quad) tests the
-// two tessellated triangles with the triangle test and keeps the nearer hit
-// (DeviceCopyableObjects.h:2211-2237); at bounce 0 invisible lights are
-// skipped. Returns the light's index or -1, and its distance.
+// The light the ray meets (intersectLights, renderer/common.h:1566-1603):
+// a quad light by intersect(Ray, Quad), which tests the two tessellated
+// triangles and keeps the nearer hit (DeviceCopyableObjects.h:2211-2237;
+// both sides lit), taken when nearer than the hit so far; an HDRI light
+// always, at distance FLT_MAX, taken when nothing was hit yet or, against
+// another light at FLT_MAX, when it is visible and that one is not. At
+// bounce 0 invisible lights are skipped. Returns the light's index or -1,
+// and its distance.
 __device__ __forceinline__ bool quadLightTriT(float3 o, float3 d, float3 v1, float3 e1, float3 e2,
                                               float tmin, float tmax, float &t) {
   const float3 s1 = cross(d, e2);
@@ -1063,13 +1195,22 @@ __device__ __forceinline__ bool quadLightTriT(float3 o, float3 d, float3 v1, flo
   t = dot(e2, s2) * idiv;
   return t >= tmin && t <= tmax;
 }
-__device__ __forceinline__ int intersectQuadLights(const DScene &S, float3 o, float3 d, float tmin,
-                                                   float tmax, unsigned bounceID, float &tl) {
+__device__ __forceinline__ int intersectLights(const DScene &S, float3 o, float3 d, float tmin,
+                                               float tmax, unsigned bounceID, float &tl) {
   int id = -1;
+  bool vis = false;
   tl = FLT_MAX;
   for (int i = 0; i < S.numLights; ++i) {
     const DLight &L = S.lights[i];
-    if (L.type != LIGHT_QUAD || (bounceID == 0 && !L.visible)) continue;
+    if ((L.type != LIGHT_QUAD && L.type != LIGHT_HDRI) || (bounceID == 0 && !L.visible)) continue;
+    if (L.type == LIGHT_HDRI) {
+      if (id < 0 || (tl == FLT_MAX && L.visible && !vis)) {
+        tl = FLT_MAX;
+        vis = L.visible != 0;
+        id = i;
+      }
+      continue;
+    }
     const float3 v1 = ld3(L.pos), e1 = ld3(L.e1), e2 = ld3(L.e2), dd = e1 + e2;
     float t1 = FLT_MAX, t2 = FLT_MAX;
     const bool h1 = quadLightTriT(o, d, v1, e1, dd, tmin, tmax, t1);
@@ -1079,6 +1220,7 @@ __device__ __forceinline__ int intersectQuadLights(const DScene &S, float3 o, fl
     if (h2 && t2 < t) t = t2;
     if ((h1 || h2) && t < tl) {
       tl = t;
+      vis = L.visible != 0;
       id = i;
     }
   }

@@ -80,14 +80,15 @@ __device__ void raycastSample(const DScene &S, const DRenderer &R, Ray ray, cons
       }
     }
   }
-  // behind the surfaces: a quad light the ray meets (its intensity, alpha
-  // 1), else the background (Raycast_impl.cpp:158-172)
+  // behind the surfaces: a quad or HDRI light the ray meets (its intensity
+  // along the ray, alpha 1), else the background (Raycast_impl.cpp:158-172)
   float4 back = bg;
   if (Full && S.areaLights) {
     float tl;
-    const int li = intersectQuadLights(S, ray.o, ray.d, ray.tmin, ray.tmax, 0, tl);
+    const int li = intersectLights(S, ray.o, ray.d, ray.tmin, ray.tmax, 0, tl);
     if (li >= 0) {
-      const float3 I = ld3(S.lights[li].intensity);
+      const DLight &L = S.lights[li];
+      const float3 I = L.type == LIGHT_HDRI ? hdriIntensity(L, ray.d) : ld3(L.intensity);
       back = make_float4(I.x, I.y, I.z, 1.f);
     }
   }
@@ -289,7 +290,7 @@ __device__ __forceinline__ void intersectAll(const DScene &S, const Ray &ray, bo
   if (Count && S.numVolumes > 0) atomicAdd(&cnt[26], (unsigned long long)(clock64() - tc0));
   bool lh = false;
   if (Full && S.areaLights) {
-    h.lightID = intersectQuadLights(S, ray.o, ray.d, ray.tmin, ray.tmax, bounceID, h.lightT);
+    h.lightID = intersectLights(S, ray.o, ray.d, ray.tmin, ray.tmax, bounceID, h.lightT);
     lh = h.lightID >= 0;
   }
   // renderer/common.h:1605-1620: a light hit takes precedence over surface
@@ -387,19 +388,26 @@ __device__ __forceinline__ void pathtracePixel(const DScene &S, const DCamera &C
           if (!hr.hit) {
             shadedColor = f3(0.f);
           } else if (Full && hr.lightHit) {
-            // a quad light seen by the ray: its intensity, weighted after a
-            // bounce by the BSDF sample's MIS weight against the light's
-            // solid-angle density, ends the path (Pathtrace_impl.cpp:139-182)
+            // a quad or HDRI light seen by the ray: its intensity, weighted
+            // after a bounce by the BSDF sample's MIS weight against the
+            // light's density for that direction, ends the path
+            // (Pathtrace_impl.cpp:139-182)
             const DLight &L = S.lights[hr.lightID];
-            shadedColor = ld3(L.intensity);
+            const bool hdri = L.type == LIGHT_HDRI;
+            shadedColor = hdri ? hdriIntensity(L, ray.d) : ld3(L.intensity);
             misWeightNEE = 1.f;
             if (bounceID > 0) {
-              const float3 hp = ray.o + hr.lightT * ray.d;
-              const float ld = length(hp - ray.o);
-              const float3 Ld = normalize(hp - ray.o);
-              const float LdotNl = fabsf(dot(-Ld, ld3(L.normal)));
-              const float solidAngle = (LdotNl * (L.area1 + L.area2)) / (ld * ld);
-              const float lightPDF = 1.f / solidAngle;
+              float lightPDF;
+              if (hdri) {
+                lightPDF = hdriHitPdf(L, ray.d);
+              } else {
+                const float3 hp = ray.o + hr.lightT * ray.d;
+                const float ld = length(hp - ray.o);
+                const float3 Ld = normalize(hp - ray.o);
+                const float LdotNl = fabsf(dot(-Ld, ld3(L.normal)));
+                const float solidAngle = (LdotNl * (L.area1 + L.area2)) / (ld * ld);
+                lightPDF = 1.f / solidAngle;
+              }
               shadedColor = shadedColor * powerHeuristic(bsdf.pdf, lightPDF / float(S.numLights));
             }
             lightHitNow = true;
@@ -467,7 +475,8 @@ __device__ __forceinline__ void pathtracePixel(const DScene &S, const DCamera &C
               int lightID = int(rnd() * S.numLights);
               if (lightID == S.numLights) lightID = 0;
               ls = sampleLight<Full>(S.lights[lightID], hitPos, rnd);
-              areaSample = Full && S.lights[lightID].type == LIGHT_QUAD;
+              areaSample = Full && (S.lights[lightID].type == LIGHT_QUAD ||
+                                    S.lights[lightID].type == LIGHT_HDRI);
             }
             const float3 lightDir = normalize(ls.dir);
             const float3 lightIntensity = ls.intensity * safeRcp(ls.dist2);

@@ -724,6 +724,54 @@ struct Material : Object {
 // commitParameters: directional (Directional.cpp:17-28), point (Point.cpp:
 // 18-24), spot (Spot.cpp:19-47; the cone cosines are taken of the angles as
 // given).
+// Inverse of a column-major 3x3 matrix by cofactors over the determinant,
+// in double, rounded to float; false (and inv untouched) when singular.
+static bool mat3Inverse(const float *m, float *inv) {
+  double a[9];
+  for (int i = 0; i < 9; ++i) a[i] = m[i];
+  const double c00 = a[4] * a[8] - a[7] * a[5], c01 = a[7] * a[2] - a[1] * a[8],
+               c02 = a[1] * a[5] - a[4] * a[2];
+  const double det = a[0] * c00 + a[3] * c01 + a[6] * c02;
+  if (det == 0.0) return false;
+  inv[0] = (float)(c00 / det);
+  inv[1] = (float)(c01 / det);
+  inv[2] = (float)(c02 / det);
+  inv[3] = (float)((a[6] * a[5] - a[3] * a[8]) / det);
+  inv[4] = (float)((a[0] * a[8] - a[6] * a[2]) / det);
+  inv[5] = (float)((a[3] * a[2] - a[0] * a[5]) / det);
+  inv[6] = (float)((a[3] * a[7] - a[6] * a[4]) / det);
+  inv[7] = (float)((a[6] * a[1] - a[0] * a[7]) / det);
+  inv[8] = (float)((a[0] * a[4] - a[3] * a[1]) / det);
+  return true;
+}
+
+// makeCDF (scene/light/HDRI.cpp:30-68): per texel the largest of r, g, b;
+// each row's running sum, its total kept for the row-sum table, then the row
+// divided by its last entry (if that is not 0); the row sums scanned and
+// normalised the same way. Sums run left to right in float.
+static void hdriCdf(const float *rgb, int W, int H, std::vector<float> &rows,
+                    std::vector<float> &lastCol) {
+  rows.assign((size_t)W * H, 0.f);
+  lastCol.assign(H, 0.f);
+  std::vector<float> sums(H);
+  for (int y = 0; y < H; ++y) {
+    float *r = rows.data() + (size_t)y * W;
+    for (int x = 0; x < W; ++x) {
+      const float *c = rgb + 3 * ((size_t)y * W + x);
+      const float lum = std::max(std::max(c[0], c[1]), c[2]);
+      r[x] = x == 0 ? lum : r[x - 1] + lum;
+    }
+    sums[y] = r[W - 1];
+    const float back = r[W - 1];
+    if (back != 0.f)
+      for (int x = 0; x < W; ++x) r[x] /= back;
+  }
+  for (int y = 0; y < H; ++y) lastCol[y] = y == 0 ? sums[0] : lastCol[y - 1] + sums[y];
+  const float back = lastCol[H - 1];
+  if (back != 0.f)
+    for (int y = 0; y < H; ++y) lastCol[y] /= back;
+}
+
 struct Light : Object {
   int type = LIGHT_DIRECTIONAL;
   float direction[3] = {0, 0, -1}, color[3] = {1, 1, 1}, position[3] = {0, 0, 0};
@@ -731,16 +779,86 @@ struct Light : Object {
   float irradiance = 1.f, angularDiameter = 0.f, intensity = 1.f;
   float cosOuter = -1.f, cosInner = -1.f;
   int visible = 1;
+  // hdri (HDRI.cpp:99-164): radiance image, CDFs, scale, frame
+  DevBuf hdriTex, hdriRows, hdriLastCol;
+  int hdriW = 0, hdriH = 0;
+  float scale = 1.f;
+  float toWorld[9] = {1, 0, 0, 0, 1, 0, 0, 0, 1}, toLocal[9] = {1, 0, 0, 0, 1, 0, 0, 0, 1};
   using Object::Object;
+  bool commitHdri() {
+    float up[3] = {1, 0, 0}, dir[3] = {0, 0, 1};
+    getv("up", VSR_FLOAT32_VEC3, up);
+    getv("direction", VSR_FLOAT32_VEC3, dir);
+    scale = 1.f; getf("scale", scale);
+    Array *rad = geto<Array>("radiance", VSR_ARRAY2D);
+    if (!rad) {
+      warn("missing required parameter 'radiance' on 'hdri' light");
+      return false;
+    }
+    if (rad->elemType != VSR_FLOAT32_VEC3 || rad->n[0] == 0 || rad->n[1] == 0) {
+      warn("'radiance' on 'hdri' light must be a non-empty FLOAT32_VEC3 Array2D");
+      return false;
+    }
+    hdriW = (int)rad->n[0];
+    hdriH = (int)rad->n[1];
+    const float *rgb = rad->as<float>();
+    std::vector<float> rows, lastCol;
+    hdriCdf(rgb, hdriW, hdriH, rows, lastCol);
+    std::vector<float> rgba((size_t)hdriW * hdriH * 4);
+    for (size_t i = 0; i < (size_t)hdriW * hdriH; ++i) {
+      rgba[4 * i] = rgb[3 * i];
+      rgba[4 * i + 1] = rgb[3 * i + 1];
+      rgba[4 * i + 2] = rgb[3 * i + 2];
+      rgba[4 * i + 3] = 1.f;
+    }
+    if (hdriTex.upload(rgba.data(), rgba.size() * sizeof(float), dev->stream) != cudaSuccess ||
+        hdriRows.upload(rows.data(), rows.size() * sizeof(float), dev->stream) != cudaSuccess ||
+        hdriLastCol.upload(lastCol.data(), lastCol.size() * sizeof(float), dev->stream) != cudaSuccess ||
+        cudaStreamSynchronize(dev->stream) != cudaSuccess) {
+      dev->report(this, kind, VSR_SEVERITY_ERROR, VSR_ERROR_OUT_OF_MEMORY, "hdri light upload failed");
+      return false;
+    }
+    // toWorld's columns: -up, then normalize(cross(col1, direction)), then
+    // normalize(cross(col0, col1)) (HDRI.cpp:146-150), each normalised by
+    // division by its length; toLocal its inverse by cofactors
+    auto norm = [](float *v) {
+      const float l = std::sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
+      for (int k = 0; k < 3; ++k) v[k] = v[k] / l;
+    };
+    auto cross = [](const float *a, const float *b, float *o) {
+      o[0] = a[1] * b[2] - a[2] * b[1];
+      o[1] = a[2] * b[0] - a[0] * b[2];
+      o[2] = a[0] * b[1] - a[1] * b[0];
+    };
+    float c0[3], c1[3] = {up[0], up[1], up[2]}, c2[3];
+    norm(c1);
+    for (float &v : c1) v = -v;
+    cross(c1, dir, c0);
+    norm(c0);
+    cross(c0, c1, c2);
+    norm(c2);
+    for (int k = 0; k < 3; ++k) {
+      toWorld[k] = c0[k];
+      toWorld[3 + k] = c1[k];
+      toWorld[6 + k] = c2[k];
+    }
+    mat3Inverse(toWorld, toLocal);
+    return true;
+  }
   void commit() override {
     type = subtype == "point"  ? LIGHT_POINT
            : subtype == "spot" ? LIGHT_SPOT
            : subtype == "quad" ? LIGHT_QUAD
+           : subtype == "hdri" ? LIGHT_HDRI
                                : LIGHT_DIRECTIONAL;
     color[0] = color[1] = color[2] = 1.f;
     getv("color", VSR_FLOAT32_VEC3, color);
     visible = 1; geti("visible", visible);
     const float maxF = std::numeric_limits<float>::max();
+    if (type == LIGHT_HDRI) {
+      valid = commitHdri();
+      return;
+    }
     if (type == LIGHT_DIRECTIONAL) {
       direction[0] = 0; direction[1] = 0; direction[2] = -1;
       getv("direction", VSR_FLOAT32_VEC3, direction);
@@ -1468,26 +1586,12 @@ struct World : Object {
       // affineInv = inverse(top_left), transInv = -translation,
       // normalXfm = transpose(affineInv)  (scene/Instance.cpp:92-98)
       const float *m = r.xfm;
-      double a[9];
-      for (int i = 0; i < 9; ++i) a[i] = m[i];
-      double c00 = a[4] * a[8] - a[7] * a[5], c01 = a[7] * a[2] - a[1] * a[8], c02 = a[1] * a[5] - a[4] * a[2];
-      double det = a[0] * c00 + a[3] * c01 + a[6] * c02;
-      if (det == 0.0) {
+      float inv[9];
+      if (!mat3Inverse(m, inv)) {
         dev->report(this, kind, VSR_SEVERITY_WARNING, VSR_ERROR_INVALID_ARGUMENT,
                     "singular instance transform; instance skipped");
         continue;
       }
-      // inverse of column-major 3x3 via cofactors (column-major output)
-      float inv[9];
-      inv[0] = (float)(c00 / det);
-      inv[1] = (float)(c01 / det);
-      inv[2] = (float)(c02 / det);
-      inv[3] = (float)((a[6] * a[5] - a[3] * a[8]) / det);
-      inv[4] = (float)((a[0] * a[8] - a[6] * a[2]) / det);
-      inv[5] = (float)((a[3] * a[2] - a[0] * a[5]) / det);
-      inv[6] = (float)((a[3] * a[7] - a[6] * a[4]) / det);
-      inv[7] = (float)((a[6] * a[1] - a[0] * a[7]) / det);
-      inv[8] = (float)((a[0] * a[4] - a[3] * a[1]) / det);
       memcpy(di.affineInv, inv, sizeof(inv));
       for (int k = 0; k < 3; ++k) di.transInv[k] = -m[9 + k];
       for (int c = 0; c < 3; ++c)
@@ -1524,6 +1628,18 @@ struct World : Object {
           dl.cosHalfAngle = 1.f;
           dl.cosOuter = L->cosOuter;
           dl.cosInner = L->cosInner;
+          if (L->type == LIGHT_HDRI) {
+            // xfmLight leaves HDRI lights untransformed (DeviceCopyableObjects.h
+            // :2424-2426)
+            dl.hdriTex = L->hdriTex.as<float4>();
+            dl.hdriRows = L->hdriRows.as<float>();
+            dl.hdriLastCol = L->hdriLastCol.as<float>();
+            dl.hdriW = L->hdriW;
+            dl.hdriH = L->hdriH;
+            dl.scale = L->scale;
+            memcpy(dl.toWorld, L->toWorld, sizeof(dl.toWorld));
+            memcpy(dl.toLocal, L->toLocal, sizeof(dl.toLocal));
+          }
           if (L->type == LIGHT_QUAD) {
             // the quad in world space (xfmLight); the areas and normal of
             // its tessellation (DeviceCopyableObjects.h:2191-2257)
@@ -1573,7 +1689,7 @@ struct World : Object {
     scene.areaLights = 0;
     for (const DLight &l : lights) {
       scene.positionalLights += l.type != LIGHT_DIRECTIONAL;
-      scene.areaLights += l.type == LIGHT_QUAD;
+      scene.areaLights += l.type == LIGHT_QUAD || l.type == LIGHT_HDRI;
     }
     scene.numVolumes = (int)vols.size();
     scene.allOpaque = allOpaque ? 1 : 0;
@@ -2368,7 +2484,7 @@ VSRObject vsrNewMaterial(VSRDevice d, const char *s) {
   return newObj<Material>(d, VSR_MATERIAL, s, {"matte", "physicallyBased"});
 }
 VSRObject vsrNewLight(VSRDevice d, const char *s) {
-  return newObj<Light>(d, VSR_LIGHT, s, {"directional", "point", "spot", "quad"});
+  return newObj<Light>(d, VSR_LIGHT, s, {"directional", "point", "spot", "quad", "hdri"});
 }
 VSRObject vsrNewSurface(VSRDevice d) { return newObj<Surface>(d, VSR_SURFACE, "", {}); }
 VSRObject vsrNewGroup(VSRDevice d) { return newObj<Group>(d, VSR_GROUP, "", {}); }

@@ -117,7 +117,7 @@ struct DMaterial {
   float pad[3];
 };
 
-enum LightType { LIGHT_DIRECTIONAL = 0, LIGHT_POINT = 1, LIGHT_SPOT = 2, LIGHT_QUAD = 3 };
+enum LightType { LIGHT_DIRECTIONAL = 0, LIGHT_POINT = 1, LIGHT_SPOT = 2, LIGHT_QUAD = 3, LIGHT_HDRI = 4 };
 
 // One light in world space (instance transforms applied on the host).
 struct DLight {
@@ -138,6 +138,16 @@ struct DLight {
   float area1, area2;
   float normal[3];
   float pad2;
+  // hdri: the radiance image (RGBA, row-major, hdriW x hdriH), its
+  // row-wise normalised CDFs (hdriW x hdriH) and the normalised CDF of the
+  // row sums (hdriH); scale; the image frame's rotation (column-major,
+  // toWorld) and its inverse
+  const float4 *hdriTex;
+  const float *hdriRows;
+  const float *hdriLastCol;
+  int hdriW, hdriH;
+  float scale;
+  float toWorld[9], toLocal[9];
 };
 
 struct DVolume {
@@ -228,7 +238,7 @@ struct DScene {
   int numGroups;
   int numLights;
   int positionalLights;  // point, spot and quad lights among them: the kernels' full variants
-  int areaLights;        // quad lights among them (hit by rays; no wavefront mode)
+  int areaLights;        // quad and HDRI lights among them (hit by rays; no wavefront mode)
   int numAnalytic;       // spheres, cones, cylinders in all groups: the kernels' full variants
   int quadGroups;        // groups with quad geometry (triNormal set): the full variants
   int numIso;            // iso-surfaces in all groups: the full variants

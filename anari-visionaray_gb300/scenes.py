@@ -23,7 +23,8 @@ is fixed in each generator. A scene is a plain dict:
                 "angularDiameter"} | {"type": "point", "position", "color", "intensity"} |
               {"type": "spot", "position", "direction", "openingAngle", "falloffAngle",
                "color", "intensity"} | {"type": "quad", "position", "edge1", "edge2",
-               "color", "intensity", "side"}; any light may carry "visible" (bool)]
+               "color", "intensity", "side"} | {"type": "hdri", "radiance": (H, W, 3) f32,
+               "up", "direction", "scale"}; any light may carry "visible" (bool)]
   instances: [{"transform": 12 floats (column-major 3x4), "surfaces": [...],
                "volumes": [...], "lights": [...]}]   (optional)
   camera   : {"type": "perspective", "position", "direction", "up", "fovy", "aspect"}
@@ -406,7 +407,16 @@ def _lights(dev, lights, keep):
         dev.set(lt, "color", L.get("color", [1, 1, 1]), vsr.FLOAT32_VEC3)
         if "visible" in L:
             dev.set(lt, "visible", bool(L["visible"]))
-        if kind == "directional":
+        if kind == "hdri":
+            rad = dev.array2d(np.ascontiguousarray(L["radiance"], np.float32))
+            keep.append(rad)
+            dev.set(lt, "radiance", rad)
+            for k in ("up", "direction"):
+                if k in L:
+                    dev.set(lt, k, L[k], vsr.FLOAT32_VEC3)
+            if "scale" in L:
+                dev.set(lt, "scale", float(L["scale"]))
+        elif kind == "directional":
             dev.set(lt, "direction", L["direction"], vsr.FLOAT32_VEC3)
             dev.set(lt, "irradiance", float(L.get("irradiance", 1.0)))
             if "angularDiameter" in L:

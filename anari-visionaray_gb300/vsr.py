@@ -273,6 +273,10 @@ class Device:
     def array1d(self, data, dtype=None):
         return self._array(data, dtype, 1)
 
+    def array2d(self, data, dtype=None):
+        """data indexed [y, x] or [y, x, component] (x fastest in memory)."""
+        return self._array(data, dtype, 2)
+
     def array3d(self, data, dtype=None):
         """data indexed [z, y, x] (x fastest in memory)."""
         return self._array(data, dtype, 3)
@@ -289,6 +293,12 @@ class Device:
             t = dtype if dtype is not None else _ARRAY_TYPES[(a.dtype, 1)]
             h = self.lib.vsrNewArray3D(self.handle, a.ctypes.data, t, nx, ny, nz)
             return Obj(h, ARRAY3D)
+        if dims == 2:
+            ny, nx = a.shape[:2]
+            comps = 1 if a.ndim == 2 else a.shape[-1]
+            t = dtype if dtype is not None else _ARRAY_TYPES[(a.dtype, comps)]
+            h = self.lib.vsrNewArray2D(self.handle, a.ctypes.data, t, nx, ny)
+            return Obj(h, ARRAY2D)
         comps = 1 if a.ndim == 1 else a.shape[-1]
         t = dtype if dtype is not None else _ARRAY_TYPES[(a.dtype, comps)]
         h = self.lib.vsrNewArray1D(self.handle, a.ctypes.data, t, a.shape[0])

@@ -348,8 +348,16 @@ void buildMajorants(Vol &vol) {
 // ---------------------------------------------------------------------------
 // Committed scene.
 // ---------------------------------------------------------------------------
+// An HDRI light's tables (scene/light/HDRI.cpp:30-164): the row-wise
+// normalised CDFs, the normalised CDF of the row sums, the image frame.
+struct Hdri {
+  std::vector<float> rows, lastCol;
+  float toWorld[9], toLocal[9];
+};
+
 struct Scene {
   const OrScene *src;
+  std::vector<Hdri> hdri;  // per light (empty tables for other types)
   std::vector<Tri> tris;
   std::vector<Vol> isoFields;  // the iso-surfaces' fields (bounds and voxel space)
   std::vector<f3> triNormal;   // quads: the shading normal per triangle (empty if none)
@@ -1198,9 +1206,126 @@ QuadGeom quadGeom(const OrLight &L) {
   return q;
 }
 
-LightSample sampleLight(const OrLight &L, f3 P, LCG &rnd) {
+// upper_bound + sample_cdf (sampleCDF.h:16-55): the first bin whose value
+// exceeds x and its probability (0 past the end, where the reference reads
+// an unset value).
+unsigned cdfBin(const float *d, unsigned n, float x, float &pdf) {
+  unsigned first = 0;
+  int count = (int)n;
+  while (count > 0) {
+    const int step = count / 2;
+    const unsigned it = first + step;
+    if (!(x < d[it])) { first = it + 1; count -= step + 1; }
+    else count = step;
+  }
+  if (first == 0) pdf = d[0];
+  else if (first < n) pdf = d[first] - d[first - 1];
+  else pdf = 0.f;
+  return first;
+}
+
+// sampleCDF (sampleCDF.h:84-94) with the light record's tables as
+// HDRI.cpp:156-157 stores them: the row from the row sums' CDF, then the
+// column from that row's CDF.
+void hdriSampleCdf(const OrLight &L, const Hdri &h, float rx, float ry, unsigned &x, unsigned &y,
+                   float &pdfx, float &pdfy) {
+  const unsigned W = (unsigned)L.hdriW, H = (unsigned)L.hdriH;
+  y = cdfBin(h.lastCol.data(), H, ry, pdfy);
+  y = std::min(y, H - 1);
+  x = cdfBin(h.rows.data() + size_t(y) * W, W, rx, pdfx);
+}
+
+// toPolar / toUV (sampleCDF.h:57-82): M_PI makes the angle arithmetic
+// double, rounded to float where the reference stores a float.
+constexpr double kPiD = 3.14159265358979323846;
+f3 hdriToPolar(float u, float v) {
+  const float theta = (float)(2.0f * kPiD * (double)u + -kPiD / 2.0f);
+  const float phi = (float)(kPiD * (double)v);
+  f3 n;
+  n.x = std::cos(theta) * std::sin(phi);
+  n.z = std::sin(theta) * std::sin(phi);
+  n.y = std::cos(phi);
+  n.x = -n.x;
+  return n;
+}
+void hdriToUV(f3 n, float &u, float &v) {
+  u = std::atan2(n.x, n.z);
+  u = (float)(((double)u + kPiD / 2.0f) / (kPiD * 2.0f) + kPiD * (double)(28.670f / 360.0f));
+  v = std::fmin(std::fmax((float)((double)std::acos(n.y) / kPiD), .001f), .999f);
+}
+
+f3 mat3CM(const float *m, f3 v) {
+  return f3((m[0] * v.x + m[3] * v.y) + m[6] * v.z, (m[1] * v.x + m[4] * v.y) + m[7] * v.z,
+            (m[2] * v.x + m[5] * v.y) + m[8] * v.z);
+}
+
+// tex2D(radiance, uv): texel centres at (i + 0.5) / n, bilinear, clamp
+// (HDRI.cpp:129-131), as Visionaray filters on the CPU.
+f3 hdriTex(const OrLight &L, float u, float v) {
+  const int W = L.hdriW, H = L.hdriH;
+  const float x = u * W - 0.5f, y = v * H - 0.5f;
+  const float fx0 = std::floor(x), fy0 = std::floor(y);
+  const float fx = x - fx0, fy = y - fy0;
+  auto cl = [](float f, int n) { return !(f >= 0.f) ? 0 : (f > (float)(n - 1) ? n - 1 : (int)f); };
+  const int x0 = cl(fx0, W), x1 = cl(fx0 + 1.f, W), y0 = cl(fy0, H), y1 = cl(fy0 + 1.f, H);
+  auto at = [&](int i, int j) {
+    const float *c = L.radiance + 3 * (size_t(j) * W + i);
+    return f3(c[0], c[1], c[2]);
+  };
+  const f3 r0 = lerp3(at(x0, y0), at(x1, y0), fx), r1 = lerp3(at(x0, y1), at(x1, y1), fx);
+  return lerp3(r0, r1, fy);
+}
+
+// intensity(dir) = tex2D(radiance, toUV(toLocal dir)).xyz * scale
+// (DeviceCopyableObjects.h:2384-2388).
+f3 hdriIntensity(const OrLight &L, const Hdri &h, f3 dir) {
+  float u, v;
+  hdriToUV(mat3CM(h.toLocal, dir), u, v);
+  return hdriTex(L, u, v) * L.scale;
+}
+
+// The HDRI density of a direction that hit the light (Pathtrace_impl.cpp:
+// 160-172): the CDFs looked up with the direction's (u, v), the bin
+// probabilities times W H / (2 pi^2 sin theta); 0 where sin theta is 0.
+float hdriHitPdf(const OrLight &L, const Hdri &h, f3 rayDir) {
+  const f3 dir = mat3CM(h.toLocal, rayDir);
+  float u, v;
+  hdriToUV(dir, u, v);
+  unsigned x, y;
+  float pdfx, pdfy;
+  hdriSampleCdf(L, h, u, v, x, y, pdfx, pdfy);
+  const float theta = std::acos(std::fmin(std::fmax(dir.y, -1.f), 1.f));
+  const float sinTheta = std::sin(theta);
+  if (sinTheta == 0.f) return 0.f;
+  return (pdfx * pdfy) * (float)((unsigned)L.hdriW * (unsigned)L.hdriH) /
+         (2.0f * kPi * kPi * sinTheta);
+}
+
+LightSample sampleLight(const Scene &sc, int li, f3 P, LCG &rnd) {
+  const OrLight &L = sc.src->lights[li];
   LightSample s;
   s.pdf = 1.f;
+  if (L.type == 4) {
+    // HDRI (DeviceCopyableObjects.h:2371-2382, renderer/common.h:1459-1461):
+    // a texel from the CDFs, the direction of its corner through toPolar
+    // and toWorld, pdf = pdfx pdfy W H / (4 pi), dist = FLT_MAX, dist2 = 1.
+    // The two draws are arguments of one call; GCC, which builds the
+    // reference's CPU device, evaluates them right to left (the row's draw
+    // first).
+    const Hdri &h = sc.hdri[li];
+    const float ry = rnd();
+    const float rx = rnd();
+    unsigned x, y;
+    float pdfx, pdfy;
+    hdriSampleCdf(L, h, rx, ry, x, y, pdfx, pdfy);
+    const float invJacobian = (float)((unsigned)L.hdriW * (unsigned)L.hdriH) / (float)(4 * kPiD);
+    s.dir = mat3CM(h.toWorld, hdriToPolar(x / (float)L.hdriW, y / (float)L.hdriH));
+    s.dist = FLT_MAX;
+    s.dist2 = 1.f;
+    s.pdf = pdfx * pdfy * invJacobian;
+    s.intensity = hdriIntensity(L, h, s.dir);
+    return s;
+  }
   if (L.type == 3) {
     // area_light<float, dco::Quad> (Visionaray, not vendored; conventions
     // restated): sample_surface(Quad) takes the first triangle when
@@ -1265,13 +1390,15 @@ LightSample sampleLight(const OrLight &L, f3 P, LCG &rnd) {
 
 inline float safe_rcp(float f) { return f > 0.f ? 1.f / f : 0.f; }
 
-// intersectLights (renderer/common.h:1566-1603), quad branch: each quad
-// light is tested as its two triangles with the ray's [tmin, tmax]
-// (intersect(Ray, Quad), DeviceCopyableObjects.h:2211-2237, the nearer hit
-// kept); both sides are lit (Quad.cpp:48-51 fixes the side to Both); at
-// bounce 0 invisible lights are skipped; the nearest light wins, the first
-// on ties. Returns the light's index or -1 and its distance in tl.
-int intersectQuadLights(const OrScene &S, const Ray &ray, unsigned bounceID, float &tl) {
+// intersectLights (renderer/common.h:1566-1603): each quad light is tested
+// as its two triangles with the ray's [tmin, tmax] (intersect(Ray, Quad),
+// DeviceCopyableObjects.h:2211-2237, the nearer hit kept; both sides lit,
+// Quad.cpp:48-51 fixes the side to Both) and taken when nearer than the hit
+// so far (the first on ties); an HDRI light is always met at FLT_MAX and
+// taken when nothing was hit yet or, against another light at FLT_MAX,
+// when it is visible and that one is not; at bounce 0 invisible lights are
+// skipped. Returns the light's index or -1 and its distance in tl.
+int intersectLights(const OrScene &S, const Ray &ray, unsigned bounceID, float &tl) {
   auto tri = [&](f3 v1, f3 e1, f3 e2, float &t) {
     f3 s1 = cross(ray.dir, e2);
     float div = dot(s1, e1);
@@ -1287,10 +1414,18 @@ int intersectQuadLights(const OrScene &S, const Ray &ray, unsigned bounceID, flo
     return t >= ray.tmin && t <= ray.tmax;
   };
   int id = -1;
+  bool hit = false, vis = false;
   tl = FLT_MAX;
   for (int i = 0; i < S.numLights; ++i) {
     const OrLight &L = S.lights[i];
-    if (L.type != 3 || (bounceID == 0 && !L.visible)) continue;
+    if (bounceID == 0 && !L.visible) continue;
+    if (L.type == 4) {
+      if (!hit || (tl == FLT_MAX && L.visible && !vis)) {
+        hit = true; vis = L.visible != 0; tl = FLT_MAX; id = i;
+      }
+      continue;
+    }
+    if (L.type != 3) continue;
     const QuadGeom q = quadGeom(L);
     float t1 = FLT_MAX, t2 = FLT_MAX;
     const bool h1 = tri(q.v1, q.e1, q.d, t1);
@@ -1298,7 +1433,7 @@ int intersectQuadLights(const OrScene &S, const Ray &ray, unsigned bounceID, flo
     float t = FLT_MAX;
     if (h1) t = t1;
     if (h2 && t2 < t) t = t2;
-    if ((h1 || h2) && t < tl) { tl = t; id = i; }
+    if ((h1 || h2) && t < tl) { hit = true; vis = L.visible != 0; tl = t; id = i; }
   }
   return id;
 }
@@ -1388,14 +1523,15 @@ f3 gradientDelta(const Vol &vol) { return vol.S * vol.cellSize; }
 // (VolumeIntegration.h:420-460): a matte surface of the sample's colour
 // along the face-forwarded gradient, lit by every light (zero-state
 // generator, as for surfaces), plus the ambient term.
-f3 gradientShade(const OrScene &S, const OrRenderer &R, const Vol &vol, f3 P, f3 viewDir, f3 rgb) {
+f3 gradientShade(const Scene &sc, const OrRenderer &R, const Vol &vol, f3 P, f3 viewDir, f3 rgb) {
+  const OrScene &S = *sc.src;
   f3 gn = fieldGradient(vol.v, P, gradientDelta(vol));
   gn = faceforward(gn, viewDir, gn);
   f3 shaded(0.f);
   if (length(gn) > 1e-10f) {
     for (int li = 0; li < S.numLights; ++li) {
       LCG dummy;  // state 0: the reference's raycast stream is never seeded
-      LightSample ls = sampleLight(S.lights[li], P, dummy);
+      LightSample ls = sampleLight(sc, li, P, dummy);
       f3 lightDir = normalize(ls.dir);
       f3 lightIntensity = ls.intensity * safe_rcp(ls.dist2);
       const float NdotL = std::fmax(0.f, dot(gn, lightDir));
@@ -1434,7 +1570,7 @@ PixelSample raycastSample(const Scene &sc, const OrRenderer &R, Ray ray, Counter
     f3 viewDir = -ray.dir;
     for (int li = 0; li < S.numLights; ++li) {
       LCG dummy;  // state 0: the reference's raycast stream is never seeded
-      LightSample ls = sampleLight(S.lights[li], hitPos, dummy);
+      LightSample ls = sampleLight(sc, li, hitPos, dummy);
       f3 lightDir = normalize(ls.dir);
       f3 lightIntensity = ls.intensity * safe_rcp(ls.dist2);
       const float NdotL = std::fmax(0.f, dot(sn, lightDir));
@@ -1466,10 +1602,11 @@ PixelSample raycastSample(const Scene &sc, const OrRenderer &R, Ray ray, Counter
   f4 back = bgColor;
   {
     float tl;
-    const int li = intersectQuadLights(S, ray, 0, tl);
+    const int li = intersectLights(S, ray, 0, tl);
     if (li >= 0) {
       const OrLight &L = S.lights[li];
-      back = f4(f3(L.color[0], L.color[1], L.color[2]) * L.intensity, 1.f);
+      back = L.type == 4 ? f4(hdriIntensity(L, sc.hdri[li], ray.dir), 1.f)
+                         : f4(f3(L.color[0], L.color[1], L.color[2]) * L.intensity, 1.f);
     }
   }
   result.color = over(f4(surfaceColor, surfaceAlpha), back);
@@ -1513,7 +1650,7 @@ PixelSample raycastSample(const Scene &sc, const OrRenderer &R, Ray ray, Counter
       f4 s = postClassify(vol.v, v);
       float stepTransmittance = std::pow(1.f - s.w, expo);
       f3 rgb = s.xyz();
-      if (R.gradientShading) rgb = gradientShade(S, R, vol, P, -l.dir, rgb);
+      if (R.gradientShading) rgb = gradientShade(sc, R, vol, P, -l.dir, rgb);
       color += transmittance * (1.f - stepTransmittance) * rgb;
       alpha += transmittance * (1.f - stepTransmittance);
       transmittance *= stepTransmittance;
@@ -1559,7 +1696,7 @@ HitRec intersectAll(const Scene &sc, const Ray &ray, LCG &rnd, Counters &c, unsi
   }
   h.surface = hr;
   h.volume = traceVolumes(sc, ray, rnd, c);
-  h.lightID = intersectQuadLights(S, ray, bounceID, h.lightT);
+  h.lightID = intersectLights(S, ray, bounceID, h.lightT);
   const bool lh = h.lightID >= 0;
   // a light hit takes precedence over surface and volume hits at equal
   // distance, a volume over a surface only when nearer
@@ -1607,16 +1744,23 @@ void shade(const Scene &sc, const OrRenderer &R, const OrFrame &F, LCG &rnd, con
       // density (the light pdf over the number of lights); the path ends
       // (Pathtrace_impl.cpp:139-182)
       const OrLight &L = S.lights[hitRec.lightID];
-      const QuadGeom q = quadGeom(L);
-      ss.shadedColor = f3(L.color[0], L.color[1], L.color[2]) * L.intensity;
+      const bool hdri = L.type == 4;
+      ss.shadedColor = hdri ? hdriIntensity(L, sc.hdri[hitRec.lightID], ray.dir)
+                            : f3(L.color[0], L.color[1], L.color[2]) * L.intensity;
       ss.misWeightNEE = 1.f;
       if (bounceID > 0) {
-        const f3 hp = ray.ori + hitRec.lightT * ray.dir;
-        const float ld = length(hp - ray.ori);
-        const f3 Ld = normalize(hp - ray.ori);
-        const float LdotNl = std::fabs(dot(-Ld, q.n));
-        const float solidAngle = (LdotNl * (q.A1 + q.A2)) / (ld * ld);
-        const float lightPDF = 1.f / solidAngle;
+        float lightPDF;
+        if (hdri) {
+          lightPDF = hdriHitPdf(L, sc.hdri[hitRec.lightID], ray.dir);
+        } else {
+          const QuadGeom q = quadGeom(L);
+          const f3 hp = ray.ori + hitRec.lightT * ray.dir;
+          const float ld = length(hp - ray.ori);
+          const f3 Ld = normalize(hp - ray.ori);
+          const float LdotNl = std::fabs(dot(-Ld, q.n));
+          const float solidAngle = (LdotNl * (q.A1 + q.A2)) / (ld * ld);
+          lightPDF = 1.f / solidAngle;
+        }
         ss.shadedColor = ss.shadedColor * power_heuristic(ss.bsdf.pdf, lightPDF / float(S.numLights));
       }
       ss.nextType = Miss;
@@ -1685,8 +1829,8 @@ void shade(const Scene &sc, const OrRenderer &R, const OrFrame &F, LCG &rnd, con
       float r = rnd();
       lightID = int(r * S.numLights);
       if (lightID == S.numLights) lightID = 0;
-      ss.light = sampleLight(S.lights[lightID], hitPos, rnd);
-      areaSample = S.lights[lightID].type == 3;
+      ss.light = sampleLight(sc, lightID, hitPos, rnd);
+      areaSample = S.lights[lightID].type == 3 || S.lights[lightID].type == 4;
     }
     f3 lightDir = normalize(ss.light.dir);
     f3 lightIntensity = ss.light.intensity * safe_rcp(ss.light.dist2);
@@ -1938,9 +2082,67 @@ void raycastPixel(const Ctx &cx, int x, int y, Counters &c) {
   }
 }
 
+// makeCDF (HDRI.cpp:30-68): per texel max(r, g, b); each row's running
+// sum in float, the row's total kept, the row divided by its last entry
+// unless that is 0; the totals scanned and normalised the same way.
+void makeHdriCdf(const OrLight &L, Hdri &h) {
+  const int W = L.hdriW, H = L.hdriH;
+  h.rows.assign(size_t(W) * H, 0.f);
+  h.lastCol.assign(H, 0.f);
+  std::vector<float> total(H);
+  for (int y = 0; y < H; ++y) {
+    float *r = h.rows.data() + size_t(y) * W;
+    float acc = 0.f;
+    for (int x = 0; x < W; ++x) {
+      const float *c = L.radiance + 3 * (size_t(y) * W + x);
+      const float lum = std::max(std::max(c[0], c[1]), c[2]);
+      acc = x == 0 ? lum : acc + lum;
+      r[x] = acc;
+    }
+    total[y] = r[W - 1];
+    const float back = r[W - 1];
+    if (back != 0.f)
+      for (int x = 0; x < W; ++x) r[x] = r[x] / back;
+  }
+  float acc = 0.f;
+  for (int y = 0; y < H; ++y) {
+    acc = y == 0 ? total[0] : acc + total[y];
+    h.lastCol[y] = acc;
+  }
+  const float back = h.lastCol[H - 1];
+  if (back != 0.f)
+    for (int y = 0; y < H; ++y) h.lastCol[y] = h.lastCol[y] / back;
+  // toWorld's columns (HDRI.cpp:146-150): -normalize(up),
+  // normalize(cross(col1, direction)), normalize(cross(col0, col1));
+  // toLocal its inverse (cofactors over the determinant in double)
+  f3 c1 = -normalize(f3(L.up[0], L.up[1], L.up[2]));
+  f3 c0 = normalize(cross(c1, f3(L.direction[0], L.direction[1], L.direction[2])));
+  f3 c2 = normalize(cross(c0, c1));
+  const f3 cols[3] = {c0, c1, c2};
+  for (int c = 0; c < 3; ++c)
+    for (int k = 0; k < 3; ++k) h.toWorld[3 * c + k] = cols[c][k];
+  double a[9];
+  for (int i = 0; i < 9; ++i) a[i] = h.toWorld[i];
+  const double c00 = a[4] * a[8] - a[7] * a[5], c01 = a[7] * a[2] - a[1] * a[8],
+               c02 = a[1] * a[5] - a[4] * a[2];
+  const double det = a[0] * c00 + a[3] * c01 + a[6] * c02;
+  h.toLocal[0] = (float)(c00 / det);
+  h.toLocal[1] = (float)(c01 / det);
+  h.toLocal[2] = (float)(c02 / det);
+  h.toLocal[3] = (float)((a[6] * a[5] - a[3] * a[8]) / det);
+  h.toLocal[4] = (float)((a[0] * a[8] - a[6] * a[2]) / det);
+  h.toLocal[5] = (float)((a[3] * a[2] - a[0] * a[5]) / det);
+  h.toLocal[6] = (float)((a[3] * a[7] - a[6] * a[4]) / det);
+  h.toLocal[7] = (float)((a[6] * a[1] - a[0] * a[7]) / det);
+  h.toLocal[8] = (float)((a[0] * a[4] - a[3] * a[1]) / det);
+}
+
 Scene *commit(const OrScene *s) {
   auto *sc = new Scene;
   sc->src = s;
+  sc->hdri.resize(s->numLights);
+  for (int i = 0; i < s->numLights; ++i)
+    if (s->lights[i].type == 4) makeHdriCdf(s->lights[i], sc->hdri[i]);
   sc->tris.resize(s->numTriangles);
   for (int i = 0; i < s->numTriangles; ++i) {
     const float *p = s->triVerts + 9 * i;

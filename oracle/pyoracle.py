@@ -70,7 +70,9 @@ class OrLight(ctypes.Structure):
     _fields_ = [("type", c_int32), ("direction", c_float * 3), ("color", c_float * 3),
                 ("irradiance", c_float), ("angularDiameter", c_float), ("visible", c_int32),
                 ("position", c_float * 3), ("intensity", c_float), ("openingAngle", c_float),
-                ("falloffAngle", c_float), ("edge1", c_float * 3), ("edge2", c_float * 3)]
+                ("falloffAngle", c_float), ("edge1", c_float * 3), ("edge2", c_float * 3),
+                ("radiance", FP), ("hdriW", c_int32), ("hdriH", c_int32), ("scale", c_float),
+                ("up", c_float * 3)]
 
 
 class OrScene(ctypes.Structure):
@@ -354,10 +356,19 @@ class Scene:
             for L in lts:
                 ol = OrLight()
                 kind = L.get("type", "directional")
-                ol.type = {"directional": 0, "point": 1, "spot": 2, "quad": 3}[kind]
+                ol.type = {"directional": 0, "point": 1, "spot": 2, "quad": 3, "hdri": 4}[kind]
                 ol.color = farr(3, L.get("color", [1, 1, 1]))
                 ol.visible = 1 if L.get("visible", True) else 0
-                if kind == "directional":
+                if kind == "hdri":
+                    # no instance transform (xfmLight leaves HDRI lights as they are)
+                    rad = np.ascontiguousarray(L["radiance"], np.float32)
+                    self._keep.append(rad)
+                    ol.radiance = fptr(rad)
+                    ol.hdriH, ol.hdriW = int(rad.shape[0]), int(rad.shape[1])
+                    ol.scale = float(L.get("scale", 1.0))
+                    ol.up = farr(3, L.get("up", [1, 0, 0]))
+                    ol.direction = farr(3, L.get("direction", [0, 0, 1]))
+                elif kind == "directional":
                     d = lin @ np.asarray(L["direction"], np.float64)
                     ol.direction = farr(3, d / np.linalg.norm(d))
                     ol.irradiance = float(L.get("irradiance", 1.0))

@@ -74,7 +74,8 @@ typedef struct OrInstance {
 } OrInstance;
 
 typedef struct OrLight {
-  int32_t type;             /* 0 = directional, 1 = point, 2 = spot, 3 = quad */
+  int32_t type;             /* 0 = directional, 1 = point, 2 = spot, 3 = quad,
+                               4 = hdri */
   float direction[3];       /* directional: direction the light travels (ANARI
                                "direction"); spot: cone axis, world space */
   float color[3];
@@ -87,6 +88,10 @@ typedef struct OrLight {
   float falloffAngle;       /* spot */
   float edge1[3], edge2[3]; /* quad: the parallelogram position + a edge1 +
                                b edge2, world space */
+  const float *radiance;    /* hdri: hdriH rows of hdriW RGB texels */
+  int32_t hdriW, hdriH;
+  float scale;              /* hdri */
+  float up[3];              /* hdri: with 'direction', the image's frame */
 } OrLight;
 
 typedef struct OrScene {

@@ -92,7 +92,7 @@ class Denoiser {
   size_t numParams_ = 0, numWt_ = 0;
   float *params_ = nullptr, *m_ = nullptr, *v_ = nullptr, *grad_ = nullptr, *loss_ = nullptr;
   unsigned *err_ = nullptr;
-  int tensorPath_ = 1;
+  int tensorPath_ = 2;  // tcgen05 at every level width (training crops reach 16 wide)
   mutable bool stallNext_ = false;
   __nv_bfloat16 *wbf_ = nullptr, *wt_ = nullptr, *wpk_ = nullptr;
   size_t numPacked_ = 0;

@@ -243,7 +243,7 @@ __global__ void __launch_bounds__(128, VSR_WAVE_DYN_MIN_BLOCKS) kWaveTraceDyn(
     const DGroup &G = S.groups[I.group];
     const float4 a = Wv.rayO[p], b = Wv.rayD[p];
     localRay(I, xyz(a), xyz(b), o, d);
-    inv = f3(1.f / d.x, 1.f / d.y, 1.f / d.z);
+    inv = f3(slabInv(d.x), slabInv(d.y), slabInv(d.z));
     oi = f3(-o.x * inv.x, -o.y * inv.y, -o.z * inv.z);
     nodes = G.nodes;
     tris = G.tris;

@@ -322,6 +322,16 @@ __device__ __forceinline__ float analyticHitT(const DGroup &G, int leaf, uint32_
   return t == -FLT_MAX ? t : t0 + t;
 }
 
+// The slab tests below evaluate (plane - o) / d as fma(plane, 1/d, -o/d).
+// A zero direction component would make 1/d infinite and the fma
+// inf - inf = NaN, so every box would be missed by axis-parallel rays
+// (orthographic cameras looking down an axis, say); such a component is
+// replaced by +-1e-30, which keeps the interval's signs and stays finite
+// for coordinates up to 1e8.
+__device__ __forceinline__ float slabInv(float d) {
+  return 1.f / (fabsf(d) < 1e-30f ? copysignf(1e-30f, d) : d);
+}
+
 // Stack-based BVH2 traversal, near child first, in the while-while form
 // (an inner-node loop, then a leaf loop) so the lanes of a warp stay in
 // step. One loop serves closest-hit and any-hit rays (anyHit stops at the
@@ -333,7 +343,7 @@ template <bool Count, bool Analytic = false>
 __device__ __forceinline__ bool traverseGroup(const DGroup &G, float3 o, float3 d, float tmin,
                                               int inst, bool anyHit, Hit &best, uint32_t &err,
                                               unsigned long long *cnt) {
-  const float3 inv = f3(1.f / d.x, 1.f / d.y, 1.f / d.z);
+  const float3 inv = f3(slabInv(d.x), slabInv(d.y), slabInv(d.z));
   const float3 oi = f3(-o.x * inv.x, -o.y * inv.y, -o.z * inv.z);
   int stack[kTraversalStack];
   int sp = 0;
@@ -468,7 +478,7 @@ template <bool Count>
 __device__ __forceinline__ bool traverseGroup4(const DGroup &G, float3 o, float3 d, float tmin,
                                                int inst, bool anyHit, Hit &best, uint32_t &err,
                                                unsigned long long *cnt) {
-  const float3 inv = f3(1.f / d.x, 1.f / d.y, 1.f / d.z);
+  const float3 inv = f3(slabInv(d.x), slabInv(d.y), slabInv(d.z));
   const float3 oi = f3(-o.x * inv.x, -o.y * inv.y, -o.z * inv.z);
   int stack[kTraversalStack];
   int sp = 0;

@@ -178,8 +178,8 @@ class Denoiser:
     def set_tensor_path(self, path):
         """0: mma.sync convolutions; 1: tcgen05 (persistent warp-specialised
         kernel with TMA loads) where a level is at least 128 pixels wide,
-        mma.sync below; 2: that kernel at every width; 3: as 1 on the
-        one-tile-per-CTA tcgen05 kernel."""
+        mma.sync below; 2 (default): that kernel at every width; 3: as 1 on
+        the one-tile-per-CTA tcgen05 kernel."""
         rc = self.lib.vsrDenoiserSetTensorPath(self.dev.handle, self.handle, path)
         if rc:
             raise RuntimeError(f"vsrDenoiserSetTensorPath failed ({rc})")

@@ -210,9 +210,9 @@ VSR_API uint64_t vsrDenoiserParameterCount(VSRDevice d, VSRDenoiser n);
 VSR_API VSRStatus vsrDenoiserGetParameters(VSRDevice d, VSRDenoiser n, float *params,
                                            uint64_t count);
 /* Which tensor-core path the convolutions take: 0 warp-level mma.sync,
-   1 (default) tcgen05 with the accumulators in tensor memory, on a
-   persistent warp-specialised kernel with TMA loads, for levels at least
-   128 pixels wide (mma.sync below), 2 the same kernel at every width, 3 as
+   1 tcgen05 with the accumulators in tensor memory, on a persistent
+   warp-specialised kernel with TMA loads, for levels at least 128 pixels
+   wide (mma.sync below), 2 (default) the same kernel at every width, 3 as
    1 on a kernel that stages one tile per CTA with cp.async. On the
    tcgen05 path the forward reads each decoder's upsampled input and skip
    connection in place instead of writing their concatenation.

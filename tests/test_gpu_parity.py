@@ -1200,3 +1200,33 @@ def test_pathtrace_hdri_expectation(pkg, device):
                      (math.pi / 2) / k)
     expect = e_nee + rho * V * s_ * integral
     assert np.all(np.abs(mean - expect) <= 5 * sigma + 1e-4 * expect), (mean, expect, sigma)
+
+
+@pytest.mark.parametrize("renderer", ["raycast", "pathtrace"])
+def test_axis_parallel_rays(pkg, device, oracle, renderer):
+    """Rays whose direction has exact zero components (an orthographic
+    camera looking straight down -z, ray origins inside and on the x / y
+    slabs of the plane's boxes): the slab test must not turn 0 x inf or
+    inf - inf into NaN and miss every box."""
+    g = 4.0
+    quad = np.array([[-g, -g, 0], [g, -g, 0], [g, g, 0], [-g, g, 0]], np.float32)
+    sc = {
+        "surfaces": [{"vertices": quad, "indices": np.array([[0, 1, 2], [0, 2, 3]], np.uint32),
+                      "material": {"type": "matte", "color": [0.6, 0.5, 0.4]}}],
+        "volumes": [],
+        "lights": [{"direction": [0.0, 0.0, -1.0], "irradiance": 2.0}],
+        "camera": {"type": "orthographic", "position": [0.0, 0.0, 10.0],
+                   "direction": [0.0, 0.0, -1.0], "up": [0.0, 1.0, 0.0], "height": 10.0,
+                   "aspect": 1.0},
+        "renderer": {"type": renderer, "pixelSamples": 1, "ambientRadiance": 0.2,
+                     "background": [0.1, 0.2, 0.3, 1.0]},
+        "frame": {"size": (20, 20)},
+    }
+    gpu = render_gpu(pkg, device, sc)
+    _, F = render_oracle(oracle, sc)
+    hit = F.depth < 1e30
+    assert 0.5 < float(hit.mean()) < 0.9  # the plane covers the middle of the view
+    assert np.array_equal(gpu["depth"] < 1e30, hit)
+    assert np.allclose(gpu["depth"][hit], 10.0, rtol=1e-5)
+    d = np.abs(gpu["color"] - F.color).max(axis=-1)
+    assert float((d <= 1e-3).mean()) >= 0.99, float((d <= 1e-3).mean())

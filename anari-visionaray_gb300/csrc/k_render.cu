@@ -79,14 +79,14 @@ cudaError_t launchRaycast(const DScene &S, const DCamera &C, const DRenderer &R,
   // the full variant for gradient shading, and for point / spot lights,
   // spheres, cones, cylinders, quads or iso-surfaces on surfaces (volume-only worlds light nothing without gradient
   // shading)
-  if (R.gradientShading || S.areaLights ||
+  if (R.gradientShading || S.areaLights || S.attributes ||
       (S.hasSurfaces && (S.positionalLights || S.numAnalytic || S.quadGroups || S.numIso))) {
     if (count) launch(kRaycast<true, true, true>);
     else launch(kRaycast<false, true, true>);
   } else if (S.hasSurfaces) {
     if (count) launch(kRaycast<true, true, false>);
     else launch(kRaycast<false, true, false>);
-  } else if (R.pixelSamples == 1 && scratch && !S.areaLights) {
+  } else if (R.pixelSamples == 1 && scratch && !S.areaLights && !S.attributes) {
     // volume-only world: set-up, segments, combination (k_volume_march.cu)
     return launchVolumeMarch(S, C, R, F, stageTFSize, count, *scratch, stream);
   } else {
@@ -107,7 +107,7 @@ cudaError_t launchPathtrace(const DScene &S, const DCamera &C, const DRenderer &
   // times shorter (a shorter tail when the last blocks finish)
   grid.z = (unsigned)chunks;
   const bool full = S.positionalLights || S.numAnalytic || S.quadGroups || S.numIso ||
-                    (S.numVolumes > 0 && R.gradientShading) || R.taa;
+                    (S.numVolumes > 0 && R.gradientShading) || R.taa || S.attributes;
   if (R.taa && (!F.taaCurr || !F.taaPrev || !F.motionVec || chunks > 1))
     return cudaErrorInvalidValue;
   auto launch = [&](auto kernel) { kernel<<<grid, block, 0, stream>>>(S, C, R, F); };

@@ -761,6 +761,218 @@ __device__ __forceinline__ float3 hitNormal(const DGroup &G, const DInstance &I,
   return normalize(cross(f3(e1.x, e1.y, e1.z), f3(e2.x, e2.y, e2.z)));
 }
 
+// -------------------------------------------------- attributes, samplers
+// toRGBA (common.h:265-360): the components an element has, the rest of
+// (0, 0, 0, 1); unorm components as value / (2^bits - 1). An index past
+// the array reads the default.
+__device__ __forceinline__ float4 attrFetch(const DAttr &a, uint32_t i) {
+  float c[4] = {0.f, 0.f, 0.f, 1.f};
+  if (i < a.len) {
+    const int n = a.comps;
+    if (a.fixedBits == 8) {
+      const uint8_t *p = (const uint8_t *)a.data + (size_t)i * n;
+      for (int k = 0; k < n; ++k) c[k] = p[k] / 255.f;
+    } else if (a.fixedBits == 16) {
+      const uint16_t *p = (const uint16_t *)a.data + (size_t)i * n;
+      for (int k = 0; k < n; ++k) c[k] = p[k] / 65535.f;
+    } else {
+      const float *p = (const float *)a.data + (size_t)i * n;
+      for (int k = 0; k < n; ++k) c[k] = p[k];
+    }
+  }
+  return make_float4(c[0], c[1], c[2], c[3]);
+}
+
+// lerp_r(a, b, c, u, v) over a triangle's corners: (1 - u - v) a + u b + v c
+__device__ __forceinline__ float4 baryLerp(float4 a, float4 b, float4 c, float u, float v) {
+  const float w = 1.f - u - v;
+  return make_float4(w * a.x + u * b.x + v * c.x, w * a.y + u * b.y + v * c.y,
+                     w * a.z + u * b.z + v * c.z, w * a.w + u * b.w + v * c.w);
+}
+
+// What getAttributes (renderer/common.h:523-543) sees of a surface hit.
+struct AttrCtx {
+  const DSurfAttr *sa;
+  const DInstAttr *ia;
+  uint32_t primID;
+  float u, v;
+  float3 worldPos, worldNormal, objectPos, objectNormal;
+};
+
+// getAttribute (renderer/common.h:365-521) for triangles: face-varying
+// values, else per-vertex values, else the primitive's, interpolated with
+// the hit's barycentrics; then the geometry's uniform value, then the
+// instance's; else (0, 0, 0, 1). Hit attributes are (value, 1).
+static __device__ __noinline__ float4 getAttr(const AttrCtx &c, int id) {
+  if (id >= ATTR_WORLD_POS && id <= ATTR_OBJECT_NORMAL) {
+    const float3 h = id == ATTR_WORLD_POS      ? c.worldPos
+                     : id == ATTR_WORLD_NORMAL ? c.worldNormal
+                     : id == ATTR_OBJECT_POS   ? c.objectPos
+                                               : c.objectNormal;
+    return make_float4(h.x, h.y, h.z, 1.f);
+  }
+  if (id < 0 || id > ATTR_COLOR || !c.sa) return make_float4(0.f, 0.f, 0.f, 1.f);
+  const DSurfAttr &s = *c.sa;
+  if (s.isTriangle) {
+    const uint32_t p = c.primID;
+    if (s.faceVarying[id].comps) {
+      return baryLerp(attrFetch(s.faceVarying[id], 3 * p), attrFetch(s.faceVarying[id], 3 * p + 1),
+                      attrFetch(s.faceVarying[id], 3 * p + 2), c.u, c.v);
+    }
+    if (s.vertex[id].comps) {
+      uint32_t i0 = 3 * p, i1 = 3 * p + 1, i2 = 3 * p + 2;
+      if (s.index) { i0 = s.index[i0]; i1 = s.index[i1]; i2 = s.index[i2]; }
+      return baryLerp(attrFetch(s.vertex[id], i0), attrFetch(s.vertex[id], i1),
+                      attrFetch(s.vertex[id], i2), c.u, c.v);
+    }
+    if (s.primitive[id].comps) return attrFetch(s.primitive[id], p);
+  }
+  if (s.uniformMask & (1u << id))
+    return make_float4(s.uniform[id][0], s.uniform[id][1], s.uniform[id][2], s.uniform[id][3]);
+  if (c.ia && (c.ia->mask & (1u << id)))
+    return make_float4(c.ia->v[id][0], c.ia->v[id][1], c.ia->v[id][2], c.ia->v[id][3]);
+  return make_float4(0.f, 0.f, 0.f, 1.f);
+}
+
+// Shading normal of a triangle hit in object space (getNormals, renderer/
+// common.h:241-264): the vertex normals interpolated and normalised (with
+// face-varying normals set, the reference reads the vertex normals at the
+// face-varying positions 3 primID + k), else the geometric normal.
+__device__ __forceinline__ float3 shadingNormal(const DSurfAttr &s, uint32_t p, float u, float v,
+                                                float3 Ng) {
+  if (!s.isTriangle || !s.vertexNormal) return Ng;
+  uint32_t i0 = 3 * p, i1 = 3 * p + 1, i2 = 3 * p + 2;
+  if (!s.fvNormal && s.index) { i0 = s.index[i0]; i1 = s.index[i1]; i2 = s.index[i2]; }
+  if (i0 >= s.numVertexNormals || i1 >= s.numVertexNormals || i2 >= s.numVertexNormals) return Ng;
+  const float *N = s.vertexNormal;
+  const float4 a = make_float4(N[3 * i0], N[3 * i0 + 1], N[3 * i0 + 2], 0.f);
+  const float4 b = make_float4(N[3 * i1], N[3 * i1 + 1], N[3 * i1 + 2], 0.f);
+  const float4 c = make_float4(N[3 * i2], N[3 * i2 + 1], N[3 * i2 + 2], 0.f);
+  const float4 n = baryLerp(a, b, c, u, v);
+  return normalize(f3(n.x, n.y, n.z));
+}
+
+// mat4 (column-major) times a vector, columns summed in order.
+__device__ __forceinline__ float4 mat4mul(const float *m, float4 v) {
+  return make_float4(((m[0] * v.x + m[4] * v.y) + m[8] * v.z) + m[12] * v.w,
+                     ((m[1] * v.x + m[5] * v.y) + m[9] * v.z) + m[13] * v.w,
+                     ((m[2] * v.x + m[6] * v.y) + m[10] * v.z) + m[14] * v.w,
+                     ((m[3] * v.x + m[7] * v.y) + m[11] * v.z) + m[15] * v.w);
+}
+
+// A texel index under the sampler's address mode: clampToEdge, repeat or
+// mirrorRepeat (toAddressMode, sampler/Sampler.cpp).
+__device__ __forceinline__ int wrapIndex(float fi, int n, int mode) {
+  const int i = !(fi > -1e9f && fi < 1e9f) ? 0 : (int)fi;
+  if (mode == WRAP_REPEAT) return ((i % n) + n) % n;
+  if (mode == WRAP_MIRROR) {
+    const int m = ((i % (2 * n)) + 2 * n) % (2 * n);
+    return m < n ? m : 2 * n - 1 - m;
+  }
+  return i < 0 ? 0 : (i > n - 1 ? n - 1 : i);
+}
+
+__device__ __forceinline__ float4 texel(const DSampler &s, int i, int j, int k) {
+  const uchar4 t = s.texels[((size_t)k * s.dims[1] + j) * s.dims[0] + i];
+  return make_float4(t.x / 255.f, t.y / 255.f, t.z / 255.f, t.w / 255.f);
+}
+
+// tex1D / tex2D / tex3D over the RGBA8 image: normalized coordinates,
+// texel centres at (i + 0.5) / n; linear: the lattice neighbours weighted
+// along x, then y, then z; nearest: the texel containing the point.
+static __device__ __noinline__ float4 imageSample(const DSampler &s, float4 tc) {
+  const int axes = s.type == SAMP_IMAGE1D ? 1 : (s.type == SAMP_IMAGE2D ? 2 : 3);
+  const float c[3] = {tc.x, tc.y, tc.z};
+  int i0[3] = {0, 0, 0}, i1[3] = {0, 0, 0};
+  float f[3] = {0.f, 0.f, 0.f};
+  for (int a = 0; a < axes; ++a) {
+    const int n = s.dims[a];
+    if (s.linear) {
+      const float x = c[a] * n - 0.5f;
+      const float fl = floorf(x);
+      f[a] = x - fl;
+      i0[a] = wrapIndex(fl, n, s.wrap[a]);
+      i1[a] = wrapIndex(fl + 1.f, n, s.wrap[a]);
+    } else {
+      i0[a] = i1[a] = wrapIndex(floorf(c[a] * n), n, s.wrap[a]);
+    }
+  }
+  auto lerp4 = [](float4 p, float4 q, float t) {
+    return make_float4(p.x + t * (q.x - p.x), p.y + t * (q.y - p.y), p.z + t * (q.z - p.z),
+                       p.w + t * (q.w - p.w));
+  };
+  const float4 c00 = lerp4(texel(s, i0[0], i0[1], i0[2]), texel(s, i1[0], i0[1], i0[2]), f[0]);
+  if (axes == 1) return c00;
+  const float4 c10 = lerp4(texel(s, i0[0], i1[1], i0[2]), texel(s, i1[0], i1[1], i0[2]), f[0]);
+  const float4 c0 = lerp4(c00, c10, f[1]);
+  if (axes == 2) return c0;
+  const float4 c01 = lerp4(texel(s, i0[0], i0[1], i1[2]), texel(s, i1[0], i0[1], i1[2]), f[0]);
+  const float4 c11 = lerp4(texel(s, i0[0], i1[1], i1[2]), texel(s, i1[0], i1[1], i1[2]), f[0]);
+  return lerp4(c0, lerp4(c01, c11, f[1]), f[2]);
+}
+
+// getSample (renderer/common.h:546-590): primitive samplers read element
+// primID + offset; transform samplers map the input attribute; image
+// samplers transform the input attribute (inTransform, inOffset), look the
+// image up and transform the texel (outTransform, outOffset).
+__device__ __forceinline__ float4 getSample(const DSampler &s, const AttrCtx &c) {
+  if (s.type == SAMP_PRIMITIVE) return attrFetch(s.prim, c.primID + s.primOffset);
+  float4 a = getAttr(c, s.inAttribute);
+  if (s.type == SAMP_TRANSFORM) {
+    const float4 r = mat4mul(s.outXfm, a);
+    return make_float4(r.x + s.outOffset[0], r.y + s.outOffset[1], r.z + s.outOffset[2],
+                       r.w + s.outOffset[3]);
+  }
+  a = mat4mul(s.inXfm, a);
+  a = make_float4(a.x + s.inOffset[0], a.y + s.inOffset[1], a.z + s.inOffset[2], a.w + s.inOffset[3]);
+  const float4 r = mat4mul(s.outXfm, imageSample(s, a));
+  return make_float4(r.x + s.outOffset[0], r.y + s.outOffset[1], r.z + s.outOffset[2],
+                     r.w + s.outOffset[3]);
+}
+
+__device__ __forceinline__ float4 materialParam(const DScene &S, int src, float4 value,
+                                                const AttrCtx &c) {
+  if (src == SRC_VALUE) return value;
+  if (src >= SRC_SAMPLER) return getSample(S.samplers[src - SRC_SAMPLER], c);
+  return getAttr(c, src);
+}
+
+// The material at a hit with its parameters looked up (getColor, getF,
+// getOpacity; renderer/common.h:642-710): base colour from the colour
+// parameter, opacity = colour.w x the opacity parameter, metallic and
+// roughness from theirs (the .x of a sample or attribute).
+static __device__ __noinline__ DMaterial resolveMaterial(const DScene &S, const DMaterial &m,
+                                                  const AttrCtx &c) {
+  DMaterial r = m;
+  const float4 col = materialParam(S, m.src[MSRC_COLOR],
+                                   make_float4(m.baseColor[0], m.baseColor[1], m.baseColor[2], 1.f), c);
+  r.baseColor[0] = col.x;
+  r.baseColor[1] = col.y;
+  r.baseColor[2] = col.z;
+  r.opacity = col.w * materialParam(S, m.src[MSRC_OPACITY], make_float4(m.opacity, 0.f, 0.f, 1.f), c).x;
+  if (m.type == MAT_PBR) {
+    r.metallic = materialParam(S, m.src[MSRC_METALLIC], make_float4(m.metallic, 0.f, 0.f, 1.f), c).x;
+    r.roughness =
+        materialParam(S, m.src[MSRC_ROUGHNESS], make_float4(m.roughness, 0.f, 0.f, 1.f), c).x;
+  }
+  return r;
+}
+
+// The attribute context of a surface hit: the surface's attribute record,
+// the instance's, the primitive (triangles: its index in the geometry) and
+// barycentrics; hit attributes as the caller fills them.
+__device__ __forceinline__ AttrCtx hitAttrCtx(const DScene &S, const DGroup &G, const Hit &h,
+                                              uint32_t surf) {
+  AttrCtx c;
+  c.sa = S.surfAttr ? S.surfAttr + surf : nullptr;
+  c.ia = S.instAttr ? S.instAttr + h.inst : nullptr;
+  c.primID = h.tri < G.numTris ? __ldg(G.triPrim + h.tri) : 0u;
+  c.u = h.u;
+  c.v = h.v;
+  c.worldPos = c.worldNormal = c.objectPos = c.objectNormal = f3(0.f);
+  return c;
+}
+
 // --------------------------------------------------------------- materials
 // renderer/common.h:793-1415 with constant parameters and no tangent frame.
 __device__ __forceinline__ float pow5(float f) { return f * f * f * f * f; }

@@ -40,13 +40,35 @@ __device__ void raycastSample(const DScene &S, const DRenderer &R, Ray ray, cons
       }
       const DInstance &I = S.instances[hr.inst];
       const DGroup &G = S.groups[I.group];
-      const DMaterial &mat = S.materials[hitSurface<Full>(G, hr)];
+      const uint32_t sid = hitSurface<Full>(G, hr);
+      const DMaterial *matP = &S.materials[sid];
       const float3 hitPos = ray.o + hr.t * ray.d;
       // getNormals (renderer/common.h:241-275)
       float3 gn = hitNormal<Full>(G, I, hr, ray.o, ray.d);
       float3 sn = gn;
-      gn = normalize(mat3mul(I.normalXfm, gn));
-      sn = normalize(mat3mul(I.normalXfm, sn));
+      DMaterial matR;
+      if (Full && S.attributes) {
+        // shading normal and attributes (Raycast_impl.cpp:45-60): the
+        // "worldNormal" attribute is the object-space normal and the
+        // "objectNormal" one the transformed normal, as the reference
+        // passes them
+        AttrCtx ac = hitAttrCtx(S, G, hr, sid);
+        if (ac.sa) sn = shadingNormal(*ac.sa, ac.primID, hr.u, hr.v, gn);
+        float3 lo, ld;
+        localRay(I, ray.o, ray.d, lo, ld);
+        ac.worldPos = hitPos;
+        ac.worldNormal = gn;
+        ac.objectPos = lo + hr.t * ld;
+        gn = normalize(mat3mul(I.normalXfm, gn));
+        sn = normalize(mat3mul(I.normalXfm, sn));
+        ac.objectNormal = gn;
+        matR = resolveMaterial(S, *matP, ac);
+        matP = &matR;
+      } else {
+        gn = normalize(mat3mul(I.normalXfm, gn));
+        sn = normalize(mat3mul(I.normalXfm, sn));
+      }
+      const DMaterial &mat = *matP;
       const float3 color = materialColor(mat);
       float3 shaded = f3(0.f);
       const float3 viewDir = -ray.d;
@@ -245,7 +267,13 @@ __device__ __forceinline__ void intersectAll(const DScene &S, const Ray &ray, bo
     int guard = 1 << 16;
     while (hit) {
       const DGroup &G = S.groups[S.instances[h.surf.inst].group];
-      const float opacity = materialOpacity(S.materials[hitSurface<Full>(G, h.surf)]);
+      const uint32_t sid = hitSurface<Full>(G, h.surf);
+      // intersectSurfaces<EvalOpacity> (renderer/common.h:1502-1543): the
+      // attributes at the hit, hit attributes zero
+      const float opacity =
+          Full && S.attributes
+              ? materialOpacity(resolveMaterial(S, S.materials[sid], hitAttrCtx(S, G, h.surf, sid)))
+              : materialOpacity(S.materials[sid]);
       const float u = rnd();
       if (u > opacity && --guard > 0) {
         const float3 hp = r.o + h.surf.t * r.d;
@@ -416,6 +444,7 @@ __device__ __forceinline__ void pathtracePixel(const DScene &S, const DCamera &C
             float3 hitPos, gn, color;
             float eps;
             const DMaterial *mat = nullptr;
+            DMaterial matR;
             if (hr.volumeHit) {
               const DInstance &I = S.instances[hr.volInst];
               hitPos = ray.o + hr.volT * ray.d;
@@ -445,12 +474,32 @@ __device__ __forceinline__ void pathtracePixel(const DScene &S, const DCamera &C
               const DGroup &G = S.groups[I.group];
               hitPos = ray.o + hr.surf.t * ray.d;
               eps = epsilonFrom(hitPos, ray.d, hr.surf.t);
-              mat = &S.materials[hitSurface<Full>(G, hr.surf)];
+              const uint32_t sid = hitSurface<Full>(G, hr.surf);
+              mat = &S.materials[sid];
               gn = hitNormal<Full>(G, I, hr.surf, ray.o, ray.d);
-              sn = normalize(mat3mul(I.normalXfm, gn));
-              gn = sn;
-              sn = faceforward(sn, viewDir, gn);
-              gn = faceforward(gn, viewDir, gn);
+              if (Full && S.attributes) {
+                // shading normal, attributes and the material's looked-up
+                // parameters (Pathtrace_impl.cpp:240-270)
+                AttrCtx ac = hitAttrCtx(S, G, hr.surf, sid);
+                sn = ac.sa ? shadingNormal(*ac.sa, ac.primID, hr.surf.u, hr.surf.v, gn) : gn;
+                float3 lo, ld;
+                localRay(I, ray.o, ray.d, lo, ld);
+                ac.worldPos = hitPos;
+                ac.worldNormal = gn;
+                ac.objectPos = lo + hr.surf.t * ld;
+                gn = normalize(mat3mul(I.normalXfm, gn));
+                sn = normalize(mat3mul(I.normalXfm, sn));
+                sn = faceforward(sn, viewDir, gn);
+                gn = faceforward(gn, viewDir, gn);
+                ac.objectNormal = gn;
+                matR = resolveMaterial(S, *mat, ac);
+                mat = &matR;
+              } else {
+                sn = normalize(mat3mul(I.normalXfm, gn));
+                gn = sn;
+                sn = faceforward(sn, viewDir, gn);
+                gn = faceforward(gn, viewDir, gn);
+              }
               color = materialColor(*mat);
             }
             if (bounceID == 0) {

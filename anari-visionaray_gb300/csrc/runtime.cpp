@@ -94,6 +94,8 @@ static size_t typeSize(VSRDataType t) {
   switch (t) {
   case VSR_BOOL: case VSR_INT32: case VSR_UINT32: case VSR_FLOAT32: case VSR_DATA_TYPE: return 4;
   case VSR_UFIXED8: return 1;
+  case VSR_UFIXED8_VEC2: return 2;
+  case VSR_UFIXED8_VEC3: return 3;
   case VSR_UFIXED16: return 2;
   case VSR_INT32_VEC2: case VSR_UINT32_VEC2: case VSR_FLOAT32_VEC2: case VSR_FLOAT32_BOX1: return 8;
   case VSR_UINT32_VEC3: case VSR_FLOAT32_VEC3: return 12;
@@ -107,7 +109,9 @@ static size_t typeSize(VSRDataType t) {
   }
 }
 
-static bool isObjectType(VSRDataType t) { return t >= VSR_OBJECT && t <= VSR_WORLD; }
+static bool isObjectType(VSRDataType t) {
+  return (t >= VSR_OBJECT && t <= VSR_WORLD) || t == VSR_SAMPLER;
+}
 
 // ------------------------------------------------------------------ objects
 struct Param {
@@ -439,6 +443,169 @@ struct Volume : Object {
 };
 
 // triangle geometry, scene/surface/geometry/Triangle.cpp:46-133
+// ------------------------------------------------------ attributes
+// toAttribute (scene/surface/common.h:13-37); -1 for "none" or unknown.
+static int attributeId(const std::string &n) {
+  static const char *names[] = {"attribute0", "attribute1", "attribute2", "attribute3", "color",
+                                "worldPosition", "worldNormal", "objectPosition", "objectNormal"};
+  for (int i = 0; i < 9; ++i)
+    if (n == names[i]) return i;
+  return -1;
+}
+static const char *kAttrNames[5] = {"attribute0", "attribute1", "attribute2", "attribute3",
+                                    "color"};
+
+// An attribute array's layout: components and element encoding, from its
+// ANARI type (getInfo, common.h:110-262); false for unsupported types.
+static bool attrLayout(VSRDataType t, uint16_t &comps, uint16_t &bits) {
+  switch (t) {
+  case VSR_FLOAT32: comps = 1; bits = 0; return true;
+  case VSR_FLOAT32_VEC2: comps = 2; bits = 0; return true;
+  case VSR_FLOAT32_VEC3: comps = 3; bits = 0; return true;
+  case VSR_FLOAT32_VEC4: comps = 4; bits = 0; return true;
+  case VSR_UFIXED8: comps = 1; bits = 8; return true;
+  case VSR_UFIXED8_VEC2: comps = 2; bits = 8; return true;
+  case VSR_UFIXED8_VEC3: comps = 3; bits = 8; return true;
+  case VSR_UFIXED8_VEC4: comps = 4; bits = 8; return true;
+  case VSR_UFIXED16: comps = 1; bits = 16; return true;
+  default: return false;
+  }
+}
+
+// A device copy of an attribute array and its record.
+struct AttrBuf {
+  DevBuf buf;
+  DAttr rec{};
+  bool load(Array *a, cudaStream_t s) {
+    rec = DAttr{};
+    if (!a) return true;
+    uint16_t comps, bits;
+    if (!attrLayout(a->elemType, comps, bits)) return false;
+    if (buf.upload(a->data.data(), a->data.size(), s) != cudaSuccess) return false;
+    rec.data = buf.p;
+    rec.len = (uint32_t)a->size();
+    rec.comps = comps;
+    rec.fixedBits = bits;
+    return true;
+  }
+};
+
+// A uniform attribute value (FLOAT32 .. FLOAT32_VEC4), the rest of
+// (0, 0, 0, 1).
+static bool uniformAttr(const Object *o, const char *name, float *v4) {
+  const Param *p = o->find(name);
+  if (!p) return false;
+  float v[4] = {0, 0, 0, 1};
+  const int n = p->type == VSR_FLOAT32 ? 1 : p->type == VSR_FLOAT32_VEC2 ? 2
+              : p->type == VSR_FLOAT32_VEC3 ? 3 : p->type == VSR_FLOAT32_VEC4 ? 4 : 0;
+  if (!n) return false;
+  memcpy(v, p->data.data(), 4 * n);
+  memcpy(v4, v, sizeof(v));
+  return true;
+}
+
+// Samplers (scene/surface/material/sampler/*.cpp).
+struct Sampler : Object {
+  DSampler rec{};
+  DevBuf texels;
+  AttrBuf prim;
+  using Object::Object;
+  static int wrapMode(const std::string &m) {
+    return m == "repeat" ? WRAP_REPEAT : (m == "mirrorRepeat" ? WRAP_MIRROR : WRAP_CLAMP);
+  }
+  // imageSamplerUpdateData (sampler/common.h:27-60): every format as RGBA8,
+  // missing channels 0 and alpha 1; floats clamped to [0, 1] and scaled by
+  // 255 with truncation (the conversion frame/common.h:31-48 uses); sRGB
+  // texels decoded to linear.
+  bool loadImage(Array *img, int dims) {
+    const size_t n = img->size();
+    std::vector<uint8_t> rgba(4 * n);
+    auto cv = [](float f) { return (uint8_t)(255.f * std::min(std::max(f, 0.f), 1.f)); };
+    const VSRDataType t = img->elemType;
+    for (size_t i = 0; i < n; ++i) {
+      uint8_t *o = &rgba[4 * i];
+      o[0] = o[1] = o[2] = 0;
+      o[3] = 255;
+      if (t == VSR_FLOAT32 || t == VSR_FLOAT32_VEC2 || t == VSR_FLOAT32_VEC3 ||
+          t == VSR_FLOAT32_VEC4) {
+        const int c = t == VSR_FLOAT32 ? 1 : t == VSR_FLOAT32_VEC2 ? 2 : t == VSR_FLOAT32_VEC3 ? 3 : 4;
+        const float *p = img->as<float>() + c * i;
+        for (int k = 0; k < c; ++k) o[k] = cv(p[k]);
+      } else if (t == VSR_UFIXED8 || t == VSR_UFIXED8_VEC2 || t == VSR_UFIXED8_VEC3 ||
+                 t == VSR_UFIXED8_VEC4) {
+        const int c = t == VSR_UFIXED8 ? 1 : t == VSR_UFIXED8_VEC2 ? 2 : t == VSR_UFIXED8_VEC3 ? 3 : 4;
+        const uint8_t *p = img->as<uint8_t>() + c * i;
+        for (int k = 0; k < c; ++k) o[k] = p[k];
+      } else if (t == VSR_UFIXED8_RGBA_SRGB) {
+        const uint8_t *p = img->as<uint8_t>() + 4 * i;
+        for (int k = 0; k < 3; ++k) {
+          const float c = p[k] / 255.f;
+          const float lin = c <= 0.04045f ? c / 12.92f : std::pow((c + 0.055f) / 1.055f, 2.4f);
+          o[k] = cv(lin);
+        }
+        o[3] = p[3];
+      } else {
+        return false;
+      }
+    }
+    for (int a = 0; a < 3; ++a) rec.dims[a] = a < dims ? (int)img->n[a] : 1;
+    if (texels.upload(rgba.data(), rgba.size(), dev->stream) != cudaSuccess ||
+        cudaStreamSynchronize(dev->stream) != cudaSuccess)
+      return false;
+    rec.texels = texels.as<uchar4>();
+    return true;
+  }
+  void commit() override {
+    valid = false;
+    rec = DSampler{};
+    const float id4[16] = {1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1};
+    memcpy(rec.inXfm, id4, sizeof(id4));
+    memcpy(rec.outXfm, id4, sizeof(id4));
+    getv("inTransform", VSR_FLOAT32_MAT4, rec.inXfm);
+    getv("outTransform", VSR_FLOAT32_MAT4, rec.outXfm);
+    getv("inOffset", VSR_FLOAT32_VEC4, rec.inOffset);
+    getv("outOffset", VSR_FLOAT32_VEC4, rec.outOffset);
+    rec.inAttribute = attributeId(gets("inAttribute", "attribute0"));
+    if (rec.inAttribute < 0) rec.inAttribute = ATTR_NONE;
+    rec.linear = gets("filter", "linear") != "nearest";
+    rec.wrap[0] = wrapMode(gets("wrapMode1", "clampToEdge"));
+    rec.wrap[1] = wrapMode(gets("wrapMode2", "clampToEdge"));
+    rec.wrap[2] = wrapMode(gets("wrapMode3", "clampToEdge"));
+    if (subtype == "transform") {
+      rec.type = SAMP_TRANSFORM;
+      valid = true;
+      return;
+    }
+    if (subtype == "primitive") {
+      rec.type = SAMP_PRIMITIVE;
+      Array *a = geto<Array>("array", VSR_ARRAY1D);
+      if (!a || !prim.load(a, dev->stream) || cudaStreamSynchronize(dev->stream) != cudaSuccess) {
+        warn("primitive sampler needs an 'array' of a supported type");
+        return;
+      }
+      rec.prim = prim.rec;
+      int off = 0;
+      geti("offset", off);
+      rec.primOffset = (uint32_t)off;
+      valid = true;
+      return;
+    }
+    const int dims = subtype == "image1D" ? 1 : subtype == "image2D" ? 2 : 3;
+    rec.type = dims == 1 ? SAMP_IMAGE1D : dims == 2 ? SAMP_IMAGE2D : SAMP_IMAGE3D;
+    const VSRDataType ak = dims == 1 ? VSR_ARRAY1D : dims == 2 ? VSR_ARRAY2D : VSR_ARRAY3D;
+    Array *img = geto<Array>("image", ak);
+    if (!img || img->size() == 0) {
+      warn("image sampler needs a non-empty 'image'");
+      return;
+    }
+    if (!loadImage(img, dims)) {
+      warn("unsupported element type of image sampler 'image'");
+      return;
+    }
+    valid = true;
+  }
+};
+
 struct Geometry : Object {
   std::vector<float> v1, e1, e2;  // per triangle, float3 packed
   // spheres, cones, cylinders: 8 floats per primitive, (p0, r0, p1, r1)
@@ -450,7 +617,66 @@ struct Geometry : Object {
   // iso-surface: the field and its iso values
   SpatialField *isoField = nullptr;
   std::vector<float> isoValues;
+  // attributes (Geometry.cpp: vertex.*, faceVarying.*, primitive.*, and
+  // the uniform "color" / "attribute0..3"); vertex normals and the index
+  // buffer (triangles)
+  AttrBuf vattr[5], fvattr[5], pattr[5];
+  DevBuf dIndex, dVertexNormal;
+  uint32_t numVertexNormals = 0;
+  bool fvNormal = false, triangleAttrs = false;
+  float uniformV[5][4] = {};
+  uint32_t uniformMask = 0;
   using Object::Object;
+  bool hasAttributes() const {
+    bool any = uniformMask != 0 || dVertexNormal.p != nullptr;
+    for (int k = 0; k < 5; ++k) any = any || vattr[k].rec.comps || fvattr[k].rec.comps || pattr[k].rec.comps;
+    return any;
+  }
+  DSurfAttr attrRecord() const {
+    DSurfAttr a{};
+    a.index = dIndex.as<uint32_t>();
+    a.vertexNormal = dVertexNormal.as<float>();
+    a.numVertexNormals = numVertexNormals;
+    a.fvNormal = fvNormal ? 1 : 0;
+    for (int k = 0; k < 5; ++k) {
+      a.vertex[k] = vattr[k].rec;
+      a.faceVarying[k] = fvattr[k].rec;
+      a.primitive[k] = pattr[k].rec;
+      memcpy(a.uniform[k], uniformV[k], sizeof(uniformV[k]));
+    }
+    a.uniformMask = uniformMask;
+    a.isTriangle = triangleAttrs ? 1 : 0;
+    return a;
+  }
+  // getAttribute's inputs for a triangle geometry (renderer/common.h:365-
+  // 521, getNormals :241-264): per-vertex, face-varying and per-primitive
+  // arrays, vertex normals, the index buffer
+  bool loadTriangleAttributes(Array *idx, size_t nv, size_t nprim) {
+    cudaStream_t st = dev->stream;
+    for (int k = 0; k < 5; ++k) {
+      const std::string n = kAttrNames[k];
+      Array *va = geto<Array>(("vertex." + n).c_str(), VSR_ARRAY1D);
+      Array *fa = geto<Array>(("faceVarying." + n).c_str(), VSR_ARRAY1D);
+      Array *pa = geto<Array>(("primitive." + n).c_str(), VSR_ARRAY1D);
+      if ((va && va->size() < nv) || (fa && fa->size() < 3 * nprim) || (pa && pa->size() < nprim))
+        warn("attribute array shorter than its geometry ('%s'); reads past it give (0, 0, 0, 1)",
+             n.c_str());
+      if (!vattr[k].load(va, st) || !fvattr[k].load(fa, st) || !pattr[k].load(pa, st)) {
+        warn("unsupported element type of geometry attribute '%s'", n.c_str());
+        return false;
+      }
+    }
+    Array *vn = geto<Array>("vertex.normal", VSR_ARRAY1D);
+    if (vn && vn->elemType == VSR_FLOAT32_VEC3) {
+      if (dVertexNormal.upload(vn->data.data(), vn->data.size(), st) != cudaSuccess) return false;
+      numVertexNormals = (uint32_t)vn->size();
+    }
+    Array *fn = geto<Array>("faceVarying.normal", VSR_ARRAY1D);
+    fvNormal = fn && fn->elemType == VSR_FLOAT32_VEC3 && fn->size() > 0;
+    if (idx && dIndex.upload(idx->data.data(), idx->data.size(), st) != cudaSuccess) return false;
+    triangleAttrs = true;
+    return cudaStreamSynchronize(st) == cudaSuccess;
+  }
   void commit() override {
     valid = false;
     v1.clear(); e1.clear(); e2.clear();
@@ -458,6 +684,17 @@ struct Geometry : Object {
     quadNormals.clear();
     isoField = nullptr;
     isoValues.clear();
+    for (int k = 0; k < 5; ++k) {
+      vattr[k].buf.release(); fvattr[k].buf.release(); pattr[k].buf.release();
+      vattr[k].rec = fvattr[k].rec = pattr[k].rec = DAttr{};
+    }
+    dIndex.release();
+    dVertexNormal.release();
+    numVertexNormals = 0;
+    fvNormal = triangleAttrs = false;
+    uniformMask = 0;
+    for (int k = 0; k < 5; ++k)
+      if (uniformAttr(this, kAttrNames[k], uniformV[k])) uniformMask |= 1u << k;
     if (subtype == "quad") {
       commitQuads();
       return;
@@ -506,9 +743,7 @@ struct Geometry : Object {
     } else {
       for (size_t i = 0; i + 2 < nv; i += 3) add(i, i + 1, i + 2);
     }
-    if (find("vertex.normal"))
-      dev->report(this, kind, VSR_SEVERITY_WARNING, VSR_OK,
-                  "'vertex.normal' is not used: shading uses the geometric normal");
+    if (!loadTriangleAttributes(idx, nv, v1.size() / 3)) return;
     valid = true;
   }
   // ISOSurface.cpp:19-60: a structured field ('field') and its iso values
@@ -688,9 +923,35 @@ struct Geometry : Object {
 // matte / physicallyBased, scene/surface/material/{Matte,PBM}.cpp
 struct Material : Object {
   DMaterial m{};
+  // per MSRC_* slot: a sampler, else an attribute (or SRC_VALUE)
+  Sampler *samp[4] = {};
+  short attrSrc[4] = {SRC_VALUE, SRC_VALUE, SRC_VALUE, SRC_VALUE};
   using Object::Object;
+  // MaterialParam* (Matte.cpp:11-31, PBM.cpp:11-86): a sampler object, else
+  // an attribute name, else the value
+  void source(const char *name, int slot) {
+    samp[slot] = geto<Sampler>(name, VSR_SAMPLER);
+    const int a = attributeId(gets(name, "none"));
+    attrSrc[slot] = (short)(a >= 0 ? a : SRC_VALUE);
+  }
+  bool usesAttributes() const {
+    for (int k = 0; k < 4; ++k)
+      if ((samp[k] && samp[k]->valid) || attrSrc[k] != SRC_VALUE) return true;
+    return false;
+  }
   void commit() override {
     m = DMaterial{};
+    for (int k = 0; k < 4; ++k) {
+      samp[k] = nullptr;
+      attrSrc[k] = SRC_VALUE;
+      m.src[k] = SRC_VALUE;
+    }
+    source(subtype == "matte" ? "color" : "baseColor", MSRC_COLOR);
+    source("opacity", MSRC_OPACITY);
+    if (subtype != "matte") {
+      source("metallic", MSRC_METALLIC);
+      source("roughness", MSRC_ROUGHNESS);
+    }
     float c4[4] = {1, 1, 1, 1};
     m.opacity = 1.f;
     getf("opacity", m.opacity);
@@ -955,9 +1216,13 @@ struct Instance : Object {
   Group *group = nullptr;
   float xfm[12] = {1, 0, 0, 0, 1, 0, 0, 0, 1, 0, 0, 0};
   uint32_t userID = ~0u;
+  DInstAttr attr{};  // uniform "color" / "attribute0..3" (Instance.cpp)
   using Object::Object;
   void commit() override {
     group = geto<Group>("group", VSR_GROUP);
+    attr = DInstAttr{};
+    for (int k = 0; k < 5; ++k)
+      if (uniformAttr(this, kAttrNames[k], attr.v[k])) attr.mask |= 1u << k;
     float m4[16];
     float i12[12] = {1, 0, 0, 0, 1, 0, 0, 0, 1, 0, 0, 0};
     memcpy(xfm, i12, sizeof(xfm));
@@ -1362,13 +1627,15 @@ struct World : Object {
   bool buildScene(uint64_t deep) {
     auto t0 = std::chrono::steady_clock::now();
     cudaStream_t s = dev->stream;
-    struct InstRec { Group *g; float xfm[12]; uint32_t userID; };
+    struct InstRec { Group *g; float xfm[12]; uint32_t userID; DInstAttr attr; };
     std::vector<InstRec> insts;
-    if (implicitUsed) insts.push_back({&implicitGroup, {1, 0, 0, 0, 1, 0, 0, 0, 1, 0, 0, 0}, ~0u});
+    if (implicitUsed)
+      insts.push_back({&implicitGroup, {1, 0, 0, 0, 1, 0, 0, 0, 1, 0, 0, 0}, ~0u, DInstAttr{}});
     for (Instance *I : instances) {
       if (!I->valid || !I->group) continue;
       InstRec r;
       r.g = I->group;
+      r.attr = I->attr;
       memcpy(r.xfm, I->xfm, sizeof(r.xfm));
       r.userID = I->userID;
       insts.push_back(r);
@@ -1379,6 +1646,8 @@ struct World : Object {
       if (!gidx.count(r.g)) { gidx[r.g] = (int)groups.size(); groups.push_back(r.g); }
 
     std::vector<DMaterial> mats;
+    std::vector<Geometry *> surfGeom;
+    std::vector<Material *> surfMat;
     std::vector<DGroup> dgroups(groups.size());
     std::vector<DVolume> vols;
     std::vector<int> groupVols;
@@ -1404,6 +1673,8 @@ struct World : Object {
         if (!sf->valid || !sf->geom->valid || !sf->mat->valid) continue;
         uint32_t sid = (uint32_t)mats.size();
         mats.push_back(sf->mat->m);
+        surfGeom.push_back(sf->geom);
+        surfMat.push_back(sf->mat);
         if (sf->mat->m.alphaMode != ALPHA_OPAQUE) allOpaque = false;
         Geometry *G = sf->geom;
         if (G->isIso()) {
@@ -1580,6 +1851,7 @@ struct World : Object {
       groupsGPU.push_back(std::move(gg));
     }
     std::vector<DInstance> dinst;
+    std::vector<DInstAttr> instAttrs;
     std::vector<DLight> lights;
     for (auto &r : insts) {
       DInstance di{};
@@ -1599,6 +1871,7 @@ struct World : Object {
       di.group = gidx[r.g];
       di.userID = r.userID;
       dinst.push_back(di);
+      instAttrs.push_back(r.attr);
       for (Light *L : r.g->lights) {
         if (!L->valid) continue;
         // xfmLight (DeviceCopyableObjects.h:2398-2430): positions by the
@@ -1666,6 +1939,7 @@ struct World : Object {
     }
     if (dInstances.upload(dinst.data(), dinst.size() * sizeof(DInstance), s) ||
         dGroups.upload(dgroups.data(), dgroups.size() * sizeof(DGroup), s) ||
+        !assembleAttributes(mats, surfGeom, surfMat, instAttrs, s) ||
         dMaterials.upload(mats.data(), mats.size() * sizeof(DMaterial), s) ||
         dLights.upload(lights.data(), lights.size() * sizeof(DLight), s) ||
         dVolumes.upload(vols.data(), vols.size() * sizeof(DVolume), s) ||
@@ -1699,6 +1973,10 @@ struct World : Object {
     scene.numIso = numIso;
     scene.maxGroupWidth = 2;
     for (const DGroup &g : dgroups) scene.maxGroupWidth = std::max(scene.maxGroupWidth, g.width);
+    scene.attributes = useAttributes ? 1 : 0;
+    scene.surfAttr = useAttributes ? dSurfAttr.as<DSurfAttr>() : nullptr;
+    scene.instAttr = useAttributes ? dInstAttr.as<DInstAttr>() : nullptr;
+    scene.samplers = useAttributes ? dSamplers.as<DSampler>() : nullptr;
     builtStamp = deep;
     commitMs = std::chrono::duration<float, std::milli>(std::chrono::steady_clock::now() - t0).count();
     return true;
@@ -1707,6 +1985,43 @@ struct World : Object {
   uint64_t deepStamp() override {
     uint64_t s = Object::deepStamp();
     return s;
+  }
+
+  // Attribute records per surface and instance, the samplers the materials
+  // use, and the materials' parameter sources (a sampler's index in the
+  // world's list); nothing when no geometry, material or instance uses
+  // attributes, samplers or vertex normals.
+  DevBuf dSurfAttr, dInstAttr, dSamplers;
+  bool useAttributes = false;
+  bool assembleAttributes(std::vector<DMaterial> &mats, const std::vector<Geometry *> &geoms,
+                          const std::vector<Material *> &ms,
+                          const std::vector<DInstAttr> &instAttrs, cudaStream_t s) {
+    useAttributes = false;
+    for (size_t i = 0; i < geoms.size(); ++i)
+      useAttributes = useAttributes || geoms[i]->hasAttributes() || ms[i]->usesAttributes();
+    for (const DInstAttr &a : instAttrs) useAttributes = useAttributes || a.mask != 0;
+    if (!useAttributes) return true;
+    std::vector<DSurfAttr> sattr;
+    std::vector<DSampler> samplers;
+    std::map<Sampler *, int> sidx;
+    for (size_t i = 0; i < geoms.size(); ++i) {
+      sattr.push_back(geoms[i]->attrRecord());
+      for (int k = 0; k < 4; ++k) {
+        Sampler *sp = ms[i]->samp[k];
+        if (sp && sp->valid) {
+          if (!sidx.count(sp)) {
+            sidx[sp] = (int)samplers.size();
+            samplers.push_back(sp->rec);
+          }
+          mats[i].src[k] = (short)(SRC_SAMPLER + sidx[sp]);
+        } else {
+          mats[i].src[k] = ms[i]->attrSrc[k];
+        }
+      }
+    }
+    return dSurfAttr.upload(sattr.data(), sattr.size() * sizeof(DSurfAttr), s) == cudaSuccess &&
+           dInstAttr.upload(instAttrs.data(), instAttrs.size() * sizeof(DInstAttr), s) == cudaSuccess &&
+           dSamplers.upload(samplers.data(), samplers.size() * sizeof(DSampler), s) == cudaSuccess;
   }
 };
 
@@ -1967,7 +2282,7 @@ VSRStatus renderFrame(Device *dev, FrameObj *F) {
   // megakernel takes such frames
   const bool wave = F->renderer->wavefront && !R.gradientShading && !W->scene.numAnalytic &&
                     !W->scene.quadGroups && !W->scene.numIso && R.sampleChunks <= 1 && !R.taa &&
-                    !W->scene.areaLights;
+                    !W->scene.areaLights && !W->scene.attributes;
   int stage = 0;
   MarchScratch ms{};
   bool segmented = false;
@@ -1977,7 +2292,7 @@ VSRStatus renderFrame(Device *dev, FrameObj *F) {
     // the segmented marcher composites unshaded samples; gradient shading
     // takes the per-pixel kernel
     segmented = !W->scene.hasSurfaces && R.pixelSamples == 1 && !R.gradientShading &&
-                !W->scene.areaLights;
+                !W->scene.areaLights && !W->scene.attributes;
     if (segmented && !F->ensureMarch()) {
       dev->report(F, VSR_FRAME, VSR_SEVERITY_ERROR, VSR_ERROR_OUT_OF_MEMORY,
                   "volume marcher scratch allocation failed");
@@ -2186,7 +2501,7 @@ VSRStatus renderFrames(Device *dev, FrameObj *const *frames, uint32_t count) {
     }
     j.F = F->record();
     j.kind = j.R.type != REND_RAYCAST ? JOB_PATHTRACE
-             : (j.R.gradientShading || j.S.areaLights ||
+             : (j.R.gradientShading || j.S.areaLights || j.S.attributes ||
                 (j.S.hasSurfaces &&
                  (j.S.positionalLights || j.S.numAnalytic || j.S.quadGroups || j.S.numIso)))
                  ? JOB_RAYCAST_FULL
@@ -2263,7 +2578,7 @@ VSRStatus renderFrames(Device *dev, FrameObj *const *frames, uint32_t count) {
       if (j.kind == JOB_PATHTRACE) {
         if (j.S.numVolumes > 0) L.pathtraceVariant |= 1;
         if (j.S.positionalLights || j.S.numAnalytic || j.S.quadGroups || j.S.numIso ||
-            (j.S.numVolumes > 0 && j.R.gradientShading))
+            j.S.attributes || (j.S.numVolumes > 0 && j.R.gradientShading))
           L.pathtraceVariant |= 2;
       }
     // one CUDA graph per frame set and configuration: the job records are
@@ -2494,6 +2809,10 @@ VSRObject vsrNewInstance(VSRDevice d, const char *s) {
 VSRObject vsrNewWorld(VSRDevice d) { return newObj<World>(d, VSR_WORLD, "", {}); }
 VSRObject vsrNewCamera(VSRDevice d, const char *s) {
   return newObj<Camera>(d, VSR_CAMERA, s, {"perspective", "matrix", "orthographic", "omnidirectional"});
+}
+VSRObject vsrNewSampler(VSRDevice d, const char *s) {
+  return newObj<Sampler>(d, VSR_SAMPLER, s,
+                         {"image1D", "image2D", "image3D", "transform", "primitive"});
 }
 VSRObject vsrNewRenderer(VSRDevice d, const char *s) {
   return newObj<Renderer>(d, VSR_RENDERER, s, {"raycast", "pathtrace", "default"});

@@ -106,6 +106,12 @@ constexpr int kMaxClipPlanes = 8;
 constexpr uint32_t kLeafCountShift = 27;
 constexpr uint32_t kLeafFirstMask = (1u << kLeafCountShift) - 1u;
 
+// Where a material parameter comes from (dco::MaterialParam*, renderer/
+// common.h:593-640): its value, a geometry / hit attribute (ATTR_*), or a
+// sampler (SRC_SAMPLER + the sampler's index in DScene::samplers).
+enum { SRC_VALUE = -1, SRC_SAMPLER = 16 };
+enum { MSRC_COLOR = 0, MSRC_OPACITY = 1, MSRC_METALLIC = 2, MSRC_ROUGHNESS = 3 };
+
 struct DMaterial {
   float baseColor[3];
   int type;
@@ -114,7 +120,66 @@ struct DMaterial {
   float sheenColor[3];
   int alphaMode;
   float alphaCutoff;
-  float pad[3];
+  short src[4];  // MSRC_*: SRC_VALUE, an ATTR_* or SRC_SAMPLER + k
+  int pad;
+};
+
+// Geometry and hit attributes (dco::Attribute, DeviceCopyableObjects.h
+// :1626-1655): attribute0..3, color, then the hit's world position, world
+// normal, object position and object normal.
+enum { ATTR_0 = 0, ATTR_1, ATTR_2, ATTR_3, ATTR_COLOR, ATTR_WORLD_POS, ATTR_WORLD_NORMAL,
+       ATTR_OBJECT_POS, ATTR_OBJECT_NORMAL, ATTR_NONE = 15 };
+
+// One attribute array: `comps` components per element, float32 or unorm8
+// / unorm16 (toRGBA, common.h:265-360); comps = 0: absent.
+struct DAttr {
+  const void *data;
+  uint32_t len;
+  uint16_t comps;
+  uint16_t fixedBits;  // 0 = float32, 8 or 16 = unorm
+};
+
+// Per surface (indexed like DScene::materials): its geometry's attributes.
+// Triangles: vertex and face-varying arrays interpolated with the hit's
+// barycentrics (vertex indices from `index`, 3 per primitive, or
+// consecutive), per-primitive arrays, then uniform values; other kinds use
+// the per-primitive and uniform ones. vertexNormal: float3 per vertex
+// (shading normals), fvNormal: the geometry has face-varying normals.
+struct DSurfAttr {
+  const uint32_t *index;
+  const float *vertexNormal;
+  uint32_t numVertexNormals;
+  int fvNormal;
+  DAttr vertex[5], faceVarying[5], primitive[5];
+  float uniform[5][4];
+  uint32_t uniformMask;
+  int isTriangle;
+};
+
+// Per instance: its uniform attributes (Instance.cpp, "color",
+// "attribute0..3").
+struct DInstAttr {
+  float v[5][4];
+  uint32_t mask;
+  int pad[3];
+};
+
+enum { SAMP_IMAGE1D = 0, SAMP_IMAGE2D = 1, SAMP_IMAGE3D = 2, SAMP_TRANSFORM = 3, SAMP_PRIMITIVE = 4 };
+enum { WRAP_CLAMP = 0, WRAP_REPEAT = 1, WRAP_MIRROR = 2 };
+
+// A sampler (scene/surface/material/sampler): image samplers hold RGBA8
+// texels (every image format is converted to 8 bits per channel, as the
+// reference's imageSamplerUpdateData does), dims[] texels per axis.
+struct DSampler {
+  int type;
+  int inAttribute;
+  int linear;       // filter "linear" (else nearest)
+  int wrap[3];
+  int dims[3];
+  const uchar4 *texels;
+  DAttr prim;       // primitive sampler: the array
+  uint32_t primOffset;
+  float inXfm[16], inOffset[4], outXfm[16], outOffset[4];  // column-major mat4
 };
 
 enum LightType { LIGHT_DIRECTIONAL = 0, LIGHT_POINT = 1, LIGHT_SPOT = 2, LIGHT_QUAD = 3, LIGHT_HDRI = 4 };
@@ -246,6 +311,12 @@ struct DScene {
   int allOpaque;
   int hasSurfaces;
   int maxGroupWidth;  // widest group BVH (2 or 4)
+  // attributes, samplers, shading normals (null / 0 when the world uses
+  // none): the kernels' full variants resolve materials per hit
+  const DSurfAttr *surfAttr;
+  const DInstAttr *instAttr;
+  const DSampler *samplers;
+  int attributes;
 };
 
 struct DCamera {

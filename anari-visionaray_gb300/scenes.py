@@ -301,12 +301,48 @@ def triangle_count(scene):
 
 
 # --------------------------------------------------------------- build via ABI
-def _material(dev, m):
+def _sampler(dev, d, keep):
+    """A sampler object from {"type": "image1D" | "image2D" | "image3D" |
+    "transform" | "primitive", "image" / "array": numpy array, "inAttribute",
+    "filter", "wrapMode1..3", "inTransform" / "outTransform" (16 floats,
+    column-major), "inOffset" / "outOffset" (4 floats), "offset"}."""
+    kind = d["type"]
+    smp = dev.sampler(kind)
+    for k, v in d.items():
+        if k == "type":
+            continue
+        if k == "image":
+            a = np.ascontiguousarray(v)
+            arr = (dev.array1d if kind == "image1D" else
+                   dev.array2d if kind == "image2D" else dev.array3d)(a)
+            keep.append(arr)
+            dev.set(smp, "image", arr)
+        elif k == "array":
+            arr = dev.array1d(np.ascontiguousarray(v))
+            keep.append(arr)
+            dev.set(smp, "array", arr)
+        elif k in ("inTransform", "outTransform"):
+            dev.set(smp, k, [float(x) for x in v], vsr.FLOAT32_MAT4)
+        elif k in ("inOffset", "outOffset"):
+            dev.set(smp, k, [float(x) for x in v], vsr.FLOAT32_VEC4)
+        elif k == "offset":
+            dev.set(smp, k, int(v))
+        else:
+            dev.set(smp, k, str(v))
+    dev.commit(smp)
+    keep.append(smp)
+    return smp
+
+
+def _material(dev, m, keep=None):
     mat = dev.material(m["type"])
     for k, v in m.items():
         if k == "type":
             continue
-        if isinstance(v, str):
+        if isinstance(v, dict):
+            # {"sampler": {...}}: the parameter comes from a sampler
+            dev.set(mat, k, _sampler(dev, v["sampler"], keep if keep is not None else []))
+        elif isinstance(v, str):
             dev.set(mat, k, v)
         elif isinstance(v, (list, tuple)):
             dev.set(mat, k, v, vsr.FLOAT32_VEC3 if len(v) == 3 else vsr.FLOAT32_VEC4)
@@ -314,6 +350,31 @@ def _material(dev, m):
             dev.set(mat, k, float(v))
     dev.commit(mat)
     return mat
+
+
+def _uniform(dev, obj, name, v):
+    v = [float(x) for x in (v if isinstance(v, (list, tuple, np.ndarray)) else [v])]
+    dev.set(obj, name, v if len(v) > 1 else v[0],
+            {1: vsr.FLOAT32, 2: vsr.FLOAT32_VEC2, 3: vsr.FLOAT32_VEC3, 4: vsr.FLOAT32_VEC4}[len(v)])
+
+
+def _geometry_attributes(dev, g, s, keep):
+    """Surface keys "normals" (vertex.normal), "attributes" (vertex.*),
+    "faceVarying" (faceVarying.*), "primitive" (primitive.*): {name: array}
+    with name "color" or "attribute0".."attribute3"; "uniform": {name:
+    value}."""
+    if "normals" in s:
+        na = dev.array1d(np.asarray(s["normals"], np.float32).reshape(-1, 3))
+        dev.set(g, "vertex.normal", na)
+        keep.append(na)
+    for key, prefix in (("attributes", "vertex."), ("faceVarying", "faceVarying."),
+                        ("primitive", "primitive.")):
+        for name, arr in s.get(key, {}).items():
+            a = dev.array1d(np.ascontiguousarray(arr))
+            dev.set(g, prefix + name, a)
+            keep.append(a)
+    for name, v in s.get("uniform", {}).items():
+        _uniform(dev, g, name, v)
 
 
 def _surfaces(dev, surfs, keep):
@@ -363,8 +424,9 @@ def _surfaces(dev, surfs, keep):
         if ia is not None:
             dev.set(g, "primitive.index", ia)
             keep += [ia]
+        _geometry_attributes(dev, g, s, keep)
         dev.commit(g)
-        mat = _material(dev, s["material"])
+        mat = _material(dev, s["material"], keep)
         sf = dev.surface()
         dev.set(sf, "geometry", g)
         dev.set(sf, "material", mat)
@@ -496,6 +558,8 @@ def build(dev, scene, channels=("color", "depth", "normal", "albedo"), collect_s
         inst = dev.instance("transform")
         dev.set(inst, "group", grp)
         dev.set(inst, "transform", I["transform"], vsr.FLOAT32_MAT3x4)
+        for name, v in I.get("attributes", {}).items():
+            _uniform(dev, inst, name, v)
         dev.commit(inst)
         keep.append(grp)
         insts.append(inst)

@@ -19,12 +19,13 @@ UNKNOWN, STRING, OBJECT, ARRAY1D, ARRAY2D, ARRAY3D, CAMERA, FRAME, GEOMETRY, GRO
     LIGHT, MATERIAL, RENDERER, SURFACE, SPATIAL_FIELD, VOLUME, WORLD, DATA_TYPE, BOOL, INT32, \
     UINT32, INT32_VEC2, UINT32_VEC2, UINT32_VEC3, FLOAT32, FLOAT32_VEC2, FLOAT32_VEC3, \
     FLOAT32_VEC4, FLOAT32_BOX1, FLOAT32_MAT4, FLOAT32_MAT3x4, UFIXED8, UFIXED8_VEC4, \
-    UFIXED8_RGBA_SRGB, UFIXED16, FLOAT64_BOX1, UINT64, FLOAT64, UINT32_VEC4 = range(40)
+    UFIXED8_RGBA_SRGB, UFIXED16, FLOAT64_BOX1, UINT64, FLOAT64, UINT32_VEC4, SAMPLER, \
+    UFIXED8_VEC2, UFIXED8_VEC3 = range(43)
 
 OK = 0
 WAIT, NO_WAIT = 1, 0
 
-_OBJECT_KINDS = set(range(OBJECT, WORLD + 1))
+_OBJECT_KINDS = set(range(OBJECT, WORLD + 1)) | {SAMPLER}
 
 _CALLBACK = ctypes.CFUNCTYPE(None, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int,
                              ctypes.c_int, ctypes.c_int, ctypes.c_char_p)
@@ -48,6 +49,7 @@ _SIGNATURES = [
     ("vsrNewWorld", _P, [_P]),
     ("vsrNewCamera", _P, [_P, ctypes.c_char_p]),
     ("vsrNewRenderer", _P, [_P, ctypes.c_char_p]),
+    ("vsrNewSampler", _P, [_P, ctypes.c_char_p]),
     ("vsrNewFrame", _P, [_P]),
     ("vsrSetParameter", ctypes.c_int, [_P, _P, ctypes.c_char_p, ctypes.c_int, _P]),
     ("vsrUnsetParameter", ctypes.c_int, [_P, _P, ctypes.c_char_p]),
@@ -150,6 +152,9 @@ _ARRAY_TYPES = {
     (np.dtype(np.uint32), 3): UINT32_VEC3,
     (np.dtype(np.uint32), 4): UINT32_VEC4,
     (np.dtype(np.uint8), 1): UFIXED8,
+    (np.dtype(np.uint8), 2): UFIXED8_VEC2,
+    (np.dtype(np.uint8), 3): UFIXED8_VEC3,
+    (np.dtype(np.uint8), 4): UFIXED8_VEC4,
     (np.dtype(np.uint16), 1): UFIXED16,
 }
 
@@ -290,7 +295,8 @@ class Device:
         a = np.ascontiguousarray(data)
         if dims == 3:
             nz, ny, nx = a.shape[:3]
-            t = dtype if dtype is not None else _ARRAY_TYPES[(a.dtype, 1)]
+            comps = 1 if a.ndim == 3 else a.shape[-1]
+            t = dtype if dtype is not None else _ARRAY_TYPES[(a.dtype, comps)]
             h = self.lib.vsrNewArray3D(self.handle, a.ctypes.data, t, nx, ny, nz)
             return Obj(h, ARRAY3D)
         if dims == 2:
@@ -341,6 +347,9 @@ class Device:
 
     def renderer(self, subtype):
         return self._new("vsrNewRenderer", RENDERER, subtype)
+
+    def sampler(self, subtype):
+        return self._new("vsrNewSampler", SAMPLER, subtype)
 
     def frame(self):
         return self._new("vsrNewFrame", FRAME)

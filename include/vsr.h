@@ -95,7 +95,10 @@ typedef enum VSRDataType {
   VSR_FLOAT64_BOX1 = 36,
   VSR_UINT64 = 37,
   VSR_FLOAT64 = 38,
-  VSR_UINT32_VEC4 = 39
+  VSR_UINT32_VEC4 = 39,
+  VSR_SAMPLER = 40,
+  VSR_UFIXED8_VEC2 = 41,
+  VSR_UFIXED8_VEC3 = 42
 } VSRDataType;
 
 typedef enum VSRWaitMask { VSR_NO_WAIT = 0, VSR_WAIT = 1 } VSRWaitMask;
@@ -142,6 +145,18 @@ VSR_API VSRObject vsrNewInstance(VSRDevice d, const char *subtype);
 VSR_API VSRObject vsrNewWorld(VSRDevice d);
 VSR_API VSRObject vsrNewCamera(VSRDevice d, const char *subtype);
 VSR_API VSRObject vsrNewRenderer(VSRDevice d, const char *subtype);
+/* Samplers (newSampler, VisionarayDevice.cpp:125-214; scene/surface/
+   material/sampler): "image1D", "image2D", "image3D" (image: Array1D / 2D /
+   3D of FLOAT32 (VEC2/3/4) or UFIXED8 (VEC2/3/4, RGBA_SRGB) texels, stored
+   as RGBA8; inAttribute, filter "linear" | "nearest", wrapMode1..3
+   "clampToEdge" | "repeat" | "mirrorRepeat", inTransform / outTransform
+   (FLOAT32_MAT4), inOffset / outOffset (FLOAT32_VEC4)), "transform"
+   (inAttribute, outTransform, outOffset) and "primitive" (array, offset).
+   A material's color / baseColor, opacity, metallic and roughness take a
+   sampler object, an attribute name (STRING: "attribute0".."attribute3",
+   "color", "worldPosition", "worldNormal", "objectPosition",
+   "objectNormal") or a value. */
+VSR_API VSRObject vsrNewSampler(VSRDevice d, const char *subtype);
 VSR_API VSRFrame vsrNewFrame(VSRDevice d);
 
 /* Parameters; replace anariSetParameter/anariUnsetParameter/

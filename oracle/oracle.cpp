@@ -358,6 +358,7 @@ struct Hdri {
 struct Scene {
   const OrScene *src;
   std::vector<Hdri> hdri;  // per light (empty tables for other types)
+  std::vector<std::vector<uint8_t>> texels;  // per sampler: its image as RGBA8
   std::vector<Tri> tris;
   std::vector<Vol> isoFields;  // the iso-surfaces' fields (bounds and voxel space)
   std::vector<f3> triNormal;   // quads: the shading normal per triangle (empty if none)
@@ -983,6 +984,186 @@ float materialOpacity(const OrMaterial &m) { // getOpacity :735-760
   return op >= m.alphaCutoff ? 1.f : 0.f;
 }
 
+// ---------------------------------------------------------------------------
+// Attributes and samplers (renderer/common.h:365-640).
+// ---------------------------------------------------------------------------
+// toRGBA (common.h:265-360): the element's components, the rest of
+// (0, 0, 0, 1); unorm as value / (2^bits - 1); past the array: the default.
+f4 attrFetch(const OrAttr &a, uint32_t i) {
+  float c[4] = {0.f, 0.f, 0.f, 1.f};
+  if (i < a.len) {
+    for (int k = 0; k < a.comps; ++k) {
+      if (a.fixedBits == 8) c[k] = ((const uint8_t *)a.data)[size_t(i) * a.comps + k] / 255.f;
+      else if (a.fixedBits == 16) c[k] = ((const uint16_t *)a.data)[size_t(i) * a.comps + k] / 65535.f;
+      else c[k] = ((const float *)a.data)[size_t(i) * a.comps + k];
+    }
+  }
+  return f4(c[0], c[1], c[2], c[3]);
+}
+
+// lerp_r(a, b, c, u, v) over a triangle: (1 - u - v) a + u b + v c
+f4 baryLerp(f4 a, f4 b, f4 c, float u, float v) {
+  const float w = 1.f - u - v;
+  return f4(w * a.x + u * b.x + v * c.x, w * a.y + u * b.y + v * c.y,
+            w * a.z + u * b.z + v * c.z, w * a.w + u * b.w + v * c.w);
+}
+
+struct AttrCtx {
+  const OrSurfAttr *sa = nullptr;
+  const OrInstance *inst = nullptr;
+  uint32_t primID = 0;
+  float u = 0.f, v = 0.f;
+  f3 worldPos, worldNormal, objectPos, objectNormal;
+};
+
+// getAttribute (renderer/common.h:365-521): triangles take face-varying,
+// else per-vertex values (barycentric), else the primitive's; then the
+// geometry's uniform value, then the instance's; else (0, 0, 0, 1).
+f4 getAttr(const AttrCtx &c, int id) {
+  if (id >= OR_ATTR_WORLD_POS && id <= OR_ATTR_OBJECT_NORMAL) {
+    const f3 h = id == OR_ATTR_WORLD_POS ? c.worldPos : id == OR_ATTR_WORLD_NORMAL ? c.worldNormal
+               : id == OR_ATTR_OBJECT_POS ? c.objectPos : c.objectNormal;
+    return f4(h, 1.f);
+  }
+  if (id < 0 || id > OR_ATTR_COLOR || !c.sa) return f4(0.f, 0.f, 0.f, 1.f);
+  const OrSurfAttr &s = *c.sa;
+  if (s.isTriangle) {
+    const uint32_t p = c.primID;
+    if (s.faceVarying[id].comps)
+      return baryLerp(attrFetch(s.faceVarying[id], 3 * p), attrFetch(s.faceVarying[id], 3 * p + 1),
+                      attrFetch(s.faceVarying[id], 3 * p + 2), c.u, c.v);
+    if (s.vertex[id].comps) {
+      uint32_t i0 = 3 * p, i1 = 3 * p + 1, i2 = 3 * p + 2;
+      if (s.index) { i0 = s.index[i0]; i1 = s.index[i1]; i2 = s.index[i2]; }
+      return baryLerp(attrFetch(s.vertex[id], i0), attrFetch(s.vertex[id], i1),
+                      attrFetch(s.vertex[id], i2), c.u, c.v);
+    }
+    if (s.primitive[id].comps) return attrFetch(s.primitive[id], p);
+  }
+  if (s.uniformMask & (1u << id))
+    return f4(s.uniform[id][0], s.uniform[id][1], s.uniform[id][2], s.uniform[id][3]);
+  if (c.inst && (c.inst->attrMask & (1u << id)))
+    return f4(c.inst->attr[id][0], c.inst->attr[id][1], c.inst->attr[id][2], c.inst->attr[id][3]);
+  return f4(0.f, 0.f, 0.f, 1.f);
+}
+
+// getNormals' shading normal (renderer/common.h:241-264): the vertex
+// normals interpolated and normalised (with face-varying normals set, the
+// reference reads the vertex normals at 3 primID + k), else Ng.
+f3 shadingNormal(const OrSurfAttr &s, uint32_t p, float u, float v, f3 Ng) {
+  if (!s.isTriangle || !s.vertexNormal) return Ng;
+  uint32_t i[3] = {3 * p, 3 * p + 1, 3 * p + 2};
+  if (!s.fvNormal && s.index)
+    for (int k = 0; k < 3; ++k) i[k] = s.index[i[k]];
+  for (int k = 0; k < 3; ++k)
+    if (i[k] >= s.numVertexNormals) return Ng;
+  const float *N = s.vertexNormal;
+  f4 n = baryLerp(f4(N[3 * i[0]], N[3 * i[0] + 1], N[3 * i[0] + 2], 0.f),
+                  f4(N[3 * i[1]], N[3 * i[1] + 1], N[3 * i[1] + 2], 0.f),
+                  f4(N[3 * i[2]], N[3 * i[2] + 1], N[3 * i[2] + 2], 0.f), u, v);
+  return normalize(n.xyz());
+}
+
+f4 mat4mul(const float *m, f4 v) {
+  return f4(((m[0] * v.x + m[4] * v.y) + m[8] * v.z) + m[12] * v.w,
+            ((m[1] * v.x + m[5] * v.y) + m[9] * v.z) + m[13] * v.w,
+            ((m[2] * v.x + m[6] * v.y) + m[10] * v.z) + m[14] * v.w,
+            ((m[3] * v.x + m[7] * v.y) + m[11] * v.z) + m[15] * v.w);
+}
+
+// toAddressMode (scene/surface/common.h:59-72): clampToEdge, repeat,
+// mirrorRepeat on texel indices.
+int wrapIndex(float fi, int n, int mode) {
+  const int i = !(fi > -1e9f && fi < 1e9f) ? 0 : (int)fi;
+  if (mode == 1) return ((i % n) + n) % n;
+  if (mode == 2) {
+    const int m = ((i % (2 * n)) + 2 * n) % (2 * n);
+    return m < n ? m : 2 * n - 1 - m;
+  }
+  return i < 0 ? 0 : (i > n - 1 ? n - 1 : i);
+}
+
+// tex1D / tex2D / tex3D on the RGBA8 image: texel centres at (i + 0.5) / n,
+// linear (x, then y, then z) or nearest.
+f4 imageSample(const OrSampler &s, const std::vector<uint8_t> &tx, f4 tc) {
+  const int axes = s.type == OR_SAMP_IMAGE1D ? 1 : (s.type == OR_SAMP_IMAGE2D ? 2 : 3);
+  const float c[3] = {tc.x, tc.y, tc.z};
+  int i0[3] = {0, 0, 0}, i1[3] = {0, 0, 0};
+  float f[3] = {0.f, 0.f, 0.f};
+  for (int a = 0; a < axes; ++a) {
+    const int n = s.dims[a];
+    if (s.linear) {
+      const float x = c[a] * n - 0.5f;
+      const float fl = std::floor(x);
+      f[a] = x - fl;
+      i0[a] = wrapIndex(fl, n, s.wrap[a]);
+      i1[a] = wrapIndex(fl + 1.f, n, s.wrap[a]);
+    } else {
+      i0[a] = i1[a] = wrapIndex(std::floor(c[a] * n), n, s.wrap[a]);
+    }
+  }
+  auto at = [&](int i, int j, int k) {
+    const uint8_t *t = &tx[4 * ((size_t(k) * s.dims[1] + j) * s.dims[0] + i)];
+    return f4(t[0] / 255.f, t[1] / 255.f, t[2] / 255.f, t[3] / 255.f);
+  };
+  auto lerp4 = [](f4 p, f4 q, float t) {
+    return f4(p.x + t * (q.x - p.x), p.y + t * (q.y - p.y), p.z + t * (q.z - p.z), p.w + t * (q.w - p.w));
+  };
+  const f4 c00 = lerp4(at(i0[0], i0[1], i0[2]), at(i1[0], i0[1], i0[2]), f[0]);
+  if (axes == 1) return c00;
+  const f4 c10 = lerp4(at(i0[0], i1[1], i0[2]), at(i1[0], i1[1], i0[2]), f[0]);
+  const f4 c0 = lerp4(c00, c10, f[1]);
+  if (axes == 2) return c0;
+  const f4 c01 = lerp4(at(i0[0], i0[1], i1[2]), at(i1[0], i0[1], i1[2]), f[0]);
+  const f4 c11 = lerp4(at(i0[0], i1[1], i1[2]), at(i1[0], i1[1], i1[2]), f[0]);
+  return lerp4(c0, lerp4(c01, c11, f[1]), f[2]);
+}
+
+// getSample (renderer/common.h:546-590).
+f4 getSample(const Scene &sc, int k, const AttrCtx &c) {
+  const OrSampler &s = sc.src->samplers[k];
+  if (s.type == OR_SAMP_PRIMITIVE) return attrFetch(s.prim, c.primID + s.primOffset);
+  f4 a = getAttr(c, s.inAttribute);
+  auto addv = [](f4 p, const float *o) { return f4(p.x + o[0], p.y + o[1], p.z + o[2], p.w + o[3]); };
+  if (s.type == OR_SAMP_TRANSFORM) return addv(mat4mul(s.outXfm, a), s.outOffset);
+  a = addv(mat4mul(s.inXfm, a), s.inOffset);
+  return addv(mat4mul(s.outXfm, imageSample(s, sc.texels[k], a)), s.outOffset);
+}
+
+f4 materialParam(const Scene &sc, int src, f4 value, const AttrCtx &c) {
+  if (src < 0) return value;
+  if (src >= 16) return getSample(sc, src - 16, c);
+  return getAttr(c, src);
+}
+
+// The material at a hit with its parameters looked up (getColor, getF,
+// getOpacity, renderer/common.h:642-710).
+OrMaterial resolveMaterial(const Scene &sc, const OrMaterial &m, const AttrCtx &c) {
+  OrMaterial r = m;
+  const f4 col = materialParam(sc, m.src[0], f4(m.baseColor[0], m.baseColor[1], m.baseColor[2], 1.f), c);
+  r.baseColor[0] = col.x;
+  r.baseColor[1] = col.y;
+  r.baseColor[2] = col.z;
+  r.opacity = col.w * materialParam(sc, m.src[1], f4(m.opacity, 0.f, 0.f, 1.f), c).x;
+  if (m.type == OR_PBR) {
+    r.metallic = materialParam(sc, m.src[2], f4(m.metallic, 0.f, 0.f, 1.f), c).x;
+    r.roughness = materialParam(sc, m.src[3], f4(m.roughness, 0.f, 0.f, 1.f), c).x;
+  }
+  return r;
+}
+
+// The attribute context of a surface hit (hit attributes zero).
+AttrCtx hitAttrCtx(const Scene &sc, const SurfHit &h) {
+  AttrCtx c;
+  const OrScene &S = *sc.src;
+  if (S.surfAttr) c.sa = &S.surfAttr[hitSurface(S, h)];
+  c.inst = &S.instances[h.inst];
+  c.primID = (h.prim < 0 && h.iso < 0) ? S.triPrimID[h.tri] : 0u;
+  c.u = h.u;
+  c.v = h.v;
+  return c;
+}
+
 f3 evalPBR(const OrMaterial &m, f3 Ns, f3 viewDir, f3 lightDir) {
   const float metallic = m.metallic, roughness = m.roughness;
   const float clearcoat = m.clearcoat, clearcoatRoughness = m.clearcoatRoughness;
@@ -1559,12 +1740,27 @@ PixelSample raycastSample(const Scene &sc, const OrRenderer &R, Ray ray, Counter
     if (++layers > (1 << 12)) break;  // same bound as the GPU path (zero epsilon would loop)
     const Inst &inst = sc.insts[hr.inst];
     uint32_t surf = hitSurface(S, hr);
-    const OrMaterial &mat = S.surfMaterial[surf];
     f3 hitPos = ray.ori + hr.t * ray.dir;
     f3 gn = hitNormal(sc, hr);
     f3 sn = gn;
-    gn = normalize(inst.normalXfm * gn);
-    sn = normalize(inst.normalXfm * sn);
+    OrMaterial mat = S.surfMaterial[surf];
+    if (S.surfAttr) {
+      // shading normal and attributes (Raycast_impl.cpp:45-60): the
+      // "worldNormal" attribute is the object-space normal, the
+      // "objectNormal" one the transformed normal, as the reference passes
+      AttrCtx ac = hitAttrCtx(sc, hr);
+      sn = shadingNormal(*ac.sa, ac.primID, hr.u, hr.v, gn);
+      ac.worldPos = hitPos;
+      ac.worldNormal = gn;
+      ac.objectPos = hr.isect_pos;
+      gn = normalize(inst.normalXfm * gn);
+      sn = normalize(inst.normalXfm * sn);
+      ac.objectNormal = gn;
+      mat = resolveMaterial(sc, mat, ac);
+    } else {
+      gn = normalize(inst.normalXfm * gn);
+      sn = normalize(inst.normalXfm * sn);
+    }
     f3 color = materialColor(mat);
     f3 shadedColor(0.f);
     f3 viewDir = -ray.dir;
@@ -1682,8 +1878,11 @@ HitRec intersectAll(const Scene &sc, const Ray &ray, LCG &rnd, Counters &c, unsi
   Ray r = ray;
   SurfHit hr = traceSurfaces(sc, r, c);
   while (hr.hit) {
+    // intersectSurfaces<EvalOpacity>: attributes at the hit, hit
+    // attributes zero (renderer/common.h:1502-1543)
     const OrMaterial &mat = S.surfMaterial[hitSurface(S, hr)];
-    float opacity = materialOpacity(mat);
+    float opacity = S.surfAttr ? materialOpacity(resolveMaterial(sc, mat, hitAttrCtx(sc, hr)))
+                               : materialOpacity(mat);
     float u = rnd();
     if (u > opacity) {
       f3 hitPos = r.ori + hr.t * r.dir;
@@ -1770,6 +1969,7 @@ void shade(const Scene &sc, const OrRenderer &R, const OrFrame &F, LCG &rnd, con
     float eps;
     f3 viewDir = -normalize(ray.dir);
     const OrMaterial *mat = nullptr;
+    OrMaterial resolved;
     if (hitRec.volumeHit) {
       const VolHit &hv = hitRec.volume;
       const Inst &inst = sc.insts[hv.inst];
@@ -1802,10 +2002,24 @@ void shade(const Scene &sc, const OrRenderer &R, const OrFrame &F, LCG &rnd, con
       mat = &S.surfMaterial[hitSurface(S, hr)];
       gn = hitNormal(sc, hr);
       sn = gn;
+      AttrCtx ac;
+      if (S.surfAttr) {
+        ac = hitAttrCtx(sc, hr);
+        sn = shadingNormal(*ac.sa, ac.primID, hr.u, hr.v, gn);
+        ac.worldPos = hitPos;
+        ac.worldNormal = gn;
+        ac.objectPos = hr.isect_pos;
+      }
       gn = normalize(inst.normalXfm * gn);
       sn = normalize(inst.normalXfm * sn);
       sn = faceforward(sn, viewDir, gn);
       gn = faceforward(gn, viewDir, gn);
+      if (S.surfAttr) {
+        // the material's looked-up parameters (Pathtrace_impl.cpp:255-270)
+        ac.objectNormal = gn;
+        resolved = resolveMaterial(sc, *mat, ac);
+        mat = &resolved;
+      }
       color = materialColor(*mat);
       if (bounceID == 0) result.depth = hr.t;
     }
@@ -2137,9 +2351,43 @@ void makeHdriCdf(const OrLight &L, Hdri &h) {
   h.toLocal[8] = (float)((a[0] * a[4] - a[3] * a[1]) / det);
 }
 
+// imageSamplerUpdateData (scene/surface/material/sampler/common.h:27-60):
+// every image format as RGBA8, missing channels 0 and alpha 1; floats
+// clamped to [0, 1], times 255, truncated (as cvt_uint32, frame/common.h:
+// 31-48, converts); sRGB texels decoded with the sRGB transfer function.
+std::vector<uint8_t> samplerTexels(const OrSampler &sp) {
+  const size_t n = size_t(sp.dims[0]) * sp.dims[1] * sp.dims[2];
+  std::vector<uint8_t> out(4 * n);
+  auto cv = [](float f) { return (uint8_t)(255.f * std::min(std::max(f, 0.f), 1.f)); };
+  for (size_t i = 0; i < n; ++i) {
+    uint8_t *o = &out[4 * i];
+    o[0] = o[1] = o[2] = 0;
+    o[3] = 255;
+    const int c = sp.imageComps;
+    if (sp.imageType == OR_IMG_FLOAT) {
+      const float *p = (const float *)sp.image + c * i;
+      for (int k = 0; k < c; ++k) o[k] = cv(p[k]);
+    } else if (sp.imageType == OR_IMG_UNORM8) {
+      const uint8_t *p = (const uint8_t *)sp.image + c * i;
+      for (int k = 0; k < c; ++k) o[k] = p[k];
+    } else {
+      const uint8_t *p = (const uint8_t *)sp.image + 4 * i;
+      for (int k = 0; k < 3; ++k) {
+        const float x = p[k] / 255.f;
+        o[k] = cv(x <= 0.04045f ? x / 12.92f : std::pow((x + 0.055f) / 1.055f, 2.4f));
+      }
+      o[3] = p[3];
+    }
+  }
+  return out;
+}
+
 Scene *commit(const OrScene *s) {
   auto *sc = new Scene;
   sc->src = s;
+  sc->texels.resize(s->numSamplers);
+  for (int i = 0; i < s->numSamplers; ++i)
+    if (s->samplers[i].type <= OR_SAMP_IMAGE3D) sc->texels[i] = samplerTexels(s->samplers[i]);
   sc->hdri.resize(s->numLights);
   for (int i = 0; i < s->numLights; ++i)
     if (s->lights[i].type == 4) makeHdriCdf(s->lights[i], sc->hdri[i]);

@@ -33,7 +33,114 @@ class OrMaterial(ctypes.Structure):
                 ("metallic", c_float), ("roughness", c_float), ("ior", c_float),
                 ("clearcoat", c_float), ("clearcoatRoughness", c_float), ("transmission", c_float),
                 ("sheenColor", c_float * 3), ("sheenRoughness", c_float), ("alphaMode", c_int32),
-                ("alphaCutoff", c_float)]
+                ("alphaCutoff", c_float), ("src", c_int32 * 4)]
+
+
+class OrAttr(ctypes.Structure):
+    _fields_ = [("data", c_void_p), ("len", c_uint32), ("comps", c_int32), ("fixedBits", c_int32)]
+
+
+class OrSurfAttr(ctypes.Structure):
+    _fields_ = [("index", UP), ("vertexNormal", FP), ("numVertexNormals", c_uint32),
+                ("fvNormal", c_int32), ("vertex", OrAttr * 5), ("faceVarying", OrAttr * 5),
+                ("primitive", OrAttr * 5), ("uniform", (c_float * 4) * 5), ("uniformMask", c_uint32),
+                ("isTriangle", c_int32)]
+
+
+class OrSampler(ctypes.Structure):
+    _fields_ = [("type", c_int32), ("inAttribute", c_int32), ("linear", c_int32),
+                ("wrap", c_int32 * 3), ("dims", c_int32 * 3), ("image", c_void_p),
+                ("imageType", c_int32), ("imageComps", c_int32), ("prim", OrAttr),
+                ("primOffset", c_uint32), ("inXfm", c_float * 16), ("inOffset", c_float * 4),
+                ("outXfm", c_float * 16), ("outOffset", c_float * 4)]
+
+
+ATTR_NAMES = ["attribute0", "attribute1", "attribute2", "attribute3", "color", "worldPosition",
+              "worldNormal", "objectPosition", "objectNormal"]
+
+
+def attribute_id(name):
+    """toAttribute (scene/surface/common.h:13-37); -1 for none / unknown."""
+    return ATTR_NAMES.index(name) if name in ATTR_NAMES else -1
+
+
+def _attr(arr, keep):
+    """An OrAttr over a numpy array of float32 or uint8 / uint16 elements
+    (1-D: one component, 2-D: the last axis)."""
+    a = OrAttr()
+    if arr is None:
+        return a
+    x = np.ascontiguousarray(arr)
+    keep.append(x)
+    a.data = x.ctypes.data
+    a.len = x.shape[0]
+    a.comps = 1 if x.ndim == 1 else x.shape[-1]
+    a.fixedBits = {np.dtype(np.float32): 0, np.dtype(np.uint8): 8, np.dtype(np.uint16): 16}[x.dtype]
+    return a
+
+
+def _uniform4(v):
+    v = [float(t) for t in (v if isinstance(v, (list, tuple, np.ndarray)) else [v])]
+    return v + [0.0, 0.0, 0.0, 1.0][len(v):]
+
+
+def surface_attributes(s, keep):
+    """The OrSurfAttr of a surface dict ("normals", "attributes",
+    "faceVarying", "primitive", "uniform"); None when it has none."""
+    keys = ("normals", "attributes", "faceVarying", "primitive", "uniform")
+    sa = OrSurfAttr()
+    tri = s.get("geometry", "triangle") == "triangle"
+    sa.isTriangle = 1 if tri else 0
+    if tri:
+        idx = np.ascontiguousarray(np.asarray(s["indices"], np.uint32).reshape(-1))
+        keep.append(idx)
+        sa.index = idx.ctypes.data_as(UP)
+        if "normals" in s:
+            n = np.ascontiguousarray(np.asarray(s["normals"], np.float32).reshape(-1, 3))
+            keep.append(n)
+            sa.vertexNormal = fptr(n)
+            sa.numVertexNormals = len(n)
+        for key, field in (("attributes", "vertex"), ("faceVarying", "faceVarying"),
+                           ("primitive", "primitive")):
+            for name, arr in s.get(key, {}).items():
+                getattr(sa, field)[ATTR_NAMES.index(name)] = _attr(arr, keep)
+    for name, v in s.get("uniform", {}).items():
+        k = ATTR_NAMES.index(name)
+        sa.uniform[k] = (c_float * 4)(*_uniform4(v))
+        sa.uniformMask |= 1 << k
+    return sa, any(k in s for k in keys)
+
+
+def sampler_struct(d, keep):
+    """An OrSampler from a sampler dict (the keys the scene builder takes)."""
+    sp = OrSampler()
+    kind = d["type"]
+    sp.type = {"image1D": 0, "image2D": 1, "image3D": 2, "transform": 3, "primitive": 4}[kind]
+    ia = attribute_id(d.get("inAttribute", "attribute0"))
+    sp.inAttribute = ia if ia >= 0 else 15
+    sp.linear = 0 if d.get("filter", "linear") == "nearest" else 1
+    wm = {"repeat": 1, "mirrorRepeat": 2}
+    sp.wrap = (c_int32 * 3)(*[wm.get(d.get(f"wrapMode{k}", "clampToEdge"), 0) for k in (1, 2, 3)])
+    eye = [1.0 if i % 5 == 0 else 0.0 for i in range(16)]
+    sp.inXfm = (c_float * 16)(*[float(x) for x in d.get("inTransform", eye)])
+    sp.outXfm = (c_float * 16)(*[float(x) for x in d.get("outTransform", eye)])
+    sp.inOffset = (c_float * 4)(*[float(x) for x in d.get("inOffset", [0, 0, 0, 0])])
+    sp.outOffset = (c_float * 4)(*[float(x) for x in d.get("outOffset", [0, 0, 0, 0])])
+    sp.dims = (c_int32 * 3)(1, 1, 1)
+    if kind == "primitive":
+        sp.prim = _attr(d["array"], keep)
+        sp.primOffset = int(d.get("offset", 0))
+    elif kind != "transform":
+        img = np.ascontiguousarray(d["image"])
+        keep.append(img)
+        axes = {"image1D": 1, "image2D": 2, "image3D": 3}[kind]
+        shape = img.shape[:axes][::-1]  # x fastest
+        sp.dims = (c_int32 * 3)(*(list(shape) + [1] * (3 - axes)))
+        sp.image = img.ctypes.data
+        sp.imageComps = 1 if img.ndim == axes else img.shape[-1]
+        srgb = d.get("srgb", False)
+        sp.imageType = 0 if img.dtype == np.float32 else (2 if srgb else 1)
+    return sp
 
 
 class OrVolume(ctypes.Structure):
@@ -54,7 +161,8 @@ class OrIso(ctypes.Structure):
 
 
 class OrInstance(ctypes.Structure):
-    _fields_ = [("xfm", c_float * 12), ("group", c_int32), ("userID", c_uint32)]
+    _fields_ = [("xfm", c_float * 12), ("group", c_int32), ("userID", c_uint32),
+                ("attr", (c_float * 4) * 5), ("attrMask", c_uint32)]
 
 
 def _linear32(m, v):
@@ -85,7 +193,8 @@ class OrScene(ctypes.Structure):
                 ("numPrims", c_int32), ("prims", FP), ("primKind", ctypes.POINTER(c_int32)),
                 ("primSurface", UP), ("triNormalFrom", ctypes.POINTER(c_int32)),
                 ("numIsos", c_int32), ("isos", ctypes.POINTER(OrIso)),
-                ("isoFields", ctypes.POINTER(OrVolume))]
+                ("isoFields", ctypes.POINTER(OrVolume)), ("surfAttr", ctypes.POINTER(OrSurfAttr)),
+                ("numSamplers", c_int32), ("samplers", ctypes.POINTER(OrSampler))]
 
 
 class OrCamera(ctypes.Structure):
@@ -170,22 +279,40 @@ def farr(n, vals):
     return (c_float * n)(*[float(v) for v in vals])
 
 
-def material(m):
+def material(m, samplers=None, keep=None):
+    """An OrMaterial; a parameter given as an attribute name or as
+    {"sampler": {...}} sets its source (the sampler appended to
+    `samplers`) and keeps the parameter's default value."""
     om = OrMaterial()
-    om.opacity = float(m.get("opacity", 1.0))
+    om.src = (c_int32 * 4)(-1, -1, -1, -1)
+
+    def param(name, slot, default):
+        v = m.get(name, default)
+        if isinstance(v, dict):
+            samplers.append(sampler_struct(v["sampler"], keep))
+            om.src[slot] = 16 + len(samplers) - 1
+            return default
+        if isinstance(v, str):
+            a = attribute_id(v)
+            if a >= 0:
+                om.src[slot] = a
+            return default
+        return v
+
+    om.opacity = float(param("opacity", 1, 1.0))
     mode = m.get("alphaMode", "opaque")
     om.alphaMode = {"opaque": 0, "blend": 1, "mask": 2}[mode]
     om.alphaCutoff = float(m.get("alphaCutoff", 0.5))
     if m["type"] == "matte":
         om.type = MATTE
-        c = m.get("color", [1, 1, 1])
+        c = param("color", 0, [1, 1, 1])
         om.baseColor = farr(3, c[:3])
     else:
         om.type = PBR
-        c = m.get("baseColor", [1, 1, 1])
+        c = param("baseColor", 0, [1, 1, 1])
         om.baseColor = farr(3, c[:3])
-        om.metallic = float(m.get("metallic", 1.0))
-        om.roughness = float(m.get("roughness", 1.0))
+        om.metallic = float(param("metallic", 2, 1.0))
+        om.roughness = float(param("roughness", 3, 1.0))
         om.ior = float(m.get("ior", 1.5))
         om.clearcoat = float(m.get("clearcoat", 0.0))
         om.clearcoatRoughness = float(m.get("clearcoatRoughness", 0.0))
@@ -261,10 +388,21 @@ class Scene:
         if scene.get("surfaces") or scene.get("volumes") or scene.get("lights"):
             groups.append((scene.get("surfaces", []), scene.get("volumes", []),
                            scene.get("lights", []), [1, 0, 0, 0, 1, 0, 0, 0, 1, 0, 0, 0]))
+        inst_attrs = [{}] if groups else []
         for inst in scene.get("instances", []):
             groups.append((inst.get("surfaces", []), inst.get("volumes", []),
                            inst.get("lights", []), inst["transform"]))
+            inst_attrs.append(inst.get("attributes", {}))
         verts, tsurf, tprim, mats, vols, ogroups, oinsts, lights = [], [], [], [], [], [], [], []
+        sattrs, samplers, any_attr = [], [], False
+
+        def add_material(s):
+            nonlocal any_attr
+            sa, has = surface_attributes(s, self._keep)
+            om = material(s["material"], samplers, self._keep)
+            sattrs.append(sa)
+            any_attr = any_attr or has or any(x != -1 for x in om.src)
+            mats.append(om)
         aps, akind, asurf = [], [], []
         nfrom, has_quads = [], False
         isos, iso_fields = [], []
@@ -290,7 +428,7 @@ class Scene:
                     oi.numValues = len(vals)
                     oi.values = fptr(vals)
                     oi.surface = len(mats)
-                    mats.append(material(s["material"]))
+                    add_material(s)
                     iso_fields.append(ov)
                     isos.append(oi)
                     continue
@@ -301,7 +439,7 @@ class Scene:
                     akind.append(np.full(len(q), {"sphere": 0, "cone": 1, "cylinder": 2}[kind],
                                          np.int32))
                     asurf.append(np.full(len(q), len(mats), np.uint32))
-                    mats.append(material(s["material"]))
+                    add_material(s)
                     nap += len(q)
                     continue
                 v = np.asarray(s["vertices"], np.float32)
@@ -318,7 +456,7 @@ class Scene:
                     nfrom.append(np.full(len(t), -1, np.int64))
                 verts.append(v[t].reshape(-1, 9))
                 sid = len(mats)
-                mats.append(material(s["material"]))
+                add_material(s)
                 tsurf.append(np.full(len(t), sid, np.uint32))
                 tprim.append(np.arange(len(t), dtype=np.uint32))
                 ntri += len(t)
@@ -350,6 +488,11 @@ class Scene:
             oi.xfm = farr(12, xfm)
             oi.group = gi
             oi.userID = 0xffffffff
+            for name, v in inst_attrs[gi].items():
+                k = ATTR_NAMES.index(name)
+                oi.attr[k] = (c_float * 4)(*_uniform4(v))
+                oi.attrMask |= 1 << k
+                any_attr = True
             oinsts.append(oi)
             lin = np.asarray(xfm, np.float64)[:9].reshape(3, 3).T  # column-major -> matrix
             tr = np.asarray(xfm, np.float32)[9:12]
@@ -406,7 +549,13 @@ class Scene:
         self.lights = (OrLight * max(1, len(lights)))(*lights)
         objid = np.zeros(max(1, len(mats)), np.uint32)
         self._keep.append(objid)
+        self.sattrs = (OrSurfAttr * max(1, len(sattrs)))(*sattrs)
+        self.samplers = (OrSampler * max(1, len(samplers)))(*samplers)
         sc = OrScene()
+        if any_attr:
+            sc.surfAttr = self.sattrs
+            sc.numSamplers = len(samplers)
+            sc.samplers = self.samplers
         sc.numTriangles = len(tri)
         sc.triVerts = fptr(tri)
         sc.triSurface = ts.ctypes.data_as(UP)

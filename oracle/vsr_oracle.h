@@ -36,7 +36,50 @@ typedef struct OrMaterial {
   float sheenRoughness;
   int32_t alphaMode;
   float alphaCutoff;
+  int32_t src[4];           /* color, opacity, metallic, roughness: -1 the value,
+                               0..8 an attribute (OR_ATTR_*), 16 + k sampler k */
 } OrMaterial;
+
+/* Attributes: attribute0..3, color, then the hit's world position, world
+   normal, object position and object normal (dco::Attribute). */
+enum { OR_ATTR_COLOR = 4, OR_ATTR_WORLD_POS = 5, OR_ATTR_WORLD_NORMAL = 6,
+       OR_ATTR_OBJECT_POS = 7, OR_ATTR_OBJECT_NORMAL = 8, OR_ATTR_NONE = 15 };
+
+typedef struct OrAttr {
+  const void *data;         /* len elements of comps float32, or unorm (fixedBits 8 / 16) */
+  uint32_t len;
+  int32_t comps;            /* 0 = absent */
+  int32_t fixedBits;
+} OrAttr;
+
+/* A surface's geometry attributes (triangles: vertex, face-varying and
+   per-primitive arrays, vertex normals; every kind: uniform values). */
+typedef struct OrSurfAttr {
+  const uint32_t *index;    /* triangles: 3 vertex indices per primitive, or null */
+  const float *vertexNormal;
+  uint32_t numVertexNormals;
+  int32_t fvNormal;         /* the geometry has face-varying normals */
+  OrAttr vertex[5], faceVarying[5], primitive[5];
+  float uniform[5][4];
+  uint32_t uniformMask;
+  int32_t isTriangle;
+} OrSurfAttr;
+
+enum { OR_SAMP_IMAGE1D = 0, OR_SAMP_IMAGE2D = 1, OR_SAMP_IMAGE3D = 2, OR_SAMP_TRANSFORM = 3,
+       OR_SAMP_PRIMITIVE = 4 };
+enum { OR_IMG_FLOAT = 0, OR_IMG_UNORM8 = 1, OR_IMG_SRGB8 = 2 };
+
+typedef struct OrSampler {
+  int32_t type, inAttribute, linear;
+  int32_t wrap[3];          /* 0 clampToEdge, 1 repeat, 2 mirrorRepeat */
+  int32_t dims[3];          /* texels per axis (1 past the image's dimension) */
+  const void *image;        /* image samplers: dims[0] * dims[1] * dims[2] texels */
+  int32_t imageType;        /* OR_IMG_* */
+  int32_t imageComps;       /* 1..4 (sRGB: 4) */
+  OrAttr prim;              /* primitive sampler */
+  uint32_t primOffset;
+  float inXfm[16], inOffset[4], outXfm[16], outOffset[4];
+} OrSampler;
 
 /* structuredRegular field + transferFunction1D volume. */
 typedef struct OrVolume {
@@ -71,6 +114,8 @@ typedef struct OrInstance {
   float xfm[12];            /* column-major 3x4 affine: 3 columns + translation */
   int32_t group;
   uint32_t userID;
+  float attr[5][4];         /* uniform attributes */
+  uint32_t attrMask;
 } OrInstance;
 
 typedef struct OrLight {
@@ -120,6 +165,9 @@ typedef struct OrScene {
   int32_t numIsos;
   const OrIso *isos;
   const OrVolume *isoFields;     /* one per iso-surface */
+  const OrSurfAttr *surfAttr;    /* per surface, or null: no attributes in the scene */
+  int32_t numSamplers;
+  const OrSampler *samplers;
 } OrScene;
 
 typedef struct OrCamera {

@@ -1230,3 +1230,69 @@ def test_axis_parallel_rays(pkg, device, oracle, renderer):
     assert np.allclose(gpu["depth"][hit], 10.0, rtol=1e-5)
     d = np.abs(gpu["color"] - F.color).max(axis=-1)
     assert float((d <= 1e-3).mean()) >= 0.99, float((d <= 1e-3).mean())
+
+
+def textured_spheres(pkg, res=96, spp=4, renderer="pathtrace"):
+    """The config-1 sphere set with geometry attributes and samplers:
+    smooth vertex normals on every sphere, vertex colours read through the
+    "color" attribute on every second sphere, a roughness image1D sampler
+    on attribute0 (the vertex height) on every third, and a nearest-filtered
+    image2D checker repeated over the ground through per-vertex texture
+    coordinates (attribute0)."""
+    sc = small_spheres(pkg, res=res, spp=spp, renderer=renderer)
+    rough = {"type": "image1D", "image": np.linspace(0.05, 0.95, 16, dtype=np.float32),
+             "inAttribute": "attribute0", "filter": "linear"}
+    for k, s in enumerate(sc["surfaces"][:-1]):
+        v = np.asarray(s["vertices"], np.float32)
+        c = v.mean(axis=0)
+        n = (v - c) / np.linalg.norm(v - c, axis=1, keepdims=True)
+        s["normals"] = n.astype(np.float32)
+        h = ((v[:, 1] - v[:, 1].min()) / max(float(np.ptp(v[:, 1])), 1e-6)).astype(np.float32)
+        s["attributes"] = {"attribute0": h}
+        if k % 2 == 0:
+            s["attributes"]["color"] = np.concatenate(
+                [0.5 + 0.5 * n, np.ones((len(n), 1), np.float32)], axis=1).astype(np.float32)
+            s["material"] = dict(s["material"])
+            key = "color" if s["material"]["type"] == "matte" else "baseColor"
+            s["material"][key] = "color"
+        if k % 3 == 0 and s["material"]["type"] == "physicallyBased":
+            s["material"] = dict(s["material"], roughness={"sampler": rough})
+    ground = sc["surfaces"][-1]
+    gv = np.asarray(ground["vertices"], np.float32)
+    ground["attributes"] = {"attribute0": (gv[:, [0, 2]] / 8.0).astype(np.float32)}
+    chk = np.indices((8, 8)).sum(axis=0) % 2
+    img = np.where(chk[..., None] == 1, [0.9, 0.85, 0.8], [0.2, 0.25, 0.3]).astype(np.float32)
+    ground["material"] = {"type": "matte", "color": {"sampler": {
+        "type": "image2D", "image": img, "filter": "nearest", "wrapMode1": "repeat",
+        "wrapMode2": "repeat"}}}
+    return sc
+
+
+def test_raycast_textured(pkg, device, oracle):
+    """Geometry attributes, vertex normals and samplers in the raycast
+    renderer (getAttributes, getNormals' vertex normals, image1D / image2D
+    samplers, material parameters from attributes)."""
+    sc = textured_spheres(pkg, res=128, renderer="raycast")
+    gpu = render_gpu(pkg, device, sc)
+    _, F = render_oracle(oracle, sc)
+    _, P = render_oracle(oracle, small_spheres(pkg, res=128, renderer="raycast"))
+    assert gpu["errorFlags"] == 0
+    assert float(np.abs(F.color - P.color).max()) > 0.1  # the attributes change the image
+    good, frac = raycast_ok(gpu, F)
+    assert good, frac
+    ad = np.abs(gpu["albedo"] - F.albedo).max(axis=-1)
+    assert float((ad <= 1e-4).mean()) >= 0.999
+
+
+@pytest.mark.parametrize("wavefront", [True, False])
+def test_pathtrace_textured_same_stream(pkg, device, oracle, wavefront):
+    """The same world in the path tracer, same stream as the oracle (frames
+    with attributes run the megakernel in either execution mode)."""
+    sc = textured_spheres(pkg, res=96, spp=8)
+    sc["renderer"]["wavefront"] = wavefront
+    gpu = render_gpu(pkg, device, sc)
+    _, F = render_oracle(oracle, sc)
+    assert gpu["errorFlags"] == 0
+    assert not np.isnan(gpu["color"]).any()
+    d = np.abs(gpu["color"][..., :3] - F.color[..., :3]).max(axis=-1)
+    assert float((d <= 1e-3).mean()) >= 0.97, float((d <= 1e-3).mean())

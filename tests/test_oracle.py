@@ -643,6 +643,163 @@ def test_hdri_pathtrace_closed_form(oracle):
     assert np.all(np.abs(mean - expect) <= 5 * np.sqrt(var / n) + 1e-4 * expect), (mean, expect)
 
 
+def _tri_scene(material, extra=None, light=(0.0, 0.0, -1.0), renderer="raycast"):
+    """One large triangle in z = 0 seen from above by an orthographic
+    camera, lit straight down (irradiance 2), ambient 0.2."""
+    v = np.array([[-6.0, -6.0, 0.0], [6.0, -6.0, 0.0], [-6.0, 6.0, 0.0]], np.float32)
+    surf = {"vertices": v, "indices": np.array([[0, 1, 2]], np.uint32), "material": material}
+    surf.update(extra or {})
+    return {
+        "surfaces": [surf], "volumes": [],
+        "lights": [{"direction": list(light), "irradiance": 2.0}],
+        "camera": {"type": "orthographic", "position": [0.0, 0.0, 10.0],
+                   "direction": [0.0, 0.0, -1.0], "up": [0.0, 1.0, 0.0], "height": 8.0,
+                   "aspect": 1.0},
+        "renderer": {"type": renderer, "ambientRadiance": 0.2, "background": [0, 0, 0, 1]},
+        "frame": {"size": (16, 16)},
+    }
+
+
+def _pixel_bary():
+    """Pixel centres of the 16 x 16 view of _tri_scene and their
+    barycentrics (u of vertex 1, v of vertex 2); mask: inside the triangle."""
+    xs = ((np.arange(16) + 0.5) / 16 - 0.5) * 8.0
+    X, Y = np.meshgrid(xs, xs)
+    u = (X + 6.0) / 12.0
+    v = (Y + 6.0) / 12.0
+    return X, Y, u, v, (u + v) <= 1.0
+
+
+def test_vertex_colors_closed_form(oracle):
+    """A matte material whose color is the "color" attribute: the vertex
+    colours interpolated with the hit's barycentrics,
+    (1 - u - v) c0 + u c1 + v c2, shade as c/pi E + c ambient."""
+    cols = np.array([[1.0, 0.0, 0.0, 1.0], [0.0, 1.0, 0.0, 1.0], [0.0, 0.0, 1.0, 1.0]], np.float32)
+    sc = _tri_scene({"type": "matte", "color": "color"}, {"attributes": {"color": cols}})
+    S = oracle.Scene(sc)
+    F = oracle.Frame(16, 16)
+    oracle.render(S, F)
+    X, Y, u, v, inside = _pixel_bary()
+    c = (1 - u - v)[..., None] * cols[0, :3] + u[..., None] * cols[1, :3] + v[..., None] * cols[2, :3]
+    expect = c / math.pi * 2.0 + c * 0.2
+    assert inside.sum() > 100
+    assert np.allclose(F.color[inside][:, :3], expect[inside], atol=1e-5)
+    assert np.allclose(F.albedo[inside], c[inside], atol=1e-6)
+
+
+def test_vertex_normals_shade(oracle):
+    """Vertex normals tilted towards +x at every corner: the shading normal
+    is the interpolated, normalised vertex normal, so the light straight
+    down gives cos = n.z / |n| while the geometric normal stays (0, 0, 1)."""
+    n = np.array([[0.6, 0.0, 0.8]] * 3, np.float32)
+    sc = _tri_scene({"type": "matte", "color": [0.5, 0.5, 0.5]}, {"normals": n})
+    S = oracle.Scene(sc)
+    F = oracle.Frame(16, 16)
+    oracle.render(S, F)
+    X, Y, u, v, inside = _pixel_bary()
+    expect = 0.5 / math.pi * 2.0 * 0.8 + 0.5 * 0.2
+    assert np.allclose(F.color[inside][:, :3], expect, atol=1e-5)
+    assert np.allclose(F.normal[inside], [0.0, 0.0, 1.0], atol=1e-6)
+
+
+@pytest.mark.parametrize("filt,wrap", [("nearest", "clampToEdge"), ("linear", "clampToEdge"),
+                                       ("nearest", "repeat"), ("nearest", "mirrorRepeat")])
+def test_image2d_sampler(oracle, filt, wrap):
+    """An image2D sampler on attribute0 (per-vertex texture coordinates
+    (0,0), (2,0), (0,2)), through inTransform (scale 0.5 in u: so the
+    coordinates reach 1 in u and 2 in v) and outOffset: texels as RGBA8
+    (float texels x 255, truncated), nearest or bilinear with texel centres
+    at (i + 0.5) / n, the address mode on texel indices."""
+    img = np.array([[[0.1, 0.2, 0.3], [0.9, 0.8, 0.7]],
+                    [[0.5, 0.0, 1.0], [0.25, 0.75, 0.5]]], np.float32)  # [y][x]
+    tc = np.array([[0.0, 0.0], [2.0, 0.0], [0.0, 2.0]], np.float32)
+    inx = [0.5, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1]
+    samp = {"type": "image2D", "image": img, "filter": filt, "wrapMode1": wrap, "wrapMode2": wrap,
+            "inTransform": inx, "outOffset": [0.01, 0.0, 0.0, 0.0]}
+    sc = _tri_scene({"type": "matte", "color": {"sampler": samp}}, {"attributes": {"attribute0": tc}})
+    S = oracle.Scene(sc)
+    F = oracle.Frame(16, 16)
+    oracle.render(S, F)
+    X, Y, u, v, inside = _pixel_bary()
+    tu, tv = 0.5 * (2.0 * u), 2.0 * v
+    q = (np.floor(255.0 * np.clip(img, 0, 1)) / 255.0).astype(np.float64)
+
+    def wrapi(i, n):
+        if wrap == "repeat":
+            return np.mod(i, n)
+        if wrap == "mirrorRepeat":
+            m = np.mod(i, 2 * n)
+            return np.where(m < n, m, 2 * n - 1 - m)
+        return np.clip(i, 0, n - 1)
+
+    if filt == "nearest":
+        c = q[wrapi(np.floor(tv * 2).astype(int), 2), wrapi(np.floor(tu * 2).astype(int), 2)]
+    else:
+        x, y = tu * 2 - 0.5, tv * 2 - 0.5
+        x0, y0 = np.floor(x), np.floor(y)
+        fx, fy = (x - x0)[..., None], (y - y0)[..., None]
+        i0, i1 = wrapi(x0.astype(int), 2), wrapi(x0.astype(int) + 1, 2)
+        j0, j1 = wrapi(y0.astype(int), 2), wrapi(y0.astype(int) + 1, 2)
+        r0 = q[j0, i0] + fx * (q[j0, i1] - q[j0, i0])
+        r1 = q[j1, i0] + fx * (q[j1, i1] - q[j1, i0])
+        c = r0 + fy * (r1 - r0)
+    c = c + np.array([0.01, 0.0, 0.0])
+    expect = c / math.pi * 2.0 + c * 0.2
+    assert np.allclose(F.color[inside][:, :3], expect[inside], atol=2e-5)
+
+
+def test_primitive_transform_and_instance_attributes(oracle):
+    """Per-primitive colours (primitive.color), a transform sampler mapping
+    attribute1 to the colour (outTransform halves it, outOffset adds 0.1),
+    and an instance's uniform colour behind a geometry without colours."""
+    X, Y, u, v, inside = _pixel_bary()
+    # primitive colour of the only triangle
+    sc = _tri_scene({"type": "matte", "color": "color"},
+                    {"primitive": {"color": np.array([[0.2, 0.4, 0.6]], np.float32)}})
+    F = oracle.Frame(16, 16)
+    oracle.render(oracle.Scene(sc), F)
+    c = np.array([0.2, 0.4, 0.6])
+    assert np.allclose(F.color[inside][:, :3], c / math.pi * 2 + c * 0.2, atol=1e-5)
+    # transform sampler on a per-vertex attribute1
+    a1 = np.array([[1.0, 0.0, 0.0], [0.0, 1.0, 0.0], [0.0, 0.0, 1.0]], np.float32)
+    xf = [0.5, 0, 0, 0, 0, 0.5, 0, 0, 0, 0, 0.5, 0, 0, 0, 0, 1]
+    samp = {"type": "transform", "inAttribute": "attribute1", "outTransform": xf,
+            "outOffset": [0.1, 0.1, 0.1, 0.0]}
+    sc = _tri_scene({"type": "matte", "color": {"sampler": samp}}, {"attributes": {"attribute1": a1}})
+    F = oracle.Frame(16, 16)
+    oracle.render(oracle.Scene(sc), F)
+    c = 0.5 * np.stack([1 - u - v, u, v], -1) + 0.1
+    assert np.allclose(F.color[inside][:, :3], (c / math.pi * 2 + c * 0.2)[inside], atol=1e-5)
+    # instance uniform colour
+    sc = _tri_scene({"type": "matte", "color": "color"})
+    inst = {"transform": [1, 0, 0, 0, 1, 0, 0, 0, 1, 0, 0, 0], "surfaces": sc.pop("surfaces"),
+            "attributes": {"color": [0.7, 0.3, 0.1, 1.0]}}
+    sc["surfaces"] = []
+    sc["instances"] = [inst]
+    F = oracle.Frame(16, 16)
+    oracle.render(oracle.Scene(sc), F)
+    c = np.array([0.7, 0.3, 0.1])
+    assert np.allclose(F.color[inside][:, :3], c / math.pi * 2 + c * 0.2, atol=1e-5)
+
+
+def test_opacity_from_attribute_blends(oracle):
+    """alphaMode blend with the opacity from attribute0's x (0.25 at every
+    vertex) and the colour's alpha (vertex colour alpha 0.8): the raycast
+    composites 0.2 of the surface over the background."""
+    a0 = np.full((3, 1), 0.25, np.float32)
+    cols = np.tile(np.array([[0.5, 0.5, 0.5, 0.8]], np.float32), (3, 1))
+    sc = _tri_scene({"type": "matte", "color": "color", "opacity": "attribute0",
+                     "alphaMode": "blend"}, {"attributes": {"attribute0": a0, "color": cols}})
+    sc["renderer"]["background"] = [0.0, 0.0, 1.0, 1.0]
+    F = oracle.Frame(16, 16)
+    oracle.render(oracle.Scene(sc), F)
+    X, Y, u, v, inside = _pixel_bary()
+    a = 0.25 * 0.8
+    shaded = 0.5 / math.pi * 2 + 0.5 * 0.2
+    expect = np.array([a * shaded, a * shaded, a * shaded + (1 - a) * 1.0])
+    assert np.allclose(F.color[inside][:, :3], expect, atol=1e-5)
+
+
 def test_emission_absorption_slab(oracle):
     """Constant field, TF alpha a: alpha after k steps is 1 - (1-a)^(k dt/ud)."""
     n = 16

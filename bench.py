@@ -412,9 +412,8 @@ def measure_batch_config3(pkg, dev, steps=3, num_scenes=64, profile_range=False)
         return time.perf_counter() - t
 
     sequential()  # commits, BVH builds, first-use allocations
-    # what caps batching: each frame's own device time in a sequential pass;
-    # if a frame kind already fills the GPU at its best rate, a batch can
-    # save at most the difference to that rate
+    # what caps batching: each frame's own device time in a sequential pass
+    # (the share of it with idle SMs comes from the committed profile)
     if profile_range:
         import torch
 
@@ -428,12 +427,7 @@ def measure_batch_config3(pkg, dev, steps=3, num_scenes=64, profile_range=False)
         W, H = sc["frame"]["size"]
         spp = sc["renderer"]["pixelSamples"] if sc["renderer"]["type"] == "pathtrace" else 1
         per.append((sc["renderer"]["type"], W * H * spp, dev.get_float(f, "duration.render")))
-    best = {}
-    for kind, w, t in per:
-        if t > 0:
-            best[kind] = max(best.get(kind, 0.0), w / t)
     t_seq_dev = sum(t for _, _, t in per)
-    t_ideal = sum(w / best[kind] for kind, w, t in per if t > 0)
     tune = 0
     while not dev.get_int(frames[0], "batch.tuned") and tune < 32:
         batched()
@@ -459,11 +453,12 @@ def measure_batch_config3(pkg, dev, steps=3, num_scenes=64, profile_range=False)
             "error_flags": err, "generate_s": gen_s,
             "cap_analysis": {
                 "sum_frame_device_ms": 1e3 * t_seq_dev,
-                "ideal_ms_every_frame_at_its_kinds_best_rate": 1e3 * t_ideal,
-                "max_speedup_from_filling_the_gpu": t_seq_dev / t_ideal if t_ideal else None,
-                "best_rate_mpxspp": {k: v / MPX for k, v in best.items()},
-                "how": "each frame's device time in a sequential pass; a batch can at best run "
-                       "every frame at the best rate any frame of its kind reaches alone"},
+                "sm_active_share": profiled_value("batch_config3.txt", "sm_active_share"),
+                "max_speedup_from_filling_idle_sms":
+                    profiled_value("batch_config3.txt", "max_speedup_from_filling_idle_sms"),
+                "how": "each frame's device time in a sequential pass (measured here); the share of "
+                       "that pass in which the SMs were active, time-weighted over its launches "
+                       "(ncu, profiles/batch_config3.txt): a batch can only fill the idle rest"},
             "timing": "host wall clock, first call to last frame done; synthetic seeded scenes"}
 
 

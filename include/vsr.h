@@ -129,10 +129,11 @@ VSR_API VSRArray vsrNewArray3D(VSRDevice d, const void *appMemory, VSRDataType t
    newLight/newSurface/newGroup/newInstance/newWorld/newCamera/newRenderer/
    newFrame (VisionarayDevice.cpp:125-214). Supported subtypes:
    spatial field "structuredRegular"; volume "transferFunction1D";
-   geometry "triangle"; material "matte", "physicallyBased"; light
-   "directional"; instance "transform"; camera "perspective", "matrix",
-   "orthographic", "omnidirectional"; renderer "raycast", "pathtrace",
-   "default" (= pathtrace, renderer/Renderer.cpp:144-152).
+   geometry "triangle", "quad", "sphere", "cone", "cylinder", "isosurface";
+   material "matte", "physicallyBased"; light "directional", "point",
+   "spot", "quad", "hdri"; instance "transform"; camera "perspective",
+   "matrix", "orthographic", "omnidirectional"; renderer "raycast",
+   "pathtrace", "default" (= pathtrace, renderer/Renderer.cpp:144-152).
    Unknown subtypes return NULL and report VSR_ERROR_UNKNOWN_SUBTYPE. */
 VSR_API VSRObject vsrNewSpatialField(VSRDevice d, const char *subtype);
 VSR_API VSRObject vsrNewVolume(VSRDevice d, const char *subtype);

@@ -114,13 +114,14 @@ __global__ void kGatherAnalytic(const float4 *leafTris, const float4 *src, const
   if (i >= n) return;
   const int k = __float_as_int(leafTris[3 * (size_t)i].w);
   if (k < 0 || k >= n) {  // not a valid group index: a sphere that is never hit
-    primsOut[2 * (size_t)i] = make_float4(__int_as_float(0x7fffffff), 0.f, 0.f, 0.f);
-    primsOut[2 * (size_t)i + 1] = make_float4(0.f, 0.f, 0.f, 0.f);
+    primsOut[kApStride * (size_t)i] = make_float4(__int_as_float(0x7fffffff), 0.f, 0.f, 0.f);
+    for (int c = 1; c < kApStride; ++c)
+      primsOut[kApStride * (size_t)i + c] = make_float4(0.f, 0.f, 0.f, 0.f);
     localOut[i] = 0;
     return;
   }
-  primsOut[2 * (size_t)i] = src[2 * (size_t)k];
-  primsOut[2 * (size_t)i + 1] = src[2 * (size_t)k + 1];
+  for (int c = 0; c < kApStride; ++c)
+    primsOut[kApStride * (size_t)i + c] = src[kApStride * (size_t)k + c];
   localOut[i] = (uint32_t)k | (kinds[k] << kApKindShift);
 }
 

@@ -201,9 +201,10 @@ cudaError_t buildGroupBVH(const float *v1, const float *e1, const float *e2, int
 // children. nodes4Out needs room for numNodes2 BVH4 nodes. Leaf codes and
 // the leaf-ordered triangles are unchanged. Returns the BVH4 node count in
 // *numNodes4 (synchronizes the stream).
-// Spheres, cones and cylinders in BVH leaf order: for leaf i with group
-// index k (the w of the leaf's first float4), primsOut[2i..2i+1] =
-// src[2k..2k+1] and localOut[i] = k | kinds[k] << kApKindShift.
+// Spheres, cones, cylinders and curves in BVH leaf order: for leaf i with
+// group index k (the w of the leaf's first float4), the kApStride records
+// primsOut[kApStride i ..] = src[kApStride k ..] and localOut[i] =
+// k | kinds[k] << kApKindShift.
 cudaError_t launchGatherAnalytic(const float4 *leafTris, const float4 *src, const uint32_t *kinds,
                                  int n, float4 *primsOut, uint32_t *localOut,
                                  cudaStream_t stream);

@@ -305,13 +305,135 @@ __device__ __forceinline__ float cylinderHitT(float3 ro, float3 rd, float4 A, fl
 // of hits by more than 1e-4 relative for a one-ulp change of the ray, and
 // the shifted forms none). An origin outside the bounding sphere keeps the
 // cone's cap selection exact.
+// ---------------------------------------------------------- Bezier curves
+// The cubic's point and derivative at t, as BezierCurve::f / dfdt write
+// them (DeviceCopyableObjects.h:1034-1057).
+struct Curve {
+  float3 w0, w1, w2, w3;
+  float r;
+  __device__ __forceinline__ float3 f(float t) const {
+    const float ti = 1.0f - t;
+    return ti * ti * ti * w0 + 3.0f * ti * ti * t * w1 + 3.0f * ti * t * t * w2 + t * t * t * w3;
+  }
+  __device__ __forceinline__ float3 dfdt(float t) const {
+    const float ti = 1.0f - t;
+    return -3.0f * ti * ti * w0 + 3.0f * (3.0f * t * t - 4.0f * t + 1.0f) * w1 +
+           3.0f * (2.0f - 3.0f * t) * t * w2 + 3.0f * t * t * w3;
+  }
+};
+
+__device__ __forceinline__ Curve loadCurve(const DGroup &G, int leaf) {
+  const float4 *P = G.apPrims + kApStride * (size_t)leaf;
+  const float4 a = __ldg(P), b = __ldg(P + 1), c = __ldg(P + 2), e = __ldg(P + 3);
+  Curve cv;
+  cv.w0 = f3(a.x, a.y, a.z);
+  cv.w1 = f3(b.x, b.y, b.z);
+  cv.w2 = f3(c.x, c.y, c.z);
+  cv.w3 = f3(e.x, e.y, e.z);
+  cv.r = a.w;
+  return cv;
+}
+
+// The Phantom ray-hair intersector (Reshetov and Luebke 2018) as
+// intersect(Ray, BezierCurve) writes it (DeviceCopyableObjects.h:1072-1289):
+// an early-out against a cylinder around the end points (radius: the
+// farther of the curve points at t = 1/3 and 2/3 from the axis, plus r),
+// the curve moved into the ray-centric frame (e3 = the normalised ray
+// direction, e1, e2 make_orthonormal_basis, origin at the ray's), then up
+// to 40 Newton steps on the ray / cone (here cylinder) test from one end
+// (the end the ray direction points away from), regula falsi when the step
+// changes sign (bisection every 4th step), the other end if that fails;
+// converged at |dt| < 5e-5. t is the distance along the normalised
+// direction; u the curve parameter. The RCC transform is applied as the
+// frame's transpose (its inverse).
+static __device__ __noinline__ float curveHitT(float3 o, float3 d, const Curve &c, float &uOut) {
+  auto distToAxis = [&](float3 pt) {
+    return length(cross(pt - c.w0, pt - c.w3)) / length(c.w3 - c.w0);
+  };
+  float rmax = fmaxf(distToAxis(c.f(0.33333f)), distToAxis(c.f(0.66667f))) + c.r;
+  const float3 axis = normalize(c.w3 - c.w0);
+  const float3 p0 = c.w0 - axis * c.r, p1 = c.w3 + axis * c.r;
+  {
+    const float3 ba = p1 - p0, oc = o - p0;
+    const float baba = dot(ba, ba), bard = dot(ba, d), baoc = dot(ba, oc);
+    const float k2 = baba - bard * bard;
+    const float k1 = baba * dot(oc, d) - baoc * bard;
+    const float k0 = baba * dot(oc, oc) - baoc * baoc - rmax * rmax * baba;
+    float h = k1 * k1 - k2 * k0;
+    if (h < 0.0f) return -FLT_MAX;
+    h = sqrtf(h);
+    float t = (-k1 - h) / k2;
+    const float y = baoc + t * bard;
+    bool hitCyl = y > 0.0f && y < baba;
+    if (!hitCyl) {
+      t = ((y < 0.0f ? 0.0f : baba) - baoc) / bard;
+      hitCyl = fabsf(k1 + k2 * t) < h;
+    }
+    if (!hitCyl) return -FLT_MAX;
+  }
+  float3 e1, e2;
+  const float3 e3 = normalize(d);
+  orthonormalBasis(e1, e2, e3);
+  auto rcc = [&](float3 p) {
+    const float3 q = p - o;
+    return f3(dot(e1, q), dot(e2, q), dot(e3, q));
+  };
+  Curve x;
+  x.w0 = rcc(c.w0);
+  x.w1 = rcc(c.w1);
+  x.w2 = rcc(c.w2);
+  x.w3 = rcc(c.w3);
+  x.r = c.r;
+  float tstart = dot(x.w3 - x.w0, d) > 0.0f ? 0.0f : 1.0f;
+  for (int ep = 0; ep < 2; ++ep) {
+    float t = tstart, told = 0.f, dt1 = 0.f, dt2 = 0.f;
+    for (int i = 0; i < 40; ++i) {
+      const float3 c0 = x.f(t), cd = x.dfdt(t);
+      // RayConeIntersection::intersect(r, 0) (appendix A)
+      const float r2 = c.r * c.r;
+      float ddd = cd.x * cd.x + cd.y * cd.y;
+      const float dp = c0.x * c0.x + c0.y * c0.y;
+      const float cdd = c0.x * cd.x + c0.y * cd.y;
+      const float cxd = c0.x * cd.y - c0.y * cd.x;
+      const float cc = ddd;
+      const float b = cd.z * (0.0f - cdd);
+      const float cdz2 = cd.z * cd.z;
+      ddd += cdz2;
+      const float a = 2.0f * 0.0f * cdd + cxd * cxd - ddd * r2 + dp * cdz2;
+      const float discr = b * b - a * cc;
+      const float sRoot = (b - (discr > 0.0f ? sqrtf(discr) : 0.0f)) / cc;
+      float dt = (sRoot * cd.z - cdd) / ddd;
+      if (discr > 0.0f && fabsf(dt) < 5e-5f) {
+        uOut = t;
+        return sRoot + c0.z;
+      }
+      dt = fminf(dt, 0.5f);
+      dt = fmaxf(dt, -0.5f);
+      dt1 = dt2;
+      dt2 = dt;
+      if (dt1 * dt2 < 0.0f) {
+        const float tnext = (i & 3) == 0 ? 0.5f * (told + t) : (dt2 * told - dt1 * t) / (dt2 - dt1);
+        told = t;
+        t = tnext;
+      } else {
+        told = t;
+        t += dt;
+      }
+      if (t < 0.0f || t > 1.0f) break;
+    }
+    tstart = 1.0f - tstart;
+  }
+  return -FLT_MAX;
+}
+
 __device__ __forceinline__ float analyticHitT(const DGroup &G, int leaf, uint32_t kind, float3 o,
                                               float3 d, float &u, float &v) {
-  const float4 A = __ldg(G.apPrims + 2 * (size_t)leaf);
+  const float4 A = __ldg(G.apPrims + kApStride * (size_t)leaf);
   u = 0.f;
   v = 0.f;
   if (kind == AP_SPHERE) return sphereHitT(o, d, A);
-  const float4 B = __ldg(G.apPrims + 2 * (size_t)leaf + 1);
+  if (kind == AP_CURVE) return curveHitT(o, d, loadCurve(G, leaf), u);
+  const float4 B = __ldg(G.apPrims + kApStride * (size_t)leaf + 1);
   const float3 pa = f3(A.x, A.y, A.z), pb = f3(B.x, B.y, B.z);
   const float R = 0.5f * length(pb - pa) + fmaxf(A.w, B.w);
   const float L2 = dot(d, d);
@@ -732,10 +854,13 @@ __device__ __forceinline__ float3 hitNormal(const DGroup &G, const DInstance &I,
     localRay(I, o, d, lo, ld);
     const float3 P = lo + h.t * ld;
     const uint32_t kind = __ldg(G.apLocal + h.leaf) >> kApKindShift;
-    const float4 A = __ldg(G.apPrims + 2 * (size_t)h.leaf);
+    const float4 A = __ldg(G.apPrims + kApStride * (size_t)h.leaf);
     const float3 v1 = f3(A.x, A.y, A.z);
     if (kind == AP_SPHERE) return normalize((P - v1) / A.w);
-    const float4 B = __ldg(G.apPrims + 2 * (size_t)h.leaf + 1);
+    if (kind == AP_CURVE) {  // getNormals: P minus the curve point at u (renderer/common.h:304-308)
+      return normalize(P - loadCurve(G, h.leaf).f(h.u));
+    }
+    const float4 B = __ldg(G.apPrims + kApStride * (size_t)h.leaf + 1);
     const float3 v2 = f3(B.x, B.y, B.z);
     if (kind == AP_CONE) {
       const float3 ba = v2 - v1;

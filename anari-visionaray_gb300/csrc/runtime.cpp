@@ -606,10 +606,32 @@ struct Sampler : Object {
   }
 };
 
+// An analytic primitive's box: a sphere's centre +- radius, a cone's or
+// cylinder's end points grown by their radii (get_bounds, DeviceCopyable
+// Objects.h:1009-1018), a curve's control points grown by its radius (the
+// convex hull holds the curve; the reference's tighter box, :1291-1346,
+// can drop the end points of an axis where the cubic term is zero).
+static void apBounds(const float *q, uint32_t kind, float *lo, float *hi) {
+  for (int a = 0; a < 3; ++a) {
+    lo[a] = q[a] - q[3];
+    hi[a] = q[a] + q[3];
+    if (kind == AP_CONE || kind == AP_CYLINDER) {
+      lo[a] = std::min(lo[a], q[4 + a] - q[7]);
+      hi[a] = std::max(hi[a], q[4 + a] + q[7]);
+    } else if (kind == AP_CURVE) {
+      for (int c = 1; c < 4; ++c) {
+        lo[a] = std::min(lo[a], q[4 * c + a] - q[3]);
+        hi[a] = std::max(hi[a], q[4 * c + a] + q[3]);
+      }
+    }
+  }
+}
+
 struct Geometry : Object {
   std::vector<float> v1, e1, e2;  // per triangle, float3 packed
-  // spheres, cones, cylinders: 8 floats per primitive, (p0, r0, p1, r1)
-  // (a sphere uses (center, radius) and zeros), all of kind apKind
+  // spheres, cones, cylinders, curves: kApFloats (16) floats per primitive:
+  // (p0, r0, p1, r1, 0...) (a sphere uses (center, radius) and zeros), a
+  // curve (w0, r, w1, 0, w2, 0, w3, 0); all of kind apKind
   std::vector<float> prims;
   int apKind = AP_SPHERE;
   // quads: the object-space shading normal of each tessellated triangle
@@ -709,6 +731,10 @@ struct Geometry : Object {
     }
     if (subtype == "cone" || subtype == "cylinder") {
       commitConesCylinders(subtype == "cone");
+      return;
+    }
+    if (subtype == "bezierCurve") {
+      commitCurves();
       return;
     }
     Array *pos = geto<Array>("vertex.position", VSR_ARRAY1D);
@@ -850,7 +876,7 @@ struct Geometry : Object {
       warn("'vertex.radius' shorter than the number of spheres");
       return;
     }
-    prims.assign(8 * n, 0.f);
+    prims.assign(kApFloats * n, 0.f);
     for (size_t i = 0; i < n; ++i) {
       const size_t v = idx ? idx->as<uint32_t>()[i] : i;
       if (v >= nv) {
@@ -858,10 +884,60 @@ struct Geometry : Object {
         prims.clear();
         return;
       }
-      for (int k = 0; k < 3; ++k) prims[8 * i + k] = P[3 * v + k];
-      prims[8 * i + 3] = rad ? rad->as<float>()[i] : globalRadius;
+      for (int k = 0; k < 3; ++k) prims[kApFloats * i + k] = P[3 * v + k];
+      prims[kApFloats * i + 3] = rad ? rad->as<float>()[i] : globalRadius;
     }
     valid = true;
+  }
+
+  // BezierCurve.cpp:19-100: cubic segments from vertex.position; with
+  // primitive.index (UINT32) entry i starts segments at indices[i], every
+  // 3 vertices up to indices[i + 1] (one segment for the last entry), with
+  // radius primitive.radius[i]; without it, segments start at vertex 0, 3,
+  // 6, ... (consecutive segments share an end vertex) with radius
+  // primitive.radius[start / 3]; else 'radius' (default 1). Segments that
+  // would read past the vertices are left out.
+  void commitCurves() {
+    apKind = AP_CURVE;
+    Array *pos = geto<Array>("vertex.position", VSR_ARRAY1D);
+    Array *idx = geto<Array>("primitive.index", VSR_ARRAY1D);
+    Array *rad = geto<Array>("primitive.radius", VSR_ARRAY1D);
+    if (!pos || pos->elemType != VSR_FLOAT32_VEC3) {
+      warn("missing required parameter 'vertex.position' on bezierCurve geometry");
+      return;
+    }
+    if ((idx && idx->elemType != VSR_UINT32) || (rad && rad->elemType != VSR_FLOAT32)) {
+      warn("unsupported type for 'primitive.index' or 'primitive.radius' on bezierCurve geometry");
+      return;
+    }
+    float globalRadius = 1.f;
+    getf("radius", globalRadius);
+    const float *P = pos->as<float>();
+    const size_t nv = pos->size(), nr = rad ? rad->size() : 0;
+    bool dropped = false;
+    auto add = [&](size_t j, float r) {
+      if (j + 3 >= nv) { dropped = true; return; }
+      std::vector<float> q(kApFloats, 0.f);
+      for (int c = 0; c < 4; ++c)
+        for (int a = 0; a < 3; ++a) q[4 * c + a] = P[3 * (j + c) + a];
+      q[3] = r;
+      prims.insert(prims.end(), q.begin(), q.end());
+    };
+    if (idx) {
+      const uint32_t *I = idx->as<uint32_t>();
+      const size_t n = idx->size();
+      for (size_t i = 0; i < n; ++i) {
+        const size_t first = I[i], last = i == n - 1 ? first + 3 : I[i + 1];
+        const float r = rad ? (i < nr ? rad->as<float>()[i] : globalRadius) : globalRadius;
+        for (size_t j = first; j < last; j += 3) add(j, r);
+      }
+    } else if (nv > 3) {
+      for (size_t i = 0; i < nv - 3; i += 3)
+        add(i, rad ? (i / 3 < nr ? rad->as<float>()[i / 3] : globalRadius) : globalRadius);
+    }
+    if (dropped) warn("bezierCurve segments past 'vertex.position' are left out");
+    valid = !prims.empty();
+    if (!valid) warn("bezierCurve geometry has no segments");
   }
 
   // Cone.cpp:31-82 and Cylinder.cpp:31-82: end points from vertex.position
@@ -897,7 +973,7 @@ struct Geometry : Object {
     const size_t nv = pos->size();
     const size_t n = idx ? idx->size() : nv / 2;
     const size_t nr = rad ? rad->size() : 0;
-    prims.assign(8 * n, 0.f);
+    prims.assign(kApFloats * n, 0.f);
     for (size_t i = 0; i < n; ++i) {
       const size_t a = idx ? idx->as<uint32_t>()[2 * i] : 2 * i;
       const size_t b = idx ? idx->as<uint32_t>()[2 * i + 1] : 2 * i + 1;
@@ -908,16 +984,16 @@ struct Geometry : Object {
         return;
       }
       for (int k = 0; k < 3; ++k) {
-        prims[8 * i + k] = P[3 * a + k];
-        prims[8 * i + 4 + k] = P[3 * b + k];
+        prims[kApFloats * i + k] = P[3 * a + k];
+        prims[kApFloats * i + 4 + k] = P[3 * b + k];
       }
-      prims[8 * i + 3] = rad ? rad->as<float>()[ra] : globalRadius;
-      prims[8 * i + 7] = rad ? rad->as<float>()[rb] : globalRadius;
+      prims[kApFloats * i + 3] = rad ? rad->as<float>()[ra] : globalRadius;
+      prims[kApFloats * i + 7] = rad ? rad->as<float>()[rb] : globalRadius;
     }
     valid = true;
   }
   size_t numTris() const { return v1.size() / 3; }
-  size_t numAnalytic() const { return prims.size() / 8; }
+  size_t numAnalytic() const { return prims.size() / kApFloats; }
 };
 
 // matte / physicallyBased, scene/surface/material/{Matte,PBM}.cpp
@@ -1574,13 +1650,10 @@ struct World : Object {
     const int n = (int)surf.size();
     std::vector<float> v1(3 * n), e1(3 * n), e2(3 * n);
     for (int k = 0; k < n; ++k) {
-      const float *q = &prims[8 * k];
+      float blo[3], bhi[3];
+      apBounds(&prims[kApFloats * k], kinds[k], blo, bhi);
       for (int a = 0; a < 3; ++a) {
-        float lo = q[a] - q[3], hi = q[a] + q[3];
-        if (kinds[k] != AP_SPHERE) {
-          lo = std::min(lo, q[4 + a] - q[7]);
-          hi = std::max(hi, q[4 + a] + q[7]);
-        }
+        const float lo = blo[a], hi = bhi[a];
         v1[3 * k + a] = lo;
         e1[3 * k + a] = hi - lo;
         e2[3 * k + a] = a == 1 ? 0.f : hi - lo;
@@ -1590,12 +1663,12 @@ struct World : Object {
     DevBuf bv1, be1, be2;
     if (bv1.upload(v1.data(), fb, s) || be1.upload(e1.data(), fb, s) ||
         be2.upload(e2.data(), fb, s) ||
-        gg.apSrc.upload(prims.data(), (size_t)n * 2 * sizeof(float4), s) ||
+        gg.apSrc.upload(prims.data(), (size_t)n * kApStride * sizeof(float4), s) ||
         gg.apKinds.upload(kinds.data(), (size_t)n * sizeof(uint32_t), s) ||
         gg.apSurface.upload(surf.data(), (size_t)n * sizeof(uint32_t), s) ||
         gg.apNodes.alloc((size_t)std::max(n - 1, 1) * 4 * sizeof(float4)) ||
         gg.apLeaf.alloc((size_t)n * 3 * sizeof(float4)) ||
-        gg.apPrims.alloc((size_t)n * 2 * sizeof(float4)) ||
+        gg.apPrims.alloc((size_t)n * kApStride * sizeof(float4)) ||
         gg.apLocal.alloc((size_t)n * sizeof(uint32_t))) {
       dev->report(this, kind, VSR_SEVERITY_ERROR, VSR_ERROR_OUT_OF_MEMORY, "scene upload failed");
       return false;
@@ -1697,14 +1770,11 @@ struct World : Object {
           for (size_t k = 0; k < G->numAnalytic(); ++k) {
             apSurf.push_back(sid);
             apKinds.push_back((uint32_t)G->apKind);
-            const float *q = &G->prims[8 * k];
+            float blo[3], bhi[3];
+            apBounds(&G->prims[kApFloats * k], (uint32_t)G->apKind, blo, bhi);
             for (int a = 0; a < 3; ++a) {
-              lo[a] = std::min(lo[a], q[a] - q[3]);
-              hi[a] = std::max(hi[a], q[a] + q[3]);
-              if (G->apKind != AP_SPHERE) {
-                lo[a] = std::min(lo[a], q[4 + a] - q[7]);
-                hi[a] = std::max(hi[a], q[4 + a] + q[7]);
-              }
+              lo[a] = std::min(lo[a], blo[a]);
+              hi[a] = std::max(hi[a], bhi[a]);
             }
           }
           continue;
@@ -2793,7 +2863,8 @@ VSRObject vsrNewVolume(VSRDevice d, const char *s) {
 }
 VSRObject vsrNewGeometry(VSRDevice d, const char *s) {
   return newObj<Geometry>(d, VSR_GEOMETRY, s,
-                         {"triangle", "quad", "sphere", "cone", "cylinder", "isosurface"});
+                         {"triangle", "quad", "sphere", "cone", "cylinder", "isosurface",
+                          "bezierCurve"});
 }
 VSRObject vsrNewMaterial(VSRDevice d, const char *s) {
   return newObj<Material>(d, VSR_MATERIAL, s, {"matte", "physicallyBased"});

@@ -238,7 +238,11 @@ struct DVolume {
 //       leaf code as for BVH2   [7] unused
 constexpr int kEmptyChild = 0x7fffffff;
 
-enum AnalyticKind { AP_SPHERE = 0, AP_CONE = 1, AP_CYLINDER = 2 };
+enum AnalyticKind { AP_SPHERE = 0, AP_CONE = 1, AP_CYLINDER = 2, AP_CURVE = 3 };
+// float4 records per analytic primitive: sphere (center, r); cone /
+// cylinder (v1, r1), (v2, r2); curve (w0, r), (w1, -), (w2, -), (w3, -)
+constexpr int kApStride = 4;
+constexpr int kApFloats = 4 * kApStride;
 
 // An iso-surface of a structured field (ISOSurface.cpp): the field as a
 // volume record (its TF fields unused), the iso values, the surface index.
@@ -263,7 +267,7 @@ struct DGroup {
   int volBegin, volEnd;   // range in DScene::groupVolumes
   float boundsLo[3], boundsHi[3];
   // analytic primitives (all sphere, cone and cylinder geometries of the
-  // group) with their own BVH2: leaf i is apPrims[2i], apPrims[2i+1]
+  // group) with their own BVH2: leaf i is apPrims[kApStride i ..]
   // (sphere: (center, radius), unused; cone / cylinder: (v1, r1), (v2, r2)),
   // apLocal[i] = the primitive's index in the group | kind << kApKindShift,
   // apSurface maps a group index to its surface. A hit on primitive k

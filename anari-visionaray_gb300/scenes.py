@@ -13,6 +13,9 @@ is fixed in each generator. A scene is a plain dict:
                "isovalues": [...], "material": {...}} |
               {"geometry": "quad", "vertices": (V,3) f32, "indices": (Q,4) u32 (optional,
                else consecutive quadruples), "material": {...}} |
+              {"geometry": "bezierCurve", "vertices": (V,3) f32 control points,
+               "indices": (N,) u32 segment starts (optional), "radii" per index entry
+               (optional), "radius" (default 1), "material": {...}} |
               {"geometry": "cone" | "cylinder", "vertices": (V,3) f32 end points,
                "indices": (N,2) u32 (optional, else consecutive pairs), "radii": per
                vertex (cone, required) or per cylinder (optional), "radius": f32
@@ -413,6 +416,15 @@ def _surfaces(dev, surfs, keep):
             if "radii" in s:
                 ra = dev.array1d(np.asarray(s["radii"], np.float32).reshape(-1))
                 dev.set(g, "primitive.radius" if kind == "cylinder" else "vertex.radius", ra)
+                keep += [ra]
+            if "radius" in s:
+                dev.set(g, "radius", float(s["radius"]))
+        elif kind == "bezierCurve":
+            if "indices" in s:
+                ia = dev.array1d(np.asarray(s["indices"], np.uint32).reshape(-1))
+            if "radii" in s:
+                ra = dev.array1d(np.asarray(s["radii"], np.float32).reshape(-1))
+                dev.set(g, "primitive.radius", ra)
                 keep += [ra]
             if "radius" in s:
                 dev.set(g, "radius", float(s["radius"]))

@@ -129,7 +129,8 @@ VSR_API VSRArray vsrNewArray3D(VSRDevice d, const void *appMemory, VSRDataType t
    newLight/newSurface/newGroup/newInstance/newWorld/newCamera/newRenderer/
    newFrame (VisionarayDevice.cpp:125-214). Supported subtypes:
    spatial field "structuredRegular"; volume "transferFunction1D";
-   geometry "triangle", "quad", "sphere", "cone", "cylinder", "isosurface";
+   geometry "triangle", "quad", "sphere", "cone", "cylinder", "isosurface",
+   "bezierCurve";
    material "matte", "physicallyBased"; light "directional", "point",
    "spot", "quad", "hdri"; instance "transform"; camera "perspective",
    "matrix", "orthographic", "omnidirectional"; renderer "raycast",

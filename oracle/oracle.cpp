@@ -529,6 +529,116 @@ float hitIso(const Vol &vol, const OrIso &iso, const Ray &l, float tmax) {
   return -FLT_MAX;
 }
 
+// Bezier curve (BezierCurve, DeviceCopyableObjects.h:1034-1057): the cubic
+// and its derivative as f / dfdt write them; q holds (w0, r, w1, -, w2, -,
+// w3, -).
+struct CurveR {
+  f3 w0, w1, w2, w3;
+  float r;
+  explicit CurveR(const float *q)
+      : w0(q[0], q[1], q[2]), w1(q[4], q[5], q[6]), w2(q[8], q[9], q[10]),
+        w3(q[12], q[13], q[14]), r(q[3]) {}
+  CurveR() : r(0.f) {}
+  f3 f(float t) const {
+    const float ti = 1.0f - t;
+    return ti * ti * ti * w0 + 3.0f * ti * ti * t * w1 + 3.0f * ti * t * t * w2 + t * t * t * w3;
+  }
+  f3 dfdt(float t) const {
+    const float ti = 1.0f - t;
+    return -3.0f * ti * ti * w0 + 3.0f * (3.0f * t * t - 4.0f * t + 1.0f) * w1 +
+           3.0f * (2.0f - 3.0f * t) * t * w2 + 3.0f * t * t * w3;
+  }
+};
+
+// intersect(Ray, BezierCurve), DeviceCopyableObjects.h:1072-1289 (the
+// Phantom ray-hair intersector, Reshetov and Luebke 2018): the early-out
+// cylinder around the end points (radius from the curve points at t = 1/3
+// and 2/3, plus r); the curve in the ray-centric frame (e3 = normalised
+// direction, e1, e2 from make_orthonormal_basis, origin at the ray's; the
+// frame's inverse applied as its transpose); up to 40 Newton steps of the
+// ray / cylinder test (RayConeIntersection with dr = 0) from the end the
+// direction points away from, regula falsi on a sign change of the step
+// (bisection every 4th), then the other end; converged at |dt| < 5e-5.
+// Returns s + c0.z (the distance along the normalised direction) or
+// -FLT_MAX, and the curve parameter in u.
+float hitCurve(const Ray &r, const float *q, float &uOut) {
+  const CurveR c(q);
+  auto distToAxis = [&](f3 pt) { return length(cross(pt - c.w0, pt - c.w3)) / length(c.w3 - c.w0); };
+  const float rmax = std::fmax(distToAxis(c.f(0.33333f)), distToAxis(c.f(0.66667f))) + c.r;
+  const f3 axis = normalize(c.w3 - c.w0);
+  const f3 p0 = c.w0 - axis * c.r, p1 = c.w3 + axis * c.r;
+  {
+    const f3 ba = p1 - p0, oc = r.ori - p0;
+    const float baba = dot(ba, ba), bard = dot(ba, r.dir), baoc = dot(ba, oc);
+    const float k2 = baba - bard * bard;
+    const float k1 = baba * dot(oc, r.dir) - baoc * bard;
+    const float k0 = baba * dot(oc, oc) - baoc * baoc - rmax * rmax * baba;
+    float h = k1 * k1 - k2 * k0;
+    if (h < 0.0f) return -FLT_MAX;
+    h = std::sqrt(h);
+    float t = (-k1 - h) / k2;
+    const float y = baoc + t * bard;
+    bool hitCyl = y > 0.0f && y < baba;
+    if (!hitCyl) {
+      t = ((y < 0.0f ? 0.0f : baba) - baoc) / bard;
+      hitCyl = std::fabs(k1 + k2 * t) < h;
+    }
+    if (!hitCyl) return -FLT_MAX;
+  }
+  f3 e1, e2;
+  const f3 e3 = normalize(r.dir);
+  make_orthonormal_basis(e1, e2, e3);
+  auto rcc = [&](f3 p) {
+    const f3 d = p - r.ori;
+    return f3(dot(e1, d), dot(e2, d), dot(e3, d));
+  };
+  CurveR x;
+  x.w0 = rcc(c.w0);
+  x.w1 = rcc(c.w1);
+  x.w2 = rcc(c.w2);
+  x.w3 = rcc(c.w3);
+  x.r = c.r;
+  float tstart = dot(x.w3 - x.w0, r.dir) > 0.0f ? 0.0f : 1.0f;
+  for (int ep = 0; ep < 2; ++ep) {
+    float t = tstart, told = 0.f, dt1 = 0.f, dt2 = 0.f;
+    for (int i = 0; i < 40; ++i) {
+      const f3 c0 = x.f(t), cd = x.dfdt(t);
+      const float r2 = c.r * c.r;
+      float ddd = cd.x * cd.x + cd.y * cd.y;
+      const float dp = c0.x * c0.x + c0.y * c0.y;
+      const float cdd = c0.x * cd.x + c0.y * cd.y;
+      const float cxd = c0.x * cd.y - c0.y * cd.x;
+      const float cc = ddd;
+      const float b = cd.z * (0.0f - cdd);
+      const float cdz2 = cd.z * cd.z;
+      ddd += cdz2;
+      const float a = 2.0f * 0.0f * cdd + cxd * cxd - ddd * r2 + dp * cdz2;
+      const float discr = b * b - a * cc;
+      const float sRoot = (b - (discr > 0.0f ? std::sqrt(discr) : 0.0f)) / cc;
+      float dt = (sRoot * cd.z - cdd) / ddd;
+      if (discr > 0.0f && std::fabs(dt) < 5e-5f) {
+        uOut = t;
+        return sRoot + c0.z;
+      }
+      dt = std::fmin(dt, 0.5f);
+      dt = std::fmax(dt, -0.5f);
+      dt1 = dt2;
+      dt2 = dt;
+      if (dt1 * dt2 < 0.0f) {
+        const float tnext = (i & 3) == 0 ? 0.5f * (told + t) : (dt2 * told - dt1 * t) / (dt2 - dt1);
+        told = t;
+        t = tnext;
+      } else {
+        told = t;
+        t += dt;
+      }
+      if (t < 0.0f || t > 1.0f) break;
+    }
+    tstart = 1.0f - tstart;
+  }
+  return -FLT_MAX;
+}
+
 // Closest hit over all instances: intersectSurfaces(Ray,TLS) with the
 // instance transform of intersect(Ray, Instance), DeviceCopyableObjects.h:
 // 1772-1839. Hits are ordered by (t, instance, triangle).
@@ -545,10 +655,12 @@ SurfHit traceSurfaces(const Scene &sc, const Ray &ray, Counters &c) {
     // structure)
     for (int k = og.apBegin; k < og.apEnd; ++k) {
       c.tris++;
-      const float *q = sc.src->prims + 8 * (size_t)k;
+      const float *q = sc.src->prims + 16 * (size_t)k;
       float u = 0.f, v = 0.f, t;
       if (sc.src->primKind[k] == 0) {
         t = hitSphere(l, q);
+      } else if (sc.src->primKind[k] == 3) {
+        t = hitCurve(l, q, u);
       } else {
         // cones and cylinders: the origin moved along the ray to twice the
         // bounding-sphere radius before the point nearest its centre (same
@@ -645,10 +757,11 @@ f3 hitNormal(const Scene &sc, const SurfHit &h) {
     return fieldGradient(vol.v, vol.pointToVoxelSpace(h.isect_pos), gradientDelta(vol));
   }
   if (h.prim >= 0) {
-    const float *q = sc.src->prims + 8 * (size_t)h.prim;
+    const float *q = sc.src->prims + 16 * (size_t)h.prim;
     const f3 P = h.isect_pos, v1(q[0], q[1], q[2]), v2(q[4], q[5], q[6]);
     const int kind = sc.src->primKind[h.prim];
     if (kind == 0) return normalize((P - v1) / q[3]);
+    if (kind == 3) return normalize(P - CurveR(q).f(h.u));  // renderer/common.h:304-308
     if (kind == 1) {
       f3 ba = v2 - v1;
       float m0 = dot(ba, ba);

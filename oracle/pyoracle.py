@@ -346,19 +346,47 @@ def build_tf(color, opacity):
 
 
 def analytic_prims(s):
-    """(N, 8) float32 records (p0, r0, p1, r1) of a sphere, cone or cylinder
-    surface, following Sphere.cpp:46-75, Cone.cpp:49-82, Cylinder.cpp:49-82:
-    sphere centres through 'indices' when given, per-sphere 'radii' (else
-    'radius', default 0.01); cone / cylinder end points from 'indices' pairs
-    (else consecutive vertices), cone radii per end vertex ('radii' required),
-    cylinder radii per cylinder ('radii') else 'radius' (default 1)."""
+    """(N, 16) float32 records of a sphere (c, r), cone or cylinder (p0, r0,
+    p1, r1) or Bezier curve (w0, r, w1, -, w2, -, w3, -) surface, following
+    Sphere.cpp:46-75, Cone.cpp:49-82, Cylinder.cpp:49-82, BezierCurve.cpp:
+    34-100: sphere centres through 'indices' when given, per-sphere 'radii'
+    (else 'radius', default 0.01); cone / cylinder end points from
+    'indices' pairs (else consecutive vertices), cone radii per end vertex
+    ('radii' required), cylinder radii per cylinder ('radii') else 'radius'
+    (default 1); curve segments every 3 vertices from each index entry to
+    the next (one for the last), or from vertex 0 without indices, radius
+    'radii' per index entry (per segment start / 3 without), else 'radius'
+    (default 1), segments past the vertices left out."""
     kind = s["geometry"]
     pos = np.asarray(s["vertices"], np.float32).reshape(-1, 3)
+    if kind == "bezierCurve":
+        nv = len(pos)
+        radii = np.asarray(s["radii"], np.float32).reshape(-1) if "radii" in s else None
+        R = float(s.get("radius", 1.0))
+        starts = []
+        if "indices" in s:
+            I = np.asarray(s["indices"], np.int64).reshape(-1)
+            for i in range(len(I)):
+                first = int(I[i])
+                last = first + 3 if i == len(I) - 1 else int(I[i + 1])
+                r = float(radii[i]) if radii is not None and i < len(radii) else R
+                starts += [(j, r) for j in range(first, last, 3)]
+        elif nv > 3:
+            for i in range(0, nv - 3, 3):
+                r = float(radii[i // 3]) if radii is not None and i // 3 < len(radii) else R
+                starts.append((i, r))
+        starts = [(j, r) for j, r in starts if j + 3 < nv]
+        q = np.zeros((len(starts), 16), np.float32)
+        for k, (j, r) in enumerate(starts):
+            for c in range(4):
+                q[k, 4 * c:4 * c + 3] = pos[j + c]
+            q[k, 3] = r
+        return q
     if kind == "sphere":
         c = pos[np.asarray(s["indices"], np.int64).reshape(-1)] if "indices" in s else pos
         r = (np.asarray(s["radii"], np.float32).reshape(-1)[:len(c)] if "radii" in s
              else np.full(len(c), s.get("radius", 0.01), np.float32))
-        q = np.zeros((len(c), 8), np.float32)
+        q = np.zeros((len(c), 16), np.float32)
         q[:, :3], q[:, 3] = c, r
         return q
     if "indices" in s:
@@ -366,7 +394,7 @@ def analytic_prims(s):
     else:
         n = len(pos) // 2
         ab = np.stack([2 * np.arange(n), 2 * np.arange(n) + 1], axis=1)
-    q = np.zeros((len(ab), 8), np.float32)
+    q = np.zeros((len(ab), 16), np.float32)
     q[:, :3], q[:, 4:7] = pos[ab[:, 0]], pos[ab[:, 1]]
     if kind == "cone":
         radii = np.asarray(s["radii"], np.float32).reshape(-1)
@@ -433,11 +461,11 @@ class Scene:
                     isos.append(oi)
                     continue
                 kind = s.get("geometry", "triangle")
-                if kind in ("sphere", "cone", "cylinder"):
+                if kind in ("sphere", "cone", "cylinder", "bezierCurve"):
                     q = analytic_prims(s)
                     aps.append(q)
-                    akind.append(np.full(len(q), {"sphere": 0, "cone": 1, "cylinder": 2}[kind],
-                                         np.int32))
+                    akind.append(np.full(len(q), {"sphere": 0, "cone": 1, "cylinder": 2,
+                                                  "bezierCurve": 3}[kind], np.int32))
                     asurf.append(np.full(len(q), len(mats), np.uint32))
                     add_material(s)
                     nap += len(q)
@@ -536,7 +564,7 @@ class Scene:
         tri = np.ascontiguousarray(np.concatenate(verts) if verts else np.zeros((0, 9), np.float32))
         ts = np.ascontiguousarray(np.concatenate(tsurf) if tsurf else np.zeros(0, np.uint32))
         tp = np.ascontiguousarray(np.concatenate(tprim) if tprim else np.zeros(0, np.uint32))
-        ap = np.ascontiguousarray(np.concatenate(aps) if aps else np.zeros((0, 8), np.float32),
+        ap = np.ascontiguousarray(np.concatenate(aps) if aps else np.zeros((0, 16), np.float32),
                                   np.float32)
         ak = np.ascontiguousarray(np.concatenate(akind) if akind else np.zeros(0, np.int32))
         asf = np.ascontiguousarray(np.concatenate(asurf) if asurf else np.zeros(0, np.uint32))

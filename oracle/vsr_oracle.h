@@ -155,10 +155,11 @@ typedef struct OrScene {
   const OrInstance *instances;
   int32_t numLights;
   const OrLight *lights;
-  int32_t numPrims;              /* spheres, cones, cylinders */
-  const float *prims;            /* 8 floats each, object space: sphere (center, radius, -);
-                                    cone / cylinder (v1, r1, v2, r2) */
-  const int32_t *primKind;       /* 0 sphere, 1 cone, 2 cylinder */
+  int32_t numPrims;              /* spheres, cones, cylinders, curves */
+  const float *prims;            /* 16 floats each, object space: sphere (center, radius, -);
+                                    cone / cylinder (v1, r1, v2, r2, -); curve (w0, r, w1, -,
+                                    w2, -, w3, -) */
+  const int32_t *primKind;       /* 0 sphere, 1 cone, 2 cylinder, 3 Bezier curve */
   const uint32_t *primSurface;   /* surface index per primitive */
   const int32_t *triNormalFrom;  /* per triangle: the triangle whose e1 x e2 is its shading
                                     normal (quads), -1 for its own; may be null */

@@ -1296,3 +1296,57 @@ def test_pathtrace_textured_same_stream(pkg, device, oracle, wavefront):
     assert not np.isnan(gpu["color"]).any()
     d = np.abs(gpu["color"][..., :3] - F.color[..., :3]).max(axis=-1)
     assert float((d <= 1e-3).mean()) >= 0.97, float((d <= 1e-3).mean())
+
+
+def hair_curves(seed=11, n=40):
+    """Seeded cubic strands above the sphere set: n multi-segment curves
+    (2 segments each through primitive.index), radii 0.08..0.2 per strand."""
+    rng = np.random.default_rng(seed)
+    verts, idx = [], []
+    for k in range(n):
+        p = rng.uniform(-9.0, 9.0, 3)
+        d = rng.normal(size=3)
+        d /= np.linalg.norm(d)
+        pts = [p + d * 2.0 * j / 6.0 + rng.normal(scale=0.6, size=3) * (j % 3 != 0)
+               for j in range(7)]
+        idx.append(len(verts))
+        verts += pts
+    return {"geometry": "bezierCurve", "vertices": np.asarray(verts, np.float32),
+            "indices": np.asarray(idx, np.uint32),
+            "radii": rng.uniform(0.08, 0.2, n).astype(np.float32),
+            "material": {"type": "physicallyBased", "baseColor": [0.8, 0.6, 0.3],
+                         "metallic": 0.2, "roughness": 0.5}}
+
+
+def test_raycast_bezier_curves(pkg, device, oracle):
+    """Cubic Bezier curves (the Phantom ray-hair intersector, curve normals)
+    beside the triangle spheres in the raycast renderer: colour, depth and
+    normal parity."""
+    sc = small_spheres(pkg, res=128, renderer="raycast")
+    sc["surfaces"] = sc["surfaces"] + [hair_curves()]
+    gpu = render_gpu(pkg, device, sc)
+    _, F = render_oracle(oracle, sc)
+    _, P = render_oracle(oracle, small_spheres(pkg, res=128, renderer="raycast"))
+    assert gpu["errorFlags"] == 0
+    strands = (F.depth < P.depth - 1e-3)
+    assert float(strands.mean()) > 0.02  # the strands cover part of the view
+    good, frac = raycast_ok(gpu, F)
+    assert good, frac
+    hit = (F.depth < 1e30) & (gpu["depth"] < 1e30)
+    rel = np.abs(gpu["depth"][hit] - F.depth[hit]) / F.depth[hit]
+    assert float((rel <= 1e-4).mean()) >= 0.999
+
+
+@pytest.mark.parametrize("wavefront", [True, False])
+def test_pathtrace_bezier_curves_same_stream(pkg, device, oracle, wavefront):
+    """The strands in the path tracer, same stream as the oracle (frames
+    with analytic primitives run the megakernel)."""
+    sc = small_spheres(pkg, res=96, spp=8)
+    sc["surfaces"] = sc["surfaces"] + [hair_curves()]
+    sc["renderer"]["wavefront"] = wavefront
+    gpu = render_gpu(pkg, device, sc)
+    _, F = render_oracle(oracle, sc)
+    assert gpu["errorFlags"] == 0
+    assert not np.isnan(gpu["color"]).any()
+    d = np.abs(gpu["color"][..., :3] - F.color[..., :3]).max(axis=-1)
+    assert float((d <= 1e-3).mean()) >= 0.97, float((d <= 1e-3).mean())

@@ -800,6 +800,72 @@ def test_opacity_from_attribute_blends(oracle):
     assert np.allclose(F.color[inside][:, :3], expect, atol=1e-5)
 
 
+def _curve_scene(vertices, radius, light=(0.0, 0.0, -1.0)):
+    return {
+        "surfaces": [{"geometry": "bezierCurve", "vertices": np.asarray(vertices, np.float32),
+                      "radius": radius, "material": {"type": "matte", "color": [0.6, 0.5, 0.4]}}],
+        "volumes": [],
+        "lights": [{"direction": list(light), "irradiance": 2.0}],
+        "camera": {"type": "orthographic", "position": [0.0, 0.0, 10.0],
+                   "direction": [0.0, 0.0, -1.0], "up": [0.0, 1.0, 0.0], "height": 2.0,
+                   "aspect": 1.0},
+        "renderer": {"type": "raycast", "ambientRadiance": 0.2, "background": [0, 0, 0, 1]},
+        "frame": {"size": (32, 32)},
+    }
+
+
+def test_straight_bezier_curve_closed_form(oracle):
+    """A cubic with evenly spaced collinear control points along x (a tube
+    of radius 0.5) seen from above: the Phantom intersector converges to the
+    tube, depth 10 - sqrt(r^2 - y^2), normal (0, y, z) / r (the hit minus
+    the curve point at the converged parameter), matte shading with the
+    light straight down."""
+    w = [[-2.0, 0.0, 0.0], [-2.0 / 3.0, 0.0, 0.0], [2.0 / 3.0, 0.0, 0.0], [2.0, 0.0, 0.0]]
+    F = oracle.Frame(32, 32)
+    oracle.render(oracle.Scene(_curve_scene(w, 0.5)), F)
+    xs = ((np.arange(32) + 0.5) / 32 - 0.5) * 2.0
+    X, Y = np.meshgrid(xs, xs)
+    inner = (np.abs(Y) < 0.45) & (np.abs(X) < 0.9)
+    outside = np.abs(Y) > 0.55
+    z = np.sqrt(np.maximum(0.25 - Y * Y, 0.0))
+    assert inner.sum() > 100
+    assert np.all(F.depth[outside] > 1e30)
+    assert np.allclose(F.depth[inner], (10.0 - z)[inner], atol=2e-4)
+    n = np.stack([np.zeros_like(Y), Y, z], -1) / 0.5
+    assert np.allclose(F.normal[inner], n[inner], atol=2e-3)
+    c = np.array([0.6, 0.5, 0.4])
+    expect = (c / math.pi * 2.0)[None, :] * (z[inner] / 0.5)[:, None] + c * 0.2
+    assert np.allclose(F.color[inner][:, :3], expect, atol=2e-3)
+
+
+def test_curved_bezier_hits_lie_on_the_tube(oracle):
+    """A bent cubic (radius 0.15) seen from above: every hit point the oracle
+    reports (from its depth) lies on the tube, i.e. at distance r from the
+    curve (dense sampling of the cubic), and the hits cover the curve."""
+    w = np.array([[-0.9, -0.6, 0.0], [-0.3, 0.9, 0.3], [0.3, -0.9, -0.3], [0.9, 0.6, 0.0]],
+                 np.float32)
+    r = 0.15
+    F = oracle.Frame(32, 32)
+    oracle.render(oracle.Scene(_curve_scene(w, r)), F)
+    xs = ((np.arange(32) + 0.5) / 32 - 0.5) * 2.0
+    X, Y = np.meshgrid(xs, xs)
+    hit = F.depth < 1e30
+    assert hit.sum() > 60
+    P = np.stack([X[hit], Y[hit], 10.0 - F.depth[hit]], -1)
+    t = np.linspace(0.0, 1.0, 20001)[:, None]
+    ti = 1 - t
+    curve = ti ** 3 * w[0] + 3 * ti ** 2 * t * w[1] + 3 * ti * t ** 2 * w[2] + t ** 3 * w[3]
+    d = np.sqrt(((P[:, None, :] - curve[None, :, :]) ** 2).sum(-1)).min(axis=1)
+    assert np.all(np.abs(d - r) < 2e-3), np.abs(d - r).max()
+    # pixels whose ray passes within 0.6 r of the projection of the curve's
+    # middle part (away from the open ends) are hit
+    mid = curve[2000:18001, :2]
+    d2 = np.sqrt(((np.stack([X, Y], -1)[..., None, :] - mid[None, None, :, :]) ** 2).sum(-1)).min(-1)
+    d2all = np.sqrt(((np.stack([X, Y], -1)[..., None, :] - curve[None, None, :, :2]) ** 2).sum(-1))
+    near_end = np.minimum(d2all[..., :2000].min(-1), d2all[..., 18001:].min(-1)) < r
+    assert np.all(hit[(d2 < 0.6 * r) & ~near_end])
+
+
 def test_emission_absorption_slab(oracle):
     """Constant field, TF alpha a: alpha after k steps is 1 - (1-a)^(k dt/ud)."""
     n = 16

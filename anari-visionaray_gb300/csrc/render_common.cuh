@@ -469,6 +469,23 @@ __device__ __forceinline__ bool traverseGroup(const DGroup &G, float3 o, float3 
   const float3 oi = f3(-o.x * inv.x, -o.y * inv.y, -o.z * inv.z);
   int stack[kTraversalStack];
   int sp = 0;
+#if VSR_SMEM_STACK > 0
+  // the stack's first VSR_SMEM_STACK entries in shared memory (one column
+  // per thread: conflict-free), deeper ones in the local array
+  __shared__ int sstack[VSR_SMEM_STACK][256];
+  const int tid = threadIdx.x + threadIdx.y * blockDim.x;
+  const bool useS = tid < 256;
+#define VSR_PUSH(v)                                                             \
+  do {                                                                          \
+    if (useS && sp < VSR_SMEM_STACK) sstack[sp][tid] = (v);                     \
+    else stack[useS ? sp - VSR_SMEM_STACK : sp] = (v);                          \
+    ++sp;                                                                       \
+  } while (0)
+#define VSR_POP() (--sp, (useS && sp < VSR_SMEM_STACK) ? sstack[sp][tid] : stack[useS ? sp - VSR_SMEM_STACK : sp])
+#else
+#define VSR_PUSH(v) (stack[sp++] = (v))
+#define VSR_POP() stack[--sp]
+#endif
   int node = 0;
   bool found = false, done = false;
   unsigned nodeVisits = 0, triTests = 0;
@@ -501,13 +518,13 @@ __device__ __forceinline__ bool traverseGroup(const DGroup &G, float3 o, float3 
           done = true;
           break;
         }
-        node = stack[--sp];
+        node = VSR_POP();
       } else {
         int near = h0 ? n3.x : n3.y;
         if (h0 && h1) {
           int far = n3.y;
           if (c1min < c0min) { near = n3.y; far = n3.x; }
-          if (sp < kTraversalStack) stack[sp++] = far;
+          if (sp < kTraversalStack) VSR_PUSH(far);
           else err |= ERR_STACK_OVERFLOW;
         }
         node = near;
@@ -569,7 +586,7 @@ __device__ __forceinline__ bool traverseGroup(const DGroup &G, float3 o, float3 
         done = true;
         break;
       }
-      node = stack[--sp];
+      node = VSR_POP();
     }
   }
   if (Count) {
@@ -594,6 +611,9 @@ __device__ __forceinline__ void cswap(float &ka, int &ca, float &kb, int &cb) {
 
 // Same contract as traverseGroup, over 4-wide nodes (vsr_device.h): one
 // 128-byte fetch tests four child boxes; hit children are ordered by entry
+#undef VSR_PUSH
+#undef VSR_POP
+
 // distance (a five-exchange sorting network), the nearest is visited next
 // and the others are pushed farthest first.
 template <bool Count>

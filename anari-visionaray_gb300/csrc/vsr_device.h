@@ -57,6 +57,9 @@ constexpr int kMaxSurfaceLayers = 1 << 12;
 #ifndef VSR_MEGA_MIN_BLOCKS
 #define VSR_MEGA_MIN_BLOCKS 16  // 32 registers, 64 warps per SM: latency hiding beats spill cost
 #endif
+#ifndef VSR_SMEM_STACK
+#define VSR_SMEM_STACK 0  // BVH2 traversal: stack entries kept in shared memory (0: all local)
+#endif
 #ifndef VSR_MEGA_MIN_BLOCKS_VOLUMES
 #define VSR_MEGA_MIN_BLOCKS_VOLUMES 8  // ~64 registers for worlds with volumes
 #endif

@@ -168,6 +168,16 @@ cudaError_t Denoiser::ensure(int N, int H, int W, bool train) {
     if (train && e == cudaSuccess) e = alloc(grd_.*z.f, z.n, &bufs_);
   }
   if (e == cudaSuccess) e = alloc(out_, P0 * kOutC, &bufs_);
+  // the tcgen05 weight gradient's partial sums (tensor path 4; allocated at
+  // its first use): the largest layer's
+  wgradPart_ = nullptr;
+  wgradPartFloats_ = 0;
+  const int levelOf[15] = {0, 0, 1, 1, 2, 2, 3, 3, 2, 2, 1, 1, 0, 0, 0};
+  for (size_t li = 0; li < layers_.size(); ++li) {
+    const int Pl = (int)(P0 >> (2 * levelOf[li]));
+    wgradPartFloats_ =
+        std::max(wgradPartFloats_, wgradPartFloats(layers_[li].cout, layers_[li].cin, Pl));
+  }
   if (train && e == cudaSuccess) {
     e = alloc(gout_, P0 * kOutC, &bufs_);
     if (e == cudaSuccess) e = cudaMemset(gout_, 0, P0 * kOutC * sizeof(__nv_bfloat16));
@@ -258,12 +268,19 @@ cudaError_t Denoiser::convBack(int li, const __nv_bfloat16 *x, int xC, const __n
   g.N = N;
   g.H = H;
   g.W = W;
-  // split the pixel reduction so that about 2048 CTAs run
-  const int tiles = ((L.cout + 63) / 64) * 9 * ((L.cin + 63) / 64);
-  const int chunks = std::max(1, std::min(2048 / tiles, P / 256));
-  const int chunk = (P + chunks - 1) / chunks;
-  g.chunk = (chunk + 15) / 16 * 16;
-  cudaError_t e = launchConvWgrad(g, s);
+  cudaError_t e = cudaSuccess;
+  if (tensorPath_ == 4 && !wgradPart_) e = alloc(wgradPart_, wgradPartFloats_, &bufs_);
+  if (tensorPath_ == 4) {
+    // tcgen05: accumulators in tensor memory, partial sums per pixel range
+    if (e == cudaSuccess) e = launchConvWgradTc(g, wgradPart_, err_, s);
+  } else {
+    // mma.sync: split the pixel reduction so that about 2048 CTAs run
+    const int tiles = ((L.cout + 63) / 64) * 9 * ((L.cin + 63) / 64);
+    const int chunks = std::max(1, std::min(2048 / tiles, P / 256));
+    const int chunk = (P + chunks - 1) / chunks;
+    g.chunk = (chunk + 15) / 16 * 16;
+    e = launchConvWgrad(g, s);
+  }
   if (e == cudaSuccess) e = launchBiasGrad(dy, L.cout, 0, L.cout, P, grad_ + L.b, s);
   if (dx) {
     ConvArgs a{};

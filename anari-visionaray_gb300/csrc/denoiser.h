@@ -74,7 +74,8 @@ class Denoiser {
   cudaError_t run(const __nv_bfloat16 *x, int N, int H, int W, float *out, cudaStream_t s,
                   bool catOut);
   bool useTc(int W) const {
-    return tensorPath_ == 2 || ((tensorPath_ == 1 || tensorPath_ == 3) && W >= 128);
+    return tensorPath_ == 2 || tensorPath_ == 4 ||
+           ((tensorPath_ == 1 || tensorPath_ == 3) && W >= 128);
   }
   // the tcgen05 convolution: the persistent warp-specialised kernel with
   // TMA loads (kConv3x3Ws), or on path 3 one tile per CTA (kConv3x3Tc)
@@ -92,6 +93,8 @@ class Denoiser {
   size_t numParams_ = 0, numWt_ = 0;
   float *params_ = nullptr, *m_ = nullptr, *v_ = nullptr, *grad_ = nullptr, *loss_ = nullptr;
   unsigned *err_ = nullptr;
+  float *wgradPart_ = nullptr;  // tcgen05 weight gradient: partial sums (tensor path 4)
+  size_t wgradPartFloats_ = 0;
   int tensorPath_ = 2;  // tcgen05 at every level width (training crops reach 16 wide)
   mutable bool stallNext_ = false;
   __nv_bfloat16 *wbf_ = nullptr, *wt_ = nullptr, *wpk_ = nullptr;

@@ -133,6 +133,11 @@ cudaError_t launchConv3x3Tc(const ConvArgs &a, unsigned *error, cudaStream_t s);
 // (k_denoise_ws.cu); split requires up
 cudaError_t launchConv3x3Ws(const ConvArgs &a, unsigned *error, cudaStream_t s);
 cudaError_t launchConvWgrad(const WgradArgs &a, cudaStream_t s);
+// the weight gradient on tcgen05 (k_denoise_wg.cu): per-CTA partial sums in
+// `part` (wgradPartFloats floats), then added into dw in a fixed order;
+// error: a device word that gets bit 1 if a bounded wait ran out
+cudaError_t launchConvWgradTc(const WgradArgs &a, float *part, unsigned *error, cudaStream_t s);
+size_t wgradPartFloats(int Cout, int Cin, int P);
 cudaError_t launchBiasGrad(const __nv_bfloat16 *dy, int dyC, int dyOff, int C, int P, float *db,
                            cudaStream_t s);
 cudaError_t launchMaxPool(const __nv_bfloat16 *x, int C, int N, int H, int W, __nv_bfloat16 *y,

@@ -3106,7 +3106,7 @@ uint64_t vsrDenoiserParameterCount(VSRDevice dv, VSRDenoiser nv) {
 
 VSRStatus vsrDenoiserSetTensorPath(VSRDevice dv, VSRDenoiser nv, int path) {
   Device *d = asDev(dv);
-  if (!d || path < 0 || path > 3) return VSR_ERROR_INVALID_ARGUMENT;
+  if (!d || path < 0 || path > 4) return VSR_ERROR_INVALID_ARGUMENT;
   std::lock_guard<std::recursive_mutex> lk(d->mtx);
   Denoiser *n = asDenoiser(d, nv);
   if (!n) return VSR_ERROR_INVALID_OBJECT;

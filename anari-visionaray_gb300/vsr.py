@@ -184,7 +184,8 @@ class Denoiser:
         """0: mma.sync convolutions; 1: tcgen05 (persistent warp-specialised
         kernel with TMA loads) where a level is at least 128 pixels wide,
         mma.sync below; 2 (default): that kernel at every width; 3: as 1 on
-        the one-tile-per-CTA tcgen05 kernel."""
+        the one-tile-per-CTA tcgen05 kernel; 4: as 2 with the weight
+        gradients on tcgen05 as well."""
         rc = self.lib.vsrDenoiserSetTensorPath(self.dev.handle, self.handle, path)
         if rc:
             raise RuntimeError(f"vsrDenoiserSetTensorPath failed ({rc})")

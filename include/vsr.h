@@ -230,7 +230,10 @@ VSR_API VSRStatus vsrDenoiserGetParameters(VSRDevice d, VSRDenoiser n, float *pa
    1 tcgen05 with the accumulators in tensor memory, on a persistent
    warp-specialised kernel with TMA loads, for levels at least 128 pixels
    wide (mma.sync below), 2 (default) the same kernel at every width, 3 as
-   1 on a kernel that stages one tile per CTA with cp.async. On the
+   1 on a kernel that stages one tile per CTA with cp.async, 4 as 2 with
+   the training's weight gradients on tcgen05 too (accumulated in tensor
+   memory over pixel ranges, summed without atomics; slower than the
+   mma.sync weight gradient at the training's crop sizes). On the
    tcgen05 path the forward reads each decoder's upsampled input and skip
    connection in place instead of writing their concatenation.
    vsrDenoiserErrors returns the device error word of the tcgen05 path

@@ -102,7 +102,8 @@ def test_gradients_match_oracle(net):
 
 
 @pytest.mark.parametrize("shape,path", [((2, 16, 16), 2), ((1, 24, 40), 2), ((1, 24, 136), 1),
-                                        ((2, 16, 256), 1), ((1, 24, 136), 3), ((2, 16, 256), 3)])
+                                        ((2, 16, 256), 1), ((1, 24, 136), 3), ((2, 16, 256), 3),
+                                        ((2, 16, 16), 4), ((1, 24, 136), 4), ((2, 16, 256), 4)])
 def test_tcgen05_path_matches_oracle(net, shape, path):
     """The tcgen05 convolutions (accumulators in tensor memory) in forward,
     where the decoders read the upsampled level and the skip connection in
@@ -111,7 +112,9 @@ def test_tcgen05_path_matches_oracle(net, shape, path):
     warp-specialised TMA kernel (tiles of 4 rows x 128 pixels far wider than
     these images, rows not a multiple of 4 at 24 / 8 = 3); path 1 switches
     to mma.sync below 128 pixels (136: a second, nearly empty tile; 256: two
-    levels on each); path 3 is path 1 on the one-tile-per-CTA kernel."""
+    levels on each); path 3 is path 1 on the one-tile-per-CTA kernel; path
+    4 is path 2 with the weight gradients on tcgen05 as well (partial sums
+    over pixel ranges of 64, here with ragged ends)."""
     import torch
     n, h, w = shape
     params = perturbed_params(5, 11)

@@ -12,8 +12,11 @@
 //     the group's ray i. Neighbouring pixels at the same depth keep the
 //     texture fetches of a warp coherent. Each segment is composited front
 //     to back in the reference's order, from (C, A, T) = (0, 0, 1).
-//  3. kVolumeCombine, one warp per group, one lane per ray: the segment
-//     composites are combined in order with the front-to-back operator
+//  3. kVolumeCombine, one warp per group, one lane per ray (or, compiled
+//     with VSR_SEG_FUSE, done by the warp that finishes a group's last work
+//     unit, which a per-group counter incremented after a memory fence
+//     tells; slower, see there): the segment composites are combined in
+//     order with the front-to-back operator
 //       (C, A, T)front o (C, A, T)back = (Cf + Tf Cb, Af + Tf Ab, Tf Tb).
 //     A segment after which the accumulated alpha reaches 0.99, and any part
 //     of a ray the segments did not cover, is marched again by the whole warp
@@ -39,6 +42,19 @@ namespace {
 #endif
 #ifndef VSR_COMBINE_PREFETCH
 #define VSR_COMBINE_PREFETCH 8
+#endif
+#ifndef VSR_SEG_FUSE
+// 1: the combination inside the segments pass (measured 0.125 ms per
+// config-0 frame against 0.067 ms with its own pass: the last groups'
+// combinations run at the end with few warps, and the fused kernel spills
+// at the segments pass's 64 registers)
+#define VSR_SEG_FUSE 0
+#endif
+#ifndef VSR_SEG_FUSED_MIN_BLOCKS
+#define VSR_SEG_FUSED_MIN_BLOCKS 4  // 64 registers, as the segments pass alone
+#endif
+#ifndef VSR_SEG_FUSED_PREFETCH
+#define VSR_SEG_FUSED_PREFETCH 4
 #endif
 #ifndef VSR_SEG_DYNAMIC
 #define VSR_SEG_DYNAMIC 0
@@ -177,7 +193,10 @@ __global__ void __launch_bounds__(256, VSR_SETUP_MIN_BLOCKS) kVolumeSetup(DScene
       it.info.w = nseg;
       items[off + rank] = it;
     }
-    if (lane == 0) groups[gid] = MarchGroup{(int)off, numRays, (int)ub, numUnits};
+    if (lane == 0) {
+      groups[gid] = MarchGroup{(int)off, numRays, (int)ub, numUnits};
+      M.groupDone[gid] = 0u;
+    }
   }
 }
 
@@ -404,7 +423,7 @@ __device__ __forceinline__ void marchUnit(const DScene &S, const DRenderer &R,
 // in order, until the one after which the accumulated alpha reaches 0.99;
 // rays with samples left (that segment, segments ending short of tmax, rays
 // without segments) are then marched by the whole warp, one at a time.
-template <bool Count>
+template <bool Count, int kPf = VSR_COMBINE_PREFETCH>
 __device__ __forceinline__ void combineGroup(const DScene &S, const DRenderer &R, const DFrame &F,
                              const MarchScratch &M, const float4 *sTF, int stageTF, int gid,
                              int lane, uint32_t &err, unsigned long long &samples) {
@@ -421,15 +440,15 @@ __device__ __forceinline__ void combineGroup(const DScene &S, const DRenderer &R
     tNext = it.o.w;
     const int nseg = it.info.w;
     const float4 *mine = reinterpret_cast<const float4 *>(segOut + (size_t)G.z * 32 + lane);
-    constexpr int kPf = VSR_COMBINE_PREFETCH;
     bool stop = false;
     for (int j0 = 0; j0 < nseg && !stop; j0 += kPf) {
       float4 sc[kPf], sm[kPf];  // loads in flight together
 #pragma unroll
       for (int k = 0; k < kPf; ++k)
         if (j0 + k < nseg) {
-          sc[k] = mine[(size_t)(j0 + k) * 64];
-          sm[k] = mine[(size_t)(j0 + k) * 64 + 1];
+          // L2 loads: in the fused pass other SMs wrote them in this grid
+          sc[k] = __ldcg(mine + (size_t)(j0 + k) * 64);
+          sm[k] = __ldcg(mine + (size_t)(j0 + k) * 64 + 1);
         }
 #pragma unroll
       for (int k = 0; k < kPf; ++k) {
@@ -483,9 +502,11 @@ __device__ __forceinline__ void combineGroup(const DScene &S, const DRenderer &R
   if (Count) samples += own;
 }
 
-// Pass 2: warp w marches work units w, w + warps, ...
-__global__ void __launch_bounds__(256, VSR_SEG_MIN_BLOCKS)
-    kVolumeSegments(DScene S, DRenderer R, MarchScratch M, int stageTF) {
+// Pass 2: warp w marches work units w, w + warps, ...; Fused: and combines
+// each group whose last unit it finished, then the groups without units.
+template <bool Fused>
+__global__ void __launch_bounds__(256, Fused ? VSR_SEG_FUSED_MIN_BLOCKS : VSR_SEG_MIN_BLOCKS)
+    kVolumeSegments(DScene S, DRenderer R, DFrame F, MarchScratch M, int stageTF) {
   extern __shared__ float4 sTF[];
   stageTable(S, sTF, stageTF);
   // the set-up pass's ray list and counters are complete and visible
@@ -494,9 +515,38 @@ __global__ void __launch_bounds__(256, VSR_SEG_MIN_BLOCKS)
   const int lane = threadIdx.x & 31;
   const unsigned numUnits = min(M.counters[2], M.unitCap);
   const unsigned warps = gridDim.x * (blockDim.x >> 5);
-  for (unsigned u = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); u < numUnits;
-       u += warps)
+  const unsigned warpId = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  uint32_t err = 0;
+  unsigned long long samples = 0;
+  for (unsigned u = warpId; u < numUnits; u += warps) {
     marchUnit(S, R, M, sTF, stageTF, u, lane);
+    if (Fused) {
+      const int gid = M.unitGroup[u];
+      if (gid < 0) continue;
+      // this unit's composites are visible before the count says so
+      __threadfence();
+      __syncwarp();
+      unsigned last = 0;
+      if (lane == 0) {
+        const int n = reinterpret_cast<const MarchGroup *>(M.groups)[gid].numUnits;
+        last = atomicAdd(&M.groupDone[gid], 1u) == (unsigned)n - 1u ? 1u : 0u;
+      }
+      if (__shfl_sync(kFull, last, 0)) {
+        __threadfence();
+        combineGroup<false, VSR_SEG_FUSED_PREFETCH>(S, R, F, M, sTF, stageTF, gid, lane, err,
+                                                    samples);
+      }
+    }
+  }
+  if (Fused) {
+    const MarchGroup *groups = reinterpret_cast<const MarchGroup *>(M.groups);
+    const unsigned numGroups = M.counters[3];
+    for (unsigned g = warpId; g < numGroups; g += warps)
+      if (groups[g].numUnits == 0)
+        combineGroup<false, VSR_SEG_FUSED_PREFETCH>(S, R, F, M, sTF, stageTF, (int)g, lane, err,
+                                                    samples);
+    if (err) atomicOr(F.errorFlags, err);
+  }
 }
 
 // Pass 3: one warp per group.
@@ -594,9 +644,16 @@ cudaError_t launchVolumeMarch(const DScene &S, const DCamera &C, const DRenderer
     cfg.numAttrs = 1;
     cudaLaunchKernelEx(&cfg, kernel, args...);
   };
-  persistent(kVolumeSegments, S, R, M, stage);
-  if (count) persistent(kVolumeCombine<true>, S, R, F, M, stage);
-  else persistent(kVolumeCombine<false>, S, R, F, M, stage);
+  if (count) {
+    // the counting frame: segments, then combination as its own pass
+    persistent(kVolumeSegments<false>, S, R, F, M, stage);
+    persistent(kVolumeCombine<true>, S, R, F, M, stage);
+  } else if (VSR_SEG_FUSE) {
+    persistent(kVolumeSegments<true>, S, R, F, M, stage);
+  } else {
+    persistent(kVolumeSegments<false>, S, R, F, M, stage);
+    persistent(kVolumeCombine<false>, S, R, F, M, stage);
+  }
   return cudaGetLastError();
 }
 

@@ -24,6 +24,7 @@ struct MarchScratch {
   int *unitGroup;
   void *segOut;
   unsigned unitCap;
+  unsigned *groupDone;  // per group: its work units finished (fused combination)
 };
 // scratch null selects the per-pixel kernel for volume-only worlds too
 cudaError_t launchRaycast(const DScene &S, const DCamera &C, const DRenderer &R, const DFrame &F,

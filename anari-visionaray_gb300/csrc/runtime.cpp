@@ -2103,7 +2103,7 @@ struct FrameObj : Object {
   VSRDataType colorType = VSR_UNKNOWN, depthType = VSR_UNKNOWN, normalType = VSR_UNKNOWN,
               albedoType = VSR_UNKNOWN, varianceType = VSR_UNKNOWN;
   DevBuf color, depth, normal, albedo, accum, errFlags, marchItems, marchGroups, marchCounters,
-      unitGroup, segOut;
+      unitGroup, segOut, groupDone;
   DevBuf variance, accumSq;                    // optional: variance of the mean (luminance)
   DevBuf denoiseIn, denoiseOut, denoiseCount;  // denoiser scratch, made on first use
   size_t marchPixels = 0;
@@ -2164,14 +2164,15 @@ struct FrameObj : Object {
               marchGroups.alloc(numGroups * 16) == cudaSuccess &&
               marchCounters.alloc(4 * sizeof(unsigned)) == cudaSuccess &&
               unitGroup.alloc(cap * sizeof(int)) == cudaSuccess &&
-              segOut.alloc(cap * 1024) == cudaSuccess;
+              segOut.alloc(cap * 1024) == cudaSuccess &&
+              groupDone.alloc(numGroups * sizeof(unsigned)) == cudaSuccess;
     unitCap = ok ? (unsigned)cap : 0;
     marchPixels = ok ? np : 0;
     return ok;
   }
   MarchScratch march() {
     return MarchScratch{marchItems.p, marchGroups.p, marchCounters.as<unsigned>(),
-                        unitGroup.as<int>(), segOut.p, unitCap};
+                        unitGroup.as<int>(), segOut.p, unitCap, groupDone.as<unsigned>()};
   }
   bool ensureWave() {
     size_t np = (size_t)width * height;

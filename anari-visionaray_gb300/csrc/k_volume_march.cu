@@ -43,6 +43,18 @@ namespace {
 #ifndef VSR_COMBINE_PREFETCH
 #define VSR_COMBINE_PREFETCH 8
 #endif
+#ifndef VSR_VOLUME_REFILL
+// 1: the one-pass marcher (kVolumeRefill): measured 0.21-0.24 ms per
+// config-0 frame (refill every 8 / 12 / 16 samples, 3 or 4 blocks per SM)
+// against 0.066 ms for the three passes
+#define VSR_VOLUME_REFILL 0
+#endif
+#ifndef VSR_REFILL_SAMPLES
+#define VSR_REFILL_SAMPLES 8
+#endif
+#ifndef VSR_REFILL_MIN_BLOCKS
+#define VSR_REFILL_MIN_BLOCKS 4
+#endif
 #ifndef VSR_SEG_FUSE
 // 1: the combination inside the segments pass (measured 0.125 ms per
 // config-0 frame against 0.067 ms with its own pass: the last groups'
@@ -549,6 +561,147 @@ __global__ void __launch_bounds__(256, Fused ? VSR_SEG_FUSED_MIN_BLOCKS : VSR_SE
   }
 }
 
+// One-pass alternative (VSR_VOLUME_REFILL): persistent warps, one ray per
+// lane marched sample after sample in the reference's order (the
+// compositing sums are the reference's, not re-associated); every
+// VSR_REFILL_SAMPLES samples the lanes whose ray ended take the next pixels
+// (one atomic per warp on the frame's pixel counter), set up their ray (camera,
+// clip planes, closest volume box entry) and write the pixels that miss
+// every volume at once.
+template <bool Count>
+__global__ void __launch_bounds__(256, VSR_REFILL_MIN_BLOCKS)
+    kVolumeRefill(DScene S, DCamera C, DRenderer R, DFrame F, MarchScratch M, int stageTF) {
+  extern __shared__ float4 sTF[];
+  stageTable(S, sTF, stageTF);
+  // the pixel counter was zeroed by kMarchReset
+  asm volatile("griddepcontrol.wait;\n" ::: "memory");
+  const int lane = threadIdx.x & 31;
+  const int numPix = F.width * F.height;
+  const bool hw = R.hwFilter != 0;
+  const float4 bg = make_float4(R.bg[0], R.bg[1], R.bg[2], R.bg[3]);
+  Rng none;
+  none.state = 0;
+  bool active = false, exhausted = false;
+  int pix = 0, vIdx = 0, steps = 0;
+  float3 o = f3(0.f), d = f3(0.f);
+  float t = 0.f, t1 = 0.f, dt = 0.f, expo = 0.f;
+  float Cr = 0.f, Cg = 0.f, Cb = 0.f, A = 0.f, T = 1.f;
+  uint32_t err = 0;
+  unsigned long long samples = 0;
+  auto finish = [&]() {
+    const float4 res = make_float4(A * Cr + (1.f - A) * bg.x, A * Cg + (1.f - A) * bg.y,
+                                   A * Cb + (1.f - A) * bg.z, A + (1.f - A) * bg.w);
+    const int y = pix / F.width;
+    writeSample(F, pix - y * F.width, y, false, res, 1e31f, f3(0.f), f3(0.f));
+    active = false;
+  };
+  for (int guard = 0; guard < (1 << 30); ++guard) {
+    // refill the lanes without a ray
+    while (!exhausted) {
+      const unsigned need = __ballot_sync(kFull, !active);
+      if (!need) break;
+      unsigned base = 0;
+      if (lane == 0) base = atomicAdd(&M.counters[0], (unsigned)__popc(need));
+      base = __shfl_sync(kFull, base, 0);
+      if (base >= (unsigned)numPix) {
+        exhausted = true;
+        break;
+      }
+      if (!active) {
+        const unsigned p = base + (unsigned)__popc(need & ((1u << lane) - 1u));
+        if (p < (unsigned)numPix) {
+          pix = (int)p;
+          const int x = pix % F.width, y = pix / F.width;
+          Ray ray = primaryRay<false>(C, none, (float)x, (float)y, (float)F.width, (float)F.height);
+          clipRay(ray, R);
+          int vi = -1;
+          float vT = FLT_MAX, vFar = 0.f;
+          float3 vlo = f3(0.f), vld = f3(0.f);
+          for (int i = 0; i < S.numInstances; ++i) {
+            const DInstance &I = S.instances[i];
+            const DGroup &G = S.groups[I.group];
+            for (int k = G.volBegin; k < G.volEnd; ++k) {
+              const int w = S.groupVolumes[k];
+              float3 lo, ld;
+              localRay(I, ray.o, ray.d, lo, ld);
+              BoxHit bh = intersectBox(lo, ld, S.volumes[w].boundsLo, S.volumes[w].boundsHi);
+              const bool h = bh.hit && bh.tfar >= ray.tmin && bh.tnear <= ray.tmax;
+              const float tt = fmaxf(ray.tmin, bh.tnear);
+              if (h && tt < vT) { vT = tt; vFar = bh.tfar; vi = w; vlo = lo; vld = ld; }
+            }
+          }
+          bool march = false;
+          if (vi >= 0) {
+            const DVolume &V = S.volumes[vi];
+            const float3 Sv = ld3(V.S);
+            o = Sv * (vlo + ld3(V.T));
+            d = Sv * vld;
+            t = vT;
+            t1 = fminf(ray.tmax, vFar);
+            dt = V.cellSize * R.samplingRateInv;
+            expo = dt / V.unitDistance;
+            vIdx = vi;
+            march = t <= t1;
+          }
+          Cr = Cg = Cb = A = 0.f;
+          T = 1.f;
+          steps = 0;
+          if (march) active = true;
+          else writeSample(F, x, y, false, bg, 1e31f, f3(0.f), f3(0.f));
+        }
+      }
+    }
+    if (!__any_sync(kFull, active)) break;
+    // rayMarchVolume<0>'s loop (VolumeIntegration.h:410-466), a few samples:
+    // the field values first (their fetches overlap), then the compositing
+    // in order with the loop's test before every sample
+    if (active) {
+      const DVolume &V = S.volumes[vIdx];
+      const float4 *tf = (stageTF && vIdx == 0) ? sTF : V.tf;
+      if (!(dt > 0.f) || steps > kMaxMarchSteps) {
+        err |= ERR_MARCH_LIMIT;
+        finish();
+      } else {
+        float val[VSR_REFILL_SAMPLES];
+        float tk = t;
+        int n = 0;
+#pragma unroll
+        for (int k = 0; k < VSR_REFILL_SAMPLES; ++k) {
+          if (tk <= t1) {
+            val[k] = fieldAt(V, o + d * tk, hw);
+            n = k + 1;
+          }
+          tk += dt;
+        }
+        bool done = n < VSR_REFILL_SAMPLES;
+#pragma unroll
+        for (int k = 0; k < VSR_REFILL_SAMPLES; ++k) {
+          if (k >= n) break;
+          if (!(A < 0.99f)) {
+            done = true;
+            break;
+          }
+          const float4 sm = classify(V, tf, val[k], hw);
+          const float stepTr = hw ? __powf(1.f - sm.w, expo) : powf(1.f - sm.w, expo);
+          const float w = T * (1.f - stepTr);
+          Cr += w * sm.x; Cg += w * sm.y; Cb += w * sm.z;
+          A += w;
+          T *= stepTr;
+          t += dt;
+          ++steps;
+          if (Count) ++samples;
+        }
+        if (done || !(t <= t1 && A < 0.99f)) finish();
+      }
+    }
+  }
+  if (Count) {
+    for (int off = 16; off > 0; off >>= 1) samples += __shfl_xor_sync(kFull, samples, off);
+    if (lane == 0 && samples) atomicAdd(&F.counters[3], samples);
+  }
+  if (err) atomicOr(F.errorFlags, err);
+}
+
 // Pass 3: one warp per group.
 template <bool Count>
 __global__ void __launch_bounds__(256) kVolumeCombine(DScene S, DRenderer R, DFrame F,
@@ -615,6 +768,23 @@ cudaError_t launchVolumeMarch(const DScene &S, const DCamera &C, const DRenderer
   const int stage = stageTFSize > 0;
   const int numPix = F.width * F.height;
   kMarchReset<<<1, 32, 0, stream>>>(M.counters);
+  if (VSR_VOLUME_REFILL) {
+    const void *fn = count ? (const void *)kVolumeRefill<true> : (const void *)kVolumeRefill<false>;
+    const int perSM = persistentBlocksPerSM(fn, smem);
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(sms * perSM);
+    cfg.blockDim = dim3(256);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = stream;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    if (count) cudaLaunchKernelEx(&cfg, kVolumeRefill<true>, S, C, R, F, M, stage);
+    else cudaLaunchKernelEx(&cfg, kVolumeRefill<false>, S, C, R, F, M, stage);
+    return cudaGetLastError();
+  }
   {
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(min((numPix + 255) / 256, sms * 8));

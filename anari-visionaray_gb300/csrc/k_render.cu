@@ -31,7 +31,7 @@ __global__ void __launch_bounds__(VSR_RAYCAST_BLOCK_X * VSR_RAYCAST_BLOCK_Y,
 // Two register budgets of the same body: worlds with volumes keep more path
 // state live during delta tracking and run faster with fewer resident
 // blocks and fewer spills (64 registers); surface-only worlds with more
-// blocks at 40 registers. Full = true adds the optional features (gradient
+// blocks at 32 registers. Full = true adds the optional features (gradient
 // shading of volume scatter events, point and spot lights).
 template <bool Count, bool Volumes, bool Full>
 __global__ void __launch_bounds__(16 * VSR_MEGA_BLOCK_Y,

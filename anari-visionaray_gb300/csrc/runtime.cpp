@@ -2109,7 +2109,7 @@ struct FrameObj : Object {
   size_t marchPixels = 0;
   unsigned unitCap = 0;
   std::map<std::string, void *> pinned;
-  uint32_t *errHost = nullptr;
+  uint32_t *errHost = nullptr;  // pinned: [0] error flags, [1] march work units the last frame needed
   cudaEvent_t evStart = nullptr, evRender = nullptr, evStop = nullptr;
   int accumID = 0;
   uint64_t lastStamp = 0;
@@ -2154,9 +2154,25 @@ struct FrameObj : Object {
   // scratch of the segmented volume marcher, made on first use: the ray list
   // (48 B per pixel), groups (16 B per 32 pixels) and work units for
   // 64 / VSR_SEG_SAMPLES segments per pixel (1 KiB per unit of 32 segments);
-  // rays beyond that are marched whole by the combining warps
+  // rays beyond that are marched whole by the combining warps, one ray at a
+  // time per warp, which is slow for long rays. The set-up pass counts the
+  // units a frame needs (copied to errHost[1] after the frame): when the
+  // last frame needed more (large volumes filling the image), the unit list
+  // grows to that count plus a quarter, up to kMaxMarchUnits, so later
+  // frames of the same view are marched by segments.
+  static constexpr size_t kMaxMarchUnits = size_t(1) << 22;  // 4 GiB of composites
   bool ensureMarch() {
     size_t np = (size_t)width * height;
+    const size_t need = errHost[1];
+    if (marchPixels == np && need > unitCap && unitCap < kMaxMarchUnits) {
+      const size_t cap = std::min(need + need / 4, kMaxMarchUnits);
+      if (unitGroup.alloc(cap * sizeof(int)) == cudaSuccess &&
+          segOut.alloc(cap * 1024) == cudaSuccess) {
+        unitCap = (unsigned)cap;
+        return true;
+      }
+      marchPixels = 0;  // allocation failed: back to the default size below
+    }
     if (marchPixels == np) return true;
     const size_t cap = std::max<size_t>(np * 2 / VSR_SEG_SAMPLES, 4096);
     const size_t numGroups = (np + 31) / 32;
@@ -2205,8 +2221,8 @@ struct FrameObj : Object {
     cudaEventCreate(&evStart);
     cudaEventCreate(&evRender);
     cudaEventCreate(&evStop);
-    cudaMallocHost((void **)&errHost, sizeof(uint32_t));
-    *errHost = 0;
+    cudaMallocHost((void **)&errHost, 2 * sizeof(uint32_t));
+    errHost[0] = errHost[1] = 0;
   }
   ~FrameObj() override {
     if (evStart) cudaEventSynchronize(evStop);
@@ -2419,6 +2435,10 @@ VSRStatus renderFrame(Device *dev, FrameObj *F) {
   }
   cudaEventRecord(F->evStop, s);
   cudaMemcpyAsync(F->errHost, F->errFlags.p, sizeof(uint32_t), cudaMemcpyDeviceToHost, s);
+  // the work units this frame needed (the set-up pass's unit counter), read
+  // by the next frame's ensureMarch
+  if (doRender && segmented)
+    cudaMemcpyAsync(F->errHost + 1, ms.counters + 2, sizeof(uint32_t), cudaMemcpyDeviceToHost, s);
   if (F->countStats)
     cudaMemcpyAsync(F->countersHost, F->counters.p, kStatCounters * sizeof(unsigned long long),
                     cudaMemcpyDeviceToHost, s);
@@ -3015,6 +3035,16 @@ int vsrGetProperty(VSRDevice dv, VSRObject ov, const char *name, VSRDataType typ
     }
     if (n == "errorFlags" && type == VSR_UINT32 && size >= 4) {
       *(uint32_t *)mem = *F->errHost;
+      return 1;
+    }
+    // segmented volume marcher: the work units the last frame needed, and
+    // how many the frame's unit list holds now
+    if (n == "march.unitsNeeded" && type == VSR_UINT32 && size >= 4) {
+      *(uint32_t *)mem = F->errHost[1];
+      return 1;
+    }
+    if (n == "march.unitCapacity" && type == VSR_UINT32 && size >= 4) {
+      *(uint32_t *)mem = F->unitCap;
       return 1;
     }
     if (n == "commitDuration" && type == VSR_FLOAT32 && size >= 4 && F->world) {

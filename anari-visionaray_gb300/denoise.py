@@ -140,26 +140,37 @@ def train(dn, x, t, steps, batch=16, crop=128, lr=1e-3, seed=0, log_every=0, war
     g = torch.Generator(device="cpu")
     g.manual_seed(seed)
     n, H, W, _ = x.shape
-    losses = []
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    for s in range(steps):
+    # every step's crops (image, row, column), drawn in the order of one
+    # step after another, moved to the device once
+    picks = []
+    for _ in range(steps):
         idx = torch.randint(0, n, (batch,), generator=g)
         oy = torch.randint(0, (H - crop) // 8 + 1, (batch,), generator=g) * 8
         ox = torch.randint(0, (W - crop) // 8 + 1, (batch,), generator=g) * 8
-        xb = torch.stack([x[int(i), int(a):int(a) + crop, int(b):int(b) + crop]
-                          for i, a, b in zip(idx, oy, ox)]).contiguous()
-        tb = torch.stack([t[int(i), int(a):int(a) + crop, int(b):int(b) + crop]
-                          for i, a, b in zip(idx, oy, ox)]).contiguous()
-        # torch made the crops on its own stream; the step runs on the device's
-        torch.cuda.synchronize()
-        ramp = min(1.0, (s + 1) / max(1, warmup if warmup is not None else steps // 20))
-        rate = lr * ramp * 0.5 * (1.0 + math.cos(math.pi * s / steps))
-        want = bool(log_every) and (s % log_every == 0 or s == steps - 1)
-        loss = dn.train_step(xb.data_ptr(), tb.data_ptr(), 4, batch, crop, crop, rate,
-                             want_loss=True)
-        if want:
-            losses.append((s, loss))
+        picks.append(torch.stack([idx, oy, ox]))
+    picks = torch.stack(picks).to(x.device)  # (steps, 3, batch)
+    ar = torch.arange(crop, device=x.device)
+    losses = []
+    # the crops are gathered on the device's own stream, so each step's
+    # kernels follow its gather without a host synchronisation; the loss is
+    # read back (which waits for the step) only where it is logged
+    stream = torch.cuda.ExternalStream(dn.dev.lib.vsrDeviceStream(dn.dev.handle))
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    with torch.cuda.stream(stream):
+        for s in range(steps):
+            idx, oy, ox = picks[s]
+            rows = (oy[:, None] + ar[None, :])[:, :, None]
+            cols = (ox[:, None] + ar[None, :])[:, None, :]
+            xb = x[idx[:, None, None], rows, cols].contiguous()
+            tb = t[idx[:, None, None], rows, cols].contiguous()
+            ramp = min(1.0, (s + 1) / max(1, warmup if warmup is not None else steps // 20))
+            rate = lr * ramp * 0.5 * (1.0 + math.cos(math.pi * s / steps))
+            want = (bool(log_every) and s % log_every == 0) or s == steps - 1
+            loss = dn.train_step(xb.data_ptr(), tb.data_ptr(), 4, batch, crop, crop, rate,
+                                 want_loss=want)
+            if want and log_every:
+                losses.append((s, loss))
     return losses, time.perf_counter() - t0
 
 

@@ -147,14 +147,17 @@ def measured_peaks():
     return 6800.0, "fallback"
 
 
-def measured_peaks_tensor():
+def measured_peaks_tensor(sustained=False):
+    """bf16 tensor peak in TFLOP/s: the burst figure (a kernel timed alone)
+    or the sustained one (a kernel timed inside a long loop)."""
+    key = "bf16_tflops_sustained" if sustained else "bf16_tflops"
     path = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(path):
         with open(path) as f:
             d = json.load(f)
-        if "bf16_tflops" in d:
-            return d["bf16_tflops"], "measured"
-    return 1900.0, "fallback"
+        if key in d:
+            return d[key], "measured"
+    return (1700.0 if sustained else 1900.0), "fallback"
 
 
 def profiled_value(name, key):
@@ -529,6 +532,25 @@ def denoiser_roofline(dn_s):
                     "decoders read upsampled level and skip in place"}
 
 
+def denoiser_train_roofline(ms_per_step, batch=16, crop=128):
+    """Tensor roofline of one training step: the forward pass, the weight
+    gradient of every layer and the input gradient of every layer but the
+    first (the network's input needs none), each 2 Cin Cout 9 flops per
+    pixel of its level, over the measured step time (which also holds the
+    loss, pooling, upsampling and Adam kernels), against the sustained bf16
+    peak (the step runs in a loop of thousands)."""
+    px = batch * crop * crop
+    per = [2.0 * ci * co * 9 * px / 4 ** lvl for ci, co, lvl in DENOISER_LAYERS]
+    flops = 2 * sum(per) + sum(per[1:])
+    peak = measured_peaks_tensor(sustained=True)
+    achieved = flops / (ms_per_step * 1e-3) / 1e12
+    return {"bound": "tensor", "achieved": achieved, "peak": peak[0], "unit": "TFLOP/s",
+            "frac": achieved / peak[0],
+            "note": f"training step of {batch} {crop}^2 crops ({flops / 1e9:.1f} GFLOP: forward, "
+                    f"weight and input gradients) over the measured step time; peak bf16 "
+                    f"sustained {peak[1]}"}
+
+
 def measure_denoiser_forward(pkg, dev):
     """The 1080p denoiser pass alone (weights as initialised; the time does
     not depend on their values), for profiling the network's kernels."""
@@ -597,6 +619,7 @@ def measure_denoiser_config4(pkg, dev, train_scenes=128, eval_scenes=8, steps=40
                    "times"},
         "pt_ms_per_spp_1080p": 1e3 * pt_s_per_spp, "denoise_ms_1080p": 1e3 * dn_s,
         "train_s": train_s, "train_ms_per_step": 1e3 * train_s / steps, "data_s": data_s,
+        "train_roofline": denoiser_train_roofline(1e3 * train_s / steps),
         "loss": losses,
         "roofline": denoiser_roofline(dn_s),
     }

@@ -181,7 +181,10 @@ VSR_API VSRStatus vsrRetain(VSRDevice d, VSRObject o);
    build), "errorFlags" (UINT32, device-side error bits of the last render:
    1 traversal stack full, 2 DDA step limit, 4 delta-tracking step limit,
    8 path pass limit, 16 ray-march step limit, 32 transparent-layer limit,
-   64 a NaN or infinite path sample was dropped); world "bvh.nodes" /
+   64 a NaN or infinite path sample was dropped), "march.unitsNeeded" and
+   "march.unitCapacity" (UINT32, volume-only raycast frames: the work units
+   of 32 ray segments the last frame needed, and the frame's unit list
+   size, which grows to the need of the frame before); world "bvh.nodes" /
    "bvh.triangles" (UINT64). Frame channel "channel.variance" (FLOAT32, an
    extension) holds the path tracer's variance of each pixel's accumulated
    mean luminance. Returns 1 if found. */

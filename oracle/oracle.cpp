@@ -484,7 +484,11 @@ inline bool hitTri(const Ray &r, const Tri &T, float tmin, float &t, float &u, f
 
 // Iso-surface test, intersect(Ray, ISOSurface), DeviceCopyableObjects.h:
 // 825-911, as the reference's CPU device runs it but without its 16^3
-// empty-space grid (which only skips cells that hold no crossing): in voxel
+// empty-space grid. A known divergence: the reference restarts the march in
+// each grid cell whose value range holds an iso value, so a lattice
+// interval straddling such a cell and an empty one is not sampled there,
+// while this march samples it (a crossing next to an empty cell may come
+// out at a slightly different t). Here: in voxel
 // space with the direction normalised, samples on the lattice anchored at
 // tmin - dt/2 (by repeated addition, dt = (min spacing / 2) |S d|) over
 // [tmin, tmax] clipped to the field box; the first lattice interval whose

@@ -1350,3 +1350,38 @@ def test_pathtrace_bezier_curves_same_stream(pkg, device, oracle, wavefront):
     assert not np.isnan(gpu["color"]).any()
     d = np.abs(gpu["color"][..., :3] - F.color[..., :3]).max(axis=-1)
     assert float((d <= 1e-3).mean()) >= 0.97, float((d <= 1e-3).mean())
+
+
+def test_raycast_volume_march_units_grow(pkg, device, oracle):
+    """A blob volume filling a 192^2 view needs more segment work units than
+    the frame's first unit list holds: the first frame marches the rays
+    beyond it whole, the next one with the list grown to the first frame's
+    need; both match the oracle at the raycast bar."""
+    import math
+    sc = pkg.scenes.config0(res=192, n=128)
+    extent = 127.0
+    view = np.array([0.6, 0.45, 0.66])
+    view /= np.linalg.norm(view)
+    eye = np.array([extent / 2] * 3) + 0.75 * math.sqrt(3.0) * extent * view
+    sc["camera"] = pkg.scenes._look_at_camera([extent / 2] * 3, list(eye), 40.0, 1.0)
+    _, F = render_oracle(oracle, sc)
+    h = pkg.scenes.build(device, sc)
+    try:
+        caps = []
+        for k in range(2):
+            assert device.render(h["frame"]) == 0
+            assert device.wait(h["frame"])
+            gpu = {"color": device.map(h["frame"], "channel.color")}
+            good, frac = raycast_ok(gpu, F)
+            assert good, (k, frac)
+            assert device.get_uint(h["frame"], "errorFlags") == 0
+            caps.append((device.get_uint(h["frame"], "march.unitsNeeded"),
+                         device.get_uint(h["frame"], "march.unitCapacity")))
+        (need0, cap0), (need1, cap1) = caps
+        assert need0 > cap0, caps  # the first frame's list was too short
+        assert need1 == need0 and cap1 >= need1, caps
+    finally:
+        for o in (h["frame"], h["renderer"], h["camera"], h["world"]):
+            device.release(o)
+        for o in h["keep"]:
+            device.release(o)

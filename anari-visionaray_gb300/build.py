@@ -24,7 +24,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC", "-I" + INCLUDE, *ARCH]
 CXX_FLAGS = ["-std=c++17", "-O2", "-fPIC", "-fvisibility=hidden", "-ffp-contract=off", "-Wall", "-I" + INCLUDE]
 
-CU_SOURCES = ["k_render.cu", "k_wavefront.cu", "k_bvh.cu", "k_bvh_ploc.cu", "k_bvh4.cu", "k_bvh_noalloc.cu", "k_volume.cu", "k_volume_march.cu", "k_batch.cu", "k_denoise.cu", "k_denoise_tc.cu", "k_denoise_ws.cu", "k_denoise_wg.cu"]
+CU_SOURCES = ["k_render.cu", "k_wavefront.cu", "k_bvh.cu", "k_bvh_ploc.cu", "k_bvh4.cu", "k_bvh_leaves.cu", "k_bvh_noalloc.cu", "k_volume.cu", "k_volume_march.cu", "k_batch.cu", "k_denoise.cu", "k_denoise_tc.cu", "k_denoise_ws.cu", "k_denoise_wg.cu"]
 CPP_SOURCES = ["runtime.cpp", "denoiser.cpp"]
 HEADERS = ["vsr_device.h", "render_common.cuh", "render_pixel.cuh", "kernels.h", "bvh_kernels.cuh", "denoiser.h"]
 

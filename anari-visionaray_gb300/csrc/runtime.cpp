@@ -1590,6 +1590,9 @@ struct GroupGPU {
   float buildMs = 0.f;
 };
 
+// world parameter bvhLeafSize when unset
+constexpr int kDefaultLeafSize = 4;
+
 struct World : Object {
   Group implicitGroup;
   bool implicitUsed = false;
@@ -1604,6 +1607,7 @@ struct World : Object {
   uint64_t bvhNodes = 0, bvhTris = 0;
   bool fastBuild = false;
   int bvhWidth = 2;
+  int bvhLeafSize = kDefaultLeafSize;
 
   World(Device *d, VSRDataType k, std::string st)
       : Object(d, k, st), implicitGroup(d, VSR_GROUP, "") {
@@ -1634,6 +1638,12 @@ struct World : Object {
     int w = 2;
     geti("bvhWidth", w);
     bvhWidth = w == 4 ? 4 : 2;
+    // most triangles per leaf of the 2-wide triangle BVHs (1: one per leaf,
+    // as built; up to 32): small subtrees become leaves where the surface-
+    // area heuristic expects fewer node visits
+    int leaf = kDefaultLeafSize;
+    geti("bvhLeafSize", leaf);
+    bvhLeafSize = std::min(std::max(leaf, 1), 32);
     implicitUsed = !implicitGroup.surfaces.empty() || !implicitGroup.volumes.empty() ||
                    !implicitGroup.lights.empty();
     valid = true;
@@ -1842,6 +1852,18 @@ struct World : Object {
         gg->numNodes = st.numNodes;
         gg->buildMs = st.buildMs;
         gg->width = 2;
+        if (bvhWidth == 2 && bvhLeafSize > 1) {
+          auto tl = std::chrono::steady_clock::now();
+          e = collapseLeaves(gg->nodes.as<float4>(), st.numNodes, gg->tris.as<float4>(), nt,
+                             bvhLeafSize, s);
+          if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+          if (e != cudaSuccess) {
+            dev->report(this, kind, VSR_SEVERITY_ERROR, VSR_ERROR_CUDA, "BVH leaf collapse failed: %s",
+                        cudaGetErrorString(e));
+            return false;
+          }
+          gg->buildMs += std::chrono::duration<float, std::milli>(std::chrono::steady_clock::now() - tl).count();
+        }
         if (bvhWidth == 4 && st.numNodes > 0) {
           int n4 = 0;
           auto t4 = std::chrono::steady_clock::now();

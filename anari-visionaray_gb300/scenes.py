@@ -583,6 +583,8 @@ def build(dev, scene, channels=("color", "depth", "normal", "albedo"), collect_s
         dev.set(world, "bvhBuild", scene["bvhBuild"])
     if "bvhWidth" in scene:
         dev.set(world, "bvhWidth", int(scene["bvhWidth"]))
+    if "bvhLeafSize" in scene:
+        dev.set(world, "bvhLeafSize", int(scene["bvhLeafSize"]))
     dev.commit(world)
     cam = dev.camera(scene["camera"]["type"])
     apply_camera(dev, cam, scene["camera"])

@@ -50,6 +50,8 @@ def parse():
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--accum-frames", type=int, default=64,
                    help="config 1 also as this many accumulated 1-spp frames (0: skip)")
+    p.add_argument("--bvh-leaf-size", type=int, default=None,
+                   help="world parameter bvhLeafSize of the config-1 scene (default: the library's)")
     p.add_argument("--sample-chunks", type=int, default=8,
                    help="config 1: the frame's samples as this many concurrent per-pixel streams "
                         "(accumulated sub-frames); 1 = one stream per pixel and frame")
@@ -468,7 +470,9 @@ def measure_batch_config3(pkg, dev, steps=3, num_scenes=64, profile_range=False)
 def time_denoiser_1080p(dev, dn, D, masked_out=None):
     """At 1920x1080: path-tracing seconds per sample per pixel, and the
     median seconds of one denoiser pass (vsrDenoiseFrame: input assembly,
-    network, gate) after 3 warm-up passes."""
+    network, gate) after 3 warm-up passes, as host wall time (with the
+    launches and the synchronisation of the call) and as device time (CUDA
+    events on the device's stream)."""
     import torch
 
     sc = D.training_scene(10001, res=1920, spp=16)
@@ -488,10 +492,17 @@ def time_denoiser_1080p(dev, dn, D, masked_out=None):
     for _ in range(3):
         dn.denoise_frame(h["frame"], out.data_ptr())
     ds = []
+    stream = torch.cuda.ExternalStream(dev.lib.vsrDeviceStream(dev.handle))
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+    dev_ms = []
     for _ in range(10):
         tt = time.perf_counter()
+        ev[0].record(stream)
         dn.denoise_frame(h["frame"], out.data_ptr())  # synchronous: returns the retry count
+        ev[1].record(stream)
         ds.append(time.perf_counter() - tt)
+        ev[1].synchronize()
+        dev_ms.append(ev[0].elapsed_time(ev[1]))
     # frames restricted to the gate's rejected pixels: device time per
     # rendered pixel-sample (warps with few rejected pixels still cost)
     mask = torch.zeros(1920 * 1080, dtype=torch.uint8, device="cuda")
@@ -511,7 +522,7 @@ def time_denoiser_1080p(dev, dn, D, masked_out=None):
     D.release(dev, h)
     if masked_out is not None:
         masked_out.update(masked or {})
-    return pt_s_per_spp, statistics.median(ds)
+    return pt_s_per_spp, statistics.median(ds), 1e-3 * statistics.median(dev_ms)
 
 
 DENOISER_LAYERS = [(16, 32, 0), (32, 32, 0), (32, 64, 1), (64, 64, 1), (64, 128, 2), (128, 128, 2),
@@ -524,8 +535,9 @@ def denoiser_roofline(dn_s):
     peak = measured_peaks_tensor()
     return {"bound": "tensor", "achieved": flops / dn_s / 1e12, "peak": peak[0],
             "unit": "TFLOP/s", "frac": flops / dn_s / 1e12 / peak[0],
-            "note": f"denoiser forward at 1920x1080 ({flops / 1e12:.3f} TFLOP incl. "
-                    f"input and gate kernels in the time); peak bf16 {peak[1]}; "
+            "note": f"denoiser forward at 1920x1080 ({flops / 1e12:.3f} TFLOP; the device "
+                    f"time of the whole pass, CUDA events, with its input and gate kernels); "
+                    f"peak bf16 {peak[1]}; "
                     "tcgen05.mma kind::f16 (bf16 -> fp32 in tensor memory), persistent "
                     "warp-specialised kernel (TMA producer, MMA thread, epilogue warps) "
                     "on 4 x 128-pixel halo tiles of channel-blocked activations; "
@@ -556,11 +568,12 @@ def measure_denoiser_forward(pkg, dev):
     not depend on their values), for profiling the network's kernels."""
     D = importlib.import_module(pkg.__name__ + ".denoise")
     dn = pkg.vsr.Denoiser(dev, seed=1)
-    pt_s_per_spp, dn_s = time_denoiser_1080p(dev, dn, D)
+    pt_s_per_spp, dn_s, dn_dev_s = time_denoiser_1080p(dev, dn, D)
     dn.close()
     return {"workload": "config4 denoiser forward at 1920x1080 (untrained weights)",
             "pt_ms_per_spp_1080p": 1e3 * pt_s_per_spp, "denoise_ms_1080p": 1e3 * dn_s,
-            "roofline": denoiser_roofline(dn_s)}
+            "denoise_device_ms_1080p": 1e3 * dn_dev_s,
+            "roofline": denoiser_roofline(dn_dev_s)}
 
 
 def measure_denoiser_config4(pkg, dev, train_scenes=128, eval_scenes=8, steps=4000,
@@ -586,7 +599,7 @@ def measure_denoiser_config4(pkg, dev, train_scenes=128, eval_scenes=8, steps=40
     ev = D.evaluate(dev, dn, list(range(10001, 10001 + eval_scenes)), res=res,
                     ref_spp=eval_ref_spp, denoise_levels=levels)
     masked = {}
-    pt_s_per_spp, dn_s = time_denoiser_1080p(dev, dn, D, masked_out=masked)
+    pt_s_per_spp, dn_s, dn_dev_s = time_denoiser_1080p(dev, dn, D, masked_out=masked)
     loop = D.evaluate_gated_loop(dev, dn, list(range(10001, 10001 + eval_scenes)), res=res,
                                  ref_spp=eval_ref_spp)
     dn.close()
@@ -618,10 +631,11 @@ def measure_denoiser_config4(pkg, dev, train_scenes=128, eval_scenes=8, steps=40
                    "at 1080p from the measured per-sample, masked per-pixel-sample and denoiser "
                    "times"},
         "pt_ms_per_spp_1080p": 1e3 * pt_s_per_spp, "denoise_ms_1080p": 1e3 * dn_s,
+        "denoise_device_ms_1080p": 1e3 * dn_dev_s,
         "train_s": train_s, "train_ms_per_step": 1e3 * train_s / steps, "data_s": data_s,
         "train_roofline": denoiser_train_roofline(1e3 * train_s / steps),
         "loss": losses,
-        "roofline": denoiser_roofline(dn_s),
+        "roofline": denoiser_roofline(dn_dev_s),
     }
 
 
@@ -730,6 +744,8 @@ def run_ours(args):
     scene = pkg.scenes.config1(res=args.res, spp=args.spp)
     scene["renderer"]["wavefront"] = args.wavefront
     scene["renderer"]["sampleChunks"] = args.sample_chunks
+    if args.bvh_leaf_size is not None:
+        scene["bvhLeafSize"] = args.bvh_leaf_size
     ntris = pkg.scenes.triangle_count(scene)
     dev = vsr.Device()
     h = pkg.scenes.build(dev, scene)

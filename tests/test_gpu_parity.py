@@ -664,6 +664,25 @@ def test_bvh_build_policies_give_the_same_image(pkg, device, build, width):
     assert float((d <= 1e-6).mean()) >= 0.995
 
 
+@pytest.mark.parametrize("leaf", [1, 2, 8, 32])
+@pytest.mark.parametrize("build", ["quality", "fast"])
+def test_bvh_leaf_sizes_give_the_same_image(pkg, device, build, leaf):
+    """Leaves of up to `leaf` triangles (world parameter bvhLeafSize, the
+    depth-first triangle order and relinked nodes of the leaf collapse)
+    against the default leaf size: the same hits, so the same depth and,
+    up to rare exact ties, the same colour, for both builders."""
+    sc = small_spheres(pkg, res=96, spp=2, n=20)
+    sc["bvhBuild"] = build
+    a = render_gpu(pkg, device, sc)
+    sc["bvhLeafSize"] = leaf
+    b = render_gpu(pkg, device, sc)
+    assert np.array_equal(a["depth"], b["depth"])
+    assert np.array_equal(a["normal"], b["normal"])
+    d = np.abs(a["color"] - b["color"]).max(axis=-1)
+    assert float((d <= 1e-6).mean()) >= 0.995
+    assert a["errorFlags"] == 0 and b["errorFlags"] == 0
+
+
 def translucent_spheres(pkg, renderer, res=96, spp=8, n=16):
     """The sphere set with non-opaque materials: a third "blend" with opacity
     0.25..0.75, a third "mask" with opacity either side of its cutoff (0.5),

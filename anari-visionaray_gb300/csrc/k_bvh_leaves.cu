@@ -1,9 +1,9 @@
 // Leaf collapse for the triangle BVHs of world commits. Both builders make
 // one triangle per leaf. A bottom-up surface-area-heuristic pass turns small
 // subtrees into leaves of up to maxLeaf triangles where that lowers the
-// expected cost of a ray (an inner-node visit tests both child boxes and
-// costs about as much as one triangle test), so rays visit fewer inner
-// nodes. The triangles are then put in depth-first leaf order, which makes
+// expected cost of a ray (an inner-node visit tests both child boxes; a
+// triangle test is priced at three quarters of one), so rays visit fewer
+// inner nodes. The triangles are then put in depth-first leaf order, which makes
 // every subtree's triangles contiguous, and the child links of the nodes
 // that remain are rewritten to the (first, count) leaf codes of
 // vsr_device.h. The inner nodes of collapsed subtrees stay in the array,
@@ -14,8 +14,11 @@
 namespace vsr {
 namespace {
 
+// relative costs (measured on the 1M-triangle sphere scene: a triangle test
+// priced at 0.5 / 0.75 / 1 inner-node visits gave 202.4 / 200.0 / 200.9 ms
+// per frame)
 constexpr float kCostInner = 1.f;  // one inner-node visit (both child boxes)
-constexpr float kCostTri = 1.f;    // one triangle test
+constexpr float kCostTri = 0.75f;  // one triangle test
 constexpr int kBlock = 256;
 
 __device__ __forceinline__ float halfArea(float lx, float hx, float ly, float hy, float lz,

@@ -1591,7 +1591,7 @@ struct GroupGPU {
 };
 
 // world parameter bvhLeafSize when unset
-constexpr int kDefaultLeafSize = 4;
+constexpr int kDefaultLeafSize = 8;
 
 struct World : Object {
   Group implicitGroup;

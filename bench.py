@@ -52,7 +52,7 @@ def parse():
                    help="config 1 also as this many accumulated 1-spp frames (0: skip)")
     p.add_argument("--bvh-leaf-size", type=int, default=None,
                    help="world parameter bvhLeafSize of the config-1 scene (default: the library's)")
-    p.add_argument("--sample-chunks", type=int, default=8,
+    p.add_argument("--sample-chunks", type=int, default=16,
                    help="config 1: the frame's samples as this many concurrent per-pixel streams "
                         "(accumulated sub-frames); 1 = one stream per pixel and frame")
     p.add_argument("--wavefront", action="store_true",

@@ -64,6 +64,8 @@ def parse():
     p.add_argument("--volume-res", type=int, nargs=2, default=[1920, 1080],
                    help="config-2 frame size (full size by default; smaller for profiling)")
     p.add_argument("--volume-spp", type=int, default=256)
+    p.add_argument("--volume-sample-chunks", type=int, default=8,
+                   help="config 2: the frame's samples as this many per-pixel streams")
     p.add_argument("--no-denoise", dest="denoise", action="store_false",
                    help="skip the config-4 denoiser training and evaluation")
     p.add_argument("--denoise-train-scenes", type=int, default=128)
@@ -639,7 +641,7 @@ def measure_denoiser_config4(pkg, dev, train_scenes=128, eval_scenes=8, steps=40
     }
 
 
-def measure_volume_config2(pkg, dev, flush, count_spp=8, res=(1920, 1080), spp=256):
+def measure_volume_config2(pkg, dev, flush, count_spp=8, res=(1920, 1080), spp=256, chunks=8):
     """Config 2 (volumetric path tracing, 512^3 value noise with 16^3-voxel
     brick majorants + the config-1 spheres, 1920x1080, 256 spp, depth 8,
     clip plane): Mpx*spp/s of one full frame, and the delta-tracking
@@ -647,10 +649,10 @@ def measure_volume_config2(pkg, dev, flush, count_spp=8, res=(1920, 1080), spp=2
     import torch
 
     scene = pkg.scenes.config2(res=tuple(res), spp=spp)
-    # the frame's samples as 8 concurrent per-pixel streams (sample chunks:
-    # the sub-frames the reference accumulates over 8 frames), 3 % faster
-    # than one stream per pixel
-    scene["renderer"]["sampleChunks"] = 8
+    # the frame's samples as concurrent per-pixel streams (sample chunks:
+    # the sub-frames the reference accumulates over that many frames); 8
+    # are 3 % faster than one stream per pixel
+    scene["renderer"]["sampleChunks"] = chunks
     W, H = scene["frame"]["size"]
     count_spp = min(count_spp, spp)
     spp = scene["renderer"]["pixelSamples"]
@@ -681,7 +683,7 @@ def measure_volume_config2(pkg, dev, flush, count_spp=8, res=(1920, 1080), spp=2
     return {"value": W * H * spp / t / MPX, "unit": "Mpx*spp/s", "ms_per_frame": 1e3 * t,
             "workload": f"config2 volumetric pathtracer {W}x{H} {spp}spp depth8, 512^3 value noise "
                         "(16^3 bricks) + 1015810 tris, clip plane",
-            "sample_chunks": 8,
+            "sample_chunks": chunks,
             "error_flags": err,
             "tracking_samples_est": track, "majorant_cells_est": cells,
             "roofline": {"bound": "hbm", "achieved": alg / t / 1e9, "peak": peak, "unit": "GB/s",
@@ -855,7 +857,8 @@ def run_ours(args):
         denoiser = measure_denoiser_config4(pkg, dev, train_scenes=args.denoise_train_scenes,
                                             eval_scenes=args.denoise_eval_scenes,
                                             steps=args.denoise_steps)
-    volume = (measure_volume_config2(pkg, dev, flush, res=args.volume_res, spp=args.volume_spp)
+    volume = (measure_volume_config2(pkg, dev, flush, res=args.volume_res, spp=args.volume_spp,
+                                     chunks=args.volume_sample_chunks)
               if args.volume else None)
 
     kernel_s = sum(durations) / len(durations)

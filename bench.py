@@ -51,7 +51,7 @@ def parse():
     p.add_argument("--accum-frames", type=int, default=64,
                    help="config 1 also as this many accumulated 1-spp frames (0: skip)")
     p.add_argument("--bvh-leaf-size", type=int, default=None,
-                   help="world parameter bvhLeafSize of the config-1 scene (default: the library's)")
+                   help="world parameter bvhLeafSize of the config-1 and -2 scenes (default: the library's)")
     p.add_argument("--sample-chunks", type=int, default=16,
                    help="config 1: the frame's samples as this many concurrent per-pixel streams "
                         "(accumulated sub-frames); 1 = one stream per pixel and frame")
@@ -641,7 +641,8 @@ def measure_denoiser_config4(pkg, dev, train_scenes=128, eval_scenes=8, steps=40
     }
 
 
-def measure_volume_config2(pkg, dev, flush, count_spp=8, res=(1920, 1080), spp=256, chunks=8):
+def measure_volume_config2(pkg, dev, flush, count_spp=8, res=(1920, 1080), spp=256, chunks=8,
+                           leaf_size=None):
     """Config 2 (volumetric path tracing, 512^3 value noise with 16^3-voxel
     brick majorants + the config-1 spheres, 1920x1080, 256 spp, depth 8,
     clip plane): Mpx*spp/s of one full frame, and the delta-tracking
@@ -653,6 +654,8 @@ def measure_volume_config2(pkg, dev, flush, count_spp=8, res=(1920, 1080), spp=2
     # the sub-frames the reference accumulates over that many frames); 8
     # are 3 % faster than one stream per pixel
     scene["renderer"]["sampleChunks"] = chunks
+    if leaf_size is not None:
+        scene["bvhLeafSize"] = leaf_size
     W, H = scene["frame"]["size"]
     count_spp = min(count_spp, spp)
     spp = scene["renderer"]["pixelSamples"]
@@ -858,7 +861,7 @@ def run_ours(args):
                                             eval_scenes=args.denoise_eval_scenes,
                                             steps=args.denoise_steps)
     volume = (measure_volume_config2(pkg, dev, flush, res=args.volume_res, spp=args.volume_spp,
-                                     chunks=args.volume_sample_chunks)
+                                     chunks=args.volume_sample_chunks, leaf_size=args.bvh_leaf_size)
               if args.volume else None)
 
     kernel_s = sum(durations) / len(durations)

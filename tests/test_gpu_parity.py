@@ -683,6 +683,20 @@ def test_bvh_leaf_sizes_give_the_same_image(pkg, device, build, leaf):
     assert a["errorFlags"] == 0 and b["errorFlags"] == 0
 
 
+def test_bvh_leaf_size_in_a_volume_world(pkg, device):
+    """Worlds with volumes keep one triangle per leaf unless bvhLeafSize is
+    set; set to 8 the same path-traced frame comes out (same hits, the same
+    random stream through the delta tracking)."""
+    sc = small_volume_scene(pkg, res=64, spp=4, spheres=12)
+    a = render_gpu(pkg, device, sc)
+    sc["bvhLeafSize"] = 8
+    b = render_gpu(pkg, device, sc)
+    assert np.array_equal(a["depth"], b["depth"])
+    d = np.abs(a["color"] - b["color"]).max(axis=-1)
+    assert float((d <= 1e-6).mean()) >= 0.995
+    assert a["errorFlags"] == 0 and b["errorFlags"] == 0
+
+
 def translucent_spheres(pkg, renderer, res=96, spp=8, n=16):
     """The sphere set with non-opaque materials: a third "blend" with opacity
     0.25..0.75, a third "mask" with opacity either side of its cutoff (0.5),

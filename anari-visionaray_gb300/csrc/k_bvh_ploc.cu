@@ -19,7 +19,11 @@
 namespace vsr {
 namespace {
 
-constexpr int kRadius = 16;
+// neighbours searched on either side of a cluster (measured on the 1M-
+// triangle sphere scene, ms per 64-spp frame at radius 8 / 16 / 32 / 64 /
+// 96 / 128 / 192: 207.8 / 198.7 / 191.5 / 184.3 / 180.5 / 178.6 / 178.6,
+// build 7.2 ms at 16 and 8.7 ms at 128)
+constexpr int kRadius = 128;
 constexpr int kBlock = 256;
 
 __device__ __forceinline__ float halfArea(const Aabb &b) {

@@ -6,9 +6,11 @@
 // inner nodes. The triangles are then put in depth-first leaf order, which makes
 // every subtree's triangles contiguous, and the child links of the nodes
 // that remain are rewritten to the (first, count) leaf codes of
-// vsr_device.h. The inner nodes of collapsed subtrees stay in the array,
-// unreferenced. Closest hits are ordered by (t, instance, triangle), so the
-// collapsed tree gives the same hits as the one it came from.
+// vsr_device.h. The remaining inner nodes are then stored in depth-first
+// order (a node's left child right after it, its subtree contiguous), which
+// drops the collapsed subtrees' nodes. Closest hits are ordered by (t,
+// instance, triangle), so the collapsed tree gives the same hits as the one
+// it came from.
 #include "bvh_kernels.cuh"
 
 namespace vsr {
@@ -49,7 +51,7 @@ __global__ void kLinks(const float4 *nodes, int numInner, int *parentInner, int 
 // root). Children's results are read from L2: other SMs wrote them.
 __global__ void kLeafCost(const float4 *nodes, int n, const int *parentInner,
                           const int *parentLeaf, int maxLeaf, int *flags, int *count, float *cost,
-                          int *collapse) {
+                          int *collapse, int *inner) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   int q = parentLeaf[i] >> 1;
@@ -75,6 +77,9 @@ __global__ void kLeafCost(const float4 *nodes, int n, const int *parentInner,
     count[q] = k;
     cost[q] = col ? leaf : split;
     collapse[q] = col ? 1 : 0;
+    // inner nodes that stay in q's subtree (none if q becomes a leaf)
+    inner[q] = col ? 0
+                   : 1 + (c.x < 0 ? 0 : __ldcg(inner + c.x)) + (c.y < 0 ? 0 : __ldcg(inner + c.y));
     const int up = parentInner[q];
     q = up >= 0 ? up >> 1 : -1;
   }
@@ -140,6 +145,41 @@ __global__ void kRelink(float4 *nodes, int numInner, const int *alive, const int
   nodes[4 * (size_t)p + 3] = make_float4(__int_as_float(out[0]), __int_as_float(out[1]), 0.f, 0.f);
 }
 
+// Depth-first (preorder) position of every remaining inner node: one for
+// each ancestor, plus the remaining inner nodes of the left subtree of every
+// ancestor whose right subtree holds the node (the links are the relinked
+// ones: collapsed and triangle children are negative and count none).
+__global__ void kNodePreorder(const float4 *nodes, int numInner, const int *parentInner,
+                              const int *alive, const int *inner, int *pre) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= numInner || !alive[p]) return;
+  int off = 0;
+  for (int link = parentInner[p]; link >= 0;) {
+    const int q = link >> 1;
+    ++off;
+    if (link & 1) {
+      const int left = childLinks(nodes, q).x;
+      if (left >= 0) off += inner[left];
+    }
+    link = parentInner[q];
+  }
+  pre[p] = off;
+}
+
+__global__ void kNodeScatter(const float4 *nodes, int numInner, const int *alive, const int *pre,
+                             float4 *out) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= numInner || !alive[p]) return;
+  const float4 *N = nodes + 4 * (size_t)p;
+  float4 *O = out + 4 * (size_t)pre[p];
+  O[0] = N[0];
+  O[1] = N[1];
+  O[2] = N[2];
+  const int2 c = childLinks(nodes, p);
+  O[3] = make_float4(__int_as_float(c.x >= 0 ? pre[c.x] : c.x),
+                     __int_as_float(c.y >= 0 ? pre[c.y] : c.y), 0.f, 0.f);
+}
+
 __global__ void kScatterTris(const float4 *in, int n, const int *pos, float4 *out) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
@@ -152,20 +192,22 @@ __global__ void kScatterTris(const float4 *in, int n, const int *pos, float4 *ou
 } // namespace
 
 cudaError_t collapseLeaves(float4 *nodes, int numInner, float4 *tris, int n, int maxLeaf,
-                           cudaStream_t stream) {
+                           int *numNodesOut, cudaStream_t stream) {
+  *numNodesOut = numInner;
   if (maxLeaf <= 1 || n < 3 || numInner != n - 1) return cudaSuccess;
   if (maxLeaf > (1 << (32 - kLeafCountShift))) maxLeaf = 1 << (32 - kLeafCountShift);
   if ((uint32_t)n > kLeafFirstMask) return cudaErrorInvalidValue;
   cudaError_t err = cudaSuccess;
   int *ints = nullptr;
   float *cost = nullptr;
-  float4 *trisIn = nullptr;
-  // parentInner, flags, count, collapse, first, alive: numInner each;
-  // parentLeaf, pos: n each
+  float4 *trisIn = nullptr, *nodesOut = nullptr;
+  int kept = 0;
+  // parentInner, flags, count, collapse, first, alive, inner, pre: numInner
+  // each; parentLeaf, pos: n each
   const size_t ni = (size_t)numInner, nt = (size_t)n;
   const int gi = (numInner + kBlock - 1) / kBlock, gt = (n + kBlock - 1) / kBlock;
-  int *parentInner, *flags, *count, *collapse, *first, *alive, *parentLeaf, *pos;
-  if ((err = cudaMallocAsync((void **)&ints, (6 * ni + 2 * nt) * sizeof(int), stream)) != cudaSuccess)
+  int *parentInner, *flags, *count, *collapse, *first, *alive, *inner, *pre, *parentLeaf, *pos;
+  if ((err = cudaMallocAsync((void **)&ints, (8 * ni + 2 * nt) * sizeof(int), stream)) != cudaSuccess)
     return err;
   parentInner = ints;
   flags = parentInner + ni;
@@ -173,10 +215,14 @@ cudaError_t collapseLeaves(float4 *nodes, int numInner, float4 *tris, int n, int
   collapse = count + ni;
   first = collapse + ni;
   alive = first + ni;
-  parentLeaf = alive + ni;
+  inner = alive + ni;
+  pre = inner + ni;
+  parentLeaf = pre + ni;
   pos = parentLeaf + nt;
   if ((err = cudaMallocAsync((void **)&cost, ni * sizeof(float), stream)) != cudaSuccess) goto done;
   if ((err = cudaMallocAsync((void **)&trisIn, 3 * nt * sizeof(float4), stream)) != cudaSuccess)
+    goto done;
+  if ((err = cudaMallocAsync((void **)&nodesOut, 4 * ni * sizeof(float4), stream)) != cudaSuccess)
     goto done;
   if ((err = cudaMemsetAsync(flags, 0, ni * sizeof(int), stream)) != cudaSuccess) goto done;
   if ((err = cudaMemcpyAsync(trisIn, tris, 3 * nt * sizeof(float4), cudaMemcpyDeviceToDevice,
@@ -184,14 +230,30 @@ cudaError_t collapseLeaves(float4 *nodes, int numInner, float4 *tris, int n, int
     goto done;
   kLinks<<<gi, kBlock, 0, stream>>>(nodes, numInner, parentInner, parentLeaf);
   kLeafCost<<<gt, kBlock, 0, stream>>>(nodes, n, parentInner, parentLeaf, maxLeaf, flags, count,
-                                       cost, collapse);
+                                       cost, collapse, inner);
   kNodeOrder<<<gi, kBlock, 0, stream>>>(nodes, numInner, parentInner, count, collapse, first,
                                         alive);
   kTriOrder<<<gt, kBlock, 0, stream>>>(nodes, n, parentInner, parentLeaf, count, collapse, pos);
   kRelink<<<gi, kBlock, 0, stream>>>(nodes, numInner, alive, collapse, count, first, pos);
   kScatterTris<<<gt, kBlock, 0, stream>>>(trisIn, n, pos, tris);
-  err = cudaGetLastError();
+  kNodePreorder<<<gi, kBlock, 0, stream>>>(nodes, numInner, parentInner, alive, inner, pre);
+  kNodeScatter<<<gi, kBlock, 0, stream>>>(nodes, numInner, alive, pre, nodesOut);
+  if ((err = cudaGetLastError()) != cudaSuccess) goto done;
+  // the root's count is the number of nodes kept
+  if ((err = cudaMemcpyAsync(&kept, inner, sizeof(int), cudaMemcpyDeviceToHost, stream)) !=
+      cudaSuccess)
+    goto done;
+  if ((err = cudaStreamSynchronize(stream)) != cudaSuccess) goto done;
+  if (kept < 1 || kept > numInner) {
+    err = cudaErrorUnknown;
+    goto done;
+  }
+  if ((err = cudaMemcpyAsync(nodes, nodesOut, 4 * (size_t)kept * sizeof(float4),
+                             cudaMemcpyDeviceToDevice, stream)) != cudaSuccess)
+    goto done;
+  *numNodesOut = kept;
 done:
+  if (nodesOut) cudaFreeAsync(nodesOut, stream);
   if (trisIn) cudaFreeAsync(trisIn, stream);
   if (cost) cudaFreeAsync(cost, stream);
   cudaFreeAsync(ints, stream);

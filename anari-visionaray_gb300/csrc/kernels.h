@@ -222,9 +222,11 @@ cudaError_t collapseBVH4(const float4 *nodes2, int numNodes2, float4 *nodes4Out,
 // root 0, numInner = n - 1 inner nodes) into leaves of up to maxLeaf
 // triangles where the surface-area heuristic expects fewer node visits,
 // reorders tris (n triangles, 3 float4 each) depth first and rewrites the
-// child links in place (k_bvh_leaves.cu). maxLeaf <= 1 leaves it as it is.
+// nodes in place, the remaining ones in depth-first order (k_bvh_leaves.cu;
+// *numNodesOut: the nodes kept; synchronizes the stream). maxLeaf <= 1
+// leaves the BVH as it is.
 cudaError_t collapseLeaves(float4 *nodes, int numInner, float4 *tris, int n, int maxLeaf,
-                           cudaStream_t stream);
+                           int *numNodesOut, cudaStream_t stream);
 
 // Same inputs/outputs, PLOC clustering instead of the Karras hierarchy:
 // tighter boxes (close to a greedy SAH build), a few ms more per 1M

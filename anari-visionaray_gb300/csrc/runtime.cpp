@@ -1861,9 +1861,11 @@ struct World : Object {
         gg->width = 2;
         if (bvhWidth == 2 && leafSize > 1) {
           auto tl = std::chrono::steady_clock::now();
+          int kept = st.numNodes;
           e = collapseLeaves(gg->nodes.as<float4>(), st.numNodes, gg->tris.as<float4>(), nt,
-                             leafSize, s);
+                             leafSize, &kept, s);
           if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+          gg->numNodes = st.numNodes = kept;
           if (e != cudaSuccess) {
             dev->report(this, kind, VSR_SEVERITY_ERROR, VSR_ERROR_CUDA, "BVH leaf collapse failed: %s",
                         cudaGetErrorString(e));

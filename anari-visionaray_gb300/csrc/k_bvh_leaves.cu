@@ -36,12 +36,17 @@ __device__ __forceinline__ int2 childLinks(const float4 *nodes, int p) {
 
 // Parent links, 2 p + side (side 1: the right child); -1 above the root.
 // The builders' leaves hold one triangle each (code ~i, count bits 0).
+// Links out of range (only in a malformed tree) are skipped; the walks below
+// then end early and report it.
 __global__ void kLinks(const float4 *nodes, int numInner, int *parentInner, int *parentLeaf) {
   const int p = blockIdx.x * blockDim.x + threadIdx.x;
   if (p >= numInner) return;
   const int2 c = childLinks(nodes, p);
-  if (c.x >= 0) parentInner[c.x] = 2 * p; else parentLeaf[~c.x] = 2 * p;
-  if (c.y >= 0) parentInner[c.y] = 2 * p + 1; else parentLeaf[~c.y] = 2 * p + 1;
+  const int ch[2] = {c.x, c.y};
+  for (int s = 0; s < 2; ++s) {
+    if (ch[s] > 0 && ch[s] < numInner) parentInner[ch[s]] = 2 * p + s;
+    else if (ch[s] < 0 && ~ch[s] <= numInner) parentLeaf[~ch[s]] = 2 * p + s;
+  }
   if (p == 0) parentInner[0] = -1;
 }
 
@@ -51,11 +56,15 @@ __global__ void kLinks(const float4 *nodes, int numInner, int *parentInner, int 
 // root). Children's results are read from L2: other SMs wrote them.
 __global__ void kLeafCost(const float4 *nodes, int n, const int *parentInner,
                           const int *parentLeaf, int maxLeaf, int *flags, int *count, float *cost,
-                          int *collapse, int *inner) {
+                          int *collapse, int *inner, int *bad) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   int q = parentLeaf[i] >> 1;
-  while (q >= 0) {
+  for (int steps = 0; q >= 0; ++steps) {
+    if (q >= n - 1 || steps >= n) {  // not a tree: give up, reported to the host
+      atomicOr(bad, 1);
+      return;
+    }
     __threadfence();
     if (atomicAdd(&flags[q], 1) == 0) return;  // the sibling's subtree is not done yet
     __threadfence();
@@ -89,13 +98,17 @@ __global__ void kLeafCost(const float4 *nodes, int n, const int *parentInner,
 // `link` (2 p + side of the element's parent), found by walking to the
 // root and adding the triangle count of every left sibling passed; `top`
 // gets the topmost collapsed node on the way (-1 if none).
-__device__ __forceinline__ int dfsFirst(const float4 *nodes, const int *parentInner,
-                                        const int *count, const int *collapse, int link,
-                                        int &top) {
+__device__ __forceinline__ int dfsFirst(const float4 *nodes, int numInner,
+                                        const int *parentInner, const int *count,
+                                        const int *collapse, int link, int &top, int *bad) {
   int off = 0;
   top = -1;
-  while (link >= 0) {
+  for (int steps = 0; link >= 0; ++steps) {
     const int p = link >> 1;
+    if (p >= numInner || steps >= numInner) {
+      atomicOr(bad, 1);
+      return 0;
+    }
     if (link & 1) {
       const int left = childLinks(nodes, p).x;
       off += left < 0 ? 1 : count[left];
@@ -109,21 +122,26 @@ __device__ __forceinline__ int dfsFirst(const float4 *nodes, const int *parentIn
 // Per inner node: its first triangle's depth-first position, and whether it
 // stays an inner node (neither it nor an ancestor collapsed).
 __global__ void kNodeOrder(const float4 *nodes, int numInner, const int *parentInner,
-                           const int *count, const int *collapse, int *first, int *alive) {
+                           const int *count, const int *collapse, int *first, int *alive,
+                           int *bad) {
   const int p = blockIdx.x * blockDim.x + threadIdx.x;
   if (p >= numInner) return;
   int top;
-  first[p] = dfsFirst(nodes, parentInner, count, collapse, parentInner[p], top);
+  first[p] = dfsFirst(nodes, numInner, parentInner, count, collapse, parentInner[p], top, bad);
   alive[p] = (top < 0 && !collapse[p]) ? 1 : 0;
 }
 
 __global__ void kTriOrder(const float4 *nodes, int n, const int *parentInner,
                           const int *parentLeaf, const int *count, const int *collapse,
-                          int *pos) {
+                          int *pos, int *bad) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   int top;
-  pos[i] = dfsFirst(nodes, parentInner, count, collapse, parentLeaf[i], top);
+  pos[i] = dfsFirst(nodes, n - 1, parentInner, count, collapse, parentLeaf[i], top, bad);
+  if (pos[i] < 0 || pos[i] >= n) {  // only for a malformed tree; the scatter skips it
+    atomicOr(bad, 1);
+    pos[i] = -1;
+  }
 }
 
 // The remaining inner nodes' child links: a triangle's new position, a
@@ -138,8 +156,8 @@ __global__ void kRelink(float4 *nodes, int numInner, const int *alive, const int
   for (int s = 0; s < 2; ++s) {
     const int ch = out[s];
     if (ch < 0)
-      out[s] = ~pos[~ch];
-    else if (collapse[ch])
+      out[s] = ~ch <= numInner ? ~pos[~ch] : ch;  // n = numInner + 1 triangles
+    else if (ch < numInner && collapse[ch])
       out[s] = ~(int)((uint32_t)first[ch] | ((uint32_t)(count[ch] - 1) << kLeafCountShift));
   }
   nodes[4 * (size_t)p + 3] = make_float4(__int_as_float(out[0]), __int_as_float(out[1]), 0.f, 0.f);
@@ -150,12 +168,16 @@ __global__ void kRelink(float4 *nodes, int numInner, const int *alive, const int
 // ancestor whose right subtree holds the node (the links are the relinked
 // ones: collapsed and triangle children are negative and count none).
 __global__ void kNodePreorder(const float4 *nodes, int numInner, const int *parentInner,
-                              const int *alive, const int *inner, int *pre) {
+                              const int *alive, const int *inner, int *pre, int *bad) {
   const int p = blockIdx.x * blockDim.x + threadIdx.x;
   if (p >= numInner || !alive[p]) return;
   int off = 0;
-  for (int link = parentInner[p]; link >= 0;) {
+  for (int link = parentInner[p], steps = 0; link >= 0; ++steps) {
     const int q = link >> 1;
+    if (q >= numInner || steps >= numInner) {
+      atomicOr(bad, 1);
+      break;
+    }
     ++off;
     if (link & 1) {
       const int left = childLinks(nodes, q).x;
@@ -167,9 +189,9 @@ __global__ void kNodePreorder(const float4 *nodes, int numInner, const int *pare
 }
 
 __global__ void kNodeScatter(const float4 *nodes, int numInner, const int *alive, const int *pre,
-                             float4 *out) {
+                             const int *kept, float4 *out) {
   const int p = blockIdx.x * blockDim.x + threadIdx.x;
-  if (p >= numInner || !alive[p]) return;
+  if (p >= numInner || !alive[p] || pre[p] < 0 || pre[p] >= *kept) return;
   const float4 *N = nodes + 4 * (size_t)p;
   float4 *O = out + 4 * (size_t)pre[p];
   O[0] = N[0];
@@ -182,7 +204,7 @@ __global__ void kNodeScatter(const float4 *nodes, int numInner, const int *alive
 
 __global__ void kScatterTris(const float4 *in, int n, const int *pos, float4 *out) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
+  if (i >= n || pos[i] < 0) return;
   const size_t j = (size_t)pos[i];
   out[3 * j] = in[3 * (size_t)i];
   out[3 * j + 1] = in[3 * (size_t)i + 1];
@@ -201,13 +223,15 @@ cudaError_t collapseLeaves(float4 *nodes, int numInner, float4 *tris, int n, int
   int *ints = nullptr;
   float *cost = nullptr;
   float4 *trisIn = nullptr, *nodesOut = nullptr;
-  int kept = 0;
+  int kept = 0, badHost = 0;
   // parentInner, flags, count, collapse, first, alive, inner, pre: numInner
-  // each; parentLeaf, pos: n each
+  // each; parentLeaf, pos: n each; the malformed-tree flag
   const size_t ni = (size_t)numInner, nt = (size_t)n;
   const int gi = (numInner + kBlock - 1) / kBlock, gt = (n + kBlock - 1) / kBlock;
-  int *parentInner, *flags, *count, *collapse, *first, *alive, *inner, *pre, *parentLeaf, *pos;
-  if ((err = cudaMallocAsync((void **)&ints, (8 * ni + 2 * nt) * sizeof(int), stream)) != cudaSuccess)
+  int *parentInner, *flags, *count, *collapse, *first, *alive, *inner, *pre, *parentLeaf, *pos,
+      *bad;
+  if ((err = cudaMallocAsync((void **)&ints, (8 * ni + 2 * nt + 1) * sizeof(int), stream)) !=
+      cudaSuccess)
     return err;
   parentInner = ints;
   flags = parentInner + ni;
@@ -219,32 +243,41 @@ cudaError_t collapseLeaves(float4 *nodes, int numInner, float4 *tris, int n, int
   pre = inner + ni;
   parentLeaf = pre + ni;
   pos = parentLeaf + nt;
+  bad = pos + nt;
   if ((err = cudaMallocAsync((void **)&cost, ni * sizeof(float), stream)) != cudaSuccess) goto done;
   if ((err = cudaMallocAsync((void **)&trisIn, 3 * nt * sizeof(float4), stream)) != cudaSuccess)
     goto done;
   if ((err = cudaMallocAsync((void **)&nodesOut, 4 * ni * sizeof(float4), stream)) != cudaSuccess)
     goto done;
+  // links not set by kLinks (only in a malformed tree) read -1: walks end there
+  if ((err = cudaMemsetAsync(ints, 0xff, (8 * ni + 2 * nt) * sizeof(int), stream)) != cudaSuccess)
+    goto done;
   if ((err = cudaMemsetAsync(flags, 0, ni * sizeof(int), stream)) != cudaSuccess) goto done;
+  if ((err = cudaMemsetAsync(bad, 0, sizeof(int), stream)) != cudaSuccess) goto done;
   if ((err = cudaMemcpyAsync(trisIn, tris, 3 * nt * sizeof(float4), cudaMemcpyDeviceToDevice,
                              stream)) != cudaSuccess)
     goto done;
   kLinks<<<gi, kBlock, 0, stream>>>(nodes, numInner, parentInner, parentLeaf);
   kLeafCost<<<gt, kBlock, 0, stream>>>(nodes, n, parentInner, parentLeaf, maxLeaf, flags, count,
-                                       cost, collapse, inner);
+                                       cost, collapse, inner, bad);
   kNodeOrder<<<gi, kBlock, 0, stream>>>(nodes, numInner, parentInner, count, collapse, first,
-                                        alive);
-  kTriOrder<<<gt, kBlock, 0, stream>>>(nodes, n, parentInner, parentLeaf, count, collapse, pos);
+                                        alive, bad);
+  kTriOrder<<<gt, kBlock, 0, stream>>>(nodes, n, parentInner, parentLeaf, count, collapse, pos,
+                                       bad);
   kRelink<<<gi, kBlock, 0, stream>>>(nodes, numInner, alive, collapse, count, first, pos);
   kScatterTris<<<gt, kBlock, 0, stream>>>(trisIn, n, pos, tris);
-  kNodePreorder<<<gi, kBlock, 0, stream>>>(nodes, numInner, parentInner, alive, inner, pre);
-  kNodeScatter<<<gi, kBlock, 0, stream>>>(nodes, numInner, alive, pre, nodesOut);
+  kNodePreorder<<<gi, kBlock, 0, stream>>>(nodes, numInner, parentInner, alive, inner, pre, bad);
+  // inner[0], the root's count, is the number of nodes kept
+  kNodeScatter<<<gi, kBlock, 0, stream>>>(nodes, numInner, alive, pre, inner, nodesOut);
   if ((err = cudaGetLastError()) != cudaSuccess) goto done;
-  // the root's count is the number of nodes kept
   if ((err = cudaMemcpyAsync(&kept, inner, sizeof(int), cudaMemcpyDeviceToHost, stream)) !=
       cudaSuccess)
     goto done;
+  if ((err = cudaMemcpyAsync(&badHost, bad, sizeof(int), cudaMemcpyDeviceToHost, stream)) !=
+      cudaSuccess)
+    goto done;
   if ((err = cudaStreamSynchronize(stream)) != cudaSuccess) goto done;
-  if (kept < 1 || kept > numInner) {
+  if (badHost || kept < 1 || kept > numInner) {
     err = cudaErrorUnknown;
     goto done;
   }

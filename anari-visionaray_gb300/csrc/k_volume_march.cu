@@ -39,17 +39,17 @@ namespace {
 #endif
 #ifndef VSR_SETUP_MIN_BLOCKS
 // 8 blocks of 256 per SM (32 registers): a 512x512 frame's set-up grid is
-// resident in one wave (config 0: 0.0658 ms per frame against 0.0665 at 4
-// blocks and 0.0673 at 6)
+// resident in one wave (a 128^3 blob volume at 512x512: 0.0658 ms per
+// frame against 0.0665 at 4 blocks and 0.0673 at 6)
 #define VSR_SETUP_MIN_BLOCKS 8
 #endif
 #ifndef VSR_COMBINE_PREFETCH
 #define VSR_COMBINE_PREFETCH 8
 #endif
 #ifndef VSR_VOLUME_REFILL
-// 1: the one-pass marcher (kVolumeRefill): measured 0.21-0.24 ms per
-// config-0 frame (refill every 8 / 12 / 16 samples, 3 or 4 blocks per SM)
-// against 0.066 ms for the three passes
+// 1: the one-pass marcher (kVolumeRefill): measured 0.21-0.24 ms per frame
+// of a 128^3 blob volume at 512x512 (refill every 8 / 12 / 16 samples, 3 or
+// 4 blocks per SM) against 0.066 ms for the three passes
 #define VSR_VOLUME_REFILL 0
 #endif
 #ifndef VSR_REFILL_SAMPLES
@@ -59,8 +59,8 @@ namespace {
 #define VSR_REFILL_MIN_BLOCKS 4
 #endif
 #ifndef VSR_SEG_FUSE
-// 1: the combination inside the segments pass (measured 0.125 ms per
-// config-0 frame against 0.067 ms with its own pass: the last groups'
+// 1: the combination inside the segments pass (measured 0.125 ms per frame
+// of the same volume against 0.067 ms with its own pass: the last groups'
 // combinations run at the end with few warps, and the fused kernel spills
 // at the segments pass's 64 registers)
 #define VSR_SEG_FUSE 0

@@ -892,7 +892,12 @@ def run_ours(args):
                    "l2": "flushed (256 MiB write) between steps", "parallelism": f"replicas{world}"},
         "e2e": {"value": e2e_value, "unit": "Mpx*spp/s", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h},
-        "gpu_launches": args.steps,
+        # this library's kernels per timed frame: the megakernel and, with
+        # sample chunks, kCombineChunks; in wavefront mode the init kernel and
+        # a trace and a shade kernel per iteration (no accumulation reset
+        # happens inside the timed loop)
+        "gpu_launches": args.steps * ((1 + 2 * iterations) if args.wavefront and iterations
+                                      else (2 if args.sample_chunks > 1 else 1)),
         # traversal and shading are issue- and latency-bound: thread
         # instructions per second against the SMs' lane-issue peak
         "roofline": dict(issue, traffic=traffic) if issue else
